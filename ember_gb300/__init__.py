@@ -1,0 +1,14 @@
+"""ember_gb300 -- GB300 (sm_103a) implementation of Ember's split-step hot path.
+
+The compute path is libember_gpu.so (hand-written FP64 CUDA kernels behind the
+C ABI of include/ember_gpu.h); this package is the host-side mirror of the
+reference's stage interfaces, for Python callers and tests.
+"""
+from ._lib import EmberGpuError, library_path  # noqa: F401
+from . import _lib  # noqa: F401
+
+__version__ = "0.1.0"
+
+
+def device_count() -> int:
+    return _lib.lib().ember_device_count()

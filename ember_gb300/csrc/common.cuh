@@ -1,0 +1,129 @@
+// Shared host/device helpers of libember_gpu: error reporting, CUDA checks,
+// stream-ordered scratch buffers and host<->device staging for the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/ember_gpu.h"
+
+namespace ember {
+
+// Last error message of the calling thread (ember_last_error()).
+void set_error(const char* fmt, ...);
+const std::string& last_error();
+
+// Run `expr` (a cudaError_t expression); on failure record the message and
+// return EMBER_ECUDA from the enclosing function.
+#define EMBER_CUDA_TRY(expr)                                                     \
+    do {                                                                         \
+        cudaError_t ember_err_ = (expr);                                         \
+        if (ember_err_ != cudaSuccess) {                                         \
+            ::ember::set_error("%s failed: %s (%s:%d)", #expr,                  \
+                               cudaGetErrorString(ember_err_), __FILE__, __LINE__); \
+            return EMBER_ECUDA;                                                  \
+        }                                                                        \
+    } while (0)
+
+#define EMBER_CHECK_ARG(cond, ...)                                               \
+    do {                                                                         \
+        if (!(cond)) {                                                           \
+            ::ember::set_error(__VA_ARGS__);                                     \
+            return EMBER_EINVAL;                                                 \
+        }                                                                        \
+    } while (0)
+
+#define EMBER_TRY(expr)                                                          \
+    do {                                                                         \
+        int ember_rc_ = (expr);                                                  \
+        if (ember_rc_ != EMBER_OK) return ember_rc_;                             \
+    } while (0)
+
+inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+// Make sure the calling thread has a usable device; keeps the default
+// memory pool from returning freed blocks to the driver so that the
+// stream-ordered scratch allocations below are cheap after the first call.
+int ensure_device();
+
+// Stream-ordered device scratch (cudaMallocAsync / cudaFreeAsync on the
+// call's stream). Freed when the object goes out of scope; the free is
+// ordered after every kernel already queued on that stream.
+class Scratch {
+public:
+    explicit Scratch(cudaStream_t s) : stream_(s) {}
+    ~Scratch() { release(); }
+    Scratch(const Scratch&) = delete;
+    Scratch& operator=(const Scratch&) = delete;
+
+    // Allocate `bytes` (rounded up to 256) and return the device pointer in *p.
+    template <class T>
+    int alloc(T** p, size_t count) {
+        size_t bytes = ((count * sizeof(T) + 255) / 256) * 256;
+        if (bytes == 0) bytes = 256;
+        void* q = nullptr;
+        cudaError_t e = cudaMallocAsync(&q, bytes, stream_);
+        if (e != cudaSuccess) {
+            set_error("cudaMallocAsync(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+            return (e == cudaErrorMemoryAllocation) ? EMBER_ENOMEM : EMBER_ECUDA;
+        }
+        ptrs_.push_back(q);
+        *p = static_cast<T*>(q);
+        return EMBER_OK;
+    }
+
+    void release() {
+        for (void* q : ptrs_) cudaFreeAsync(q, stream_);
+        ptrs_.clear();
+    }
+
+private:
+    cudaStream_t stream_;
+    std::vector<void*> ptrs_;
+};
+
+// View an argument array on the device: for EMBER_MEM_DEVICE the pointer is
+// used as is; for EMBER_MEM_HOST a scratch copy is made on `stream`.
+template <class T>
+int stage_in(Scratch& sc, const T* src, size_t count, int mem, cudaStream_t stream, const T** dev) {
+    if (src == nullptr || mem == EMBER_MEM_DEVICE) {
+        *dev = src;
+        return EMBER_OK;
+    }
+    T* d = nullptr;
+    EMBER_TRY(sc.alloc(&d, count));
+    if (count) EMBER_CUDA_TRY(cudaMemcpyAsync(d, src, count * sizeof(T), cudaMemcpyHostToDevice, stream));
+    *dev = d;
+    return EMBER_OK;
+}
+
+// Output array: device pointer as is, or a scratch buffer to copy back later
+// with stage_out().
+template <class T>
+int stage_buffer(Scratch& sc, T* dst, size_t count, int mem, T** dev) {
+    if (dst == nullptr || mem == EMBER_MEM_DEVICE) {
+        *dev = dst;
+        return EMBER_OK;
+    }
+    return sc.alloc(dev, count);
+}
+
+template <class T>
+int stage_out(T* dst, const T* dev, size_t count, int mem, cudaStream_t stream) {
+    if (dst == nullptr || mem == EMBER_MEM_DEVICE || count == 0) return EMBER_OK;
+    EMBER_CUDA_TRY(cudaMemcpyAsync(dst, dev, count * sizeof(T), cudaMemcpyDeviceToHost, stream));
+    return EMBER_OK;
+}
+
+// Check the launch and, for host-memory calls, wait for the stream.
+int finish_call(int mem, cudaStream_t stream);
+
+inline int blocks_for(int64_t n, int threads) {
+    return static_cast<int>((n + threads - 1) / threads);
+}
+
+}  // namespace ember

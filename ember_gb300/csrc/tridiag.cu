@@ -1,0 +1,427 @@
+// Batched tridiagonal integrator and diffusion stage (sm_103a, FP64).
+//
+// Scheme (reference: src/integrator.cpp:37-47, 133-204): the first step after
+// initialize() is 8 first-order BDF sub-steps of h/8 sharing one Thomas
+// factorisation of (A - 8/h I); later steps are second-order BDF with
+// (A - 3/(2h) I) factorised once at the second step. Matrix rows come from
+// DiffusionSystem::get_A / get_k (src/diffusionSystem.cpp:10-76) and the step
+// size from FlameSolver::setDiffusionSolverState (src/flameSolver.cpp:702-718).
+//
+// The kernels here follow the reference's operation order with explicitly
+// rounded intrinsics (no FMA contraction), so a system integrated by
+// tri_step_serial is bitwise identical to the CPU restatement compiled with
+// -ffp-contract=off.
+#include "common.cuh"
+#include "tridiag.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace ember {
+
+// ---------------------------------------------------------------- kernels --
+
+__global__ void k_tridiag_step(TriBatchView v) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.n_systems) return;
+    TriSys sys = v.system(s);
+    int sc = v.step_count[s];
+    double t = v.t[s];
+    tri_step_serial(sys, t, v.h[s], sc, v.lu_b0[s]);
+    v.step_count[s] = sc;
+    v.t[s] = t;
+}
+
+__global__ void k_tridiag_integrate(TriBatchView v, const double* __restrict__ t_end) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.n_systems) return;
+    TriSys sys = v.system(s);
+    int sc = v.step_count[s];
+    double t = v.t[s];
+    double h = v.h[s];
+    int st = tri_integrate_serial(sys, t, h, sc, v.lu_b0[s], t_end[s]);
+    v.step_count[s] = sc;
+    v.t[s] = t;
+    v.h[s] = h;
+    if (v.status) v.status[s] = st;
+}
+
+__global__ void k_tridiag_ydot(TriBatchView v, double* __restrict__ ydot) {
+    int s = blockIdx.y;
+    const int64_t o = v.off[s];
+    const int N = static_cast<int>(v.off[s + 1] - o);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const double* a = v.a + o;
+        const double* b = v.b + o;
+        const double* c = v.c + o;
+        const double* y = v.y + o;
+        double r;
+        if (i == 0) {
+            r = __dadd_rn(__dadd_rn(__dmul_rn(b[0], y[0]), __dmul_rn(c[0], y[1])), v.k[o]);
+        } else if (i == N - 1) {
+            r = __dadd_rn(__dadd_rn(__dmul_rn(a[i], y[i - 1]), __dmul_rn(b[i], y[i])), v.k[o + i]);
+        } else {
+            r = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(a[i], y[i - 1]), __dmul_rn(b[i], y[i])),
+                                    __dmul_rn(c[i], y[i + 1])),
+                          v.k[o + i]);
+        }
+        ydot[o + i] = r;
+    }
+}
+
+// Rows of DiffusionSystem::get_A / get_k for every (flame, variable) system.
+// One thread per matrix row; each row is what the reference's sequence of
+// writes (left BC, right BC, interior loop) leaves in it, starting from the
+// zeroed arrays of TridiagonalIntegrator::resize.
+__global__ void k_diffusion_rows(DiffusionView v) {
+    for (int s = blockIdx.y; s < v.n_systems; s += gridDim.y) {
+        const DiffSysInfo info = v.info[s];
+        const int N = info.n;
+        const double* x = v.x + info.grid_off;
+        const int64_t o = info.off;
+        const double* B = v.B + o;
+        const double* D = v.D + o;
+        for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
+            DiffRow row = diffusion_row(j, N, x, info.alpha, info.left_bc, info.right_bc, B, D,
+                                        v.wall_const ? v.wall_const[s] : 0.0);
+            double k = v.split_const ? v.split_const[o + j] : 0.0;
+            if (j == 0 && info.left_bc == EMBER_BC_WALL_FLUX) {
+                double hh0 = __dsub_rn(x[1], x[0]);
+                double wc = v.wall_const ? v.wall_const[s] : 0.0;
+                double yi = v.y_inf ? v.y_inf[s] : 0.0;
+                k = __dadd_rn(k, __dmul_rn(__dmul_rn(__ddiv_rn(__dmul_rn(B[0], static_cast<double>(info.alpha + 1)), hh0), wc), yi));
+            }
+            v.a[o + j] = row.a;
+            v.b[o + j] = row.b;
+            v.c[o + j] = row.c;
+            v.k[o + j] = k;
+        }
+    }
+}
+
+// Step size rule of setDiffusionSolverState followed by initialize(t0, h) and
+// integrateToTime(t1), one thread per system.
+__global__ void k_diffusion_integrate_serial(DiffusionView v, TriBatchView tb, double t0, double t1,
+                                             double mult, double gdt) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.n_systems) return;
+    const DiffSysInfo info = v.info[s];
+    double h;
+    if (v.h) {
+        h = v.h[s];
+    } else {
+        h = diffusion_step_size(info.n, v.x + info.grid_off, v.B + info.off, v.D + info.off, mult, gdt);
+    }
+    TriSys sys = tb.system(s);
+    int sc = 0;
+    double t = t0;
+    double lu_b0 = 0.0;
+    int st = tri_integrate_serial(sys, t, h, sc, lu_b0, t1);
+    if (v.status) v.status[s] = st;
+}
+
+}  // namespace ember
+
+// ------------------------------------------------------------ C ABI: batch --
+
+using namespace ember;
+
+struct ember_tridiag_s {
+    int n_systems = 0;
+    int64_t n_total = 0;
+    std::vector<int64_t> h_off;
+    int64_t* off = nullptr;
+    double* arr = nullptr;  // a b c k y yprev luc inv  (8 * n_total)
+    double* sys = nullptr;  // t h lu_b0                (3 * n_systems)
+    int* step_count = nullptr;
+    int* status = nullptr;
+
+    TriBatchView view() const {
+        TriBatchView v;
+        v.n_systems = n_systems;
+        v.off = off;
+        v.a = arr;
+        v.b = arr + n_total;
+        v.c = arr + 2 * n_total;
+        v.k = arr + 3 * n_total;
+        v.y = arr + 4 * n_total;
+        v.yprev = arr + 5 * n_total;
+        v.luc = arr + 6 * n_total;
+        v.inv = arr + 7 * n_total;
+        v.t = sys;
+        v.h = sys + n_systems;
+        v.lu_b0 = sys + 2 * n_systems;
+        v.step_count = step_count;
+        v.status = status;
+        return v;
+    }
+};
+
+static int check_batch(ember_tridiag b) {
+    EMBER_CHECK_ARG(b != nullptr, "null ember_tridiag handle");
+    return EMBER_OK;
+}
+
+static int copy_in(double* dst, const double* src, size_t n, int mem, cudaStream_t st) {
+    EMBER_CHECK_ARG(src != nullptr, "null array argument");
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_CUDA_TRY(cudaMemcpyAsync(dst, src, n * sizeof(double),
+                                   mem == EMBER_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
+    return EMBER_OK;
+}
+
+extern "C" int ember_tridiag_create(int n_systems, const int64_t* offsets, ember_tridiag* out) {
+    EMBER_CHECK_ARG(out != nullptr, "null output handle pointer");
+    *out = nullptr;
+    EMBER_CHECK_ARG(n_systems > 0, "n_systems must be positive (got %d)", n_systems);
+    EMBER_CHECK_ARG(offsets != nullptr, "null offsets");
+    EMBER_CHECK_ARG(offsets[0] == 0, "offsets[0] must be 0");
+    for (int s = 0; s < n_systems; ++s)
+        EMBER_CHECK_ARG(offsets[s + 1] - offsets[s] >= 2, "system %d has %lld points; at least 2 are needed", s,
+                        (long long)(offsets[s + 1] - offsets[s]));
+    EMBER_CHECK_ARG(offsets[n_systems] - offsets[n_systems - 1] < (int64_t(1) << 31), "system too large");
+    EMBER_TRY(ensure_device());
+    auto* b = new ember_tridiag_s;
+    b->n_systems = n_systems;
+    b->n_total = offsets[n_systems];
+    b->h_off.assign(offsets, offsets + n_systems + 1);
+    cudaError_t e = cudaMalloc(&b->off, sizeof(int64_t) * (n_systems + 1));
+    if (e == cudaSuccess) e = cudaMalloc(&b->arr, sizeof(double) * 8 * b->n_total);
+    if (e == cudaSuccess) e = cudaMalloc(&b->sys, sizeof(double) * 3 * n_systems);
+    if (e == cudaSuccess) e = cudaMalloc(&b->step_count, sizeof(int) * n_systems);
+    if (e == cudaSuccess) e = cudaMalloc(&b->status, sizeof(int) * n_systems);
+    if (e == cudaSuccess) e = cudaMemcpy(b->off, offsets, sizeof(int64_t) * (n_systems + 1), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(b->arr, 0, sizeof(double) * 8 * b->n_total);
+    if (e == cudaSuccess) e = cudaMemset(b->sys, 0, sizeof(double) * 3 * n_systems);
+    if (e == cudaSuccess) e = cudaMemset(b->step_count, 0, sizeof(int) * n_systems);
+    if (e == cudaSuccess) e = cudaMemset(b->status, 0, sizeof(int) * n_systems);
+    if (e != cudaSuccess) {
+        set_error("ember_tridiag_create: %s", cudaGetErrorString(e));
+        ember_tridiag_destroy(b);
+        return e == cudaErrorMemoryAllocation ? EMBER_ENOMEM : EMBER_ECUDA;
+    }
+    *out = b;
+    return EMBER_OK;
+}
+
+extern "C" int ember_tridiag_destroy(ember_tridiag b) {
+    if (!b) return EMBER_OK;
+    cudaFree(b->off);
+    cudaFree(b->arr);
+    cudaFree(b->sys);
+    cudaFree(b->step_count);
+    cudaFree(b->status);
+    delete b;
+    return EMBER_OK;
+}
+
+extern "C" int ember_tridiag_set_coefficients(ember_tridiag b, const double* a, const double* bb, const double* c,
+                                              const double* k, int mem, void* stream) {
+    EMBER_TRY(check_batch(b));
+    cudaStream_t st = as_stream(stream);
+    EMBER_TRY(copy_in(b->arr, a, b->n_total, mem, st));
+    EMBER_TRY(copy_in(b->arr + b->n_total, bb, b->n_total, mem, st));
+    EMBER_TRY(copy_in(b->arr + 2 * b->n_total, c, b->n_total, mem, st));
+    EMBER_TRY(copy_in(b->arr + 3 * b->n_total, k, b->n_total, mem, st));
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_tridiag_set_y0(ember_tridiag b, const double* y0, int mem, void* stream) {
+    EMBER_TRY(check_batch(b));
+    cudaStream_t st = as_stream(stream);
+    TriBatchView v = b->view();
+    EMBER_TRY(copy_in(v.y, y0, b->n_total, mem, st));
+    EMBER_CUDA_TRY(cudaMemsetAsync(b->step_count, 0, sizeof(int) * b->n_systems, st));
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_tridiag_initialize(ember_tridiag b, const double* t0, const double* h, int mem, void* stream) {
+    EMBER_TRY(check_batch(b));
+    cudaStream_t st = as_stream(stream);
+    TriBatchView v = b->view();
+    EMBER_TRY(copy_in(v.t, t0, b->n_systems, mem, st));
+    EMBER_TRY(copy_in(v.h, h, b->n_systems, mem, st));
+    EMBER_CUDA_TRY(cudaMemsetAsync(b->step_count, 0, sizeof(int) * b->n_systems, st));
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_tridiag_step(ember_tridiag b, void* stream) {
+    EMBER_TRY(check_batch(b));
+    cudaStream_t st = as_stream(stream);
+    k_tridiag_step<<<blocks_for(b->n_systems, 128), 128, 0, st>>>(b->view());
+    return finish_call(EMBER_MEM_DEVICE, st);
+}
+
+extern "C" int ember_tridiag_integrate_to_time(ember_tridiag b, const double* t_end, int mem, void* stream) {
+    EMBER_TRY(check_batch(b));
+    EMBER_CHECK_ARG(t_end != nullptr, "null t_end");
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    const double* d_tend = nullptr;
+    EMBER_TRY(stage_in(sc, t_end, b->n_systems, mem, st, &d_tend));
+    k_tridiag_integrate<<<blocks_for(b->n_systems, 128), 128, 0, st>>>(b->view(), d_tend);
+    EMBER_TRY(finish_call(mem, st));
+    if (mem == EMBER_MEM_HOST) {
+        std::vector<int> status(b->n_systems);
+        EMBER_CUDA_TRY(cudaMemcpy(status.data(), b->status, sizeof(int) * b->n_systems, cudaMemcpyDeviceToHost));
+        for (int s = 0; s < b->n_systems; ++s) {
+            if (status[s] != 0) {
+                set_error("system %d: integrate_to_time failed with status %d", s, status[s]);
+                return EMBER_EFAIL;
+            }
+        }
+    }
+    return EMBER_OK;
+}
+
+extern "C" int ember_tridiag_get_state(ember_tridiag b, double* y, double* t, double* h, int mem, void* stream) {
+    EMBER_TRY(check_batch(b));
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    cudaStream_t st = as_stream(stream);
+    TriBatchView v = b->view();
+    cudaMemcpyKind kind = mem == EMBER_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (y) EMBER_CUDA_TRY(cudaMemcpyAsync(y, v.y, sizeof(double) * b->n_total, kind, st));
+    if (t) EMBER_CUDA_TRY(cudaMemcpyAsync(t, v.t, sizeof(double) * b->n_systems, kind, st));
+    if (h) EMBER_CUDA_TRY(cudaMemcpyAsync(h, v.h, sizeof(double) * b->n_systems, kind, st));
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_tridiag_get_ydot(ember_tridiag b, double* ydot, int mem, void* stream) {
+    EMBER_TRY(check_batch(b));
+    EMBER_CHECK_ARG(ydot != nullptr, "null ydot");
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    double* d_ydot = nullptr;
+    EMBER_TRY(stage_buffer(sc, ydot, b->n_total, mem, &d_ydot));
+    EMBER_CHECK_ARG(b->n_systems <= 65535, "get_ydot supports at most 65535 systems");
+    int64_t nmax = 0;
+    for (int s = 0; s < b->n_systems; ++s) nmax = std::max(nmax, b->h_off[s + 1] - b->h_off[s]);
+    dim3 grid(std::min(blocks_for(nmax, 256), 64), b->n_systems);
+    k_tridiag_ydot<<<grid, 256, 0, st>>>(b->view(), d_ydot);
+    EMBER_TRY(stage_out(ydot, d_ydot, b->n_total, mem, st));
+    return finish_call(mem, st);
+}
+
+// ------------------------------------------------------ C ABI: diffusion --
+
+extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_grid* grids, int n_vars,
+                                         const double* x, const double* B, const double* D,
+                                         const double* split_const, double* y,
+                                         const ember_diffusion_options* opts, int* status, int mem,
+                                         void* stream) {
+    EMBER_CHECK_ARG(n_flames > 0 && grids != nullptr, "need at least one flame");
+    EMBER_CHECK_ARG(n_vars > 0, "n_vars must be positive");
+    EMBER_CHECK_ARG(x && B && D && y && opts, "null array or options argument");
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_TRY(ensure_device());
+    const int n_sys = n_flames * n_vars;
+    std::vector<DiffSysInfo> info(n_sys);
+    int64_t n_pts = 0, n_vals = 0;
+    for (int f = 0; f < n_flames; ++f) {
+        const ember_diffusion_grid& g = grids[f];
+        EMBER_CHECK_ARG(g.n_points >= 3, "flame %d: n_points must be >= 3 (got %d)", f, g.n_points);
+        EMBER_CHECK_ARG(g.left_bc >= 0 && g.left_bc <= 4, "flame %d: bad left_bc %d", f, g.left_bc);
+        EMBER_CHECK_ARG(g.right_bc == EMBER_BC_FIXED_VALUE || g.right_bc == EMBER_BC_ZERO_GRADIENT ||
+                            g.right_bc == EMBER_BC_FLOATING,
+                        "flame %d: bad right_bc %d", f, g.right_bc);
+        EMBER_CHECK_ARG(g.alpha >= 0, "flame %d: bad alpha %d", f, g.alpha);
+        for (int v = 0; v < n_vars; ++v) {
+            DiffSysInfo& s = info[f * n_vars + v];
+            s.n = g.n_points;
+            s.left_bc = g.left_bc;
+            s.right_bc = g.right_bc;
+            s.alpha = g.alpha;
+            s.grid_off = n_pts;
+            s.off = n_vals + int64_t(v) * g.n_points;
+        }
+        n_pts += g.n_points;
+        n_vals += int64_t(n_vars) * g.n_points;
+    }
+    EMBER_CHECK_ARG(opts->h != nullptr || (opts->dt_multiplier > 0 && opts->global_timestep > 0),
+                    "without explicit h, dt_multiplier and global_timestep must be positive");
+    EMBER_CHECK_ARG(opts->t_end > opts->t_start, "t_end must exceed t_start");
+
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    DiffSysInfo* d_info = nullptr;
+    EMBER_TRY(sc.alloc(&d_info, n_sys));
+    EMBER_CUDA_TRY(cudaMemcpyAsync(d_info, info.data(), sizeof(DiffSysInfo) * n_sys, cudaMemcpyHostToDevice, st));
+
+    DiffusionView dv;
+    dv.n_systems = n_sys;
+    dv.info = d_info;
+    EMBER_TRY(stage_in(sc, x, n_pts, mem, st, &dv.x));
+    EMBER_TRY(stage_in(sc, B, n_vals, mem, st, &dv.B));
+    EMBER_TRY(stage_in(sc, D, n_vals, mem, st, &dv.D));
+    EMBER_TRY(stage_in(sc, split_const, n_vals, mem, st, &dv.split_const));
+    EMBER_TRY(stage_in(sc, opts->h, n_sys, mem, st, &dv.h));
+    EMBER_TRY(stage_in(sc, opts->wall_const, n_sys, mem, st, &dv.wall_const));
+    EMBER_TRY(stage_in(sc, opts->y_inf, n_sys, mem, st, &dv.y_inf));
+    int* d_status = nullptr;
+    EMBER_TRY(sc.alloc(&d_status, n_sys));
+    dv.status = d_status;
+
+    // Matrix rows and integrator workspace.
+    double* work = nullptr;
+    EMBER_TRY(sc.alloc(&work, size_t(7) * n_vals));
+    dv.a = work;
+    dv.b = work + n_vals;
+    dv.c = work + 2 * n_vals;
+    dv.k = work + 3 * n_vals;
+
+    // State in/out.
+    double* d_y = nullptr;
+    if (mem == EMBER_MEM_DEVICE) {
+        d_y = y;
+    } else {
+        EMBER_TRY(sc.alloc(&d_y, n_vals));
+        EMBER_CUDA_TRY(cudaMemcpyAsync(d_y, y, sizeof(double) * n_vals, cudaMemcpyHostToDevice, st));
+    }
+
+    int nmax = 0;
+    for (int f = 0; f < n_flames; ++f) nmax = std::max(nmax, grids[f].n_points);
+    dim3 grid_rows(std::min(blocks_for(nmax, 256), 32), std::min(n_sys, 65535));
+    k_diffusion_rows<<<grid_rows, 256, 0, st>>>(dv);
+
+    TriBatchView tb;
+    tb.n_systems = n_sys;
+    tb.off = nullptr;
+    tb.info = d_info;
+    tb.a = dv.a;
+    tb.b = dv.b;
+    tb.c = dv.c;
+    tb.k = dv.k;
+    tb.y = d_y;
+    tb.yprev = work + 4 * n_vals;
+    tb.luc = work + 5 * n_vals;
+    tb.inv = work + 6 * n_vals;
+    k_diffusion_integrate_serial<<<blocks_for(n_sys, 64), 64, 0, st>>>(dv, tb, opts->t_start, opts->t_end,
+                                                                        opts->dt_multiplier, opts->global_timestep);
+    if (mem == EMBER_MEM_HOST) {
+        EMBER_CUDA_TRY(cudaMemcpyAsync(y, d_y, sizeof(double) * n_vals, cudaMemcpyDeviceToHost, st));
+    }
+    std::vector<int> h_status(n_sys);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    if (status) {
+        if (mem == EMBER_MEM_HOST) {
+            EMBER_CUDA_TRY(cudaMemcpyAsync(h_status.data(), d_status, sizeof(int) * n_sys, cudaMemcpyDeviceToHost, st));
+        } else {
+            EMBER_CUDA_TRY(cudaMemcpyAsync(status, d_status, sizeof(int) * n_sys, cudaMemcpyDeviceToDevice, st));
+        }
+    }
+    sc.release();
+    EMBER_TRY(finish_call(mem, st));
+    if (status && mem == EMBER_MEM_HOST) {
+        int bad = 0;
+        for (int s = 0; s < n_sys; ++s) {
+            status[s] = h_status[s];
+            if (h_status[s] != 0) ++bad;
+        }
+        if (bad) {
+            set_error("%d of %d diffusion systems failed (see status)", bad, n_sys);
+            return EMBER_EFAIL;
+        }
+    }
+    return EMBER_OK;
+}

@@ -1,0 +1,179 @@
+/*
+ * ember_gpu.h -- C ABI of the GB300 (sm_103a) split-step hot path of Ember.
+ *
+ * The library (libember_gpu.so) replaces, at the stage level, the two CPU
+ * loops of Ember's operator-split step:
+ *
+ *   - the diffusion stage: one TridiagonalIntegrator per state variable,
+ *     fed by a DiffusionSystem (src/integrator.cpp:37-204,
+ *     src/diffusionSystem.cpp:10-90), driven by
+ *     FlameSolver::integrateDiffusionTerms / setDiffusionSolverState
+ *     (src/flameSolver.cpp:702-718, 838-854);
+ *   - the production (chemistry source term) stage: one SourceSystem per grid
+ *     point (src/sourceSystem.cpp, src/qssintegrator.cpp), driven by
+ *     FlameSolver::integrateProductionTerms (src/flameSolver.cpp:754-836).
+ *
+ * Conventions
+ *   - Every entry point returns int: EMBER_OK (0) on success, a negative
+ *     EMBER_E* code on failure. None throws; the message of the last failure
+ *     on the calling thread is available from ember_last_error().
+ *   - Array arguments are borrowed for the duration of the call only.
+ *     `mem` selects where they live: EMBER_MEM_HOST (pageable or pinned host
+ *     memory; the call copies in and out and synchronises its stream) or
+ *     EMBER_MEM_DEVICE (device pointers; the call is asynchronous on
+ *     `stream` unless stated otherwise).
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *     stream), so this header needs no CUDA include.
+ *   - All arithmetic is IEEE binary64.
+ */
+#ifndef EMBER_GPU_H
+#define EMBER_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define EMBER_OK          0
+#define EMBER_EINVAL     -1   /* bad argument (size, pointer, option)          */
+#define EMBER_ECUDA      -2   /* a CUDA runtime call failed                      */
+#define EMBER_ENOMEM     -3   /* device allocation failed                        */
+#define EMBER_EFAIL      -4   /* at least one system/point failed: see status[] */
+
+#define EMBER_MEM_HOST    0
+#define EMBER_MEM_DEVICE  1
+
+/* Boundary conditions, same numbering as BoundaryCondition::BC in the
+ * reference (src/grid.h:7-26). Floating behaves as ZeroGradient in the
+ * diffusion matrix, as in DiffusionSystem::get_A (src/diffusionSystem.cpp:47-58). */
+#define EMBER_BC_FIXED_VALUE     0
+#define EMBER_BC_ZERO_GRADIENT   1
+#define EMBER_BC_CONTROL_VOLUME  2
+#define EMBER_BC_WALL_FLUX       3
+#define EMBER_BC_FLOATING        4
+
+/* Copy the last error message of the calling thread into buf (NUL-terminated,
+ * truncated to n bytes). Returns the full message length. */
+int ember_last_error(char* buf, size_t n);
+
+/* Library version as major*10000 + minor*100 + patch. */
+int ember_version(void);
+
+/* Number of CUDA devices visible (0 when none; never fails). */
+int ember_device_count(void);
+
+/* Measured FP64 throughput of the current device in FLOP/s, used as the
+ * roofline denominator of the FP64-bound kernels. kind 0: FP64 FMA pipe
+ * (DFMA); kind 1: FP64 tensor path (DMMA m8n8k4). No reference counterpart
+ * (the reference has no GPU code). */
+int ember_probe_fp64_rate(int kind, double* flops_per_second);
+
+/* ======================================================================
+ * Batched tridiagonal integrator
+ *
+ * A batch of independent linear ODE systems  y' = A y + k  with tridiagonal
+ * A (sub-diagonal a, diagonal b, super-diagonal c), integrated with the
+ * reference's TridiagonalIntegrator scheme (src/integrator.cpp:133-204):
+ * the first step after initialize() is 8 BDF1 sub-steps of h/8, later steps
+ * are BDF2, each a Thomas solve with the factorisation cached per step kind;
+ * integrate_to_time() rounds to an integral number of steps
+ * (src/integrator.cpp:37-47).
+ *
+ * System s occupies elements [offsets[s], offsets[s+1]) of every per-point
+ * array (CSR layout). Each system needs at least 2 points.
+ * The batch object keeps y, y_prev, t, h, the step count and the factorised
+ * coefficients on the device between calls, like one TridiagonalIntegrator
+ * per system.
+ * ==================================================================== */
+typedef struct ember_tridiag_s* ember_tridiag;
+
+/* Create a batch of n_systems systems; offsets (host, n_systems+1 entries,
+ * offsets[0] == 0, strictly increasing by >= 2) is copied.
+ * Replaces: TridiagonalIntegrator(ode) + resize(N) (src/integrator.cpp:77-108). */
+int ember_tridiag_create(int n_systems, const int64_t* offsets, ember_tridiag* out);
+int ember_tridiag_destroy(ember_tridiag batch);
+
+/* Set the constant ODE coefficients a, b, c, k (each offsets[n] values).
+ * Replaces: TridiagonalODE::get_A / get_k (src/integrator.h:22-35). */
+int ember_tridiag_set_coefficients(ember_tridiag batch, const double* a, const double* b,
+                                   const double* c, const double* k, int mem, void* stream);
+
+/* Set the state (offsets[n] values) and reset the step count.
+ * Replaces: TridiagonalIntegrator::set_y0 (src/integrator.cpp:111-115). */
+int ember_tridiag_set_y0(ember_tridiag batch, const double* y0, int mem, void* stream);
+
+/* Set start time and step size per system (n_systems values each) and reset
+ * the step count. Replaces: TridiagonalIntegrator::initialize (src/integrator.cpp:117-122). */
+int ember_tridiag_initialize(ember_tridiag batch, const double* t0, const double* h,
+                             int mem, void* stream);
+
+/* One step of every system. Replaces: TridiagonalIntegrator::step (src/integrator.cpp:133-204). */
+int ember_tridiag_step(ember_tridiag batch, void* stream);
+
+/* Integrate every system to its t_end (n_systems values).
+ * Replaces: Integrator::integrateToTime (src/integrator.cpp:37-47). */
+int ember_tridiag_integrate_to_time(ember_tridiag batch, const double* t_end, int mem, void* stream);
+
+/* Read back y (offsets[n] values), t and h (n_systems values each; either may be NULL).
+ * Replaces: get_y / get_t / get_h (src/integrator.cpp:25-35). */
+int ember_tridiag_get_state(ember_tridiag batch, double* y, double* t, double* h,
+                            int mem, void* stream);
+
+/* y' = A y + k for the current state (offsets[n] values).
+ * Replaces: TridiagonalIntegrator::get_ydot (src/integrator.cpp:124-131). */
+int ember_tridiag_get_ydot(ember_tridiag batch, double* ydot, int mem, void* stream);
+
+/* ======================================================================
+ * Diffusion stage
+ *
+ * One call = FlameSolver::integrateDiffusionTerms() for a batch of flames
+ * (src/flameSolver.cpp:838-854 with setDiffusionSolverState, 702-718):
+ * for every flame f and state variable v the matrix of DiffusionSystem::get_A
+ * and the constant of get_k are built from the grid, B, D, the split constant
+ * and the boundary conditions (src/diffusionSystem.cpp:10-76); the step size is
+ *     h = min(dt_multiplier * min_{1<=j<=N-2} dlj_j^2 / (B_j D_j), global_timestep)
+ * unless h is given explicitly; the system is initialised at t_start and
+ * integrated to t_end with the tridiagonal scheme above.
+ *
+ * Layout: flame f has n_points N_f; per-point arrays are concatenated over
+ * flames, and inside flame f they are variable-major: element (v, j) of
+ * flame f is at  var_offset_f + v*N_f + j  where var_offset_f =
+ * n_vars * sum_{g<f} N_g. (This is the row layout of DiffusionSystem::B/D/
+ * splitConst and of state.row(v).) Grid coordinates x are concatenated over
+ * flames (point_offset_f = sum_{g<f} N_g).
+ * ==================================================================== */
+typedef struct {
+    int n_points;   /* N_f >= 3                                          */
+    int left_bc;    /* EMBER_BC_*                                        */
+    int right_bc;   /* EMBER_BC_FIXED_VALUE / ZERO_GRADIENT / FLOATING   */
+    int alpha;      /* grid curvature exponent: 0 planar, 1 cylindrical  */
+} ember_diffusion_grid;
+
+typedef struct {
+    double t_start;            /* tStageStart                                   */
+    double t_end;              /* tStageEnd                                     */
+    double dt_multiplier;      /* Times.diffusionTimestepMultiplier (10)        */
+    double global_timestep;    /* Times.globalTimestep (2e-5)                   */
+    const double* h;           /* NULL, or explicit step per (flame, var)       */
+    const double* wall_const;  /* NULL (0), or per (flame, var): DiffusionSystem::wallConst */
+    const double* y_inf;       /* NULL (0), or per (flame, var): DiffusionSystem::yInf      */
+} ember_diffusion_options;
+
+/* x: grid coordinates; B, D, split_const: per point and variable (layout
+ * above); y: state in/out (same layout); status: n_flames*n_vars ints
+ * (0 = ok), may be NULL. Per-(flame,var) option arrays live in the same
+ * memory space as the other arrays. */
+int ember_diffusion_integrate(int n_flames, const ember_diffusion_grid* grids, int n_vars,
+                              const double* x, const double* B, const double* D,
+                              const double* split_const, double* y,
+                              const ember_diffusion_options* opts, int* status,
+                              int mem, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EMBER_GPU_H */
