@@ -1,0 +1,345 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 source-term / diffusion hot path.
+
+Default workload (the configuration the headline metric is quoted on): the
+isolated batched source-term step -- 4096 seeded constant-pressure reactor
+states of the seeded synthetic 150-species / 1000-reaction mechanism, each
+integrated over its own dt (log-uniform 1e-6..1e-4 s) by the QSS integrator
+with the reference's default options (interp kinetics), FP64, one launch per
+step. Metric: source-term point-integrations per second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload qss|bdf|diffusion]
+
+N > 1 runs under torch.distributed.run: every rank integrates its own batch
+of points (no data exchange; the path has none), value = all points / max
+time over ranks ("scaling": "weak").
+
+--impl reference times the reference algorithm's CPU implementation on the
+host cores: the reference itself (C++ on Cantera/SUNDIALS) cannot be built
+here, so this is the CPU oracle port (oracle/), threaded over points like the
+reference's TBB loop.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+N_POINTS = 4096
+MECH_SEED = 150_1000
+STATE_SEED = 4096
+METRIC = "source-term point-integrations/s"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--workload", default="qss", choices=["qss", "bdf", "diffusion"])
+    p.add_argument("--points", type=int, default=N_POINTS)
+    p.add_argument("--kinetics", default="interp", choices=["interp", "standard"])
+    p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ---------------------------------------------------------------- clocks --
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------ utilities --
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def workload_inputs(n_points: int, rank: int):
+    from ember_gb300.mechanism import synthetic_mechanism, reactor_states
+    mech = synthetic_mechanism(seed=MECH_SEED)
+    state, dt = reactor_states(mech, n_points, seed=STATE_SEED + rank)
+    return mech, state, dt
+
+
+def source_options(kinetics: str, method: str):
+    from ember_gb300.source import SourceOptions, KINETICS_INTERP, KINETICS_STANDARD
+    return SourceOptions.defaults(kinetics_model=KINETICS_INTERP if kinetics == "interp" else KINETICS_STANDARD)
+
+
+def cpu_sample_rate(mech, state, dt, opts, method: int, target_s: float, threads: int):
+    """Points/s of the CPU oracle on a bounded sample of the workload."""
+    from oracle import chem
+    om = chem.OracleMech(mech)
+    n = 16
+    t = 0.0
+    while True:
+        t0 = time.perf_counter()
+        om.integrate(method, state[:n], dt[:n], opts, n_threads=threads)
+        t = time.perf_counter() - t0
+        if t >= 0.25 * target_s or n >= len(state):
+            break
+        n = min(len(state), int(n * max(2.0, min(8.0, 0.3 * target_s / max(t, 1e-3)))))
+    # one more pass at the final sample size for the figure
+    t0 = time.perf_counter()
+    om.integrate(method, state[:n], dt[:n], opts, n_threads=threads)
+    t = time.perf_counter() - t0
+    return n / t, n, t
+
+
+# ------------------------------------------------------- reference arm --
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    from oracle import chem
+    method = chem.QSS if args.workload == "qss" else chem.BDF
+    mech, state, dt = workload_inputs(args.points, 0)
+    opts = source_options(args.kinetics, args.workload)
+    threads = os.cpu_count() or 1
+    om = chem.OracleMech(mech)
+    # size one step's sample to ~args.cpu_seconds/2 of host work
+    rate, n, t = cpu_sample_rate(mech, state, dt, opts, method, args.cpu_seconds / 2, threads)
+    for _ in range(args.warmup):
+        om.integrate(method, state[:n], dt[:n], opts, n_threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        om.integrate(method, state[:n], dt[:n], opts, n_threads=threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = n * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "points/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"C2 isolated source-term step, {args.workload.upper()}, {args.kinetics} kinetics, "
+                               f"synthetic 150-species/1000-reaction mechanism, {args.points} seeded states",
+                   "sample_points_per_step": n},
+        "cpu_baseline": {"value": value, "unit": "points/s", "cores": threads, "kind": "port",
+                         "sample": f"{n} of the {args.points} states per step, all host threads"},
+        "e2e": {"value": value, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# -------------------------------------------------------------- our arm --
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from ember_gb300 import _lib
+    from ember_gb300 import roofline
+    from ember_gb300.source import GpuMechanism, integrate_production_terms, QSS, BDF, STATS_WIDTH
+    import ctypes as C
+
+    lib = _lib.lib()
+    method = QSS if args.workload == "qss" else BDF
+    mech, state, dt = workload_inputs(args.points, rank)
+    opts = source_options(args.kinetics, args.workload)
+    gm = GpuMechanism(mech)
+    dev = torch.device("cuda", local)
+    st_d = torch.as_tensor(state, device=dev)
+    dt_d = torch.as_tensor(dt, device=dev)
+    out_d = torch.empty_like(st_d)
+    status_d = torch.zeros(args.points, dtype=torch.int32, device=dev)
+    stats_d = torch.zeros((args.points, STATS_WIDTH), dtype=torch.int32, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > 129 MB L2
+    stream = torch.cuda.current_stream()
+
+    peak = C.c_double()
+    _lib.check(lib.ember_probe_fp64_rate(0, C.byref(peak)), "probe")
+    fp64_peak = peak.value
+
+    def step():
+        integrate_production_terms(gm, method, st_d, dt_d, opts, out=out_d, status=status_d, stats=stats_d,
+                                   stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    w0 = time.perf_counter()
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record(stream)
+        step()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    wall = time.perf_counter() - w0
+    kernel_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(kernel_ms)
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+
+    # end to end through the public API with pinned host buffers (copies inside the call)
+    st_h = torch.as_tensor(state).pin_memory()
+    dt_h = torch.as_tensor(dt).pin_memory()
+    out_h = torch.empty_like(st_h).pin_memory()
+    status_h = torch.zeros(args.points, dtype=torch.int32).pin_memory()
+    stats_h = torch.zeros((args.points, STATS_WIDTH), dtype=torch.int32).pin_memory()
+
+    def step_host():
+        integrate_production_terms(gm, method, st_h.numpy(), dt_h.numpy(), opts, out=out_h.numpy(),
+                                   status=status_h.numpy(), stats=stats_h.numpy())
+
+    step_host()
+    if ws > 1:
+        torch.distributed.barrier()
+    e2e_times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step_host()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_s = sum(e2e_times)
+    if ws > 1:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    clocks = sampler.stop()
+
+    status = status_d.cpu().numpy()
+    stats = stats_d.cpu().numpy()
+    n_fail = int((status != 0).sum())
+    flops = float(roofline.qss_point_flops(mech, opts.kinetics_model, stats[:, 0], stats[:, 1]).sum())
+    avg_launch_s = total_ms / args.steps / 1e3
+    achieved = flops / avg_launch_s / 1e12
+    peak_t = fp64_peak / 1e12
+
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "qss_traffic.json")
+    if os.path.exists(prof):
+        try:
+            with open(prof) as f:
+                traffic = json.load(f).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+
+    line = {
+        "metric": METRIC, "value": ws * args.points * args.steps / (total_ms / 1e3), "unit": "points/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded mechanism and reactor states)",
+        "config": {"workload": f"C2 isolated source-term step, {args.workload.upper()}, {args.kinetics} kinetics, "
+                               f"synthetic 150-species/1000-reaction mechanism, {args.points} seeded states per GPU",
+                   "points_per_gpu": args.points, "n_vars": mech.n_vars, "n_reactions": mech.n_reactions,
+                   "l2": "256 MB buffer written between timed iterations", "parallelism": f"replicas x{ws}",
+                   "failed_points": n_fail,
+                   "mean_steps_per_point": float(stats[:, 0].mean()),
+                   "mean_rhs_calls_per_point": float(stats[:, 1].mean())},
+        "e2e": {"value": ws * args.points * args.steps / e2e_s, "unit": "points/s",
+                "h2d_bytes_per_step": int(state.nbytes + dt.nbytes),
+                "d2h_bytes_per_step": int(state.nbytes + status_h.numpy().nbytes + stats_h.numpy().nbytes)},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_t, "unit": "TFLOP/s",
+                     "frac": achieved / peak_t, "traffic": traffic,
+                     "peak_source": "live DFMA throughput probe (ember_probe_fp64_rate); MEASURED_PEAKS.json "
+                                    "has no FP64 figure",
+                     "work_model": "algorithmic flops of ember_gb300/roofline.py (exp/log/div = 1 flop)"},
+        "clocks": clocks,
+        "wall_s_timed_region": wall,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle import chem
+        threads = os.cpu_count() or 1
+        rate, n, t = cpu_sample_rate(mech, state, dt, opts, method, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
+                                "sample": f"first {n} of the {args.points} states, {t:.1f} s on {threads} threads"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -17,6 +17,9 @@ CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libember_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Translation units whose arithmetic must match the CPU oracle operation by
+# operation: no automatic multiply-add contraction (explicit fma() only).
+FILE_FLAGS = {"source.cu": ["--fmad=false"], "bdf.cu": ["--fmad=false"]}
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
@@ -51,7 +54,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
 
     def compile_one(src: str) -> str:
         obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
-        cmd = [cc, "-c", src, "-o", obj] + flags
+        cmd = [cc, "-c", src, "-o", obj] + flags + FILE_FLAGS.get(os.path.basename(src), [])
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {os.path.basename(src)}:\n{r.stdout}\n{r.stderr}")

@@ -60,6 +60,17 @@ def _declare(lib):
         "ember_tridiag_get_ydot": (C.c_int, [vp, vp, C.c_int, vp]),
         "ember_diffusion_integrate": (C.c_int, [C.c_int, C.POINTER(DiffusionGrid), C.c_int, vp, vp, vp, vp, vp,
                                                 C.POINTER(DiffusionOptions), vp, C.c_int, vp]),
+        "ember_probe_fp64_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
+        "ember_mech_create": (C.c_int, [vp, C.POINTER(vp)]),
+        "ember_mech_destroy": (C.c_int, [vp]),
+        "ember_mech_set_multipliers": (C.c_int, [vp, vp, C.c_int, vp]),
+        "ember_gas_eval": (C.c_int, [vp, C.c_int, C.c_double, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp,
+                                     C.c_int, vp]),
+        "ember_source_options_default": (C.c_int, [vp]),
+        "ember_selftest_qss_cesium": (C.c_int, [C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
+                                                C.c_int, C.c_int, C.c_double, C.c_int, vp, vp]),
+        "ember_source_integrate": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp, vp, vp,
+                                             C.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -1,0 +1,752 @@
+// Production (chemistry source term) stage on the GPU: mechanism upload,
+// thermo/rate evaluation and the QSS source-term integrator.
+//
+// One warp integrates one grid point; warps of a persistent grid take points
+// from an atomic work counter, so that points needing many sub-steps do not
+// hold up the others (the reference runs the same per-point integrations
+// from a TBB parallel_for over points, src/flameSolver.cpp:754-836).
+//
+// Compiled with --fmad=false: only the fma() calls written in chem.cuh,
+// emath.cuh and here are fused, in the same places as in the CPU oracle.
+#include "common.cuh"
+#include "chem.cuh"
+#include "qss.cuh"
+#include "source.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace ember {
+
+// ------------------------------------------------------- table building --
+
+// Rate constants and 1/Kc at the table nodes (one warp per node), from the
+// same device functions as the standard model: InterpKinetics::updateROP /
+// MultiArrheniusInterp::rebuildInterpData (src/chemistry0d.cpp:278-326, 401-436).
+__global__ void k_build_tables(MechView m, double* work) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (warp >= m.nT) return;
+    ChemSmem w;
+    w.carve(work + size_t(warp) * ChemSmem::doubles(m.S, m.R), m.S, m.R);
+    const double T = m.Tmin + ((double)warp) / (m.nT - 1) * (m.Tmax - m.Tmin);
+    chem_rate_constants(m, w, T, 0);
+    double2* kf = const_cast<double2*>(m.kf_tab) + size_t(warp) * m.R;
+    double2* kc = const_cast<double2*>(m.kc_tab) + size_t(warp) * m.R;
+    for (int i = lane_id(); i < m.R; i += 32) {
+        kf[i].x = w.kf[i];
+        kc[i].x = w.rkc[i];
+    }
+}
+
+__global__ void k_table_slopes(MechView m) {
+    const double dT = (m.Tmax - m.Tmin) / (m.nT - 1);
+    const size_t total = size_t(m.nT) * m.R;
+    for (size_t e = blockIdx.x * size_t(blockDim.x) + threadIdx.x; e < total; e += size_t(gridDim.x) * blockDim.x) {
+        const int n = static_cast<int>(e / m.R);
+        double2* kf = const_cast<double2*>(m.kf_tab);
+        double2* kc = const_cast<double2*>(m.kc_tab);
+        if (n < m.nT - 1) {
+            kf[e].y = (kf[e + m.R].x - kf[e].x) / dT;
+            kc[e].y = (kc[e + m.R].x - kc[e].x) / dT;
+        } else {
+            kf[e].y = 0.0;
+            kc[e].y = 0.0;
+        }
+    }
+}
+
+// ------------------------------------------------------------- gas eval --
+
+__global__ void k_gas_eval(MechView m, int n, double p, int model, int mode, const double* __restrict__ T,
+                           const double* __restrict__ Y, double* creation, double* destruction, double* net,
+                           double* hk, double* cp_mass, double* density) {
+    extern __shared__ double smem[];
+    const int wib = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    const size_t per = ChemSmem::doubles(m.S, m.R) + m.S;
+    double* base = smem + wib * per;
+    ChemSmem w;
+    w.carve(base, m.S, m.R);
+    double* y = base + ChemSmem::doubles(m.S, m.R);
+    for (int j = blockIdx.x * wpb + wib; j < n; j += gridDim.x * wpb) {
+        for (int k = lane_id(); k < m.S; k += 32) y[k] = Y[size_t(j) * m.S + k];
+        __syncwarp();
+        const double Tj = T[j];
+        chem_rate_constants(m, w, Tj, model == KIN_INTERP);
+        double rho, cp;
+        chem_rates(m, w, p, mode, Tj, y, rho, cp, true);
+        for (int k = lane_id(); k < m.S; k += 32) {
+            const size_t o = size_t(j) * m.S + k;
+            if (creation) creation[o] = w.wq[k];
+            if (destruction) destruction[o] = w.wd[k];
+            if (net) net[o] = w.wn[k];
+            if (hk) hk[o] = w.hk[k];
+        }
+        if (lane_id() == 0) {
+            if (cp_mass) cp_mass[j] = cp;
+            if (density) density[j] = rho;
+        }
+        __syncwarp();
+    }
+}
+
+// ------------------------------------------------------ QSS source term --
+
+// SourceSystemQSS::odefun (src/sourceSystem.cpp:445-499): q/d of
+// [U, T, Y]; T and the thermo (h_k, rho, cp) are refreshed only on
+// predictor calls (src/sourceSystem.cpp:461-463, 501-515).
+struct SourceQssOde {
+    const MechView* m;
+    ChemSmem* w;
+    const SourceArgs* a;
+    const double* split;  // this point's split constants (global) or null
+    double x;
+    double T;
+    double rho, cp;
+    double cachedT;
+    double* hk_pred;      // [S] in shared memory
+
+    __device__ void eval(double t, const double* y, double* q, double* d, bool corrector) {
+        const MechView& M = *m;
+        const int S = M.S;
+        const int lane = lane_id();
+        if (!corrector) T = y[1];
+        if (!(cachedT == T)) {
+            chem_rate_constants(M, *w, T, a->kinetics_model == KIN_INTERP);
+            cachedT = T;
+        }
+        double rho_c, cp_c;
+        chem_rates(M, *w, a->pressure, STATE_NORMALIZED, T, y + 2, rho_c, cp_c, false);
+        if (!corrector) {
+            for (int k = lane; k < S; k += 32) hk_pred[k] = w->hk[k];
+            rho = rho_c;
+            cp = cp_c;
+            __syncwarp();
+        }
+        double part = 0.0;
+        for (int k = lane; k < S; k += 32) part = part + (w->wq[k] - w->wd[k]) * hk_pred[k];
+        const double qdot = -warp_sum_partial(part) + igniter(*a, t, x);
+        const double rc = rho * cp;
+        for (int i = lane; i < S + 2; i += 32) {
+            const double sc = split ? split[i] : 0.0;
+            if (i == 0) {
+                q[0] = sc;
+                d[0] = 0.0;
+            } else if (i == 1) {
+                q[1] = qdot / rc + sc;
+                d[1] = 0.0 / rc;
+            } else {
+                const int k = i - 2;
+                q[i] = (w->wq[k] * M.W[k]) / rho + sc;
+                d[i] = (w->wd[k] * M.W[k]) / rho;
+            }
+        }
+        __syncwarp();
+    }
+};
+
+struct EnforceNotMomentum {
+    __device__ bool operator()(int i) const { return i != 0; }
+};
+
+__global__ void __launch_bounds__(128) k_source_qss(MechView m, SourceArgs a, int* counter) {
+    extern __shared__ double smem[];
+    const int n = m.S + 2;
+    const int wib = threadIdx.x >> 5;
+    const size_t per = qss_smem_doubles(m.S, m.R);
+    double* base = smem + wib * per;
+    ChemSmem w;
+    w.carve(base, m.S, m.R);
+    QssSmem v;
+    v.carve(base + ChemSmem::doubles(m.S, m.R), n);
+    double* hk_pred = base + ChemSmem::doubles(m.S, m.R) + QssSmem::doubles(n);
+    QssParams P;
+    P.epsmin = a.qss_epsmin;
+    P.epsmax = a.qss_epsmax;
+    P.dtmin = a.qss_dtmin;
+    P.dtmax = a.qss_dtmax;
+    P.abstol = a.qss_abstol;
+    P.itermax = a.qss_itermax;
+    P.stability_check = a.qss_stability_check;
+    P.max_steps = a.max_steps;
+    SourceQssOde ode;
+    ode.m = &m;
+    ode.w = &w;
+    ode.a = &a;
+    ode.hk_pred = hk_pred;
+    ode.cachedT = __longlong_as_double(0x7ff8000000000000LL);  // NaN: nothing cached
+    const int lane = lane_id();
+    for (;;) {
+        int j = 0;
+        if (lane == 0) j = atomicAdd(counter, 1);
+        j = __shfl_sync(0xffffffffu, j, 0);
+        if (j >= a.n) break;
+        const double* yin = a.state_in + size_t(j) * n;
+        for (int i = lane; i < n; i += 32) {
+            v.y[i] = yin[i];
+            v.ymin[i] = (i == 0) ? -1e4 : a.qss_minval;
+        }
+        __syncwarp();
+        ode.split = a.split ? a.split + size_t(j) * n : nullptr;
+        ode.x = a.x ? a.x[j] : 0.0;
+        ode.T = v.y[1];
+        ode.rho = 1.0;
+        ode.cp = 1.0;
+        QssStats st;
+        int ret = qss_integrate_warp(ode, v, n, P, EnforceNotMomentum(), a.dt[j], a.t_start, st);
+        bool finite = true;
+        double* yout = a.state_out + size_t(j) * n;
+        for (int i = lane; i < n; i += 32) {
+            const double yi = v.y[i];
+            finite = finite && isfinite(yi);
+            yout[i] = yi;
+        }
+        finite = __all_sync(0xffffffffu, finite);
+        if (ret == 0 && !finite) ret = -21;
+        if (lane == 0) {
+            a.status[j] = ret;
+            if (a.stats) {
+                a.stats[4 * size_t(j) + 0] = st.steps;
+                a.stats[4 * size_t(j) + 1] = st.gcount;
+                a.stats[4 * size_t(j) + 2] = st.rcount;
+                a.stats[4 * size_t(j) + 3] = 0;
+            }
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace ember
+
+// ================================================================ C ABI ==
+
+using namespace ember;
+
+struct ember_mech_s {
+    int S = 0, R = 0;
+    void* blob = nullptr;  // one device allocation holding every table
+    MechView view{};
+    std::vector<double> mult_host;
+};
+
+namespace {
+
+template <class T>
+T* carve_dev(char*& p, size_t count) {
+    T* r = reinterpret_cast<T*>(p);
+    p += ((count * sizeof(T) + 255) / 256) * 256;
+    return r;
+}
+
+size_t carve_size(size_t count, size_t elem) { return ((count * elem + 255) / 256) * 256; }
+
+}  // namespace
+
+extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
+    EMBER_CHECK_ARG(out != nullptr && d != nullptr, "null argument");
+    *out = nullptr;
+    const int S = d->n_species, R = d->n_reactions;
+    EMBER_CHECK_ARG(S >= 1 && R >= 0 && R < (1 << 24), "bad mechanism size (S=%d, R=%d)", S, R);
+    EMBER_CHECK_ARG(d->mol_weight && d->nasa_tmid && d->nasa_coeffs, "null species arrays");
+    EMBER_CHECK_ARG(R == 0 || (d->rxn_type && d->reversible && d->reactants && d->products && d->arrhenius &&
+                               d->arrhenius_low && d->troe && d->default_efficiency && d->efficiency_offsets),
+                    "null reaction arrays");
+    for (int k = 0; k < S; ++k) EMBER_CHECK_ARG(d->mol_weight[k] > 0, "species %d: molecular weight must be > 0", k);
+    const int64_t ne = R ? d->efficiency_offsets[R] : 0;
+    EMBER_CHECK_ARG(R == 0 || d->efficiency_offsets[0] == 0, "efficiency_offsets[0] must be 0");
+    for (int i = 0; i < R; ++i) {
+        EMBER_CHECK_ARG(d->rxn_type[i] >= 0 && d->rxn_type[i] <= 3, "reaction %d: bad type %d", i, d->rxn_type[i]);
+        EMBER_CHECK_ARG(d->efficiency_offsets[i + 1] >= d->efficiency_offsets[i], "reaction %d: bad efficiency offsets", i);
+        int nr = 0, np = 0;
+        for (int o = 0; o < EMBER_MAX_STOICH; ++o) {
+            int r = d->reactants[i * EMBER_MAX_STOICH + o], p = d->products[i * EMBER_MAX_STOICH + o];
+            EMBER_CHECK_ARG(r >= -1 && r < S && p >= -1 && p < S, "reaction %d: species index out of range", i);
+            nr += r >= 0;
+            np += p >= 0;
+        }
+        EMBER_CHECK_ARG(nr >= 1 && np >= 1, "reaction %d: needs at least one reactant and one product", i);
+    }
+    EMBER_CHECK_ARG(ne == 0 || (d->efficiency_species && d->efficiency_values), "null efficiency arrays");
+    for (int64_t e = 0; e < ne; ++e)
+        EMBER_CHECK_ARG(d->efficiency_species[e] >= 0 && d->efficiency_species[e] < S, "efficiency entry %lld: bad species",
+                        (long long)e);
+    EMBER_TRY(ensure_device());
+
+    // Host-side derived tables.
+    std::vector<double> rW(S), hc(size_t(S) * 10), sc(size_t(S) * 8), dn(std::max(R, 1)), mult(std::max(R, 1), 1.0);
+    for (int k = 0; k < S; ++k) {
+        rW[k] = 1.0 / d->mol_weight[k];
+        for (int r = 0; r < 2; ++r) {
+            const double* a = d->nasa_coeffs + 14 * k + 7 * r;
+            double* h = hc.data() + 10 * k + 5 * r;
+            double* s = sc.data() + 8 * k + 4 * r;
+            h[0] = a[0];
+            h[1] = a[1] / 2.0;
+            h[2] = a[2] / 3.0;
+            h[3] = a[3] / 4.0;
+            h[4] = a[4] / 5.0;
+            s[0] = a[1];
+            s[1] = a[2] / 2.0;
+            s[2] = a[3] / 3.0;
+            s[3] = a[4] / 4.0;
+        }
+    }
+    std::vector<int> sp_off(S + 1, 0), sp_ent;
+    std::vector<std::vector<int>> lists(S);
+    for (int i = 0; i < R; ++i) {
+        std::vector<std::pair<int, int>> cnt;  // species -> occurrences as product (low 4 bits) / reactant (x16)
+        auto bump = [&](int k, int isprod) {
+            for (auto& c : cnt)
+                if ((c.first & 0xffffff) == k) {
+                    c.second += isprod ? 1 : 16;
+                    return;
+                }
+            cnt.push_back({k, isprod ? 1 : 16});
+        };
+        int nprod = 0, nreac = 0;
+        for (int o = 0; o < EMBER_MAX_STOICH; ++o) {
+            int p = d->products[i * EMBER_MAX_STOICH + o];
+            int r = d->reactants[i * EMBER_MAX_STOICH + o];
+            if (p >= 0) { bump(p, 1); ++nprod; }
+            if (r >= 0) { bump(r, 0); ++nreac; }
+        }
+        dn[i] = static_cast<double>(nprod - nreac);
+        for (auto& c : cnt) {
+            int npk = c.second & 15, nrk = c.second >> 4;
+            lists[c.first].push_back(i | (npk << 24) | (nrk << 28));
+        }
+    }
+    for (int k = 0; k < S; ++k) {
+        sp_off[k + 1] = sp_off[k] + static_cast<int>(lists[k].size());
+        sp_ent.insert(sp_ent.end(), lists[k].begin(), lists[k].end());
+    }
+    std::vector<int> eff_off(R + 1, 0);
+    for (int i = 0; i <= R; ++i) eff_off[i] = R ? static_cast<int>(d->efficiency_offsets[i]) : 0;
+
+    const int nT = 200;
+    const size_t Rs = std::max(R, 1);
+    size_t bytes = carve_size(S, 8) * 3 + carve_size(size_t(S) * 14, 8) + carve_size(size_t(S) * 10, 8) +
+                   carve_size(size_t(S) * 8, 8) + carve_size(Rs, 4) * 2 + carve_size(Rs * 4, 4) * 2 +
+                   carve_size(Rs * 3, 8) * 2 + carve_size(Rs * 4, 8) + carve_size(Rs, 8) * 3 +
+                   carve_size(Rs + 1, 4) + carve_size(std::max<int64_t>(ne, 1), 4) +
+                   carve_size(std::max<int64_t>(ne, 1), 8) + carve_size(S + 1, 4) +
+                   carve_size(std::max<size_t>(sp_ent.size(), 1), 4) + carve_size(size_t(nT) * Rs, 16) * 2;
+    auto* mh = new ember_mech_s;
+    mh->S = S;
+    mh->R = R;
+    cudaError_t e = cudaMalloc(&mh->blob, bytes);
+    if (e != cudaSuccess) {
+        delete mh;
+        set_error("ember_mech_create: cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+        return EMBER_ENOMEM;
+    }
+    char* p = static_cast<char*>(mh->blob);
+    MechView& v = mh->view;
+    v.S = S;
+    v.R = R;
+    v.nT = nT;
+    v.Tmin = 273.0;
+    v.Tmax = 3500.0;
+    double* W = carve_dev<double>(p, S);
+    double* rWd = carve_dev<double>(p, S);
+    double* tmid = carve_dev<double>(p, S);
+    double* nasa = carve_dev<double>(p, size_t(S) * 14);
+    double* hcd = carve_dev<double>(p, size_t(S) * 10);
+    double* scd = carve_dev<double>(p, size_t(S) * 8);
+    int* type = carve_dev<int>(p, Rs);
+    int* rev = carve_dev<int>(p, Rs);
+    int* reac = carve_dev<int>(p, Rs * 4);
+    int* prod = carve_dev<int>(p, Rs * 4);
+    double* arr = carve_dev<double>(p, Rs * 3);
+    double* arr_low = carve_dev<double>(p, Rs * 3);
+    double* troe = carve_dev<double>(p, Rs * 4);
+    double* def_eff = carve_dev<double>(p, Rs);
+    double* multd = carve_dev<double>(p, Rs);
+    double* dnd = carve_dev<double>(p, Rs);
+    int* eoff = carve_dev<int>(p, Rs + 1);
+    int* esp = carve_dev<int>(p, std::max<int64_t>(ne, 1));
+    double* eval = carve_dev<double>(p, std::max<int64_t>(ne, 1));
+    int* spo = carve_dev<int>(p, S + 1);
+    int* spe = carve_dev<int>(p, std::max<size_t>(sp_ent.size(), 1));
+    double2* kft = carve_dev<double2>(p, size_t(nT) * Rs);
+    double2* kct = carve_dev<double2>(p, size_t(nT) * Rs);
+    auto up = [&](void* dst, const void* src, size_t n) {
+        if (e == cudaSuccess && n) e = cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice);
+    };
+    up(W, d->mol_weight, sizeof(double) * S);
+    up(rWd, rW.data(), sizeof(double) * S);
+    up(tmid, d->nasa_tmid, sizeof(double) * S);
+    up(nasa, d->nasa_coeffs, sizeof(double) * S * 14);
+    up(hcd, hc.data(), sizeof(double) * S * 10);
+    up(scd, sc.data(), sizeof(double) * S * 8);
+    if (R) {
+        up(type, d->rxn_type, sizeof(int) * R);
+        up(rev, d->reversible, sizeof(int) * R);
+        up(reac, d->reactants, sizeof(int) * R * 4);
+        up(prod, d->products, sizeof(int) * R * 4);
+        up(arr, d->arrhenius, sizeof(double) * R * 3);
+        up(arr_low, d->arrhenius_low, sizeof(double) * R * 3);
+        up(troe, d->troe, sizeof(double) * R * 4);
+        up(def_eff, d->default_efficiency, sizeof(double) * R);
+        up(multd, mult.data(), sizeof(double) * R);
+        up(dnd, dn.data(), sizeof(double) * R);
+        up(eoff, eff_off.data(), sizeof(int) * (R + 1));
+        up(esp, d->efficiency_species, sizeof(int) * ne);
+        up(eval, d->efficiency_values, sizeof(double) * ne);
+    }
+    up(spo, sp_off.data(), sizeof(int) * (S + 1));
+    up(spe, sp_ent.data(), sizeof(int) * sp_ent.size());
+    v.W = W;
+    v.rW = rWd;
+    v.tmid = tmid;
+    v.nasa = nasa;
+    v.hc = hcd;
+    v.sc = scd;
+    v.type = type;
+    v.rev = rev;
+    v.reac = reac;
+    v.prod = prod;
+    v.arr = arr;
+    v.arr_low = arr_low;
+    v.troe = troe;
+    v.def_eff = def_eff;
+    v.eff_off = eoff;
+    v.eff_sp = esp;
+    v.eff_val = eval;
+    v.mult = multd;
+    v.dn = dnd;
+    v.sp_off = spo;
+    v.sp_ent = spe;
+    v.kf_tab = kft;
+    v.kc_tab = kct;
+    if (e == cudaSuccess && R) {
+        double* work = nullptr;
+        e = cudaMalloc(&work, sizeof(double) * ChemSmem::doubles(S, R) * nT);
+        if (e == cudaSuccess) {
+            k_build_tables<<<(nT * 32 + 127) / 128, 128>>>(v, work);
+            k_table_slopes<<<std::min<int64_t>((int64_t(nT) * R + 255) / 256, 4096), 256>>>(v);
+            e = cudaDeviceSynchronize();
+            cudaFree(work);
+        }
+    }
+    if (e != cudaSuccess) {
+        set_error("ember_mech_create: %s", cudaGetErrorString(e));
+        cudaFree(mh->blob);
+        delete mh;
+        return EMBER_ECUDA;
+    }
+    mh->mult_host = mult;
+    *out = mh;
+    return EMBER_OK;
+}
+
+extern "C" int ember_mech_destroy(ember_mech m) {
+    if (!m) return EMBER_OK;
+    cudaFree(m->blob);
+    delete m;
+    return EMBER_OK;
+}
+
+extern "C" int ember_mech_set_multipliers(ember_mech m, const double* mult, int mem, void* stream) {
+    EMBER_CHECK_ARG(m != nullptr, "null mechanism");
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    if (m->R == 0) return EMBER_OK;
+    cudaStream_t st = as_stream(stream);
+    double* dst = const_cast<double*>(m->view.mult);
+    if (mult == nullptr) {
+        std::vector<double> ones(m->R, 1.0);
+        EMBER_CUDA_TRY(cudaMemcpyAsync(dst, ones.data(), sizeof(double) * m->R, cudaMemcpyHostToDevice, st));
+        EMBER_CUDA_TRY(cudaStreamSynchronize(st));
+        return EMBER_OK;
+    }
+    EMBER_CUDA_TRY(cudaMemcpyAsync(dst, mult, sizeof(double) * m->R,
+                                   mem == EMBER_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
+    return finish_call(mem, st);
+}
+
+namespace ember {
+const MechView* mech_view(ember_mech m) { return m ? &m->view : nullptr; }
+}  // namespace ember
+
+extern "C" int ember_gas_eval(ember_mech m, int n, double pressure, int model, int mode, const double* T,
+                              const double* Y, double* creation, double* destruction, double* net, double* hk,
+                              double* cp_mass, double* density, int mem, void* stream) {
+    EMBER_CHECK_ARG(m != nullptr, "null mechanism");
+    EMBER_CHECK_ARG(n >= 0 && T && Y, "bad points / null T or Y");
+    EMBER_CHECK_ARG(model == EMBER_KINETICS_STANDARD || model == EMBER_KINETICS_INTERP, "bad kinetics model");
+    EMBER_CHECK_ARG(mode == EMBER_STATE_NORMALIZED || mode == EMBER_STATE_NO_NORM, "bad state mode");
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_CHECK_ARG(pressure > 0, "pressure must be positive");
+    if (n == 0) return EMBER_OK;
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    const int S = m->S;
+    const double *dT, *dY;
+    EMBER_TRY(stage_in(sc, T, n, mem, st, &dT));
+    EMBER_TRY(stage_in(sc, Y, size_t(n) * S, mem, st, &dY));
+    double *c1, *c2, *c3, *c4, *c5, *c6;
+    EMBER_TRY(stage_buffer(sc, creation, size_t(n) * S, mem, &c1));
+    EMBER_TRY(stage_buffer(sc, destruction, size_t(n) * S, mem, &c2));
+    EMBER_TRY(stage_buffer(sc, net, size_t(n) * S, mem, &c3));
+    EMBER_TRY(stage_buffer(sc, hk, size_t(n) * S, mem, &c4));
+    EMBER_TRY(stage_buffer(sc, cp_mass, n, mem, &c5));
+    EMBER_TRY(stage_buffer(sc, density, n, mem, &c6));
+    const size_t per = (ChemSmem::doubles(S, m->R) + S) * sizeof(double);
+    int warps = 4;
+    while (warps > 1 && per * warps > 200 * 1024) warps /= 2;
+    EMBER_CHECK_ARG(per * warps <= 227 * 1024, "mechanism too large for the shared-memory work area");
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_gas_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per * warps)));
+    const int blocks = std::min((n + warps - 1) / warps, 65535);
+    k_gas_eval<<<blocks, 32 * warps, per * warps, st>>>(m->view, n, pressure, model, mode, dT, dY, c1, c2, c3, c4,
+                                                        c5, c6);
+    EMBER_TRY(stage_out(creation, c1, size_t(n) * S, mem, st));
+    EMBER_TRY(stage_out(destruction, c2, size_t(n) * S, mem, st));
+    EMBER_TRY(stage_out(net, c3, size_t(n) * S, mem, st));
+    EMBER_TRY(stage_out(hk, c4, size_t(n) * S, mem, st));
+    EMBER_TRY(stage_out(cp_mass, c5, n, mem, st));
+    EMBER_TRY(stage_out(density, c6, n, mem, st));
+    sc.release();
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_source_options_default(ember_source_options* o) {
+    EMBER_CHECK_ARG(o != nullptr, "null options");
+    *o = ember_source_options{};
+    o->pressure = 101325.0;
+    o->kinetics_model = EMBER_KINETICS_INTERP;
+    o->max_steps = 1000000;
+    o->qss_epsmin = 2e-2;
+    o->qss_epsmax = 10.0;
+    o->qss_dtmin = 1e-16;
+    o->qss_dtmax = 1e-6;
+    o->qss_abstol = 1e-11;
+    o->qss_minval = 1e-60;
+    o->qss_iteration_count = 1;
+    o->qss_stability_check = 0;
+    o->bdf_reltol = 1e-6;
+    o->bdf_abstol_momentum = 1e-7;
+    o->bdf_abstol_energy = 1e-8;
+    o->bdf_abstol_species = 1e-13;
+    o->bdf_min_step = 1e-18;
+    o->bdf_max_num_steps = 1000000;
+    o->ignition_duration = 1e-3;
+    o->ignition_stddev = 1e-4;
+    return EMBER_OK;
+}
+
+namespace ember {
+
+int source_check_options(const ember_source_options* o) {
+    EMBER_CHECK_ARG(o != nullptr, "null options");
+    EMBER_CHECK_ARG(o->pressure > 0, "pressure must be positive");
+    EMBER_CHECK_ARG(o->kinetics_model == EMBER_KINETICS_STANDARD || o->kinetics_model == EMBER_KINETICS_INTERP,
+                    "bad kinetics model %d", o->kinetics_model);
+    EMBER_CHECK_ARG(o->max_steps > 0, "max_steps must be positive");
+    EMBER_CHECK_ARG(o->qss_epsmin > 0 && o->qss_epsmax > 0 && o->qss_dtmax > 0 && o->qss_iteration_count >= 0,
+                    "bad QSS tolerances");
+    EMBER_CHECK_ARG(o->bdf_reltol > 0 && o->bdf_abstol_momentum > 0 && o->bdf_abstol_energy > 0 &&
+                        o->bdf_abstol_species > 0 && o->bdf_max_num_steps > 0,
+                    "bad BDF tolerances");
+    return EMBER_OK;
+}
+
+SourceArgs make_source_args(const ember_source_options* o, int n, const double* state_in, const double* split,
+                            const double* dt, double t_start, const double* x, double* state_out, int* status,
+                            int* stats) {
+    SourceArgs a{};
+    a.n = n;
+    a.state_in = state_in;
+    a.split = split;
+    a.dt = dt;
+    a.t_start = t_start;
+    a.x = x;
+    a.state_out = state_out;
+    a.status = status;
+    a.stats = stats;
+    a.pressure = o->pressure;
+    a.kinetics_model = o->kinetics_model;
+    a.max_steps = o->max_steps;
+    a.qss_epsmin = o->qss_epsmin;
+    a.qss_epsmax = o->qss_epsmax;
+    a.qss_dtmin = o->qss_dtmin;
+    a.qss_dtmax = o->qss_dtmax;
+    a.qss_abstol = o->qss_abstol;
+    a.qss_minval = o->qss_minval;
+    a.qss_itermax = o->qss_iteration_count;
+    a.qss_stability_check = o->qss_stability_check;
+    a.bdf_reltol = o->bdf_reltol;
+    a.bdf_atol_u = o->bdf_abstol_momentum;
+    a.bdf_atol_t = o->bdf_abstol_energy;
+    a.bdf_atol_y = o->bdf_abstol_species;
+    a.bdf_min_step = o->bdf_min_step;
+    a.bdf_max_steps = o->bdf_max_num_steps;
+    a.ign_tstart = o->ignition_tstart;
+    a.ign_duration = o->ignition_duration;
+    a.ign_energy = o->ignition_energy;
+    a.ign_center = o->ignition_center;
+    a.ign_stddev = o->ignition_stddev;
+    return a;
+}
+
+int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, cudaStream_t st) {
+    const int n = m.S + 2;
+    const size_t per = qss_smem_doubles(m.S, m.R) * sizeof(double);
+    int warps = 4;
+    while (warps > 1 && per * warps > 227 * 1024) warps /= 2;
+    EMBER_CHECK_ARG(per * warps <= 227 * 1024, "mechanism too large for the QSS shared-memory work area (%zu B)", per);
+    (void)n;
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_qss, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per * warps)));
+    int dev = 0, sms = 0, per_sm = 0;
+    EMBER_CUDA_TRY(cudaGetDevice(&dev));
+    EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    EMBER_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_source_qss, 32 * warps, per * warps));
+    per_sm = std::max(per_sm, 1);
+    const int blocks = std::max(1, std::min((a.n + warps - 1) / warps, sms * per_sm));
+    k_source_qss<<<blocks, 32 * warps, per * warps, st>>>(m, a, counter);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
+}  // namespace ember
+
+extern "C" int ember_source_integrate(ember_mech m, int method, int n, const double* state_in,
+                                      const double* split_const, const double* dt, double t_start, const double* x,
+                                      const ember_source_options* opts, double* state_out, int* status, int* stats,
+                                      int mem, void* stream) {
+    EMBER_CHECK_ARG(m != nullptr, "null mechanism");
+    EMBER_CHECK_ARG(method == EMBER_SOURCE_QSS || method == EMBER_SOURCE_BDF, "bad method %d", method);
+    EMBER_CHECK_ARG(n >= 0, "n_points must be >= 0");
+    EMBER_CHECK_ARG(n == 0 || (state_in && dt && state_out && status), "null state_in/dt/state_out/status");
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_TRY(source_check_options(opts));
+    if (n == 0) return EMBER_OK;
+    EMBER_TRY(ensure_device());
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    const int nv = m->S + 2;
+    const double *d_in, *d_split, *d_dt, *d_x;
+    EMBER_TRY(stage_in(sc, state_in, size_t(n) * nv, mem, st, &d_in));
+    EMBER_TRY(stage_in(sc, split_const, size_t(n) * nv, mem, st, &d_split));
+    EMBER_TRY(stage_in(sc, dt, n, mem, st, &d_dt));
+    EMBER_TRY(stage_in(sc, x, n, mem, st, &d_x));
+    double* d_out;
+    int *d_status, *d_stats;
+    EMBER_TRY(stage_buffer(sc, state_out, size_t(n) * nv, mem, &d_out));
+    EMBER_TRY(stage_buffer(sc, status, n, mem, &d_status));
+    EMBER_TRY(stage_buffer(sc, stats, size_t(n) * EMBER_STATS_WIDTH, mem, &d_stats));
+    int* counter = nullptr;
+    EMBER_TRY(sc.alloc(&counter, 1));
+    EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
+    SourceArgs a = make_source_args(opts, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, d_stats);
+    if (method == EMBER_SOURCE_QSS) {
+        EMBER_TRY(launch_source_qss(m->view, a, counter, st));
+    } else {
+        EMBER_TRY(launch_source_bdf(m->view, a, counter, st));
+    }
+    EMBER_TRY(stage_out(state_out, d_out, size_t(n) * nv, mem, st));
+    EMBER_TRY(stage_out(status, d_status, n, mem, st));
+    EMBER_TRY(stage_out(stats, d_stats, size_t(n) * EMBER_STATS_WIDTH, mem, st));
+    sc.release();
+    EMBER_TRY(finish_call(mem, st));
+    if (mem == EMBER_MEM_HOST) {
+        int bad = 0;
+        for (int j = 0; j < n; ++j) bad += status[j] != 0;
+        if (bad) {
+            set_error("%d of %d points failed (see status)", bad, n);
+            return EMBER_EFAIL;
+        }
+    }
+    return EMBER_OK;
+}
+
+// ------------------------------------------- QSS known-answer self-test --
+
+namespace ember {
+
+// The CHEMEQ2 cesium relaxation problem of the reference's legacy QSS test
+// (test/old/test_qssintegrator.cpp:11-83) as a q/d right-hand side.
+struct CesiumOde {
+    __device__ void eval(double, const double* y, double* q, double* d, bool) {
+        if (lane_id() == 0) {
+            const double o2m = y[0], csp = y[1], cs = y[2], cso2 = y[3], o2 = y[4], n2 = y[5];
+            const double ne = (csp - o2m > 0.0) ? csp - o2m : 0.0;
+            const double cr1 = 5.00e-08 * o2m * csp;
+            const double cr2 = 1.00e-12 * csp * ne;
+            const double cr3 = 3.24e-03 * cs;
+            const double cr4 = 4.00e-01 * o2m;
+            const double cr5 = 1.00e-31 * o2 * cs * (cs + cso2 + n2 + o2);
+            const double cr6 = 1.24e-30 * o2 * o2 * ne;
+            const double cr7 = 1.00e-31 * o2 * n2 * ne;
+            for (int i = 0; i < 7; ++i) q[i] = d[i] = 0.0;
+            q[0] = cr6 + cr7;
+            d[0] = cr1 + cr4;
+            q[1] = cr3;
+            d[1] = cr1 + cr2;
+            q[2] = cr1 + cr2;
+            d[2] = cr3 + cr5;
+            q[3] = cr5;
+            q[4] = cr1 + cr4;
+            d[4] = cr5 + cr6 + cr7;
+        }
+        __syncwarp();
+    }
+};
+
+struct EnforceAll {
+    __device__ bool operator()(int) const { return true; }
+};
+
+__global__ void k_qss_cesium(QssParams P, double* y7, double tf, int* stats, int* ret) {
+    __shared__ double buf[12 * 7];
+    QssSmem v;
+    v.carve(buf, 7);
+    for (int i = lane_id(); i < 7; i += 32) {
+        v.y[i] = y7[i];
+        v.ymin[i] = 1e-20;
+    }
+    __syncwarp();
+    CesiumOde ode;
+    QssStats st;
+    int r = qss_integrate_warp(ode, v, 7, P, EnforceAll(), tf, 0.0, st);
+    if (lane_id() == 0) {
+        for (int i = 0; i < 7; ++i) y7[i] = v.y[i];
+        y7[6] = y7[1] - y7[0];
+        stats[0] = st.steps;
+        stats[1] = st.gcount;
+        stats[2] = st.rcount;
+        stats[3] = 0;
+        *ret = r;
+    }
+}
+
+}  // namespace ember
+
+extern "C" int ember_selftest_qss_cesium(double epsmin, double epsmax, double dtmin, double dtmax, double abstol,
+                                         int itermax, int stability_check, double tf, int max_steps, double* y7,
+                                         int* stats) {
+    EMBER_CHECK_ARG(y7 != nullptr && stats != nullptr, "null argument");
+    EMBER_CHECK_ARG(max_steps > 0 && itermax >= 0 && epsmin > 0, "bad parameters");
+    EMBER_TRY(ensure_device());
+    QssParams P{epsmin, epsmax, dtmin, dtmax, abstol, itermax, stability_check, max_steps};
+    double* dy = nullptr;
+    int* di = nullptr;
+    EMBER_CUDA_TRY(cudaMalloc(&dy, sizeof(double) * 7));
+    cudaError_t e = cudaMalloc(&di, sizeof(int) * 5);
+    if (e == cudaSuccess) e = cudaMemcpy(dy, y7, sizeof(double) * 7, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_qss_cesium<<<1, 32>>>(P, dy, tf, di, di + 4);
+        e = cudaGetLastError();
+    }
+    int ret = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(y7, dy, sizeof(double) * 7, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(stats, di, sizeof(int) * 4, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&ret, di + 4, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(dy);
+    cudaFree(di);
+    if (e != cudaSuccess) {
+        set_error("ember_selftest_qss_cesium: %s", cudaGetErrorString(e));
+        return EMBER_ECUDA;
+    }
+    return ret;
+}

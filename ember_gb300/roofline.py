@@ -1,0 +1,73 @@
+"""Algorithmic work model of the hot-path kernels (roofline numerators).
+
+Counts each +, -, *, /, exp, log and pow as one flop, over the formulas the
+reference evaluates, so the figures do not depend on how the GPU code is
+written. Per-point call counts come from the integrator statistics (steps and
+right-hand-side calls), which are identical on the GPU and in the CPU oracle.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .mechanism import Mechanism, RXN_ELEMENTARY, RXN_THREE_BODY, RXN_TROE
+
+
+def _occurrences(mech: Mechanism):
+    nr = (mech.reactants >= 0).sum(axis=1)
+    npr = (mech.products >= 0).sum(axis=1)
+    return nr, npr
+
+
+def rhs_flops(mech: Mechanism, kinetics_model: int):
+    """(flops of the temperature-dependent part, flops of the
+    composition-dependent part) of one source-term right-hand side."""
+    S = mech.n_species
+    nr, npr = _occurrences(mech)
+    ty = mech.rxn_type
+    n_eff = np.diff(mech.efficiency_offsets)
+    falloff = (ty == 2) | (ty == 3)
+    # thermo per species: cp/R 8, h/RT 10, s/R 9, g 1
+    f_T = 28 * S + 3  # + log T, 1/T, log(RT/p0)
+    arr = ~falloff
+    if kinetics_model == 0:
+        f_T += int(np.sum(np.where(arr, 5, 0)))                             # A exp(b lnT - Ea/(RT))
+        f_T += int(np.sum(np.where(mech.reversible != 0, nr + npr + 4, 0)))  # dG, exp, cap
+    else:
+        f_T += int(np.sum(np.where(arr, 2, 0)))                             # table lookups
+        f_T += int(np.sum(np.where(mech.reversible != 0, 2, 0)))
+        f_T += 4                                                            # table index
+    # composition: clip/normalise 4/species, concentration 1, mean weight 1
+    f_c = 6 * S + 4
+    f_rop = np.zeros(mech.n_reactions)
+    f_rop += np.where(ty != RXN_ELEMENTARY, 1 + 2 * n_eff, 0)               # [M]
+    f_rop += np.where(falloff, 10 + 5, 0)                                   # k0, kinf, Pr, blend
+    f_rop += np.where(ty == RXN_TROE, 24, 0)                                # Fcent, F
+    f_rop += 1 + np.where(ty == RXN_THREE_BODY, 1, 0)                        # multiplier, [M]
+    f_rop += nr + np.where(mech.reversible != 0, npr + 1, 0)                # mass action
+    f_acc = 2 * int(np.sum(nr + npr))                                       # creation + destruction
+    f_src = 8 * S + 4                                                       # q, d, qdot, cp
+    return float(f_T), float(f_c + f_rop.sum() + f_acc + f_src)
+
+
+def qss_point_flops(mech: Mechanism, kinetics_model: int, steps, rhs_calls):
+    """Flops of QSS integrations given per-point step and RHS-call counts:
+    every step re-evaluates the temperature-dependent part once (predictor
+    call); every call evaluates the composition part; the integrator does
+    about 40 flops per component per call (Pade predictor, corrector, error
+    test)."""
+    f_T, f_rhs = rhs_flops(mech, kinetics_model)
+    n = mech.n_vars
+    steps = np.asarray(steps, dtype=float)
+    calls = np.asarray(rhs_calls, dtype=float)
+    return steps * f_T + calls * (f_rhs + 40.0 * n)
+
+
+def tridiag_flops_per_point() -> float:
+    """Diffusion system per point for one BDF1x8 step: matrix rows ~12,
+    factorisation ~5, 8 sub-steps x (2 right-hand side + 3 forward + 2 back)."""
+    return 12.0 + 5.0 + 8 * 7.0
+
+
+def tridiag_bytes_per_point() -> float:
+    """B, D, split constant and y read, y written (8 bytes each)."""
+    return 40.0

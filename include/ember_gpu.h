@@ -172,6 +172,144 @@ int ember_diffusion_integrate(int n_flames, const ember_diffusion_grid* grids, i
                               const ember_diffusion_options* opts, int* status,
                               int mem, void* stream);
 
+/* ======================================================================
+ * Mechanism tables
+ *
+ * A gas-phase mechanism compiled once into structure-of-arrays device
+ * tables: NASA7 thermo per species and, per reaction, modified Arrhenius
+ * parameters, third-body efficiencies, Lindemann/Troe falloff data and the
+ * species occurrences on each side. Units are Cantera's internal SI-kmol
+ * units (kmol, m^3, s, K; activation energies as Ea/R in K).
+ * Replaces the Cantera objects built by CanteraGas::initialize
+ * (src/chemistry0d.cpp:455-485) for the kinetics/thermo the source term uses.
+ * ==================================================================== */
+#define EMBER_MAX_STOICH 4        /* species occurrences per reaction side */
+
+#define EMBER_RXN_ELEMENTARY 0
+#define EMBER_RXN_THREE_BODY 1    /* rate multiplied by [M]                  */
+#define EMBER_RXN_LINDEMANN  2    /* falloff, F = 1                          */
+#define EMBER_RXN_TROE       3    /* falloff, Troe F                         */
+
+typedef struct {
+    int n_species;
+    int n_reactions;
+    const double* mol_weight;        /* [S] kg/kmol                                        */
+    const double* nasa_tmid;         /* [S] K; the low-T coefficients apply for T <= tmid  */
+    const double* nasa_coeffs;       /* [S][14]: a0..a6 low range, then a0..a6 high range  */
+    const int* rxn_type;             /* [R] EMBER_RXN_*                                     */
+    const int* reversible;           /* [R] 0 or 1                                          */
+    const int* reactants;            /* [R][EMBER_MAX_STOICH] species per occurrence, -1 = none */
+    const int* products;             /* [R][EMBER_MAX_STOICH]                               */
+    const double* arrhenius;         /* [R][3]: A, b, Ea/R; high-pressure limit for falloff */
+    const double* arrhenius_low;     /* [R][3]: low-pressure limit (falloff rows only)      */
+    const double* troe;              /* [R][4]: a, T3, T1, T2 (T2 == 0: term absent)        */
+    const double* default_efficiency;/* [R] third-body default efficiency                   */
+    const int64_t* efficiency_offsets;/* [R+1] CSR into the two arrays below                */
+    const int* efficiency_species;
+    const double* efficiency_values;
+} ember_mech_desc;
+
+typedef struct ember_mech_s* ember_mech;
+
+/* Validate and upload a mechanism; builds the per-species reaction lists and
+ * the interpolation tables of the 'interp' kinetics model on the device. */
+int ember_mech_create(const ember_mech_desc* desc, ember_mech* out);
+int ember_mech_destroy(ember_mech mech);
+
+/* Per-reaction rate multipliers (n_reactions values; NULL resets to 1).
+ * Replaces: Kinetics::setMultiplier as used by CanteraGas::setRateMultiplier
+ * (src/chemistry0d.cpp:634-642), per reaction. */
+int ember_mech_set_multipliers(ember_mech mech, const double* multipliers, int mem, void* stream);
+
+/* Kinetics models (Chemistry.kineticsModel, python/ember/input.py:371). */
+#define EMBER_KINETICS_STANDARD 0  /* rate constants and equilibrium constants from the formulas */
+#define EMBER_KINETICS_INTERP   1  /* InterpKinetics + MultiArrheniusInterp tables
+                                      (src/chemistry0d.cpp:271-436)          */
+
+/* Composition handling of the state setter. */
+#define EMBER_STATE_NORMALIZED 0   /* setState_TPY: negative Y clipped, sum normalised */
+#define EMBER_STATE_NO_NORM    1   /* setMassFractions_NoNorm + setState_TP            */
+
+/* Thermo and rates for a batch of states (n_points; Y point-major [n][S]).
+ * Outputs (any may be NULL): creation/destruction/net production rates
+ * [n][S] kmol/m^3/s, partial molar enthalpies hk [n][S] J/kmol, cp_mass [n]
+ * J/kg/K, density [n] kg/m^3. Replaces: CanteraGas::setStateMass /
+ * getCreationRates / getDestructionRates / getReactionRates / getEnthalpies /
+ * getSpecificHeatCapacity / getDensity (src/chemistry0d.cpp:487-672). */
+int ember_gas_eval(ember_mech mech, int n_points, double pressure, int kinetics_model, int state_mode,
+                   const double* T, const double* Y, double* creation, double* destruction, double* net,
+                   double* hk, double* cp_mass, double* density, int mem, void* stream);
+
+/* ======================================================================
+ * Production (chemistry source term) stage
+ *
+ * One call = FlameSolver::integrateProductionTerms() for a batch of grid
+ * points (src/flameSolver.cpp:754-836): every point is an independent
+ * constant-pressure reactor with state [U, T, Y_0..Y_{S-1}] (nVars = S+2,
+ * the column of FlameSolver::state), integrated over its own dt with the
+ * split constant of SourceSystem::splitConst, by
+ *   EMBER_SOURCE_QSS: SourceSystemQSS + QssIntegrator
+ *                     (src/sourceSystem.cpp:403-531, src/qssintegrator.cpp);
+ *   EMBER_SOURCE_BDF: SourceSystemCVODE's right-hand side integrated by a
+ *                     variable-order BDF with Newton iteration over a dense
+ *                     LU of an analytic Jacobian, following CVODE's published
+ *                     method (replaces src/sundialsUtils.cpp:33-172).
+ * Per-point arrays are point-major: element (j, i) at j*nVars + i.
+ * ==================================================================== */
+#define EMBER_SOURCE_QSS 0
+#define EMBER_SOURCE_BDF 1
+
+/* Per-point status (the int returned by SourceSystem::integrateToTime). */
+#define EMBER_SRC_OK            0
+#define EMBER_SRC_DTMIN        -1    /* QSS: step below dtmin (qssintegrator.cpp:198-215)      */
+#define EMBER_SRC_TOO_MUCH_WORK -11  /* BDF: max_num_steps reached (CVODE CV_TOO_MUCH_WORK)     */
+#define EMBER_SRC_ERR_FAILURE   -13  /* BDF: repeated error-test failures (CV_ERR_FAILURE)      */
+#define EMBER_SRC_CONV_FAILURE  -14  /* BDF: repeated Newton failures (CV_CONV_FAILURE)         */
+#define EMBER_SRC_STEP_LIMIT    -20  /* QSS: the device step cap max_steps was reached          */
+#define EMBER_SRC_NONFINITE     -21  /* a NaN/inf appeared in the state                         */
+
+#define EMBER_STATS_WIDTH 4          /* per point: steps, rhs calls, repeats/failures, Jacobians */
+
+typedef struct {
+    double pressure;              /* Pa (General.pressure)                              */
+    int kinetics_model;           /* EMBER_KINETICS_*                                   */
+    int max_steps;                /* device cap on internal steps per point (> 0)      */
+    /* QssTolerances (python/ember/input.py:752-775) */
+    double qss_epsmin, qss_epsmax, qss_dtmin, qss_dtmax, qss_abstol, qss_minval;
+    int qss_iteration_count, qss_stability_check;
+    /* CvodeTolerances (python/ember/input.py:733-745) */
+    double bdf_reltol, bdf_abstol_momentum, bdf_abstol_energy, bdf_abstol_species, bdf_min_step;
+    int bdf_max_num_steps;
+    int bdf_reserved;
+    /* ignition source of SourceSystem::getQdotIgniter (src/sourceSystem.cpp:33-45);
+     * ignition_energy == 0 disables it */
+    double ignition_tstart, ignition_duration, ignition_energy, ignition_center, ignition_stddev;
+} ember_source_options;
+
+/* Fill `opts` with the reference's defaults (pressure 1 atm, interp kinetics). */
+int ember_source_options_default(ember_source_options* opts);
+
+/* state_in/state_out: [n_points][nVars]; split_const: same layout or NULL (0);
+ * dt: [n_points] integration interval (tf relative to t_start); x: grid
+ * positions for the igniter or NULL; status: [n_points] EMBER_SRC_*; stats:
+ * [n_points][EMBER_STATS_WIDTH] or NULL. Returns EMBER_EFAIL (after writing
+ * every output) when at least one point failed. */
+int ember_source_integrate(ember_mech mech, int method, int n_points, const double* state_in,
+                           const double* split_const, const double* dt, double t_start, const double* x,
+                           const ember_source_options* opts, double* state_out, int* status, int* stats,
+                           int mem, void* stream);
+
+/* Known-answer self-test of the device QSS integrator: integrates the
+ * CHEMEQ2 cesium relaxation problem of the reference's QSS test
+ * (test/old/test_qssintegrator.cpp:11-83) from y7 (7 values, in/out) over
+ * [0, tf] with the given QssIntegrator settings, and sets y7[6] from charge
+ * balance as that test does. stats: steps, right-hand-side calls, repeats, 0.
+ * Returns the integrator's status (0, -1 dtmin, -20 step cap) or an EMBER_E*
+ * code. */
+int ember_selftest_qss_cesium(double epsmin, double epsmax, double dtmin, double dtmax, double abstol,
+                              int itermax, int stability_check, double tf, int max_steps, double* y7,
+                              int* stats);
+
 #ifdef __cplusplus
 }
 #endif

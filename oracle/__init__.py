@@ -36,9 +36,8 @@ def _declare(l):
     l.oracle_diffusion_step_size.restype = d
     l.oracle_diffusion_system.argtypes = [i, vp, i, i, i, vp, vp, vp, d, d, d, d, d, d, d, vp]
     l.oracle_diffusion_system.restype = None
-    if hasattr(l, "oracle_chem_setup"):
-        from . import chem as _chem
-        _chem.declare(l)
+    from . import chem as _chem
+    _chem.declare(l)
 
 
 def _f(a):

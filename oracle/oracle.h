@@ -39,6 +39,92 @@ void oracle_diffusion_system(int N, const double* x, int alpha, int left_bc, int
                              const double* D, const double* split_const, double wall_const, double y_inf,
                              double h, double mult, double gdt, double t0, double t1, double* y);
 
+/* ---- chemistry ---------------------------------------------------------- */
+
+#define ORACLE_MAX_STOICH 4
+#define ORACLE_RXN_ELEMENTARY 0
+#define ORACLE_RXN_THREE_BODY 1
+#define ORACLE_RXN_LINDEMANN 2
+#define ORACLE_RXN_TROE 3
+#define ORACLE_STATE_NORMALIZED 0
+#define ORACLE_STATE_NO_NORM 1
+
+/* Same field layout as the product's ember_mech_desc. */
+typedef struct {
+    int n_species, n_reactions;
+    const double *mol_weight, *nasa_tmid, *nasa_coeffs;
+    const int *rxn_type, *reversible, *reactants, *products;
+    const double *arrhenius, *arrhenius_low, *troe, *default_efficiency;
+    const int64_t* efficiency_offsets;
+    const int* efficiency_species;
+    const double* efficiency_values;
+} oracle_mech_desc;
+
+typedef struct {
+    int S, R;
+    double *W, *rW, *tmid, *nasa, *hc, *sc;
+    int *type, *rev, *reac, *prod;
+    double *arr, *arr_low, *troe, *def_eff;
+    int64_t* eff_off;
+    int* eff_sp;
+    double *eff_val, *mult, *dn;
+    int nT;
+    double Tmin, Tmax;
+    double *kf_c, *kf_s, *kc_c, *kc_s;
+} oracle_mech;
+
+typedef struct {
+    double *cp_R, *h_RT, *g_RT, *c, *ym, *tmp, *kf, *rkc, *ropf, *ropr, *wq, *wd, *wn, *hk, *v;
+    double kT;
+    int kModel;
+} oracle_ws;
+
+/* Same field layout as the product's ember_source_options. */
+typedef struct {
+    double pressure;
+    int kinetics_model;
+    int max_steps;
+    double qss_epsmin, qss_epsmax, qss_dtmin, qss_dtmax, qss_abstol, qss_minval;
+    int qss_iteration_count, qss_stability_check;
+    double bdf_reltol, bdf_abstol_momentum, bdf_abstol_energy, bdf_abstol_species, bdf_min_step;
+    int bdf_max_num_steps;
+    int bdf_reserved;
+    double ignition_tstart, ignition_duration, ignition_energy, ignition_center, ignition_stddev;
+} oracle_source_options;
+
+/* QSS integrator on any q/d right-hand side (QssOde::odefun). */
+typedef void (*oracle_qss_fn)(void* ctx, double t, const double* y, double* q, double* d, int corrector);
+typedef struct {
+    double epsmin, epsmax, dtmin, dtmax, abstol;
+    int itermax, stability_check;
+} oracle_qss_params;
+int oracle_qss_integrate(int n, oracle_qss_fn f, void* ctx, const oracle_qss_params* o, double* y,
+                         const double* ymin, const int* enforce, double tf, double tstart, int max_steps,
+                         double* work, int* stats);
+/* The CHEMEQ2 cesium problem of test/old/test_qssintegrator.cpp. */
+int oracle_qss_cesium(const oracle_qss_params* o, double* y7, double tf, int max_steps, int* stats);
+
+double oracle_exp(double x);
+double oracle_log(double x);
+oracle_mech* oracle_mech_create(const oracle_mech_desc* d);
+void oracle_mech_destroy(oracle_mech* m);
+void oracle_mech_set_multipliers(oracle_mech* m, const double* mult);
+oracle_ws* oracle_ws_create(const oracle_mech* m);
+void oracle_ws_free(oracle_ws* w);
+void oracle_rate_constants(const oracle_mech* m, oracle_ws* w, double T, int use_tables);
+void oracle_rates(const oracle_mech* m, oracle_ws* w, double p, int model, int mode, double T, const double* Y,
+                  double* rho_out, double* cp_out);
+void oracle_gas_eval(const oracle_mech* m, double p, int model, int mode, int n, const double* T, const double* Y,
+                     double* creation, double* destruction, double* net, double* hk, double* cp_mass,
+                     double* density);
+int oracle_qss_point(const oracle_mech* m, oracle_ws* w, const oracle_source_options* o, double* y,
+                     const double* split, double tf, double t_start, double x, int* stats);
+int oracle_bdf_point(const oracle_mech* m, oracle_ws* w, const oracle_source_options* o, double* y,
+                     const double* split, double tf, double t_start, double x, int* stats);
+void oracle_source_batch(const oracle_mech* m, int method, int n, const double* state_in, const double* split,
+                         const double* dt, double t_start, const double* x, const oracle_source_options* o,
+                         double* state_out, int* status, int* stats, int n_threads);
+
 #ifdef __cplusplus
 }
 #endif

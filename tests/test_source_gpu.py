@@ -1,0 +1,160 @@
+"""GPU parity of the chemistry source term through the C ABI: thermo/rates
+(ember_gas_eval) and the QSS source-term integrator (ember_source_integrate)
+against the CPU oracle, bit for bit, plus the device QSS integrator on the
+reference's CHEMEQ2 cesium known-answer test."""
+import ctypes as C
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import chem
+from ember_gb300 import _lib as L
+from ember_gb300.mechanism import synthetic_mechanism, reactor_states
+from ember_gb300.source import (GpuMechanism, SourceOptions, integrate_production_terms, QSS,
+                                KINETICS_STANDARD, KINETICS_INTERP, STATE_NORMALIZED, STATE_NO_NORM)
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def small_mech():
+    return synthetic_mechanism(n_species=40, n_reactions=200, seed=7)
+
+
+@pytest.fixture(scope="module")
+def big_mech():
+    return synthetic_mechanism()  # 150 species, 1000 reactions
+
+
+@pytest.fixture(scope="module")
+def pair_small(gpu_lib, small_mech):
+    return GpuMechanism(small_mech), chem.OracleMech(small_mech)
+
+
+@pytest.fixture(scope="module")
+def pair_big(gpu_lib, big_mech):
+    return GpuMechanism(big_mech), chem.OracleMech(big_mech)
+
+
+def _states(mech, n, seed):
+    st, dt = reactor_states(mech, n, seed=seed)
+    rng = np.random.default_rng(seed)
+    st[:, 2:] += 1e-6 * rng.uniform(0, 1, st[:, 2:].shape)
+    return st, dt
+
+
+@pytest.mark.parametrize("model", [KINETICS_STANDARD, KINETICS_INTERP])
+@pytest.mark.parametrize("mode", [STATE_NORMALIZED, STATE_NO_NORM])
+def test_gas_eval_bitwise(pair_small, small_mech, model, mode):
+    g, o = pair_small
+    st, _ = _states(small_mech, 48, seed=11)
+    T = st[:, 1].copy()
+    T[:3] = [250.0, 3500.0, 3900.0]  # below / at / above the table range
+    Y = st[:, 2:].copy()
+    Y[5, 3] = -1e-4  # a negative mass fraction
+    a = g.gas_eval(T, Y, model=model, mode=mode)
+    b = o.gas_eval(T, Y, model=model, mode=mode)
+    for key in ("creation", "destruction", "net", "hk", "cp_mass", "density"):
+        np.testing.assert_array_equal(a[key], b[key], err_msg=key)
+
+
+def test_gas_eval_big_mechanism_bitwise(pair_big, big_mech):
+    g, o = pair_big
+    st, _ = _states(big_mech, 64, seed=12)
+    for model in (KINETICS_STANDARD, KINETICS_INTERP):
+        a = g.gas_eval(st[:, 1], st[:, 2:], model=model)
+        b = o.gas_eval(st[:, 1], st[:, 2:], model=model)
+        for key in ("creation", "destruction", "net", "hk", "cp_mass", "density"):
+            np.testing.assert_array_equal(a[key], b[key], err_msg=key)
+
+
+@pytest.mark.parametrize("model", [KINETICS_STANDARD, KINETICS_INTERP])
+def test_qss_bitwise_vs_oracle(pair_small, small_mech, model):
+    g, o = pair_small
+    st, dt = _states(small_mech, 96, seed=13)
+    opts = SourceOptions.defaults(kinetics_model=model)
+    out, status, stats = integrate_production_terms(g, QSS, st, dt, opts)
+    ro, rs, rst = o.integrate(chem.QSS, st, dt, opts)
+    np.testing.assert_array_equal(status, rs)
+    np.testing.assert_array_equal(stats, rst)
+    np.testing.assert_array_equal(out, ro)
+
+
+def test_qss_big_mechanism_bitwise(pair_big, big_mech):
+    g, o = pair_big
+    st, dt = _states(big_mech, 48, seed=14)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_INTERP)
+    out, status, stats = integrate_production_terms(g, QSS, st, dt, opts)
+    ro, rs, rst = o.integrate(chem.QSS, st, dt, opts)
+    assert (status == 0).all()
+    np.testing.assert_array_equal(stats, rst)
+    np.testing.assert_array_equal(out, ro)
+
+
+def test_qss_split_constants_multipliers_igniter(pair_small, small_mech):
+    g, o = pair_small
+    st, dt = _states(small_mech, 32, seed=15)
+    rng = np.random.default_rng(15)
+    split = rng.normal(scale=1e-2, size=st.shape)
+    split[:, 0] = rng.normal(scale=10.0, size=len(st))
+    split[:, 1] = rng.normal(scale=1e4, size=len(st))
+    x = rng.uniform(-1e-3, 1e-3, len(st))
+    mult = np.exp(rng.normal(scale=0.3, size=small_mech.n_reactions))
+    g.set_multipliers(mult)
+    o.set_multipliers(mult)
+    try:
+        opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD, ignition_energy=5e6, ignition_tstart=0.0,
+                                      ignition_duration=1e-3, ignition_center=0.0, ignition_stddev=3e-4)
+        out, status, stats = integrate_production_terms(g, QSS, st, dt, opts, split_const=split, t_start=1e-4, x=x)
+        ro, rs, rst = o.integrate(chem.QSS, st, dt, opts, split_const=split, t_start=1e-4, x=x)
+        np.testing.assert_array_equal(status, rs)
+        np.testing.assert_array_equal(out, ro)
+    finally:
+        g.set_multipliers(None)
+        o.set_multipliers(None)
+
+
+def test_qss_device_memory_path(pair_small, small_mech):
+    torch = pytest.importorskip("torch")
+    g, _ = pair_small
+    st, dt = _states(small_mech, 40, seed=16)
+    opts = SourceOptions.defaults()
+    host, hs, _ = integrate_production_terms(g, QSS, st, dt, opts)
+    dev, ds, _ = integrate_production_terms(g, QSS, torch.as_tensor(st, device="cuda"),
+                                            torch.as_tensor(dt, device="cuda"), opts)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(dev.cpu().numpy(), host)
+    np.testing.assert_array_equal(ds.cpu().numpy(), hs)
+
+
+def test_qss_failures_reported(pair_small, small_mech):
+    g, o = pair_small
+    st, dt = _states(small_mech, 8, seed=17)
+    opts = SourceOptions.defaults(qss_dtmin=1.0)
+    out, status, _ = integrate_production_terms(g, QSS, st, dt, opts)
+    assert (np.asarray(status) == -1).all()
+    opts = SourceOptions.defaults(max_steps=3)
+    out, status, stats = integrate_production_terms(g, QSS, st, dt, opts)
+    ro, rs, _ = o.integrate(chem.QSS, st, dt, opts)
+    np.testing.assert_array_equal(status, rs)
+    assert (np.asarray(status) == -20).any()
+    np.testing.assert_array_equal(out, ro)
+
+
+def test_qss_cesium_known_answer_on_gpu(gpu_lib, golden_dir):
+    with open(os.path.join(golden_dir, "qss_cesium.json")) as f:
+        ces = json.load(f)
+    yi, yf = np.array(ces["YI"]), np.array(ces["YF"])
+    for eps in ces["eps_cases"]:
+        y = yi.copy()
+        stats = np.zeros(4, dtype=np.int32)
+        r = gpu_lib.ember_selftest_qss_cesium(eps, 20.0, 1e-15, 1e300, 1e-8, ces["itermax"], 1, ces["t_final"],
+                                              10_000_000, y.ctypes.data, stats.ctypes.data)
+        assert r == 0
+        yo, ro, so = chem.qss_cesium(yi, ces["t_final"], eps, itermax=ces["itermax"])
+        np.testing.assert_array_equal(y, yo)
+        np.testing.assert_array_equal(stats, so)
+        rel = np.abs(y - yf) / np.minimum(y, yf)
+        assert np.sqrt(np.sum(rel ** 2) / 6) < 0.1 * eps
