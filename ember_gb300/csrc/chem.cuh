@@ -1,17 +1,26 @@
-// Device thermo / kinetics of the source term, evaluated by one warp per
-// grid point (lanes split species and reactions). Restates what the
-// reference obtains from Cantera in SourceSystemQSS::odefun and
-// SourceSystemCVODE::f (src/sourceSystem.cpp:128-164, 445-499) and the
-// 'interp' model of InterpKinetics / MultiArrheniusInterp
-// (src/chemistry0d.cpp:271-436):
+// Device thermo / kinetics of the source term, evaluated by one CTA of
+// kChemThreads threads per grid point. Restates what the reference obtains
+// from Cantera in SourceSystemQSS::odefun and SourceSystemCVODE::f
+// (src/sourceSystem.cpp:128-164, 445-499) and the 'interp' model of
+// InterpKinetics / MultiArrheniusInterp (src/chemistry0d.cpp:271-436):
 //   NASA7 cp/R, h/RT, s/R; modified Arrhenius rates; third-body
 //   concentrations from efficiencies; Lindemann / Troe falloff; reverse rates
 //   through 1/Kc = exp(dG0/RT) (RT/p0)^dn capped at 1e300; creation,
 //   destruction and net production rates.
-// Every sum over species is a warp reduction in one fixed order (element k
-// in lane k mod 32, lanes combined by an xor butterfly). The translation unit
-// is compiled without automatic FMA contraction; the multiply-adds that are
-// fused are written as fma(), in the same places as in the CPU oracle.
+//
+// Work is split into uniform passes so that no thread runs a long branch the
+// others skip: temperature-only terms (thermo, rate constants, 1/Kc, the
+// Arrhenius limits and log10 Fcent of falloff reactions) once per
+// temperature; then per composition: [M] over the third-body list, falloff
+// blending over the falloff list, rates of progress over all reactions, and
+// a per-species gather of production rates in reaction order.
+//
+// Every sum over species is a block reduction in one fixed order: element k
+// goes to the partial sum of thread k mod 128 (sequential in k); the 128
+// partials are folded into 32 as ((p[l] + p[l+32]) + p[l+64]) + p[l+96] and
+// combined by an xor butterfly. The translation unit is compiled without
+// automatic FMA contraction; the multiply-adds that are fused are written as
+// fma(), in the same places as in the CPU oracle.
 #pragma once
 
 #include <cstdint>
@@ -25,6 +34,7 @@ constexpr double kOneAtm = 101325.0;
 constexpr double kBigNumber = 1e300;
 constexpr double kSmallNumber = 1e-300;
 constexpr int kMaxStoich = 4;
+constexpr int kChemThreads = 128;  // threads per grid point (4 warps)
 
 enum : int { RXN_ELEMENTARY = 0, RXN_THREE_BODY = 1, RXN_LINDEMANN = 2, RXN_TROE = 3 };
 enum : int { KIN_STANDARD = 0, KIN_INTERP = 1 };
@@ -33,51 +43,65 @@ enum : int { STATE_NORMALIZED = 0, STATE_NO_NORM = 1 };
 // Device tables of one mechanism (all arrays in global memory).
 struct MechView {
     int S, R, nT;
+    int n_tb, n_fo;       // reactions with [M] (three-body and falloff); falloff reactions
     double Tmin, Tmax;
     const double* W;      // [S]
     const double* rW;     // [S] 1/W
     const double* tmid;   // [S]
     const double* nasa;   // [S][14]
-    const double* hc;     // [S][10] h/RT polynomial coefficients a0, a1/2, a2/3, a3/4, a4/5 per range
-    const double* sc;     // [S][8]  s/R polynomial coefficients a1, a2/2, a3/3, a4/4 per range
-    const int* type;      // [R]
-    const int* rev;       // [R]
-    const int* reac;      // [R][4]
-    const int* prod;      // [R][4]
+    const double* hc;     // [S][10] h/RT polynomial a0, a1/2, a2/3, a3/4, a4/5 per range
+    const double* sc;     // [S][8]  s/R polynomial a1, a2/2, a3/3, a4/4 per range
+    const int4* stoich;   // [R] reactants (x: r0|r1<<16, y: r2|r3<<16), products (z, w); 0xffff = none
+    const int* rinfo;     // [R] type | rev<<2 | n_reac<<3 | n_prod<<6 | tb_slot<<9 (tb_slot = 0x3fffff: none)
     const double* arr;    // [R][3]
-    const double* arr_low;// [R][3]
-    const double* troe;   // [R][4]
-    const double* def_eff;// [R]
-    const int* eff_off;   // [R+1]
-    const int* eff_sp;
-    const double* eff_val;
     const double* mult;   // [R]
     const double* dn;     // [R]
-    const int* sp_off;    // [S+1] reactions in which species k occurs
-    const int* sp_ent;    // packed: reaction | n_product_occurrences << 24 | n_reactant_occurrences << 28
+    const int* tb_rxn;    // [n_tb] reaction of each third-body slot
+    const int* tb_off;    // [n_tb+1] efficiency CSR per slot
+    const int* tb_sp;
+    const double* tb_eff; // efficiency - default efficiency
+    const double* tb_def; // [n_tb] default efficiency
+    const int* fo_rxn;    // [n_fo] reaction of each falloff slot
+    const int* fo_tb;     // [n_fo] third-body slot of each falloff slot
+    const double* fo_arr; // [n_fo][3] low-pressure Arrhenius
+    const double* fo_troe;// [n_fo][4] a, T3, T1, T2 (type Lindemann: unused)
+    const int* sp_off;    // [S+1] reactions in which species k occurs, in reaction order
+    const int* sp_ent;    // reaction | n_product_occurrences << 24 | n_reactant_occurrences << 28
     const double2* kf_tab;// [nT][R] (value, slope)
     const double2* kc_tab;// [nT][R]
 };
 
-// Per-warp shared-memory work area of the kinetics.
+__device__ __forceinline__ int rinfo_type(int r) { return r & 3; }
+__device__ __forceinline__ int rinfo_rev(int r) { return (r >> 2) & 1; }
+__device__ __forceinline__ int rinfo_tbslot(int r) { return (r >> 9) & 0x3fffff; }
+
+// Per-point shared-memory work area of the kinetics.
 struct ChemSmem {
     double* c;     // [S] concentrations
     double* ym;    // [S]
     double* cpR;   // [S]
     double* hRT;   // [S]
     double* gRT;   // [S]
-    double* kf;    // [R] forward rate constants at the cached T (falloff rows: unused)
-    double* rkc;   // [R] 1/Kc at the cached T
-    double* ropf;  // [R]
-    double* ropr;  // [R]
     double* wq;    // [S] creation
     double* wd;    // [S] destruction
     double* wn;    // [S] net
     double* hk;    // [S] partial molar enthalpies [J/kmol]
+    double* kf;    // [R] forward rate constants (falloff rows: refreshed per composition)
+    double* rkc;   // [R] 1/Kc
+    double* ropf;  // [R]
+    double* ropr;  // [R]
+    double* concm; // [n_tb]
+    double* fo_kinf;  // [n_fo]
+    double* fo_k0;    // [n_fo]
+    double* fo_lfc;   // [n_fo] log10 Fcent (Troe)
+    double* red;      // [kChemThreads + 2] reduction scratch
 
-    static __host__ __device__ size_t doubles(int S, int R) { return size_t(9) * S + size_t(4) * R; }
+    static __host__ __device__ size_t doubles(int S, int R, int n_tb, int n_fo) {
+        return size_t(9) * S + size_t(4) * R + n_tb + size_t(3) * n_fo + kChemThreads + 2;
+    }
 
-    __device__ void carve(double* base, int S, int R) {
+    __device__ void carve(double* base, const MechView& m) {
+        const int S = m.S, R = m.R;
         c = base;
         ym = c + S;
         cpR = ym + S;
@@ -91,43 +115,68 @@ struct ChemSmem {
         rkc = kf + R;
         ropf = rkc + R;
         ropr = ropf + R;
+        concm = ropr + R;
+        fo_kinf = concm + m.n_tb;
+        fo_k0 = fo_kinf + m.n_fo;
+        fo_lfc = fo_k0 + m.n_fo;
+        red = fo_lfc + m.n_fo;
     }
 };
 
 __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 
-__device__ __forceinline__ double warp_sum_partial(double p) {
+__device__ __forceinline__ double dmaxr(double a, double b) { return (a < b) ? b : a; }  // std::max
+__device__ __forceinline__ double dminr(double a, double b) { return (b < a) ? b : a; }  // std::min
+
+// Block sum of the threads' partial sums in the fixed order described above.
+// Every thread of the CTA must call it; all receive the result.
+__device__ __forceinline__ double block_sum(double* red, double partial) {
+    const int t = threadIdx.x;
+    red[t] = partial;
+    __syncthreads();
+    if (t < 32) {
+        double q = red[t];
 #pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) p = p + __shfl_xor_sync(0xffffffffu, p, off);
-    return p;
+        for (int w = 1; w < kChemThreads / 32; ++w) q = q + red[t + 32 * w];
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) q = q + __shfl_xor_sync(0xffffffffu, q, off);
+        if (t == 0) red[kChemThreads] = q;
+    }
+    __syncthreads();
+    const double r = red[kChemThreads];
+    __syncthreads();
+    return r;
 }
 
-// Sum of x[0..n) in the fixed warp order (x in shared memory).
-__device__ __forceinline__ double warp_sum(const double* x, int n) {
-    double p = 0.0;
-    for (int k = lane_id(); k < n; k += 32) p = p + x[k];
-    return warp_sum_partial(p);
-}
-
-__device__ __forceinline__ double warp_max(double v) {
+__device__ __forceinline__ double block_max(double* red, double v) {
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
         double o = __shfl_xor_sync(0xffffffffu, v, off);
         v = (v < o) ? o : v;
     }
-    return v;
+    if (lane_id() == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = red[0];
+#pragma unroll
+    for (int w = 1; w < kChemThreads / 32; ++w) r = dmaxr(r, red[w]);
+    __syncthreads();
+    return r;
 }
-
-__device__ __forceinline__ double dmaxr(double a, double b) { return (a < b) ? b : a; }  // std::max
-__device__ __forceinline__ double dminr(double a, double b) { return (b < a) ? b : a; }  // std::min
 
 __device__ __forceinline__ double arrhenius(const double* p, double lnT, double rT) {
     return p[0] * em_exp(fma(p[1], lnT, -(p[2] * rT)));
 }
 
-// NASA7 thermo of every species at T into cpR, hRT, gRT (lanes over species).
-__device__ __forceinline__ void chem_thermo(const MechView& m, ChemSmem& w, double T, double lnT, double rT) {
-    for (int k = lane_id(); k < m.S; k += 32) {
+__device__ __forceinline__ int unpack_lo(int v) { return v & 0xffff; }
+__device__ __forceinline__ int unpack_hi(int v) { return (v >> 16) & 0xffff; }
+
+// Temperature-only part: NASA7 thermo, rate constants of non-falloff
+// reactions, 1/Kc (standard formulas or interpolation tables), and the
+// Arrhenius limits and log10 Fcent of falloff reactions. Ends with a barrier.
+__device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem& w, double T, int use_tables) {
+    const int t = threadIdx.x;
+    const double lnT = em_log(T), rT = 1.0 / T;
+    for (int k = t; k < m.S; k += kChemThreads) {
         const int r = (T <= m.tmid[k]) ? 0 : 1;
         const double* a = m.nasa + 14 * k + 7 * r;
         const double* h = m.hc + 10 * k + 5 * r;
@@ -140,14 +189,7 @@ __device__ __forceinline__ void chem_thermo(const MechView& m, ChemSmem& w, doub
         w.hRT[k] = hr;
         w.gRT[k] = hr - sr;
     }
-    __syncwarp();
-}
-
-// Temperature-only part: thermo, forward rate constants of non-falloff
-// reactions and 1/Kc, standard formulas or interpolation tables.
-__device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem& w, double T, int use_tables) {
-    const double lnT = em_log(T), rT = 1.0 / T;
-    chem_thermo(m, w, T, lnT, rT);
+    __syncthreads();
     const double lnRTp = em_log((kGasConstant * T) / kOneAtm);
     const bool in_table = use_tables && T >= m.Tmin && T <= m.Tmax;
     int n = 0;
@@ -158,8 +200,9 @@ __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem&
         if (n > m.nT - 1) n = m.nT - 1;
         dT = T - static_cast<double>(n) * (m.Tmax - m.Tmin) / (m.nT - 1) - m.Tmin;
     }
-    for (int i = lane_id(); i < m.R; i += 32) {
-        const int ty = m.type[i];
+    for (int i = t; i < m.R; i += kChemThreads) {
+        const int info = m.rinfo[i];
+        const int ty = rinfo_type(info);
         double kf = 0.0;
         if (ty == RXN_ELEMENTARY || ty == RXN_THREE_BODY) {
             if (in_table) {
@@ -170,118 +213,146 @@ __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem&
             }
         }
         double rkc = 0.0;
-        if (m.rev[i]) {
+        if (rinfo_rev(info)) {
             if (in_table) {
                 double2 e = m.kc_tab[size_t(n) * m.R + i];
                 rkc = e.x + e.y * dT;
             } else {
+                const int4 st = m.stoich[i];
+                const int pr[4] = {unpack_lo(st.z), unpack_hi(st.z), unpack_lo(st.w), unpack_hi(st.w)};
+                const int rc[4] = {unpack_lo(st.x), unpack_hi(st.x), unpack_lo(st.y), unpack_hi(st.y)};
                 double dg = 0.0;
-                const int* pr = m.prod + kMaxStoich * i;
-                const int* rc = m.reac + kMaxStoich * i;
 #pragma unroll
                 for (int o = 0; o < kMaxStoich; ++o)
-                    if (pr[o] >= 0) dg = dg + w.gRT[pr[o]];
+                    if (pr[o] != 0xffff) dg = dg + w.gRT[pr[o]];
 #pragma unroll
                 for (int o = 0; o < kMaxStoich; ++o)
-                    if (rc[o] >= 0) dg = dg - w.gRT[rc[o]];
+                    if (rc[o] != 0xffff) dg = dg - w.gRT[rc[o]];
                 rkc = dminr(em_exp(fma(m.dn[i], lnRTp, dg)), kBigNumber);
             }
         }
         w.kf[i] = kf;
         w.rkc[i] = rkc;
     }
-    __syncwarp();
+    for (int f = t; f < m.n_fo; f += kChemThreads) {
+        const int i = m.fo_rxn[f];
+        w.fo_kinf[f] = arrhenius(m.arr + 3 * i, lnT, rT);
+        w.fo_k0[f] = arrhenius(m.fo_arr + 3 * f, lnT, rT);
+        double lfc = 0.0;
+        if (rinfo_type(m.rinfo[i]) == RXN_TROE) {
+            const double* tp = m.fo_troe + 4 * f;
+            double fc = (1.0 - tp[0]) * em_exp(-T / tp[1]) + tp[0] * em_exp(-T / tp[2]);
+            if (tp[3] != 0.0) fc = fc + em_exp(-tp[3] * rT);
+            lfc = em_log10(dmaxr(fc, kSmallNumber));
+        }
+        w.fo_lfc[f] = lfc;
+    }
+    __syncthreads();
 }
 
 // Composition part of the state setter (setState_TPY or NoNorm), rates of
 // progress, production rates and thermo outputs at (T, Y). Rate constants
 // must be current for T (chem_rate_constants). Y is in shared memory.
-// Returns rho and cp_mass on every lane.
+// Returns rho and cp_mass on every thread. Ends with a barrier.
 __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, double p, int mode, double T,
                                            const double* Y, double& rho_out, double& cp_out, bool want_net) {
     const int S = m.S;
-    const int lane = lane_id();
+    const int t = threadIdx.x;
     if (mode == STATE_NORMALIZED) {
         double part = 0.0;
-        for (int k = lane; k < S; k += 32) part = part + dmaxr(Y[k], 0.0);
-        const double rnorm = 1.0 / warp_sum_partial(part);
-        for (int k = lane; k < S; k += 32) w.ym[k] = (dmaxr(Y[k], 0.0) * rnorm) * m.rW[k];
+        for (int k = t; k < S; k += kChemThreads) part = part + dmaxr(Y[k], 0.0);
+        const double rnorm = 1.0 / block_sum(w.red, part);
+        for (int k = t; k < S; k += kChemThreads) w.ym[k] = (dmaxr(Y[k], 0.0) * rnorm) * m.rW[k];
     } else {
-        for (int k = lane; k < S; k += 32) w.ym[k] = Y[k] * m.rW[k];
+        for (int k = t; k < S; k += kChemThreads) w.ym[k] = Y[k] * m.rW[k];
     }
     double part = 0.0;
-    for (int k = lane; k < S; k += 32) part = part + w.ym[k];
-    const double mmw = 1.0 / warp_sum_partial(part);
+    for (int k = t; k < S; k += kChemThreads) part = part + w.ym[k];
+    const double mmw = 1.0 / block_sum(w.red, part);
     const double rho = (p * mmw) / (kGasConstant * T);
-    for (int k = lane; k < S; k += 32) w.c[k] = w.ym[k] * rho;
-    __syncwarp();
+    for (int k = t; k < S; k += kChemThreads) w.c[k] = w.ym[k] * rho;
+    __syncthreads();
     const double ctot = rho / mmw;
-    const double lnT = em_log(T), rT = 1.0 / T;
-    for (int i = lane; i < m.R; i += 32) {
-        const int ty = m.type[i];
-        double kf = w.kf[i];
-        double concm = 0.0;
-        if (ty != RXN_ELEMENTARY) {
-            const double de = m.def_eff[i];
-            concm = de * ctot;
-            for (int e = m.eff_off[i]; e < m.eff_off[i + 1]; ++e)
-                concm = fma(m.eff_val[e] - de, w.c[m.eff_sp[e]], concm);
+    // [M] of third-body and falloff reactions
+    for (int s = t; s < m.n_tb; s += kChemThreads) {
+        const double de = m.tb_def[s];
+        double concm = de * ctot;
+        for (int e = m.tb_off[s]; e < m.tb_off[s + 1]; ++e) concm = fma(m.tb_eff[e], w.c[m.tb_sp[e]], concm);
+        w.concm[s] = concm;
+    }
+    __syncthreads();
+    // falloff blending: k = kinf * Pr/(1+Pr) * F
+    for (int f = t; f < m.n_fo; f += kChemThreads) {
+        const int i = m.fo_rxn[f];
+        const double kinf = w.fo_kinf[f];
+        const double pr = (w.concm[m.fo_tb[f]] * w.fo_k0[f]) / (kinf + kSmallNumber);
+        double F = 1.0;
+        if (rinfo_type(m.rinfo[i]) == RXN_TROE) {
+            const double lfc = w.fo_lfc[f];
+            const double lpr = em_log10(dmaxr(pr, kSmallNumber));
+            const double cc = -0.4 - 0.67 * lfc;
+            const double nn = 0.75 - 1.27 * lfc;
+            const double x = lpr + cc;
+            const double f1 = x / (nn - 0.14 * x);
+            F = em_exp10(lfc / (1.0 + f1 * f1));
         }
-        if (ty == RXN_LINDEMANN || ty == RXN_TROE) {
-            const double kinf = arrhenius(m.arr + 3 * i, lnT, rT);
-            const double k0 = arrhenius(m.arr_low + 3 * i, lnT, rT);
-            const double pr = (concm * k0) / (kinf + kSmallNumber);
-            double F = 1.0;
-            if (ty == RXN_TROE) {
-                const double* tp = m.troe + 4 * i;
-                double fc = (1.0 - tp[0]) * em_exp(-T / tp[1]) + tp[0] * em_exp(-T / tp[2]);
-                if (tp[3] != 0.0) fc = fc + em_exp(-tp[3] * rT);
-                const double lfc = em_log10(dmaxr(fc, kSmallNumber));
-                const double lpr = em_log10(dmaxr(pr, kSmallNumber));
-                const double cc = -0.4 - 0.67 * lfc;
-                const double nn = 0.75 - 1.27 * lfc;
-                const double x = lpr + cc;
-                const double f1 = x / (nn - 0.14 * x);
-                F = em_exp10(lfc / (1.0 + f1 * f1));
-            }
-            kf = (pr * (F / (1.0 + pr))) * kinf;
-        }
-        double rf = kf * m.mult[i];
-        if (ty == RXN_THREE_BODY) rf = rf * concm;
-        double ropf = rf, ropr = 0.0;
-        const int* rc = m.reac + kMaxStoich * i;
-        const int* pd = m.prod + kMaxStoich * i;
-#pragma unroll
-        for (int o = 0; o < kMaxStoich; ++o)
-            if (rc[o] >= 0) ropf = ropf * w.c[rc[o]];
-        if (m.rev[i]) {
+        w.kf[i] = (pr * (F / (1.0 + pr))) * kinf;
+    }
+    __syncthreads();
+    // rates of progress
+    for (int i = t; i < m.R; i += kChemThreads) {
+        const int info = m.rinfo[i];
+        const int4 st = m.stoich[i];
+        double rf = w.kf[i] * m.mult[i];
+        if (rinfo_type(info) == RXN_THREE_BODY) rf = rf * w.concm[rinfo_tbslot(info)];
+        double ropf = rf;
+        const int r0 = unpack_lo(st.x), r1 = unpack_hi(st.x), r2 = unpack_lo(st.y), r3 = unpack_hi(st.y);
+        ropf = ropf * w.c[r0];
+        if (r1 != 0xffff) ropf = ropf * w.c[r1];
+        if (r2 != 0xffff) ropf = ropf * w.c[r2];
+        if (r3 != 0xffff) ropf = ropf * w.c[r3];
+        double ropr = 0.0;
+        if (rinfo_rev(info)) {
+            const int p0 = unpack_lo(st.z), p1 = unpack_hi(st.z), p2 = unpack_lo(st.w), p3 = unpack_hi(st.w);
             ropr = rf * w.rkc[i];
-#pragma unroll
-            for (int o = 0; o < kMaxStoich; ++o)
-                if (pd[o] >= 0) ropr = ropr * w.c[pd[o]];
+            ropr = ropr * w.c[p0];
+            if (p1 != 0xffff) ropr = ropr * w.c[p1];
+            if (p2 != 0xffff) ropr = ropr * w.c[p2];
+            if (p3 != 0xffff) ropr = ropr * w.c[p3];
         }
         w.ropf[i] = ropf;
         w.ropr[i] = ropr;
     }
-    __syncwarp();
+    __syncthreads();
     const double RT = kGasConstant * T;
     double cpart = 0.0;
-    for (int k = lane; k < S; k += 32) {
+    for (int k = t; k < S; k += kChemThreads) {
         double q = 0.0, d = 0.0, nt = 0.0;
-        for (int e = m.sp_off[k]; e < m.sp_off[k + 1]; ++e) {
+        const int e1 = m.sp_off[k + 1];
+        for (int e = m.sp_off[k]; e < e1; ++e) {
             const int ent = m.sp_ent[e];
             const int i = ent & 0xffffff;
             const int np = (ent >> 24) & 0xf;
             const int nr = (ent >> 28) & 0xf;
             const double f = w.ropf[i], r = w.ropr[i];
-            for (int o = 0; o < np; ++o) q = q + f;
-            for (int o = 0; o < nr; ++o) q = q + r;
-            for (int o = 0; o < nr; ++o) d = d + f;
-            for (int o = 0; o < np; ++o) d = d + r;
-            if (want_net) {
-                const double net = f - r;
-                for (int o = 0; o < np; ++o) nt = nt + net;
-                for (int o = 0; o < nr; ++o) nt = nt - net;
+            if (np == 1 && nr == 0) {
+                q = q + f;
+                d = d + r;
+                if (want_net) nt = nt + (f - r);
+            } else if (np == 0 && nr == 1) {
+                q = q + r;
+                d = d + f;
+                if (want_net) nt = nt - (f - r);
+            } else {
+                for (int o = 0; o < np; ++o) q = q + f;
+                for (int o = 0; o < nr; ++o) q = q + r;
+                for (int o = 0; o < nr; ++o) d = d + f;
+                for (int o = 0; o < np; ++o) d = d + r;
+                if (want_net) {
+                    const double net = f - r;
+                    for (int o = 0; o < np; ++o) nt = nt + net;
+                    for (int o = 0; o < nr; ++o) nt = nt - net;
+                }
             }
         }
         w.wq[k] = q;
@@ -290,9 +361,8 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
         w.hk[k] = w.hRT[k] * RT;  // updateThermo: h_k [J/kmol]
         cpart = cpart + (w.ym[k] * mmw) * w.cpR[k];
     }
-    cp_out = (kGasConstant * warp_sum_partial(cpart)) / mmw;
+    cp_out = (kGasConstant * block_sum(w.red, cpart)) / mmw;
     rho_out = rho;
-    __syncwarp();
 }
 
 }  // namespace ember

@@ -1,9 +1,9 @@
 // Production (chemistry source term) stage on the GPU: mechanism upload,
 // thermo/rate evaluation and the QSS source-term integrator.
 //
-// One warp integrates one grid point; warps of a persistent grid take points
-// from an atomic work counter, so that points needing many sub-steps do not
-// hold up the others (the reference runs the same per-point integrations
+// One CTA of kChemThreads threads integrates one grid point; the CTAs of a
+// persistent grid take points from an atomic work counter, so that points
+// needing many sub-steps do not hold up the others (the reference runs the same per-point integrations
 // from a TBB parallel_for over points, src/flameSolver.cpp:754-836).
 //
 // Compiled with --fmad=false: only the fma() calls written in chem.cuh,
@@ -21,20 +21,20 @@ namespace ember {
 
 // ------------------------------------------------------- table building --
 
-// Rate constants and 1/Kc at the table nodes (one warp per node), from the
+// Rate constants and 1/Kc at the table nodes (one CTA per node), from the
 // same device functions as the standard model: InterpKinetics::updateROP /
 // MultiArrheniusInterp::rebuildInterpData (src/chemistry0d.cpp:278-326, 401-436).
-__global__ void k_build_tables(MechView m, double* work) {
-    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (warp >= m.nT) return;
+__global__ void __launch_bounds__(kChemThreads) k_build_tables(MechView m, double* work) {
+    const int node = blockIdx.x;
     ChemSmem w;
-    w.carve(work + size_t(warp) * ChemSmem::doubles(m.S, m.R), m.S, m.R);
-    const double T = m.Tmin + ((double)warp) / (m.nT - 1) * (m.Tmax - m.Tmin);
+    w.carve(work + size_t(node) * ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo), m);
+    const double T = m.Tmin + ((double)node) / (m.nT - 1) * (m.Tmax - m.Tmin);
     chem_rate_constants(m, w, T, 0);
-    double2* kf = const_cast<double2*>(m.kf_tab) + size_t(warp) * m.R;
-    double2* kc = const_cast<double2*>(m.kc_tab) + size_t(warp) * m.R;
-    for (int i = lane_id(); i < m.R; i += 32) {
-        kf[i].x = w.kf[i];
+    double2* kf = const_cast<double2*>(m.kf_tab) + size_t(node) * m.R;
+    double2* kc = const_cast<double2*>(m.kc_tab) + size_t(node) * m.R;
+    for (int i = threadIdx.x; i < m.R; i += kChemThreads) {
+        const int ty = rinfo_type(m.rinfo[i]);
+        kf[i].x = (ty == RXN_ELEMENTARY || ty == RXN_THREE_BODY) ? w.kf[i] : 0.0;
         kc[i].x = w.rkc[i];
     }
 }
@@ -58,36 +58,32 @@ __global__ void k_table_slopes(MechView m) {
 
 // ------------------------------------------------------------- gas eval --
 
-__global__ void k_gas_eval(MechView m, int n, double p, int model, int mode, const double* __restrict__ T,
-                           const double* __restrict__ Y, double* creation, double* destruction, double* net,
-                           double* hk, double* cp_mass, double* density) {
+__global__ void __launch_bounds__(kChemThreads) k_gas_eval(MechView m, int n, double p, int model, int mode,
+                                                          const double* __restrict__ T, const double* __restrict__ Y,
+                                                          double* creation, double* destruction, double* net,
+                                                          double* hk, double* cp_mass, double* density) {
     extern __shared__ double smem[];
-    const int wib = threadIdx.x >> 5;
-    const int wpb = blockDim.x >> 5;
-    const size_t per = ChemSmem::doubles(m.S, m.R) + m.S;
-    double* base = smem + wib * per;
     ChemSmem w;
-    w.carve(base, m.S, m.R);
-    double* y = base + ChemSmem::doubles(m.S, m.R);
-    for (int j = blockIdx.x * wpb + wib; j < n; j += gridDim.x * wpb) {
-        for (int k = lane_id(); k < m.S; k += 32) y[k] = Y[size_t(j) * m.S + k];
-        __syncwarp();
+    w.carve(smem, m);
+    double* y = smem + ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo);
+    for (int j = blockIdx.x; j < n; j += gridDim.x) {
+        for (int k = threadIdx.x; k < m.S; k += kChemThreads) y[k] = Y[size_t(j) * m.S + k];
         const double Tj = T[j];
-        chem_rate_constants(m, w, Tj, model == KIN_INTERP);
+        chem_rate_constants(m, w, Tj, model == KIN_INTERP);  // begins with a barrier-free pass, ends with one
         double rho, cp;
         chem_rates(m, w, p, mode, Tj, y, rho, cp, true);
-        for (int k = lane_id(); k < m.S; k += 32) {
+        for (int k = threadIdx.x; k < m.S; k += kChemThreads) {
             const size_t o = size_t(j) * m.S + k;
             if (creation) creation[o] = w.wq[k];
             if (destruction) destruction[o] = w.wd[k];
             if (net) net[o] = w.wn[k];
             if (hk) hk[o] = w.hk[k];
         }
-        if (lane_id() == 0) {
+        if (threadIdx.x == 0) {
             if (cp_mass) cp_mass[j] = cp;
             if (density) density[j] = rho;
         }
-        __syncwarp();
+        __syncthreads();
     }
 }
 
@@ -97,8 +93,10 @@ __global__ void k_gas_eval(MechView m, int n, double p, int model, int mode, con
 // [U, T, Y]; T and the thermo (h_k, rho, cp) are refreshed only on
 // predictor calls (src/sourceSystem.cpp:461-463, 501-515).
 struct SourceQssOde {
-    const MechView* m;
-    ChemSmem* w;
+    MechView m;
+    ChemSmem w;
+    double pressure;
+    int kinetics_model;
     const SourceArgs* a;
     const double* split;  // this point's split constants (global) or null
     double x;
@@ -108,27 +106,25 @@ struct SourceQssOde {
     double* hk_pred;      // [S] in shared memory
 
     __device__ void eval(double t, const double* y, double* q, double* d, bool corrector) {
-        const MechView& M = *m;
-        const int S = M.S;
-        const int lane = lane_id();
+        const int S = m.S;
+        const int tid = threadIdx.x;
         if (!corrector) T = y[1];
         if (!(cachedT == T)) {
-            chem_rate_constants(M, *w, T, a->kinetics_model == KIN_INTERP);
+            chem_rate_constants(m, w, T, kinetics_model == KIN_INTERP);
             cachedT = T;
         }
         double rho_c, cp_c;
-        chem_rates(M, *w, a->pressure, STATE_NORMALIZED, T, y + 2, rho_c, cp_c, false);
+        chem_rates(m, w, pressure, STATE_NORMALIZED, T, y + 2, rho_c, cp_c, false);
         if (!corrector) {
-            for (int k = lane; k < S; k += 32) hk_pred[k] = w->hk[k];
+            for (int k = tid; k < S; k += kChemThreads) hk_pred[k] = w.hk[k];
             rho = rho_c;
             cp = cp_c;
-            __syncwarp();
         }
         double part = 0.0;
-        for (int k = lane; k < S; k += 32) part = part + (w->wq[k] - w->wd[k]) * hk_pred[k];
-        const double qdot = -warp_sum_partial(part) + igniter(*a, t, x);
+        for (int k = tid; k < S; k += kChemThreads) part = part + (w.wq[k] - w.wd[k]) * hk_pred[k];
+        const double qdot = -block_sum(w.red, part) + igniter(*a, t, x);
         const double rc = rho * cp;
-        for (int i = lane; i < S + 2; i += 32) {
+        for (int i = tid; i < S + 2; i += kChemThreads) {
             const double sc = split ? split[i] : 0.0;
             if (i == 0) {
                 q[0] = sc;
@@ -138,11 +134,11 @@ struct SourceQssOde {
                 d[1] = 0.0 / rc;
             } else {
                 const int k = i - 2;
-                q[i] = (w->wq[k] * M.W[k]) / rho + sc;
-                d[i] = (w->wd[k] * M.W[k]) / rho;
+                q[i] = (w.wq[k] * m.W[k]) / rho + sc;
+                d[i] = (w.wd[k] * m.W[k]) / rho;
             }
         }
-        __syncwarp();
+        __syncthreads();
     }
 };
 
@@ -150,17 +146,21 @@ struct EnforceNotMomentum {
     __device__ bool operator()(int i) const { return i != 0; }
 };
 
-__global__ void __launch_bounds__(128) k_source_qss(MechView m, SourceArgs a, int* counter) {
+__global__ void __launch_bounds__(kChemThreads) k_source_qss(MechView m, SourceArgs a, int* counter) {
     extern __shared__ double smem[];
+    __shared__ int next_point;
     const int n = m.S + 2;
-    const int wib = threadIdx.x >> 5;
-    const size_t per = qss_smem_doubles(m.S, m.R);
-    double* base = smem + wib * per;
-    ChemSmem w;
-    w.carve(base, m.S, m.R);
+    const size_t cd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo);
+    SourceQssOde ode;
+    ode.m = m;
+    ode.w.carve(smem, m);
     QssSmem v;
-    v.carve(base + ChemSmem::doubles(m.S, m.R), n);
-    double* hk_pred = base + ChemSmem::doubles(m.S, m.R) + QssSmem::doubles(n);
+    v.carve(smem + cd, n);
+    ode.hk_pred = smem + cd + QssSmem::doubles(n);
+    ode.pressure = a.pressure;
+    ode.kinetics_model = a.kinetics_model;
+    ode.a = &a;
+    ode.cachedT = __longlong_as_double(0x7ff8000000000000LL);  // NaN: nothing cached
     QssParams P;
     P.epsmin = a.qss_epsmin;
     P.epsmax = a.qss_epsmax;
@@ -170,41 +170,35 @@ __global__ void __launch_bounds__(128) k_source_qss(MechView m, SourceArgs a, in
     P.itermax = a.qss_itermax;
     P.stability_check = a.qss_stability_check;
     P.max_steps = a.max_steps;
-    SourceQssOde ode;
-    ode.m = &m;
-    ode.w = &w;
-    ode.a = &a;
-    ode.hk_pred = hk_pred;
-    ode.cachedT = __longlong_as_double(0x7ff8000000000000LL);  // NaN: nothing cached
-    const int lane = lane_id();
+    const int tid = threadIdx.x;
     for (;;) {
-        int j = 0;
-        if (lane == 0) j = atomicAdd(counter, 1);
-        j = __shfl_sync(0xffffffffu, j, 0);
+        if (tid == 0) next_point = atomicAdd(counter, 1);
+        __syncthreads();
+        const int j = next_point;
+        __syncthreads();
         if (j >= a.n) break;
         const double* yin = a.state_in + size_t(j) * n;
-        for (int i = lane; i < n; i += 32) {
+        for (int i = tid; i < n; i += kChemThreads) {
             v.y[i] = yin[i];
             v.ymin[i] = (i == 0) ? -1e4 : a.qss_minval;
         }
-        __syncwarp();
         ode.split = a.split ? a.split + size_t(j) * n : nullptr;
         ode.x = a.x ? a.x[j] : 0.0;
-        ode.T = v.y[1];
+        ode.T = yin[1];
         ode.rho = 1.0;
         ode.cp = 1.0;
         QssStats st;
-        int ret = qss_integrate_warp(ode, v, n, P, EnforceNotMomentum(), a.dt[j], a.t_start, st);
-        bool finite = true;
+        int ret = qss_integrate_block(ode, v, n, P, EnforceNotMomentum(), a.dt[j], a.t_start, ode.w.red, st);
+        int nonfinite = 0;
         double* yout = a.state_out + size_t(j) * n;
-        for (int i = lane; i < n; i += 32) {
+        for (int i = tid; i < n; i += kChemThreads) {
             const double yi = v.y[i];
-            finite = finite && isfinite(yi);
+            nonfinite |= !isfinite(yi);
             yout[i] = yi;
         }
-        finite = __all_sync(0xffffffffu, finite);
-        if (ret == 0 && !finite) ret = -21;
-        if (lane == 0) {
+        nonfinite = __syncthreads_or(nonfinite);
+        if (ret == 0 && nonfinite) ret = -21;
+        if (tid == 0) {
             a.status[j] = ret;
             if (a.stats) {
                 a.stats[4 * size_t(j) + 0] = st.steps;
@@ -213,7 +207,6 @@ __global__ void __launch_bounds__(128) k_source_qss(MechView m, SourceArgs a, in
                 a.stats[4 * size_t(j) + 3] = 0;
             }
         }
-        __syncwarp();
     }
 }
 
@@ -227,27 +220,13 @@ struct ember_mech_s {
     int S = 0, R = 0;
     void* blob = nullptr;  // one device allocation holding every table
     MechView view{};
-    std::vector<double> mult_host;
 };
-
-namespace {
-
-template <class T>
-T* carve_dev(char*& p, size_t count) {
-    T* r = reinterpret_cast<T*>(p);
-    p += ((count * sizeof(T) + 255) / 256) * 256;
-    return r;
-}
-
-size_t carve_size(size_t count, size_t elem) { return ((count * elem + 255) / 256) * 256; }
-
-}  // namespace
 
 extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
     EMBER_CHECK_ARG(out != nullptr && d != nullptr, "null argument");
     *out = nullptr;
     const int S = d->n_species, R = d->n_reactions;
-    EMBER_CHECK_ARG(S >= 1 && R >= 0 && R < (1 << 24), "bad mechanism size (S=%d, R=%d)", S, R);
+    EMBER_CHECK_ARG(S >= 1 && S < 0xffff && R >= 0 && R < (1 << 22), "bad mechanism size (S=%d, R=%d)", S, R);
     EMBER_CHECK_ARG(d->mol_weight && d->nasa_tmid && d->nasa_coeffs, "null species arrays");
     EMBER_CHECK_ARG(R == 0 || (d->rxn_type && d->reversible && d->reactants && d->products && d->arrhenius &&
                                d->arrhenius_low && d->troe && d->default_efficiency && d->efficiency_offsets),
@@ -255,6 +234,7 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
     for (int k = 0; k < S; ++k) EMBER_CHECK_ARG(d->mol_weight[k] > 0, "species %d: molecular weight must be > 0", k);
     const int64_t ne = R ? d->efficiency_offsets[R] : 0;
     EMBER_CHECK_ARG(R == 0 || d->efficiency_offsets[0] == 0, "efficiency_offsets[0] must be 0");
+    EMBER_CHECK_ARG(ne < (int64_t(1) << 31), "too many efficiency entries");
     for (int i = 0; i < R; ++i) {
         EMBER_CHECK_ARG(d->rxn_type[i] >= 0 && d->rxn_type[i] <= 3, "reaction %d: bad type %d", i, d->rxn_type[i]);
         EMBER_CHECK_ARG(d->efficiency_offsets[i + 1] >= d->efficiency_offsets[i], "reaction %d: bad efficiency offsets", i);
@@ -269,12 +249,12 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
     }
     EMBER_CHECK_ARG(ne == 0 || (d->efficiency_species && d->efficiency_values), "null efficiency arrays");
     for (int64_t e = 0; e < ne; ++e)
-        EMBER_CHECK_ARG(d->efficiency_species[e] >= 0 && d->efficiency_species[e] < S, "efficiency entry %lld: bad species",
-                        (long long)e);
+        EMBER_CHECK_ARG(d->efficiency_species[e] >= 0 && d->efficiency_species[e] < S,
+                        "efficiency entry %lld: bad species", (long long)e);
     EMBER_TRY(ensure_device());
 
-    // Host-side derived tables.
-    std::vector<double> rW(S), hc(size_t(S) * 10), sc(size_t(S) * 8), dn(std::max(R, 1)), mult(std::max(R, 1), 1.0);
+    // ---- host-side derived tables ----
+    std::vector<double> rW(S), hc(size_t(S) * 10), sc(size_t(S) * 8);
     for (int k = 0; k < S; ++k) {
         rW[k] = 1.0 / d->mol_weight[k];
         for (int r = 0; r < 2; ++r) {
@@ -292,46 +272,106 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
             s[3] = a[4] / 4.0;
         }
     }
-    std::vector<int> sp_off(S + 1, 0), sp_ent;
+    const size_t Rs = std::max(R, 1);
+    std::vector<int4> stoich(Rs, make_int4(-1, -1, -1, -1));
+    std::vector<int> rinfo(Rs, 0), tb_rxn, tb_off(1, 0), tb_sp, fo_rxn, fo_tb;
+    std::vector<double> dn(Rs, 0.0), mult(Rs, 1.0), tb_eff, tb_def, fo_arr, fo_troe;
     std::vector<std::vector<int>> lists(S);
     for (int i = 0; i < R; ++i) {
-        std::vector<std::pair<int, int>> cnt;  // species -> occurrences as product (low 4 bits) / reactant (x16)
-        auto bump = [&](int k, int isprod) {
+        // occurrences, compacted in order (unused slots: 0xffff)
+        int rc[4] = {0xffff, 0xffff, 0xffff, 0xffff}, pr[4] = {0xffff, 0xffff, 0xffff, 0xffff};
+        int nr = 0, np = 0;
+        for (int o = 0; o < EMBER_MAX_STOICH; ++o) {
+            int r = d->reactants[i * EMBER_MAX_STOICH + o], p = d->products[i * EMBER_MAX_STOICH + o];
+            if (r >= 0) rc[nr++] = r;
+            if (p >= 0) pr[np++] = p;
+        }
+        stoich[i] = make_int4(rc[0] | (rc[1] << 16), rc[2] | (rc[3] << 16), pr[0] | (pr[1] << 16), pr[2] | (pr[3] << 16));
+        dn[i] = static_cast<double>(np - nr);
+        const int ty = d->rxn_type[i];
+        int slot = 0x3fffff;
+        if (ty != EMBER_RXN_ELEMENTARY) {
+            slot = static_cast<int>(tb_rxn.size());
+            tb_rxn.push_back(i);
+            const double de = d->default_efficiency[i];
+            tb_def.push_back(de);
+            for (int64_t e = d->efficiency_offsets[i]; e < d->efficiency_offsets[i + 1]; ++e) {
+                tb_sp.push_back(d->efficiency_species[e]);
+                tb_eff.push_back(d->efficiency_values[e] - de);
+            }
+            tb_off.push_back(static_cast<int>(tb_sp.size()));
+        }
+        if (ty == EMBER_RXN_LINDEMANN || ty == EMBER_RXN_TROE) {
+            fo_rxn.push_back(i);
+            fo_tb.push_back(slot);
+            for (int q = 0; q < 3; ++q) fo_arr.push_back(d->arrhenius_low[3 * i + q]);
+            for (int q = 0; q < 4; ++q) fo_troe.push_back(d->troe[4 * i + q]);
+        }
+        rinfo[i] = ty | ((d->reversible[i] ? 1 : 0) << 2) | (nr << 3) | (np << 6) | (slot << 9);
+        // per-species participation: (product count, reactant count)
+        std::vector<std::pair<int, int>> cnt;
+        auto bump = [&](int k, int add) {
             for (auto& c : cnt)
-                if ((c.first & 0xffffff) == k) {
-                    c.second += isprod ? 1 : 16;
+                if (c.first == k) {
+                    c.second += add;
                     return;
                 }
-            cnt.push_back({k, isprod ? 1 : 16});
+            cnt.push_back({k, add});
         };
-        int nprod = 0, nreac = 0;
-        for (int o = 0; o < EMBER_MAX_STOICH; ++o) {
-            int p = d->products[i * EMBER_MAX_STOICH + o];
-            int r = d->reactants[i * EMBER_MAX_STOICH + o];
-            if (p >= 0) { bump(p, 1); ++nprod; }
-            if (r >= 0) { bump(r, 0); ++nreac; }
-        }
-        dn[i] = static_cast<double>(nprod - nreac);
-        for (auto& c : cnt) {
-            int npk = c.second & 15, nrk = c.second >> 4;
-            lists[c.first].push_back(i | (npk << 24) | (nrk << 28));
-        }
+        for (int o = 0; o < np; ++o) bump(pr[o], 1);
+        for (int o = 0; o < nr; ++o) bump(rc[o], 16);
+        for (auto& c : cnt) lists[c.first].push_back(i | ((c.second & 15) << 24) | ((c.second >> 4) << 28));
     }
+    std::vector<int> sp_off(S + 1, 0), sp_ent;
     for (int k = 0; k < S; ++k) {
         sp_off[k + 1] = sp_off[k] + static_cast<int>(lists[k].size());
         sp_ent.insert(sp_ent.end(), lists[k].begin(), lists[k].end());
     }
-    std::vector<int> eff_off(R + 1, 0);
-    for (int i = 0; i <= R; ++i) eff_off[i] = R ? static_cast<int>(d->efficiency_offsets[i]) : 0;
-
+    const int n_tb = static_cast<int>(tb_rxn.size()), n_fo = static_cast<int>(fo_rxn.size());
     const int nT = 200;
-    const size_t Rs = std::max(R, 1);
-    size_t bytes = carve_size(S, 8) * 3 + carve_size(size_t(S) * 14, 8) + carve_size(size_t(S) * 10, 8) +
-                   carve_size(size_t(S) * 8, 8) + carve_size(Rs, 4) * 2 + carve_size(Rs * 4, 4) * 2 +
-                   carve_size(Rs * 3, 8) * 2 + carve_size(Rs * 4, 8) + carve_size(Rs, 8) * 3 +
-                   carve_size(Rs + 1, 4) + carve_size(std::max<int64_t>(ne, 1), 4) +
-                   carve_size(std::max<int64_t>(ne, 1), 8) + carve_size(S + 1, 4) +
-                   carve_size(std::max<size_t>(sp_ent.size(), 1), 4) + carve_size(size_t(nT) * Rs, 16) * 2;
+
+    // ---- one device allocation for every table ----
+    struct Piece {
+        void** dst;
+        const void* src;
+        size_t bytes;
+    };
+    MechView v{};
+    v.S = S;
+    v.R = R;
+    v.nT = nT;
+    v.n_tb = n_tb;
+    v.n_fo = n_fo;
+    v.Tmin = 273.0;
+    v.Tmax = 3500.0;
+    std::vector<Piece> pieces = {
+        {(void**)&v.W, d->mol_weight, sizeof(double) * S},
+        {(void**)&v.rW, rW.data(), sizeof(double) * S},
+        {(void**)&v.tmid, d->nasa_tmid, sizeof(double) * S},
+        {(void**)&v.nasa, d->nasa_coeffs, sizeof(double) * S * 14},
+        {(void**)&v.hc, hc.data(), sizeof(double) * S * 10},
+        {(void**)&v.sc, sc.data(), sizeof(double) * S * 8},
+        {(void**)&v.stoich, stoich.data(), sizeof(int4) * Rs},
+        {(void**)&v.rinfo, rinfo.data(), sizeof(int) * Rs},
+        {(void**)&v.arr, R ? d->arrhenius : nullptr, sizeof(double) * 3 * Rs},
+        {(void**)&v.mult, mult.data(), sizeof(double) * Rs},
+        {(void**)&v.dn, dn.data(), sizeof(double) * Rs},
+        {(void**)&v.tb_rxn, tb_rxn.data(), sizeof(int) * std::max(n_tb, 1)},
+        {(void**)&v.tb_off, tb_off.data(), sizeof(int) * (n_tb + 1)},
+        {(void**)&v.tb_sp, tb_sp.data(), sizeof(int) * std::max<size_t>(tb_sp.size(), 1)},
+        {(void**)&v.tb_eff, tb_eff.data(), sizeof(double) * std::max<size_t>(tb_eff.size(), 1)},
+        {(void**)&v.tb_def, tb_def.data(), sizeof(double) * std::max(n_tb, 1)},
+        {(void**)&v.fo_rxn, fo_rxn.data(), sizeof(int) * std::max(n_fo, 1)},
+        {(void**)&v.fo_tb, fo_tb.data(), sizeof(int) * std::max(n_fo, 1)},
+        {(void**)&v.fo_arr, fo_arr.data(), sizeof(double) * 3 * std::max(n_fo, 1)},
+        {(void**)&v.fo_troe, fo_troe.data(), sizeof(double) * 4 * std::max(n_fo, 1)},
+        {(void**)&v.sp_off, sp_off.data(), sizeof(int) * (S + 1)},
+        {(void**)&v.sp_ent, sp_ent.data(), sizeof(int) * std::max<size_t>(sp_ent.size(), 1)},
+        {(void**)&v.kf_tab, nullptr, sizeof(double2) * size_t(nT) * Rs},
+        {(void**)&v.kc_tab, nullptr, sizeof(double2) * size_t(nT) * Rs},
+    };
+    size_t bytes = 0;
+    for (auto& pc : pieces) bytes += ((pc.bytes + 255) / 256) * 256;
     auto* mh = new ember_mech_s;
     mh->S = S;
     mh->R = R;
@@ -342,89 +382,30 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
         return EMBER_ENOMEM;
     }
     char* p = static_cast<char*>(mh->blob);
-    MechView& v = mh->view;
-    v.S = S;
-    v.R = R;
-    v.nT = nT;
-    v.Tmin = 273.0;
-    v.Tmax = 3500.0;
-    double* W = carve_dev<double>(p, S);
-    double* rWd = carve_dev<double>(p, S);
-    double* tmid = carve_dev<double>(p, S);
-    double* nasa = carve_dev<double>(p, size_t(S) * 14);
-    double* hcd = carve_dev<double>(p, size_t(S) * 10);
-    double* scd = carve_dev<double>(p, size_t(S) * 8);
-    int* type = carve_dev<int>(p, Rs);
-    int* rev = carve_dev<int>(p, Rs);
-    int* reac = carve_dev<int>(p, Rs * 4);
-    int* prod = carve_dev<int>(p, Rs * 4);
-    double* arr = carve_dev<double>(p, Rs * 3);
-    double* arr_low = carve_dev<double>(p, Rs * 3);
-    double* troe = carve_dev<double>(p, Rs * 4);
-    double* def_eff = carve_dev<double>(p, Rs);
-    double* multd = carve_dev<double>(p, Rs);
-    double* dnd = carve_dev<double>(p, Rs);
-    int* eoff = carve_dev<int>(p, Rs + 1);
-    int* esp = carve_dev<int>(p, std::max<int64_t>(ne, 1));
-    double* eval = carve_dev<double>(p, std::max<int64_t>(ne, 1));
-    int* spo = carve_dev<int>(p, S + 1);
-    int* spe = carve_dev<int>(p, std::max<size_t>(sp_ent.size(), 1));
-    double2* kft = carve_dev<double2>(p, size_t(nT) * Rs);
-    double2* kct = carve_dev<double2>(p, size_t(nT) * Rs);
-    auto up = [&](void* dst, const void* src, size_t n) {
-        if (e == cudaSuccess && n) e = cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice);
-    };
-    up(W, d->mol_weight, sizeof(double) * S);
-    up(rWd, rW.data(), sizeof(double) * S);
-    up(tmid, d->nasa_tmid, sizeof(double) * S);
-    up(nasa, d->nasa_coeffs, sizeof(double) * S * 14);
-    up(hcd, hc.data(), sizeof(double) * S * 10);
-    up(scd, sc.data(), sizeof(double) * S * 8);
-    if (R) {
-        up(type, d->rxn_type, sizeof(int) * R);
-        up(rev, d->reversible, sizeof(int) * R);
-        up(reac, d->reactants, sizeof(int) * R * 4);
-        up(prod, d->products, sizeof(int) * R * 4);
-        up(arr, d->arrhenius, sizeof(double) * R * 3);
-        up(arr_low, d->arrhenius_low, sizeof(double) * R * 3);
-        up(troe, d->troe, sizeof(double) * R * 4);
-        up(def_eff, d->default_efficiency, sizeof(double) * R);
-        up(multd, mult.data(), sizeof(double) * R);
-        up(dnd, dn.data(), sizeof(double) * R);
-        up(eoff, eff_off.data(), sizeof(int) * (R + 1));
-        up(esp, d->efficiency_species, sizeof(int) * ne);
-        up(eval, d->efficiency_values, sizeof(double) * ne);
+    for (auto& pc : pieces) {
+        *pc.dst = p;
+        if (e == cudaSuccess && pc.src && pc.bytes) {
+            // sources shorter than the padded count (empty lists) copy what exists
+            size_t nbytes = pc.bytes;
+            if (pc.src == tb_rxn.data()) nbytes = sizeof(int) * n_tb;
+            else if (pc.src == tb_sp.data()) nbytes = sizeof(int) * tb_sp.size();
+            else if (pc.src == tb_eff.data()) nbytes = sizeof(double) * tb_eff.size();
+            else if (pc.src == tb_def.data()) nbytes = sizeof(double) * n_tb;
+            else if (pc.src == fo_rxn.data()) nbytes = sizeof(int) * n_fo;
+            else if (pc.src == fo_tb.data()) nbytes = sizeof(int) * n_fo;
+            else if (pc.src == fo_arr.data()) nbytes = sizeof(double) * fo_arr.size();
+            else if (pc.src == fo_troe.data()) nbytes = sizeof(double) * fo_troe.size();
+            else if (pc.src == sp_ent.data()) nbytes = sizeof(int) * sp_ent.size();
+            else if (pc.src == d->arrhenius) nbytes = sizeof(double) * 3 * R;
+            if (nbytes) e = cudaMemcpy(p, pc.src, nbytes, cudaMemcpyHostToDevice);
+        }
+        p += ((pc.bytes + 255) / 256) * 256;
     }
-    up(spo, sp_off.data(), sizeof(int) * (S + 1));
-    up(spe, sp_ent.data(), sizeof(int) * sp_ent.size());
-    v.W = W;
-    v.rW = rWd;
-    v.tmid = tmid;
-    v.nasa = nasa;
-    v.hc = hcd;
-    v.sc = scd;
-    v.type = type;
-    v.rev = rev;
-    v.reac = reac;
-    v.prod = prod;
-    v.arr = arr;
-    v.arr_low = arr_low;
-    v.troe = troe;
-    v.def_eff = def_eff;
-    v.eff_off = eoff;
-    v.eff_sp = esp;
-    v.eff_val = eval;
-    v.mult = multd;
-    v.dn = dnd;
-    v.sp_off = spo;
-    v.sp_ent = spe;
-    v.kf_tab = kft;
-    v.kc_tab = kct;
     if (e == cudaSuccess && R) {
         double* work = nullptr;
-        e = cudaMalloc(&work, sizeof(double) * ChemSmem::doubles(S, R) * nT);
+        e = cudaMalloc(&work, sizeof(double) * ChemSmem::doubles(S, R, n_tb, n_fo) * nT);
         if (e == cudaSuccess) {
-            k_build_tables<<<(nT * 32 + 127) / 128, 128>>>(v, work);
+            k_build_tables<<<nT, kChemThreads>>>(v, work);
             k_table_slopes<<<std::min<int64_t>((int64_t(nT) * R + 255) / 256, 4096), 256>>>(v);
             e = cudaDeviceSynchronize();
             cudaFree(work);
@@ -436,7 +417,7 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
         delete mh;
         return EMBER_ECUDA;
     }
-    mh->mult_host = mult;
+    mh->view = v;
     *out = mh;
     return EMBER_OK;
 }
@@ -492,14 +473,12 @@ extern "C" int ember_gas_eval(ember_mech m, int n, double pressure, int model, i
     EMBER_TRY(stage_buffer(sc, hk, size_t(n) * S, mem, &c4));
     EMBER_TRY(stage_buffer(sc, cp_mass, n, mem, &c5));
     EMBER_TRY(stage_buffer(sc, density, n, mem, &c6));
-    const size_t per = (ChemSmem::doubles(S, m->R) + S) * sizeof(double);
-    int warps = 4;
-    while (warps > 1 && per * warps > 200 * 1024) warps /= 2;
-    EMBER_CHECK_ARG(per * warps <= 227 * 1024, "mechanism too large for the shared-memory work area");
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_gas_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per * warps)));
-    const int blocks = std::min((n + warps - 1) / warps, 65535);
-    k_gas_eval<<<blocks, 32 * warps, per * warps, st>>>(m->view, n, pressure, model, mode, dT, dY, c1, c2, c3, c4,
-                                                        c5, c6);
+    const MechView& v = m->view;
+    const size_t per = (ChemSmem::doubles(S, m->R, v.n_tb, v.n_fo) + S) * sizeof(double);
+    EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the shared-memory work area (%zu B)", per);
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_gas_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
+    const int blocks = std::min(n, 65535);
+    k_gas_eval<<<blocks, kChemThreads, per, st>>>(v, n, pressure, model, mode, dT, dY, c1, c2, c3, c4, c5, c6);
     EMBER_TRY(stage_out(creation, c1, size_t(n) * S, mem, st));
     EMBER_TRY(stage_out(destruction, c2, size_t(n) * S, mem, st));
     EMBER_TRY(stage_out(net, c3, size_t(n) * S, mem, st));
@@ -590,20 +569,16 @@ SourceArgs make_source_args(const ember_source_options* o, int n, const double* 
 }
 
 int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, cudaStream_t st) {
-    const int n = m.S + 2;
-    const size_t per = qss_smem_doubles(m.S, m.R) * sizeof(double);
-    int warps = 4;
-    while (warps > 1 && per * warps > 227 * 1024) warps /= 2;
-    EMBER_CHECK_ARG(per * warps <= 227 * 1024, "mechanism too large for the QSS shared-memory work area (%zu B)", per);
-    (void)n;
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_qss, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per * warps)));
+    const size_t per = qss_smem_doubles(m) * sizeof(double);
+    EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the QSS shared-memory work area (%zu B)", per);
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_qss, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
     int dev = 0, sms = 0, per_sm = 0;
     EMBER_CUDA_TRY(cudaGetDevice(&dev));
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    EMBER_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_source_qss, 32 * warps, per * warps));
+    EMBER_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_source_qss, kChemThreads, per));
     per_sm = std::max(per_sm, 1);
-    const int blocks = std::max(1, std::min((a.n + warps - 1) / warps, sms * per_sm));
-    k_source_qss<<<blocks, 32 * warps, per * warps, st>>>(m, a, counter);
+    const int blocks = std::max(1, std::min(a.n, sms * per_sm));
+    k_source_qss<<<blocks, kChemThreads, per, st>>>(m, a, counter);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }
@@ -668,7 +643,7 @@ namespace ember {
 // (test/old/test_qssintegrator.cpp:11-83) as a q/d right-hand side.
 struct CesiumOde {
     __device__ void eval(double, const double* y, double* q, double* d, bool) {
-        if (lane_id() == 0) {
+        if (threadIdx.x == 0) {
             const double o2m = y[0], csp = y[1], cs = y[2], cso2 = y[3], o2 = y[4], n2 = y[5];
             const double ne = (csp - o2m > 0.0) ? csp - o2m : 0.0;
             const double cr1 = 5.00e-08 * o2m * csp;
@@ -689,7 +664,7 @@ struct CesiumOde {
             q[4] = cr1 + cr4;
             d[4] = cr5 + cr6 + cr7;
         }
-        __syncwarp();
+        __syncthreads();
     }
 };
 
@@ -697,19 +672,20 @@ struct EnforceAll {
     __device__ bool operator()(int) const { return true; }
 };
 
-__global__ void k_qss_cesium(QssParams P, double* y7, double tf, int* stats, int* ret) {
+__global__ void __launch_bounds__(kChemThreads) k_qss_cesium(QssParams P, double* y7, double tf, int* stats, int* ret) {
     __shared__ double buf[12 * 7];
+    __shared__ double red[kChemThreads + 2];
     QssSmem v;
     v.carve(buf, 7);
-    for (int i = lane_id(); i < 7; i += 32) {
+    for (int i = threadIdx.x; i < 7; i += kChemThreads) {
         v.y[i] = y7[i];
         v.ymin[i] = 1e-20;
     }
-    __syncwarp();
+    __syncthreads();
     CesiumOde ode;
     QssStats st;
-    int r = qss_integrate_warp(ode, v, 7, P, EnforceAll(), tf, 0.0, st);
-    if (lane_id() == 0) {
+    int r = qss_integrate_block(ode, v, 7, P, EnforceAll(), tf, 0.0, red, st);
+    if (threadIdx.x == 0) {
         for (int i = 0; i < 7; ++i) y7[i] = v.y[i];
         y7[6] = y7[1] - y7[0];
         stats[0] = st.steps;
@@ -735,7 +711,7 @@ extern "C" int ember_selftest_qss_cesium(double epsmin, double epsmax, double dt
     cudaError_t e = cudaMalloc(&di, sizeof(int) * 5);
     if (e == cudaSuccess) e = cudaMemcpy(dy, y7, sizeof(double) * 7, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
-        k_qss_cesium<<<1, 32>>>(P, dy, tf, di, di + 4);
+        k_qss_cesium<<<1, kChemThreads>>>(P, dy, tf, di, di + 4);
         e = cudaGetLastError();
     }
     int ret = 0;

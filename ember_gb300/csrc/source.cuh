@@ -40,10 +40,10 @@ __device__ __forceinline__ double igniter(const SourceArgs& a, double t, double 
     return 0.0;
 }
 
-// Shared memory (doubles) of one QSS warp: kinetics work area, QSS vectors,
+// Shared memory (doubles) of one QSS point: kinetics work area, QSS vectors,
 // predictor enthalpies.
-__host__ __device__ inline size_t qss_smem_doubles(int S, int R) {
-    return ChemSmem::doubles(S, R) + QssSmem::doubles(S + 2) + size_t(S);
+__host__ __device__ inline size_t qss_smem_doubles(const MechView& m) {
+    return ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo) + QssSmem::doubles(m.S + 2) + size_t(m.S);
 }
 
 int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, cudaStream_t st);

@@ -22,9 +22,8 @@
  * PARITY UNPINNED: the reference's tests hold no rates, equilibrium constants
  * or thermo values, and Cantera and its mechanism files are absent.
  *
- * Sums over species use one fixed order (element k goes to partial sum
- * k mod 32, partial sums combined by a butterfly), the order the GPU warp
- * reductions use; the reference leaves this order to Eigen.
+ * Sums over species use one fixed order (see wsum), the order of the GPU
+ * block reductions; the reference leaves this order to Eigen.
  */
 #include <math.h>
 #include <pthread.h>
@@ -118,17 +117,21 @@ static double oracle_exp10(double x) { return oracle_exp(x * 2.302585092994046);
 static double dmax(double a, double b) { return (a < b) ? b : a; } /* std::max */
 static double dmin(double a, double b) { return (b < a) ? b : a; } /* std::min */
 
-/* Sum in the fixed order of a 32-lane warp reduction. */
+/* Sum in the fixed order of the GPU block reduction: element k goes to the
+ * partial sum of thread k mod 128 (sequential in k); the 128 partials are
+ * folded into 32 as ((p[l] + p[l+32]) + p[l+64]) + p[l+96] and combined by
+ * an xor butterfly. */
 static double wsum(const double* x, int n) {
-    double p[32];
-    for (int l = 0; l < 32; ++l) p[l] = 0.0;
-    for (int k = 0; k < n; ++k) p[k & 31] += x[k];
+    double p[128], q[32];
+    for (int l = 0; l < 128; ++l) p[l] = 0.0;
+    for (int k = 0; k < n; ++k) p[k & 127] += x[k];
+    for (int l = 0; l < 32; ++l) q[l] = ((p[l] + p[l + 32]) + p[l + 64]) + p[l + 96];
     for (int off = 16; off >= 1; off >>= 1) {
-        double q[32];
-        for (int l = 0; l < 32; ++l) q[l] = p[l] + p[l ^ off];
-        memcpy(p, q, sizeof p);
+        double r[32];
+        for (int l = 0; l < 32; ++l) r[l] = q[l] + q[l ^ off];
+        memcpy(q, r, sizeof q);
     }
-    return p[0];
+    return q[0];
 }
 
 /* ---- mechanism ------------------------------------------------------- */
