@@ -60,6 +60,8 @@ def _declare(lib):
         "ember_tridiag_get_ydot": (C.c_int, [vp, vp, C.c_int, vp]),
         "ember_diffusion_integrate": (C.c_int, [C.c_int, C.POINTER(DiffusionGrid), C.c_int, vp, vp, vp, vp, vp,
                                                 C.POINTER(DiffusionOptions), vp, C.c_int, vp]),
+        "ember_diffusion_integrate_noalloc": (C.c_int, [C.c_int, C.POINTER(DiffusionGrid), C.c_int, vp, vp, vp,
+                                                        vp, vp, C.POINTER(DiffusionOptions), vp, vp]),
         "ember_probe_fp64_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
         "ember_mech_create": (C.c_int, [vp, C.POINTER(vp)]),
         "ember_mech_destroy": (C.c_int, [vp]),

@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
 
 namespace ember {
@@ -423,5 +424,143 @@ extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_gri
             return EMBER_EFAIL;
         }
     }
+    return EMBER_OK;
+}
+
+// ------------------------------------------ allocation-free diffusion stage --
+//
+// Some callers cannot allocate device memory while they run a time step: a
+// solver embedded in an application whose device memory is owned by another
+// allocator (a framework's caching pool, a fixed budget set at start-up), or
+// code that must keep its footprint constant after initialisation. For them,
+// ember_diffusion_integrate_noalloc runs the same kernels as
+// ember_diffusion_integrate with its workspace in the file-scope device array
+// below instead of stream-ordered allocations. The array is sized for
+// EMBER_NOALLOC_MAX_VALUES values and EMBER_NOALLOC_MAX_SYSTEMS systems and is
+// held by every GPU that loads the library until the process exits.
+
+namespace {
+
+constexpr size_t kNoAllocWorkBytes = size_t(7) * EMBER_NOALLOC_MAX_VALUES * sizeof(double);
+constexpr size_t kNoAllocInfoBytes = size_t(EMBER_NOALLOC_MAX_SYSTEMS) * sizeof(ember::DiffSysInfo);
+constexpr size_t kNoAllocStatusBytes = size_t(EMBER_NOALLOC_MAX_SYSTEMS) * sizeof(int);
+constexpr size_t kNoAllocBytes = kNoAllocWorkBytes + kNoAllocInfoBytes + kNoAllocStatusBytes;
+
+// Workspace of the allocation-free entry point: matrix rows a, b, c, k and
+// integrator arrays y_prev, lu_c, 1/denominator (7 doubles per value), then
+// the per-system descriptors and status words.
+static __device__ __align__(256) unsigned char g_diffusion_noalloc_scratch[kNoAllocBytes];
+
+// Device address of the array per device; host code cannot use the symbol
+// itself (in host code it names a host-side stand-in).
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[64] = {};
+
+int noalloc_scratch(void** out) {
+    int dev = 0;
+    EMBER_CUDA_TRY(cudaGetDevice(&dev));
+    EMBER_CHECK_ARG(dev >= 0 && dev < 64, "device index %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_diffusion_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            set_error("cudaGetSymbolAddress of the diffusion scratch failed: %s", cudaGetErrorString(e));
+            return EMBER_ECUDA;
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return EMBER_OK;
+}
+
+}  // namespace
+
+extern "C" int ember_diffusion_integrate_noalloc(int n_flames, const ember_diffusion_grid* grids, int n_vars,
+                                                 const double* x, const double* B, const double* D,
+                                                 const double* split_const, double* y,
+                                                 const ember_diffusion_options* opts, int* status, void* stream) {
+    EMBER_CHECK_ARG(n_flames > 0 && grids != nullptr, "need at least one flame");
+    EMBER_CHECK_ARG(n_vars > 0, "n_vars must be positive");
+    EMBER_CHECK_ARG(x && B && D && y && opts, "null array or options argument");
+    const int64_t n_sys = int64_t(n_flames) * n_vars;
+    EMBER_CHECK_ARG(n_sys <= EMBER_NOALLOC_MAX_SYSTEMS,
+                    "ember_diffusion_integrate_noalloc: %lld systems exceed the maximum of %d "
+                    "(use ember_diffusion_integrate)",
+                    (long long)n_sys, EMBER_NOALLOC_MAX_SYSTEMS);
+    std::vector<DiffSysInfo> info(n_sys);
+    int64_t n_pts = 0, n_vals = 0;
+    int nmax = 0;
+    for (int f = 0; f < n_flames; ++f) {
+        const ember_diffusion_grid& g = grids[f];
+        EMBER_CHECK_ARG(g.n_points >= 3, "flame %d: n_points must be >= 3 (got %d)", f, g.n_points);
+        EMBER_CHECK_ARG(g.left_bc >= 0 && g.left_bc <= 4, "flame %d: bad left_bc %d", f, g.left_bc);
+        EMBER_CHECK_ARG(g.right_bc == EMBER_BC_FIXED_VALUE || g.right_bc == EMBER_BC_ZERO_GRADIENT ||
+                            g.right_bc == EMBER_BC_FLOATING,
+                        "flame %d: bad right_bc %d", f, g.right_bc);
+        EMBER_CHECK_ARG(g.alpha >= 0, "flame %d: bad alpha %d", f, g.alpha);
+        for (int v = 0; v < n_vars; ++v) {
+            DiffSysInfo& s = info[int64_t(f) * n_vars + v];
+            s.n = g.n_points;
+            s.left_bc = g.left_bc;
+            s.right_bc = g.right_bc;
+            s.alpha = g.alpha;
+            s.grid_off = n_pts;
+            s.off = n_vals + int64_t(v) * g.n_points;
+        }
+        n_pts += g.n_points;
+        n_vals += int64_t(n_vars) * g.n_points;
+        nmax = std::max(nmax, g.n_points);
+    }
+    EMBER_CHECK_ARG(n_vals <= EMBER_NOALLOC_MAX_VALUES,
+                    "ember_diffusion_integrate_noalloc: %lld values (variables x points) exceed the maximum of %d "
+                    "(use ember_diffusion_integrate)",
+                    (long long)n_vals, EMBER_NOALLOC_MAX_VALUES);
+    EMBER_CHECK_ARG(opts->h != nullptr || (opts->dt_multiplier > 0 && opts->global_timestep > 0),
+                    "without explicit h, dt_multiplier and global_timestep must be positive");
+    EMBER_CHECK_ARG(opts->t_end > opts->t_start, "t_end must exceed t_start");
+
+    void* base = nullptr;
+    EMBER_TRY(noalloc_scratch(&base));
+    char* p = static_cast<char*>(base);
+    double* work = reinterpret_cast<double*>(p);
+    DiffSysInfo* d_info = reinterpret_cast<DiffSysInfo*>(p + kNoAllocWorkBytes);
+    int* d_status = reinterpret_cast<int*>(p + kNoAllocWorkBytes + kNoAllocInfoBytes);
+    cudaStream_t st = as_stream(stream);
+    EMBER_CUDA_TRY(cudaMemcpyAsync(d_info, info.data(), sizeof(DiffSysInfo) * n_sys, cudaMemcpyHostToDevice, st));
+
+    DiffusionView dv;
+    dv.n_systems = static_cast<int>(n_sys);
+    dv.info = d_info;
+    dv.x = x;
+    dv.B = B;
+    dv.D = D;
+    dv.split_const = split_const;
+    dv.h = opts->h;
+    dv.wall_const = opts->wall_const;
+    dv.y_inf = opts->y_inf;
+    dv.status = status ? status : d_status;
+    dv.a = work;
+    dv.b = work + EMBER_NOALLOC_MAX_VALUES;
+    dv.c = work + 2 * int64_t(EMBER_NOALLOC_MAX_VALUES);
+    dv.k = work + 3 * int64_t(EMBER_NOALLOC_MAX_VALUES);
+    dim3 grid_rows(std::min(blocks_for(nmax, 256), 32), std::min<int64_t>(n_sys, 65535));
+    k_diffusion_rows<<<grid_rows, 256, 0, st>>>(dv);
+
+    TriBatchView tb;
+    tb.n_systems = static_cast<int>(n_sys);
+    tb.off = nullptr;
+    tb.info = d_info;
+    tb.a = dv.a;
+    tb.b = dv.b;
+    tb.c = dv.c;
+    tb.k = dv.k;
+    tb.y = y;
+    tb.yprev = work + 4 * int64_t(EMBER_NOALLOC_MAX_VALUES);
+    tb.luc = work + 5 * int64_t(EMBER_NOALLOC_MAX_VALUES);
+    tb.inv = work + 6 * int64_t(EMBER_NOALLOC_MAX_VALUES);
+    k_diffusion_integrate_serial<<<blocks_for(n_sys, 64), 64, 0, st>>>(dv, tb, opts->t_start, opts->t_end,
+                                                                        opts->dt_multiplier, opts->global_timestep);
+    EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }

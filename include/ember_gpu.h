@@ -172,6 +172,33 @@ int ember_diffusion_integrate(int n_flames, const ember_diffusion_grid* grids, i
                               const ember_diffusion_options* opts, int* status,
                               int mem, void* stream);
 
+/* Allocation-free variant of ember_diffusion_integrate, for callers that
+ * must not allocate device memory while they step: an application whose
+ * device memory is owned by another allocator (a framework's caching pool or
+ * a budget fixed at start-up), or code whose footprint must stay constant
+ * after initialisation. It has no counterpart in the reference (which runs on
+ * the CPU). Same arguments and results as ember_diffusion_integrate with
+ * EMBER_MEM_DEVICE (all arrays are device pointers; the call is asynchronous
+ * on `stream`), but its workspace is a fixed device array inside the library,
+ * sized for EMBER_NOALLOC_MAX_VALUES values (n_vars x total points) and
+ * EMBER_NOALLOC_MAX_SYSTEMS (flame, variable) systems, about 28.3 MiB that
+ * every GPU which loads the library keeps until the process exits. Larger
+ * problems are rejected with EMBER_EINVAL. The call allocates nothing: no
+ * cudaMalloc, cudaFree or allocating library routine.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Every call uses the same array: calls whose kernels can overlap on the GPU
+ * (other streams, other host threads) race and corrupt each other's results;
+ * issue them on one stream. No part of the array needs to start at zero:
+ * every element a call reads is written earlier in the same call. With
+ * status == NULL the per-system status is kept in the array. */
+#define EMBER_NOALLOC_MAX_VALUES  524288
+#define EMBER_NOALLOC_MAX_SYSTEMS 8192
+int ember_diffusion_integrate_noalloc(int n_flames, const ember_diffusion_grid* grids, int n_vars,
+                                      const double* x, const double* B, const double* D,
+                                      const double* split_const, double* y,
+                                      const ember_diffusion_options* opts, int* status, void* stream);
+
 /* ======================================================================
  * Mechanism tables
  *
