@@ -312,7 +312,7 @@ def run_ours(args):
         "e2e": {"value": ws * args.points * args.steps / e2e_s, "unit": "points/s",
                 "h2d_bytes_per_step": int(state.nbytes + dt.nbytes),
                 "d2h_bytes_per_step": int(state.nbytes + status_h.numpy().nbytes + stats_h.numpy().nbytes)},
-        "gpu_launches": args.steps,
+        "gpu_launches": 4 * args.steps,  # per call: 3 work-order kernels + the integrator
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak_t, "unit": "TFLOP/s",
                      "frac": achieved / peak_t, "traffic": traffic,
                      "peak_source": "live DFMA throughput probe (ember_probe_fp64_rate); MEASURED_PEAKS.json "

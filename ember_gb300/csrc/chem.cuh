@@ -1,26 +1,30 @@
-// Device thermo / kinetics of the source term, evaluated by one CTA of
-// kChemThreads threads per grid point. Restates what the reference obtains
-// from Cantera in SourceSystemQSS::odefun and SourceSystemCVODE::f
-// (src/sourceSystem.cpp:128-164, 445-499) and the 'interp' model of
-// InterpKinetics / MultiArrheniusInterp (src/chemistry0d.cpp:271-436):
+// Device thermo / kinetics of the source term, evaluated by one CTA of NT
+// threads per grid point (NT a multiple of 32, chosen from the mechanism
+// size). Restates what the reference obtains from Cantera in
+// SourceSystemQSS::odefun and SourceSystemCVODE::f (src/sourceSystem.cpp:
+// 128-164, 445-499) and the 'interp' model of InterpKinetics /
+// MultiArrheniusInterp (src/chemistry0d.cpp:271-436):
 //   NASA7 cp/R, h/RT, s/R; modified Arrhenius rates; third-body
 //   concentrations from efficiencies; Lindemann / Troe falloff; reverse rates
 //   through 1/Kc = exp(dG0/RT) (RT/p0)^dn capped at 1e300; creation,
 //   destruction and net production rates.
 //
 // Work is split into uniform passes so that no thread runs a long branch the
-// others skip: temperature-only terms (thermo, rate constants, 1/Kc, the
-// Arrhenius limits and log10 Fcent of falloff reactions) once per
-// temperature; then per composition: [M] over the third-body list, falloff
-// blending over the falloff list, rates of progress over all reactions, and
-// a per-species gather of production rates in reaction order.
+// others skip: temperature-only terms (thermo, rate constants times the
+// reaction multipliers, 1/Kc, the Arrhenius limits and log10 Fcent of
+// falloff reactions) once per temperature; then per composition: [M] over
+// the third-body list, falloff blending over the falloff list, rates of
+// progress over all reactions, and a per-species gather of production rates
+// in reaction order. The temperature-only per-reaction values live in a
+// per-CTA slice of global memory (L2-resident), everything else in shared
+// memory.
 //
 // Every sum over species is a block reduction in one fixed order: element k
-// goes to the partial sum of thread k mod 128 (sequential in k); the 128
-// partials are folded into 32 as ((p[l] + p[l+32]) + p[l+64]) + p[l+96] and
-// combined by an xor butterfly. The translation unit is compiled without
-// automatic FMA contraction; the multiply-adds that are fused are written as
-// fma(), in the same places as in the CPU oracle.
+// goes to the partial sum of thread k mod NT (sequential in k); the NT
+// partials are folded into 32 as p[l] + p[l+32] + p[l+64] + ... (in that
+// order) and combined by an xor butterfly. The translation unit is compiled
+// without automatic FMA contraction; the multiply-adds that are fused are
+// written as fma(), in the same places as in the CPU oracle.
 #pragma once
 
 #include <cstdint>
@@ -34,11 +38,21 @@ constexpr double kOneAtm = 101325.0;
 constexpr double kBigNumber = 1e300;
 constexpr double kSmallNumber = 1e-300;
 constexpr int kMaxStoich = 4;
-constexpr int kChemThreads = 128;  // threads per grid point (4 warps)
+constexpr int kMaxChemThreads = 256;
 
 enum : int { RXN_ELEMENTARY = 0, RXN_THREE_BODY = 1, RXN_LINDEMANN = 2, RXN_TROE = 3 };
 enum : int { KIN_STANDARD = 0, KIN_INTERP = 1 };
 enum : int { STATE_NORMALIZED = 0, STATE_NO_NORM = 1 };
+
+// Threads per grid point for a mechanism with S species: the state vector
+// (S+2 values) fits in one pass.
+__host__ __device__ inline int chem_threads_for(int S) {
+    const int n = S + 2;
+    if (n <= 64) return 64;
+    if (n <= 128) return 128;
+    if (n <= 160) return 160;
+    return 256;
+}
 
 // Device tables of one mechanism (all arrays in global memory).
 struct MechView {
@@ -64,7 +78,7 @@ struct MechView {
     const int* fo_rxn;    // [n_fo] reaction of each falloff slot
     const int* fo_tb;     // [n_fo] third-body slot of each falloff slot
     const double* fo_arr; // [n_fo][3] low-pressure Arrhenius
-    const double* fo_troe;// [n_fo][4] a, T3, T1, T2 (type Lindemann: unused)
+    const double* fo_troe;// [n_fo][4] a, 1/T3, 1/T1, T2 (type Lindemann: unused)
     const int* sp_off;    // [S+1] reactions in which species k occurs, in reaction order
     const int* sp_ent;    // reaction | n_product_occurrences << 24 | n_reactant_occurrences << 28
     const double2* kf_tab;// [nT][R] (value, slope)
@@ -75,7 +89,8 @@ __device__ __forceinline__ int rinfo_type(int r) { return r & 3; }
 __device__ __forceinline__ int rinfo_rev(int r) { return (r >> 2) & 1; }
 __device__ __forceinline__ int rinfo_tbslot(int r) { return (r >> 9) & 0x3fffff; }
 
-// Per-point shared-memory work area of the kinetics.
+// Work area of the kinetics of one point: shared memory, plus the
+// temperature-only per-reaction values in global memory.
 struct ChemSmem {
     double* c;     // [S] concentrations
     double* ym;    // [S]
@@ -84,23 +99,27 @@ struct ChemSmem {
     double* gRT;   // [S]
     double* wq;    // [S] creation
     double* wd;    // [S] destruction
-    double* wn;    // [S] net
+    double* wn;    // [S] net (only when the caller wants it; may alias wd otherwise)
     double* hk;    // [S] partial molar enthalpies [J/kmol]
-    double* kf;    // [R] forward rate constants (falloff rows: refreshed per composition)
-    double* rkc;   // [R] 1/Kc
     double* ropf;  // [R]
     double* ropr;  // [R]
     double* concm; // [n_tb]
     double* fo_kinf;  // [n_fo]
+    double* fo_rkinf; // [n_fo] 1/(kinf + 1e-300)
     double* fo_k0;    // [n_fo]
     double* fo_lfc;   // [n_fo] log10 Fcent (Troe)
-    double* red;      // [kChemThreads + 2] reduction scratch
+    double* red;      // [kMaxChemThreads + 2] reduction scratch
+    double* kfm;   // global [R]: rate constant x multiplier (falloff rows: refreshed per composition)
+    double* rkc;   // global [R]: 1/Kc
 
-    static __host__ __device__ size_t doubles(int S, int R, int n_tb, int n_fo) {
-        return size_t(9) * S + size_t(4) * R + n_tb + size_t(3) * n_fo + kChemThreads + 2;
+    // shared-memory doubles (with_net: a separate wn array)
+    static __host__ __device__ size_t doubles(int S, int R, int n_tb, int n_fo, bool with_net) {
+        return size_t(with_net ? 9 : 8) * S + size_t(2) * R + n_tb + size_t(4) * n_fo + kMaxChemThreads + 2;
     }
+    // global doubles per point slot
+    static __host__ __device__ size_t global_doubles(int R) { return size_t(2) * R; }
 
-    __device__ void carve(double* base, const MechView& m) {
+    __device__ void carve(double* base, double* gbase, const MechView& m, bool with_net) {
         const int S = m.S, R = m.R;
         c = base;
         ym = c + S;
@@ -109,17 +128,18 @@ struct ChemSmem {
         gRT = hRT + S;
         wq = gRT + S;
         wd = wq + S;
-        wn = wd + S;
-        hk = wn + S;
-        kf = hk + S;
-        rkc = kf + R;
-        ropf = rkc + R;
+        hk = wd + S;
+        wn = with_net ? hk + S : wd;
+        ropf = hk + S + (with_net ? S : 0);
         ropr = ropf + R;
         concm = ropr + R;
         fo_kinf = concm + m.n_tb;
-        fo_k0 = fo_kinf + m.n_fo;
+        fo_rkinf = fo_kinf + m.n_fo;
+        fo_k0 = fo_rkinf + m.n_fo;
         fo_lfc = fo_k0 + m.n_fo;
         red = fo_lfc + m.n_fo;
+        kfm = gbase;
+        rkc = gbase + R;
     }
 };
 
@@ -130,6 +150,7 @@ __device__ __forceinline__ double dminr(double a, double b) { return (b < a) ? b
 
 // Block sum of the threads' partial sums in the fixed order described above.
 // Every thread of the CTA must call it; all receive the result.
+template <int NT>
 __device__ __forceinline__ double block_sum(double* red, double partial) {
     const int t = threadIdx.x;
     red[t] = partial;
@@ -137,17 +158,18 @@ __device__ __forceinline__ double block_sum(double* red, double partial) {
     if (t < 32) {
         double q = red[t];
 #pragma unroll
-        for (int w = 1; w < kChemThreads / 32; ++w) q = q + red[t + 32 * w];
+        for (int w = 1; w < NT / 32; ++w) q = q + red[t + 32 * w];
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) q = q + __shfl_xor_sync(0xffffffffu, q, off);
-        if (t == 0) red[kChemThreads] = q;
+        if (t == 0) red[kMaxChemThreads] = q;
     }
     __syncthreads();
-    const double r = red[kChemThreads];
+    const double r = red[kMaxChemThreads];
     __syncthreads();
     return r;
 }
 
+template <int NT>
 __device__ __forceinline__ double block_max(double* red, double v) {
 #pragma unroll
     for (int off = 16; off >= 1; off >>= 1) {
@@ -158,7 +180,7 @@ __device__ __forceinline__ double block_max(double* red, double v) {
     __syncthreads();
     double r = red[0];
 #pragma unroll
-    for (int w = 1; w < kChemThreads / 32; ++w) r = dmaxr(r, red[w]);
+    for (int w = 1; w < NT / 32; ++w) r = dmaxr(r, red[w]);
     __syncthreads();
     return r;
 }
@@ -170,13 +192,16 @@ __device__ __forceinline__ double arrhenius(const double* p, double lnT, double 
 __device__ __forceinline__ int unpack_lo(int v) { return v & 0xffff; }
 __device__ __forceinline__ int unpack_hi(int v) { return (v >> 16) & 0xffff; }
 
-// Temperature-only part: NASA7 thermo, rate constants of non-falloff
-// reactions, 1/Kc (standard formulas or interpolation tables), and the
-// Arrhenius limits and log10 Fcent of falloff reactions. Ends with a barrier.
+// Temperature-only part: NASA7 thermo, rate constants x multipliers of
+// non-falloff reactions, 1/Kc (standard formulas or interpolation tables),
+// and the Arrhenius limits and log10 Fcent of falloff reactions. Also
+// h_k = RT h/RT. Ends with a barrier.
+template <int NT>
 __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem& w, double T, int use_tables) {
     const int t = threadIdx.x;
     const double lnT = em_log(T), rT = 1.0 / T;
-    for (int k = t; k < m.S; k += kChemThreads) {
+    const double RT = kGasConstant * T;
+    for (int k = t; k < m.S; k += NT) {
         const int r = (T <= m.tmid[k]) ? 0 : 1;
         const double* a = m.nasa + 14 * k + 7 * r;
         const double* h = m.hc + 10 * k + 5 * r;
@@ -188,9 +213,10 @@ __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem&
         w.cpR[k] = cp;
         w.hRT[k] = hr;
         w.gRT[k] = hr - sr;
+        w.hk[k] = hr * RT;  // updateThermo: h_k [J/kmol]
     }
     __syncthreads();
-    const double lnRTp = em_log((kGasConstant * T) / kOneAtm);
+    const double lnRTp = em_log(RT / kOneAtm);
     const bool in_table = use_tables && T >= m.Tmin && T <= m.Tmax;
     int n = 0;
     double dT = 0.0;
@@ -200,14 +226,14 @@ __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem&
         if (n > m.nT - 1) n = m.nT - 1;
         dT = T - static_cast<double>(n) * (m.Tmax - m.Tmin) / (m.nT - 1) - m.Tmin;
     }
-    for (int i = t; i < m.R; i += kChemThreads) {
+    for (int i = t; i < m.R; i += NT) {
         const int info = m.rinfo[i];
         const int ty = rinfo_type(info);
         double kf = 0.0;
         if (ty == RXN_ELEMENTARY || ty == RXN_THREE_BODY) {
             if (in_table) {
                 double2 e = m.kf_tab[size_t(n) * m.R + i];
-                kf = e.x + e.y * dT;
+                kf = fma(e.y, dT, e.x);
             } else {
                 kf = arrhenius(m.arr + 3 * i, lnT, rT);
             }
@@ -216,7 +242,7 @@ __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem&
         if (rinfo_rev(info)) {
             if (in_table) {
                 double2 e = m.kc_tab[size_t(n) * m.R + i];
-                rkc = e.x + e.y * dT;
+                rkc = fma(e.y, dT, e.x);
             } else {
                 const int4 st = m.stoich[i];
                 const int pr[4] = {unpack_lo(st.z), unpack_hi(st.z), unpack_lo(st.w), unpack_hi(st.w)};
@@ -231,17 +257,19 @@ __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem&
                 rkc = dminr(em_exp(fma(m.dn[i], lnRTp, dg)), kBigNumber);
             }
         }
-        w.kf[i] = kf;
+        w.kfm[i] = kf * m.mult[i];
         w.rkc[i] = rkc;
     }
-    for (int f = t; f < m.n_fo; f += kChemThreads) {
+    for (int f = t; f < m.n_fo; f += NT) {
         const int i = m.fo_rxn[f];
-        w.fo_kinf[f] = arrhenius(m.arr + 3 * i, lnT, rT);
+        const double kinf = arrhenius(m.arr + 3 * i, lnT, rT);
+        w.fo_kinf[f] = kinf;
+        w.fo_rkinf[f] = 1.0 / (kinf + kSmallNumber);
         w.fo_k0[f] = arrhenius(m.fo_arr + 3 * f, lnT, rT);
         double lfc = 0.0;
         if (rinfo_type(m.rinfo[i]) == RXN_TROE) {
             const double* tp = m.fo_troe + 4 * f;
-            double fc = (1.0 - tp[0]) * em_exp(-T / tp[1]) + tp[0] * em_exp(-T / tp[2]);
+            double fc = fma(1.0 - tp[0], em_exp(-T * tp[1]), tp[0] * em_exp(-T * tp[2]));
             if (tp[3] != 0.0) fc = fc + em_exp(-tp[3] * rT);
             lfc = em_log10(dmaxr(fc, kSmallNumber));
         }
@@ -254,56 +282,62 @@ __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem&
 // progress, production rates and thermo outputs at (T, Y). Rate constants
 // must be current for T (chem_rate_constants). Y is in shared memory.
 // Returns rho and cp_mass on every thread. Ends with a barrier.
+template <int NT>
 __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, double p, int mode, double T,
                                            const double* Y, double& rho_out, double& cp_out, bool want_net) {
     const int S = m.S;
     const int t = threadIdx.x;
     if (mode == STATE_NORMALIZED) {
         double part = 0.0;
-        for (int k = t; k < S; k += kChemThreads) part = part + dmaxr(Y[k], 0.0);
-        const double rnorm = 1.0 / block_sum(w.red, part);
-        for (int k = t; k < S; k += kChemThreads) w.ym[k] = (dmaxr(Y[k], 0.0) * rnorm) * m.rW[k];
+        for (int k = t; k < S; k += NT) part = part + dmaxr(Y[k], 0.0);
+        const double rnorm = 1.0 / block_sum<NT>(w.red, part);
+        for (int k = t; k < S; k += NT) w.ym[k] = (dmaxr(Y[k], 0.0) * rnorm) * m.rW[k];
     } else {
-        for (int k = t; k < S; k += kChemThreads) w.ym[k] = Y[k] * m.rW[k];
+        for (int k = t; k < S; k += NT) w.ym[k] = Y[k] * m.rW[k];
     }
     double part = 0.0;
-    for (int k = t; k < S; k += kChemThreads) part = part + w.ym[k];
-    const double mmw = 1.0 / block_sum(w.red, part);
+    for (int k = t; k < S; k += NT) part = part + w.ym[k];
+    const double mmw = 1.0 / block_sum<NT>(w.red, part);
     const double rho = (p * mmw) / (kGasConstant * T);
-    for (int k = t; k < S; k += kChemThreads) w.c[k] = w.ym[k] * rho;
+    double cpart = 0.0;
+    for (int k = t; k < S; k += NT) {
+        const double ymk = w.ym[k];
+        w.c[k] = ymk * rho;
+        cpart = fma(ymk * mmw, w.cpR[k], cpart);
+    }
     __syncthreads();
     const double ctot = rho / mmw;
     // [M] of third-body and falloff reactions
-    for (int s = t; s < m.n_tb; s += kChemThreads) {
-        const double de = m.tb_def[s];
-        double concm = de * ctot;
-        for (int e = m.tb_off[s]; e < m.tb_off[s + 1]; ++e) concm = fma(m.tb_eff[e], w.c[m.tb_sp[e]], concm);
+    for (int s = t; s < m.n_tb; s += NT) {
+        double concm = m.tb_def[s] * ctot;
+        const int e1 = m.tb_off[s + 1];
+        for (int e = m.tb_off[s]; e < e1; ++e) concm = fma(m.tb_eff[e], w.c[m.tb_sp[e]], concm);
         w.concm[s] = concm;
     }
     __syncthreads();
     // falloff blending: k = kinf * Pr/(1+Pr) * F
-    for (int f = t; f < m.n_fo; f += kChemThreads) {
+    for (int f = t; f < m.n_fo; f += NT) {
         const int i = m.fo_rxn[f];
         const double kinf = w.fo_kinf[f];
-        const double pr = (w.concm[m.fo_tb[f]] * w.fo_k0[f]) / (kinf + kSmallNumber);
+        const double pr = (w.concm[m.fo_tb[f]] * w.fo_k0[f]) * w.fo_rkinf[f];
         double F = 1.0;
         if (rinfo_type(m.rinfo[i]) == RXN_TROE) {
             const double lfc = w.fo_lfc[f];
             const double lpr = em_log10(dmaxr(pr, kSmallNumber));
-            const double cc = -0.4 - 0.67 * lfc;
-            const double nn = 0.75 - 1.27 * lfc;
+            const double cc = fma(-0.67, lfc, -0.4);
+            const double nn = fma(-1.27, lfc, 0.75);
             const double x = lpr + cc;
-            const double f1 = x / (nn - 0.14 * x);
-            F = em_exp10(lfc / (1.0 + f1 * f1));
+            const double f1 = x / fma(-0.14, x, nn);
+            F = em_exp10(lfc / fma(f1, f1, 1.0));
         }
-        w.kf[i] = (pr * (F / (1.0 + pr))) * kinf;
+        w.kfm[i] = ((pr * (F / (1.0 + pr))) * kinf) * m.mult[i];
     }
     __syncthreads();
     // rates of progress
-    for (int i = t; i < m.R; i += kChemThreads) {
+    for (int i = t; i < m.R; i += NT) {
         const int info = m.rinfo[i];
         const int4 st = m.stoich[i];
-        double rf = w.kf[i] * m.mult[i];
+        double rf = w.kfm[i];
         if (rinfo_type(info) == RXN_THREE_BODY) rf = rf * w.concm[rinfo_tbslot(info)];
         double ropf = rf;
         const int r0 = unpack_lo(st.x), r1 = unpack_hi(st.x), r2 = unpack_lo(st.y), r3 = unpack_hi(st.y);
@@ -324,9 +358,7 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
         w.ropr[i] = ropr;
     }
     __syncthreads();
-    const double RT = kGasConstant * T;
-    double cpart = 0.0;
-    for (int k = t; k < S; k += kChemThreads) {
+    for (int k = t; k < S; k += NT) {
         double q = 0.0, d = 0.0, nt = 0.0;
         const int e1 = m.sp_off[k + 1];
         for (int e = m.sp_off[k]; e < e1; ++e) {
@@ -357,11 +389,9 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
         }
         w.wq[k] = q;
         w.wd[k] = d;
-        w.wn[k] = nt;
-        w.hk[k] = w.hRT[k] * RT;  // updateThermo: h_k [J/kmol]
-        cpart = cpart + (w.ym[k] * mmw) * w.cpR[k];
+        if (want_net) w.wn[k] = nt;
     }
-    cp_out = (kGasConstant * block_sum(w.red, cpart)) / mmw;
+    cp_out = (kGasConstant * block_sum<NT>(w.red, cpart)) / mmw;
     rho_out = rho;
 }
 

@@ -1,11 +1,18 @@
 // CTA-per-point QSS integrator: the CHEMEQ2-style predictor-corrector of
 // QssIntegrator (src/qssintegrator.cpp:58-265), with the state vectors of one
-// point in shared memory (element i on thread i mod kChemThreads) and every
-// scalar of the step control replicated across the CTA. Generic over the
-// right-hand side (QssOde::odefun, src/qssintegrator.h:6-21): `Ode` provides
+// point in shared memory (element i on thread i mod NT) and every scalar of
+// the step control replicated across the CTA. Generic over the right-hand
+// side (QssOde::odefun, src/qssintegrator.h:6-21): `Ode` provides
 //     __device__ void eval(double t, const double* y, double* q, double* d, bool corrector)
 // called by all threads with y, q, d in shared memory; it must end with a
 // barrier.
+//
+// Arithmetic forms (identical in the CPU oracle): the Pade factors are
+// evaluated in Horner form with fma, and the predictor and corrector updates
+// are each written over a single division,
+//     predictor:  (q - d) den / (den + num),  num/den = r(180+r(60+r(11+r))) / (360+r(60+r(12+r)))
+//     corrector:  (qs (ad - an) + q an - ys rb ad / dt) / (ad + an rb),  alpha = an/ad
+// which are the reference's expressions multiplied through by den (resp. ad).
 #pragma once
 
 #include "chem.cuh"
@@ -18,11 +25,12 @@ struct QssParams {
     int max_steps;
 };
 
-// Shared-memory vectors of one point (n entries each).
+// Shared-memory vectors of one point (n entries each; ym1/ym2 only with the
+// stability check).
 struct QssSmem {
-    double *y, *q, *d, *rtau, *rtaus, *y1, *ys, *qs, *ym1, *ym2, *scratch, *ymin;
-    static __host__ __device__ size_t doubles(int n) { return size_t(12) * n; }
-    __device__ void carve(double* base, int n) {
+    double *y, *q, *d, *rtau, *rtaus, *y1, *ys, *qs, *scratch, *ym1, *ym2;
+    static __host__ __device__ size_t doubles(int n, bool stab) { return size_t(stab ? 11 : 9) * n; }
+    __device__ void carve(double* base, int n, bool stab) {
         y = base;
         q = y + n;
         d = q + n;
@@ -31,10 +39,9 @@ struct QssSmem {
         y1 = rtaus + n;
         ys = y1 + n;
         qs = ys + n;
-        ym1 = qs + n;
-        ym2 = ym1 + n;
-        scratch = ym2 + n;
-        ymin = scratch + n;
+        scratch = qs + n;
+        ym1 = stab ? scratch + n : nullptr;
+        ym2 = stab ? ym1 + n : nullptr;
     }
 };
 
@@ -44,28 +51,34 @@ struct QssStats {
 
 __device__ __forceinline__ double rsign(double x) { return (x > 0) ? 1.0 : (x < 0) ? -1.0 : 0.0; }
 
-// enforce(i): whether component i is limited to ymin (QssIntegrator::enforce_ymin).
-// red: block reduction scratch (kChemThreads + 2 doubles).
-template <class Ode, class Enforce>
-__device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, const QssParams& P, Enforce enforce, double tf,
-                                   double tstart, double* red, QssStats& st) {
+// Pade numerator / denominator of the QSS predictor and corrector.
+__device__ __forceinline__ double pade_num(double r) { return r * fma(r, fma(r, 11.0 + r, 60.0), 180.0); }
+__device__ __forceinline__ double pade_den(double r) { return fma(r, fma(r, 12.0 + r, 60.0), 360.0); }
+__device__ __forceinline__ double pade_an(double r) { return fma(r, fma(r, 11.0 + r, 60.0), 180.0); }
+
+// enforce(i): whether component i is limited to ymin(i) (QssIntegrator::enforce_ymin / ymin).
+// red: block reduction scratch (kMaxChemThreads + 2 doubles).
+template <int NT, class Ode, class Enforce, class Ymin>
+__device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, const QssParams& P, Enforce enforce,
+                                                   Ymin ymin, double tf, double tstart, double* red, QssStats& st) {
     const int t0 = threadIdx.x;
-    constexpr int NT = kChemThreads;
     const double tfd = 1.000008;
+    const bool stab_on = P.stability_check != 0;
     // setState: y limited to ymin where enforced; q, d zeroed (initialize()).
     for (int i = t0; i < n; i += NT) {
-        v.y[i] = enforce(i) ? dmaxr(v.y[i], v.ymin[i]) : v.y[i];
+        v.y[i] = enforce(i) ? dmaxr(v.y[i], ymin(i)) : v.y[i];
         v.q[i] = 0.0;
         v.d[i] = 0.0;
-        v.ym1[i] = 0.0;
-        v.ym2[i] = 0.0;
+        if (stab_on) {
+            v.ym1[i] = 0.0;
+            v.ym2[i] = 0.0;
+        }
     }
     __syncthreads();
     double tn = 0.0, ts = 0.0, dt = 0.0;
     bool first = true;
     int gcount = 0, rcount = 0, steps = 0;
     int ret = 0;
-    const bool stab_on = P.stability_check != 0;
     while (tfd * tn < tf) {
         if (steps >= P.max_steps) {
             ret = -20;
@@ -86,7 +99,7 @@ __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, 
                     scrtch = dmaxr(dmaxr(scr1, -fabs(absq - v.d[i]) * scr2), scrtch);
                 }
             }
-            scrtch = block_max(red, scrtch);
+            scrtch = block_max<NT>(red, scrtch);
             const double sqreps = 0.5;
             dt = dminr(sqreps / scrtch, tf);
             dt = dminr(dt, P.dtmax);
@@ -101,10 +114,11 @@ __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, 
         }
         int step_ret = 1;  // 1: keep looping
         while (step_ret == 1) {
+            const double rdt = 1.0 / dt;
             for (int i = t0; i < n; i += NT) {
                 const double r = v.rtau[i];
-                v.scratch[i] = (v.q[i] - v.d[i]) /
-                               (1.0 + r * (180 + r * (60 + r * (11 + r))) / (360 + r * (60 + r * (12 + r))));
+                const double den = pade_den(r);
+                v.scratch[i] = ((v.q[i] - v.d[i]) * den) / (den + pade_num(r));
             }
             double eps = 1e-10;
             for (int iter = 0; iter < P.itermax; ++iter) {
@@ -113,7 +127,7 @@ __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, 
                         v.ym2[i] = v.ym1[i];
                         v.ym1[i] = v.y[i];
                     }
-                    const double yi = dmaxr(v.ymin[i], v.ys[i] + dt * v.scratch[i]);
+                    const double yi = dmaxr(ymin(i), fma(dt, v.scratch[i], v.ys[i]));
                     v.y[i] = yi;
                     if (iter == 0) v.y1[i] = yi;
                 }
@@ -124,18 +138,21 @@ __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, 
                 eps = 1.0e-10;
                 for (int i = t0; i < n; i += NT) {
                     const double rb = enforce(i) ? 0.5 * (v.rtaus[i] + dt * v.d[i] / v.y[i]) : 0.0;
-                    const double alpha = (180. + rb * (60. + rb * (11. + rb))) / (360. + rb * (60. + rb * (12. + rb)));
-                    v.scratch[i] = (v.qs[i] * (1.0 - alpha) + v.q[i] * alpha - v.ys[i] * rb / dt) / (1.0 + alpha * rb);
+                    const double an = pade_an(rb);
+                    const double ad = pade_den(rb);
+                    const double num = fma(v.qs[i], ad - an, v.q[i] * an) - ((v.ys[i] * rb) * ad) * rdt;
+                    v.scratch[i] = num / fma(an, rb, ad);
                 }
             }
             double epsl = eps;
             for (int i = t0; i < n; i += NT) {
-                double scr2 = v.ys[i] + dt * v.scratch[i];
-                if (enforce(i)) scr2 = dmaxr(scr2, v.ymin[i]);
+                const double ym = ymin(i);
+                double scr2 = fma(dt, v.scratch[i], v.ys[i]);
+                if (enforce(i)) scr2 = dmaxr(scr2, ym);
                 double scr1 = fabs(scr2 - v.y1[i]);
-                const double yi = dmaxr(scr2, v.ymin[i]);
+                const double yi = dmaxr(scr2, ym);
                 v.y[i] = yi;
-                if (fabs(yi) > P.abstol && 0.25 * (v.ys[i] + yi) > v.ymin[i]) {
+                if (fabs(yi) > P.abstol && 0.25 * (v.ys[i] + yi) > ym) {
                     scr1 = scr1 / yi;
                     epsl = dmaxr(.5 * (scr1 + dminr(fabs(v.q[i] - v.d[i]) / (v.q[i] + v.d[i] + 1e-30), scr1)), epsl);
                 }
@@ -144,7 +161,7 @@ __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, 
                     v.ym1[i] = yi;
                 }
             }
-            eps = block_max(red, epsl);  // includes a barrier: y is complete
+            eps = block_max<NT>(red, epsl);  // includes a barrier: y is complete
             eps /= P.epsmin;
             if (dt <= P.dtmin + 1e-16 * tn) {
                 step_ret = -1;
@@ -157,7 +174,7 @@ __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, 
                 for (int i = t0; i < n; i += NT)
                     if (fabs(v.y[i]) > P.abstol)
                         sl = dmaxr(sl, fabs(v.y[i] - v.ym1[i]) / (fabs(v.ym1[i] - v.ym2[i]) + 1e-20 * v.y[i]));
-                stab = block_max(red, sl);
+                stab = block_max<NT>(red, sl);
             }
             if (eps <= P.epsmax && stab <= 1.0) {
                 if (tf <= tn * tfd) {
@@ -176,7 +193,8 @@ __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, 
             if (stab_on) dt = dminr(dt, dto / (stab + .001));
             if (eps > P.epsmax || stab > 1) {
                 rcount += 1;
-                for (int i = t0; i < n; i += NT) v.rtaus[i] *= dt / dto;
+                const double ratio = dt / dto;
+                for (int i = t0; i < n; i += NT) v.rtaus[i] *= ratio;
             } else {
                 step_ret = 0;
             }

@@ -24,17 +24,21 @@ namespace ember {
 // Rate constants and 1/Kc at the table nodes (one CTA per node), from the
 // same device functions as the standard model: InterpKinetics::updateROP /
 // MultiArrheniusInterp::rebuildInterpData (src/chemistry0d.cpp:278-326, 401-436).
-__global__ void __launch_bounds__(kChemThreads) k_build_tables(MechView m, double* work) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_build_tables(MechView m, double* work) {
     const int node = blockIdx.x;
+    const size_t sd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, false);
+    double* base = work + size_t(node) * (sd + ChemSmem::global_doubles(m.R));
     ChemSmem w;
-    w.carve(work + size_t(node) * ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo), m);
+    w.carve(base, base + sd, m, false);
     const double T = m.Tmin + ((double)node) / (m.nT - 1) * (m.Tmax - m.Tmin);
-    chem_rate_constants(m, w, T, 0);
+    chem_rate_constants<NT>(m, w, T, 0);
     double2* kf = const_cast<double2*>(m.kf_tab) + size_t(node) * m.R;
     double2* kc = const_cast<double2*>(m.kc_tab) + size_t(node) * m.R;
-    for (int i = threadIdx.x; i < m.R; i += kChemThreads) {
+    for (int i = threadIdx.x; i < m.R; i += NT) {
         const int ty = rinfo_type(m.rinfo[i]);
-        kf[i].x = (ty == RXN_ELEMENTARY || ty == RXN_THREE_BODY) ? w.kf[i] : 0.0;
+        // w.kfm holds kf * multiplier; the multipliers are 1 while tables are built
+        kf[i].x = (ty == RXN_ELEMENTARY || ty == RXN_THREE_BODY) ? w.kfm[i] : 0.0;
         kc[i].x = w.rkc[i];
     }
 }
@@ -58,21 +62,22 @@ __global__ void k_table_slopes(MechView m) {
 
 // ------------------------------------------------------------- gas eval --
 
-__global__ void __launch_bounds__(kChemThreads) k_gas_eval(MechView m, int n, double p, int model, int mode,
-                                                          const double* __restrict__ T, const double* __restrict__ Y,
-                                                          double* creation, double* destruction, double* net,
-                                                          double* hk, double* cp_mass, double* density) {
+template <int NT>
+__global__ void __launch_bounds__(NT) k_gas_eval(MechView m, int n, double p, int model, int mode,
+                                                const double* __restrict__ T, const double* __restrict__ Y,
+                                                double* kcache, double* creation, double* destruction, double* net,
+                                                double* hk, double* cp_mass, double* density) {
     extern __shared__ double smem[];
     ChemSmem w;
-    w.carve(smem, m);
-    double* y = smem + ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo);
+    w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), m, true);
+    double* y = smem + ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true);
     for (int j = blockIdx.x; j < n; j += gridDim.x) {
-        for (int k = threadIdx.x; k < m.S; k += kChemThreads) y[k] = Y[size_t(j) * m.S + k];
+        for (int k = threadIdx.x; k < m.S; k += NT) y[k] = Y[size_t(j) * m.S + k];
         const double Tj = T[j];
-        chem_rate_constants(m, w, Tj, model == KIN_INTERP);  // begins with a barrier-free pass, ends with one
+        chem_rate_constants<NT>(m, w, Tj, model == KIN_INTERP);
         double rho, cp;
-        chem_rates(m, w, p, mode, Tj, y, rho, cp, true);
-        for (int k = threadIdx.x; k < m.S; k += kChemThreads) {
+        chem_rates<NT>(m, w, p, mode, Tj, y, rho, cp, true);
+        for (int k = threadIdx.x; k < m.S; k += NT) {
             const size_t o = size_t(j) * m.S + k;
             if (creation) creation[o] = w.wq[k];
             if (destruction) destruction[o] = w.wd[k];
@@ -91,51 +96,48 @@ __global__ void __launch_bounds__(kChemThreads) k_gas_eval(MechView m, int n, do
 
 // SourceSystemQSS::odefun (src/sourceSystem.cpp:445-499): q/d of
 // [U, T, Y]; T and the thermo (h_k, rho, cp) are refreshed only on
-// predictor calls (src/sourceSystem.cpp:461-463, 501-515).
+// predictor calls (src/sourceSystem.cpp:461-463, 501-515). With T frozen in
+// the corrector, h_k (a function of T only) is the predictor's.
+template <int NT>
 struct SourceQssOde {
     MechView m;
     ChemSmem w;
-    double pressure;
-    int kinetics_model;
     const SourceArgs* a;
     const double* split;  // this point's split constants (global) or null
     double x;
     double T;
-    double rho, cp;
+    double rrho, rrc;     // 1/rho and 1/(rho cp) of the last predictor call
     double cachedT;
-    double* hk_pred;      // [S] in shared memory
 
     __device__ void eval(double t, const double* y, double* q, double* d, bool corrector) {
         const int S = m.S;
         const int tid = threadIdx.x;
         if (!corrector) T = y[1];
         if (!(cachedT == T)) {
-            chem_rate_constants(m, w, T, kinetics_model == KIN_INTERP);
+            chem_rate_constants<NT>(m, w, T, a->kinetics_model == KIN_INTERP);
             cachedT = T;
         }
         double rho_c, cp_c;
-        chem_rates(m, w, pressure, STATE_NORMALIZED, T, y + 2, rho_c, cp_c, false);
+        chem_rates<NT>(m, w, a->pressure, STATE_NORMALIZED, T, y + 2, rho_c, cp_c, false);
         if (!corrector) {
-            for (int k = tid; k < S; k += kChemThreads) hk_pred[k] = w.hk[k];
-            rho = rho_c;
-            cp = cp_c;
+            rrho = 1.0 / rho_c;
+            rrc = 1.0 / (rho_c * cp_c);
         }
         double part = 0.0;
-        for (int k = tid; k < S; k += kChemThreads) part = part + (w.wq[k] - w.wd[k]) * hk_pred[k];
-        const double qdot = -block_sum(w.red, part) + igniter(*a, t, x);
-        const double rc = rho * cp;
-        for (int i = tid; i < S + 2; i += kChemThreads) {
+        for (int k = tid; k < S; k += NT) part = fma(w.wq[k] - w.wd[k], w.hk[k], part);
+        const double qdot = -block_sum<NT>(w.red, part) + igniter(*a, t, x);
+        for (int i = tid; i < S + 2; i += NT) {
             const double sc = split ? split[i] : 0.0;
             if (i == 0) {
                 q[0] = sc;
                 d[0] = 0.0;
             } else if (i == 1) {
-                q[1] = qdot / rc + sc;
-                d[1] = 0.0 / rc;
+                q[1] = fma(qdot, rrc, sc);
+                d[1] = 0.0 * rrc;
             } else {
                 const int k = i - 2;
-                q[i] = (w.wq[k] * m.W[k]) / rho + sc;
-                d[i] = (w.wd[k] * m.W[k]) / rho;
+                q[i] = fma(w.wq[k] * m.W[k], rrho, sc);
+                d[i] = (w.wd[k] * m.W[k]) * rrho;
             }
         }
         __syncthreads();
@@ -146,19 +148,62 @@ struct EnforceNotMomentum {
     __device__ bool operator()(int i) const { return i != 0; }
 };
 
-__global__ void __launch_bounds__(kChemThreads) k_source_qss(MechView m, SourceArgs a, int* counter) {
+struct SourceYmin {
+    double minval;
+    __device__ double operator()(int i) const { return i == 0 ? -1e4 : minval; }
+};
+
+// ---- longest-first work order ----------------------------------------------
+// A point's cost grows with its interval (at least dt/dtmax steps), so the
+// work queue hands out points by decreasing dt, bucketed by the binary
+// exponent of dt (bucket 0: dt >= 32 s; each bucket spans a factor 2). The
+// results do not depend on the order: every point is integrated on its own.
+
+__device__ __forceinline__ int dt_bucket(double dt) {
+    if (!(dt > 0.0)) return 63;
+    const int e = static_cast<int>((__double_as_longlong(dt) >> 52) & 0x7ff);
+    const int b = 1023 + 5 - e;
+    return b < 0 ? 0 : (b > 63 ? 63 : b);
+}
+
+__global__ void k_order_hist(const double* __restrict__ dt, int n, int* counts) {
+    __shared__ int local[64];
+    if (threadIdx.x < 64) local[threadIdx.x] = 0;
+    __syncthreads();
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        atomicAdd(&local[dt_bucket(dt[j])], 1);
+    __syncthreads();
+    if (threadIdx.x < 64 && local[threadIdx.x]) atomicAdd(&counts[threadIdx.x], local[threadIdx.x]);
+}
+
+__global__ void k_order_scan(int* counts) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        int acc = 0;
+        for (int b = 0; b < 64; ++b) {
+            const int c = counts[b];
+            counts[b] = acc;  // becomes the bucket's cursor
+            acc += c;
+        }
+    }
+}
+
+__global__ void k_order_scatter(const double* __restrict__ dt, int n, int* cursor, int* order) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        order[atomicAdd(&cursor[dt_bucket(dt[j])], 1)] = j;
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT) k_source_qss(MechView m, SourceArgs a, int* counter, const int* order, double* kcache) {
     extern __shared__ double smem[];
     __shared__ int next_point;
     const int n = m.S + 2;
-    const size_t cd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo);
-    SourceQssOde ode;
+    const bool stab = a.qss_stability_check != 0;
+    const size_t cd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, false);
+    SourceQssOde<NT> ode;
     ode.m = m;
-    ode.w.carve(smem, m);
+    ode.w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), m, false);
     QssSmem v;
-    v.carve(smem + cd, n);
-    ode.hk_pred = smem + cd + QssSmem::doubles(n);
-    ode.pressure = a.pressure;
-    ode.kinetics_model = a.kinetics_model;
+    v.carve(smem + cd, n, stab);
     ode.a = &a;
     ode.cachedT = __longlong_as_double(0x7ff8000000000000LL);  // NaN: nothing cached
     QssParams P;
@@ -172,26 +217,27 @@ __global__ void __launch_bounds__(kChemThreads) k_source_qss(MechView m, SourceA
     P.max_steps = a.max_steps;
     const int tid = threadIdx.x;
     for (;;) {
-        if (tid == 0) next_point = atomicAdd(counter, 1);
+        if (tid == 0) {
+            const int slot = atomicAdd(counter, 1);
+            next_point = slot < a.n ? order[slot] : a.n;
+        }
         __syncthreads();
         const int j = next_point;
         __syncthreads();
         if (j >= a.n) break;
         const double* yin = a.state_in + size_t(j) * n;
-        for (int i = tid; i < n; i += kChemThreads) {
-            v.y[i] = yin[i];
-            v.ymin[i] = (i == 0) ? -1e4 : a.qss_minval;
-        }
+        for (int i = tid; i < n; i += NT) v.y[i] = yin[i];
         ode.split = a.split ? a.split + size_t(j) * n : nullptr;
         ode.x = a.x ? a.x[j] : 0.0;
         ode.T = yin[1];
-        ode.rho = 1.0;
-        ode.cp = 1.0;
+        ode.rrho = 1.0;
+        ode.rrc = 1.0;
         QssStats st;
-        int ret = qss_integrate_block(ode, v, n, P, EnforceNotMomentum(), a.dt[j], a.t_start, ode.w.red, st);
+        int ret = qss_integrate_block<NT>(ode, v, n, P, EnforceNotMomentum(), SourceYmin{a.qss_minval}, a.dt[j],
+                                          a.t_start, ode.w.red, st);
         int nonfinite = 0;
         double* yout = a.state_out + size_t(j) * n;
-        for (int i = tid; i < n; i += kChemThreads) {
+        for (int i = tid; i < n; i += NT) {
             const double yi = v.y[i];
             nonfinite |= !isfinite(yi);
             yout[i] = yi;
@@ -305,7 +351,11 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
             fo_rxn.push_back(i);
             fo_tb.push_back(slot);
             for (int q = 0; q < 3; ++q) fo_arr.push_back(d->arrhenius_low[3 * i + q]);
-            for (int q = 0; q < 4; ++q) fo_troe.push_back(d->troe[4 * i + q]);
+            // a, 1/T3, 1/T1, T2 (reciprocals as Cantera's Troe rate keeps them)
+            fo_troe.push_back(d->troe[4 * i + 0]);
+            fo_troe.push_back(1.0 / d->troe[4 * i + 1]);
+            fo_troe.push_back(1.0 / d->troe[4 * i + 2]);
+            fo_troe.push_back(d->troe[4 * i + 3]);
         }
         rinfo[i] = ty | ((d->reversible[i] ? 1 : 0) << 2) | (nr << 3) | (np << 6) | (slot << 9);
         // per-species participation: (product count, reactant count)
@@ -403,9 +453,15 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
     }
     if (e == cudaSuccess && R) {
         double* work = nullptr;
-        e = cudaMalloc(&work, sizeof(double) * ChemSmem::doubles(S, R, n_tb, n_fo) * nT);
+        e = cudaMalloc(&work, sizeof(double) * (ChemSmem::doubles(S, R, n_tb, n_fo, false) +
+                                                 ChemSmem::global_doubles(R)) * nT);
         if (e == cudaSuccess) {
-            k_build_tables<<<nT, kChemThreads>>>(v, work);
+            switch (chem_threads_for(S)) {
+                case 64: k_build_tables<64><<<nT, 64>>>(v, work); break;
+                case 128: k_build_tables<128><<<nT, 128>>>(v, work); break;
+                case 160: k_build_tables<160><<<nT, 160>>>(v, work); break;
+                default: k_build_tables<256><<<nT, 256>>>(v, work); break;
+            }
             k_table_slopes<<<std::min<int64_t>((int64_t(nT) * R + 255) / 256, 4096), 256>>>(v);
             e = cudaDeviceSynchronize();
             cudaFree(work);
@@ -474,11 +530,25 @@ extern "C" int ember_gas_eval(ember_mech m, int n, double pressure, int model, i
     EMBER_TRY(stage_buffer(sc, cp_mass, n, mem, &c5));
     EMBER_TRY(stage_buffer(sc, density, n, mem, &c6));
     const MechView& v = m->view;
-    const size_t per = (ChemSmem::doubles(S, m->R, v.n_tb, v.n_fo) + S) * sizeof(double);
+    const int NTh = chem_threads_for(S);
+    const size_t per = (ChemSmem::doubles(S, m->R, v.n_tb, v.n_fo, true) + S) * sizeof(double);
     EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the shared-memory work area (%zu B)", per);
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_gas_eval, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
-    const int blocks = std::min(n, 65535);
-    k_gas_eval<<<blocks, kChemThreads, per, st>>>(v, n, pressure, model, mode, dT, dY, c1, c2, c3, c4, c5, c6);
+    int dev = 0, sms = 0;
+    EMBER_CUDA_TRY(cudaGetDevice(&dev));
+    EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int blocks = std::min(n, sms * 4);
+    double* kcache = nullptr;
+    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m->R)));
+#define EMBER_GAS_EVAL(NTV)                                                                                  \
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_gas_eval<NTV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per))); \
+    k_gas_eval<NTV><<<blocks, NTV, per, st>>>(v, n, pressure, model, mode, dT, dY, kcache, c1, c2, c3, c4, c5, c6)
+    switch (NTh) {
+        case 64: EMBER_GAS_EVAL(64); break;
+        case 128: EMBER_GAS_EVAL(128); break;
+        case 160: EMBER_GAS_EVAL(160); break;
+        default: EMBER_GAS_EVAL(256); break;
+    }
+#undef EMBER_GAS_EVAL
     EMBER_TRY(stage_out(creation, c1, size_t(n) * S, mem, st));
     EMBER_TRY(stage_out(destruction, c2, size_t(n) * S, mem, st));
     EMBER_TRY(stage_out(net, c3, size_t(n) * S, mem, st));
@@ -568,19 +638,47 @@ SourceArgs make_source_args(const ember_source_options* o, int n, const double* 
     return a;
 }
 
-int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, cudaStream_t st) {
-    const size_t per = qss_smem_doubles(m) * sizeof(double);
+// Longest-first processing order of the points (see k_order_hist).
+int make_work_order(const SourceArgs& a, Scratch& sc, cudaStream_t st, int** order_out) {
+    int *counts = nullptr, *order = nullptr;
+    EMBER_TRY(sc.alloc(&counts, 64));
+    EMBER_TRY(sc.alloc(&order, a.n));
+    EMBER_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int) * 64, st));
+    const int blocks = std::min(blocks_for(a.n, 256), 1024);
+    k_order_hist<<<blocks, 256, 0, st>>>(a.dt, a.n, counts);
+    k_order_scan<<<1, 32, 0, st>>>(counts);
+    k_order_scatter<<<blocks, 256, 0, st>>>(a.dt, a.n, counts, order);
+    *order_out = order;
+    return EMBER_OK;
+}
+
+template <int NT>
+static int launch_qss_nt(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
+    const size_t per = qss_smem_doubles(m, a.qss_stability_check != 0) * sizeof(double);
     EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the QSS shared-memory work area (%zu B)", per);
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_qss, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_qss<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
     int dev = 0, sms = 0, per_sm = 0;
     EMBER_CUDA_TRY(cudaGetDevice(&dev));
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    EMBER_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_source_qss, kChemThreads, per));
+    EMBER_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_source_qss<NT>, NT, per));
     per_sm = std::max(per_sm, 1);
     const int blocks = std::max(1, std::min(a.n, sms * per_sm));
-    k_source_qss<<<blocks, kChemThreads, per, st>>>(m, a, counter);
+    double* kcache = nullptr;
+    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
+    int* order = nullptr;
+    EMBER_TRY(make_work_order(a, sc, st, &order));
+    k_source_qss<NT><<<blocks, NT, per, st>>>(m, a, counter, order, kcache);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
+}
+
+int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
+    switch (chem_threads_for(m.S)) {
+        case 64: return launch_qss_nt<64>(m, a, counter, sc, st);
+        case 128: return launch_qss_nt<128>(m, a, counter, sc, st);
+        case 160: return launch_qss_nt<160>(m, a, counter, sc, st);
+        default: return launch_qss_nt<256>(m, a, counter, sc, st);
+    }
 }
 
 }  // namespace ember
@@ -615,9 +713,9 @@ extern "C" int ember_source_integrate(ember_mech m, int method, int n, const dou
     EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
     SourceArgs a = make_source_args(opts, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, d_stats);
     if (method == EMBER_SOURCE_QSS) {
-        EMBER_TRY(launch_source_qss(m->view, a, counter, st));
+        EMBER_TRY(launch_source_qss(m->view, a, counter, sc, st));
     } else {
-        EMBER_TRY(launch_source_bdf(m->view, a, counter, st));
+        EMBER_TRY(launch_source_bdf(m->view, a, counter, sc, st));
     }
     EMBER_TRY(stage_out(state_out, d_out, size_t(n) * nv, mem, st));
     EMBER_TRY(stage_out(status, d_status, n, mem, st));
@@ -672,19 +770,20 @@ struct EnforceAll {
     __device__ bool operator()(int) const { return true; }
 };
 
-__global__ void __launch_bounds__(kChemThreads) k_qss_cesium(QssParams P, double* y7, double tf, int* stats, int* ret) {
-    __shared__ double buf[12 * 7];
-    __shared__ double red[kChemThreads + 2];
+struct CesiumYmin {
+    __device__ double operator()(int) const { return 1e-20; }
+};
+
+__global__ void __launch_bounds__(64) k_qss_cesium(QssParams P, double* y7, double tf, int* stats, int* ret) {
+    __shared__ double buf[11 * 7];
+    __shared__ double red[kMaxChemThreads + 2];
     QssSmem v;
-    v.carve(buf, 7);
-    for (int i = threadIdx.x; i < 7; i += kChemThreads) {
-        v.y[i] = y7[i];
-        v.ymin[i] = 1e-20;
-    }
+    v.carve(buf, 7, P.stability_check != 0);
+    for (int i = threadIdx.x; i < 7; i += 64) v.y[i] = y7[i];
     __syncthreads();
     CesiumOde ode;
     QssStats st;
-    int r = qss_integrate_block(ode, v, 7, P, EnforceAll(), tf, 0.0, red, st);
+    int r = qss_integrate_block<64>(ode, v, 7, P, EnforceAll(), CesiumYmin(), tf, 0.0, red, st);
     if (threadIdx.x == 0) {
         for (int i = 0; i < 7; ++i) y7[i] = v.y[i];
         y7[6] = y7[1] - y7[0];
@@ -711,7 +810,7 @@ extern "C" int ember_selftest_qss_cesium(double epsmin, double epsmax, double dt
     cudaError_t e = cudaMalloc(&di, sizeof(int) * 5);
     if (e == cudaSuccess) e = cudaMemcpy(dy, y7, sizeof(double) * 7, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
-        k_qss_cesium<<<1, kChemThreads>>>(P, dy, tf, di, di + 4);
+        k_qss_cesium<<<1, 64>>>(P, dy, tf, di, di + 4);
         e = cudaGetLastError();
     }
     int ret = 0;

@@ -40,13 +40,14 @@ __device__ __forceinline__ double igniter(const SourceArgs& a, double t, double 
     return 0.0;
 }
 
-// Shared memory (doubles) of one QSS point: kinetics work area, QSS vectors,
-// predictor enthalpies.
-__host__ __device__ inline size_t qss_smem_doubles(const MechView& m) {
-    return ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo) + QssSmem::doubles(m.S + 2) + size_t(m.S);
+// Shared memory (doubles) of one QSS point: kinetics work area and QSS vectors.
+__host__ __device__ inline size_t qss_smem_doubles(const MechView& m, bool stab) {
+    return ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, false) + QssSmem::doubles(m.S + 2, stab);
 }
 
-int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, cudaStream_t st);
-int launch_source_bdf(const MechView& m, const SourceArgs& a, int* counter, cudaStream_t st);
+class Scratch;
+int make_work_order(const SourceArgs& a, Scratch& sc, cudaStream_t st, int** order_out);
+int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st);
+int launch_source_bdf(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st);
 
 }  // namespace ember

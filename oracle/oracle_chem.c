@@ -22,8 +22,9 @@
  * PARITY UNPINNED: the reference's tests hold no rates, equilibrium constants
  * or thermo values, and Cantera and its mechanism files are absent.
  *
- * Sums over species use one fixed order (see wsum), the order of the GPU
- * block reductions; the reference leaves this order to Eigen.
+ * Sums over species use one fixed order (see block_sum), the order of the
+ * GPU block reductions; the reference leaves this order to Eigen. Where the
+ * GPU code fuses a multiply-add, this file writes the same fma().
  */
 #include <math.h>
 #include <pthread.h>
@@ -117,15 +118,30 @@ static double oracle_exp10(double x) { return oracle_exp(x * 2.302585092994046);
 static double dmax(double a, double b) { return (a < b) ? b : a; } /* std::max */
 static double dmin(double a, double b) { return (b < a) ? b : a; } /* std::min */
 
-/* Sum in the fixed order of the GPU block reduction: element k goes to the
- * partial sum of thread k mod 128 (sequential in k); the 128 partials are
- * folded into 32 as ((p[l] + p[l+32]) + p[l+64]) + p[l+96] and combined by
- * an xor butterfly. */
-static double wsum(const double* x, int n) {
-    double p[128], q[32];
-    for (int l = 0; l < 128; ++l) p[l] = 0.0;
-    for (int k = 0; k < n; ++k) p[k & 127] += x[k];
-    for (int l = 0; l < 32; ++l) q[l] = ((p[l] + p[l + 32]) + p[l + 64]) + p[l + 96];
+/* Threads per grid point of the GPU kernels for S species (the state
+ * vector of S+2 values fits one pass): the width of the reduction order. */
+static int reduction_width(int S) {
+    const int n = S + 2;
+    if (n <= 64) return 64;
+    if (n <= 128) return 128;
+    if (n <= 160) return 160;
+    return 256;
+}
+
+/* Sum of a[k] (b == NULL) or of a[k] * b[k] accumulated by fma, in the fixed
+ * order of the GPU block reduction: element k goes to the partial sum of
+ * thread k mod W (sequential in k); the W partials are folded into 32 as
+ * p[l] + p[l+32] + p[l+64] + ... (in that order) and combined by an xor
+ * butterfly. */
+static double block_sum(const double* a, const double* b, int n, int W) {
+    double p[256], q[32];
+    for (int l = 0; l < W; ++l) p[l] = 0.0;
+    for (int k = 0; k < n; ++k) p[k % W] = b ? fma(a[k], b[k], p[k % W]) : p[k % W] + a[k];
+    for (int l = 0; l < 32; ++l) {
+        double v = p[l];
+        for (int w = 1; w < W / 32; ++w) v = v + p[l + 32 * w];
+        q[l] = v;
+    }
     for (int off = 16; off >= 1; off >>= 1) {
         double r[32];
         for (int l = 0; l < 32; ++l) r[l] = q[l] + q[l ^ off];
@@ -307,7 +323,7 @@ static double arrhenius(const double* p, double lnT, double rT) {
 void oracle_rate_constants(const oracle_mech* m, oracle_ws* w, double T, int use_tables) {
     thermo(m, w, T);
     const double lnT = oracle_log(T), rT = 1.0 / T;
-    const double lnRTp = oracle_log((GAS_CONSTANT * T) / ONE_ATM);
+    const double lnRTp = oracle_log((GAS_CONSTANT * T) / ONE_ATM);  /* RT / p0 */
     const int in_table = use_tables && T >= m->Tmin && T <= m->Tmax;
     size_t n = 0;
     double dT = 0.0;
@@ -320,7 +336,7 @@ void oracle_rate_constants(const oracle_mech* m, oracle_ws* w, double T, int use
         const int ty = m->type[i];
         if (ty == ORACLE_RXN_ELEMENTARY || ty == ORACLE_RXN_THREE_BODY) {
             if (in_table)
-                w->kf[i] = m->kf_c[(size_t)i * m->nT + n] + m->kf_s[(size_t)i * m->nT + n] * dT;
+                w->kf[i] = fma(m->kf_s[(size_t)i * m->nT + n], dT, m->kf_c[(size_t)i * m->nT + n]);
             else
                 w->kf[i] = arrhenius(m->arr + 3 * i, lnT, rT);
         } else {
@@ -329,7 +345,7 @@ void oracle_rate_constants(const oracle_mech* m, oracle_ws* w, double T, int use
         if (!m->rev[i]) {
             w->rkc[i] = 0.0;
         } else if (in_table) {
-            w->rkc[i] = m->kc_c[(size_t)i * m->nT + n] + m->kc_s[(size_t)i * m->nT + n] * dT;
+            w->rkc[i] = fma(m->kc_s[(size_t)i * m->nT + n], dT, m->kc_c[(size_t)i * m->nT + n]);
         } else {
             double dg = 0.0;
             for (int o = 0; o < ORACLE_MAX_STOICH; ++o) {
@@ -353,12 +369,12 @@ static void set_composition(const oracle_mech* m, oracle_ws* w, double p, double
     const int S = m->S;
     if (mode == ORACLE_STATE_NORMALIZED) {
         for (int k = 0; k < S; ++k) w->tmp[k] = dmax(Y[k], 0.0);
-        const double rnorm = 1.0 / wsum(w->tmp, S);
+        const double rnorm = 1.0 / block_sum(w->tmp, NULL, S, reduction_width(S));
         for (int k = 0; k < S; ++k) w->ym[k] = (w->tmp[k] * rnorm) * m->rW[k];
     } else {
         for (int k = 0; k < S; ++k) w->ym[k] = Y[k] * m->rW[k];
     }
-    const double mmw = 1.0 / wsum(w->ym, S);
+    const double mmw = 1.0 / block_sum(w->ym, NULL, S, reduction_width(S));
     const double rho = (p * mmw) / (GAS_CONSTANT * T);
     for (int k = 0; k < S; ++k) w->c[k] = w->ym[k] * rho;
     *rho_out = rho;
@@ -387,19 +403,20 @@ void oracle_rates(const oracle_mech* m, oracle_ws* w, double p, int model, int m
         if (ty == ORACLE_RXN_LINDEMANN || ty == ORACLE_RXN_TROE) {
             const double kinf = arrhenius(m->arr + 3 * i, lnT, rT);
             const double k0 = arrhenius(m->arr_low + 3 * i, lnT, rT);
-            const double pr = (concm * k0) / (kinf + SMALL_NUMBER);
+            const double pr = (concm * k0) * (1.0 / (kinf + SMALL_NUMBER));
             double F = 1.0;
             if (ty == ORACLE_RXN_TROE) {
                 const double* tp = m->troe + 4 * i;
-                double fc = (1.0 - tp[0]) * oracle_exp(-T / tp[1]) + tp[0] * oracle_exp(-T / tp[2]);
+                /* Fcent with the reciprocals 1/T3, 1/T1, as Cantera's Troe rate keeps them */
+                double fc = fma(1.0 - tp[0], oracle_exp(-T * (1.0 / tp[1])), tp[0] * oracle_exp(-T * (1.0 / tp[2])));
                 if (tp[3] != 0.0) fc += oracle_exp(-tp[3] * rT);
                 const double lfc = oracle_log10(dmax(fc, SMALL_NUMBER));
                 const double lpr = oracle_log10(dmax(pr, SMALL_NUMBER));
-                const double cc = -0.4 - 0.67 * lfc;
-                const double nn = 0.75 - 1.27 * lfc;
+                const double cc = fma(-0.67, lfc, -0.4);   /* -0.4 - 0.67 log Fcent */
+                const double nn = fma(-1.27, lfc, 0.75);   /* 0.75 - 1.27 log Fcent */
                 const double x = lpr + cc;
-                const double f1 = x / (nn - 0.14 * x);
-                F = oracle_exp10(lfc / (1.0 + f1 * f1));
+                const double f1 = x / fma(-0.14, x, nn);
+                F = oracle_exp10(lfc / fma(f1, f1, 1.0));
             }
             kf = (pr * (F / (1.0 + pr))) * kinf;
         }
@@ -436,9 +453,9 @@ void oracle_rates(const oracle_mech* m, oracle_ws* w, double p, int model, int m
     const double RT = GAS_CONSTANT * T;
     for (int k = 0; k < S; ++k) {
         w->hk[k] = w->h_RT[k] * RT;
-        w->tmp[k] = (w->ym[k] * mmw) * w->cp_R[k];
+        w->tmp[k] = w->ym[k] * mmw;
     }
-    *cp_out = (GAS_CONSTANT * wsum(w->tmp, S)) / mmw;
+    *cp_out = (GAS_CONSTANT * block_sum(w->tmp, w->cp_R, S, reduction_width(S))) / mmw;
     *rho_out = rho;
 }
 
@@ -479,7 +496,7 @@ typedef struct {
     const double* split;
     double x;
     double T;               /* temperature frozen during corrector calls */
-    double rho, cp;         /* thermo of the last predictor call        */
+    double rrho, rrc;       /* 1/rho and 1/(rho cp) of the last predictor call */
 } qss_ode;
 
 /* SourceSystemQSS::odefun (src/sourceSystem.cpp:445-499) */
@@ -491,25 +508,29 @@ static void qss_odefun(qss_ode* ode, double t, const double* y, double* q, doubl
     double rho, cp;
     oracle_rates(m, w, ode->o->pressure, ode->o->kinetics_model, ORACLE_STATE_NORMALIZED, ode->T, y + 2, &rho, &cp);
     if (!corrector) {
-        /* updateThermo: hk was refreshed by oracle_rates at T; keep the
-         * predictor's hk/rho/cp for the corrector calls */
-        memcpy(w->v, w->hk, sizeof(double) * S);
-        ode->rho = rho;
-        ode->cp = cp;
+        /* updateThermo on predictor calls only; h_k depends on T alone, which
+         * the corrector calls keep, so w->hk is the predictor's */
+        ode->rrho = 1.0 / rho;
+        ode->rrc = 1.0 / (rho * cp);
     }
-    const double* hk = w->v;
-    for (int k = 0; k < S; ++k) w->tmp[k] = (w->wq[k] - w->wd[k]) * hk[k];
-    const double qdot = -wsum(w->tmp, S) + qdot_igniter(ode->o, t, ode->x);
+    for (int k = 0; k < S; ++k) w->tmp[k] = w->wq[k] - w->wd[k];
+    const double qdot = -block_sum(w->tmp, w->hk, S, reduction_width(S)) + qdot_igniter(ode->o, t, ode->x);
     const double* sc = ode->split;
     q[0] = sc ? sc[0] : 0.0;
     d[0] = 0.0;
-    q[1] = qdot / (ode->rho * ode->cp) + (sc ? sc[1] : 0.0);
-    d[1] = 0.0 / (ode->rho * ode->cp);
+    q[1] = fma(qdot, ode->rrc, sc ? sc[1] : 0.0);
+    d[1] = 0.0 * ode->rrc;
     for (int k = 0; k < S; ++k) {
-        q[2 + k] = (w->wq[k] * m->W[k]) / ode->rho + (sc ? sc[2 + k] : 0.0);
-        d[2 + k] = (w->wd[k] * m->W[k]) / ode->rho;
+        q[2 + k] = fma(w->wq[k] * m->W[k], ode->rrho, sc ? sc[2 + k] : 0.0);
+        d[2 + k] = (w->wd[k] * m->W[k]) * ode->rrho;
     }
 }
+
+/* Pade numerator / denominator of the QSS predictor and corrector, Horner
+ * form with fma (the same on the GPU). */
+static double pade_num(double r) { return r * fma(r, fma(r, 11.0 + r, 60.0), 180.0); }
+static double pade_den(double r) { return fma(r, fma(r, 12.0 + r, 60.0), 360.0); }
+static double pade_an(double r) { return fma(r, fma(r, 11.0 + r, 60.0), 180.0); }
 
 static double rsign(double x) { return (x > 0) ? 1.0 : (x < 0) ? -1.0 : 0.0; }
 
@@ -554,10 +575,14 @@ static int qss_one_step(qss_state* s, oracle_qss_fn f, void* ctx, const oracle_q
     memcpy(s->rtaus, s->rtau, sizeof(double) * n);
     const int stab_on = o->stability_check;
     while (1) {
+        /* The reference's predictor (q-d)/(1 + num/den) and corrector
+         * (qs(1-a) + q a - ys rb/dt)/(1 + a rb), a = an/ad, each multiplied
+         * through by den (ad) so that one division remains. */
+        const double rdt = 1.0 / s->dt;
         for (int i = 0; i < n; ++i) {
             const double r = s->rtau[i];
-            s->scratch[i] = (s->q[i] - s->d[i]) /
-                            (1.0 + r * (180 + r * (60 + r * (11 + r))) / (360 + r * (60 + r * (12 + r))));
+            const double den = pade_den(r);
+            s->scratch[i] = ((s->q[i] - s->d[i]) * den) / (den + pade_num(r));
         }
         double eps = 1e-10;
         for (int iter = 0; iter < o->itermax; ++iter) {
@@ -565,7 +590,7 @@ static int qss_one_step(qss_state* s, oracle_qss_fn f, void* ctx, const oracle_q
                 memcpy(s->ym2, s->ym1, sizeof(double) * n);
                 memcpy(s->ym1, s->y, sizeof(double) * n);
             }
-            for (int i = 0; i < n; ++i) s->y[i] = dmax(s->ymin[i], s->ys[i] + s->dt * s->scratch[i]);
+            for (int i = 0; i < n; ++i) s->y[i] = dmax(s->ymin[i], fma(s->dt, s->scratch[i], s->ys[i]));
             if (iter == 0) {
                 s->tn = s->ts + s->dt;
                 memcpy(s->y1, s->y, sizeof(double) * n);
@@ -575,13 +600,13 @@ static int qss_one_step(qss_state* s, oracle_qss_fn f, void* ctx, const oracle_q
             eps = 1.0e-10;
             for (int i = 0; i < n; ++i) {
                 const double rb = en[i] ? 0.5 * (s->rtaus[i] + s->dt * s->d[i] / s->y[i]) : 0.0;
-                const double alpha = (180. + rb * (60. + rb * (11. + rb))) / (360. + rb * (60. + rb * (12. + rb)));
-                s->scratch[i] = (s->qs[i] * (1.0 - alpha) + s->q[i] * alpha - s->ys[i] * rb / s->dt) /
-                                (1.0 + alpha * rb);
+                const double an = pade_an(rb), ad = pade_den(rb);
+                const double num = fma(s->qs[i], ad - an, s->q[i] * an) - ((s->ys[i] * rb) * ad) * rdt;
+                s->scratch[i] = num / fma(an, rb, ad);
             }
         }
         for (int i = 0; i < n; ++i) {
-            double scr2 = s->ys[i] + s->dt * s->scratch[i];
+            double scr2 = fma(s->dt, s->scratch[i], s->ys[i]);
             if (en[i]) scr2 = dmax(scr2, s->ymin[i]);
             double scr1 = fabs(scr2 - s->y1[i]);
             s->y[i] = dmax(scr2, s->ymin[i]);
@@ -617,7 +642,8 @@ static int qss_one_step(qss_state* s, oracle_qss_fn f, void* ctx, const oracle_q
         if (stab_on) s->dt = dmin(s->dt, dto / (stab + .001));
         if (eps > o->epsmax || stab > 1) {
             s->rcount += 1;
-            for (int i = 0; i < n; ++i) s->rtaus[i] *= s->dt / dto;
+            const double ratio = s->dt / dto;
+            for (int i = 0; i < n; ++i) s->rtaus[i] *= ratio;
         } else {
             return 0;
         }
