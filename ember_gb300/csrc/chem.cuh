@@ -79,6 +79,7 @@ struct MechView {
     const int* fo_tb;     // [n_fo] third-body slot of each falloff slot
     const double* fo_arr; // [n_fo][3] low-pressure Arrhenius
     const double* fo_troe;// [n_fo][4] a, 1/T3, 1/T1, T2 (type Lindemann: unused)
+    const int* tb_fo;     // [n_tb] falloff slot of each third-body slot, -1 for three-body reactions
     const int* sp_off;    // [S+1] reactions in which species k occurs, in reaction order
     const int* sp_ent;    // reaction | n_product_occurrences << 24 | n_reactant_occurrences << 28
     const double2* kf_tab;// [nT][R] (value, slope)
@@ -109,6 +110,9 @@ struct ChemSmem {
     double* fo_k0;    // [n_fo]
     double* fo_lfc;   // [n_fo] log10 Fcent (Troe)
     double* red;      // [kMaxChemThreads + 2] reduction scratch
+    double* fo_F;     // [n_fo] falloff F of the last composition (only when set; for Jacobians)
+    double* fo_pr;    // [n_fo] reduced pressure Pr of the last composition (idem)
+    double mmw;       // mean molecular weight of the last composition (set by chem_rates)
     double* kfm;   // global [R]: rate constant x multiplier (falloff rows: refreshed per composition)
     double* rkc;   // global [R]: 1/Kc
 
@@ -138,6 +142,9 @@ struct ChemSmem {
         fo_k0 = fo_rkinf + m.n_fo;
         fo_lfc = fo_k0 + m.n_fo;
         red = fo_lfc + m.n_fo;
+        fo_F = nullptr;
+        fo_pr = nullptr;
+        mmw = 0.0;
         kfm = gbase;
         rkc = gbase + R;
     }
@@ -331,6 +338,10 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
             F = em_exp10(lfc / fma(f1, f1, 1.0));
         }
         w.kfm[i] = ((pr * (F / (1.0 + pr))) * kinf) * m.mult[i];
+        if (w.fo_F) {
+            w.fo_F[f] = F;
+            w.fo_pr[f] = pr;
+        }
     }
     __syncthreads();
     // rates of progress
@@ -393,6 +404,7 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
     }
     cp_out = (kGasConstant * block_sum<NT>(w.red, cpart)) / mmw;
     rho_out = rho;
+    w.mmw = mmw;
 }
 
 }  // namespace ember

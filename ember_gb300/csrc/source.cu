@@ -320,7 +320,7 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
     }
     const size_t Rs = std::max(R, 1);
     std::vector<int4> stoich(Rs, make_int4(-1, -1, -1, -1));
-    std::vector<int> rinfo(Rs, 0), tb_rxn, tb_off(1, 0), tb_sp, fo_rxn, fo_tb;
+    std::vector<int> rinfo(Rs, 0), tb_rxn, tb_off(1, 0), tb_sp, fo_rxn, fo_tb, tb_fo;
     std::vector<double> dn(Rs, 0.0), mult(Rs, 1.0), tb_eff, tb_def, fo_arr, fo_troe;
     std::vector<std::vector<int>> lists(S);
     for (int i = 0; i < R; ++i) {
@@ -346,6 +346,7 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
                 tb_eff.push_back(d->efficiency_values[e] - de);
             }
             tb_off.push_back(static_cast<int>(tb_sp.size()));
+            tb_fo.push_back(ty == EMBER_RXN_LINDEMANN || ty == EMBER_RXN_TROE ? static_cast<int>(fo_rxn.size()) : -1);
         }
         if (ty == EMBER_RXN_LINDEMANN || ty == EMBER_RXN_TROE) {
             fo_rxn.push_back(i);
@@ -415,6 +416,7 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
         {(void**)&v.fo_tb, fo_tb.data(), sizeof(int) * std::max(n_fo, 1)},
         {(void**)&v.fo_arr, fo_arr.data(), sizeof(double) * 3 * std::max(n_fo, 1)},
         {(void**)&v.fo_troe, fo_troe.data(), sizeof(double) * 4 * std::max(n_fo, 1)},
+        {(void**)&v.tb_fo, tb_fo.data(), sizeof(int) * std::max(n_tb, 1)},
         {(void**)&v.sp_off, sp_off.data(), sizeof(int) * (S + 1)},
         {(void**)&v.sp_ent, sp_ent.data(), sizeof(int) * std::max<size_t>(sp_ent.size(), 1)},
         {(void**)&v.kf_tab, nullptr, sizeof(double2) * size_t(nT) * Rs},
@@ -445,6 +447,7 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
             else if (pc.src == fo_tb.data()) nbytes = sizeof(int) * n_fo;
             else if (pc.src == fo_arr.data()) nbytes = sizeof(double) * fo_arr.size();
             else if (pc.src == fo_troe.data()) nbytes = sizeof(double) * fo_troe.size();
+            else if (pc.src == tb_fo.data()) nbytes = sizeof(int) * tb_fo.size();
             else if (pc.src == sp_ent.data()) nbytes = sizeof(int) * sp_ent.size();
             else if (pc.src == d->arrhenius) nbytes = sizeof(double) * 3 * R;
             if (nbytes) e = cudaMemcpy(p, pc.src, nbytes, cudaMemcpyHostToDevice);

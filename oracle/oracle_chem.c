@@ -133,7 +133,10 @@ static int reduction_width(int S) {
  * thread k mod W (sequential in k); the W partials are folded into 32 as
  * p[l] + p[l+32] + p[l+64] + ... (in that order) and combined by an xor
  * butterfly. */
-static double block_sum(const double* a, const double* b, int n, int W) {
+double oracle_block_sum(const double* a, const double* b, int n, int W);
+int oracle_reduction_width(int S) { return reduction_width(S); }
+#define block_sum oracle_block_sum
+double oracle_block_sum(const double* a, const double* b, int n, int W) {
     double p[256], q[32];
     for (int l = 0; l < W; ++l) p[l] = 0.0;
     for (int k = 0; k < n; ++k) p[k % W] = b ? fma(a[k], b[k], p[k % W]) : p[k % W] + a[k];
@@ -283,6 +286,12 @@ oracle_ws* oracle_ws_create(const oracle_mech* m) {
     w->wn = (double*)calloc(S, sizeof(double));
     w->hk = (double*)calloc(S, sizeof(double));
     w->v = (double*)calloc((size_t)n * 16, sizeof(double));
+    w->kf_fall = (double*)calloc(R, sizeof(double));
+    w->k0_fall = (double*)calloc(R, sizeof(double));
+    w->F_fall = (double*)calloc(R, sizeof(double));
+    w->pr_fall = (double*)calloc(R, sizeof(double));
+    w->concm = (double*)calloc(R, sizeof(double));
+    w->jdense = (double*)calloc(S, sizeof(double));
     w->kT = NAN;
     return w;
 }
@@ -292,6 +301,7 @@ void oracle_ws_free(oracle_ws* w) {
     free(w->cp_R); free(w->h_RT); free(w->g_RT); free(w->c); free(w->ym); free(w->tmp);
     free(w->kf); free(w->rkc); free(w->ropf); free(w->ropr); free(w->wq); free(w->wd); free(w->wn);
     free(w->hk); free(w->v);
+    free(w->kf_fall); free(w->k0_fall); free(w->F_fall); free(w->pr_fall); free(w->concm); free(w->jdense);
     free(w);
 }
 
@@ -389,6 +399,8 @@ void oracle_rates(const oracle_mech* m, oracle_ws* w, double p, int model, int m
     double rho, mmw;
     set_composition(m, w, p, T, Y, mode, &rho, &mmw);
     const double ctot = rho / mmw;
+    w->ctot = ctot;
+    w->mmw = mmw;
     const double lnT = oracle_log(T), rT = 1.0 / T;
     for (int i = 0; i < R; ++i) {
         const int ty = m->type[i];
@@ -419,7 +431,12 @@ void oracle_rates(const oracle_mech* m, oracle_ws* w, double p, int model, int m
                 F = oracle_exp10(lfc / fma(f1, f1, 1.0));
             }
             kf = (pr * (F / (1.0 + pr))) * kinf;
+            w->kf_fall[i] = kf;
+            w->k0_fall[i] = k0;
+            w->F_fall[i] = F;
+            w->pr_fall[i] = pr;
         }
+        w->concm[i] = concm;
         double rf = kf * m->mult[i];
         if (ty == ORACLE_RXN_THREE_BODY) rf *= concm;
         double ropf = rf, ropr = 0.0;

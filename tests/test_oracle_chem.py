@@ -137,3 +137,45 @@ def test_qss_dtmin_failure_reported(mech, omech):
     opts = SourceOptions.defaults(kinetics_model=chem.KINETICS_STANDARD, qss_dtmin=1.0)
     out, status, stats = omech.integrate(chem.QSS, st, dt, opts, n_threads=1)
     assert (status == -1).all()
+
+
+def test_bdf_matches_tight_radau(mech, omech):
+    """The oracle's CVODE-path integrator against a converged implicit
+    Runge-Kutta solution (scipy Radau, rtol 1e-11) of the same right-hand side
+    (SourceSystemCVODE::f): final states within a small multiple of the
+    configured tolerances (CvodeTolerances defaults: rtol 1e-6, atol U 1e-7,
+    T 1e-8, Y 1e-13)."""
+    from scipy.integrate import solve_ivp
+    S = mech.n_species
+    st, dt = reactor_states(mech, 4, seed=21)
+    opts = SourceOptions.defaults(kinetics_model=chem.KINETICS_STANDARD)
+    out, status, stats = omech.integrate(chem.BDF, st, dt, opts, n_threads=4)
+    assert (status == 0).all(), status
+
+    def f(t, y):
+        r = omech.gas_eval(np.array([y[1]]), y[None, 2:], model=chem.KINETICS_STANDARD, mode=chem.STATE_NO_NORM)
+        wn, hk, cp, rho = r["net"][0], r["hk"][0], r["cp_mass"][0], r["density"][0]
+        yd = np.zeros_like(y)
+        yd[1] = -(wn @ hk) / (rho * cp)
+        yd[2:] = wn * mech.mol_weight / rho
+        return yd
+
+    tol = np.r_[1e-7, 1e-8, np.full(S, 1e-13)]
+    for j in range(len(st)):
+        ref = solve_ivp(f, (0, dt[j]), st[j], method="Radau", rtol=1e-11, atol=1e-18).y[:, -1]
+        err = np.abs(out[j] - ref) / (1e-6 * np.abs(ref) + tol)
+        assert err.max() < 50.0, (j, err.max())
+        assert abs(out[j, 1] - ref[1]) < 1e-4 * ref[1]
+
+
+def test_bdf_split_constants_and_failures(mech, omech):
+    st, dt = reactor_states(mech, 3, seed=22)
+    split = np.zeros_like(st)
+    split[:, 0] = 5.0
+    opts = SourceOptions.defaults(kinetics_model=chem.KINETICS_INTERP)
+    out, status, stats = omech.integrate(chem.BDF, st, dt, opts, split_const=split, n_threads=1)
+    assert (status == 0).all()
+    np.testing.assert_allclose(out[:, 0], st[:, 0] + 5.0 * dt, rtol=1e-6)
+    opts = SourceOptions.defaults(bdf_max_num_steps=3)
+    out, status, stats = omech.integrate(chem.BDF, st, dt, opts, n_threads=1)
+    assert (status == -11).all()

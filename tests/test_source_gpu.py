@@ -158,3 +158,50 @@ def test_qss_cesium_known_answer_on_gpu(gpu_lib, golden_dir):
         np.testing.assert_array_equal(stats, so)
         rel = np.abs(y - yf) / np.minimum(y, yf)
         assert np.sqrt(np.sum(rel ** 2) / 6) < 0.1 * eps
+
+
+@pytest.mark.parametrize("model", [KINETICS_STANDARD, KINETICS_INTERP])
+def test_bdf_bitwise_vs_oracle(pair_small, small_mech, model):
+    from ember_gb300.source import BDF
+    g, o = pair_small
+    st, dt = _states(small_mech, 24, seed=31)
+    opts = SourceOptions.defaults(kinetics_model=model)
+    out, status, stats = integrate_production_terms(g, BDF, st, dt, opts)
+    ro, rs, rst = o.integrate(chem.BDF, st, dt, opts)
+    np.testing.assert_array_equal(status, rs)
+    np.testing.assert_array_equal(stats, rst)
+    np.testing.assert_array_equal(out, ro)
+
+
+def test_bdf_big_mechanism_bitwise(pair_big, big_mech):
+    from ember_gb300.source import BDF
+    g, o = pair_big
+    st, dt = _states(big_mech, 8, seed=32)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_INTERP)
+    out, status, stats = integrate_production_terms(g, BDF, st, dt, opts)
+    ro, rs, rst = o.integrate(chem.BDF, st, dt, opts)
+    assert (status == 0).all()
+    np.testing.assert_array_equal(stats, rst)
+    np.testing.assert_array_equal(out, ro)
+
+
+def test_bdf_split_igniter_failures(pair_small, small_mech):
+    from ember_gb300.source import BDF
+    g, o = pair_small
+    st, dt = _states(small_mech, 12, seed=33)
+    rng = np.random.default_rng(33)
+    split = rng.normal(scale=1e-2, size=st.shape)
+    split[:, 1] = rng.normal(scale=1e4, size=len(st))
+    x = rng.uniform(-1e-3, 1e-3, len(st))
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD, ignition_energy=5e6, ignition_duration=1e-3,
+                                  ignition_stddev=3e-4)
+    out, status, stats = integrate_production_terms(g, BDF, st, dt, opts, split_const=split, t_start=1e-4, x=x)
+    ro, rs, rst = o.integrate(chem.BDF, st, dt, opts, split_const=split, t_start=1e-4, x=x)
+    np.testing.assert_array_equal(status, rs)
+    np.testing.assert_array_equal(out, ro)
+    opts = SourceOptions.defaults(bdf_max_num_steps=5)
+    out, status, stats = integrate_production_terms(g, BDF, st, dt, opts)
+    ro, rs, rst = o.integrate(chem.BDF, st, dt, opts)
+    np.testing.assert_array_equal(status, rs)
+    assert (np.asarray(status) == -11).any()
+    np.testing.assert_array_equal(out, ro)
