@@ -334,8 +334,146 @@ def run_ours(args):
     return 0
 
 
+# ------------------------------------------------- diffusion workload (C3) --
+
+DIFF_METRIC = "tridiagonal value-updates/s"
+
+
+def diffusion_inputs(rank: int):
+    from ember_gb300.diffusion import synthetic_flames
+    return synthetic_flames(seed=6455 + rank)
+
+
+def run_reference_diffusion(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    import oracle
+    grids, B, D, S, Y, h = diffusion_inputs(0)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        oracle.diffusion_batch(grids, B, D, S, Y, 0.0, 1e-5, h=h, n_threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.diffusion_batch(grids, B, D, S, Y, 0.0, 1e-5, h=h, n_threads=threads)
+    total = time.perf_counter() - t0
+    value = Y.size * args.steps / total
+    print(json.dumps({
+        "impl": "reference", "metric": DIFF_METRIC, "value": value, "unit": "values/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "C3 batched tridiagonal diffusion: 64 flames x 55 variables, N uniform 100-4000, "
+                               "one BDF1x8 step of 1e-5 s", "values": int(Y.size)},
+        "cpu_baseline": {"value": value, "unit": "values/s", "cores": threads, "kind": "port",
+                         "sample": "the whole workload per step, all host threads"},
+        "e2e": {"value": value, "unit": "values/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+    return 0
+
+
+def run_ours_diffusion(args):
+    import numpy as np
+    import torch
+    import ctypes as C
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        torch.distributed.init_process_group("nccl")
+    from ember_gb300 import _lib, roofline
+    from ember_gb300.diffusion import integrate_diffusion_terms
+    lib = _lib.lib()
+    grids, B, D, S, Y, h = diffusion_inputs(rank)
+    dev = torch.device("cuda", local)
+    Bd, Dd, Sd = (torch.as_tensor(v, device=dev) for v in (B, D, S))
+    Y0 = torch.as_tensor(Y, device=dev)
+    Yd = Y0.clone()
+    xd = torch.as_tensor(np.concatenate([g.x for g in grids]), device=dev)
+    hd = torch.as_tensor(h, device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    peak = C.c_double()
+    _lib.check(lib.ember_probe_fp64_rate(0, C.byref(peak)), "probe")
+
+    def step():
+        Yd.copy_(Y0)
+        integrate_diffusion_terms(grids, Bd, Dd, Sd, Yd, 0.0, 1e-5, h=hd, stream=stream, x=xd)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        Yd.copy_(Y0)
+        flush.zero_()
+        starts[i].record(stream)
+        integrate_diffusion_terms(grids, Bd, Dd, Sd, Yd, 0.0, 1e-5, h=hd, stream=stream, x=xd)
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    # end to end with host arrays (copies inside the call)
+    Yh = Y.copy()
+    e2e = []
+    for _ in range(args.steps):
+        Yh[:] = Y
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        integrate_diffusion_terms(grids, B, D, S, Yh, 0.0, 1e-5, h=h)
+        e2e.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    n_vals = int(Y.size)
+    avg_s = total_ms / args.steps / 1e3
+    flops = roofline.tridiag_flops_per_point() * n_vals
+    achieved = flops / avg_s / 1e12
+    line = {
+        "metric": DIFF_METRIC, "value": ws * n_vals * args.steps / (total_ms / 1e3), "unit": "values/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded grids, diffusivities and profiles)",
+        "config": {"workload": "C3 batched tridiagonal diffusion: 64 flames x 55 variables, N uniform 100-4000, "
+                               "one BDF1x8 step of 1e-5 s per system", "values": n_vals,
+                   "l2": "256 MB buffer written between timed iterations"},
+        "e2e": {"value": ws * n_vals * args.steps / sum(e2e), "unit": "values/s",
+                "h2d_bytes_per_step": int(B.nbytes + D.nbytes + S.nbytes + Y.nbytes),
+                "d2h_bytes_per_step": int(Y.nbytes)},
+        "gpu_launches": 2 * args.steps,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / (peak.value / 1e12), "traffic": None,
+                     "hbm_achieved_gbs": roofline.tridiag_bytes_per_point() * n_vals / avg_s / 1e9,
+                     "peak_source": "live DFMA throughput probe (ember_probe_fp64_rate)"},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        import oracle
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < args.cpu_seconds:
+            oracle.diffusion_batch(grids, B, D, S, Y, 0.0, 1e-5, h=h, n_threads=threads)
+            reps += 1
+        tcpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n_vals * reps / tcpu, "unit": "values/s", "cores": threads, "kind": "port",
+                                "sample": f"the whole workload x{reps}, {tcpu:.1f} s on {threads} threads"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.workload == "diffusion":
+        return run_reference_diffusion(args) if args.impl == "reference" else run_ours_diffusion(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

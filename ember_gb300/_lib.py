@@ -36,7 +36,9 @@ class DiffusionGrid(C.Structure):
 class DiffusionOptions(C.Structure):
     _fields_ = [("t_start", C.c_double), ("t_end", C.c_double), ("dt_multiplier", C.c_double),
                 ("global_timestep", C.c_double), ("h", C.c_void_p), ("wall_const", C.c_void_p),
-                ("y_inf", C.c_void_p)]
+                ("y_inf", C.c_void_p), ("algorithm", C.c_int)]
+
+DIFFUSION_PARALLEL, DIFFUSION_SERIAL = 0, 1
 
 
 _lock = threading.Lock()

@@ -124,7 +124,8 @@ class FlameGrid:
 
 
 def integrate_diffusion_terms(grids, B, D, split_const, y, t_start, t_end, *, h=None, dt_multiplier=10.0,
-                              global_timestep=2e-5, wall_const=None, y_inf=None, stream=None):
+                              global_timestep=2e-5, wall_const=None, y_inf=None, stream=None, x=None,
+                              algorithm=L.DIFFUSION_PARALLEL):
     """One diffusion stage for a batch of flames.
 
     ``B``, ``D``, ``split_const`` and ``y`` are either lists with one
@@ -132,7 +133,11 @@ def integrate_diffusion_terms(grids, B, D, split_const, y, t_start, t_end, *, h=
     (variable-major per flame, flames concatenated); flat torch CUDA tensors
     are used in place on the device. Returns the integrated state in the same
     form as ``y`` (lists are returned as new arrays; flat arrays in place)
-    and the per-(flame, variable) status array.
+    and the per-(flame, variable) status array. ``algorithm`` selects the
+    warp-parallel solver (default) or the serial one that reproduces the
+    reference bit for bit. ``x`` may pass the
+    concatenated grid coordinates (e.g. already on the device); per-system
+    arrays (h, wall_const, y_inf) may be device tensors for device calls.
     """
     n_flames = len(grids)
     as_list = isinstance(y, (list, tuple))
@@ -155,16 +160,15 @@ def integrate_diffusion_terms(grids, B, D, split_const, y, t_start, t_end, *, h=
     else:
         import torch
         dev = Y_.device
-        x_ = torch.as_tensor(np.concatenate([_f64(g.x) for g in grids]), device=dev)
+        x_ = x if x is not None else torch.as_tensor(np.concatenate([_f64(g.x) for g in grids]), device=dev)
         status = torch.zeros(n_flames * n_vars, dtype=torch.int32, device=dev)
-        per_sys = lambda v: torch.as_tensor(np.broadcast_to(np.asarray(v, dtype=np.float64),
-                                                            (n_flames * n_vars,)).copy(), device=dev) \
-            if v is not None else None
+        per_sys = lambda v: v if (v is None or hasattr(v, "data_ptr")) else torch.as_tensor(
+            np.broadcast_to(np.asarray(v, dtype=np.float64), (n_flames * n_vars,)).copy(), device=dev)
     h_, wc_, yi_ = per_sys(h), per_sys(wall_const), per_sys(y_inf)
     garr = (L.DiffusionGrid * n_flames)(*[L.DiffusionGrid(g.n_points, g.left_bc, g.right_bc, g.alpha)
                                           for g in grids])
     opts = L.DiffusionOptions(float(t_start), float(t_end), float(dt_multiplier), float(global_timestep),
-                              L.ptr(h_), L.ptr(wc_), L.ptr(yi_))
+                              L.ptr(h_), L.ptr(wc_), L.ptr(yi_), int(algorithm))
     rc = L.lib().ember_diffusion_integrate(n_flames, garr, n_vars, L.ptr(x_), L.ptr(B_), L.ptr(D_), L.ptr(S_),
                                            L.ptr(Y_), C.byref(opts), L.ptr(status), mem, L.stream_ptr(stream))
     if rc not in (L.OK, L.EFAIL):
@@ -177,3 +181,35 @@ def integrate_diffusion_terms(grids, B, D, split_const, y, t_start, t_end, *, h=
             o += n
         return out, status
     return Y_, status
+
+
+def synthetic_flames(n_flames: int = 64, n_vars: int = 55, n_min: int = 100, n_max: int = 4000, seed: int = 6455,
+                     dt: float = 1e-5):
+    """Seeded batch of diffusion stages with uneven grids: N_f uniform in
+    [n_min, n_max]; a non-uniform grid whose neighbouring spacings differ by
+    at most a factor 1.5 (log-ratio random walk, base spacing 2e-5 m);
+    D log-uniform in [1e-6, 1e-3] m^2/s per (variable, point); B = 1 (the
+    equations of the variables are scaled as DiffusionSystem's B = 1/rho
+    with rho = 1); split constant 0; smooth initial profiles; both boundary
+    conditions FixedValue; an explicit step h = dt so that one stage is one
+    BDF1 x 8 step (TridiagonalIntegrator::initialize(0, dt) then
+    integrateToTime(dt)). Returns (grids, B, D, split, y, h) with the flat
+    arrays in the layout of ember_diffusion_integrate."""
+    rng = np.random.default_rng(seed)
+    grids, Bs, Ds, Ys = [], [], [], []
+    for f in range(n_flames):
+        n = int(rng.integers(n_min, n_max + 1))
+        steps = np.clip(np.cumsum(rng.uniform(-0.3, 0.3, n - 1)), np.log(1 / 20), np.log(20))
+        dx = 2e-5 * np.exp(steps)
+        ratio = dx[1:] / dx[:-1]
+        assert ratio.max() <= 1.5 and ratio.min() >= 1 / 1.5
+        x = np.concatenate([[0.0], np.cumsum(dx)])
+        grids.append(FlameGrid(x=x))
+        Bs.append(np.ones((n_vars, n)))
+        Ds.append(np.exp(rng.uniform(np.log(1e-6), np.log(1e-3), (n_vars, n))))
+        xs = (x - x[0]) / (x[-1] - x[0])
+        phase = rng.uniform(0, 2 * np.pi, (n_vars, 1))
+        Ys.append(1.0 + 0.5 * np.tanh(8 * (xs[None, :] - 0.5)) + 0.1 * np.sin(6 * np.pi * xs[None, :] + phase))
+    flat = lambda arrs: np.concatenate([a.reshape(-1) for a in arrs])
+    B, D, Y = flat(Bs), flat(Ds), flat(Ys)
+    return grids, B, D, np.zeros_like(B), Y, np.full(n_flames * n_vars, dt)

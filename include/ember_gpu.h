@@ -160,7 +160,18 @@ typedef struct {
     const double* h;           /* NULL, or explicit step per (flame, var)       */
     const double* wall_const;  /* NULL (0), or per (flame, var): DiffusionSystem::wallConst */
     const double* y_inf;       /* NULL (0), or per (flame, var): DiffusionSystem::yInf      */
+    int algorithm;             /* EMBER_DIFFUSION_PARALLEL (0) or EMBER_DIFFUSION_SERIAL (1) */
 } ember_diffusion_options;
+
+/* EMBER_DIFFUSION_PARALLEL: one warp per system; the Thomas factorisation and
+ * every forward / backward sweep are split into 32 chunks joined by exact
+ * prefix scans (Moebius 2x2 products for the factorisation, affine maps for
+ * the sweeps); agrees with the reference's sequential Thomas algorithm to
+ * rounding (~1e-15 relative).
+ * EMBER_DIFFUSION_SERIAL: one thread per system in the reference's operation
+ * order, bitwise identical to TridiagonalIntegrator on the CPU. */
+#define EMBER_DIFFUSION_PARALLEL 0
+#define EMBER_DIFFUSION_SERIAL   1
 
 /* x: grid coordinates; B, D, split_const: per point and variable (layout
  * above); y: state in/out (same layout); status: n_flames*n_vars ints

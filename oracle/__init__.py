@@ -36,6 +36,8 @@ def _declare(l):
     l.oracle_diffusion_step_size.restype = d
     l.oracle_diffusion_system.argtypes = [i, vp, i, i, i, vp, vp, vp, d, d, d, d, d, d, d, vp]
     l.oracle_diffusion_system.restype = None
+    l.oracle_diffusion_batch.argtypes = [i, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, d, d, d, d, vp, i]
+    l.oracle_diffusion_batch.restype = None
     from . import chem as _chem
     _chem.declare(l)
 
@@ -81,4 +83,25 @@ def diffusion_system(x, B, D, y, t0, t1, split_const=None, alpha=0, left_bc=0, r
     lib().oracle_diffusion_system(len(x), x.ctypes.data, alpha, left_bc, right_bc, B.ctypes.data, D.ctypes.data,
                                   s.ctypes.data if s is not None else None, wall_const, y_inf, h, mult, gdt,
                                   t0, t1, y.ctypes.data)
+    return y
+
+
+def diffusion_batch(grids, B, D, S, Y, t0, t1, h=None, mult=10.0, gdt=2e-5, n_threads=None):
+    """Every (flame, variable) system of a diffusion stage, threaded over
+    systems (flat arrays in the layout of ember_diffusion_integrate)."""
+    import os as _os
+    nf = len(grids)
+    npts = np.array([g.n_points for g in grids], dtype=np.int32)
+    n_vars = np.asarray(Y).size // int(npts.sum())
+    ci = lambda v: np.ascontiguousarray(v, dtype=np.int32)
+    lb, rb, al = ci([g.left_bc for g in grids]), ci([g.right_bc for g in grids]), ci([g.alpha for g in grids])
+    x = _f(np.concatenate([np.asarray(g.x, dtype=np.float64) for g in grids]))
+    B, D = _f(B), _f(D)
+    S = _f(S) if S is not None else None
+    hh = _f(h) if h is not None else None
+    y = _f(Y).copy()
+    lib().oracle_diffusion_batch(nf, n_vars, npts.ctypes.data, lb.ctypes.data, rb.ctypes.data, al.ctypes.data,
+                                 x.ctypes.data, B.ctypes.data, D.ctypes.data, S.ctypes.data if S is not None else None,
+                                 hh.ctypes.data if hh is not None else None, mult, gdt, t0, t1, y.ctypes.data,
+                                 int(n_threads or _os.cpu_count() or 1))
     return y

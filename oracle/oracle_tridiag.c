@@ -238,3 +238,64 @@ void oracle_diffusion_system(int N, const double* x, int alpha, int left_bc, int
     oracle_tridiag_free(&s);
     free(buf);
 }
+
+/* ---- threaded batch (CPU baseline of the diffusion stage) -------------- */
+
+#include <pthread.h>
+
+typedef struct {
+    int n_flames, n_vars;
+    const int* npts;
+    const int* left_bc;
+    const int* right_bc;
+    const int* alpha;
+    const int64_t* pt_off;   /* grid offsets per flame */
+    const int64_t* val_off;  /* value offsets per flame */
+    const double *x, *B, *D, *S, *h;
+    double mult, gdt, t0, t1;
+    double* y;
+    int next;
+    pthread_mutex_t lock;
+} diff_job;
+
+static void* diff_worker(void* arg) {
+    diff_job* J = (diff_job*)arg;
+    const int total = J->n_flames * J->n_vars;
+    for (;;) {
+        pthread_mutex_lock(&J->lock);
+        int s = J->next++;
+        pthread_mutex_unlock(&J->lock);
+        if (s >= total) break;
+        const int f = s / J->n_vars, v = s % J->n_vars;
+        const int N = J->npts[f];
+        const int64_t o = J->val_off[f] + (int64_t)v * N;
+        oracle_diffusion_system(N, J->x + J->pt_off[f], J->alpha[f], J->left_bc[f], J->right_bc[f], J->B + o,
+                                J->D + o, J->S ? J->S + o : NULL, 0.0, 0.0, J->h ? J->h[s] : 0.0, J->mult, J->gdt,
+                                J->t0, J->t1, J->y + o);
+    }
+    return NULL;
+}
+
+void oracle_diffusion_batch(int n_flames, int n_vars, const int* npts, const int* left_bc, const int* right_bc,
+                            const int* alpha, const double* x, const double* B, const double* D, const double* S,
+                            const double* h, double mult, double gdt, double t0, double t1, double* y,
+                            int n_threads) {
+    int64_t* pt_off = (int64_t*)malloc(sizeof(int64_t) * (n_flames + 1));
+    int64_t* val_off = (int64_t*)malloc(sizeof(int64_t) * (n_flames + 1));
+    pt_off[0] = val_off[0] = 0;
+    for (int f = 0; f < n_flames; ++f) {
+        pt_off[f + 1] = pt_off[f] + npts[f];
+        val_off[f + 1] = val_off[f] + (int64_t)npts[f] * n_vars;
+    }
+    diff_job J = {n_flames, n_vars, npts, left_bc, right_bc, alpha, pt_off, val_off, x, B, D, S, h,
+                  mult, gdt, t0, t1, y, 0};
+    pthread_mutex_init(&J.lock, NULL);
+    if (n_threads < 1) n_threads = 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * n_threads);
+    for (int t = 0; t < n_threads; ++t) pthread_create(&th[t], NULL, diff_worker, &J);
+    for (int t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
+    pthread_mutex_destroy(&J.lock);
+    free(th);
+    free(pt_off);
+    free(val_off);
+}

@@ -42,7 +42,7 @@ def _run(torch, lib, fn_name, grids, n_vars, x, B, D, S, Y, t0, t1):
     nsys = len(grids) * n_vars
     status = torch.full((nsys,), 99, dtype=torch.int32, device="cuda")
     garr = (L.DiffusionGrid * len(grids))(*grids)
-    opts = L.DiffusionOptions(t0, t1, 10.0, 2e-5, None, None, None)
+    opts = L.DiffusionOptions(t0, t1, 10.0, 2e-5, None, None, None, L.DIFFUSION_PARALLEL)
     args = [len(grids), garr, n_vars, xd.data_ptr(), Bd.data_ptr(), Dd.data_ptr(), Sd.data_ptr(), Yd.data_ptr(),
             C.byref(opts), status.data_ptr()]
     if fn_name == "ember_diffusion_integrate":
@@ -72,7 +72,7 @@ def test_noalloc_rejects_oversized_problem():
     n_vars = 8
     n = 70000  # 8 x 70000 = 560000 values > EMBER_NOALLOC_MAX_VALUES (524288)
     grids = (L.DiffusionGrid * 1)(L.DiffusionGrid(n, 0, 0, 0))
-    opts = L.DiffusionOptions(0.0, 1e-5, 10.0, 2e-5, None, None, None)
+    opts = L.DiffusionOptions(0.0, 1e-5, 10.0, 2e-5, None, None, None, L.DIFFUSION_PARALLEL)
     dummy = C.c_void_p(16)  # never dereferenced: the size check comes first
     rc = lib.ember_diffusion_integrate_noalloc(1, grids, n_vars, dummy, dummy, dummy, None, dummy, C.byref(opts),
                                                None, None)
