@@ -283,19 +283,18 @@ def run_ours(args):
     status = status_d.cpu().numpy()
     stats = stats_d.cpu().numpy()
     n_fail = int((status != 0).sum())
-    flops = float(roofline.qss_point_flops(mech, opts.kinetics_model, stats[:, 0], stats[:, 1]).sum())
+    if method == QSS:
+        flops = float(roofline.qss_point_flops(mech, opts.kinetics_model, stats[:, 0], stats[:, 1]).sum())
+    else:
+        flops = float(roofline.bdf_point_flops(mech, opts.kinetics_model, stats[:, 0], stats[:, 1],
+                                               stats[:, 3]).sum())
     avg_launch_s = total_ms / args.steps / 1e3
     achieved = flops / avg_launch_s / 1e12
     peak_t = fp64_peak / 1e12
 
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "qss_traffic.json")
-    if os.path.exists(prof):
-        try:
-            with open(prof) as f:
-                traffic = json.load(f).get("dram_bytes_per_launch")
-        except (OSError, ValueError):
-            traffic = None
+    # DRAM bytes per launch from the ncu capture of the integration kernel
+    # (608 points), scaled to this launch's points; none captured for BDF yet.
+    traffic = roofline.QSS_DRAM_BYTES_PER_POINT * args.points if method == QSS else None
 
     line = {
         "metric": METRIC, "value": ws * args.points * args.steps / (total_ms / 1e3), "unit": "points/s",

@@ -242,9 +242,8 @@ struct BdfPoint {
             }
         }
         // temperature column by forward difference
-        for (int i = tid; i < n; i += NT) v.ycopy[i] = yv[i];
         const double dT = fabs(T) * 1.4901161193847656e-08;
-        if (tid == 0) v.ycopy[1] = T + dT;
+        for (int i = tid; i < n; i += NT) v.ycopy[i] = i == 1 ? T + dT : yv[i];
         __syncthreads();
         const double saved_rho = rho, saved_cp = cp, saved_qdot = qdot;
         f(t, v.ycopy, v.f1);
@@ -257,7 +256,9 @@ struct BdfPoint {
     }
 
     // LU with partial pivoting of column-major M (first maximum as pivot;
-    // multipliers a_ik * (1/a_kk)). Returns 0 or k+1 for a zero pivot.
+    // multipliers a_ik * (1/a_kk)). Returns 0, or k+1 when column k has no
+    // usable pivot: all zeros, or a NaN anywhere in it (then no row index is
+    // chosen at all, so nothing is swapped or read out of range).
     __device__ int lu_factor() {
         const int tid = threadIdx.x;
         __shared__ double sbest[32];
@@ -268,8 +269,10 @@ struct BdfPoint {
             double* colk = M + size_t(k) * n;
             double best = -1.0;
             int bi = n;
+            int has_nan = 0;
             for (int i = k + tid; i < n; i += NT) {
                 const double vv = fabs(colk[i]);
+                if (vv != vv) has_nan = 1;
                 if (vv > best) {
                     best = vv;
                     bi = i;
@@ -288,7 +291,8 @@ struct BdfPoint {
                 sbest[tid >> 5] = best;
                 sidx[tid >> 5] = bi;
             }
-            __syncthreads();
+            const int col_nan = __syncthreads_or(has_nan);
+            if (col_nan) return k + 1;
             if (tid == 0) {
                 double b = sbest[0];
                 int p = sidx[0];

@@ -342,6 +342,8 @@ extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_gri
     EMBER_CHECK_ARG(opts->h != nullptr || (opts->dt_multiplier > 0 && opts->global_timestep > 0),
                     "without explicit h, dt_multiplier and global_timestep must be positive");
     EMBER_CHECK_ARG(opts->t_end > opts->t_start, "t_end must exceed t_start");
+    EMBER_CHECK_ARG(opts->algorithm == EMBER_DIFFUSION_PARALLEL || opts->algorithm == EMBER_DIFFUSION_SERIAL,
+                    "bad diffusion algorithm %d", opts->algorithm);
 
     cudaStream_t st = as_stream(stream);
     Scratch sc(st);
@@ -363,14 +365,6 @@ extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_gri
     EMBER_TRY(sc.alloc(&d_status, n_sys));
     dv.status = d_status;
 
-    // Matrix rows and integrator workspace.
-    double* work = nullptr;
-    EMBER_TRY(sc.alloc(&work, size_t(7) * n_vals));
-    dv.a = work;
-    dv.b = work + n_vals;
-    dv.c = work + 2 * n_vals;
-    dv.k = work + 3 * n_vals;
-
     // State in/out.
     double* d_y = nullptr;
     if (mem == EMBER_MEM_DEVICE) {
@@ -380,25 +374,37 @@ extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_gri
         EMBER_CUDA_TRY(cudaMemcpyAsync(d_y, y, sizeof(double) * n_vals, cudaMemcpyHostToDevice, st));
     }
 
-    int nmax = 0;
-    for (int f = 0; f < n_flames; ++f) nmax = std::max(nmax, grids[f].n_points);
-    dim3 grid_rows(std::min(blocks_for(nmax, 256), 32), std::min(n_sys, 65535));
-    k_diffusion_rows<<<grid_rows, 256, 0, st>>>(dv);
+    if (opts->algorithm == EMBER_DIFFUSION_PARALLEL) {
+        EMBER_TRY(launch_diffusion_warp(dv, n_flames, n_vars, info, n_pts, d_y, opts->t_start, opts->t_end,
+                                        opts->dt_multiplier, opts->global_timestep, sc, st));
+    } else {
+        // Matrix rows and integrator workspace.
+        double* work = nullptr;
+        EMBER_TRY(sc.alloc(&work, size_t(7) * n_vals));
+        dv.a = work;
+        dv.b = work + n_vals;
+        dv.c = work + 2 * n_vals;
+        dv.k = work + 3 * n_vals;
+        int nmax = 0;
+        for (int f = 0; f < n_flames; ++f) nmax = std::max(nmax, grids[f].n_points);
+        dim3 grid_rows(std::min(blocks_for(nmax, 256), 32), std::min(n_sys, 65535));
+        k_diffusion_rows<<<grid_rows, 256, 0, st>>>(dv);
 
-    TriBatchView tb;
-    tb.n_systems = n_sys;
-    tb.off = nullptr;
-    tb.info = d_info;
-    tb.a = dv.a;
-    tb.b = dv.b;
-    tb.c = dv.c;
-    tb.k = dv.k;
-    tb.y = d_y;
-    tb.yprev = work + 4 * n_vals;
-    tb.luc = work + 5 * n_vals;
-    tb.inv = work + 6 * n_vals;
-    k_diffusion_integrate_serial<<<blocks_for(n_sys, 64), 64, 0, st>>>(dv, tb, opts->t_start, opts->t_end,
-                                                                        opts->dt_multiplier, opts->global_timestep);
+        TriBatchView tb;
+        tb.n_systems = n_sys;
+        tb.off = nullptr;
+        tb.info = d_info;
+        tb.a = dv.a;
+        tb.b = dv.b;
+        tb.c = dv.c;
+        tb.k = dv.k;
+        tb.y = d_y;
+        tb.yprev = work + 4 * n_vals;
+        tb.luc = work + 5 * n_vals;
+        tb.inv = work + 6 * n_vals;
+        k_diffusion_integrate_serial<<<blocks_for(n_sys, 64), 64, 0, st>>>(
+            dv, tb, opts->t_start, opts->t_end, opts->dt_multiplier, opts->global_timestep);
+    }
     if (mem == EMBER_MEM_HOST) {
         EMBER_CUDA_TRY(cudaMemcpyAsync(y, d_y, sizeof(double) * n_vals, cudaMemcpyDeviceToHost, st));
     }

@@ -2,11 +2,16 @@
 // diffusion matrix (see tridiag.cu for the scheme and references).
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstdint>
+#include <vector>
 
 #include "../../include/ember_gpu.h"
 
 namespace ember {
+
+class Scratch;
 
 // One (flame, variable) diffusion system.
 struct DiffSysInfo {
@@ -265,5 +270,13 @@ __device__ __forceinline__ double diffusion_step_size(int N, const double* x, co
     double h = __dmul_rn(mult, m);
     return gdt < h ? gdt : h;  // std::min(h, gdt)
 }
+
+// Warp-parallel diffusion stage (diffusion_warp.cu): the rows, step size and
+// integration of every system of `dv` with one warp per system; the state
+// `y` (device, variable-major per flame) is updated in place. `info` is the
+// host copy of dv.info, `n_pts` the number of grid points of all flames.
+int launch_diffusion_warp(const DiffusionView& dv, int n_flames, int n_vars, const std::vector<DiffSysInfo>& info,
+                          int64_t n_pts, double* y, double t0, double t1, double mult, double gdt, Scratch& sc,
+                          cudaStream_t st);
 
 }  // namespace ember

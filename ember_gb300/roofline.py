@@ -62,6 +62,38 @@ def qss_point_flops(mech: Mechanism, kinetics_model: int, steps, rhs_calls):
     return steps * f_T + calls * (f_rhs + 40.0 * n)
 
 
+def bdf_point_flops(mech: Mechanism, kinetics_model: int, steps, rhs_calls, jacobians):
+    """Flops of BDF (CVODE-path) integrations given per-point counts of steps,
+    right-hand-side calls and Jacobian evaluations. Every call evaluates the
+    whole right-hand side (temperature changes between Newton iterations) and
+    is followed by one Newton correction (solve with the LU factors, 2 n^2,
+    plus about 12 n for the update, weights and norms); every Jacobian costs
+    the analytic species part (per reaction, the derivatives of the rate of
+    progress with respect to each participating species and the third-body
+    sum, scattered to every participating species), the finite-difference
+    temperature column (one right-hand side, not in the call count), the
+    iteration matrix I - gamma J (n^2) and its LU factorisation (2 n^3 / 3).
+    A lower bound: factorisations that reuse a Jacobian after a step-size
+    change are not counted."""
+    f_T, f_rhs = rhs_flops(mech, kinetics_model)
+    n = float(mech.n_vars)
+    nr, npr = _occurrences(mech)
+    n_eff = np.diff(mech.efficiency_offsets)
+    occ = (nr + npr).astype(float)
+    f_jac_species = float(np.sum(2.0 * occ * occ + 2.0 * n_eff * occ))
+    f_jac = f_jac_species + (f_T + f_rhs) + n * n + 2.0 * n ** 3 / 3.0
+    steps = np.asarray(steps, dtype=float)
+    calls = np.asarray(rhs_calls, dtype=float)
+    jac = np.asarray(jacobians, dtype=float)
+    return calls * (f_T + f_rhs + 2.0 * n * n + 12.0 * n) + jac * f_jac + steps * 20.0 * n
+
+
+# DRAM bytes of one k_source_qss launch per integrated point, from the ncu
+# capture of 608 points (dram__bytes_read.sum 4,297,728 + dram__bytes_write.sum
+# 427,776 bytes): state in and out plus the per-CTA rate-constant cache.
+QSS_DRAM_BYTES_PER_POINT = (4297728 + 427776) / 608
+
+
 def tridiag_flops_per_point() -> float:
     """Diffusion system per point for one BDF1x8 step: matrix rows ~12,
     factorisation ~5, 8 sub-steps x (2 right-hand side + 3 forward + 2 back)."""

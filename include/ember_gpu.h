@@ -190,7 +190,8 @@ int ember_diffusion_integrate(int n_flames, const ember_diffusion_grid* grids, i
  * after initialisation. It has no counterpart in the reference (which runs on
  * the CPU). Same arguments and results as ember_diffusion_integrate with
  * EMBER_MEM_DEVICE (all arrays are device pointers; the call is asynchronous
- * on `stream`), but its workspace is a fixed device array inside the library,
+ * on `stream`; it always runs EMBER_DIFFUSION_SERIAL, whatever
+ * opts->algorithm says), but its workspace is a fixed device array inside the library,
  * sized for EMBER_NOALLOC_MAX_VALUES values (n_vars x total points) and
  * EMBER_NOALLOC_MAX_SYSTEMS (flame, variable) systems, about 28.3 MiB that
  * every GPU which loads the library keeps until the process exits. Larger

@@ -210,20 +210,23 @@ static void bdf_jacobian(bdf_ode* ode, double t, const double* y, const double* 
 /* ---- dense LU with partial pivoting ----------------------------------- */
 
 /* In place on row-major M (n x n); pivot row = first maximum of |a_ik|.
- * Multipliers are a_ik * (1/a_kk). Returns 0, or k+1 for a zero pivot. */
+ * Multipliers are a_ik * (1/a_kk). Returns 0, or k+1 when column k has no
+ * usable pivot (all zeros, or a NaN anywhere in it). */
 static int lu_factor(double* M, int* piv, int n) {
     for (int k = 0; k < n; ++k) {
         int p = k;
         double best = fabs(M[(size_t)k * n + k]);
+        int has_nan = best != best;
         for (int i = k + 1; i < n; ++i) {
             const double v = fabs(M[(size_t)i * n + k]);
+            if (v != v) has_nan = 1;
             if (v > best) {
                 best = v;
                 p = i;
             }
         }
         piv[k] = p;
-        if (best == 0.0) return k + 1;
+        if (has_nan || best == 0.0) return k + 1;
         if (p != k)
             for (int j = 0; j < n; ++j) {
                 const double t = M[(size_t)k * n + j];

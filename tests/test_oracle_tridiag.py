@@ -131,3 +131,24 @@ def test_step_size_rule():
     dlj = 0.5 * (x[2:] - x[:-2])
     expect = min(10 * np.min(dlj ** 2 / (B[1:-1] * D[1:-1])), 2e-5)
     assert oracle.diffusion_step_size(x, B, D, 10.0, 2e-5) == pytest.approx(expect, rel=1e-15)
+
+
+def test_extended_precision_restatement_matches_oracle():
+    # The extended-precision diffusion stage (used to measure accuracy on
+    # badly scaled grids) agrees with the double-precision restatement to the
+    # latter's rounding on a moderate grid, for every boundary condition.
+    from oracle import extended
+    rng = np.random.default_rng(5)
+    for left in range(5):
+        for right in (0, 1, 4):
+            n = 60
+            x = np.cumsum(np.full(n, 3e-5) * np.exp(rng.uniform(-0.2, 0.2, n)))
+            B = np.exp(rng.uniform(-1, 1, n))
+            D = np.exp(rng.uniform(np.log(1e-6), np.log(1e-3), n))
+            S = rng.normal(size=n)
+            y0 = np.cumsum(rng.normal(size=n))
+            alpha = left % 2
+            kw = dict(split_const=S, alpha=alpha, left_bc=left, right_bc=right, wall_const=1.5, y_inf=0.3)
+            ref = oracle.diffusion_system(x, B, D, y0, 0.0, 1e-5, h=2e-6, **kw)
+            ext = extended.diffusion_system(x, B, D, y0, 0.0, 1e-5, 2e-6, **kw)
+            assert np.abs(ext - ref).max() <= 1e-13 * np.abs(ref).max(), (left, right)

@@ -112,19 +112,22 @@ def test_stepwise_matches_integrate(gpu_lib):
 
 # ---- diffusion stage -------------------------------------------------------
 
-def _flame(rng, n, left, right, alpha):
-    dx = rng.uniform(1e-5, 1e-4) * np.exp(np.cumsum(rng.uniform(-0.4, 0.4, n - 1)))
+def _flame(rng, n, left, right, alpha, spread=0.4, max_ratio=None):
+    walk = np.cumsum(rng.uniform(-spread, spread, n - 1))
+    if max_ratio is not None:  # keep the smallest spacing (and the step-size rule's h) bounded
+        walk = np.clip(walk, -np.log(max_ratio), np.log(max_ratio))
+    dx = rng.uniform(1e-5, 1e-4) * np.exp(walk)
     x = np.concatenate([[rng.uniform(0.0, 1e-3) if alpha else -1e-3], dx]).cumsum()
     return FlameGrid(x=x, left_bc=left, right_bc=right, alpha=alpha)
 
 
-def _diffusion_case(rng, n_flames, n_vars, nmin, nmax, all_bcs=True):
+def _diffusion_case(rng, n_flames, n_vars, nmin, nmax, all_bcs=True, **grid_kw):
     grids = []
     for f in range(n_flames):
         n = int(rng.integers(nmin, nmax + 1))
         left = int(rng.integers(0, 5)) if all_bcs else 0
         right = int(rng.choice([0, 1, 4])) if all_bcs else 0
-        grids.append(_flame(rng, n, left, right, int(rng.integers(0, 2)) if all_bcs else 0))
+        grids.append(_flame(rng, n, left, right, int(rng.integers(0, 2)) if all_bcs else 0, **grid_kw))
     B = [np.exp(rng.uniform(-1, 1, (n_vars, g.n_points))) for g in grids]
     D = [np.exp(rng.uniform(np.log(1e-6), np.log(1e-3), (n_vars, g.n_points))) for g in grids]
     S = [rng.normal(scale=10.0, size=(n_vars, g.n_points)) for g in grids]
@@ -158,11 +161,57 @@ def test_diffusion_stage_bitwise_vs_oracle(gpu_lib, explicit_h):
     wall = rng.uniform(0, 5, nsys)
     yinf = rng.normal(size=nsys)
     t0, t1 = 1e-3, 1e-3 + 1e-5
-    out, status = integrate_diffusion_terms(grids, B, D, S, Y, t0, t1, h=h, wall_const=wall, y_inf=yinf)
+    out, status = integrate_diffusion_terms(grids, B, D, S, Y, t0, t1, h=h, wall_const=wall, y_inf=yinf,
+                                            algorithm=L.DIFFUSION_SERIAL)
     assert (np.asarray(status) == 0).all()
     ref = _oracle_stage(grids, B, D, S, Y, t0, t1, h=h, wall=wall, yinf=yinf)
     for f in range(n_flames):
         assert np.array_equal(out[f], ref[f]), f"flame {f} (bc {grids[f].left_bc},{grids[f].right_bc}) differs"
+
+
+# The warp-parallel solver re-associates the Thomas algorithm (chunk carries
+# by prefix scans, 1/den folded into the coefficients), so it agrees with the
+# reference to rounding, not bit for bit. The reference's own rounding error
+# on these systems, measured against the same recurrences in 80-bit extended
+# precision, reaches 1.6e-13 of max|y| (many BDF2 steps of a stiff,
+# ControlVolume-bounded system), so the bound per system is
+# |y_gpu - y_ref| <= 1e-12 * max|y_ref|.
+PARALLEL_TOL = 1e-12
+
+
+def _assert_close_per_system(out, ref, what):
+    for v in range(ref.shape[0]):
+        scale = np.abs(ref[v]).max()
+        err = np.abs(out[v] - ref[v]).max()
+        assert err <= PARALLEL_TOL * scale, f"{what}, variable {v}: max error {err:.3e} vs max|y| {scale:.3e}"
+
+
+@pytest.mark.parametrize("explicit_h", [False, True])
+def test_diffusion_stage_parallel_vs_oracle(gpu_lib, explicit_h):
+    rng = np.random.default_rng(4048 + explicit_h)
+    n_flames, n_vars = 14, 5
+    grids, B, D, S, Y = _diffusion_case(rng, n_flames, n_vars, 3, 700, spread=0.1, max_ratio=4.0)
+    nsys = n_flames * n_vars
+    h = rng.uniform(1e-7, 4e-6, nsys) if explicit_h else None  # 3 to 100 steps: BDF1 x 8, then BDF2
+    wall = rng.uniform(0, 5, nsys)
+    yinf = rng.normal(size=nsys)
+    t0, t1 = 1e-3, 1e-3 + 1e-5
+    out, status = integrate_diffusion_terms(grids, B, D, S, Y, t0, t1, h=h, wall_const=wall, y_inf=yinf)
+    assert (np.asarray(status) == 0).all()
+    ref = _oracle_stage(grids, B, D, S, Y, t0, t1, h=h, wall=wall, yinf=yinf)
+    for f in range(n_flames):
+        _assert_close_per_system(out[f], ref[f], f"flame {f} (N {grids[f].n_points}, bc {grids[f].left_bc},"
+                                                 f"{grids[f].right_bc}, alpha {grids[f].alpha})")
+
+
+def test_diffusion_parallel_long_grid(gpu_lib):
+    # 20000 points: 625 points per lane, many Moebius renormalisations.
+    rng = np.random.default_rng(31)
+    grids, B, D, S, Y = _diffusion_case(rng, 1, 3, 20000, 20000, spread=0.1, max_ratio=4.0)
+    out, status = integrate_diffusion_terms(grids, B, D, S, Y, 0.0, 1e-5, h=[1e-5, 2e-6, 1e-5])
+    assert (np.asarray(status) == 0).all()
+    ref = _oracle_stage(grids, B, D, S, Y, 0.0, 1e-5, h=[1e-5, 2e-6, 1e-5])
+    _assert_close_per_system(out[0], ref[0], "20000-point flame")
 
 
 def test_diffusion_reference_properties_on_gpu(gpu_lib):
@@ -197,9 +246,10 @@ def test_diffusion_device_memory_matches_host(gpu_lib):
 
 
 def test_diffusion_large_flames_c3_subset(gpu_lib):
-    # Config-3 shapes: 55 variables, grids up to 4000 points, dt = 1e-5.
+    # Config-3 shapes: 55 variables, grids of 3000-4000 points whose spacing
+    # varies by at most 16x, dt = 1e-5.
     rng = np.random.default_rng(77)
-    grids, B, D, S, Y = _diffusion_case(rng, 3, 55, 3000, 4000, all_bcs=False)
+    grids, B, D, S, Y = _diffusion_case(rng, 3, 55, 3000, 4000, all_bcs=False, spread=0.1, max_ratio=4.0)
     S = [np.zeros_like(s) for s in S]
     h = np.full(3 * 55, 1e-5)
     out, status = integrate_diffusion_terms(grids, B, D, S, Y, 0.0, 1e-5, h=h)
@@ -207,7 +257,39 @@ def test_diffusion_large_flames_c3_subset(gpu_lib):
     for f in range(3):
         for v in (0, 17, 54):
             ref = oracle.diffusion_system(grids[f].x, B[f][v], D[f][v], Y[f][v], 0.0, 1e-5, h=1e-5)
-            np.testing.assert_allclose(out[f][v], ref, rtol=1e-12, atol=1e-300)
+            _assert_close_per_system(out[f][v][None, :], ref[None, :], f"flame {f}")
+
+
+@pytest.mark.parametrize("algorithm", [L.DIFFUSION_PARALLEL, L.DIFFUSION_SERIAL])
+def test_diffusion_extreme_grid_vs_extended_precision(gpu_lib, algorithm):
+    # Grids whose spacing spans 1e-13 to 1e-1 m: matrix coefficients reach
+    # 1e23 against a BDF shift of 8e5, so b - shift keeps none of the shift and
+    # the reference's own result is off by up to 1e-10 of max|y|. The
+    # parallel solver carries the pivots in u = 1 + lu_c with positive terms
+    # only and stays within 1e-12 of the exact solution of the same discrete
+    # problem (extended-precision restatement); the serial one reproduces the
+    # reference bit for bit, so it is held to the reference's own error.
+    from oracle import extended
+    rng = np.random.default_rng(77)
+    grids, B, D, S, Y = _diffusion_case(rng, 3, 55, 3000, 4000, all_bcs=False)
+    S = [np.zeros_like(s) for s in S]
+    out, status = integrate_diffusion_terms(grids, B, D, S, Y, 0.0, 1e-5, h=np.full(3 * 55, 1e-5),
+                                            algorithm=algorithm)
+    assert (np.asarray(status) == 0).all()
+    worst_ref = 0.0
+    for f in range(3):
+        for v in (0, 54):
+            exact = extended.diffusion_system(grids[f].x, B[f][v], D[f][v], Y[f][v], 0.0, 1e-5, 1e-5)
+            ref = oracle.diffusion_system(grids[f].x, B[f][v], D[f][v], Y[f][v], 0.0, 1e-5, h=1e-5)
+            scale = np.abs(exact).max()
+            err_ref = np.abs(ref - exact).max() / scale
+            err = np.abs(out[f][v] - exact).max() / scale
+            worst_ref = max(worst_ref, err_ref)
+            if algorithm == L.DIFFUSION_PARALLEL:
+                assert err <= 1e-12, f"flame {f} var {v}: {err:.3e} of max|y| from the exact solution"
+            else:
+                assert np.array_equal(out[f][v], ref)
+    assert worst_ref > 1e-11  # the case does exercise the reference's rounding limit
 
 
 def test_bad_step_reports_status(gpu_lib):

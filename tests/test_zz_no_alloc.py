@@ -42,7 +42,8 @@ def _run(torch, lib, fn_name, grids, n_vars, x, B, D, S, Y, t0, t1):
     nsys = len(grids) * n_vars
     status = torch.full((nsys,), 99, dtype=torch.int32, device="cuda")
     garr = (L.DiffusionGrid * len(grids))(*grids)
-    opts = L.DiffusionOptions(t0, t1, 10.0, 2e-5, None, None, None, L.DIFFUSION_PARALLEL)
+    # the allocation-free entry point runs the serial algorithm; compare like with like
+    opts = L.DiffusionOptions(t0, t1, 10.0, 2e-5, None, None, None, L.DIFFUSION_SERIAL)
     args = [len(grids), garr, n_vars, xd.data_ptr(), Bd.data_ptr(), Dd.data_ptr(), Sd.data_ptr(), Yd.data_ptr(),
             C.byref(opts), status.data_ptr()]
     if fn_name == "ember_diffusion_integrate":
