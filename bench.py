@@ -9,7 +9,7 @@ with the reference's default options (interp kinetics), FP64, one launch per
 step. Metric: source-term point-integrations per second.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload qss|bdf|diffusion]
+                    [--workload qss|bdf|diffusion|split]
 
 N > 1 runs under torch.distributed.run: every rank integrates its own batch
 of points (no data exchange; the path has none), value = all points / max
@@ -47,7 +47,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="qss", choices=["qss", "bdf", "diffusion"])
+    p.add_argument("--workload", default="qss", choices=["qss", "bdf", "diffusion", "split"])
     p.add_argument("--points", type=int, default=N_POINTS)
     p.add_argument("--kinetics", default="interp", choices=["interp", "standard"])
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
@@ -469,10 +469,166 @@ def run_ours_diffusion(args):
     return 0
 
 
+# ------------------------------------------------ split-step workload (C5) --
+
+SPLIT_METRIC = "ms per split step"
+SPLIT_DT = 2e-5
+SPLIT_WORKLOAD = ("C5 strain-sweep proxy: 32 seeded flame-like profiles (150-700 points), synthetic "
+                  "150-species/1000-reaction mechanism, balanced D-S-D split step (dt 2e-5 s; diffusion "
+                  "h rule, QSS source, interp kinetics), convection not integrated")
+
+
+def split_inputs(rank: int):
+    from ember_gb300.mechanism import synthetic_mechanism
+    from ember_gb300.split import flame_batch
+    mech = synthetic_mechanism(seed=MECH_SEED)
+    return (mech,) + flame_batch(mech, n_flames=32, n_min=150, n_max=700, seed=3232 + rank)
+
+
+def run_reference_split(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    from oracle.chem import OracleMech
+    from oracle import split as osplit
+    from ember_gb300.source import QSS
+    mech, grids, state, B, D, rho_u, ju, jb = split_inputs(0)
+    opts = source_options(args.kinetics, "qss")
+    om = OracleMech(mech)
+    # bounded sample: the first flame, one split step per timed step
+    g0 = grids[:1]
+    n0 = g0[0].n_points
+    nv = mech.n_vars
+    st0, B0, D0 = state[:n0], B[:nv * n0], D[:nv * n0]
+    for _ in range(args.warmup):
+        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, QSS, opts)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, QSS, opts)
+    per_flame = (time.perf_counter() - t0) / args.steps
+    # scaled to the 32-flame batch by points
+    ms = 1e3 * per_flame * len(state) / n0
+    threads = os.cpu_count() or 1
+    print(json.dumps({
+        "impl": "reference", "metric": SPLIT_METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": SPLIT_WORKLOAD, "points": int(len(state))},
+        "cpu_baseline": {"value": ms, "unit": "ms", "cores": threads, "kind": "port",
+                         "sample": f"flame 0 ({n0} points) per step, scaled to {len(state)} points"},
+        "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+    return 0
+
+
+def run_ours_split(args):
+    import ctypes as C
+    import numpy as np
+    import torch
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        torch.distributed.init_process_group("nccl")
+    from ember_gb300 import _lib, roofline
+    from ember_gb300.source import GpuMechanism, QSS
+    from ember_gb300.split import FlameBatchSplitSolver
+    mech, grids, state, B, D, rho_u, ju, jb = split_inputs(rank)
+    opts = source_options(args.kinetics, "qss")
+    gm = GpuMechanism(mech)
+    solver = FlameBatchSplitSolver(gm, grids, SPLIT_DT, method=QSS, source_options=opts)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    peak = C.c_double()
+    _lib.check(_lib.lib().ember_probe_fp64_rate(0, C.byref(peak)), "probe")
+    solver.set_state(0.0, state)
+    solver.set_transport(B, D)
+    solver.step(args.warmup, graph=True, stream=stream)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    src_flops = 0.0
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record(stream)
+        solver.step(1, graph=True, stream=stream)
+        ends[i].record(stream)
+        torch.cuda.synchronize()
+        _, stats = solver.source_status()
+        src_flops += float(roofline.qss_point_flops(mech, opts.kinetics_model, stats[:, 0], stats[:, 1]).sum())
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    n_fail_src, n_fail_diff = solver.failures()
+    # end to end: host state in, one step, host state out
+    e2e = []
+    host = np.array(state)
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        solver.set_state(0.0, host)
+        solver.step(1, graph=True)
+        out, _ = solver.state()
+        e2e.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    ms = total_ms / args.steps
+    n_vals = state.size
+    flops = src_flops / args.steps + 4 * roofline.tridiag_flops_per_point() * n_vals
+    achieved = flops / (ms / 1e3) / 1e12
+    line = {
+        "metric": SPLIT_METRIC, "value": ms, "unit": "ms", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded flame-like profiles, synthetic transport)",
+        "config": {"workload": SPLIT_WORKLOAD, "points": int(len(state)), "flames": len(grids),
+                   "points_per_s": len(state) / (ms / 1e3), "l2": "256 MB buffer written between timed steps",
+                   "graph": True, "failed_source_points": n_fail_src, "failed_diffusion_systems": n_fail_diff},
+        "e2e": {"value": 1e3 * sum(e2e) / len(e2e), "unit": "ms", "h2d_bytes_per_step": int(state.nbytes),
+                "d2h_bytes_per_step": int(state.nbytes)},
+        # per step: begin, 2 x (transpose, 2 x (stage, failure count, delta), transpose back), stage dt,
+        # 3 work-order kernels + QSS, failure count, end, mass fractions, clock
+        "gpu_launches": 26 * args.steps,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / (peak.value / 1e12), "traffic": None,
+                     "peak_source": "live DFMA throughput probe (ember_probe_fp64_rate)",
+                     "work_model": "QSS flops of the source stage (roofline.py) + 4 diffusion stages x 73 flops/value"},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle.chem import OracleMech
+        from oracle import split as osplit
+        om = OracleMech(mech)
+        n0 = grids[0].n_points
+        nv = mech.n_vars
+        t0 = time.perf_counter()
+        reps = 0
+        while time.perf_counter() - t0 < args.cpu_seconds or reps == 0:
+            osplit.split_steps(om, grids[:1], state[:n0], 0.0, B[:nv * n0], D[:nv * n0], SPLIT_DT, 1, QSS, opts)
+            reps += 1
+        tcpu = (time.perf_counter() - t0) / reps
+        threads = os.cpu_count() or 1
+        line["cpu_baseline"] = {"value": 1e3 * tcpu * len(state) / n0, "unit": "ms", "cores": threads,
+                                "kind": "port",
+                                "sample": f"flame 0 ({n0} points) x{reps} on {threads} threads, scaled by points"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse_args()
     if args.workload == "diffusion":
         return run_reference_diffusion(args) if args.impl == "reference" else run_ours_diffusion(args)
+    if args.workload == "split":
+        return run_reference_split(args) if args.impl == "reference" else run_ours_split(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

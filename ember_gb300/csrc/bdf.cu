@@ -715,7 +715,7 @@ __global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int
         P.x = a.x ? a.x[j] : 0.0;
         __syncthreads();
         int st4[4];
-        int ret = bdf_integrate<NT>(P, a.dt[j], a.t_start, st4);
+        int ret = bdf_integrate<NT>(P, a.dt[j], a.t_start_dev ? *a.t_start_dev : a.t_start, st4);
         int nonfinite = 0;
         double* yout = a.state_out + size_t(j) * n;
         for (int i = tid; i < n; i += NT) {
@@ -733,8 +733,9 @@ __global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int
     }
 }
 
+// Dynamic shared memory and persistent grid size of the BDF kernel.
 template <int NT>
-static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
+static int bdf_config(const MechView& m, const SourceArgs& a, size_t* per_out, int* blocks_out) {
     const int n = m.S + 2;
     const size_t per = (ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(2) * m.n_fo +
                         BdfSmem::doubles(n)) * sizeof(double);
@@ -745,7 +746,38 @@ static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, S
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     EMBER_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_source_bdf<NT>, NT, per));
     per_sm = std::max(per_sm, 1);
-    const int blocks = std::max(1, std::min(a.n, sms * per_sm));
+    *per_out = per;
+    *blocks_out = std::max(1, std::min(a.n, sms * per_sm));
+    return EMBER_OK;
+}
+
+template <int NT>
+static int bdf_scratch_nt(const MechView& m, const SourceArgs& a, size_t* bytes) {
+    size_t per = 0;
+    int blocks = 0;
+    EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
+    const size_t n = size_t(m.S) + 2;
+    *bytes = Scratch::rounded(sizeof(double) * size_t(blocks) * ChemSmem::global_doubles(m.R)) +
+             Scratch::rounded(sizeof(double) * size_t(blocks) * 2 * n * n) + Scratch::rounded(sizeof(int) * 64) +
+             Scratch::rounded(sizeof(int) * size_t(a.n));
+    return EMBER_OK;
+}
+
+int source_bdf_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes) {
+    switch (chem_threads_for(m.S)) {
+        case 64: return bdf_scratch_nt<64>(m, a, bytes);
+        case 128: return bdf_scratch_nt<128>(m, a, bytes);
+        case 160: return bdf_scratch_nt<160>(m, a, bytes);
+        default: return bdf_scratch_nt<256>(m, a, bytes);
+    }
+}
+
+template <int NT>
+static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
+    const int n = m.S + 2;
+    size_t per = 0;
+    int blocks = 0;
+    EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
     double *kcache = nullptr, *jm = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
     EMBER_TRY(sc.alloc(&jm, size_t(blocks) * 2 * size_t(n) * n));

@@ -53,18 +53,39 @@ int ensure_device();
 // Stream-ordered device scratch (cudaMallocAsync / cudaFreeAsync on the
 // call's stream). Freed when the object goes out of scope; the free is
 // ordered after every kernel already queued on that stream.
+//
+// Arena mode (the second constructor): allocations are carved in order out of
+// a caller-owned device buffer and nothing is freed; no allocation call is
+// made, so launches that take a Scratch can be captured into a CUDA graph and
+// replayed with the same buffers.
 class Scratch {
 public:
     explicit Scratch(cudaStream_t s) : stream_(s) {}
+    Scratch(cudaStream_t s, void* arena, size_t arena_bytes)
+        : stream_(s), arena_(static_cast<char*>(arena)), arena_bytes_(arena_bytes) {}
     ~Scratch() { release(); }
     Scratch(const Scratch&) = delete;
     Scratch& operator=(const Scratch&) = delete;
 
+    static size_t rounded(size_t bytes) {
+        bytes = ((bytes + 255) / 256) * 256;
+        return bytes == 0 ? 256 : bytes;
+    }
+
     // Allocate `bytes` (rounded up to 256) and return the device pointer in *p.
     template <class T>
     int alloc(T** p, size_t count) {
-        size_t bytes = ((count * sizeof(T) + 255) / 256) * 256;
-        if (bytes == 0) bytes = 256;
+        size_t bytes = rounded(count * sizeof(T));
+        if (arena_) {
+            if (arena_used_ + bytes > arena_bytes_) {
+                set_error("scratch arena too small (%zu of %zu bytes used, %zu more requested)", arena_used_,
+                          arena_bytes_, bytes);
+                return EMBER_ENOMEM;
+            }
+            *p = reinterpret_cast<T*>(arena_ + arena_used_);
+            arena_used_ += bytes;
+            return EMBER_OK;
+        }
         void* q = nullptr;
         cudaError_t e = cudaMallocAsync(&q, bytes, stream_);
         if (e != cudaSuccess) {
@@ -84,6 +105,9 @@ public:
 private:
     cudaStream_t stream_;
     std::vector<void*> ptrs_;
+    char* arena_ = nullptr;
+    size_t arena_bytes_ = 0;
+    size_t arena_used_ = 0;
 };
 
 // View an argument array on the device: for EMBER_MEM_DEVICE the pointer is

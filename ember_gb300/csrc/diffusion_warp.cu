@@ -77,7 +77,8 @@ struct WarpDiffView {
     double* ws;
     int* status;
     unsigned int* counter;
-    double t0, t1, mult, gdt;
+    StageTime tm;
+    double mult, gdt;
 };
 
 // Geometric factors of the interior rows, one grid point per thread:
@@ -367,13 +368,15 @@ __global__ void __launch_bounds__(128) k_diffusion_warp(WarpDiffView v) {
             h = v.gdt < hm ? v.gdt : hm;
         }
         // Integrator::integrateToTime step rounding.
-        const double q = __dadd_rn(__ddiv_rn(__dsub_rn(v.t1, v.t0), h), 1e-5);
+        double t0, t1;
+        v.tm.get(t0, t1);
+        const double q = __dadd_rn(__ddiv_rn(__dsub_rn(t1, t0), h), 1e-5);
         if (!(h > 0.0) || !(q < 2147483647.0)) {
             if (lane == 0 && v.status) v.status[s] = TRI_BAD_STEP;
             continue;
         }
         const int n_steps = q >= 1.0 ? static_cast<int>(q) : 1;
-        h = __ddiv_rn(__dsub_rn(v.t1, v.t0), static_cast<double>(n_steps));
+        h = __ddiv_rn(__dsub_rn(t1, t0), static_cast<double>(n_steps));
 
         double* y = v.y + info.off;
         for (int j = 0; j < ch.cnt; ++j) {
@@ -403,62 +406,82 @@ __global__ void __launch_bounds__(128) k_diffusion_warp(WarpDiffView v) {
     }
 }
 
+// Resident warps per SM of the persistent grid (EMBER_DIFFUSION_WARPS_PER_SM
+// overrides). Fewer warps keep more of the workspace in L2, more warps hide
+// more latency; on the 64-flame, 55-variable batch (N 100-4000) 12 was best.
 int warps_per_sm() {
     static int w = [] {
         const char* e = std::getenv("EMBER_DIFFUSION_WARPS_PER_SM");
         int v = e ? std::atoi(e) : 0;
-        return (v >= 1 && v <= 64) ? v : 8;
+        return (v >= 1 && v <= 64) ? v : 12;  // 4: 3.22 ms, 8: 2.24, 12: 1.75, 16: 1.83 on the 64-flame batch
     }();
     return w;
 }
 
 }  // namespace
 
-int launch_diffusion_warp(const DiffusionView& dv, int n_flames, int n_vars, const std::vector<DiffSysInfo>& info,
-                          int64_t n_pts, double* y, double t0, double t1, double mult, double gdt, Scratch& sc,
-                          cudaStream_t st) {
-    const int n_sys = dv.n_systems;
+size_t diffusion_warp_plan_bytes(const std::vector<DiffSysInfo>& info, int64_t n_pts) {
+    int64_t total = 0;
+    for (const DiffSysInfo& d : info) total += int64_t(kSlots) * 32 * ((d.n + 31) / 32);
+    const size_t n_sys = info.size();
+    return Scratch::rounded(sizeof(double) * size_t(total)) + Scratch::rounded(sizeof(double2) * size_t(n_pts)) +
+           Scratch::rounded(sizeof(int64_t) * n_sys) + Scratch::rounded(sizeof(int) * n_sys) +
+           Scratch::rounded(sizeof(unsigned int));
+}
+
+int diffusion_warp_plan_init(DiffusionWarpPlan* p, const std::vector<DiffSysInfo>& info, int n_flames, int n_vars,
+                             int64_t n_pts, Scratch& sc, cudaStream_t st) {
+    const int n_sys = static_cast<int>(info.size());
     // Workspace offsets and the largest-first order.
     std::vector<int64_t> off(n_sys);
     int64_t total = 0;
+    int nmax = 0;
     for (int s = 0; s < n_sys; ++s) {
         off[s] = total;
         total += int64_t(kSlots) * 32 * ((info[s].n + 31) / 32);
+        nmax = std::max(nmax, info[s].n);
     }
     std::vector<int> order(n_sys);
     std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int p, int q) { return info[p].n > info[q].n; });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return info[a].n > info[b].n; });
 
-    double* ws = nullptr;
-    double2* geo = nullptr;
-    int64_t* d_off = nullptr;
-    int* d_order = nullptr;
-    unsigned int* counter = nullptr;
-    EMBER_TRY(sc.alloc(&ws, size_t(total)));
-    EMBER_TRY(sc.alloc(&geo, size_t(n_pts)));
-    EMBER_TRY(sc.alloc(&d_off, size_t(n_sys)));
-    EMBER_TRY(sc.alloc(&d_order, size_t(n_sys)));
-    EMBER_TRY(sc.alloc(&counter, 1));
-    EMBER_CUDA_TRY(cudaMemcpyAsync(d_off, off.data(), sizeof(int64_t) * n_sys, cudaMemcpyHostToDevice, st));
-    EMBER_CUDA_TRY(cudaMemcpyAsync(d_order, order.data(), sizeof(int) * n_sys, cudaMemcpyHostToDevice, st));
-    EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned int), st));
-
-    int nmax = 0;
-    for (int f = 0; f < n_flames; ++f) nmax = std::max(nmax, info[int64_t(f) * n_vars].n);
-    dim3 ggeo(std::min(blocks_for(nmax, 256), 16), std::min(n_flames, 65535));
-    k_diffusion_geometry<<<ggeo, 256, 0, st>>>(dv.info, n_flames, n_vars, dv.x, geo);
+    p->n_sys = n_sys;
+    p->n_flames = n_flames;
+    p->n_vars = n_vars;
+    p->n_pts = n_pts;
+    p->nmax = nmax;
+    EMBER_TRY(sc.alloc(&p->ws, size_t(total)));
+    EMBER_TRY(sc.alloc(&p->geo, size_t(n_pts)));
+    EMBER_TRY(sc.alloc(&p->ws_off, size_t(n_sys)));
+    EMBER_TRY(sc.alloc(&p->order, size_t(n_sys)));
+    EMBER_TRY(sc.alloc(&p->counter, 1));
+    EMBER_CUDA_TRY(cudaMemcpyAsync(p->ws_off, off.data(), sizeof(int64_t) * n_sys, cudaMemcpyHostToDevice, st));
+    EMBER_CUDA_TRY(cudaMemcpyAsync(p->order, order.data(), sizeof(int) * n_sys, cudaMemcpyHostToDevice, st));
 
     int dev = 0, sms = 0;
     EMBER_CUDA_TRY(cudaGetDevice(&dev));
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int64_t warps = std::min<int64_t>(n_sys, int64_t(sms) * warps_per_sm());
+    p->warps = std::min<int64_t>(n_sys, int64_t(sms) * warps_per_sm());
+    return EMBER_OK;
+}
+
+int diffusion_warp_geometry(const DiffusionWarpPlan& p, const DiffSysInfo* d_info, const double* x, cudaStream_t st) {
+    dim3 ggeo(std::min(blocks_for(p.nmax, 256), 16), std::min(p.n_flames, 65535));
+    k_diffusion_geometry<<<ggeo, 256, 0, st>>>(d_info, p.n_flames, p.n_vars, x, p.geo);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
+int diffusion_warp_run(const DiffusionWarpPlan& p, const DiffusionView& dv, double* y, const StageTime& tm,
+                       double mult, double gdt, cudaStream_t st) {
+    EMBER_CUDA_TRY(cudaMemsetAsync(p.counter, 0, sizeof(unsigned int), st));
     WarpDiffView v;
-    v.n_systems = n_sys;
+    v.n_systems = p.n_sys;
     v.info = dv.info;
-    v.order = d_order;
-    v.ws_off = d_off;
+    v.order = p.order;
+    v.ws_off = p.ws_off;
     v.x = dv.x;
-    v.geo = geo;
+    v.geo = p.geo;
     v.B = dv.B;
     v.D = dv.D;
     v.split_const = dv.split_const;
@@ -466,14 +489,13 @@ int launch_diffusion_warp(const DiffusionView& dv, int n_flames, int n_vars, con
     v.wall_const = dv.wall_const;
     v.y_inf = dv.y_inf;
     v.y = y;
-    v.ws = ws;
+    v.ws = p.ws;
     v.status = dv.status;
-    v.counter = counter;
-    v.t0 = t0;
-    v.t1 = t1;
+    v.counter = p.counter;
+    v.tm = tm;
     v.mult = mult;
     v.gdt = gdt;
-    k_diffusion_warp<<<blocks_for(warps * 32, 128), 128, 0, st>>>(v);
+    k_diffusion_warp<<<blocks_for(p.warps * 32, 128), 128, 0, st>>>(v);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }

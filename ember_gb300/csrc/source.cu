@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(NT) k_source_qss(MechView m, SourceArgs a, int
         ode.rrc = 1.0;
         QssStats st;
         int ret = qss_integrate_block<NT>(ode, v, n, P, EnforceNotMomentum(), SourceYmin{a.qss_minval}, a.dt[j],
-                                          a.t_start, ode.w.red, st);
+                                          a.t_start_dev ? *a.t_start_dev : a.t_start, ode.w.red, st);
         int nonfinite = 0;
         double* yout = a.state_out + size_t(j) * n;
         for (int i = tid; i < n; i += NT) {
@@ -261,12 +261,6 @@ __global__ void __launch_bounds__(NT) k_source_qss(MechView m, SourceArgs a, int
 // ================================================================ C ABI ==
 
 using namespace ember;
-
-struct ember_mech_s {
-    int S = 0, R = 0;
-    void* blob = nullptr;  // one device allocation holding every table
-    MechView view{};
-};
 
 extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
     EMBER_CHECK_ARG(out != nullptr && d != nullptr, "null argument");
@@ -655,8 +649,9 @@ int make_work_order(const SourceArgs& a, Scratch& sc, cudaStream_t st, int** ord
     return EMBER_OK;
 }
 
+// Dynamic shared memory and persistent grid size of the QSS kernel.
 template <int NT>
-static int launch_qss_nt(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
+static int qss_config(const MechView& m, const SourceArgs& a, size_t* per_out, int* blocks_out) {
     const size_t per = qss_smem_doubles(m, a.qss_stability_check != 0) * sizeof(double);
     EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the QSS shared-memory work area (%zu B)", per);
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_qss<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
@@ -665,7 +660,35 @@ static int launch_qss_nt(const MechView& m, const SourceArgs& a, int* counter, S
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     EMBER_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_source_qss<NT>, NT, per));
     per_sm = std::max(per_sm, 1);
-    const int blocks = std::max(1, std::min(a.n, sms * per_sm));
+    *per_out = per;
+    *blocks_out = std::max(1, std::min(a.n, sms * per_sm));
+    return EMBER_OK;
+}
+
+template <int NT>
+static int qss_scratch_nt(const MechView& m, const SourceArgs& a, size_t* bytes) {
+    size_t per = 0;
+    int blocks = 0;
+    EMBER_TRY(qss_config<NT>(m, a, &per, &blocks));
+    *bytes = Scratch::rounded(sizeof(double) * size_t(blocks) * ChemSmem::global_doubles(m.R)) +
+             Scratch::rounded(sizeof(int) * 64) + Scratch::rounded(sizeof(int) * size_t(a.n));
+    return EMBER_OK;
+}
+
+int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes) {
+    switch (chem_threads_for(m.S)) {
+        case 64: return qss_scratch_nt<64>(m, a, bytes);
+        case 128: return qss_scratch_nt<128>(m, a, bytes);
+        case 160: return qss_scratch_nt<160>(m, a, bytes);
+        default: return qss_scratch_nt<256>(m, a, bytes);
+    }
+}
+
+template <int NT>
+static int launch_qss_nt(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
+    size_t per = 0;
+    int blocks = 0;
+    EMBER_TRY(qss_config<NT>(m, a, &per, &blocks));
     double* kcache = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
     int* order = nullptr;

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include "../../include/ember_gpu.h"
 #include "chem.cuh"
 #include "qss.cuh"
 
@@ -15,6 +16,7 @@ struct SourceArgs {
     const double* split;      // [n][S+2] or null
     const double* dt;         // [n]
     double t_start;
+    const double* t_start_dev;  // null, or device scalar used instead of t_start (graph replays)
     const double* x;          // [n] or null
     double* state_out;        // [n][S+2]
     int* status;              // [n]
@@ -49,5 +51,20 @@ class Scratch;
 int make_work_order(const SourceArgs& a, Scratch& sc, cudaStream_t st, int** order_out);
 int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st);
 int launch_source_bdf(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st);
+// SourceArgs from the public options (source.cu).
+SourceArgs make_source_args(const ember_source_options* o, int n, const double* state_in, const double* split,
+                            const double* dt, double t_start, const double* x, double* state_out, int* status,
+                            int* stats);
+int source_check_options(const ember_source_options* o);
+// Device bytes a launch above takes from its Scratch (for an arena sized up front).
+int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes);
+int source_bdf_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes);
 
 }  // namespace ember
+
+// A compiled mechanism (ember_mech handle).
+struct ember_mech_s {
+    int S = 0, R = 0;
+    void* blob = nullptr;  // one device allocation holding every table
+    ember::MechView view{};
+};

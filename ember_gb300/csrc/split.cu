@@ -1,0 +1,705 @@
+// Device split step for a batch of flames (the orchestration of
+// SplitSolver::step / integrateSplitTerms, src/splitSolver.cpp:34-121, with
+// the stage hooks of FlameSolver, src/flameSolver.cpp:702-854, and
+// FlameSolver::finishStep's mass-fraction correction, src/flameSolver.cpp:
+// 219-224, 942-949).
+//
+// One step on the device, with every array resident in HBM:
+//   split constants from the previous step's time derivatives;
+//   diffusion [t, t+dt/4] and [t+dt/4, t+dt/2];
+//   source term [t, t+dt] (QSS or BDF, every grid point of every flame);
+//   diffusion [t+dt/2, t+3dt/4] and [t+3dt/4, t+dt];
+//   time derivatives (delta / dt - split constant), mass-fraction
+//   correction, t += dt.
+// The convection stages of the reference are not integrated here (the
+// convection system is not part of this library); a caller that has them
+// supplies their effect through ddt_cross. Stage times are read from a device
+// clock, so a captured step replays as a CUDA graph.
+//
+// Layouts: the flame state is point-major [point][n_vars] (U, T, Y_0..), as
+// FlameSolver::state; the diffusion stages work on a variable-major copy
+// [flame][variable][point] (the rows DiffusionSystem integrates), produced
+// and consumed by transpose kernels around each pair of diffusion stages.
+//
+// Compiled with --fmad=false: every multiply and add is rounded as written,
+// so with the serial diffusion algorithm the step reproduces the CPU
+// restatement bit for bit.
+#include "common.cuh"
+#include "source.cuh"
+#include "tridiag.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace ember {
+namespace {
+
+struct SplitTables {
+    int64_t n_pts;
+    int n;                     // variables per point
+    const int64_t* vm_base;    // per point: variable-major index of variable 0
+    const int* npt;            // per point: points of its flame (variable stride)
+};
+
+__device__ __forceinline__ int64_t vm_index(const SplitTables& t, int64_t p, int v) {
+    return t.vm_base[p] + int64_t(v) * t.npt[p];
+}
+
+// Point-major state -> variable-major copy (and the stage-start snapshot).
+__global__ void k_to_varmajor(SplitTables tb, const double* __restrict__ state, double* __restrict__ yv,
+                              double* __restrict__ ystart) {
+    const int64_t total = tb.n_pts * tb.n;
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t p = e / tb.n;
+        const int v = static_cast<int>(e - p * tb.n);
+        const int64_t q = vm_index(tb, p, v);
+        const double val = state[e];
+        yv[q] = val;
+        ystart[q] = val;
+    }
+}
+
+// Variable-major copy -> point-major state (and, when given, a snapshot).
+__global__ void k_to_pointmajor(SplitTables tb, const double* __restrict__ yv, double* __restrict__ state,
+                                double* __restrict__ snap) {
+    const int64_t total = tb.n_pts * tb.n;
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t p = e / tb.n;
+        const int v = static_cast<int>(e - p * tb.n);
+        const double val = yv[vm_index(tb, p, v)];
+        state[e] = val;
+        if (snap) snap[e] = val;
+    }
+}
+
+// deltaDiff += state - startState after a diffusion stage (variable-major),
+// and the next stage's start snapshot.
+__global__ void k_diff_accumulate(int64_t n_vals, const double* __restrict__ yv, double* __restrict__ ystart,
+                                  double* __restrict__ delta) {
+    for (int64_t q = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; q < n_vals; q += int64_t(gridDim.x) * blockDim.x) {
+        const double y = yv[q];
+        delta[q] = delta[q] + (y - ystart[q]);
+        ystart[q] = y;
+    }
+}
+
+// Start of a step (SplitSolver::step, src/splitSolver.cpp:38-46): split
+// constants from the previous step's time derivatives, deltaDiff = 0.
+// Balanced splitting of the two integrated operators gives each half of the
+// total rate: c_D = (f_S + f_X - f_D) / 2, c_S = (f_D + f_X - f_S) / 2; the
+// plain Strang variant uses c_D = f_X, c_S = 0.
+__global__ void k_split_begin(SplitTables tb, int balanced, const double* __restrict__ ddt_diff,
+                              const double* __restrict__ ddt_prod, const double* __restrict__ ddt_cross,
+                              double* __restrict__ sc_diff, double* __restrict__ sc_diff_vm,
+                              double* __restrict__ sc_prod, double* __restrict__ delta_diff_vm) {
+    const int64_t total = tb.n_pts * tb.n;
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t p = e / tb.n;
+        const int v = static_cast<int>(e - p * tb.n);
+        const double fx = ddt_cross ? ddt_cross[e] : 0.0;
+        double cd, cs;
+        if (balanced) {
+            cd = 0.5 * ((ddt_prod[e] + fx) - ddt_diff[e]);
+            cs = 0.5 * ((ddt_diff[e] + fx) - ddt_prod[e]);
+        } else {
+            cd = fx;
+            cs = 0.0;
+        }
+        const int64_t q = vm_index(tb, p, v);
+        sc_diff[e] = cd;
+        sc_diff_vm[q] = cd;
+        sc_prod[e] = cs;
+        delta_diff_vm[q] = 0.0;
+    }
+}
+
+// Local duration of the source stage, (t + dt) - t, and its start time.
+__global__ void k_stage_dt(int64_t n_pts, const double* __restrict__ t_dev, double dt, double* __restrict__ dtp) {
+    const double t = *t_dev;
+    const double d = (t + dt) - t;
+    for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < n_pts; p += int64_t(gridDim.x) * blockDim.x)
+        dtp[p] = d;
+}
+
+// End of a step: SplitSolver::calculateTimeDerivatives (src/splitSolver.cpp:
+// 27-32) with deltaProd = state(after S) - state(before S).
+__global__ void k_split_end(SplitTables tb, double dt, const double* __restrict__ xS, const double* __restrict__ xD2,
+                            const double* __restrict__ delta_diff_vm, const double* __restrict__ sc_diff,
+                            const double* __restrict__ sc_prod, double* __restrict__ ddt_diff,
+                            double* __restrict__ ddt_prod) {
+    const int64_t total = tb.n_pts * tb.n;
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t p = e / tb.n;
+        const int v = static_cast<int>(e - p * tb.n);
+        const double delta_prod = xS[e] - xD2[e];
+        ddt_diff[e] = delta_diff_vm[vm_index(tb, p, v)] / dt - sc_diff[e];
+        ddt_prod[e] = delta_prod / dt - sc_prod[e];
+    }
+}
+
+// FlameSolver::correctMassFractions (src/flameSolver.cpp:942-949): Cantera's
+// setState_TPY followed by getMassFractions, i.e. negative mass fractions
+// set to zero and the rest scaled by 1 / (their sequential sum). One thread
+// per point.
+__global__ void k_correct_mass_fractions(int64_t n_pts, int n, double* __restrict__ state) {
+    for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < n_pts; p += int64_t(gridDim.x) * blockDim.x) {
+        double* Y = state + p * n + 2;
+        double sum = 0.0;
+        for (int k = 0; k < n - 2; ++k) sum = sum + (Y[k] < 0.0 ? 0.0 : Y[k]);  // std::max(y, 0.0)
+        const double r = 1.0 / sum;
+        for (int k = 0; k < n - 2; ++k) Y[k] = (Y[k] < 0.0 ? 0.0 : Y[k]) * r;
+    }
+}
+
+__global__ void k_advance_clock(double* t_dev, double dt) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *t_dev = *t_dev + dt;
+}
+
+// Running count of failed systems / points (status != 0) over the steps.
+__global__ void k_count_failures(int n, const int* __restrict__ status, unsigned long long* count) {
+    unsigned long long local = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) local += status[i] != 0;
+    if (local) atomicAdd(count, local);
+}
+
+// ---- objectives ------------------------------------------------------------
+
+__global__ void k_gather_TY(int64_t n_pts, int n, const double* __restrict__ state, double* __restrict__ T,
+                            double* __restrict__ Y) {
+    const int S = n - 2;
+    const int64_t total = n_pts * S;
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t p = e / S;
+        const int k = static_cast<int>(e - p * S);
+        Y[e] = state[p * n + 2 + k];
+        if (k == 0) T[p] = state[p * n + 1];
+    }
+}
+
+// FlameSolver::calculateQdot (src/flameSolver.cpp:926-940): q_j = -sum_k
+// wdot_k h_k (sequential sum), and q_j / cp_j.
+__global__ void k_qdot(int64_t n_pts, int S, const double* __restrict__ net, const double* __restrict__ hk,
+                       const double* __restrict__ cp, double* __restrict__ qdot, double* __restrict__ qcp) {
+    for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < n_pts; p += int64_t(gridDim.x) * blockDim.x) {
+        double s = 0.0;
+        for (int k = 0; k < S; ++k) s = s + net[p * S + k] * hk[p * S + k];
+        const double q = -s;
+        qdot[p] = q;
+        qcp[p] = q / cp[p];
+    }
+}
+
+// mathUtils::integrate (src/mathUtils.h:338-358) of a natural cubic spline
+// through (x, y) (computeSplines, src/mathUtils.h:189-237), one thread per
+// flame; work: 3 doubles per point.
+__device__ double spline_integral(int n, const double* x, const double* y, double* u, double* v, double* z) {
+    // h_i and b_i are recomputed where used (same expressions, same rounding).
+    auto hh = [&](int i) { return x[i + 1] - x[i]; };
+    auto bb = [&](int i) { return (y[i + 1] - y[i]) / hh(i); };
+    u[0] = 0;
+    v[0] = 0;
+    u[1] = 2 * (hh(0) + hh(1));
+    v[1] = 6 * (bb(1) - bb(0));
+    for (int i = 2; i < n - 1; i++) {
+        u[i] = 2 * (hh(i - 1) + hh(i)) - hh(i - 1) * hh(i - 1) / u[i - 1];
+        v[i] = 6 * (bb(i) - bb(i - 1)) - hh(i - 1) * v[i - 1] / u[i - 1];
+    }
+    z[n - 1] = 0;
+    for (int i = n - 2; i > 0; i--) z[i] = (v[i] - hh(i) * z[i + 1]) / u[i];
+    z[0] = 0;
+    double I = 0;
+    for (int i = 0; i < n - 1; i++) {
+        const double h = hh(i);
+        const double c0 = y[i];
+        const double c1 = -h / 6 * z[i + 1] - h / 3 * z[i] + (y[i + 1] - y[i]) / h;
+        const double c2 = 0.5 * z[i];
+        const double c3 = (z[i + 1] - z[i]) / (6 * h);
+        const double dx = x[i + 1] - x[i];
+        I += dx * (c0 + dx * (c1 / 2 + dx * (c2 / 3 + dx * c3 / 4)));
+    }
+    return I;
+}
+
+// FlameSolver::getHeatReleaseRate / getConsumptionSpeed (src/flameSolver.cpp:
+// 951-961): Q = integral of q dx, S_c = integral of q/cp dx / (rho_u (T_b - T_u)).
+__global__ void k_flame_objectives(int n_flames, const int* __restrict__ npts, const int64_t* __restrict__ goff,
+                                   const double* __restrict__ x, const double* __restrict__ qdot,
+                                   const double* __restrict__ qcp, const double* __restrict__ T,
+                                   const double* __restrict__ rho_u, const int* __restrict__ ju,
+                                   const int* __restrict__ jb, double* __restrict__ work,
+                                   double* __restrict__ heat_release, double* __restrict__ cons_speed) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_flames) return;
+    const int n = npts[f];
+    const int64_t o = goff[f];
+    double* u = work + 3 * o;
+    double* v = u + n;
+    double* z = v + n;
+    const double Q = spline_integral(n, x + o, qdot + o, u, v, z);
+    if (heat_release) heat_release[f] = Q;
+    if (cons_speed) {
+        const double QoverCp = spline_integral(n, x + o, qcp + o, u, v, z);
+        const double rhouDeltaT = rho_u[f] * (T[o + jb[f]] - T[o + ju[f]]);
+        cons_speed[f] = QoverCp / rhouDeltaT;
+    }
+}
+
+int grid_for(int64_t n, int threads = 256) {
+    return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 4096)));
+}
+
+}  // namespace
+}  // namespace ember
+
+using namespace ember;
+
+struct ember_split_s {
+    ember_mech mech = nullptr;
+    ember_split_options opt{};
+    int n_flames = 0, n_vars = 0, nmax = 0;
+    int64_t n_pts = 0, n_vals = 0;
+    std::vector<ember_diffusion_grid> grids;
+    std::vector<DiffSysInfo> info;
+    std::vector<int64_t> h_goff;
+    // one device allocation for every fixed-size array
+    void* blob = nullptr;
+    DiffSysInfo* d_info = nullptr;
+    double* x = nullptr;
+    int64_t* vm_base = nullptr;
+    int* npt = nullptr;
+    int* flame_npts = nullptr;
+    int64_t* flame_goff = nullptr;
+    double *state = nullptr, *xD2 = nullptr, *xS = nullptr;
+    double *sc_diff = nullptr, *sc_diff_vm = nullptr, *sc_prod = nullptr;
+    double *ddt_diff = nullptr, *ddt_prod = nullptr, *ddt_cross = nullptr;
+    double *yv = nullptr, *ystart = nullptr, *delta_vm = nullptr;
+    double *B = nullptr, *D = nullptr;
+    double *dtp = nullptr, *t_dev = nullptr;
+    int *diff_status = nullptr, *src_status = nullptr, *src_stats = nullptr, *src_counter = nullptr;
+    unsigned long long* fails = nullptr;  // [0] source points, [1] diffusion systems
+    double* serial_work = nullptr;
+    void* diff_arena = nullptr;
+    size_t diff_arena_bytes = 0;
+    void* src_arena = nullptr;
+    size_t src_arena_bytes = 0;
+    bool have_cross = false;
+    DiffusionWarpPlan plan;
+    cudaStream_t capture_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+
+    SplitTables tables() const { return SplitTables{n_pts, n_vars, vm_base, npt}; }
+
+    SourceArgs source_args() const {
+        SourceArgs a = make_source_args(&opt.source, static_cast<int>(n_pts), state, sc_prod, dtp, 0.0, x, state,
+                                        src_status, src_stats);
+        a.t_start_dev = t_dev;
+        return a;
+    }
+
+    DiffusionView diffusion_view(int* status) const {
+        DiffusionView dv{};
+        dv.n_systems = static_cast<int>(info.size());
+        dv.info = d_info;
+        dv.x = x;
+        dv.B = B;
+        dv.D = D;
+        dv.split_const = sc_diff_vm;
+        dv.h = nullptr;
+        dv.wall_const = nullptr;
+        dv.y_inf = nullptr;
+        dv.status = status;
+        return dv;
+    }
+};
+
+namespace {
+
+int check_split(ember_split h) {
+    EMBER_CHECK_ARG(h != nullptr, "null ember_split handle");
+    return EMBER_OK;
+}
+
+int copy_to_device(double* dst, const double* src, size_t n, int mem, cudaStream_t st) {
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_CUDA_TRY(cudaMemcpyAsync(dst, src, n * sizeof(double),
+                                   mem == EMBER_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
+    return EMBER_OK;
+}
+
+// Two diffusion stages back to back on the variable-major copy.
+int enqueue_diffusion_pair(ember_split h, double f0, double f1, double f2, cudaStream_t st) {
+    const SplitTables tb = h->tables();
+    const int g = grid_for(h->n_vals);
+    k_to_varmajor<<<g, 256, 0, st>>>(tb, h->state, h->yv, h->ystart);
+    const DiffusionView dv = h->diffusion_view(h->diff_status);
+    const double fr[3] = {f0, f1, f2};
+    for (int k = 0; k < 2; ++k) {
+        StageTime tm;
+        tm.t_dev = h->t_dev;
+        tm.f0 = fr[k];
+        tm.f1 = fr[k + 1];
+        tm.dt = h->opt.dt;
+        if (h->opt.diffusion_algorithm == EMBER_DIFFUSION_PARALLEL) {
+            EMBER_TRY(diffusion_warp_run(h->plan, dv, h->yv, tm, h->opt.dt_multiplier, h->opt.dt, st));
+        } else {
+            EMBER_TRY(diffusion_serial_run(dv, h->yv, h->serial_work, h->n_vals, h->nmax, tm, h->opt.dt_multiplier,
+                                           h->opt.dt, st));
+        }
+        k_count_failures<<<grid_for(dv.n_systems), 256, 0, st>>>(dv.n_systems, h->diff_status, h->fails + 1);
+        k_diff_accumulate<<<g, 256, 0, st>>>(h->n_vals, h->yv, h->ystart, h->delta_vm);
+    }
+    return EMBER_OK;
+}
+
+// One split step, enqueued on `st` (kernel launches and device copies only).
+int enqueue_step(ember_split h, cudaStream_t st) {
+    const SplitTables tb = h->tables();
+    const int g = grid_for(h->n_vals);
+    k_split_begin<<<g, 256, 0, st>>>(tb, h->opt.balanced, h->ddt_diff, h->ddt_prod,
+                                     h->have_cross ? h->ddt_cross : nullptr, h->sc_diff, h->sc_diff_vm, h->sc_prod,
+                                     h->delta_vm);
+    // diffusion 1/4 and 2/4
+    EMBER_TRY(enqueue_diffusion_pair(h, 0.0, 0.25, 0.5, st));
+    k_to_pointmajor<<<g, 256, 0, st>>>(tb, h->yv, h->state, h->xD2);
+    // source term over the whole step
+    k_stage_dt<<<grid_for(h->n_pts), 256, 0, st>>>(h->n_pts, h->t_dev, h->opt.dt, h->dtp);
+    {
+        Scratch sc(st, h->src_arena, h->src_arena_bytes);
+        EMBER_CUDA_TRY(cudaMemsetAsync(h->src_counter, 0, sizeof(int), st));
+        const SourceArgs a = h->source_args();
+        if (h->opt.method == EMBER_SOURCE_QSS) {
+            EMBER_TRY(launch_source_qss(h->mech->view, a, h->src_counter, sc, st));
+        } else {
+            EMBER_TRY(launch_source_bdf(h->mech->view, a, h->src_counter, sc, st));
+        }
+    }
+    k_count_failures<<<grid_for(h->n_pts), 256, 0, st>>>(static_cast<int>(h->n_pts), h->src_status, h->fails);
+    EMBER_CUDA_TRY(cudaMemcpyAsync(h->xS, h->state, sizeof(double) * h->n_vals, cudaMemcpyDeviceToDevice, st));
+    // diffusion 3/4 and 4/4
+    EMBER_TRY(enqueue_diffusion_pair(h, 0.5, 0.75, 1.0, st));
+    k_to_pointmajor<<<g, 256, 0, st>>>(tb, h->yv, h->state, nullptr);
+    k_split_end<<<g, 256, 0, st>>>(tb, h->opt.dt, h->xS, h->xD2, h->delta_vm, h->sc_diff, h->sc_prod, h->ddt_diff,
+                                   h->ddt_prod);
+    k_correct_mass_fractions<<<grid_for(h->n_pts, 128), 128, 0, st>>>(h->n_pts, h->n_vars, h->state);
+    k_advance_clock<<<1, 32, 0, st>>>(h->t_dev, h->opt.dt);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
+void free_split(ember_split h) {
+    if (!h) return;
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
+    cudaFree(h->blob);
+    delete h;
+}
+
+}  // namespace
+
+extern "C" int ember_split_create(ember_mech mech, int n_flames, const ember_diffusion_grid* grids, const double* x,
+                                  const ember_split_options* opts, ember_split* out) {
+    EMBER_CHECK_ARG(out != nullptr, "null output handle pointer");
+    *out = nullptr;
+    EMBER_CHECK_ARG(mech != nullptr, "null mechanism");
+    EMBER_CHECK_ARG(n_flames > 0 && grids != nullptr && x != nullptr, "need at least one flame and its grid");
+    EMBER_CHECK_ARG(opts != nullptr, "null options");
+    EMBER_CHECK_ARG(opts->method == EMBER_SOURCE_QSS || opts->method == EMBER_SOURCE_BDF, "bad method %d",
+                    opts->method);
+    EMBER_CHECK_ARG(opts->diffusion_algorithm == EMBER_DIFFUSION_PARALLEL ||
+                        opts->diffusion_algorithm == EMBER_DIFFUSION_SERIAL,
+                    "bad diffusion algorithm %d", opts->diffusion_algorithm);
+    EMBER_CHECK_ARG(opts->dt > 0 && opts->dt_multiplier > 0, "dt and dt_multiplier must be positive");
+    EMBER_TRY(source_check_options(&opts->source));
+    const int n_vars = mech->S + 2;
+
+    // System table (flame-major, then variable) and the transpose tables.
+    std::vector<DiffSysInfo> info;
+    std::vector<int64_t> vm_base, goff(n_flames);
+    std::vector<int> npt, fnpts(n_flames);
+    int64_t n_pts = 0, n_vals = 0;
+    int nmax = 0;
+    for (int f = 0; f < n_flames; ++f) {
+        const ember_diffusion_grid& g = grids[f];
+        EMBER_CHECK_ARG(g.n_points >= 3, "flame %d: n_points must be >= 3 (got %d)", f, g.n_points);
+        EMBER_CHECK_ARG(g.left_bc >= 0 && g.left_bc <= 4, "flame %d: bad left_bc %d", f, g.left_bc);
+        EMBER_CHECK_ARG(g.right_bc == EMBER_BC_FIXED_VALUE || g.right_bc == EMBER_BC_ZERO_GRADIENT ||
+                            g.right_bc == EMBER_BC_FLOATING,
+                        "flame %d: bad right_bc %d", f, g.right_bc);
+        EMBER_CHECK_ARG(g.alpha >= 0, "flame %d: bad alpha %d", f, g.alpha);
+        for (int v = 0; v < n_vars; ++v) {
+            DiffSysInfo s{};
+            s.off = n_vals + int64_t(v) * g.n_points;
+            s.grid_off = n_pts;
+            s.n = g.n_points;
+            s.left_bc = g.left_bc;
+            s.right_bc = g.right_bc;
+            s.alpha = g.alpha;
+            info.push_back(s);
+        }
+        for (int i = 0; i < g.n_points; ++i) {
+            vm_base.push_back(n_vals + i);
+            npt.push_back(g.n_points);
+        }
+        goff[f] = n_pts;
+        fnpts[f] = g.n_points;
+        n_pts += g.n_points;
+        n_vals += int64_t(n_vars) * g.n_points;
+        nmax = std::max(nmax, g.n_points);
+    }
+    EMBER_CHECK_ARG(n_pts < (int64_t(1) << 31) && info.size() < (size_t(1) << 31), "batch too large");
+    EMBER_TRY(ensure_device());
+
+    // Sizes of everything the step touches, one allocation.
+    const int n_sys = static_cast<int>(info.size());
+    const bool serial = opts->diffusion_algorithm == EMBER_DIFFUSION_SERIAL;
+    const size_t plan_bytes = serial ? 0 : diffusion_warp_plan_bytes(info, n_pts);
+    SourceArgs probe = make_source_args(&opts->source, static_cast<int>(n_pts), nullptr, nullptr, nullptr, 0.0,
+                                        nullptr, nullptr, nullptr, nullptr);
+    size_t src_bytes = 0;
+    if (opts->method == EMBER_SOURCE_QSS) {
+        EMBER_TRY(source_qss_scratch_bytes(mech->view, probe, &src_bytes));
+    } else {
+        EMBER_TRY(source_bdf_scratch_bytes(mech->view, probe, &src_bytes));
+    }
+    const size_t R = Scratch::rounded(1);
+    auto bd = [&](size_t n) { return Scratch::rounded(n * sizeof(double)); };
+    const size_t total = Scratch::rounded(sizeof(DiffSysInfo) * n_sys) + bd(n_pts) +
+                         Scratch::rounded(sizeof(int64_t) * n_pts) + Scratch::rounded(sizeof(int) * n_pts) +
+                         Scratch::rounded(sizeof(int) * n_flames) + Scratch::rounded(sizeof(int64_t) * n_flames) +
+                         14 * bd(n_vals) + bd(n_pts) + bd(1) + Scratch::rounded(sizeof(int) * n_sys) +
+                         Scratch::rounded(sizeof(int) * n_pts) + Scratch::rounded(sizeof(int) * 4 * n_pts) + R +
+                         Scratch::rounded(2 * sizeof(unsigned long long)) + (serial ? bd(7 * n_vals) : 0) +
+                         plan_bytes + src_bytes;
+
+    auto* h = new ember_split_s;
+    h->mech = mech;
+    h->opt = *opts;
+    h->n_flames = n_flames;
+    h->n_vars = n_vars;
+    h->nmax = nmax;
+    h->n_pts = n_pts;
+    h->n_vals = n_vals;
+    h->grids.assign(grids, grids + n_flames);
+    h->info = info;
+    h->h_goff = goff;
+    cudaError_t e = cudaMalloc(&h->blob, total);
+    if (e == cudaSuccess) e = cudaMemset(h->blob, 0, total);  // before anything is uploaded into it
+    if (e != cudaSuccess) {
+        set_error("ember_split_create: cudaMalloc(%zu bytes) failed: %s", total, cudaGetErrorString(e));
+        free_split(h);
+        return e == cudaErrorMemoryAllocation ? EMBER_ENOMEM : EMBER_ECUDA;
+    }
+    int rc = EMBER_OK;
+    {
+        Scratch a(nullptr, h->blob, total);
+        auto carve = [&](auto** p, size_t n) {
+            if (rc == EMBER_OK) rc = a.alloc(p, n);
+        };
+        carve(&h->d_info, n_sys);
+        carve(&h->x, n_pts);
+        carve(&h->vm_base, n_pts);
+        carve(&h->npt, n_pts);
+        carve(&h->flame_npts, n_flames);
+        carve(&h->flame_goff, n_flames);
+        double** big[14] = {&h->state, &h->xD2,      &h->xS,       &h->sc_diff, &h->sc_diff_vm,
+                            &h->sc_prod, &h->ddt_diff, &h->ddt_prod, &h->ddt_cross, &h->yv,
+                            &h->ystart,  &h->delta_vm, &h->B,        &h->D};
+        for (double** q : big) carve(q, n_vals);
+        carve(&h->dtp, n_pts);
+        carve(&h->t_dev, 1);
+        carve(&h->diff_status, n_sys);
+        carve(&h->src_status, n_pts);
+        carve(&h->src_stats, 4 * n_pts);
+        carve(&h->src_counter, 1);
+        carve(&h->fails, 2);
+        if (serial) carve(&h->serial_work, 7 * n_vals);
+        if (rc == EMBER_OK && !serial) {
+            rc = diffusion_warp_plan_init(&h->plan, info, n_flames, n_vars, n_pts, a, nullptr);
+        }
+        if (rc == EMBER_OK) rc = a.alloc(reinterpret_cast<char**>(&h->src_arena), src_bytes);
+        h->src_arena_bytes = src_bytes;
+    }
+    if (rc != EMBER_OK) {
+        free_split(h);
+        return rc;
+    }
+    e = cudaMemcpy(h->d_info, info.data(), sizeof(DiffSysInfo) * n_sys, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->x, x, sizeof(double) * n_pts, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->vm_base, vm_base.data(), sizeof(int64_t) * n_pts, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->npt, npt.data(), sizeof(int) * n_pts, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->flame_npts, fnpts.data(), sizeof(int) * n_flames, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->flame_goff, goff.data(), sizeof(int64_t) * n_flames, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        set_error("ember_split_create: %s", cudaGetErrorString(e));
+        free_split(h);
+        return EMBER_ECUDA;
+    }
+    if (!serial) {
+        // the plan's tables were queued on the legacy stream; wait for them
+        rc = diffusion_warp_geometry(h->plan, h->d_info, h->x, nullptr);
+        if (rc == EMBER_OK && cudaDeviceSynchronize() != cudaSuccess) {
+            set_error("ember_split_create: %s", cudaGetErrorString(cudaGetLastError()));
+            rc = EMBER_ECUDA;
+        }
+        if (rc != EMBER_OK) {
+            free_split(h);
+            return rc;
+        }
+    }
+    *out = h;
+    return EMBER_OK;
+}
+
+extern "C" int ember_split_destroy(ember_split h) {
+    free_split(h);
+    return EMBER_OK;
+}
+
+extern "C" int ember_split_set_state(ember_split h, double t, const double* state, int mem, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(state != nullptr, "null state");
+    cudaStream_t st = as_stream(stream);
+    EMBER_TRY(copy_to_device(h->state, state, size_t(h->n_vals), mem, st));
+    EMBER_CUDA_TRY(cudaMemcpyAsync(h->t_dev, &t, sizeof(double), cudaMemcpyHostToDevice, st));
+    EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_diff, 0, sizeof(double) * h->n_vals, st));
+    EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_prod, 0, sizeof(double) * h->n_vals, st));
+    EMBER_CUDA_TRY(cudaMemsetAsync(h->fails, 0, 2 * sizeof(unsigned long long), st));
+    // the host value of t must outlive the copy
+    EMBER_CUDA_TRY(cudaStreamSynchronize(st));
+    return EMBER_OK;
+}
+
+extern "C" int ember_split_set_transport(ember_split h, const double* B, const double* D, const double* ddt_cross,
+                                         int mem, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(B != nullptr && D != nullptr, "null B or D");
+    cudaStream_t st = as_stream(stream);
+    EMBER_TRY(copy_to_device(h->B, B, size_t(h->n_vals), mem, st));
+    EMBER_TRY(copy_to_device(h->D, D, size_t(h->n_vals), mem, st));
+    if (ddt_cross) {
+        EMBER_TRY(copy_to_device(h->ddt_cross, ddt_cross, size_t(h->n_vals), mem, st));
+    } else {
+        EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_cross, 0, sizeof(double) * h->n_vals, st));
+    }
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_split_step(ember_split h, int n_steps, int use_graph, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(n_steps >= 0, "n_steps must be >= 0");
+    cudaStream_t st = as_stream(stream);
+    if (!use_graph) {
+        for (int k = 0; k < n_steps; ++k) EMBER_TRY(enqueue_step(h, st));
+        return EMBER_OK;
+    }
+    if (!h->graph_exec) {
+        EMBER_CUDA_TRY(cudaStreamBeginCapture(h->capture_stream, cudaStreamCaptureModeRelaxed));
+        const int rc = enqueue_step(h, h->capture_stream);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(h->capture_stream, &g);
+        if (rc != EMBER_OK) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        EMBER_CUDA_TRY(e);
+        h->graph = g;
+        EMBER_CUDA_TRY(cudaGraphInstantiate(&h->graph_exec, h->graph, 0));
+    }
+    for (int k = 0; k < n_steps; ++k) EMBER_CUDA_TRY(cudaGraphLaunch(h->graph_exec, st));
+    return EMBER_OK;
+}
+
+extern "C" int ember_split_get_state(ember_split h, double* state, double* t, int mem, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    cudaStream_t st = as_stream(stream);
+    const cudaMemcpyKind kind = mem == EMBER_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (state) EMBER_CUDA_TRY(cudaMemcpyAsync(state, h->state, sizeof(double) * h->n_vals, kind, st));
+    if (t) EMBER_CUDA_TRY(cudaMemcpyAsync(t, h->t_dev, sizeof(double), kind, st));
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_split_get_derivatives(ember_split h, double* ddt_diff, double* ddt_prod, int mem, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    cudaStream_t st = as_stream(stream);
+    const cudaMemcpyKind kind = mem == EMBER_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (ddt_diff) EMBER_CUDA_TRY(cudaMemcpyAsync(ddt_diff, h->ddt_diff, sizeof(double) * h->n_vals, kind, st));
+    if (ddt_prod) EMBER_CUDA_TRY(cudaMemcpyAsync(ddt_prod, h->ddt_prod, sizeof(double) * h->n_vals, kind, st));
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_split_source_status(ember_split h, int* status, int* stats, int mem, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    cudaStream_t st = as_stream(stream);
+    const cudaMemcpyKind kind = mem == EMBER_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (status) EMBER_CUDA_TRY(cudaMemcpyAsync(status, h->src_status, sizeof(int) * h->n_pts, kind, st));
+    if (stats) EMBER_CUDA_TRY(cudaMemcpyAsync(stats, h->src_stats, sizeof(int) * 4 * h->n_pts, kind, st));
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_split_failures(ember_split h, int64_t* source_points, int64_t* diffusion_systems,
+                                    void* stream) {
+    EMBER_TRY(check_split(h));
+    cudaStream_t st = as_stream(stream);
+    unsigned long long f[2] = {0, 0};
+    EMBER_CUDA_TRY(cudaMemcpyAsync(f, h->fails, sizeof(f), cudaMemcpyDeviceToHost, st));
+    EMBER_CUDA_TRY(cudaStreamSynchronize(st));
+    if (source_points) *source_points = static_cast<int64_t>(f[0]);
+    if (diffusion_systems) *diffusion_systems = static_cast<int64_t>(f[1]);
+    return EMBER_OK;
+}
+
+extern "C" int ember_split_objectives(ember_split h, const double* rho_u, const int* ju, const int* jb,
+                                      double* qdot, double* heat_release, double* consumption_speed, int mem,
+                                      void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_CHECK_ARG(!consumption_speed || (rho_u && ju && jb), "consumption speed needs rho_u, ju and jb");
+    if (consumption_speed && mem == EMBER_MEM_HOST) {
+        for (int f = 0; f < h->n_flames; ++f)
+            EMBER_CHECK_ARG(ju[f] >= 0 && ju[f] < h->grids[f].n_points && jb[f] >= 0 && jb[f] < h->grids[f].n_points,
+                            "flame %d: ju/jb out of range", f);
+    }
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    const int S = h->mech->S;
+    double *T, *Y, *net, *hk, *cp, *q, *qcp, *work;
+    EMBER_TRY(sc.alloc(&T, h->n_pts));
+    EMBER_TRY(sc.alloc(&Y, size_t(h->n_pts) * S));
+    EMBER_TRY(sc.alloc(&net, size_t(h->n_pts) * S));
+    EMBER_TRY(sc.alloc(&hk, size_t(h->n_pts) * S));
+    EMBER_TRY(sc.alloc(&cp, h->n_pts));
+    EMBER_TRY(sc.alloc(&qcp, h->n_pts));
+    EMBER_TRY(sc.alloc(&work, 3 * h->n_pts));
+    EMBER_TRY(stage_buffer(sc, qdot, size_t(h->n_pts), mem, &q));
+    if (!q) EMBER_TRY(sc.alloc(&q, h->n_pts));
+    double *hr = nullptr, *cs = nullptr;
+    EMBER_TRY(stage_buffer(sc, heat_release, size_t(h->n_flames), mem, &hr));
+    EMBER_TRY(stage_buffer(sc, consumption_speed, size_t(h->n_flames), mem, &cs));
+    const double* d_rho = nullptr;
+    const int *d_ju = nullptr, *d_jb = nullptr;
+    if (consumption_speed) {
+        EMBER_TRY(stage_in(sc, rho_u, size_t(h->n_flames), mem, st, &d_rho));
+        EMBER_TRY(stage_in(sc, ju, size_t(h->n_flames), mem, st, &d_ju));
+        EMBER_TRY(stage_in(sc, jb, size_t(h->n_flames), mem, st, &d_jb));
+    }
+    k_gather_TY<<<grid_for(h->n_pts * S), 256, 0, st>>>(h->n_pts, h->n_vars, h->state, T, Y);
+    EMBER_TRY(ember_gas_eval(h->mech, static_cast<int>(h->n_pts), h->opt.source.pressure,
+                             h->opt.source.kinetics_model, EMBER_STATE_NORMALIZED, T, Y, nullptr, nullptr, net, hk,
+                             cp, nullptr, EMBER_MEM_DEVICE, stream));
+    k_qdot<<<grid_for(h->n_pts, 128), 128, 0, st>>>(h->n_pts, S, net, hk, cp, q, qcp);
+    if (hr || cs)
+        k_flame_objectives<<<blocks_for(h->n_flames, 64), 64, 0, st>>>(h->n_flames, h->flame_npts, h->flame_goff, h->x,
+                                                                        q, qcp, T, d_rho, d_ju, d_jb, work, hr, cs);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    EMBER_TRY(stage_out(qdot, q, size_t(h->n_pts), mem, st));
+    EMBER_TRY(stage_out(heat_release, hr, size_t(h->n_flames), mem, st));
+    EMBER_TRY(stage_out(consumption_speed, cs, size_t(h->n_flames), mem, st));
+    sc.release();
+    return finish_call(mem, st);
+}

@@ -103,10 +103,12 @@ __global__ void k_diffusion_rows(DiffusionView v) {
 
 // Step size rule of setDiffusionSolverState followed by initialize(t0, h) and
 // integrateToTime(t1), one thread per system.
-__global__ void k_diffusion_integrate_serial(DiffusionView v, TriBatchView tb, double t0, double t1,
-                                             double mult, double gdt) {
+__global__ void k_diffusion_integrate_serial(DiffusionView v, TriBatchView tb, StageTime tm, double mult,
+                                             double gdt) {
     int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= v.n_systems) return;
+    double t0, t1;
+    tm.get(t0, t1);
     const DiffSysInfo info = v.info[s];
     double h;
     if (v.h) {
@@ -306,6 +308,38 @@ extern "C" int ember_tridiag_get_ydot(ember_tridiag b, double* ydot, int mem, vo
 
 // ------------------------------------------------------ C ABI: diffusion --
 
+namespace ember {
+
+int diffusion_serial_run(const DiffusionView& dv_in, double* y, double* work, int64_t n_vals, int nmax,
+                         const StageTime& tm, double mult, double gdt, cudaStream_t st) {
+    // Matrix rows and integrator workspace (a b c k | y_prev lu_c 1/den).
+    DiffusionView dv = dv_in;
+    dv.a = work;
+    dv.b = work + n_vals;
+    dv.c = work + 2 * n_vals;
+    dv.k = work + 3 * n_vals;
+    const int n_sys = dv.n_systems;
+    dim3 grid_rows(std::min(blocks_for(nmax, 256), 32), std::min(n_sys, 65535));
+    k_diffusion_rows<<<grid_rows, 256, 0, st>>>(dv);
+    TriBatchView tb;
+    tb.n_systems = n_sys;
+    tb.off = nullptr;
+    tb.info = dv.info;
+    tb.a = dv.a;
+    tb.b = dv.b;
+    tb.c = dv.c;
+    tb.k = dv.k;
+    tb.y = y;
+    tb.yprev = work + 4 * n_vals;
+    tb.luc = work + 5 * n_vals;
+    tb.inv = work + 6 * n_vals;
+    k_diffusion_integrate_serial<<<blocks_for(n_sys, 64), 64, 0, st>>>(dv, tb, tm, mult, gdt);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
+}  // namespace ember
+
 extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_grid* grids, int n_vars,
                                          const double* x, const double* B, const double* D,
                                          const double* split_const, double* y,
@@ -374,36 +408,21 @@ extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_gri
         EMBER_CUDA_TRY(cudaMemcpyAsync(d_y, y, sizeof(double) * n_vals, cudaMemcpyHostToDevice, st));
     }
 
+    StageTime tm;
+    tm.t0 = opts->t_start;
+    tm.t1 = opts->t_end;
     if (opts->algorithm == EMBER_DIFFUSION_PARALLEL) {
-        EMBER_TRY(launch_diffusion_warp(dv, n_flames, n_vars, info, n_pts, d_y, opts->t_start, opts->t_end,
-                                        opts->dt_multiplier, opts->global_timestep, sc, st));
+        DiffusionWarpPlan plan;
+        EMBER_TRY(diffusion_warp_plan_init(&plan, info, n_flames, n_vars, n_pts, sc, st));
+        EMBER_TRY(diffusion_warp_geometry(plan, d_info, dv.x, st));
+        EMBER_TRY(diffusion_warp_run(plan, dv, d_y, tm, opts->dt_multiplier, opts->global_timestep, st));
     } else {
-        // Matrix rows and integrator workspace.
         double* work = nullptr;
         EMBER_TRY(sc.alloc(&work, size_t(7) * n_vals));
-        dv.a = work;
-        dv.b = work + n_vals;
-        dv.c = work + 2 * n_vals;
-        dv.k = work + 3 * n_vals;
         int nmax = 0;
         for (int f = 0; f < n_flames; ++f) nmax = std::max(nmax, grids[f].n_points);
-        dim3 grid_rows(std::min(blocks_for(nmax, 256), 32), std::min(n_sys, 65535));
-        k_diffusion_rows<<<grid_rows, 256, 0, st>>>(dv);
-
-        TriBatchView tb;
-        tb.n_systems = n_sys;
-        tb.off = nullptr;
-        tb.info = d_info;
-        tb.a = dv.a;
-        tb.b = dv.b;
-        tb.c = dv.c;
-        tb.k = dv.k;
-        tb.y = d_y;
-        tb.yprev = work + 4 * n_vals;
-        tb.luc = work + 5 * n_vals;
-        tb.inv = work + 6 * n_vals;
-        k_diffusion_integrate_serial<<<blocks_for(n_sys, 64), 64, 0, st>>>(
-            dv, tb, opts->t_start, opts->t_end, opts->dt_multiplier, opts->global_timestep);
+        EMBER_TRY(diffusion_serial_run(dv, d_y, work, n_vals, nmax, tm, opts->dt_multiplier, opts->global_timestep,
+                                       st));
     }
     if (mem == EMBER_MEM_HOST) {
         EMBER_CUDA_TRY(cudaMemcpyAsync(y, d_y, sizeof(double) * n_vals, cudaMemcpyDeviceToHost, st));
@@ -565,8 +584,11 @@ extern "C" int ember_diffusion_integrate_noalloc(int n_flames, const ember_diffu
     tb.yprev = work + 4 * int64_t(EMBER_NOALLOC_MAX_VALUES);
     tb.luc = work + 5 * int64_t(EMBER_NOALLOC_MAX_VALUES);
     tb.inv = work + 6 * int64_t(EMBER_NOALLOC_MAX_VALUES);
-    k_diffusion_integrate_serial<<<blocks_for(n_sys, 64), 64, 0, st>>>(dv, tb, opts->t_start, opts->t_end,
-                                                                        opts->dt_multiplier, opts->global_timestep);
+    StageTime tm;
+    tm.t0 = opts->t_start;
+    tm.t1 = opts->t_end;
+    k_diffusion_integrate_serial<<<blocks_for(n_sys, 64), 64, 0, st>>>(dv, tb, tm, opts->dt_multiplier,
+                                                                        opts->global_timestep);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }

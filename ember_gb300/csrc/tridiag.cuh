@@ -94,6 +94,27 @@ struct DiffusionView {
     int* status;
 };
 
+// Interval [t0, t1] of one diffusion stage: given on the host, or read from a
+// device clock t (for graph replays, where launch parameters are fixed):
+// t0 = t + f0*dt (t itself when f0 == 0) and t1 = t + f1*dt, the stage
+// boundaries of SplitSolver::integrateSplitTerms (src/splitSolver.cpp:60-75).
+struct StageTime {
+    double t0 = 0.0, t1 = 0.0;
+    const double* t_dev = nullptr;
+    double f0 = 0.0, f1 = 0.0, dt = 0.0;
+
+    __device__ void get(double& a, double& b) const {
+        if (t_dev) {
+            const double t = *t_dev;
+            a = f0 == 0.0 ? t : t + f0 * dt;
+            b = t + f1 * dt;
+        } else {
+            a = t0;
+            b = t1;
+        }
+    }
+};
+
 // Status codes of one system.
 enum : int {
     TRI_OK = 0,
@@ -271,12 +292,36 @@ __device__ __forceinline__ double diffusion_step_size(int N, const double* x, co
     return gdt < h ? gdt : h;  // std::min(h, gdt)
 }
 
-// Warp-parallel diffusion stage (diffusion_warp.cu): the rows, step size and
-// integration of every system of `dv` with one warp per system; the state
-// `y` (device, variable-major per flame) is updated in place. `info` is the
-// host copy of dv.info, `n_pts` the number of grid points of all flames.
-int launch_diffusion_warp(const DiffusionView& dv, int n_flames, int n_vars, const std::vector<DiffSysInfo>& info,
-                          int64_t n_pts, double* y, double t0, double t1, double mult, double gdt, Scratch& sc,
-                          cudaStream_t st);
+// Warp-parallel diffusion stage (diffusion_warp.cu). A plan holds the
+// per-system workspace, the geometric factors of every grid point, the
+// largest-first order and the work counter of one batch of flames.
+struct DiffusionWarpPlan {
+    int n_sys = 0, n_flames = 0, n_vars = 0, nmax = 0;
+    int64_t n_pts = 0;
+    int64_t warps = 0;
+    double* ws = nullptr;
+    double2* geo = nullptr;
+    int64_t* ws_off = nullptr;
+    int* order = nullptr;
+    unsigned int* counter = nullptr;
+};
+
+// Allocate the plan's buffers from `sc` and upload its tables (host copies of
+// the system descriptors in `info`).
+int diffusion_warp_plan_init(DiffusionWarpPlan* p, const std::vector<DiffSysInfo>& info, int n_flames, int n_vars,
+                             int64_t n_pts, Scratch& sc, cudaStream_t st);
+// Bytes diffusion_warp_plan_init takes from its Scratch.
+size_t diffusion_warp_plan_bytes(const std::vector<DiffSysInfo>& info, int64_t n_pts);
+// Geometric factors of every grid point (x: all flames' coordinates).
+int diffusion_warp_geometry(const DiffusionWarpPlan& p, const DiffSysInfo* d_info, const double* x, cudaStream_t st);
+// One stage: rows, step size and integration of every system of `dv`, with
+// one warp per system; `y` (device, variable-major per flame) in place.
+int diffusion_warp_run(const DiffusionWarpPlan& p, const DiffusionView& dv, double* y, const StageTime& tm,
+                       double mult, double gdt, cudaStream_t st);
+
+// Serial (bitwise reference order) stage on a device workspace of
+// 7 * n_vals doubles: rows, then one thread per system (tridiag.cu).
+int diffusion_serial_run(const DiffusionView& dv, double* y, double* work, int64_t n_vals, int nmax,
+                         const StageTime& tm, double mult, double gdt, cudaStream_t st);
 
 }  // namespace ember

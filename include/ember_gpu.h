@@ -349,6 +349,81 @@ int ember_selftest_qss_cesium(double epsmin, double epsmax, double dtmin, double
                               int itermax, int stability_check, double tf, int max_steps, double* y7,
                               int* stats);
 
+/* ======================================================================
+ * Split step of a batch of flames on the device
+ *
+ * One ember_split_step = SplitSolver::step for every flame of the batch
+ * (src/splitSolver.cpp:34-121): split constants from the previous step's
+ * time derivatives; diffusion over [t, t+dt/4] and [t+dt/4, t+dt/2]; source
+ * term over [t, t+dt]; diffusion over [t+dt/2, t+3dt/4] and [t+3dt/4, t+dt];
+ * time derivatives ddt = delta/dt - split constant
+ * (SplitSolver::calculateTimeDerivatives, 27-32); the mass-fraction
+ * correction of FlameSolver::finishStep (src/flameSolver.cpp:219-224,
+ * 942-949); t += dt. The stage hooks are those of FlameSolver
+ * (integrateDiffusionTerms / integrateProductionTerms, src/flameSolver.cpp:
+ * 702-854), batched over flames.
+ *
+ * Not integrated here: the convection stages (ConvectionSystemSplit is not
+ * part of this library). A caller that runs them supplies their rate through
+ * ddt_cross. With balanced splitting the split constants of the two
+ * integrated operators give each half of the total rate,
+ *   c_diff = (ddt_prod + ddt_cross - ddt_diff) / 2,
+ *   c_prod = (ddt_diff + ddt_cross - ddt_prod) / 2
+ * (the reference's three-operator rule gives 1/4, 1/4, 1/2); without it,
+ * c_diff = ddt_cross and c_prod = 0 as in the reference.
+ *
+ * The state is point-major [n_points][S+2] (U, T, Y_0..), flames
+ * concatenated, as FlameSolver::state. B and D are the diffusion
+ * coefficients of every (flame, variable) row, variable-major per flame as
+ * in ember_diffusion_integrate (DiffusionSystem::B, D: 1/rho and mu for U,
+ * 1/(rho cp) and lambda for T, 1/rho and rho D_k for Y_k,
+ * src/flameSolver.cpp:160-172); they are held fixed until the next
+ * ember_split_set_transport. Every array lives on the device between calls;
+ * a step launches kernels and device copies only, so it can be captured:
+ * ember_split_step(.., use_graph = 1, ..) captures one step into a CUDA graph
+ * on first use and replays it (stage times come from a device clock).
+ * ==================================================================== */
+typedef struct ember_split_s* ember_split;
+
+typedef struct {
+    int method;                  /* EMBER_SOURCE_QSS or EMBER_SOURCE_BDF           */
+    int diffusion_algorithm;     /* EMBER_DIFFUSION_PARALLEL or _SERIAL            */
+    int balanced;                /* splittingMethod == "balanced"                  */
+    double dt;                   /* options.globalTimestep                         */
+    double dt_multiplier;        /* options.diffusionTimestepMultiplier (10)       */
+    ember_source_options source; /* source-term options                            */
+} ember_split_options;
+
+/* grids / x (host): the flames' grids (x concatenated). The mechanism must
+ * outlive the split object. */
+int ember_split_create(ember_mech mech, int n_flames, const ember_diffusion_grid* grids, const double* x,
+                       const ember_split_options* opts, ember_split* out);
+int ember_split_destroy(ember_split split);
+/* State at time t; resets the time derivatives (and so the split
+ * constants of the next step) and the failure counters. */
+int ember_split_set_state(ember_split split, double t, const double* state, int mem, void* stream);
+/* B, D: variable-major per flame; ddt_cross: point-major or NULL (zero). */
+int ember_split_set_transport(ember_split split, const double* B, const double* D, const double* ddt_cross,
+                              int mem, void* stream);
+/* n_steps split steps, asynchronous on `stream`. */
+int ember_split_step(ember_split split, int n_steps, int use_graph, void* stream);
+int ember_split_get_state(ember_split split, double* state, double* t, int mem, void* stream);
+/* ddtDiff and ddtProd of the last step, point-major. */
+int ember_split_get_derivatives(ember_split split, double* ddt_diff, double* ddt_prod, int mem, void* stream);
+/* Source-stage status [n_points] and stats [n_points][EMBER_STATS_WIDTH] of the last step. */
+int ember_split_source_status(ember_split split, int* status, int* stats, int mem, void* stream);
+/* Failed source points and diffusion systems summed over the steps since
+ * ember_split_set_state (synchronises `stream`). */
+int ember_split_failures(ember_split split, int64_t* source_points, int64_t* diffusion_systems, void* stream);
+/* FlameSolver::calculateQdot / getHeatReleaseRate / getConsumptionSpeed
+ * (src/flameSolver.cpp:926-961) of the current state: qdot [n_points]
+ * (W/m^3), heat_release [n_flames] (integral of qdot dx, natural cubic
+ * spline as mathUtils::integrate) and consumption_speed [n_flames]
+ * (integral of qdot/cp dx / (rho_u (T[jb] - T[ju]))); any output may be
+ * NULL; rho_u, ju, jb (per flame) are needed for the consumption speed. */
+int ember_split_objectives(ember_split split, const double* rho_u, const int* ju, const int* jb, double* qdot,
+                           double* heat_release, double* consumption_speed, int mem, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
