@@ -64,6 +64,8 @@ def _declare(lib):
                                                 C.POINTER(DiffusionOptions), vp, C.c_int, vp]),
         "ember_diffusion_integrate_noalloc": (C.c_int, [C.c_int, C.POINTER(DiffusionGrid), C.c_int, vp, vp, vp,
                                                         vp, vp, C.POINTER(DiffusionOptions), vp, vp]),
+        "ember_diffusion_adjoint": (C.c_int, [C.c_int, C.POINTER(DiffusionGrid), C.c_int, vp, vp, vp, vp,
+                                              C.POINTER(DiffusionOptions), vp, C.c_int, vp]),
         "ember_probe_fp64_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
         "ember_mech_create": (C.c_int, [vp, C.POINTER(vp)]),
         "ember_mech_destroy": (C.c_int, [vp]),
@@ -75,6 +77,8 @@ def _declare(lib):
                                                 C.c_int, C.c_int, C.c_double, C.c_int, vp, vp]),
         "ember_source_integrate": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp, vp, vp,
                                              C.c_int, vp]),
+        "ember_source_adjoint": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp, C.c_int, vp, vp, vp, vp,
+                                           C.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -66,6 +66,7 @@ struct BdfPoint {
     double rho, cp, qdot;
     double cachedT;
     int nfe;
+    double* tape;  // this point's tape, or null
 
     __device__ double atol(int i) const { return i == 0 ? a->bdf_atol_u : (i == 1 ? a->bdf_atol_t : a->bdf_atol_y); }
 
@@ -157,9 +158,12 @@ struct BdfPoint {
                     dropdm = rf * (pf - kr * pp);
                     rf = rf * w.concm[slot];
                 } else if (ty == RXN_LINDEMANN || ty == RXN_TROE) {
+                    // d/d[M] of kinf mult Pr/(1+Pr) F(Pr), Pr = k0 [M] / kinf
                     const int fs = m.tb_fo[slot];
                     const double pr1 = 1.0 + w.fo_pr[fs];
-                    dropdm = ((w.fo_F[fs] * (w.fo_k0[fs] * m.mult[i])) / (pr1 * pr1)) * (pf - kr * pp);
+                    const double k0m = w.fo_k0[fs] * m.mult[i];
+                    dropdm = ((w.fo_F[fs] * k0m) / (pr1 * pr1) + (k0m * (w.fo_pr[fs] / pr1)) * w.fo_dF[fs]) *
+                             (pf - kr * pp);
                 }
                 double dv[8];
                 int dj[8];
@@ -333,6 +337,69 @@ struct BdfPoint {
         return 0;
     }
 
+    // Solve M^T w = b in place with the factors and pivots of lu_factor
+    // (P M = L U, so M^T = U^T L^T P): U^T forward, L^T backward, then the
+    // row interchanges undone in reverse order.
+    __device__ void lu_solve_transpose(double* b) {
+        const int tid = threadIdx.x;
+        for (int k = 0; k < n; ++k) {
+            const double zk = b[k] / M[size_t(k) * n + k];
+            __syncthreads();
+            if (tid == 0) b[k] = zk;
+            for (int j = k + 1 + tid; j < n; j += NT) b[j] = fma(-M[size_t(j) * n + k], zk, b[j]);
+            __syncthreads();
+        }
+        for (int k = n - 1; k >= 1; --k) {
+            const double uk = b[k];
+            for (int i = tid; i < k; i += NT) b[i] = fma(-M[size_t(i) * n + k], uk, b[i]);
+            __syncthreads();
+        }
+        if (tid == 0)
+            for (int k = n - 1; k >= 0; --k) {
+                const int p = v.piv[k];
+                if (p != k) {
+                    const double tt = b[k];
+                    b[k] = b[p];
+                    b[p] = tt;
+                }
+            }
+        __syncthreads();
+    }
+
+    // out = J^T vec (J column-major: column c holds d f_r / d y_c).
+    __device__ void jacobian_transpose_times(const double* vec, double* out, bool accumulate) {
+        for (int c = threadIdx.x; c < n; c += NT) {
+            const double* col = J + size_t(c) * n;
+            double acc = 0.0;
+            for (int r = 0; r < n; ++r) acc = fma(col[r], vec[r], acc);
+            out[c] = accumulate ? out[c] + acc : acc;
+        }
+        __syncthreads();
+    }
+
+    // pbar_i += vec . d f / d ln(multiplier_i) at the state of the last f()
+    // call: reaction i's net rate of progress r_i enters dY_k/dt as
+    // nu_ki r_i W_k / rho and dT/dt as -(sum_k nu_ki h_k) r_i / (rho cp).
+    __device__ void multiplier_vjp(const double* vec, double* pbar) {
+        const double rrho = 1.0 / rho, rrc = 1.0 / (rho * cp);
+        for (int i = threadIdx.x; i < m.R; i += NT) {
+            const double r = w.ropf[i] - w.ropr[i];
+            const int4 st = m.stoich[i];
+            const int sp[8] = {unpack_lo(st.x), unpack_hi(st.x), unpack_lo(st.y), unpack_hi(st.y),
+                               unpack_lo(st.z), unpack_hi(st.z), unpack_lo(st.w), unpack_hi(st.w)};
+            double ey = 0.0, eh = 0.0;
+#pragma unroll
+            for (int o = 0; o < 8; ++o) {
+                const int k = sp[o];
+                if (k == 0xffff) continue;
+                const double sg = o < 4 ? -1.0 : 1.0;
+                ey = fma(sg * m.W[k], vec[2 + k], ey);
+                eh = fma(sg, w.hk[k], eh);
+            }
+            pbar[i] += r * (ey * rrho - eh * (vec[1] * rrc));
+        }
+    }
+
     __device__ void lu_solve(double* b) {
         const int tid = threadIdx.x;
         if (tid == 0)
@@ -440,6 +507,7 @@ __device__ int bdf_integrate(BdfPoint<NT>& P, double tf, double t_start, int* st
 
     int q = 1, qwait = 2, nstlp = 0, nstlj = 0, qsave = 0;
     bool have_m = false, have_acorp = false;
+    bool restart_pending = false;  // for the tape: a q = 1 restart since the last accepted step
     double gammap = 0.0, crate = 1.0, etamax = 10000.0, acnrm = 0.0, hsave = 0.0;
     double l[kQmax + 2];
 
@@ -552,6 +620,7 @@ __device__ int bdf_integrate(BdfPoint<NT>& P, double tf, double t_start, int* st
                     const double eta = dmaxr(0.1, hmin / h);
                     h *= eta;
                     q = 1;
+                    restart_pending = true;
                     P.f(t_start + t, v.z[0], v.ft);
                     for (int i = tid; i < n; i += NT) v.z[1][i] = h * v.ft[i];
                 }
@@ -597,6 +666,17 @@ __device__ int bdf_integrate(BdfPoint<NT>& P, double tf, double t_start, int* st
         for (int j = 0; j <= q; ++j)
             for (int i = tid; i < n; i += NT) v.z[j][i] = fma(l[j], v.acor[i], v.z[j][i]);
         set_ewt(v.z[0]);
+        if (P.tape && nst <= a.tape_cap) {
+            double* rec = P.tape + kTapeHeader + int64_t(nst - 1) * (n + 4);
+            if (tid == 0) {
+                rec[0] = t;
+                rec[1] = h;
+                rec[2] = q;
+                rec[3] = restart_pending ? 1.0 : 0.0;
+            }
+            for (int i = tid; i < n; i += NT) rec[4 + i] = v.z[0][i];
+        }
+        restart_pending = false;
         __syncthreads();
         const double etaq = 1.0 / (bdf_pow(6.0 * dsm, 1.0 / (q + 1)) + 1e-6);
         double eta = etaq;
@@ -673,6 +753,14 @@ __device__ int bdf_integrate(BdfPoint<NT>& P, double tf, double t_start, int* st
         for (int i = tid; i < n; i += NT) v.y[i] = v.z[0][i];
     }
     __syncthreads();
+    if (P.tape && tid == 0) {
+        P.tape[0] = nst < a.tape_cap ? nst : a.tape_cap;
+        P.tape[1] = q;
+        P.tape[2] = t;
+        P.tape[3] = nst > a.tape_cap ? 1.0 : 0.0;
+        P.tape[4] = status;
+        P.tape[5] = tf;
+    }
     stats[0] = nst;
     stats[1] = P.nfe;
     stats[2] = nef_total + ncf_total;
@@ -692,7 +780,8 @@ __global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int
     P.w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), m, true);
     P.w.fo_F = smem + cd;
     P.w.fo_pr = P.w.fo_F + m.n_fo;
-    P.v.carve(P.w.fo_pr + m.n_fo, n);
+    P.w.fo_dF = P.w.fo_pr + m.n_fo;
+    P.v.carve(P.w.fo_dF + m.n_fo, n);
     P.a = &a;
     P.n = n;
     P.S = m.S;
@@ -713,6 +802,7 @@ __global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int
         for (int i = tid; i < n; i += NT) P.v.z[0][i] = yin[i];
         P.split = a.split ? a.split + size_t(j) * n : nullptr;
         P.x = a.x ? a.x[j] : 0.0;
+        P.tape = a.tape ? a.tape + size_t(j) * a.tape_stride : nullptr;
         __syncthreads();
         int st4[4];
         int ret = bdf_integrate<NT>(P, a.dt[j], a.t_start_dev ? *a.t_start_dev : a.t_start, st4);
@@ -737,7 +827,7 @@ __global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int
 template <int NT>
 static int bdf_config(const MechView& m, const SourceArgs& a, size_t* per_out, int* blocks_out) {
     const int n = m.S + 2;
-    const size_t per = (ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(2) * m.n_fo +
+    const size_t per = (ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(3) * m.n_fo +
                         BdfSmem::doubles(n)) * sizeof(double);
     EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the BDF shared-memory work area (%zu B)", per);
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_bdf<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
@@ -788,6 +878,351 @@ static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, S
     return EMBER_OK;
 }
 
+// ------------------------------------------------------------------ adjoint --
+//
+// Discrete adjoint of the BDF integration of one point, replayed backwards
+// over the tape of its accepted steps. Each step is linearised with the step
+// sizes, orders and the converged corrector held fixed:
+//   predictor   z_p = Pascal(z)                         (transpose: reversed sums)
+//   corrector   acor = gamma f(z_p0 + acor) - z_p1 / l1, so
+//               (I - gamma J) d acor = gamma J d z_p0 - d z_p1 / l1 + gamma f_p d p
+//   update      z_j = z_pj + l_j acor,  order increase  z_{q+1} = l_q/(q+1) acor
+//   rescaling   z_j *= (h_next/h)^j, or a q = 1 restart z = [z0, h f(z0)]
+//   start       z = [y0, h0 f(y0)],  end  y(tf) = sum_j z_j s^j.
+// J is the analytic Jacobian (exact falloff derivative, forward-difference
+// temperature column) at the step's end state, recomputed from the tape; the
+// transposed solve reuses the LU of I - gamma J. The gradient with respect to
+// ln(multiplier_i) of every reaction is accumulated per point.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_source_bdf_adjoint(MechView m, SourceArgs a, int* counter, double* kcache,
+                                                          double* jm, const double* __restrict__ ybar_out,
+                                                          double* __restrict__ ybar_in, double* __restrict__ pbar,
+                                                          int* __restrict__ adj_status) {
+    extern __shared__ double smem[];
+    __shared__ int next_point;
+    const int n = m.S + 2;
+    const size_t cd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true);
+    BdfPoint<NT> P;
+    P.m = m;
+    P.w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), m, true);
+    P.w.fo_F = smem + cd;
+    P.w.fo_pr = P.w.fo_F + m.n_fo;
+    P.w.fo_dF = P.w.fo_pr + m.n_fo;
+    P.v.carve(P.w.fo_dF + m.n_fo, n);
+    P.a = &a;
+    P.n = n;
+    P.S = m.S;
+    P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
+    P.M = P.J + size_t(n) * n;
+    P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
+    P.tape = nullptr;
+    BdfSmem& v = P.v;
+    double* const* zb = v.z;  // adjoint of the Nordsieck array
+    const int tid = threadIdx.x;
+    const double t_start = a.t_start_dev ? *a.t_start_dev : a.t_start;
+    for (;;) {
+        if (tid == 0) {
+            const int slot = atomicAdd(counter, 1);
+            next_point = slot < a.n ? slot : a.n;
+        }
+        __syncthreads();
+        const int j = next_point;
+        __syncthreads();
+        if (j >= a.n) break;
+        const double* tape = a.tape + size_t(j) * a.tape_stride;
+        double* pb = pbar + size_t(j) * m.R;
+        for (int i = tid; i < m.R; i += NT) pb[i] = 0.0;
+        const int N = static_cast<int>(tape[0]);
+        const int fstat = static_cast<int>(tape[4]);
+        int status = 0;
+        if (tape[3] != 0.0) status = -30;  // tape overflow
+        if (fstat != 0) status = fstat;
+        if (N < 1 && status == 0) status = -31;
+        if (status != 0) {
+            for (int i = tid; i < n; i += NT) ybar_in[size_t(j) * n + i] = 0.0;
+            if (tid == 0) adj_status[j] = status;
+            __syncthreads();
+            continue;
+        }
+        const int rec_len = n + 4;
+        const double tf = tape[5];
+        const double* last = tape + kTapeHeader + int64_t(N - 1) * rec_len;
+        const int q_final = static_cast<int>(tape[1]);
+        {
+            const double s = (tf - tape[2]) / last[1];
+            for (int jj = 0; jj <= kQmax + 1; ++jj)
+                for (int i = tid; i < n; i += NT) zb[jj][i] = 0.0;
+            __syncthreads();
+            double sp = 1.0;
+            for (int jj = 0; jj <= q_final; ++jj, sp *= s)
+                for (int i = tid; i < n; i += NT) zb[jj][i] = sp * ybar_out[size_t(j) * n + i];
+        }
+        int q_next = q_final;
+        double h_next = last[1];
+        bool restart_next = false;
+        double l[kQmax + 2];
+        for (int r = N - 1; r >= 0 && status == 0; --r) {
+            const double* rec = tape + kTapeHeader + int64_t(r) * rec_len;
+            const double t_r = rec[0], h_r = rec[1];
+            const int q_r = static_cast<int>(rec[2]);
+            const bool flag_r = rec[3] != 0.0;
+            for (int i = tid; i < n; i += NT) v.y[i] = rec[4 + i];
+            __syncthreads();
+            P.f(t_start + t_r, v.y, v.ft);
+            P.jacobian(t_start + t_r, v.y, v.ft);
+            // v.acorp: the vector whose J^T and f_p^T products this step adds to zb0 and pbar
+            if (restart_next) {
+                for (int i = tid; i < n; i += NT) {
+                    v.acorp[i] = h_next * zb[1][i];
+                    for (int jj = 1; jj <= kQmax + 1; ++jj) zb[jj][i] = 0.0;
+                }
+            } else {
+                const double ratio = h_next / h_r;
+                double sc = ratio;
+                for (int jj = 1; jj <= q_next; ++jj, sc *= ratio)
+                    for (int i = tid; i < n; i += NT) zb[jj][i] *= sc;
+                for (int i = tid; i < n; i += NT) v.acorp[i] = 0.0;
+            }
+            __syncthreads();
+            bdf_l(q_r, l);
+            for (int i = tid; i < n; i += NT) {
+                double ab = 0.0;
+                if (!restart_next && q_next == q_r + 1) {
+                    ab = (l[q_r] / (q_r + 1)) * zb[q_r + 1][i];
+                    zb[q_r + 1][i] = 0.0;
+                }
+                for (int jj = 0; jj <= q_r; ++jj) ab = fma(l[jj], zb[jj][i], ab);
+                v.bb[i] = ab;
+            }
+            const double gamma = h_r / l[1];
+            const double rl1 = 1.0 / l[1];
+            for (size_t e = tid; e < size_t(n) * n; e += NT) {
+                const int c = static_cast<int>(e / n), rr = static_cast<int>(e - size_t(c) * n);
+                P.M[e] = (rr == c ? 1.0 : 0.0) - gamma * P.J[e];
+            }
+            __syncthreads();
+            if (P.lu_factor() != 0) {
+                status = -32;  // singular iteration matrix
+                break;
+            }
+            P.lu_solve_transpose(v.bb);  // w
+            for (int i = tid; i < n; i += NT) {
+                v.acorp[i] = fma(gamma, v.bb[i], v.acorp[i]);
+                zb[1][i] = fma(-rl1, v.bb[i], zb[1][i]);
+            }
+            __syncthreads();
+            P.jacobian_transpose_times(v.acorp, zb[0], true);
+            P.f(t_start + t_r, v.y, v.ft);  // rates at the step's end state again (the FD column moved them)
+            P.multiplier_vjp(v.acorp, pb);
+            __syncthreads();
+            // predictor transpose: the forward ran z[j-1] += z[j] for k = 1..q, j = q..k
+            for (int k = q_r; k >= 1; --k)
+                for (int jj = k; jj <= q_r; ++jj)
+                    for (int i = tid; i < n; i += NT) zb[jj][i] += zb[jj - 1][i];
+            __syncthreads();
+            q_next = q_r;
+            h_next = h_r;
+            restart_next = flag_r;
+        }
+        if (status == 0) {
+            // z at the start of the first step: [y0, h0 f(y0)]
+            const double* y0 = a.state_in + size_t(j) * n;
+            for (int i = tid; i < n; i += NT) {
+                v.y[i] = y0[i];
+                v.acorp[i] = h_next * zb[1][i];
+            }
+            __syncthreads();
+            P.f(t_start, v.y, v.ft);
+            P.jacobian(t_start, v.y, v.ft);
+            P.jacobian_transpose_times(v.acorp, zb[0], true);
+            P.f(t_start, v.y, v.ft);
+            P.multiplier_vjp(v.acorp, pb);
+            for (int i = tid; i < n; i += NT) ybar_in[size_t(j) * n + i] = zb[0][i];
+        } else {
+            for (int i = tid; i < n; i += NT) ybar_in[size_t(j) * n + i] = 0.0;
+        }
+        if (tid == 0) adj_status[j] = status;
+        __syncthreads();
+    }
+}
+
+template <int NT>
+static int launch_bdf_adjoint_nt(const MechView& m, const SourceArgs& a, int* counter, const double* ybar_out,
+                                 double* ybar_in, double* pbar, int* adj_status, Scratch& sc, cudaStream_t st) {
+    const int n = m.S + 2;
+    size_t per = 0;
+    int blocks = 0;
+    EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_bdf_adjoint<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        int(per)));
+    double *kcache = nullptr, *jm = nullptr;
+    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
+    EMBER_TRY(sc.alloc(&jm, size_t(blocks) * 2 * size_t(n) * n));
+    k_source_bdf_adjoint<NT><<<blocks, NT, per, st>>>(m, a, counter, kcache, jm, ybar_out, ybar_in, pbar,
+                                                      adj_status);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
+// Gradient, at each point's state y = [U, T, Y] (Y >= 0), of
+//   psi = gq * qdot + gcp * cp + gT * T,
+// qdot = -sum_k wdot_k h_k and cp the mass heat capacity of the normalised
+// state (FlameSolver::calculateQdot, setState_TPY). The NoNorm derivatives
+// come from the analytic Jacobian of the source right-hand side with the
+// split constant and igniter off: d qdot = rho cp d(dT/dt) + dT/dt d(rho cp);
+// rho cp = (p/T) B/A and cp = R B with A = sum_k Y_k/W_k, B = sum_k
+// Y_k cp_k/(R W_k); then the normalisation Y/sum(Y) is projected out. Also
+// d psi / d ln(multiplier_i) = gq * (-sum_k nu_ki h_k) r_i, per point.
+template <int NT>
+__global__ void __launch_bounds__(NT) k_objective_vjp(MechView m, SourceArgs a, int n_pts,
+                                                     const double* __restrict__ state, const double* __restrict__ gq,
+                                                     const double* __restrict__ gcp, const double* __restrict__ gT,
+                                                     int* counter, double* kcache, double* jm,
+                                                     double* __restrict__ ybar, double* __restrict__ pbar) {
+    extern __shared__ double smem[];
+    __shared__ int next_point;
+    const int n = m.S + 2;
+    const size_t cd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true);
+    BdfPoint<NT> P;
+    P.m = m;
+    P.w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), m, true);
+    P.w.fo_F = smem + cd;
+    P.w.fo_pr = P.w.fo_F + m.n_fo;
+    P.w.fo_dF = P.w.fo_pr + m.n_fo;
+    P.v.carve(P.w.fo_dF + m.n_fo, n);
+    P.a = &a;
+    P.n = n;
+    P.S = m.S;
+    P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
+    P.M = P.J + size_t(n) * n;
+    P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
+    P.tape = nullptr;
+    P.split = nullptr;
+    P.x = 0.0;
+    BdfSmem& v = P.v;
+    const int tid = threadIdx.x;
+    const int S = m.S;
+    for (;;) {
+        if (tid == 0) {
+            const int slot = atomicAdd(counter, 1);
+            next_point = slot < n_pts ? slot : n_pts;
+        }
+        __syncthreads();
+        const int j = next_point;
+        __syncthreads();
+        if (j >= n_pts) break;
+        for (int i = tid; i < n; i += NT) v.y[i] = state[size_t(j) * n + i];
+        __syncthreads();
+        P.f(0.0, v.y, v.ft);
+        P.jacobian(0.0, v.y, v.ft);
+        const double T = v.y[1];
+        const double rho = P.rho, cp = P.cp, rc = rho * cp;
+        const double A = 1.0 / P.w.mmw;
+        double bpart = 0.0, dbpart = 0.0, ysum_part = 0.0;
+        for (int k = tid; k < S; k += NT) {
+            const double yk = v.y[2 + k] * m.rW[k];
+            const int r = (T <= m.tmid[k]) ? 0 : 1;
+            const double* c = m.nasa + 14 * k + 7 * r;
+            const double dcp = fma(fma(fma(4.0 * c[4], T, 3.0 * c[3]), T, 2.0 * c[2]), T, c[1]);
+            bpart = fma(yk, P.w.cpR[k], bpart);
+            dbpart = fma(yk, dcp, dbpart);
+            ysum_part += v.y[2 + k];
+        }
+        const double B = block_sum<NT>(P.w.red, bpart);
+        const double dB = block_sum<NT>(P.w.red, dbpart);
+        const double ysum = block_sum<NT>(P.w.red, ysum_part);
+        const double p = a.pressure, dTdt = v.ft[1];
+        const double g_q = gq[j], g_cp = gcp ? gcp[j] : 0.0, g_T = gT ? gT[j] : 0.0;
+        // d psi / d y_c (NoNorm) into v.bb
+        for (int c = tid; c < n; c += NT) {
+            double drc, dcpc;
+            if (c == 0) {
+                drc = 0.0;
+                dcpc = 0.0;
+            } else if (c == 1) {
+                drc = -rc / T + (p / (T * A)) * dB;
+                dcpc = kGasConstant * dB;
+            } else {
+                const int mm = c - 2;
+                drc = (p / T) * ((P.w.cpR[mm] * m.rW[mm]) / A - (B * m.rW[mm]) / (A * A));
+                dcpc = kGasConstant * (P.w.cpR[mm] * m.rW[mm]);
+            }
+            const double dq = fma(rc, P.J[size_t(c) * n + 1], dTdt * drc);
+            v.bb[c] = g_q * dq + g_cp * dcpc + (c == 1 ? g_T : 0.0);
+        }
+        __syncthreads();
+        // project out the normalisation of Y
+        double proj = 0.0;
+        for (int k = tid; k < S; k += NT) proj = fma(v.y[2 + k], v.bb[2 + k], proj);
+        const double pr = block_sum<NT>(P.w.red, proj);
+        for (int c = tid; c < n; c += NT) {
+            double g = v.bb[c];
+            if (c >= 2) g = (g - pr / ysum) / ysum;
+            ybar[size_t(j) * n + c] = g;
+        }
+        // rate multipliers (the FD column of the Jacobian moved the rates: evaluate again)
+        P.f(0.0, v.y, v.ft);
+        double* pb = pbar + size_t(j) * m.R;
+        for (int i = tid; i < m.R; i += NT) {
+            const double r = P.w.ropf[i] - P.w.ropr[i];
+            const int4 st = m.stoich[i];
+            const int sp[8] = {unpack_lo(st.x), unpack_hi(st.x), unpack_lo(st.y), unpack_hi(st.y),
+                               unpack_lo(st.z), unpack_hi(st.z), unpack_lo(st.w), unpack_hi(st.w)};
+            double eh = 0.0;
+#pragma unroll
+            for (int o = 0; o < 8; ++o) {
+                if (sp[o] == 0xffff) continue;
+                eh = fma(o < 4 ? -1.0 : 1.0, P.w.hk[sp[o]], eh);
+            }
+            pb[i] = g_q * (-eh * r);
+        }
+        __syncthreads();
+    }
+}
+
+template <int NT>
+static int launch_objective_vjp_nt(const MechView& m, const SourceArgs& a, int n_pts, const double* state,
+                                   const double* gq, const double* gcp, const double* gT, double* ybar, double* pbar,
+                                   Scratch& sc, cudaStream_t st) {
+    const int n = m.S + 2;
+    size_t per = 0;
+    int blocks = 0;
+    SourceArgs b = a;
+    b.n = n_pts;
+    EMBER_TRY(bdf_config<NT>(m, b, &per, &blocks));
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_objective_vjp<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
+    double *kcache = nullptr, *jm = nullptr;
+    int* counter = nullptr;
+    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
+    EMBER_TRY(sc.alloc(&jm, size_t(blocks) * 2 * size_t(n) * n));
+    EMBER_TRY(sc.alloc(&counter, 1));
+    EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
+    k_objective_vjp<NT><<<blocks, NT, per, st>>>(m, b, n_pts, state, gq, gcp, gT, counter, kcache, jm, ybar, pbar);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
+int launch_objective_vjp(const MechView& m, const SourceArgs& a, int n_pts, const double* state, const double* gq,
+                         const double* gcp, const double* gT, double* ybar, double* pbar, Scratch& sc,
+                         cudaStream_t st) {
+    switch (chem_threads_for(m.S)) {
+        case 64: return launch_objective_vjp_nt<64>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
+        case 128: return launch_objective_vjp_nt<128>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
+        case 160: return launch_objective_vjp_nt<160>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
+        default: return launch_objective_vjp_nt<256>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
+    }
+}
+
+int launch_source_bdf_adjoint(const MechView& m, const SourceArgs& a, int* counter, const double* ybar_out,
+                              double* ybar_in, double* pbar, int* adj_status, Scratch& sc, cudaStream_t st) {
+    switch (chem_threads_for(m.S)) {
+        case 64: return launch_bdf_adjoint_nt<64>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
+        case 128: return launch_bdf_adjoint_nt<128>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
+        case 160: return launch_bdf_adjoint_nt<160>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
+        default: return launch_bdf_adjoint_nt<256>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
+    }
+}
+
 int launch_source_bdf(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
     switch (chem_threads_for(m.S)) {
         case 64: return launch_bdf_nt<64>(m, a, counter, sc, st);
@@ -798,3 +1233,90 @@ int launch_source_bdf(const MechView& m, const SourceArgs& a, int* counter, Scra
 }
 
 }  // namespace ember
+
+namespace ember {
+namespace {
+
+// Sum of the per-point gradients [n][R] over points, in point order.
+__global__ void k_sum_points(int n, int R, const double* __restrict__ rows, double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int j = 0; j < n; ++j) s += rows[size_t(j) * R + i];
+        out[i] = s;
+    }
+}
+
+}  // namespace
+
+int source_bdf_adjoint_run(const MechView& m, SourceArgs a, int tape_cap, const double* ybar_out, double* ybar_in,
+                           double* lnk_bar, double* lnk_bar_points, int* adj_status, Scratch& sc, cudaStream_t st) {
+    const int n = m.S + 2;
+    a.tape_cap = tape_cap;
+    a.tape_stride = bdf_tape_doubles(n, tape_cap);
+    EMBER_TRY(sc.alloc(&a.tape, size_t(a.n) * a.tape_stride));
+    int* counter = nullptr;
+    EMBER_TRY(sc.alloc(&counter, 2));
+    EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, 2 * sizeof(int), st));
+    EMBER_TRY(launch_source_bdf(m, a, counter, sc, st));
+    double* rows = lnk_bar_points;
+    if (!rows) EMBER_TRY(sc.alloc(&rows, size_t(a.n) * std::max(m.R, 1)));
+    EMBER_TRY(launch_source_bdf_adjoint(m, a, counter + 1, ybar_out, ybar_in, rows, adj_status, sc, st));
+    if (lnk_bar && m.R > 0)
+        k_sum_points<<<blocks_for(m.R, 128), 128, 0, st>>>(a.n, m.R, rows, lnk_bar);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
+}  // namespace ember
+
+using namespace ember;
+
+extern "C" int ember_source_adjoint(ember_mech m, int n, const double* state_in, const double* split_const,
+                                    const double* dt, double t_start, const double* x,
+                                    const ember_source_options* opts, const double* state_bar, int tape_cap,
+                                    double* state_out, int* status, double* state_in_bar, double* lnk_bar, int mem,
+                                    void* stream) {
+    EMBER_CHECK_ARG(m != nullptr, "null mechanism");
+    EMBER_CHECK_ARG(n > 0 && state_in && dt && state_bar && state_out && status && state_in_bar,
+                    "need points, state_in, dt, state_bar, state_out, status and state_in_bar");
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_CHECK_ARG(tape_cap >= 0 && tape_cap <= (1 << 20), "bad tape_cap %d", tape_cap);
+    EMBER_TRY(source_check_options(opts));
+    EMBER_TRY(ensure_device());
+    if (tape_cap == 0) tape_cap = 1024;
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    const int nv = m->S + 2;
+    const double *d_in, *d_split, *d_dt, *d_x, *d_bar;
+    EMBER_TRY(stage_in(sc, state_in, size_t(n) * nv, mem, st, &d_in));
+    EMBER_TRY(stage_in(sc, split_const, size_t(n) * nv, mem, st, &d_split));
+    EMBER_TRY(stage_in(sc, dt, n, mem, st, &d_dt));
+    EMBER_TRY(stage_in(sc, x, n, mem, st, &d_x));
+    EMBER_TRY(stage_in(sc, state_bar, size_t(n) * nv, mem, st, &d_bar));
+    double *d_out, *d_inbar, *d_lnk = nullptr;
+    int *d_status, *d_adj;
+    EMBER_TRY(stage_buffer(sc, state_out, size_t(n) * nv, mem, &d_out));
+    EMBER_TRY(stage_buffer(sc, status, n, mem, &d_status));
+    EMBER_TRY(stage_buffer(sc, state_in_bar, size_t(n) * nv, mem, &d_inbar));
+    EMBER_TRY(stage_buffer(sc, lnk_bar, size_t(std::max(m->R, 1)), mem, &d_lnk));
+    EMBER_TRY(sc.alloc(&d_adj, n));
+    SourceArgs a = make_source_args(opts, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, nullptr);
+    EMBER_TRY(source_bdf_adjoint_run(m->view, a, tape_cap, d_bar, d_inbar, d_lnk, nullptr, d_adj, sc, st));
+    // status: the forward's, or the adjoint's when the forward succeeded
+    EMBER_CUDA_TRY(cudaMemcpyAsync(d_status, d_adj, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
+    EMBER_TRY(stage_out(state_out, d_out, size_t(n) * nv, mem, st));
+    EMBER_TRY(stage_out(status, d_status, n, mem, st));
+    EMBER_TRY(stage_out(state_in_bar, d_inbar, size_t(n) * nv, mem, st));
+    if (lnk_bar) EMBER_TRY(stage_out(lnk_bar, d_lnk, size_t(m->R), mem, st));
+    sc.release();
+    EMBER_TRY(finish_call(mem, st));
+    if (mem == EMBER_MEM_HOST) {
+        int bad = 0;
+        for (int j = 0; j < n; ++j) bad += status[j] != 0;
+        if (bad) {
+            set_error("%d of %d points failed (see status)", bad, n);
+            return EMBER_EFAIL;
+        }
+    }
+    return EMBER_OK;
+}

@@ -112,6 +112,7 @@ struct ChemSmem {
     double* red;      // [kMaxChemThreads + 2] reduction scratch
     double* fo_F;     // [n_fo] falloff F of the last composition (only when set; for Jacobians)
     double* fo_pr;    // [n_fo] reduced pressure Pr of the last composition (idem)
+    double* fo_dF;    // [n_fo] dF/dPr of the last composition (idem)
     double mmw;       // mean molecular weight of the last composition (set by chem_rates)
     double* kfm;   // global [R]: rate constant x multiplier (falloff rows: refreshed per composition)
     double* rkc;   // global [R]: 1/Kc
@@ -144,6 +145,7 @@ struct ChemSmem {
         red = fo_lfc + m.n_fo;
         fo_F = nullptr;
         fo_pr = nullptr;
+        fo_dF = nullptr;
         mmw = 0.0;
         kfm = gbase;
         rkc = gbase + R;
@@ -327,7 +329,7 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
         const int i = m.fo_rxn[f];
         const double kinf = w.fo_kinf[f];
         const double pr = (w.concm[m.fo_tb[f]] * w.fo_k0[f]) * w.fo_rkinf[f];
-        double F = 1.0;
+        double F = 1.0, dF = 0.0;  // dF: dF/dPr (for Jacobians)
         if (rinfo_type(m.rinfo[i]) == RXN_TROE) {
             const double lfc = w.fo_lfc[f];
             const double lpr = em_log10(dmaxr(pr, kSmallNumber));
@@ -335,13 +337,20 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
             const double nn = fma(-1.27, lfc, 0.75);
             const double x = lpr + cc;
             const double f1 = x / fma(-0.14, x, nn);
-            F = em_exp10(lfc / fma(f1, f1, 1.0));
+            const double g = fma(f1, f1, 1.0);
+            F = em_exp10(lfc / g);
+            if (w.fo_dF && pr > kSmallNumber) {
+                // d log10 F / d f1 = -2 lfc f1 / g^2; d f1 / dx = nn / (nn - 0.14 x)^2; dx / dPr = 1/(Pr ln 10)
+                const double den = fma(-0.14, x, nn);
+                dF = ((F * ((-2.0 * lfc * f1) / (g * g))) * (nn / (den * den))) / pr;
+            }
         }
         w.kfm[i] = ((pr * (F / (1.0 + pr))) * kinf) * m.mult[i];
         if (w.fo_F) {
             w.fo_F[f] = F;
             w.fo_pr[f] = pr;
         }
+        if (w.fo_dF) w.fo_dF[f] = dF;
     }
     __syncthreads();
     // rates of progress

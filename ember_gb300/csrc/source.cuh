@@ -29,7 +29,20 @@ struct SourceArgs {
     double bdf_reltol, bdf_atol_u, bdf_atol_t, bdf_atol_y, bdf_min_step;
     int bdf_max_steps;
     double ign_tstart, ign_duration, ign_energy, ign_center, ign_stddev;
+    // BDF trajectory tape for the adjoint (null: none): per point, at
+    // tape + j * tape_stride, a header of kTapeHeader doubles and one record
+    // of n + 4 doubles per accepted step (at most tape_cap records).
+    double* tape;
+    int64_t tape_stride;
+    int tape_cap;
 };
+
+// Tape header: accepted steps recorded, order after the last step, t after
+// the last step, overflow flag, integrator status, tf. Record: t after the
+// step, h, q, restart flag (a q = 1 restart with z1 = h f(z0) preceded the
+// step), then y after the step (n values).
+constexpr int kTapeHeader = 8;
+__host__ __device__ inline int64_t bdf_tape_doubles(int n, int cap) { return kTapeHeader + int64_t(cap) * (n + 4); }
 
 // SourceSystem::getQdotIgniter (src/sourceSystem.cpp:33-45).
 __device__ __forceinline__ double igniter(const SourceArgs& a, double t, double x) {
@@ -51,6 +64,24 @@ class Scratch;
 int make_work_order(const SourceArgs& a, Scratch& sc, cudaStream_t st, int** order_out);
 int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st);
 int launch_source_bdf(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st);
+// Discrete adjoint of a BDF launch that recorded a tape (a.tape): from the
+// adjoint of the end states (ybar_out, [n][S+2]) to that of the start states
+// (ybar_in) and, per point, of ln(multiplier) of every reaction (pbar,
+// [n][R]); adj_status [n]: 0, the forward status, or -30 (tape overflow),
+// -31 (no step), -32 (singular matrix).
+int launch_source_bdf_adjoint(const MechView& m, const SourceArgs& a, int* counter, const double* ybar_out,
+                              double* ybar_in, double* pbar, int* adj_status, Scratch& sc, cudaStream_t st);
+// Gradient at point-major states of psi = gq qdot + gcp cp + gT T per point
+// (qdot, cp of the normalised state): ybar [n_pts][S+2], pbar [n_pts][R]
+// (d psi / d ln multiplier). `a` supplies pressure and kinetics model.
+int launch_objective_vjp(const MechView& m, const SourceArgs& a, int n_pts, const double* state, const double* gq,
+                         const double* gcp, const double* gT, double* ybar, double* pbar, Scratch& sc,
+                         cudaStream_t st);
+// Forward BDF with a tape (tape_cap accepted steps per point) followed by its
+// adjoint; lnk_bar: gradient summed over points ([R], or null);
+// lnk_bar_points: per point ([n][R], or null: scratch).
+int source_bdf_adjoint_run(const MechView& m, SourceArgs a, int tape_cap, const double* ybar_out, double* ybar_in,
+                           double* lnk_bar, double* lnk_bar_points, int* adj_status, Scratch& sc, cudaStream_t st);
 // SourceArgs from the public options (source.cu).
 SourceArgs make_source_args(const ember_source_options* o, int n, const double* state_in, const double* split,
                             const double* dt, double t_start, const double* x, double* state_out, int* status,

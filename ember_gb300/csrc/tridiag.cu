@@ -124,6 +124,24 @@ __global__ void k_diffusion_integrate_serial(DiffusionView v, TriBatchView tb, S
     if (v.status) v.status[s] = st;
 }
 
+// Adjoint of the stage of k_diffusion_integrate_serial, one thread per system.
+__global__ void k_diffusion_adjoint(DiffusionView v, TriBatchView tb, StageTime tm, double mult, double gdt) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= v.n_systems) return;
+    double t0, t1;
+    tm.get(t0, t1);
+    const DiffSysInfo info = v.info[s];
+    double h;
+    if (v.h) {
+        h = v.h[s];
+    } else {
+        h = diffusion_step_size(info.n, v.x + info.grid_off, v.B + info.off, v.D + info.off, mult, gdt);
+    }
+    TriSys sys = tb.system(s);
+    const int st = tri_integrate_adjoint(sys, t0, h, t1);
+    if (v.status) v.status[s] = st;
+}
+
 }  // namespace ember
 
 // ------------------------------------------------------------ C ABI: batch --
@@ -338,6 +356,33 @@ int diffusion_serial_run(const DiffusionView& dv_in, double* y, double* work, in
     return EMBER_OK;
 }
 
+int diffusion_adjoint_run(const DiffusionView& dv_in, double* y, double* work, int64_t n_vals, int nmax,
+                          const StageTime& tm, double mult, double gdt, cudaStream_t st) {
+    DiffusionView dv = dv_in;
+    dv.a = work;
+    dv.b = work + n_vals;
+    dv.c = work + 2 * n_vals;
+    dv.k = work + 3 * n_vals;
+    const int n_sys = dv.n_systems;
+    dim3 grid_rows(std::min(blocks_for(nmax, 256), 32), std::min(n_sys, 65535));
+    k_diffusion_rows<<<grid_rows, 256, 0, st>>>(dv);
+    TriBatchView tb;
+    tb.n_systems = n_sys;
+    tb.off = nullptr;
+    tb.info = dv.info;
+    tb.a = dv.a;
+    tb.b = dv.b;
+    tb.c = dv.c;
+    tb.k = dv.k;
+    tb.y = y;
+    tb.yprev = work + 4 * n_vals;
+    tb.luc = work + 5 * n_vals;
+    tb.inv = work + 6 * n_vals;
+    k_diffusion_adjoint<<<blocks_for(n_sys, 64), 64, 0, st>>>(dv, tb, tm, mult, gdt);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
 }  // namespace ember
 
 extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_grid* grids, int n_vars,
@@ -450,6 +495,82 @@ extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_gri
         }
     }
     return EMBER_OK;
+}
+
+// ------------------------------------------------- C ABI: diffusion adjoint --
+
+extern "C" int ember_diffusion_adjoint(int n_flames, const ember_diffusion_grid* grids, int n_vars, const double* x,
+                                       const double* B, const double* D, double* ybar,
+                                       const ember_diffusion_options* opts, int* status, int mem, void* stream) {
+    EMBER_CHECK_ARG(n_flames > 0 && grids != nullptr, "need at least one flame");
+    EMBER_CHECK_ARG(n_vars > 0, "n_vars must be positive");
+    EMBER_CHECK_ARG(x && B && D && ybar && opts, "null array or options argument");
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_CHECK_ARG(opts->h != nullptr || (opts->dt_multiplier > 0 && opts->global_timestep > 0),
+                    "without explicit h, dt_multiplier and global_timestep must be positive");
+    EMBER_CHECK_ARG(opts->t_end > opts->t_start, "t_end must exceed t_start");
+    EMBER_TRY(ensure_device());
+    const int n_sys = n_flames * n_vars;
+    std::vector<DiffSysInfo> info(n_sys);
+    int64_t n_pts = 0, n_vals = 0;
+    int nmax = 0;
+    for (int f = 0; f < n_flames; ++f) {
+        const ember_diffusion_grid& g = grids[f];
+        EMBER_CHECK_ARG(g.n_points >= 3, "flame %d: n_points must be >= 3 (got %d)", f, g.n_points);
+        EMBER_CHECK_ARG(g.left_bc >= 0 && g.left_bc <= 4, "flame %d: bad left_bc %d", f, g.left_bc);
+        EMBER_CHECK_ARG(g.right_bc == EMBER_BC_FIXED_VALUE || g.right_bc == EMBER_BC_ZERO_GRADIENT ||
+                            g.right_bc == EMBER_BC_FLOATING,
+                        "flame %d: bad right_bc %d", f, g.right_bc);
+        EMBER_CHECK_ARG(g.alpha >= 0, "flame %d: bad alpha %d", f, g.alpha);
+        for (int v = 0; v < n_vars; ++v) {
+            DiffSysInfo& s = info[f * n_vars + v];
+            s.n = g.n_points;
+            s.left_bc = g.left_bc;
+            s.right_bc = g.right_bc;
+            s.alpha = g.alpha;
+            s.grid_off = n_pts;
+            s.off = n_vals + int64_t(v) * g.n_points;
+        }
+        n_pts += g.n_points;
+        n_vals += int64_t(n_vars) * g.n_points;
+        nmax = std::max(nmax, g.n_points);
+    }
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    DiffSysInfo* d_info = nullptr;
+    EMBER_TRY(sc.alloc(&d_info, n_sys));
+    EMBER_CUDA_TRY(cudaMemcpyAsync(d_info, info.data(), sizeof(DiffSysInfo) * n_sys, cudaMemcpyHostToDevice, st));
+    DiffusionView dv{};
+    dv.n_systems = n_sys;
+    dv.info = d_info;
+    EMBER_TRY(stage_in(sc, x, n_pts, mem, st, &dv.x));
+    EMBER_TRY(stage_in(sc, B, n_vals, mem, st, &dv.B));
+    EMBER_TRY(stage_in(sc, D, n_vals, mem, st, &dv.D));
+    EMBER_TRY(stage_in(sc, opts->h, n_sys, mem, st, &dv.h));
+    EMBER_TRY(stage_in(sc, opts->wall_const, n_sys, mem, st, &dv.wall_const));
+    int* d_status = nullptr;
+    EMBER_TRY(stage_buffer(sc, status, n_sys, mem, &d_status));
+    if (!d_status) EMBER_TRY(sc.alloc(&d_status, n_sys));
+    dv.status = d_status;
+    double* d_y = nullptr;
+    if (mem == EMBER_MEM_DEVICE) {
+        d_y = ybar;
+    } else {
+        EMBER_TRY(sc.alloc(&d_y, n_vals));
+        EMBER_CUDA_TRY(cudaMemcpyAsync(d_y, ybar, sizeof(double) * n_vals, cudaMemcpyHostToDevice, st));
+    }
+    double* work = nullptr;
+    EMBER_TRY(sc.alloc(&work, size_t(7) * n_vals));
+    StageTime tm;
+    tm.t0 = opts->t_start;
+    tm.t1 = opts->t_end;
+    EMBER_TRY(diffusion_adjoint_run(dv, d_y, work, n_vals, nmax, tm, opts->dt_multiplier, opts->global_timestep, st));
+    if (mem == EMBER_MEM_HOST) {
+        EMBER_CUDA_TRY(cudaMemcpyAsync(ybar, d_y, sizeof(double) * n_vals, cudaMemcpyDeviceToHost, st));
+    }
+    EMBER_TRY(stage_out(status, d_status, n_sys, mem, st));
+    sc.release();
+    return finish_call(mem, st);
 }
 
 // ------------------------------------------ allocation-free diffusion stage --

@@ -193,6 +193,79 @@ __device__ __forceinline__ int tri_integrate_serial(const TriSys& s, double& t, 
     return TRI_OK;
 }
 
+// ---- adjoint of a stage --------------------------------------------------
+// The stage is linear in y: y_out = M y_in + (terms of k). The adjoint maps
+// ybar = d phi / d y_out to d phi / d y_in = M^T ybar by running the sub-steps
+// backwards with transposed solves; L^T of L = A - shift I has sub-diagonal
+// c_{i-1}, diagonal b_i - shift and super-diagonal a_{i+1}.
+__device__ __forceinline__ void tri_factor_transpose(const TriSys& s, double shift, double& lu_b0) {
+    double lb0 = s.b[0] - shift;
+    double lc = s.N > 1 ? s.a[1] / lb0 : 0.0;
+    s.luc[0] = lc;
+    for (int i = 1; i < s.N; ++i) {
+        double den = (s.b[i] - shift) - lc * s.c[i - 1];
+        double iv = 1.0 / den;
+        s.inv[i] = iv;
+        lc = i + 1 < s.N ? s.a[i + 1] * iv : 0.0;
+        s.luc[i] = lc;
+    }
+    lu_b0 = lb0;
+}
+
+// Solve L^T x = r in place (r in v).
+__device__ __forceinline__ void tri_solve_transpose(const TriSys& s, double lu_b0, double* v) {
+    double d = v[0] / lu_b0;
+    v[0] = d;
+    for (int i = 1; i < s.N; ++i) {
+        d = (v[i] - d * s.c[i - 1]) * s.inv[i];
+        v[i] = d;
+    }
+    double yn = d;
+    for (int i = s.N - 2; i >= 0; --i) {
+        yn = v[i] - s.luc[i] * yn;
+        v[i] = yn;
+    }
+}
+
+// Adjoint of initialize(t, h) + integrateToTime(t_end) of one system: s.y
+// holds ybar on entry and the adjoint of the start state on exit; s.yprev is
+// workspace. Returns a TRI_* code (the forward's step rule).
+__device__ __forceinline__ int tri_integrate_adjoint(const TriSys& s, double t, double h, double t_end) {
+    double q = (t_end - t) / h + 1e-5;
+    if (!(h > 0.0) || !(q < 2147483647.0)) return TRI_BAD_STEP;
+    const int n_steps = q >= 1.0 ? static_cast<int>(q) : 1;
+    h = (t_end - t) / static_cast<double>(n_steps);
+    double lu_b0 = 0.0;
+    double* g = s.y;       // adjoint of the newest state
+    double* gp = s.yprev;  // adjoint of the state before it
+    for (int i = 0; i < s.N; ++i) gp[i] = 0.0;
+    if (n_steps > 1) {
+        // BDF2 steps j = n-1..1: Y_{8+j} = L2^{-1} (-(2/h) Y_{8+j-1} + (1/(2h)) P_j - k),
+        // P_1 = Y_0 (the state before the first step), P_j = Y_{8+j-2}.
+        tri_factor_transpose(s, 3.0 / (2.0 * h), lu_b0);
+        for (int j = n_steps - 1; j >= 1; --j) {
+            tri_solve_transpose(s, lu_b0, g);
+            for (int i = 0; i < s.N; ++i) {
+                const double w = g[i];
+                g[i] = gp[i] - (2.0 / h) * w;
+                gp[i] = (1.0 / (2.0 * h)) * w;  // for j = 1: the term of Y_0, added at the end
+            }
+        }
+    }
+    // BDF1 sub-steps m = 7..0: Y_{m+1} = L1^{-1} (-Y_m / h8 - k)
+    const double h8 = h / 8.0;
+    tri_factor_transpose(s, 1.0 / h8, lu_b0);
+    for (int m = 7; m >= 0; --m) {
+        tri_solve_transpose(s, lu_b0, g);
+        for (int i = 0; i < s.N; ++i) g[i] = -g[i] / h8;
+    }
+    for (int i = 0; i < s.N; ++i) {
+        g[i] += gp[i];
+        if (!isfinite(g[i])) return TRI_NONFINITE;
+    }
+    return TRI_OK;
+}
+
 // ---- DiffusionSystem::get_A (src/diffusionSystem.cpp:10-66) -------------
 struct DiffRow {
     double a, b, c;
@@ -318,6 +391,11 @@ int diffusion_warp_geometry(const DiffusionWarpPlan& p, const DiffSysInfo* d_inf
 // one warp per system; `y` (device, variable-major per flame) in place.
 int diffusion_warp_run(const DiffusionWarpPlan& p, const DiffusionView& dv, double* y, const StageTime& tm,
                        double mult, double gdt, cudaStream_t st);
+
+// Adjoint of a stage (B, D, split constants fixed): y holds d phi / d y_out
+// on entry and d phi / d y_in on exit; work: 7 * n_vals doubles.
+int diffusion_adjoint_run(const DiffusionView& dv, double* y, double* work, int64_t n_vals, int nmax,
+                          const StageTime& tm, double mult, double gdt, cudaStream_t st);
 
 // Serial (bitwise reference order) stage on a device workspace of
 // 7 * n_vals doubles: rows, then one thread per system (tridiag.cu).

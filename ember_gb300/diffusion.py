@@ -183,6 +183,30 @@ def integrate_diffusion_terms(grids, B, D, split_const, y, t_start, t_end, *, h=
     return Y_, status
 
 
+def diffusion_adjoint(grids, B, D, ybar, t_start, t_end, *, h=None, dt_multiplier=10.0, global_timestep=2e-5,
+                      wall_const=None):
+    """Gradient of phi = ybar . y_out of one diffusion stage with respect to
+    its start state (``ember_diffusion_adjoint``): flat host arrays in the
+    layout of ``integrate_diffusion_terms``; returns (ybar_in, status)."""
+    n_flames = len(grids)
+    total_pts = sum(g.n_points for g in grids)
+    y = _f64(ybar).copy()
+    n_vars = y.size // total_pts
+    B_, D_ = _f64(B), _f64(D)
+    x_ = np.concatenate([_f64(g.x) for g in grids])
+    per_sys = lambda v: _f64(np.broadcast_to(np.asarray(v, dtype=np.float64), (n_flames * n_vars,))) \
+        if v is not None else None
+    h_, wc_ = per_sys(h), per_sys(wall_const)
+    status = np.zeros(n_flames * n_vars, dtype=np.int32)
+    garr = (L.DiffusionGrid * n_flames)(*[L.DiffusionGrid(g.n_points, g.left_bc, g.right_bc, g.alpha)
+                                          for g in grids])
+    opts = L.DiffusionOptions(float(t_start), float(t_end), float(dt_multiplier), float(global_timestep),
+                              L.ptr(h_), L.ptr(wc_), None, L.DIFFUSION_SERIAL)
+    L.check(L.lib().ember_diffusion_adjoint(n_flames, garr, n_vars, L.ptr(x_), L.ptr(B_), L.ptr(D_), L.ptr(y),
+                                            C.byref(opts), L.ptr(status), L.MEM_HOST, None), "ember_diffusion_adjoint")
+    return y, status
+
+
 def synthetic_flames(n_flames: int = 64, n_vars: int = 55, n_min: int = 100, n_max: int = 4000, seed: int = 6455,
                      dt: float = 1e-5):
     """Seeded batch of diffusion stages with uneven grids: N_f uniform in

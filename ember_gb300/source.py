@@ -133,3 +133,27 @@ def integrate_production_terms(gmech: GpuMechanism, method: int, state, dt, opts
     if rc not in (L.OK, L.EFAIL):
         L.check(rc, "ember_source_integrate")
     return out, status, stats
+
+
+def source_adjoint(gmech: GpuMechanism, state, dt, opts: SourceOptions, state_bar, split_const=None, t_start=0.0,
+                   x=None, tape_cap: int = 0):
+    """Discrete adjoint of a BDF source-term integration
+    (``ember_source_adjoint``): for phi = sum(state_bar * state_out), returns
+    (state_out, status, d phi / d state, d phi / d ln(multiplier) per reaction).
+    Host (numpy) arrays."""
+    state = np.ascontiguousarray(state, dtype=np.float64)
+    n = state.shape[0]
+    dt = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,)))
+    bar = np.ascontiguousarray(state_bar, dtype=np.float64).reshape(state.shape)
+    sc = np.ascontiguousarray(split_const, dtype=np.float64) if split_const is not None else None
+    xx = np.ascontiguousarray(x, dtype=np.float64) if x is not None else None
+    out = np.empty_like(state)
+    status = np.zeros(n, dtype=np.int32)
+    gin = np.empty_like(state)
+    glnk = np.zeros(max(gmech.mech.n_reactions, 1))
+    rc = L.lib().ember_source_adjoint(gmech.handle, n, L.ptr(state), L.ptr(sc), L.ptr(dt), float(t_start), L.ptr(xx),
+                                      C.byref(opts), L.ptr(bar), int(tape_cap), L.ptr(out), L.ptr(status),
+                                      L.ptr(gin), L.ptr(glnk), L.MEM_HOST, None)
+    if rc not in (L.OK, L.EFAIL):
+        L.check(rc, "ember_source_adjoint")
+    return out, status, gin, glnk[:gmech.mech.n_reactions]

@@ -183,6 +183,16 @@ int ember_diffusion_integrate(int n_flames, const ember_diffusion_grid* grids, i
                               const ember_diffusion_options* opts, int* status,
                               int mem, void* stream);
 
+/* Adjoint of ember_diffusion_integrate with respect to the state: the stage
+ * is linear in y (y_out = M y_in + terms of the split constants), so for
+ * phi = ybar . y_out the gradient d phi / d y_in = M^T ybar; ybar (layout of
+ * y) is replaced by it. The sub-steps are run backwards with transposed
+ * Thomas solves (same rows, step-size rule and step count as the forward
+ * stage). B, D, wall_const are held fixed; split_const and y_inf do not enter M. */
+int ember_diffusion_adjoint(int n_flames, const ember_diffusion_grid* grids, int n_vars, const double* x,
+                            const double* B, const double* D, double* ybar, const ember_diffusion_options* opts,
+                            int* status, int mem, void* stream);
+
 /* Allocation-free variant of ember_diffusion_integrate, for callers that
  * must not allocate device memory while they step: an application whose
  * device memory is owned by another allocator (a framework's caching pool or
@@ -337,6 +347,23 @@ int ember_source_integrate(ember_mech mech, int method, int n_points, const doub
                            const double* split_const, const double* dt, double t_start, const double* x,
                            const ember_source_options* opts, double* state_out, int* status, int* stats,
                            int mem, void* stream);
+
+/* Discrete adjoint of a BDF source-term integration (EMBER_SOURCE_BDF, same
+ * arguments as ember_source_integrate): for phi = sum over points of
+ * state_bar . state_out, returns state_in_bar = d phi / d state_in
+ * [n_points][nVars] and lnk_bar = d phi / d ln(multiplier_i) of every
+ * reaction [n_reactions], summed over points (or NULL). The forward pass
+ * records every accepted step (at most tape_cap per point; 0: 1024); the
+ * backward pass linearises each step with its step size and order held
+ * fixed and the corrector converged, with the analytic Jacobian recomputed at
+ * the step's end state and the transposed solve on the LU of I - gamma J.
+ * There is no counterpart in the reference (CVODE is run forward only); it
+ * serves the gradients of FlameSolver's objectives. status: as
+ * ember_source_integrate, or -30 (tape overflow), -32 (singular matrix). */
+int ember_source_adjoint(ember_mech mech, int n_points, const double* state_in, const double* split_const,
+                         const double* dt, double t_start, const double* x, const ember_source_options* opts,
+                         const double* state_bar, int tape_cap, double* state_out, int* status,
+                         double* state_in_bar, double* lnk_bar, int mem, void* stream);
 
 /* Known-answer self-test of the device QSS integrator: integrates the
  * CHEMEQ2 cesium relaxation problem of the reference's QSS test

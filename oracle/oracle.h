@@ -76,6 +76,7 @@ typedef struct {
 typedef struct {
     double *cp_R, *h_RT, *g_RT, *c, *ym, *tmp, *kf, *rkc, *ropf, *ropr, *wq, *wd, *wn, *hk, *v;
     double *kf_fall, *k0_fall, *F_fall, *pr_fall, *concm, *jdense;  /* falloff terms, [M], Jacobian scratch */
+    double* dF_fall;                                                /* dF/dPr of the falloff blending */
     double ctot, mmw;
     double kT;
     int kModel;

@@ -125,8 +125,11 @@ static void bdf_jacobian(bdf_ode* ode, double t, const double* y, const double* 
             dropdm = rf * (pf - kr * pp);
             rf = rf * w->concm[i];
         } else if (fall) {
+            /* d/d[M] of kinf mult Pr/(1+Pr) F(Pr), Pr = k0 [M] / kinf */
             const double pr1 = 1.0 + w->pr_fall[i];
-            dropdm = ((w->F_fall[i] * (w->k0_fall[i] * m->mult[i])) / (pr1 * pr1)) * (pf - kr * pp);
+            const double k0m = w->k0_fall[i] * m->mult[i];
+            dropdm = ((w->F_fall[i] * k0m) / (pr1 * pr1) + (k0m * (w->pr_fall[i] / pr1)) * w->dF_fall[i]) *
+                     (pf - kr * pp);
         }
         /* derivative of the net rate of progress w.r.t. each species occurrence */
         double dv[2 * ORACLE_MAX_STOICH];

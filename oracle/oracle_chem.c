@@ -290,6 +290,7 @@ oracle_ws* oracle_ws_create(const oracle_mech* m) {
     w->k0_fall = (double*)calloc(R, sizeof(double));
     w->F_fall = (double*)calloc(R, sizeof(double));
     w->pr_fall = (double*)calloc(R, sizeof(double));
+    w->dF_fall = (double*)calloc(R, sizeof(double));
     w->concm = (double*)calloc(R, sizeof(double));
     w->jdense = (double*)calloc(S, sizeof(double));
     w->kT = NAN;
@@ -301,7 +302,7 @@ void oracle_ws_free(oracle_ws* w) {
     free(w->cp_R); free(w->h_RT); free(w->g_RT); free(w->c); free(w->ym); free(w->tmp);
     free(w->kf); free(w->rkc); free(w->ropf); free(w->ropr); free(w->wq); free(w->wd); free(w->wn);
     free(w->hk); free(w->v);
-    free(w->kf_fall); free(w->k0_fall); free(w->F_fall); free(w->pr_fall); free(w->concm); free(w->jdense);
+    free(w->kf_fall); free(w->k0_fall); free(w->F_fall); free(w->pr_fall); free(w->dF_fall); free(w->concm); free(w->jdense);
     free(w);
 }
 
@@ -416,7 +417,7 @@ void oracle_rates(const oracle_mech* m, oracle_ws* w, double p, int model, int m
             const double kinf = arrhenius(m->arr + 3 * i, lnT, rT);
             const double k0 = arrhenius(m->arr_low + 3 * i, lnT, rT);
             const double pr = (concm * k0) * (1.0 / (kinf + SMALL_NUMBER));
-            double F = 1.0;
+            double F = 1.0, dF = 0.0; /* dF: dF/dPr */
             if (ty == ORACLE_RXN_TROE) {
                 const double* tp = m->troe + 4 * i;
                 /* Fcent with the reciprocals 1/T3, 1/T1, as Cantera's Troe rate keeps them */
@@ -428,12 +429,19 @@ void oracle_rates(const oracle_mech* m, oracle_ws* w, double p, int model, int m
                 const double nn = fma(-1.27, lfc, 0.75);   /* 0.75 - 1.27 log Fcent */
                 const double x = lpr + cc;
                 const double f1 = x / fma(-0.14, x, nn);
-                F = oracle_exp10(lfc / fma(f1, f1, 1.0));
+                const double g = fma(f1, f1, 1.0);
+                F = oracle_exp10(lfc / g);
+                if (pr > SMALL_NUMBER) {
+                    /* d log10 F / d f1 = -2 lfc f1 / g^2; d f1 / dx = nn / (nn - 0.14 x)^2; dx / dPr = 1/(Pr ln 10) */
+                    const double den = fma(-0.14, x, nn);
+                    dF = ((F * ((-2.0 * lfc * f1) / (g * g))) * (nn / (den * den))) / pr;
+                }
             }
             kf = (pr * (F / (1.0 + pr))) * kinf;
             w->kf_fall[i] = kf;
             w->k0_fall[i] = k0;
             w->F_fall[i] = F;
+            w->dF_fall[i] = dF;
             w->pr_fall[i] = pr;
         }
         w->concm[i] = concm;
