@@ -9,7 +9,7 @@ with the reference's default options (interp kinetics), FP64, one launch per
 step. Metric: source-term point-integrations per second.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload qss|bdf|diffusion|split]
+                    [--workload qss|bdf|diffusion|split|adjoint]
 
 N > 1 runs under torch.distributed.run: every rank integrates its own batch
 of points (no data exchange; the path has none), value = all points / max
@@ -47,7 +47,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="qss", choices=["qss", "bdf", "diffusion", "split"])
+    p.add_argument("--workload", default="qss", choices=["qss", "bdf", "diffusion", "split", "adjoint"])
     p.add_argument("--points", type=int, default=N_POINTS)
     p.add_argument("--kinetics", default="interp", choices=["interp", "standard"])
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
@@ -623,12 +623,139 @@ def run_ours_split(args):
     return 0
 
 
+# ---------------------------------------------------- adjoint workload (C4) --
+
+ADJ_METRIC = "adjoint/forward cost"
+ADJ_DT = 2e-5
+ADJ_WORKLOAD = ("C4 proxy: one flame-like profile of 400 points, synthetic 53-species/325-reaction mechanism "
+                "(GRI-3.0 sizes), balanced D-S-D split step (dt 2e-5 s, BDF source with CVODE default tolerances), "
+                "gradient of heat release + consumption speed w.r.t. the start state and ln A of every reaction")
+
+
+def adjoint_inputs(rank: int):
+    from ember_gb300.mechanism import synthetic_mechanism
+    from ember_gb300.split import flame_batch
+    mech = synthetic_mechanism(n_species=53, n_reactions=325, seed=53325)
+    return (mech,) + flame_batch(mech, n_flames=1, n_min=400, n_max=400, seed=4000 + rank)
+
+
+def run_reference_adjoint(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    from oracle.chem import OracleMech
+    from oracle import split as osplit
+    from ember_gb300.source import BDF
+    mech, grids, state, B, D, rho_u, ju, jb = adjoint_inputs(0)
+    opts = source_options(args.kinetics, "bdf")
+    om = OracleMech(mech)
+    for _ in range(args.warmup):
+        osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, BDF, opts)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, BDF, opts)
+    fwd = (time.perf_counter() - t0) / args.steps
+    # the reference has no adjoint: central differences need 2 forward steps per ln A
+    ratio = 2.0 * mech.n_reactions
+    threads = os.cpu_count() or 1
+    print(json.dumps({
+        "impl": "reference", "metric": ADJ_METRIC, "value": ratio, "unit": "x", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * fwd * ratio, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": ADJ_WORKLOAD, "forward_ms": 1e3 * fwd,
+                   "gradient_method": "central differences of the CPU split step (2 steps per ln A)"},
+        "cpu_baseline": {"value": ratio, "unit": "x", "cores": threads, "kind": "port",
+                         "sample": f"one forward split step of the 400-point flame, {1e3 * fwd:.1f} ms"},
+        "e2e": {"value": ratio, "unit": "x", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+    return 0
+
+
+def run_ours_adjoint(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        torch.distributed.init_process_group("nccl")
+    from ember_gb300.source import GpuMechanism, BDF
+    from ember_gb300.split import FlameBatchSplitSolver
+    mech, grids, state, B, D, rho_u, ju, jb = adjoint_inputs(rank)
+    opts = source_options(args.kinetics, "bdf")
+    gm = GpuMechanism(mech)
+    solver = FlameBatchSplitSolver(gm, grids, ADJ_DT, method=BDF, source_options=opts)
+    solver.set_transport(B, D)
+    stream = torch.cuda.current_stream()
+    wq, wsc = np.ones(1), np.ones(1)
+
+    def forward():
+        solver.set_state(0.0, state)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        solver.step(1, stream=stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    def adjoint():
+        solver.set_state(0.0, state)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = solver.adjoint(wq, wsc, rho_u, ju, jb, tape_cap=4096)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), out
+
+    for _ in range(args.warmup):
+        forward()
+        adjoint()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    fw, ad = [], []
+    for _ in range(args.steps):
+        fw.append(forward())
+        t_ad, (hr, cs, sbar, lbar) = adjoint()
+        ad.append(t_ad)
+    clocks = sampler.stop()
+    fwd_ms, adj_ms = sum(fw) / len(fw), sum(ad) / len(ad)
+    line = {
+        "metric": ADJ_METRIC, "value": adj_ms / fwd_ms, "unit": "x", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": adj_ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded flame-like profile, synthetic transport)",
+        "config": {"workload": ADJ_WORKLOAD, "forward_ms": fwd_ms, "adjoint_ms": adj_ms,
+                   "gradients": int(state.size + mech.n_reactions), "heat_release": float(hr[0]),
+                   "consumption_speed": float(cs[0])},
+        "e2e": {"value": adj_ms / fwd_ms, "unit": "x", "h2d_bytes_per_step": int(state.nbytes),
+                "d2h_bytes_per_step": int(state.nbytes + 8 * mech.n_reactions)},
+        "gpu_launches": None,
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        from oracle.chem import OracleMech
+        from oracle import split as osplit
+        om = OracleMech(mech)
+        t0 = time.perf_counter()
+        osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, BDF, opts)
+        tcpu = time.perf_counter() - t0
+        threads = os.cpu_count() or 1
+        line["cpu_baseline"] = {"value": 2.0 * mech.n_reactions, "unit": "x", "cores": threads, "kind": "port",
+                                "sample": f"central differences on the CPU split step: 2 x {mech.n_reactions} "
+                                          f"forward steps of {1e3 * tcpu:.0f} ms each ({threads} threads)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse_args()
     if args.workload == "diffusion":
         return run_reference_diffusion(args) if args.impl == "reference" else run_ours_diffusion(args)
     if args.workload == "split":
         return run_reference_split(args) if args.impl == "reference" else run_ours_split(args)
+    if args.workload == "adjoint":
+        return run_reference_adjoint(args) if args.impl == "reference" else run_ours_adjoint(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -57,16 +57,16 @@ struct BdfPoint {
     MechView m;
     ChemSmem w;
     BdfSmem v;
-    const SourceArgs* a;
-    const double* split;
-    double x;
-    double* J;       // global, column-major n x n
-    double* M;       // global, column-major n x n (LU factors)
-    int n, S;
-    double rho, cp, qdot;
-    double cachedT;
-    int nfe;
-    double* tape;  // this point's tape, or null
+    const SourceArgs* a = nullptr;
+    const double* split = nullptr;
+    double x = 0.0;
+    double* J = nullptr;  // global, column-major n x n
+    double* M = nullptr;  // global, column-major n x n (LU factors)
+    int n = 0, S = 0;
+    double rho = 0.0, cp = 0.0, qdot = 0.0;
+    double cachedT = 0.0;
+    int nfe = 0;
+    double* tape = nullptr;  // this point's tape, or null
 
     __device__ double atol(int i) const { return i == 0 ? a->bdf_atol_u : (i == 1 ? a->bdf_atol_t : a->bdf_atol_y); }
 
@@ -930,6 +930,8 @@ __global__ void __launch_bounds__(NT) k_source_bdf_adjoint(MechView m, SourceArg
         __syncthreads();
         if (j >= a.n) break;
         const double* tape = a.tape + size_t(j) * a.tape_stride;
+        P.split = a.split ? a.split + size_t(j) * n : nullptr;
+        P.x = a.x ? a.x[j] : 0.0;
         double* pb = pbar + size_t(j) * m.R;
         for (int i = tid; i < m.R; i += NT) pb[i] = 0.0;
         const int N = static_cast<int>(tape[0]);

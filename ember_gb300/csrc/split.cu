@@ -244,6 +244,124 @@ __global__ void k_flame_objectives(int n_flames, const int* __restrict__ npts, c
     }
 }
 
+// ---- adjoint of the objectives and of the mass-fraction correction ------
+
+// d I / d y_i of the spline integral I(y) = mathUtils::integrate(x, y): the
+// integral is linear in y, so these weights are the reverse pass of
+// spline_integral (one thread per flame; work: 4 doubles per point).
+__global__ void k_spline_weights(int n_flames, const int* __restrict__ npts, const int64_t* __restrict__ goff,
+                                 const double* __restrict__ x, double* __restrict__ work, double* __restrict__ w) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_flames) return;
+    const int n = npts[f];
+    const int64_t o = goff[f];
+    const double* xf = x + o;
+    double* wf = w + o;
+    double* u = work + 4 * o;
+    double* vb = u + n;
+    double* zb = vb + n;
+    double* bb = zb + n;
+    auto hh = [&](int i) { return xf[i + 1] - xf[i]; };
+    u[1] = 2 * (hh(0) + hh(1));
+    for (int i = 2; i < n - 1; i++) u[i] = 2 * (hh(i - 1) + hh(i)) - hh(i - 1) * hh(i - 1) / u[i - 1];
+    for (int i = 0; i < n; ++i) {
+        wf[i] = 0.0;
+        zb[i] = 0.0;
+        vb[i] = 0.0;
+        bb[i] = 0.0;
+    }
+    // I = sum_i h_i y_i + h_i^2 c1_i / 2 + h_i^3 c2_i / 3 + h_i^4 c3_i / 4
+    for (int i = 0; i < n - 1; i++) {
+        const double h = hh(i);
+        wf[i] += h - 0.5 * h;
+        wf[i + 1] += 0.5 * h;
+        const double h3 = h * h * h;
+        zb[i] += -h3 / 24.0;
+        zb[i + 1] += -h3 / 24.0;
+    }
+    // z_i = (v_i - h_i z_{i+1}) / u_i, computed for i = n-2..1 (z_0 = z_{n-1} = 0)
+    for (int i = 1; i <= n - 2; i++) {
+        const double t = zb[i] / u[i];
+        vb[i] += t;
+        zb[i + 1] -= hh(i) * t;
+    }
+    // v_i = 6 (b_i - b_{i-1}) - h_{i-1} v_{i-1} / u_{i-1} (i >= 2), v_1 = 6 (b_1 - b_0)
+    for (int i = n - 2; i >= 2; i--) {
+        bb[i] += 6 * vb[i];
+        bb[i - 1] -= 6 * vb[i];
+        vb[i - 1] -= hh(i - 1) / u[i - 1] * vb[i];
+    }
+    if (n >= 3) {
+        bb[1] += 6 * vb[1];
+        bb[0] -= 6 * vb[1];
+    }
+    // b_i = (y_{i+1} - y_i) / h_i
+    for (int i = 0; i < n - 1; i++) {
+        const double t = bb[i] / hh(i);
+        wf[i + 1] += t;
+        wf[i] -= t;
+    }
+}
+
+// Per point: gq = d J / d qdot, gcp = d J / d cp, gT = d J / d T for
+// J = sum_f wq_f Q_f + ws_f S_c,f (one thread per flame).
+__global__ void k_objective_weights(int n_flames, const int* __restrict__ npts, const int64_t* __restrict__ goff,
+                                    const double* __restrict__ omega, const double* __restrict__ qdot,
+                                    const double* __restrict__ cp, const double* __restrict__ T,
+                                    const double* __restrict__ wq, const double* __restrict__ ws,
+                                    const double* __restrict__ rho_u, const int* __restrict__ ju,
+                                    const int* __restrict__ jb, const double* __restrict__ sc_val,
+                                    double* __restrict__ gq, double* __restrict__ gcp, double* __restrict__ gT) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_flames) return;
+    const int n = npts[f];
+    const int64_t o = goff[f];
+    const double a = wq ? wq[f] : 0.0;
+    const double b = ws ? ws[f] : 0.0;
+    double D = 1.0, dT = 1.0;
+    if (b != 0.0) {
+        dT = T[o + jb[f]] - T[o + ju[f]];
+        D = rho_u[f] * dT;
+    }
+    for (int i = 0; i < n; ++i) {
+        const int64_t p = o + i;
+        const double c = cp[p];
+        gq[p] = omega[p] * (a + (b != 0.0 ? b / (c * D) : 0.0));
+        gcp[p] = b != 0.0 ? -b * omega[p] * qdot[p] / (c * c * D) : 0.0;
+        gT[p] = 0.0;
+    }
+    if (b != 0.0) {
+        const double s = sc_val[f];
+        gT[o + jb[f]] += -b * s / dT;
+        gT[o + ju[f]] += b * s / dT;
+    }
+}
+
+// Adjoint of k_correct_mass_fractions: Y' = max(Y, 0) / sum max(Y, 0).
+__global__ void k_correct_mass_fractions_adjoint(int64_t n_pts, int n, const double* __restrict__ xF,
+                                                 double* __restrict__ ybar) {
+    for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < n_pts; p += int64_t(gridDim.x) * blockDim.x) {
+        const double* Y = xF + p * n + 2;
+        double* g = ybar + p * n + 2;
+        double sum = 0.0;
+        for (int k = 0; k < n - 2; ++k) sum = sum + (Y[k] < 0.0 ? 0.0 : Y[k]);
+        const double r = 1.0 / sum;
+        double dot = 0.0;
+        for (int k = 0; k < n - 2; ++k) dot = fma((Y[k] < 0.0 ? 0.0 : Y[k]) * r, g[k], dot);
+        for (int k = 0; k < n - 2; ++k) g[k] = Y[k] < 0.0 ? 0.0 : (g[k] - dot) * r;
+    }
+}
+
+// Sum of per-point rows [n_pts][R] (two arrays) over points, in point order.
+__global__ void k_sum_rows2(int64_t n_pts, int R, const double* __restrict__ a, const double* __restrict__ b,
+                            double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < R; i += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int64_t j = 0; j < n_pts; ++j) s += a[j * R + i] + b[j * R + i];
+        out[i] = s;
+    }
+}
+
 int grid_for(int64_t n, int threads = 256) {
     return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 4096)));
 }
@@ -282,7 +400,6 @@ struct ember_split_s {
     size_t diff_arena_bytes = 0;
     void* src_arena = nullptr;
     size_t src_arena_bytes = 0;
-    bool have_cross = false;
     DiffusionWarpPlan plan;
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
@@ -291,7 +408,8 @@ struct ember_split_s {
     SplitTables tables() const { return SplitTables{n_pts, n_vars, vm_base, npt}; }
 
     SourceArgs source_args() const {
-        SourceArgs a = make_source_args(&opt.source, static_cast<int>(n_pts), state, sc_prod, dtp, 0.0, x, state,
+        // input from the snapshot taken before the stage (the adjoint's last step reads it)
+        SourceArgs a = make_source_args(&opt.source, static_cast<int>(n_pts), xD2, sc_prod, dtp, 0.0, x, state,
                                         src_status, src_stats);
         a.t_start_dev = t_dev;
         return a;
@@ -353,12 +471,21 @@ int enqueue_diffusion_pair(ember_split h, double f0, double f1, double f2, cudaS
 }
 
 // One split step, enqueued on `st` (kernel launches and device copies only).
-int enqueue_step(ember_split h, cudaStream_t st) {
+// What a taped step (the forward pass of ember_split_adjoint) keeps.
+struct StepTape {
+    double* t_saved;  // device clock at the start of the step
+    double* buf;      // BDF tape of the source stage
+    int64_t stride;
+    int cap;
+    double* xF;       // state before the mass-fraction correction
+};
+
+int enqueue_step(ember_split h, cudaStream_t st, const StepTape* tape = nullptr) {
     const SplitTables tb = h->tables();
     const int g = grid_for(h->n_vals);
-    k_split_begin<<<g, 256, 0, st>>>(tb, h->opt.balanced, h->ddt_diff, h->ddt_prod,
-                                     h->have_cross ? h->ddt_cross : nullptr, h->sc_diff, h->sc_diff_vm, h->sc_prod,
-                                     h->delta_vm);
+    if (tape) EMBER_CUDA_TRY(cudaMemcpyAsync(tape->t_saved, h->t_dev, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    k_split_begin<<<g, 256, 0, st>>>(tb, h->opt.balanced, h->ddt_diff, h->ddt_prod, h->ddt_cross, h->sc_diff,
+                                     h->sc_diff_vm, h->sc_prod, h->delta_vm);
     // diffusion 1/4 and 2/4
     EMBER_TRY(enqueue_diffusion_pair(h, 0.0, 0.25, 0.5, st));
     k_to_pointmajor<<<g, 256, 0, st>>>(tb, h->yv, h->state, h->xD2);
@@ -367,7 +494,12 @@ int enqueue_step(ember_split h, cudaStream_t st) {
     {
         Scratch sc(st, h->src_arena, h->src_arena_bytes);
         EMBER_CUDA_TRY(cudaMemsetAsync(h->src_counter, 0, sizeof(int), st));
-        const SourceArgs a = h->source_args();
+        SourceArgs a = h->source_args();
+        if (tape) {
+            a.tape = tape->buf;
+            a.tape_stride = tape->stride;
+            a.tape_cap = tape->cap;
+        }
         if (h->opt.method == EMBER_SOURCE_QSS) {
             EMBER_TRY(launch_source_qss(h->mech->view, a, h->src_counter, sc, st));
         } else {
@@ -381,6 +513,7 @@ int enqueue_step(ember_split h, cudaStream_t st) {
     k_to_pointmajor<<<g, 256, 0, st>>>(tb, h->yv, h->state, nullptr);
     k_split_end<<<g, 256, 0, st>>>(tb, h->opt.dt, h->xS, h->xD2, h->delta_vm, h->sc_diff, h->sc_prod, h->ddt_diff,
                                    h->ddt_prod);
+    if (tape) EMBER_CUDA_TRY(cudaMemcpyAsync(tape->xF, h->state, sizeof(double) * h->n_vals, cudaMemcpyDeviceToDevice, st));
     k_correct_mass_fractions<<<grid_for(h->n_pts, 128), 128, 0, st>>>(h->n_pts, h->n_vars, h->state);
     k_advance_clock<<<1, 32, 0, st>>>(h->t_dev, h->opt.dt);
     EMBER_CUDA_TRY(cudaGetLastError());
@@ -700,6 +833,131 @@ extern "C" int ember_split_objectives(ember_split h, const double* rho_u, const 
     EMBER_TRY(stage_out(qdot, q, size_t(h->n_pts), mem, st));
     EMBER_TRY(stage_out(heat_release, hr, size_t(h->n_flames), mem, st));
     EMBER_TRY(stage_out(consumption_speed, cs, size_t(h->n_flames), mem, st));
+    sc.release();
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_split_adjoint(ember_split h, const double* w_heat_release, const double* w_consumption_speed,
+                                   const double* rho_u, const int* ju, const int* jb, int tape_cap,
+                                   double* heat_release, double* consumption_speed, double* state_bar,
+                                   double* lnk_bar, int mem, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(h->opt.method == EMBER_SOURCE_BDF, "the split-step adjoint needs EMBER_SOURCE_BDF");
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_CHECK_ARG(w_heat_release || w_consumption_speed, "no objective weights");
+    EMBER_CHECK_ARG(!w_consumption_speed || (rho_u && ju && jb), "consumption speed needs rho_u, ju and jb");
+    EMBER_CHECK_ARG(tape_cap >= 0 && tape_cap <= (1 << 20), "bad tape_cap %d", tape_cap);
+    if (tape_cap == 0) tape_cap = 1024;
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    const MechView& m = h->mech->view;
+    const int n = h->n_vars, S = m.S, R = std::max(m.R, 1);
+    const int64_t np = h->n_pts, nv = h->n_vals;
+    const int nf = h->n_flames;
+    // ---- forward: one taped step, then the objectives
+    StepTape tape{};
+    tape.cap = tape_cap;
+    tape.stride = bdf_tape_doubles(n, tape_cap);
+    EMBER_TRY(sc.alloc(&tape.t_saved, 1));
+    EMBER_TRY(sc.alloc(&tape.buf, size_t(np) * tape.stride));
+    EMBER_TRY(sc.alloc(&tape.xF, size_t(nv)));
+    EMBER_TRY(enqueue_step(h, st, &tape));
+    double *T, *Y, *net, *hk, *cp, *q, *qcp, *work, *hr, *cs;
+    EMBER_TRY(sc.alloc(&T, np));
+    EMBER_TRY(sc.alloc(&Y, size_t(np) * S));
+    EMBER_TRY(sc.alloc(&net, size_t(np) * S));
+    EMBER_TRY(sc.alloc(&hk, size_t(np) * S));
+    EMBER_TRY(sc.alloc(&cp, np));
+    EMBER_TRY(sc.alloc(&q, np));
+    EMBER_TRY(sc.alloc(&qcp, np));
+    EMBER_TRY(sc.alloc(&work, 4 * np));
+    EMBER_TRY(sc.alloc(&hr, nf));
+    EMBER_TRY(sc.alloc(&cs, nf));
+    const double *d_wq = nullptr, *d_ws = nullptr, *d_rho = nullptr;
+    const int *d_ju = nullptr, *d_jb = nullptr;
+    EMBER_TRY(stage_in(sc, w_heat_release, size_t(nf), mem, st, &d_wq));
+    EMBER_TRY(stage_in(sc, w_consumption_speed, size_t(nf), mem, st, &d_ws));
+    if (w_consumption_speed) {
+        EMBER_TRY(stage_in(sc, rho_u, size_t(nf), mem, st, &d_rho));
+        EMBER_TRY(stage_in(sc, ju, size_t(nf), mem, st, &d_ju));
+        EMBER_TRY(stage_in(sc, jb, size_t(nf), mem, st, &d_jb));
+    }
+    k_gather_TY<<<grid_for(np * S), 256, 0, st>>>(np, n, h->state, T, Y);
+    EMBER_TRY(ember_gas_eval(h->mech, static_cast<int>(np), h->opt.source.pressure, h->opt.source.kinetics_model,
+                             EMBER_STATE_NORMALIZED, T, Y, nullptr, nullptr, net, hk, cp, nullptr, EMBER_MEM_DEVICE,
+                             stream));
+    k_qdot<<<grid_for(np, 128), 128, 0, st>>>(np, S, net, hk, cp, q, qcp);
+    k_flame_objectives<<<blocks_for(nf, 64), 64, 0, st>>>(nf, h->flame_npts, h->flame_goff, h->x, q, qcp, T, d_rho,
+                                                          d_ju, d_jb, work, hr, d_ws ? cs : nullptr);
+    // ---- backward: objectives -> end state
+    double *omega, *gq, *gcp, *gT, *ybar, *prow_obj, *prow_src, *ybar2;
+    int* adj_status;
+    EMBER_TRY(sc.alloc(&omega, np));
+    EMBER_TRY(sc.alloc(&gq, np));
+    EMBER_TRY(sc.alloc(&gcp, np));
+    EMBER_TRY(sc.alloc(&gT, np));
+    EMBER_TRY(sc.alloc(&ybar, nv));
+    EMBER_TRY(sc.alloc(&ybar2, nv));
+    EMBER_TRY(sc.alloc(&prow_obj, size_t(np) * R));
+    EMBER_TRY(sc.alloc(&prow_src, size_t(np) * R));
+    EMBER_TRY(sc.alloc(&adj_status, np));
+    k_spline_weights<<<blocks_for(nf, 64), 64, 0, st>>>(nf, h->flame_npts, h->flame_goff, h->x, work, omega);
+    k_objective_weights<<<blocks_for(nf, 64), 64, 0, st>>>(nf, h->flame_npts, h->flame_goff, omega, q, cp, T, d_wq,
+                                                           d_ws, d_rho, d_ju, d_jb, cs, gq, gcp, gT);
+    SourceArgs oa = make_source_args(&h->opt.source, static_cast<int>(np), nullptr, nullptr, nullptr, 0.0, nullptr,
+                                     nullptr, nullptr, nullptr);
+    oa.ign_energy = 0.0;  // calculateQdot has no igniter term
+    EMBER_TRY(launch_objective_vjp(m, oa, static_cast<int>(np), h->state, gq, gcp, gT, ybar, prow_obj, sc, st));
+    // mass-fraction correction
+    k_correct_mass_fractions_adjoint<<<grid_for(np, 128), 128, 0, st>>>(np, n, tape.xF, ybar);
+    // diffusion 4/4 and 3/4 (transposed), in the variable-major layout
+    const SplitTables tb = h->tables();
+    const int g = grid_for(nv);
+    double* dwork;
+    EMBER_TRY(sc.alloc(&dwork, size_t(7) * nv));
+    auto diffusion_pair_adjoint = [&](double fa, double fb, double fc) -> int {
+        k_to_varmajor<<<g, 256, 0, st>>>(tb, ybar, ybar2, h->ystart);
+        const DiffusionView dv = h->diffusion_view(h->diff_status);
+        const double fr[3] = {fa, fb, fc};
+        for (int k = 1; k >= 0; --k) {
+            StageTime tm;
+            tm.t_dev = tape.t_saved;
+            tm.f0 = fr[k];
+            tm.f1 = fr[k + 1];
+            tm.dt = h->opt.dt;
+            EMBER_TRY(diffusion_adjoint_run(dv, ybar2, dwork, nv, h->nmax, tm, h->opt.dt_multiplier, h->opt.dt, st));
+        }
+        k_to_pointmajor<<<g, 256, 0, st>>>(tb, ybar2, ybar, nullptr);
+        return EMBER_OK;
+    };
+    EMBER_TRY(diffusion_pair_adjoint(0.5, 0.75, 1.0));
+    // source stage
+    {
+        SourceArgs a = h->source_args();
+        a.t_start_dev = tape.t_saved;
+        a.tape = tape.buf;
+        a.tape_stride = tape.stride;
+        a.tape_cap = tape.cap;
+        int* counter = nullptr;
+        EMBER_TRY(sc.alloc(&counter, 1));
+        EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
+        EMBER_TRY(launch_source_bdf_adjoint(m, a, counter, ybar, ybar2, prow_src, adj_status, sc, st));
+        EMBER_CUDA_TRY(cudaMemcpyAsync(ybar, ybar2, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st));
+        k_count_failures<<<grid_for(np), 256, 0, st>>>(static_cast<int>(np), adj_status, h->fails);
+    }
+    // diffusion 2/4 and 1/4
+    EMBER_TRY(diffusion_pair_adjoint(0.0, 0.25, 0.5));
+    // ---- outputs
+    double* d_lnk = nullptr;
+    EMBER_TRY(stage_buffer(sc, lnk_bar, size_t(R), mem, &d_lnk));
+    if (d_lnk) k_sum_rows2<<<blocks_for(R, 128), 128, 0, st>>>(np, R, prow_obj, prow_src, d_lnk);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    const cudaMemcpyKind kind = mem == EMBER_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (state_bar) EMBER_CUDA_TRY(cudaMemcpyAsync(state_bar, ybar, sizeof(double) * nv, kind, st));
+    if (heat_release) EMBER_CUDA_TRY(cudaMemcpyAsync(heat_release, hr, sizeof(double) * nf, kind, st));
+    if (consumption_speed && d_ws)
+        EMBER_CUDA_TRY(cudaMemcpyAsync(consumption_speed, cs, sizeof(double) * nf, kind, st));
+    if (lnk_bar) EMBER_TRY(stage_out(lnk_bar, d_lnk, size_t(m.R), mem, st));
     sc.release();
     return finish_call(mem, st);
 }

@@ -41,6 +41,7 @@ def _declare(lib):
         "ember_split_source_status": (C.c_int, [vp, vp, vp, C.c_int, vp]),
         "ember_split_failures": (C.c_int, [vp, vp, vp, vp]),
         "ember_split_objectives": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, C.c_int, vp]),
+        "ember_split_adjoint": (C.c_int, [vp, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, C.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -171,6 +172,27 @@ class FlameBatchSplitSolver:
         L.check(_lib().ember_split_objectives(self._h, L.ptr(r), L.ptr(a), L.ptr(b), q.ctypes.data, hr.ctypes.data,
                                               L.ptr(cs), L.MEM_HOST, None), "objectives")
         return q, hr, cs
+
+    def adjoint(self, w_heat_release=None, w_consumption_speed=None, rho_u=None, ju=None, jb=None,
+                tape_cap: int = 0):
+        """One split step from the current state and the gradient of
+        J = sum_f w_heat_release[f] Q_f + w_consumption_speed[f] S_c,f at its end
+        with respect to the state at its start and ln(multiplier) of every
+        reaction (``ember_split_adjoint``; BDF source). Returns (Q, S_c or None,
+        d J / d state [n_points, S+2], d J / d ln multiplier [R])."""
+        nf = len(self.grids)
+        f64 = lambda v: np.ascontiguousarray(v, dtype=np.float64) if v is not None else None
+        i32 = lambda v: np.ascontiguousarray(v, dtype=np.int32) if v is not None else None
+        wq, ws, r = f64(w_heat_release), f64(w_consumption_speed), f64(rho_u)
+        a, b = i32(ju), i32(jb)
+        hr = np.empty(nf)
+        cs = np.empty(nf) if ws is not None else None
+        sbar = np.empty((self.n_points, self.n_vars))
+        lbar = np.empty(max(self.gmech.mech.n_reactions, 1))
+        L.check(_lib().ember_split_adjoint(self._h, L.ptr(wq), L.ptr(ws), L.ptr(r), L.ptr(a), L.ptr(b), int(tape_cap),
+                                           hr.ctypes.data, L.ptr(cs), sbar.ctypes.data, lbar.ctypes.data, L.MEM_HOST,
+                                           None), "ember_split_adjoint")
+        return hr, cs, sbar, lbar[:self.gmech.mech.n_reactions]
 
 
 def mixture_properties(mech: Mechanism, state, pressure: float = 101325.0):

@@ -451,6 +451,24 @@ int ember_split_failures(ember_split split, int64_t* source_points, int64_t* dif
 int ember_split_objectives(ember_split split, const double* rho_u, const int* ju, const int* jb, double* qdot,
                            double* heat_release, double* consumption_speed, int mem, void* stream);
 
+/* One split step from the current state (which it advances, as
+ * ember_split_step) and the gradient of
+ *   J = sum_f w_heat_release[f] Q_f + w_consumption_speed[f] S_c,f
+ * at the end of that step (either weight array may be NULL) with respect to
+ * the state at its start (state_bar, point-major) and to ln(multiplier) of
+ * every reaction (lnk_bar [n_reactions]). Needs EMBER_SOURCE_BDF. Backward
+ * pass: the objectives' gradient at the end state (spline weights of
+ * mathUtils::integrate, the analytic Jacobian of qdot and cp), the
+ * mass-fraction correction, the transposed diffusion stages, the discrete
+ * adjoint of the BDF source stage (see ember_source_adjoint; tape_cap
+ * accepted steps per point, 0: 1024), the first two diffusion stages. The
+ * split constants of the step are held fixed (they come from the previous
+ * step's time derivatives). Q_f and S_c,f of the step are returned in
+ * heat_release / consumption_speed when given. */
+int ember_split_adjoint(ember_split split, const double* w_heat_release, const double* w_consumption_speed,
+                        const double* rho_u, const int* ju, const int* jb, int tape_cap, double* heat_release,
+                        double* consumption_speed, double* state_bar, double* lnk_bar, int mem, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,3 +101,63 @@ def test_diffusion_adjoint_is_the_transpose_of_the_stage(gpu_lib, explicit_h):
         M[:, i] = out
     ref = M.T @ ybar
     np.testing.assert_allclose(got, ref, rtol=1e-11, atol=1e-12 * np.abs(ref).max())
+
+
+def test_split_step_gradients_match_central_differences_of_the_oracle(gpu_lib):
+    # Heat release and consumption speed after one balanced D-S-D split step
+    # (BDF source, serial diffusion): gradients through torch.autograd (the
+    # discrete adjoint of the step) against central differences of the CPU
+    # restatement of the same step.
+    torch = pytest.importorskip("torch")
+    from oracle import split as osplit
+    from oracle.chem import OracleMech
+    from ember_gb300 import _lib as L
+    from ember_gb300.autograd import split_step_objectives
+    from ember_gb300.source import GpuMechanism
+    from ember_gb300.split import FlameBatchSplitSolver, flame_batch
+    mech = synthetic_mechanism(n_species=20, n_reactions=60, seed=3)
+    grids, state, B, D, rho_u, ju, jb = flame_batch(mech, n_flames=2, n_min=10, n_max=12, seed=5, width=2e-3,
+                                                    thickness=3e-4, T_b=1500.0)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD, bdf_reltol=1e-9, bdf_abstol_momentum=1e-9,
+                                  bdf_abstol_energy=1e-9, bdf_abstol_species=1e-15)
+    dt = 1e-6
+    gm = GpuMechanism(mech)
+    solver = FlameBatchSplitSolver(gm, grids, dt, method=BDF, source_options=opts,
+                                   diffusion_algorithm=L.DIFFUSION_SERIAL)
+    solver.set_transport(B, D)
+    R = mech.n_reactions
+    s0 = torch.tensor(state, dtype=torch.float64, requires_grad=True)
+    lk = torch.zeros(R, dtype=torch.float64, requires_grad=True)
+    out = split_step_objectives(solver, s0, lk, 0.0, rho_u, ju, jb, 4096)
+    w = torch.tensor([1.0, -0.5, 2e3, 1e3], dtype=torch.float64)  # Q_0, Q_1, S_c,0, S_c,1
+    (out * w).sum().backward()
+    g_state = s0.grad.numpy()
+    g_lnk = lk.grad.numpy()
+    om = OracleMech(mech)
+
+    def J(st, mult=None):
+        om.set_multipliers(mult)
+        y, *_ = osplit.split_steps(om, grids, st, 0.0, B, D, dt, 1, BDF, opts)
+        _, hr, cs = osplit.objectives(om, grids, y, opts.pressure, opts.kinetics_model, rho_u, ju, jb)
+        return float(np.dot(w.numpy(), np.concatenate([hr, cs])))
+
+    # the forward values are the oracle's (serial diffusion, bitwise source and objectives)
+    om.set_multipliers(None)
+    y_ref, *_ = osplit.split_steps(om, grids, state, 0.0, B, D, dt, 1, BDF, opts)
+    _, hr_ref, cs_ref = osplit.objectives(om, grids, y_ref, opts.pressure, opts.kinetics_model, rho_u, ju, jb)
+    assert np.array_equal(out.detach().numpy(), np.concatenate([hr_ref, cs_ref]))
+    n0 = grids[0].n_points
+    # state entries away from Y = 0, where the clipping of setState_TPY makes J one-sided
+    for (p, k) in [(3, 1), (n0 + 5, 1), (4, 2), (n0 + 6, 3), (2, 4), (n0 - 2, 5)]:
+        assert state[p, k] > 1e-6
+        hstep = 1e-4 * max(abs(state[p, k]), 1e-6)
+        e = np.zeros_like(state)
+        e[p, k] = hstep
+        fd = (J(state + e) - J(state - e)) / (2 * hstep)
+        assert abs(g_state[p, k] - fd) <= 2e-3 * abs(fd) + 1e-9 * np.abs(g_state).max(), (p, k, g_state[p, k], fd)
+    for i in np.argsort(-np.abs(g_lnk))[:3]:
+        mp, mm = np.ones(R), np.ones(R)
+        mp[i], mm[i] = np.exp(1e-3), np.exp(-1e-3)
+        fd = (J(state, mp) - J(state, mm)) / 2e-3
+        assert abs(g_lnk[i] - fd) <= 2e-3 * abs(fd), (i, g_lnk[i], fd)
+    om.set_multipliers(None)
