@@ -324,12 +324,13 @@ struct BdfPoint {
             const double r = 1.0 / colk[k];
             for (int i = k + 1 + tid; i < n; i += NT) colk[i] = colk[i] * r;
             __syncthreads();
-            // trailing update: one thread per row, columns in order
-            for (int i = k + 1 + tid; i < n; i += NT) {
-                const double l = colk[i];
-                for (int j = k + 1; j < n; ++j) {
-                    double* aij = M + size_t(j) * n + i;
-                    *aij = fma(-l, M[size_t(j) * n + k], *aij);
+            // trailing update a_ij -= l_i a_kj: one warp per column, lanes over rows
+            {
+                const int warp = tid >> 5, lane = tid & 31;
+                for (int j = k + 1 + warp; j < n; j += NT / 32) {
+                    double* colj = M + size_t(j) * n;
+                    const double akj = colj[k];
+                    for (int i = k + 1 + lane; i < n; i += 32) colj[i] = fma(-colk[i], akj, colj[i]);
                 }
             }
             __syncthreads();
@@ -341,28 +342,31 @@ struct BdfPoint {
     // (P M = L U, so M^T = U^T L^T P): U^T forward, L^T backward, then the
     // row interchanges undone in reverse order.
     __device__ void lu_solve_transpose(double* b) {
-        const int tid = threadIdx.x;
-        for (int k = 0; k < n; ++k) {
-            const double zk = b[k] / M[size_t(k) * n + k];
-            __syncthreads();
-            if (tid == 0) b[k] = zk;
-            for (int j = k + 1 + tid; j < n; j += NT) b[j] = fma(-M[size_t(j) * n + k], zk, b[j]);
-            __syncthreads();
-        }
-        for (int k = n - 1; k >= 1; --k) {
-            const double uk = b[k];
-            for (int i = tid; i < k; i += NT) b[i] = fma(-M[size_t(i) * n + k], uk, b[i]);
-            __syncthreads();
-        }
-        if (tid == 0)
-            for (int k = n - 1; k >= 0; --k) {
-                const int p = v.piv[k];
-                if (p != k) {
-                    const double tt = b[k];
-                    b[k] = b[p];
-                    b[p] = tt;
-                }
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            for (int k = 0; k < n; ++k) {
+                const double zk = b[k] / M[size_t(k) * n + k];
+                __syncwarp();
+                if (lane == 0) b[k] = zk;
+                for (int j = k + 1 + lane; j < n; j += 32) b[j] = fma(-M[size_t(j) * n + k], zk, b[j]);
+                __syncwarp();
             }
+            for (int k = n - 1; k >= 1; --k) {
+                const double uk = b[k];
+                for (int i = lane; i < k; i += 32) b[i] = fma(-M[size_t(i) * n + k], uk, b[i]);
+                __syncwarp();
+            }
+            if (lane == 0)
+                for (int k = n - 1; k >= 0; --k) {
+                    const int p = v.piv[k];
+                    if (p != k) {
+                        const double tt = b[k];
+                        b[k] = b[p];
+                        b[p] = tt;
+                    }
+                }
+        }
         __syncthreads();
     }
 
@@ -400,32 +404,38 @@ struct BdfPoint {
         }
     }
 
+    // Forward and back substitution with the factors, by the first warp
+    // (warp barriers instead of block barriers between the n steps).
     __device__ void lu_solve(double* b) {
-        const int tid = threadIdx.x;
-        if (tid == 0)
-            for (int k = 0; k < n; ++k) {
-                const int p = v.piv[k];
-                if (p != k) {
-                    const double tt = b[k];
-                    b[k] = b[p];
-                    b[p] = tt;
-                }
-            }
         __syncthreads();
-        for (int k = 0; k < n; ++k) {
-            const double bk = b[k];
-            const double* colk = M + size_t(k) * n;
-            for (int i = k + 1 + tid; i < n; i += NT) b[i] = fma(-colk[i], bk, b[i]);
-            __syncthreads();
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            if (lane == 0)
+                for (int k = 0; k < n; ++k) {
+                    const int p = v.piv[k];
+                    if (p != k) {
+                        const double tt = b[k];
+                        b[k] = b[p];
+                        b[p] = tt;
+                    }
+                }
+            __syncwarp();
+            for (int k = 0; k < n; ++k) {
+                const double bk = b[k];
+                const double* colk = M + size_t(k) * n;
+                for (int i = k + 1 + lane; i < n; i += 32) b[i] = fma(-colk[i], bk, b[i]);
+                __syncwarp();
+            }
+            for (int k = n - 1; k >= 0; --k) {
+                const double* colk = M + size_t(k) * n;
+                const double bk = b[k] / colk[k];
+                __syncwarp();
+                if (lane == 0) b[k] = bk;
+                for (int i = lane; i < k; i += 32) b[i] = fma(-colk[i], bk, b[i]);
+                __syncwarp();
+            }
         }
-        for (int k = n - 1; k >= 0; --k) {
-            const double* colk = M + size_t(k) * n;
-            const double bk = b[k] / colk[k];
-            __syncthreads();
-            if (tid == 0) b[k] = bk;
-            for (int i = tid; i < k; i += NT) b[i] = fma(-colk[i], bk, b[i]);
-            __syncthreads();
-        }
+        __syncthreads();
     }
 };
 
@@ -770,7 +780,7 @@ __device__ int bdf_integrate(BdfPoint<NT>& P, double tf, double t_start, int* st
 
 template <int NT>
 __global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int* counter, const int* order,
-                                                  double* kcache, double* jm) {
+                                                  double* kcache, double* jm, int jm_smem) {
     extern __shared__ double smem[];
     __shared__ int next_point;
     const int n = m.S + 2;
@@ -785,7 +795,11 @@ __global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int
     P.a = &a;
     P.n = n;
     P.S = m.S;
-    P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
+    if (jm_smem) {
+        P.J = P.w.fo_dF + m.n_fo + BdfSmem::doubles(n);
+    } else {
+        P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
+    }
     P.M = P.J + size_t(n) * n;
     P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
     const int tid = threadIdx.x;
@@ -823,12 +837,22 @@ __global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int
     }
 }
 
+// Whether the Jacobian and the LU factors (2 n^2 doubles) go to shared memory
+// next to the kinetics and BDF vectors (else a per-CTA slice of global memory).
+inline bool bdf_jm_in_smem(const MechView& m) {
+    const int n = m.S + 2;
+    const size_t base = (ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(3) * m.n_fo +
+                         BdfSmem::doubles(n)) * sizeof(double);
+    return base + size_t(2) * n * n * sizeof(double) <= 225 * 1024;  // room for the static shared arrays
+}
+
 // Dynamic shared memory and persistent grid size of the BDF kernel.
 template <int NT>
 static int bdf_config(const MechView& m, const SourceArgs& a, size_t* per_out, int* blocks_out) {
     const int n = m.S + 2;
-    const size_t per = (ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(3) * m.n_fo +
-                        BdfSmem::doubles(n)) * sizeof(double);
+    size_t per = (ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(3) * m.n_fo +
+                  BdfSmem::doubles(n)) * sizeof(double);
+    if (bdf_jm_in_smem(m)) per += size_t(2) * n * n * sizeof(double);
     EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the BDF shared-memory work area (%zu B)", per);
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_bdf<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
     int dev = 0, sms = 0, per_sm = 0;
@@ -873,7 +897,7 @@ static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, S
     EMBER_TRY(sc.alloc(&jm, size_t(blocks) * 2 * size_t(n) * n));
     int* order = nullptr;
     EMBER_TRY(make_work_order(a, sc, st, &order));
-    k_source_bdf<NT><<<blocks, NT, per, st>>>(m, a, counter, order, kcache, jm);
+    k_source_bdf<NT><<<blocks, NT, per, st>>>(m, a, counter, order, kcache, jm, bdf_jm_in_smem(m) ? 1 : 0);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }
@@ -895,7 +919,7 @@ static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, S
 // ln(multiplier_i) of every reaction is accumulated per point.
 template <int NT>
 __global__ void __launch_bounds__(NT) k_source_bdf_adjoint(MechView m, SourceArgs a, int* counter, double* kcache,
-                                                          double* jm, const double* __restrict__ ybar_out,
+                                                          double* jm, int jm_smem, const double* __restrict__ ybar_out,
                                                           double* __restrict__ ybar_in, double* __restrict__ pbar,
                                                           int* __restrict__ adj_status) {
     extern __shared__ double smem[];
@@ -912,7 +936,11 @@ __global__ void __launch_bounds__(NT) k_source_bdf_adjoint(MechView m, SourceArg
     P.a = &a;
     P.n = n;
     P.S = m.S;
-    P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
+    if (jm_smem) {
+        P.J = P.w.fo_dF + m.n_fo + BdfSmem::doubles(n);
+    } else {
+        P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
+    }
     P.M = P.J + size_t(n) * n;
     P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
     P.tape = nullptr;
@@ -1060,8 +1088,8 @@ static int launch_bdf_adjoint_nt(const MechView& m, const SourceArgs& a, int* co
     double *kcache = nullptr, *jm = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
     EMBER_TRY(sc.alloc(&jm, size_t(blocks) * 2 * size_t(n) * n));
-    k_source_bdf_adjoint<NT><<<blocks, NT, per, st>>>(m, a, counter, kcache, jm, ybar_out, ybar_in, pbar,
-                                                      adj_status);
+    k_source_bdf_adjoint<NT><<<blocks, NT, per, st>>>(m, a, counter, kcache, jm, bdf_jm_in_smem(m) ? 1 : 0,
+                                                      ybar_out, ybar_in, pbar, adj_status);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }
@@ -1079,7 +1107,7 @@ template <int NT>
 __global__ void __launch_bounds__(NT) k_objective_vjp(MechView m, SourceArgs a, int n_pts,
                                                      const double* __restrict__ state, const double* __restrict__ gq,
                                                      const double* __restrict__ gcp, const double* __restrict__ gT,
-                                                     int* counter, double* kcache, double* jm,
+                                                     int* counter, double* kcache, double* jm, int jm_smem,
                                                      double* __restrict__ ybar, double* __restrict__ pbar) {
     extern __shared__ double smem[];
     __shared__ int next_point;
@@ -1095,7 +1123,11 @@ __global__ void __launch_bounds__(NT) k_objective_vjp(MechView m, SourceArgs a, 
     P.a = &a;
     P.n = n;
     P.S = m.S;
-    P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
+    if (jm_smem) {
+        P.J = P.w.fo_dF + m.n_fo + BdfSmem::doubles(n);
+    } else {
+        P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
+    }
     P.M = P.J + size_t(n) * n;
     P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
     P.tape = nullptr;
@@ -1199,7 +1231,8 @@ static int launch_objective_vjp_nt(const MechView& m, const SourceArgs& a, int n
     EMBER_TRY(sc.alloc(&jm, size_t(blocks) * 2 * size_t(n) * n));
     EMBER_TRY(sc.alloc(&counter, 1));
     EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
-    k_objective_vjp<NT><<<blocks, NT, per, st>>>(m, b, n_pts, state, gq, gcp, gT, counter, kcache, jm, ybar, pbar);
+    k_objective_vjp<NT><<<blocks, NT, per, st>>>(m, b, n_pts, state, gq, gcp, gT, counter, kcache, jm,
+                                                 bdf_jm_in_smem(m) ? 1 : 0, ybar, pbar);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }
