@@ -125,7 +125,8 @@ struct BdfPoint {
         for (size_t e = tid; e < size_t(n) * n; e += NT) J[e] = 0.0;
         __syncthreads();
         // rows of d wdot / dc: one thread per species row, reactions in order
-        for (int k = tid; k < S; k += NT) {
+        for (int kk = tid; kk < S; kk += NT) {
+            const int k = m.sp_order[kk];
             double* colk = J + (size_t(2) * n + 2 + k);  // element (2+k, 2+j) at colk[j*n]
             double dense = 0.0;
             const int e1 = m.sp_off[k + 1];

@@ -82,6 +82,7 @@ struct MechView {
     const int* tb_fo;     // [n_tb] falloff slot of each third-body slot, -1 for three-body reactions
     const int* sp_off;    // [S+1] reactions in which species k occurs, in reaction order
     const int* sp_ent;    // reaction | n_product_occurrences << 24 | n_reactant_occurrences << 28
+    const int* sp_order;  // [S] species by descending number of reactions (thread order of per-species loops)
     const double2* kf_tab;// [nT][R] (value, slope)
     const double2* kc_tab;// [nT][R]
 };
@@ -378,7 +379,8 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
         w.ropr[i] = ropr;
     }
     __syncthreads();
-    for (int k = t; k < S; k += NT) {
+    for (int kk = t; kk < S; kk += NT) {
+        const int k = m.sp_order[kk];
         double q = 0.0, d = 0.0, nt = 0.0;
         const int e1 = m.sp_off[k + 1];
         for (int e = m.sp_off[k]; e < e1; ++e) {

@@ -192,8 +192,14 @@ __global__ void k_order_scatter(const double* __restrict__ dt, int n, int* curso
         order[atomicAdd(&cursor[dt_bucket(dt[j])], 1)] = j;
 }
 
+// Resident CTAs per SM the register budget is sized for: with NT <= 160
+// threads, 4 CTAs fit in 96 registers per thread without spills (the 3 of an
+// unconstrained build leave the FP64 pipe idle on shared-memory latency).
+constexpr int qss_min_blocks(int nt) { return nt <= 160 ? 4 : 2; }
+
 template <int NT>
-__global__ void __launch_bounds__(NT) k_source_qss(MechView m, SourceArgs a, int* counter, const int* order, double* kcache) {
+__global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView m, SourceArgs a, int* counter,
+                                                                      const int* order, double* kcache) {
     extern __shared__ double smem[];
     __shared__ int next_point;
     const int n = m.S + 2;
@@ -372,6 +378,12 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
         sp_off[k + 1] = sp_off[k] + static_cast<int>(lists[k].size());
         sp_ent.insert(sp_ent.end(), lists[k].begin(), lists[k].end());
     }
+    // Species by descending number of reactions, the thread order of the
+    // per-species loops: the lanes of a warp then walk lists of similar length.
+    std::vector<int> sp_order(S);
+    for (int k = 0; k < S; ++k) sp_order[k] = k;
+    std::stable_sort(sp_order.begin(), sp_order.end(),
+                     [&](int a, int b) { return lists[a].size() > lists[b].size(); });
     const int n_tb = static_cast<int>(tb_rxn.size()), n_fo = static_cast<int>(fo_rxn.size());
     const int nT = 200;
 
@@ -413,6 +425,7 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
         {(void**)&v.tb_fo, tb_fo.data(), sizeof(int) * std::max(n_tb, 1)},
         {(void**)&v.sp_off, sp_off.data(), sizeof(int) * (S + 1)},
         {(void**)&v.sp_ent, sp_ent.data(), sizeof(int) * std::max<size_t>(sp_ent.size(), 1)},
+        {(void**)&v.sp_order, sp_order.data(), sizeof(int) * S},
         {(void**)&v.kf_tab, nullptr, sizeof(double2) * size_t(nT) * Rs},
         {(void**)&v.kc_tab, nullptr, sizeof(double2) * size_t(nT) * Rs},
     };
@@ -655,6 +668,8 @@ static int qss_config(const MechView& m, const SourceArgs& a, size_t* per_out, i
     const size_t per = qss_smem_doubles(m, a.qss_stability_check != 0) * sizeof(double);
     EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the QSS shared-memory work area (%zu B)", per);
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_qss<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_qss<NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                        int(cudaSharedmemCarveoutMaxShared)));
     int dev = 0, sms = 0, per_sm = 0;
     EMBER_CUDA_TRY(cudaGetDevice(&dev));
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));

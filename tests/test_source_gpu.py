@@ -205,3 +205,21 @@ def test_bdf_split_igniter_failures(pair_small, small_mech):
     np.testing.assert_array_equal(status, rs)
     assert (np.asarray(status) == -11).any()
     np.testing.assert_array_equal(out, ro)
+
+
+@pytest.mark.parametrize("method", ["qss", "bdf"])
+def test_empty_and_single_point_batches(pair_small, small_mech, method):
+    # Edge sizes: an empty batch is a no-op; one point alone gives the same
+    # bits as that point inside a batch (no cross-point state).
+    from ember_gb300.source import BDF
+    m = QSS if method == "qss" else BDF
+    g, o = pair_small
+    st, dt = _states(small_mech, 5, seed=44)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    out0, status0, stats0 = integrate_production_terms(g, m, st[:0], dt[:0], opts)
+    assert out0.shape == (0, st.shape[1]) and status0.size == 0
+    full, fst, fstats = integrate_production_terms(g, m, st, dt, opts)
+    for j in (0, 4):
+        one, ost, ostats = integrate_production_terms(g, m, st[j:j + 1], dt[j:j + 1], opts)
+        assert np.array_equal(one[0], full[j]) and ost[0] == fst[j]
+        assert np.array_equal(ostats[0], fstats[j])

@@ -298,3 +298,30 @@ def test_bad_step_reports_status(gpu_lib):
     h = np.array([1e-6, -1.0, 1e-6, 1e-6])
     out, status = integrate_diffusion_terms(grids, B, D, S, Y, 0.0, 1e-5, h=h)
     assert list(np.asarray(status)) == [0, -1, 0, 0]
+
+
+@pytest.mark.parametrize("algorithm", [L.DIFFUSION_PARALLEL, L.DIFFUSION_SERIAL])
+def test_diffusion_minimal_grids(gpu_lib, algorithm):
+    # Three-point grids (the smallest the stage accepts) with every boundary
+    # pair, and 31/32/33-point grids around one point per lane.
+    rng = np.random.default_rng(12)
+    grids = []
+    for left in range(5):
+        for right in (0, 1, 4):
+            grids.append(_flame(rng, 3, left, right, left % 2))
+    for n in (31, 32, 33):
+        grids.append(_flame(rng, n, 0, 0, 0))
+    n_vars = 2
+    B = [np.exp(rng.uniform(-1, 1, (n_vars, g.n_points))) for g in grids]
+    D = [np.exp(rng.uniform(np.log(1e-6), np.log(1e-4), (n_vars, g.n_points))) for g in grids]
+    S = [rng.normal(size=(n_vars, g.n_points)) for g in grids]
+    Y = [rng.normal(size=(n_vars, g.n_points)) for g in grids]
+    h = np.full(len(grids) * n_vars, 2e-6)
+    out, status = integrate_diffusion_terms(grids, B, D, S, Y, 0.0, 1e-5, h=h, algorithm=algorithm)
+    assert (np.asarray(status) == 0).all()
+    ref = _oracle_stage(grids, B, D, S, Y, 0.0, 1e-5, h=h)
+    for f in range(len(grids)):
+        if algorithm == L.DIFFUSION_SERIAL:
+            assert np.array_equal(out[f], ref[f])
+        else:
+            _assert_close_per_system(out[f], ref[f], f"grid {f}")
