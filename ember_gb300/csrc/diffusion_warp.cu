@@ -50,7 +50,6 @@
 #include <algorithm>
 #include <cstdlib>
 #include <numeric>
-#include <string>
 #include <vector>
 
 namespace ember {
@@ -407,387 +406,9 @@ __global__ void __launch_bounds__(128) k_diffusion_warp(WarpDiffView v) {
     }
 }
 
-// ---------------------------------------------------- one CTA per system --
-//
-// The same algorithm with the whole system on chip: a CTA of kBlockThreads
-// lanes per system (at most kBlockMaxM points per lane), the state and the
-// carry factors G and H of each lane's points in registers, the per-point
-// coefficients (alpha, c', e, kappa, y_prev) in shared memory, and the
-// chunk carries joined by a block-wide scan (warp shuffles, then the warp
-// totals in shared memory). Nothing but the inputs and the result touches
-// HBM. Used when every system has at most kBlockThreads * kBlockMaxM points.
-constexpr int kBlockThreads = 512;
-constexpr int kBlockWarps = kBlockThreads / 32;
-constexpr int kBlockMaxM = 8;
-constexpr int kBlockMaxN = kBlockThreads * kBlockMaxM;
-// shared memory: 5 coefficient slots of kBlockMaxN doubles, then the scans' scratch
-constexpr int kBlockSlots = 5;
-enum : int { B_ALPHA = 0, B_CP = 1, B_E = 2, B_KAPPA = 3, B_YP = 4 };
-constexpr size_t kBlockSmemBytes = (size_t(kBlockSlots) * kBlockMaxN + 10 * kBlockWarps + 8) * sizeof(double);
-
-struct BlockScratch {
-    double* m4;   // [kBlockWarps][4] warp-total matrices, then [kBlockWarps][2] entry vectors
-    double* fs;   // [kBlockWarps] forward warp-total slopes
-    double* bs;   // [kBlockWarps] backward warp-total slopes
-    double* fo;   // [kBlockWarps] forward warp-total offsets
-    double* bo;   // [kBlockWarps] backward warp-total offsets
-};
-
-// Block-wide minimum of (have, value) pairs.
-__device__ __forceinline__ double block_min_have(double mn, bool have, double* red, bool& any) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double t = __shfl_xor_sync(kFull, mn, o);
-        const bool th = __shfl_xor_sync(kFull, have, o);
-        if (th && (!have || t < mn)) mn = t;
-        have = have || th;
-    }
-    __syncthreads();
-    if (lane == 0) {
-        red[2 * warp] = mn;
-        red[2 * warp + 1] = have ? 1.0 : 0.0;
-    }
-    __syncthreads();
-    double r = 0.0;
-    bool h = false;
-    for (int w = 0; w < kBlockWarps; ++w) {
-        const bool hw = red[2 * w + 1] != 0.0;
-        if (hw && (!h || red[2 * w] < r)) r = red[2 * w];
-        h = h || hw;
-    }
-    __syncthreads();
-    any = h;
-    return r;
-}
-
-struct BlockChunk {
-    int N, i0, cnt;
-    double* sm;  // coefficient slots
-    __device__ double& at(int slot, int j) const { return sm[size_t(slot) * kBlockMaxN + j * kBlockThreads + threadIdx.x]; }
-};
-
-// Factorisation for one CTA; leaves alpha, c', e, kappa in shared memory,
-// G and H in registers, and the scan coefficients of the affine maps.
-__device__ void block_factorize(const RowCtx& r, const BlockChunk& ch, const BlockScratch& bs, double shift,
-                                double srhs, double (&G)[kBlockMaxM], double (&H)[kBlockMaxM], double (&pf)[5],
-                                double (&pb)[5], double& fex, double& bex) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // Pass R: rows and the chunk's matrix in u = 1 + lu_c coordinates
-    double m11 = 1.0, m12 = 0.0, m21 = 0.0, m22 = 1.0;
-    {
-        double c2m = 0.0;
-        for (int j = 0; j < ch.cnt; ++j) {
-            const int i = ch.i0 + j;
-            double a, c, xs, k;
-            if (i >= 2 && i <= r.N - 3) {
-                if (j == 0 || i == 2) {
-                    const double2 gp = r.geo[i - 1];
-                    c2m = (r.D[i - 1] + r.D[i]) * gp.y;
-                }
-                const double2 g = r.geo[i];
-                const double c1 = r.B[i] * g.x;
-                const double c2 = (r.D[i] + r.D[i + 1]) * g.y;
-                a = c1 * c2m;
-                c = c1 * c2;
-                xs = 0.0;
-                k = r.S ? r.S[i] : 0.0;
-                c2m = c2;
-            } else {
-                boundary_row(r, i, a, c, xs, k);
-            }
-            const double sg = shift + xs;
-            ch.at(B_ALPHA, j) = a;
-            ch.at(B_CP, j) = c;
-            ch.at(B_E, j) = sg;
-            ch.at(B_KAPPA, j) = k;
-            const double p1 = a * m11, p2 = a * m12, cs = c + sg;
-            const double n11 = fma(sg, m21, p1), n12 = fma(sg, m22, p2);
-            const double n21 = fma(cs, m21, p1), n22 = fma(cs, m22, p2);
-            m11 = n11;
-            m12 = n12;
-            m21 = n21;
-            m22 = n22;
-            if ((j & 3) == 3) normalize(m11, m12, m21, m22);
-        }
-        normalize(m11, m12, m21, m22);
-    }
-    // intra-warp inclusive scan of the matrices (later lanes on the left)
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const double u11 = shfl_up(m11, o), u12 = shfl_up(m12, o), u21 = shfl_up(m21, o), u22 = shfl_up(m22, o);
-        if (lane >= o) {
-            const double r11 = fma(m11, u11, m12 * u21), r12 = fma(m11, u12, m12 * u22);
-            const double r21 = fma(m21, u11, m22 * u21), r22 = fma(m21, u12, m22 * u22);
-            m11 = r11;
-            m12 = r12;
-            m21 = r21;
-            m22 = r22;
-            normalize(m11, m12, m21, m22);
-        }
-    }
-    if (lane == 31) {
-        bs.m4[4 * warp + 0] = m11;
-        bs.m4[4 * warp + 1] = m12;
-        bs.m4[4 * warp + 2] = m21;
-        bs.m4[4 * warp + 3] = m22;
-    }
-    __syncthreads();
-    // vectors entering each warp: the warps before it applied to [1; 1], by one thread
-    if (threadIdx.x == 0) {
-        double p = 1.0, q = 1.0;
-        for (int w = 0; w < kBlockWarps; ++w) {
-            const double t11 = bs.m4[4 * w], t12 = bs.m4[4 * w + 1], t21 = bs.m4[4 * w + 2], t22 = bs.m4[4 * w + 3];
-            bs.m4[4 * kBlockWarps + 2 * w] = p;
-            bs.m4[4 * kBlockWarps + 2 * w + 1] = q;
-            const double np_ = fma(t11, p, t12 * q), nq = fma(t21, p, t22 * q);
-            // keep the vector's scale in range
-            const int e = max(exponent_field(np_), exponent_field(nq));
-            const double sc = __hiloint2double(min(max(2046 - e, 1), 2046) << 20, 0);
-            p = np_ * sc;
-            q = nq * sc;
-        }
-    }
-    __syncthreads();
-    double u;
-    {
-        const double vp = bs.m4[4 * kBlockWarps + 2 * warp], vq = bs.m4[4 * kBlockWarps + 2 * warp + 1];
-        double e11 = shfl_up(m11, 1), e12 = shfl_up(m12, 1), e21 = shfl_up(m21, 1), e22 = shfl_up(m22, 1);
-        if (lane == 0) {
-            e11 = 1.0;
-            e12 = 0.0;
-            e21 = 0.0;
-            e22 = 1.0;
-        }
-        u = fma(e11, vp, e12 * vq) / fma(e21, vp, e22 * vq);
-    }
-    // Pass F: the recurrence with the per-point coefficients; G in registers
-    double Gp = 1.0;
-#pragma unroll
-    for (int j = 0; j < kBlockMaxM; ++j) {
-        if (j < ch.cnt) {
-            const int i = ch.i0 + j;
-            const double a = ch.at(B_ALPHA, j), c = ch.at(B_CP, j);
-            const double sg = ch.at(B_E, j), k = ch.at(B_KAPPA, j);
-            const double t = fma(a, u, sg);
-            const double rd = 1.0 / (t + c);
-            const double ar = a * rd;
-            Gp *= ar;
-            u = t * rd;
-            ch.at(B_ALPHA, j) = -ar;
-            ch.at(B_CP, j) = i == r.N - 1 ? 0.0 : -c * rd;
-            ch.at(B_E, j) = -srhs * rd;
-            ch.at(B_KAPPA, j) = k * rd;
-            G[j] = Gp;
-        } else {
-            G[j] = 1.0;
-        }
-    }
-    // Pass H: running products of -c' from the chunk's end
-    double Hp = 1.0;
-#pragma unroll
-    for (int j = kBlockMaxM - 1; j >= 0; --j) {
-        if (j < ch.cnt) {
-            Hp *= -ch.at(B_CP, j);
-            H[j] = Hp;
-        } else {
-            H[j] = 1.0;
-        }
-    }
-    // scan coefficients of the affine maps: intra-warp Kogge-Stone slopes,
-    // the exclusive intra-warp slope of each lane, and the warp totals
-    double P = Gp, Q = Hp;
-#pragma unroll
-    for (int lev = 0, o = 1; lev < 5; ++lev, o <<= 1) {
-        pf[lev] = P;
-        pb[lev] = Q;
-        const double tp = shfl_up(P, o), tq = shfl_down(Q, o);
-        if (lane >= o) P *= tp;
-        if (lane + o < 32) Q *= tq;
-    }
-    fex = shfl_up(P, 1);
-    if (lane == 0) fex = 1.0;
-    bex = shfl_down(Q, 1);
-    if (lane == 31) bex = 1.0;
-    if (lane == 31) bs.fs[warp] = P;
-    if (lane == 0) bs.bs[warp] = Q;
-    __syncthreads();
-}
-
-template <bool kBdf2>
-__device__ __forceinline__ void block_substep(const BlockChunk& ch, const BlockScratch& bs, double (&W)[kBlockMaxM],
-                                              const double (&G)[kBlockMaxM], const double (&H)[kBlockMaxM],
-                                              const double (&pf)[5], const double (&pb)[5], double fex, double bex,
-                                              double& cb) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double d = 0.0;
-#pragma unroll
-    for (int j = 0; j < kBlockMaxM; ++j) {
-        if (j < ch.cnt) {
-            double yv = fma(H[j], cb, W[j]);
-            if (kBdf2) {
-                const double yp = ch.at(B_YP, j);
-                ch.at(B_YP, j) = yv;
-                yv = fma(-0.25, yp, yv);
-            }
-            const double rho = fma(ch.at(B_E, j), yv, ch.at(B_KAPPA, j));
-            d = fma(-ch.at(B_ALPHA, j), d, rho);
-            W[j] = d;
-        }
-    }
-    // forward carries: intra-warp scan of the offsets, then across the warps
-#pragma unroll
-    for (int lev = 0, o = 1; lev < 5; ++lev, o <<= 1) {
-        const double t = shfl_up(d, o);
-        if (lane >= o) d = fma(pf[lev], t, d);
-    }
-    if (lane == 31) bs.fo[warp] = d;
-    double dex = shfl_up(d, 1);
-    if (lane == 0) dex = 0.0;
-    __syncthreads();
-    double cw = 0.0;
-    for (int w = 0; w < warp; ++w) cw = fma(bs.fs[w], cw, bs.fo[w]);
-    const double cf = fma(fex, cw, dex);
-    double yv = 0.0;
-#pragma unroll
-    for (int j = kBlockMaxM - 1; j >= 0; --j) {
-        if (j < ch.cnt) {
-            const double dd = fma(G[j], cf, W[j]);
-            yv = fma(-ch.at(B_CP, j), yv, dd);
-            W[j] = yv;
-        }
-    }
-#pragma unroll
-    for (int lev = 0, o = 1; lev < 5; ++lev, o <<= 1) {
-        const double t = shfl_down(yv, o);
-        if (lane + o < 32) yv = fma(pb[lev], t, yv);
-    }
-    if (lane == 0) bs.bo[warp] = yv;
-    double yex = shfl_down(yv, 1);
-    if (lane == 31) yex = 0.0;
-    __syncthreads();
-    double cwb = 0.0;
-    for (int w = kBlockWarps - 1; w > warp; --w) cwb = fma(bs.bs[w], cwb, bs.bo[w]);
-    cb = fma(bex, cwb, yex);
-}
-
-__global__ void __launch_bounds__(kBlockThreads, 1) k_diffusion_block(WarpDiffView v) {
-    extern __shared__ double bsm[];
-    __shared__ unsigned int next_sys;
-    BlockScratch bs;
-    double* tail = bsm + size_t(kBlockSlots) * kBlockMaxN;
-    bs.m4 = tail;
-    bs.fs = tail + 6 * kBlockWarps;
-    bs.bs = bs.fs + kBlockWarps;
-    bs.fo = bs.bs + kBlockWarps;
-    bs.bo = bs.fo + kBlockWarps;  // fo and bo also serve as the 2 * kBlockWarps scratch of block_min_have
-    const int tid = threadIdx.x;
-    for (;;) {
-        if (tid == 0) next_sys = atomicAdd(v.counter, 1u);
-        __syncthreads();
-        const unsigned int next = next_sys;
-        __syncthreads();
-        if (next >= static_cast<unsigned int>(v.n_systems)) return;
-        const int s = v.order[next];
-        const DiffSysInfo info = v.info[s];
-        const int N = info.n;
-        const int m = (N + kBlockThreads - 1) / kBlockThreads;
-        BlockChunk ch;
-        ch.N = N;
-        ch.i0 = min(tid * m, N);
-        ch.cnt = min(N - ch.i0, m);
-        ch.sm = bsm;
-
-        RowCtx r;
-        r.N = N;
-        r.alpha = info.alpha;
-        r.left_bc = info.left_bc;
-        r.right_bc = info.right_bc;
-        r.x = v.x + info.grid_off;
-        r.geo = v.geo + info.grid_off;
-        r.B = v.B + info.off;
-        r.D = v.D + info.off;
-        r.S = v.split_const ? v.split_const + info.off : nullptr;
-        r.wall_const = v.wall_const ? v.wall_const[s] : 0.0;
-        r.y_inf = v.y_inf ? v.y_inf[s] : 0.0;
-
-        double h;
-        if (v.h) {
-            h = v.h[s];
-        } else {
-            double mn = 0.0;
-            bool have = false;
-            for (int j = 0; j < ch.cnt; ++j) {
-                const int i = ch.i0 + j;
-                if (i < 1 || i > N - 2) continue;
-                const double dlj = __dmul_rn(0.5, __dsub_rn(r.x[i + 1], r.x[i - 1]));
-                const double q = __ddiv_rn(__dmul_rn(dlj, dlj), __dmul_rn(r.B[i], r.D[i]));
-                if (!have || q < mn) mn = q;
-                have = true;
-            }
-            bool any;
-            mn = block_min_have(mn, have, bs.fo, any);
-            const double hm = __dmul_rn(v.mult, mn);
-            h = v.gdt < hm ? v.gdt : hm;
-        }
-        double t0, t1;
-        v.tm.get(t0, t1);
-        const double q = __dadd_rn(__ddiv_rn(__dsub_rn(t1, t0), h), 1e-5);
-        if (!(h > 0.0) || !(q < 2147483647.0)) {
-            if (tid == 0 && v.status) v.status[s] = TRI_BAD_STEP;
-            continue;
-        }
-        const int n_steps = q >= 1.0 ? static_cast<int>(q) : 1;
-        h = __ddiv_rn(__dsub_rn(t1, t0), static_cast<double>(n_steps));
-
-        double* y = v.y + info.off;
-        double W[kBlockMaxM], G[kBlockMaxM], H[kBlockMaxM];
-#pragma unroll
-        for (int j = 0; j < kBlockMaxM; ++j) {
-            W[j] = 0.0;
-            if (j < ch.cnt) {
-                W[j] = y[ch.i0 + j];
-                if (n_steps > 1) ch.at(B_YP, j) = W[j];
-            }
-        }
-        double pf[5], pb[5], fex, bex;
-        double cb = 0.0;
-        block_factorize(r, ch, bs, 8.0 / h, -8.0 / h, G, H, pf, pb, fex, bex);
-        for (int sub = 0; sub < 8; ++sub) block_substep<false>(ch, bs, W, G, H, pf, pb, fex, bex, cb);
-        if (n_steps > 1) {
-#pragma unroll
-            for (int j = 0; j < kBlockMaxM; ++j) W[j] = fma(H[j], cb, W[j]);
-            cb = 0.0;
-            block_factorize(r, ch, bs, 1.5 / h, -2.0 / h, G, H, pf, pb, fex, bex);
-            for (int step = 1; step < n_steps; ++step) block_substep<true>(ch, bs, W, G, H, pf, pb, fex, bex, cb);
-        }
-        bool finite = true;
-#pragma unroll
-        for (int j = 0; j < kBlockMaxM; ++j) {
-            if (j < ch.cnt) {
-                const double yv = fma(H[j], cb, W[j]);
-                y[ch.i0 + j] = yv;
-                finite = finite && isfinite(yv);
-            }
-        }
-        const int all_finite = __syncthreads_and(finite ? 1 : 0);
-        if (tid == 0 && v.status) v.status[s] = all_finite ? TRI_OK : TRI_NONFINITE;
-    }
-}
-
 // Resident warps per SM of the persistent grid (EMBER_DIFFUSION_WARPS_PER_SM
 // overrides). Fewer warps keep more of the workspace in L2, more warps hide
 // more latency; on the 64-flame, 55-variable batch (N 100-4000) 12 was best.
-// Kernel choice: the CTA-per-system kernel when every system fits on chip,
-// unless EMBER_DIFFUSION_KERNEL=warp asks for the warp-per-system one.
-bool force_warp_kernel() {
-    static bool f = [] {
-        const char* e = std::getenv("EMBER_DIFFUSION_KERNEL");
-        return e && std::string(e) == "warp";
-    }();
-    return f;
-}
-
 int warps_per_sm() {
     static int w = [] {
         const char* e = std::getenv("EMBER_DIFFUSION_WARPS_PER_SM");
@@ -841,7 +462,6 @@ int diffusion_warp_plan_init(DiffusionWarpPlan* p, const std::vector<DiffSysInfo
     EMBER_CUDA_TRY(cudaGetDevice(&dev));
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     p->warps = std::min<int64_t>(n_sys, int64_t(sms) * warps_per_sm());
-    p->sms = sms;
     return EMBER_OK;
 }
 
@@ -875,14 +495,7 @@ int diffusion_warp_run(const DiffusionWarpPlan& p, const DiffusionView& dv, doub
     v.tm = tm;
     v.mult = mult;
     v.gdt = gdt;
-    if (p.nmax <= kBlockMaxN && !force_warp_kernel()) {
-        EMBER_CUDA_TRY(cudaFuncSetAttribute(k_diffusion_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            int(kBlockSmemBytes)));
-        const int blocks = std::max(1, std::min(p.n_sys, p.sms));
-        k_diffusion_block<<<blocks, kBlockThreads, kBlockSmemBytes, st>>>(v);
-    } else {
-        k_diffusion_warp<<<blocks_for(p.warps * 32, 128), 128, 0, st>>>(v);
-    }
+    k_diffusion_warp<<<blocks_for(p.warps * 32, 128), 128, 0, st>>>(v);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }

@@ -372,7 +372,6 @@ struct DiffusionWarpPlan {
     int n_sys = 0, n_flames = 0, n_vars = 0, nmax = 0;
     int64_t n_pts = 0;
     int64_t warps = 0;
-    int sms = 1;
     double* ws = nullptr;
     double2* geo = nullptr;
     int64_t* ws_off = nullptr;
