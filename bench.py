@@ -292,9 +292,10 @@ def run_ours(args):
     achieved = flops / avg_launch_s / 1e12
     peak_t = fp64_peak / 1e12
 
-    # DRAM bytes per launch from the ncu capture of the integration kernel
-    # (608 points), scaled to this launch's points; none captured for BDF yet.
-    traffic = roofline.QSS_DRAM_BYTES_PER_POINT * args.points if method == QSS else None
+    # DRAM bytes per launch from the ncu captures of the integration kernels
+    # (150-species mechanism), scaled to this launch's points.
+    per_point = roofline.QSS_DRAM_BYTES_PER_POINT if method == QSS else roofline.BDF_DRAM_BYTES_PER_POINT
+    traffic = per_point * args.points
 
     line = {
         "metric": METRIC, "value": ws * args.points * args.steps / (total_ms / 1e3), "unit": "points/s",
