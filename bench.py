@@ -52,6 +52,8 @@ def parse_args():
     p.add_argument("--kinetics", default="interp", choices=["interp", "standard"])
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--threads", type=int, default=0,
+                   help="QSS threads per point; 0: ember_source_autotune picks it before the timed region")
     return p.parse_args()
 
 
@@ -198,7 +200,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
     from ember_gb300 import _lib
     from ember_gb300 import roofline
-    from ember_gb300.source import GpuMechanism, integrate_production_terms, QSS, BDF, STATS_WIDTH
+    from ember_gb300.source import GpuMechanism, integrate_production_terms, autotune, QSS, BDF, STATS_WIDTH
     import ctypes as C
 
     lib = _lib.lib()
@@ -218,6 +220,14 @@ def run_ours(args):
     peak = C.c_double()
     _lib.check(lib.ember_probe_fp64_rate(0, C.byref(peak)), "probe")
     fp64_peak = peak.value
+
+    # launch width: autotuned on this batch (outside the timed region), or given
+    tune_ms = {}
+    if method == QSS and args.threads == 0:
+        width, tune_ms = autotune(gm, QSS, st_d, dt_d, opts, stream=stream)
+    else:
+        width = args.threads
+        opts.threads_per_point = width
 
     def step():
         integrate_production_terms(gm, method, st_d, dt_d, opts, out=out_d, status=status_d, stats=stats_d,
@@ -308,7 +318,9 @@ def run_ours(args):
                    "l2": "256 MB buffer written between timed iterations", "parallelism": f"replicas x{ws}",
                    "failed_points": n_fail,
                    "mean_steps_per_point": float(stats[:, 0].mean()),
-                   "mean_rhs_calls_per_point": float(stats[:, 1].mean())},
+                   "mean_rhs_calls_per_point": float(stats[:, 1].mean()),
+                   "threads_per_point": width or "default for the mechanism size",
+                   "autotune_ms": {str(k): round(v, 2) for k, v in tune_ms.items()}},
         "e2e": {"value": ws * args.points * args.steps / e2e_s, "unit": "points/s",
                 "h2d_bytes_per_step": int(state.nbytes + dt.nbytes),
                 "d2h_bytes_per_step": int(state.nbytes + status_h.numpy().nbytes + stats_h.numpy().nbytes)},
@@ -530,11 +542,13 @@ def run_ours_split(args):
     if ws > 1:
         torch.distributed.init_process_group("nccl")
     from ember_gb300 import _lib, roofline
-    from ember_gb300.source import GpuMechanism, QSS
+    from ember_gb300.source import GpuMechanism, QSS, autotune
     from ember_gb300.split import FlameBatchSplitSolver
     mech, grids, state, B, D, rho_u, ju, jb = split_inputs(rank)
     opts = source_options(args.kinetics, "qss")
     gm = GpuMechanism(mech)
+    # QSS launch width tuned on the flames' start states over one step (before the solver takes it)
+    width, tune_ms = autotune(gm, QSS, state, np.full(len(state), SPLIT_DT), opts)
     solver = FlameBatchSplitSolver(gm, grids, SPLIT_DT, method=QSS, source_options=opts)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
@@ -589,7 +603,8 @@ def run_ours_split(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded flame-like profiles, synthetic transport)",
         "config": {"workload": SPLIT_WORKLOAD, "points": int(len(state)), "flames": len(grids),
                    "points_per_s": len(state) / (ms / 1e3), "l2": "256 MB buffer written between timed steps",
-                   "graph": True, "failed_source_points": n_fail_src, "failed_diffusion_systems": n_fail_diff},
+                   "graph": True, "failed_source_points": n_fail_src, "failed_diffusion_systems": n_fail_diff,
+                   "threads_per_point": width, "autotune_ms": {str(k): round(v, 2) for k, v in tune_ms.items()}},
         "e2e": {"value": 1e3 * sum(e2e) / len(e2e), "unit": "ms", "h2d_bytes_per_step": int(state.nbytes),
                 "d2h_bytes_per_step": int(state.nbytes)},
         # per step: begin, 2 x (transpose, 2 x (stage, failure count, delta), transpose back), stage dt,

@@ -79,6 +79,11 @@ def _declare(lib):
                                              C.c_int, vp]),
         "ember_source_adjoint": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp, C.c_int, vp, vp, vp, vp,
                                            C.c_int, vp]),
+        "ember_source_autotune": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp, vp, C.c_int,
+                                            vp]),
+        "ember_transport_create": (C.c_int, [vp, vp, vp]),
+        "ember_transport_destroy": (C.c_int, [vp]),
+        "ember_transport_eval": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, vp, vp, vp, C.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

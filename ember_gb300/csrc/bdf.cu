@@ -34,11 +34,19 @@ struct BdfSmem {
     double* zs[kQmax + 1];  // saved array for step retries
     double *acor, *acorp, *ewt, *y, *ft, *bb, *f0, *ycopy, *f1;
     int* piv;
-    static __host__ __device__ size_t doubles(int n) { return size_t(2 * kQmax + 3 + 9) * n + (n + 1) / 2; }
-    __device__ void carve(double* base, int n) {
+    // shared-memory doubles (zs_smem: the saved array in shared memory)
+    static __host__ __device__ size_t doubles(int n, bool zs_smem = true) {
+        return size_t(zs_smem ? 2 * kQmax + 3 + 9 : kQmax + 2 + 9) * n + (n + 1) / 2;
+    }
+    // zs_global: (kQmax + 1) n doubles of global memory for zs, or null
+    __device__ void carve(double* base, int n, double* zs_global = nullptr) {
         double* p = base;
         for (int j = 0; j <= kQmax + 1; ++j, p += n) z[j] = p;
-        for (int j = 0; j <= kQmax; ++j, p += n) zs[j] = p;
+        if (zs_global) {
+            for (int j = 0; j <= kQmax; ++j) zs[j] = zs_global + size_t(j) * n;
+        } else {
+            for (int j = 0; j <= kQmax; ++j, p += n) zs[j] = p;
+        }
         acor = p; p += n;
         acorp = p; p += n;
         ewt = p; p += n;
@@ -80,9 +88,8 @@ struct BdfPoint {
         }
         double rho_c, cp_c;
         chem_rates<NT>(m, w, a->pressure, STATE_NO_NORM, T, y + 2, rho_c, cp_c, true);
-        double part = 0.0;
-        for (int k = tid; k < S; k += NT) part = fma(w.wn[k], w.hk[k], part);
-        double qd = -block_sum<NT>(w.red, part);
+        const double *wn = w.wn, *hk = w.hk;
+        double qd = -block_sum<NT>(w.red, S, [&](int k, double p) { return fma(wn[k], hk[k], p); });
         qd = qd + igniter(*a, t, x);
         const double rrho = 1.0 / rho_c;
         const double rrc = 1.0 / (rho_c * cp_c);
@@ -102,12 +109,12 @@ struct BdfPoint {
     }
 
     __device__ double wrms(const double* vec) {
-        double part = 0.0;
-        for (int i = threadIdx.x; i < n; i += NT) {
-            const double xv = vec[i] * v.ewt[i];
-            part = fma(xv, xv, part);
-        }
-        return sqrt(block_sum<NT>(w.red, part) / n);
+        const double* ewt = v.ewt;
+        return sqrt(block_sum<NT>(w.red, n, [&](int i, double p) {
+                        const double xv = vec[i] * ewt[i];
+                        return fma(xv, xv, p);
+                    }) /
+                    n);
     }
 
     __device__ double jc(int r, int c) const { return J[size_t(c) * n + r]; }
@@ -118,9 +125,8 @@ struct BdfPoint {
         const int tid = threadIdx.x;
         const double T = yv[1];
         const double A = 1.0 / w.mmw;
-        double bpart = 0.0;
-        for (int k = tid; k < S; k += NT) bpart = fma(yv[2 + k] * m.rW[k], w.cpR[k], bpart);
-        const double B = block_sum<NT>(w.red, bpart);
+        const double *rW = m.rW, *cpR = w.cpR;
+        const double B = block_sum<NT>(w.red, S, [&](int k, double p) { return fma(yv[2 + k] * rW[k], cpR[k], p); });
         const double rhoj = rho, rc = rho * cp;
         for (size_t e = tid; e < size_t(n) * n; e += NT) J[e] = 0.0;
         __syncthreads();
@@ -439,6 +445,62 @@ struct BdfPoint {
         __syncthreads();
     }
 };
+
+// Where a point's Jacobian J and LU factors M (n^2 doubles each) live:
+//   BDF_JM_SMEM   both in shared memory, next to the kinetics and BDF vectors;
+//   BDF_M_SMEM    M in shared memory, J in a per-CTA slice of global memory
+//                 (M is read by every Newton solve, J once per matrix update);
+//                 to make room, the rates of progress and the saved Nordsieck
+//                 array move to that slice as well;
+//   BDF_JM_GLOBAL both in the global slice.
+enum : int { BDF_JM_GLOBAL = 0, BDF_JM_SMEM = 1, BDF_M_SMEM = 2 };
+
+struct BdfLayout {
+    int mode;
+    size_t smem_bytes;      // dynamic shared memory per CTA
+    size_t global_doubles;  // global slice per CTA
+};
+
+constexpr size_t kBdfSmemBudget = 225 * 1024;  // leaves room for the static shared arrays
+
+inline BdfLayout bdf_layout(const MechView& m) {
+    const size_t n = size_t(m.S) + 2, nn = n * n;
+    const size_t full = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(3) * m.n_fo + BdfSmem::doubles(int(n));
+    const size_t lean = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true, false) + size_t(3) * m.n_fo +
+                        BdfSmem::doubles(int(n), false);
+    if ((full + 2 * nn) * sizeof(double) <= kBdfSmemBudget) return {BDF_JM_SMEM, (full + 2 * nn) * sizeof(double), 0};
+    if ((lean + nn) * sizeof(double) <= kBdfSmemBudget)
+        return {BDF_M_SMEM, (lean + nn) * sizeof(double), nn + size_t(kQmax + 1) * n + size_t(2) * m.R};
+    return {BDF_JM_GLOBAL, full * sizeof(double), 2 * nn};
+}
+
+// Carves one CTA's work areas: smem (dynamic shared memory), kc (its slice of
+// the rate-constant cache), g (its global slice of bdf_layout().global_doubles).
+template <int NT>
+__device__ __forceinline__ void bdf_carve(BdfPoint<NT>& P, double* smem, double* kc, double* g, int mode) {
+    const MechView& m = P.m;
+    const int n = m.S + 2;
+    const size_t nn = size_t(n) * n;
+    const bool lean = mode == BDF_M_SMEM;
+    P.w.carve(smem, kc, m, true, lean ? g + nn + size_t(kQmax + 1) * n : nullptr);
+    P.w.fo_F = smem + ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true, !lean);
+    P.w.fo_pr = P.w.fo_F + m.n_fo;
+    P.w.fo_dF = P.w.fo_pr + m.n_fo;
+    P.v.carve(P.w.fo_dF + m.n_fo, n, lean ? g + nn : nullptr);
+    double* after = P.w.fo_dF + m.n_fo + BdfSmem::doubles(n, !lean);
+    if (mode == BDF_JM_SMEM) {
+        P.J = after;
+        P.M = after + nn;
+    } else if (lean) {
+        P.J = g;
+        P.M = after;
+    } else {
+        P.J = g;
+        P.M = g + nn;
+    }
+    P.n = n;
+    P.S = m.S;
+}
 
 __device__ __forceinline__ void bdf_l(int q, double* l) {
     for (int j = 0; j <= kQmax + 1; ++j) l[j] = 0.0;
@@ -781,27 +843,15 @@ __device__ int bdf_integrate(BdfPoint<NT>& P, double tf, double t_start, int* st
 
 template <int NT>
 __global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int* counter, const int* order,
-                                                  double* kcache, double* jm, int jm_smem) {
+                                                  double* kcache, double* jm, size_t jm_stride, int jm_mode) {
     extern __shared__ double smem[];
     __shared__ int next_point;
     const int n = m.S + 2;
-    const size_t cd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true);
     BdfPoint<NT> P;
     P.m = m;
-    P.w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), m, true);
-    P.w.fo_F = smem + cd;
-    P.w.fo_pr = P.w.fo_F + m.n_fo;
-    P.w.fo_dF = P.w.fo_pr + m.n_fo;
-    P.v.carve(P.w.fo_dF + m.n_fo, n);
+    bdf_carve(P, smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), jm + size_t(blockIdx.x) * jm_stride,
+              jm_mode);
     P.a = &a;
-    P.n = n;
-    P.S = m.S;
-    if (jm_smem) {
-        P.J = P.w.fo_dF + m.n_fo + BdfSmem::doubles(n);
-    } else {
-        P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
-    }
-    P.M = P.J + size_t(n) * n;
     P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
     const int tid = threadIdx.x;
     for (;;) {
@@ -838,22 +888,10 @@ __global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int
     }
 }
 
-// Whether the Jacobian and the LU factors (2 n^2 doubles) go to shared memory
-// next to the kinetics and BDF vectors (else a per-CTA slice of global memory).
-inline bool bdf_jm_in_smem(const MechView& m) {
-    const int n = m.S + 2;
-    const size_t base = (ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(3) * m.n_fo +
-                         BdfSmem::doubles(n)) * sizeof(double);
-    return base + size_t(2) * n * n * sizeof(double) <= 225 * 1024;  // room for the static shared arrays
-}
-
 // Dynamic shared memory and persistent grid size of the BDF kernel.
 template <int NT>
 static int bdf_config(const MechView& m, const SourceArgs& a, size_t* per_out, int* blocks_out) {
-    const int n = m.S + 2;
-    size_t per = (ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(3) * m.n_fo +
-                  BdfSmem::doubles(n)) * sizeof(double);
-    if (bdf_jm_in_smem(m)) per += size_t(2) * n * n * sizeof(double);
+    const size_t per = bdf_layout(m).smem_bytes;
     EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the BDF shared-memory work area (%zu B)", per);
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_bdf<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
     int dev = 0, sms = 0, per_sm = 0;
@@ -871,10 +909,9 @@ static int bdf_scratch_nt(const MechView& m, const SourceArgs& a, size_t* bytes)
     size_t per = 0;
     int blocks = 0;
     EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
-    const size_t n = size_t(m.S) + 2;
     *bytes = Scratch::rounded(sizeof(double) * size_t(blocks) * ChemSmem::global_doubles(m.R)) +
-             Scratch::rounded(sizeof(double) * size_t(blocks) * 2 * n * n) + Scratch::rounded(sizeof(int) * 64) +
-             Scratch::rounded(sizeof(int) * size_t(a.n));
+             Scratch::rounded(sizeof(double) * size_t(blocks) * bdf_layout(m).global_doubles) +
+             Scratch::rounded(sizeof(int) * 64) + Scratch::rounded(sizeof(int) * size_t(a.n));
     return EMBER_OK;
 }
 
@@ -889,16 +926,16 @@ int source_bdf_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* byt
 
 template <int NT>
 static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
-    const int n = m.S + 2;
     size_t per = 0;
     int blocks = 0;
     EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
     double *kcache = nullptr, *jm = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
-    EMBER_TRY(sc.alloc(&jm, size_t(blocks) * 2 * size_t(n) * n));
+    const BdfLayout lay = bdf_layout(m);
+    EMBER_TRY(sc.alloc(&jm, size_t(blocks) * lay.global_doubles));
     int* order = nullptr;
     EMBER_TRY(make_work_order(a, sc, st, &order));
-    k_source_bdf<NT><<<blocks, NT, per, st>>>(m, a, counter, order, kcache, jm, bdf_jm_in_smem(m) ? 1 : 0);
+    k_source_bdf<NT><<<blocks, NT, per, st>>>(m, a, counter, order, kcache, jm, lay.global_doubles, lay.mode);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }
@@ -920,29 +957,18 @@ static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, S
 // ln(multiplier_i) of every reaction is accumulated per point.
 template <int NT>
 __global__ void __launch_bounds__(NT) k_source_bdf_adjoint(MechView m, SourceArgs a, int* counter, double* kcache,
-                                                          double* jm, int jm_smem, const double* __restrict__ ybar_out,
+                                                          double* jm, size_t jm_stride, int jm_mode,
+                                                          const double* __restrict__ ybar_out,
                                                           double* __restrict__ ybar_in, double* __restrict__ pbar,
                                                           int* __restrict__ adj_status) {
     extern __shared__ double smem[];
     __shared__ int next_point;
     const int n = m.S + 2;
-    const size_t cd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true);
     BdfPoint<NT> P;
     P.m = m;
-    P.w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), m, true);
-    P.w.fo_F = smem + cd;
-    P.w.fo_pr = P.w.fo_F + m.n_fo;
-    P.w.fo_dF = P.w.fo_pr + m.n_fo;
-    P.v.carve(P.w.fo_dF + m.n_fo, n);
+    bdf_carve(P, smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), jm + size_t(blockIdx.x) * jm_stride,
+              jm_mode);
     P.a = &a;
-    P.n = n;
-    P.S = m.S;
-    if (jm_smem) {
-        P.J = P.w.fo_dF + m.n_fo + BdfSmem::doubles(n);
-    } else {
-        P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
-    }
-    P.M = P.J + size_t(n) * n;
     P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
     P.tape = nullptr;
     BdfSmem& v = P.v;
@@ -1080,7 +1106,6 @@ __global__ void __launch_bounds__(NT) k_source_bdf_adjoint(MechView m, SourceArg
 template <int NT>
 static int launch_bdf_adjoint_nt(const MechView& m, const SourceArgs& a, int* counter, const double* ybar_out,
                                  double* ybar_in, double* pbar, int* adj_status, Scratch& sc, cudaStream_t st) {
-    const int n = m.S + 2;
     size_t per = 0;
     int blocks = 0;
     EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
@@ -1088,8 +1113,9 @@ static int launch_bdf_adjoint_nt(const MechView& m, const SourceArgs& a, int* co
                                         int(per)));
     double *kcache = nullptr, *jm = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
-    EMBER_TRY(sc.alloc(&jm, size_t(blocks) * 2 * size_t(n) * n));
-    k_source_bdf_adjoint<NT><<<blocks, NT, per, st>>>(m, a, counter, kcache, jm, bdf_jm_in_smem(m) ? 1 : 0,
+    const BdfLayout lay = bdf_layout(m);
+    EMBER_TRY(sc.alloc(&jm, size_t(blocks) * lay.global_doubles));
+    k_source_bdf_adjoint<NT><<<blocks, NT, per, st>>>(m, a, counter, kcache, jm, lay.global_doubles, lay.mode,
                                                       ybar_out, ybar_in, pbar, adj_status);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
@@ -1108,28 +1134,16 @@ template <int NT>
 __global__ void __launch_bounds__(NT) k_objective_vjp(MechView m, SourceArgs a, int n_pts,
                                                      const double* __restrict__ state, const double* __restrict__ gq,
                                                      const double* __restrict__ gcp, const double* __restrict__ gT,
-                                                     int* counter, double* kcache, double* jm, int jm_smem,
+                                                     int* counter, double* kcache, double* jm, size_t jm_stride, int jm_mode,
                                                      double* __restrict__ ybar, double* __restrict__ pbar) {
     extern __shared__ double smem[];
     __shared__ int next_point;
     const int n = m.S + 2;
-    const size_t cd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true);
     BdfPoint<NT> P;
     P.m = m;
-    P.w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), m, true);
-    P.w.fo_F = smem + cd;
-    P.w.fo_pr = P.w.fo_F + m.n_fo;
-    P.w.fo_dF = P.w.fo_pr + m.n_fo;
-    P.v.carve(P.w.fo_dF + m.n_fo, n);
+    bdf_carve(P, smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), jm + size_t(blockIdx.x) * jm_stride,
+              jm_mode);
     P.a = &a;
-    P.n = n;
-    P.S = m.S;
-    if (jm_smem) {
-        P.J = P.w.fo_dF + m.n_fo + BdfSmem::doubles(n);
-    } else {
-        P.J = jm + size_t(blockIdx.x) * 2 * size_t(n) * n;
-    }
-    P.M = P.J + size_t(n) * n;
     P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
     P.tape = nullptr;
     P.split = nullptr;
@@ -1153,19 +1167,15 @@ __global__ void __launch_bounds__(NT) k_objective_vjp(MechView m, SourceArgs a, 
         const double T = v.y[1];
         const double rho = P.rho, cp = P.cp, rc = rho * cp;
         const double A = 1.0 / P.w.mmw;
-        double bpart = 0.0, dbpart = 0.0, ysum_part = 0.0;
-        for (int k = tid; k < S; k += NT) {
-            const double yk = v.y[2 + k] * m.rW[k];
+        const double *yv = v.y, *cpR = P.w.cpR;
+        const double B = block_sum<NT>(P.w.red, S, [&](int k, double q) { return fma(yv[2 + k] * m.rW[k], cpR[k], q); });
+        const double dB = block_sum<NT>(P.w.red, S, [&](int k, double q) {
             const int r = (T <= m.tmid[k]) ? 0 : 1;
             const double* c = m.nasa + 14 * k + 7 * r;
             const double dcp = fma(fma(fma(4.0 * c[4], T, 3.0 * c[3]), T, 2.0 * c[2]), T, c[1]);
-            bpart = fma(yk, P.w.cpR[k], bpart);
-            dbpart = fma(yk, dcp, dbpart);
-            ysum_part += v.y[2 + k];
-        }
-        const double B = block_sum<NT>(P.w.red, bpart);
-        const double dB = block_sum<NT>(P.w.red, dbpart);
-        const double ysum = block_sum<NT>(P.w.red, ysum_part);
+            return fma(yv[2 + k] * m.rW[k], dcp, q);
+        });
+        const double ysum = block_sum<NT>(P.w.red, S, [&](int k, double q) { return q + yv[2 + k]; });
         const double p = a.pressure, dTdt = v.ft[1];
         const double g_q = gq[j], g_cp = gcp ? gcp[j] : 0.0, g_T = gT ? gT[j] : 0.0;
         // d psi / d y_c (NoNorm) into v.bb
@@ -1187,9 +1197,8 @@ __global__ void __launch_bounds__(NT) k_objective_vjp(MechView m, SourceArgs a, 
         }
         __syncthreads();
         // project out the normalisation of Y
-        double proj = 0.0;
-        for (int k = tid; k < S; k += NT) proj = fma(v.y[2 + k], v.bb[2 + k], proj);
-        const double pr = block_sum<NT>(P.w.red, proj);
+        const double* bb = v.bb;
+        const double pr = block_sum<NT>(P.w.red, S, [&](int k, double q) { return fma(yv[2 + k], bb[2 + k], q); });
         for (int c = tid; c < n; c += NT) {
             double g = v.bb[c];
             if (c >= 2) g = (g - pr / ysum) / ysum;
@@ -1219,7 +1228,6 @@ template <int NT>
 static int launch_objective_vjp_nt(const MechView& m, const SourceArgs& a, int n_pts, const double* state,
                                    const double* gq, const double* gcp, const double* gT, double* ybar, double* pbar,
                                    Scratch& sc, cudaStream_t st) {
-    const int n = m.S + 2;
     size_t per = 0;
     int blocks = 0;
     SourceArgs b = a;
@@ -1229,11 +1237,12 @@ static int launch_objective_vjp_nt(const MechView& m, const SourceArgs& a, int n
     double *kcache = nullptr, *jm = nullptr;
     int* counter = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
-    EMBER_TRY(sc.alloc(&jm, size_t(blocks) * 2 * size_t(n) * n));
+    const BdfLayout lay = bdf_layout(m);
+    EMBER_TRY(sc.alloc(&jm, size_t(blocks) * lay.global_doubles));
     EMBER_TRY(sc.alloc(&counter, 1));
     EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
     k_objective_vjp<NT><<<blocks, NT, per, st>>>(m, b, n_pts, state, gq, gcp, gT, counter, kcache, jm,
-                                                 bdf_jm_in_smem(m) ? 1 : 0, ybar, pbar);
+                                                 lay.global_doubles, lay.mode, ybar, pbar);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }

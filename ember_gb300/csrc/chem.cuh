@@ -19,12 +19,13 @@
 // per-CTA slice of global memory (L2-resident), everything else in shared
 // memory.
 //
-// Every sum over species is a block reduction in one fixed order: element k
-// goes to the partial sum of thread k mod NT (sequential in k); the NT
-// partials are folded into 32 as p[l] + p[l+32] + p[l+64] + ... (in that
-// order) and combined by an xor butterfly. The translation unit is compiled
-// without automatic FMA contraction; the multiply-adds that are fused are
-// written as fma(), in the same places as in the CPU oracle.
+// Every sum over species is a reduction in one fixed order that does not
+// depend on NT: element k goes to the partial sum of lane k mod 32
+// (sequential in k) and the 32 partials are combined by an xor butterfly.
+// The results are therefore bit-identical for every CTA width. The
+// translation unit is compiled without automatic FMA contraction; the
+// multiply-adds that are fused are written as fma(), in the same places as
+// in the CPU oracle.
 #pragma once
 
 #include <cstdint>
@@ -39,6 +40,11 @@ constexpr double kBigNumber = 1e300;
 constexpr double kSmallNumber = 1e-300;
 constexpr int kMaxStoich = 4;
 constexpr int kMaxChemThreads = 256;
+// Reduction scratch: one slot per warp (block_max) and the broadcast slot of block_sum.
+constexpr int kRedSumSlot = kMaxChemThreads / 32;
+constexpr int kRedDoubles = kRedSumSlot + 2;
+// Launch widths (threads per grid point) of the QSS kernel.
+constexpr int kQssThreadChoices[] = {32, 64, 96, 128, 160, 192, 256};
 
 enum : int { RXN_ELEMENTARY = 0, RXN_THREE_BODY = 1, RXN_LINDEMANN = 2, RXN_TROE = 3 };
 enum : int { KIN_STANDARD = 0, KIN_INTERP = 1 };
@@ -57,6 +63,7 @@ __host__ __device__ inline int chem_threads_for(int S) {
 // Device tables of one mechanism (all arrays in global memory).
 struct MechView {
     int S, R, nT;
+    int qss_threads;      // QSS launch width chosen by ember_source_autotune (0: none)
     int n_tb, n_fo;       // reactions with [M] (three-body and falloff); falloff reactions
     double Tmin, Tmax;
     const double* W;      // [S]
@@ -103,14 +110,14 @@ struct ChemSmem {
     double* wd;    // [S] destruction
     double* wn;    // [S] net (only when the caller wants it; may alias wd otherwise)
     double* hk;    // [S] partial molar enthalpies [J/kmol]
-    double* ropf;  // [R]
+    double* ropf;  // [R] (shared memory, or global when the point's matrices take the shared memory)
     double* ropr;  // [R]
     double* concm; // [n_tb]
     double* fo_kinf;  // [n_fo]
     double* fo_rkinf; // [n_fo] 1/(kinf + 1e-300)
     double* fo_k0;    // [n_fo]
     double* fo_lfc;   // [n_fo] log10 Fcent (Troe)
-    double* red;      // [kMaxChemThreads + 2] reduction scratch
+    double* red;      // [kRedDoubles] reduction scratch
     double* fo_F;     // [n_fo] falloff F of the last composition (only when set; for Jacobians)
     double* fo_pr;    // [n_fo] reduced pressure Pr of the last composition (idem)
     double* fo_dF;    // [n_fo] dF/dPr of the last composition (idem)
@@ -118,14 +125,16 @@ struct ChemSmem {
     double* kfm;   // global [R]: rate constant x multiplier (falloff rows: refreshed per composition)
     double* rkc;   // global [R]: 1/Kc
 
-    // shared-memory doubles (with_net: a separate wn array)
-    static __host__ __device__ size_t doubles(int S, int R, int n_tb, int n_fo, bool with_net) {
-        return size_t(with_net ? 9 : 8) * S + size_t(2) * R + n_tb + size_t(4) * n_fo + kMaxChemThreads + 2;
+    // shared-memory doubles (with_net: a separate wn array; rop_smem: ropf and
+    // ropr in shared memory)
+    static __host__ __device__ size_t doubles(int S, int R, int n_tb, int n_fo, bool with_net, bool rop_smem = true) {
+        return size_t(with_net ? 9 : 8) * S + (rop_smem ? size_t(2) * R : 0) + n_tb + size_t(4) * n_fo + kRedDoubles;
     }
     // global doubles per point slot
     static __host__ __device__ size_t global_doubles(int R) { return size_t(2) * R; }
 
-    __device__ void carve(double* base, double* gbase, const MechView& m, bool with_net) {
+    // rop_global: 2R doubles of global memory for ropf/ropr, or null (shared memory)
+    __device__ void carve(double* base, double* gbase, const MechView& m, bool with_net, double* rop_global = nullptr) {
         const int S = m.S, R = m.R;
         c = base;
         ym = c + S;
@@ -136,9 +145,16 @@ struct ChemSmem {
         wd = wq + S;
         hk = wd + S;
         wn = with_net ? hk + S : wd;
-        ropf = hk + S + (with_net ? S : 0);
-        ropr = ropf + R;
-        concm = ropr + R;
+        double* p = hk + S + (with_net ? S : 0);
+        if (rop_global) {
+            ropf = rop_global;
+            ropr = rop_global + R;
+        } else {
+            ropf = p;
+            ropr = p + R;
+            p += 2 * R;
+        }
+        concm = p;
         fo_kinf = concm + m.n_tb;
         fo_rkinf = fo_kinf + m.n_fo;
         fo_k0 = fo_rkinf + m.n_fo;
@@ -158,23 +174,24 @@ __device__ __forceinline__ int lane_id() { return threadIdx.x & 31; }
 __device__ __forceinline__ double dmaxr(double a, double b) { return (a < b) ? b : a; }  // std::max
 __device__ __forceinline__ double dminr(double a, double b) { return (b < a) ? b : a; }  // std::min
 
-// Block sum of the threads' partial sums in the fixed order described above.
-// Every thread of the CTA must call it; all receive the result.
-template <int NT>
-__device__ __forceinline__ double block_sum(double* red, double partial) {
+// Sum over count elements in the fixed order described above. term(k, p)
+// returns the partial sum p advanced by element k (p + a[k], or
+// fma(a[k], b[k], p)); it is evaluated by the first warp only, after a
+// barrier, so it may read what any thread wrote before the call. Every
+// thread of the CTA must call it; all receive the result.
+template <int NT, class Term>
+__device__ __forceinline__ double block_sum(double* red, int count, Term term) {
     const int t = threadIdx.x;
-    red[t] = partial;
     __syncthreads();
     if (t < 32) {
-        double q = red[t];
-#pragma unroll
-        for (int w = 1; w < NT / 32; ++w) q = q + red[t + 32 * w];
+        double q = 0.0;
+        for (int k = t; k < count; k += 32) q = term(k, q);
 #pragma unroll
         for (int off = 16; off >= 1; off >>= 1) q = q + __shfl_xor_sync(0xffffffffu, q, off);
-        if (t == 0) red[kMaxChemThreads] = q;
+        if (t == 0) red[kRedSumSlot] = q;
     }
     __syncthreads();
-    const double r = red[kMaxChemThreads];
+    const double r = red[kRedSumSlot];
     __syncthreads();
     return r;
 }
@@ -298,24 +315,17 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
     const int S = m.S;
     const int t = threadIdx.x;
     if (mode == STATE_NORMALIZED) {
-        double part = 0.0;
-        for (int k = t; k < S; k += NT) part = part + dmaxr(Y[k], 0.0);
-        const double rnorm = 1.0 / block_sum<NT>(w.red, part);
+        const double rnorm = 1.0 / block_sum<NT>(w.red, S, [&](int k, double q) { return q + dmaxr(Y[k], 0.0); });
         for (int k = t; k < S; k += NT) w.ym[k] = (dmaxr(Y[k], 0.0) * rnorm) * m.rW[k];
     } else {
         for (int k = t; k < S; k += NT) w.ym[k] = Y[k] * m.rW[k];
     }
-    double part = 0.0;
-    for (int k = t; k < S; k += NT) part = part + w.ym[k];
-    const double mmw = 1.0 / block_sum<NT>(w.red, part);
+    const double* ym = w.ym;
+    const double mmw = 1.0 / block_sum<NT>(w.red, S, [&](int k, double q) { return q + ym[k]; });
     const double rho = (p * mmw) / (kGasConstant * T);
-    double cpart = 0.0;
-    for (int k = t; k < S; k += NT) {
-        const double ymk = w.ym[k];
-        w.c[k] = ymk * rho;
-        cpart = fma(ymk * mmw, w.cpR[k], cpart);
-    }
-    __syncthreads();
+    for (int k = t; k < S; k += NT) w.c[k] = ym[k] * rho;
+    const double* cpR = w.cpR;
+    const double cpsum = block_sum<NT>(w.red, S, [&](int k, double q) { return fma(ym[k] * mmw, cpR[k], q); });
     const double ctot = rho / mmw;
     // [M] of third-body and falloff reactions
     for (int s = t; s < m.n_tb; s += NT) {
@@ -413,9 +423,10 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
         w.wd[k] = d;
         if (want_net) w.wn[k] = nt;
     }
-    cp_out = (kGasConstant * block_sum<NT>(w.red, cpart)) / mmw;
+    cp_out = (kGasConstant * cpsum) / mmw;
     rho_out = rho;
     w.mmw = mmw;
+    __syncthreads();  // the species loop above is in participation order, not thread order
 }
 
 }  // namespace ember

@@ -123,9 +123,9 @@ struct SourceQssOde {
             rrho = 1.0 / rho_c;
             rrc = 1.0 / (rho_c * cp_c);
         }
-        double part = 0.0;
-        for (int k = tid; k < S; k += NT) part = fma(w.wq[k] - w.wd[k], w.hk[k], part);
-        const double qdot = -block_sum<NT>(w.red, part) + igniter(*a, t, x);
+        const double *wq = w.wq, *wd = w.wd, *hk = w.hk;
+        const double qdot =
+            -block_sum<NT>(w.red, S, [&](int k, double p) { return fma(wq[k] - wd[k], hk[k], p); }) + igniter(*a, t, x);
         for (int i = tid; i < S + 2; i += NT) {
             const double sc = split ? split[i] : 0.0;
             if (i == 0) {
@@ -192,10 +192,10 @@ __global__ void k_order_scatter(const double* __restrict__ dt, int n, int* curso
         order[atomicAdd(&cursor[dt_bucket(dt[j])], 1)] = j;
 }
 
-// Resident CTAs per SM the register budget is sized for: with NT <= 160
-// threads, 4 CTAs fit in 96 registers per thread without spills (the 3 of an
-// unconstrained build leave the FP64 pipe idle on shared-memory latency).
-constexpr int qss_min_blocks(int nt) { return nt <= 160 ? 4 : 2; }
+// Resident CTAs per SM the register budget is sized for (none of the widths
+// spills): 5 for NT <= 128 (the shared-memory limit of the 150-species
+// mechanism), 4 for 160, 3 for 192, 2 for 256.
+constexpr int qss_min_blocks(int nt) { return nt <= 128 ? 5 : (nt <= 160 ? 4 : (nt <= 192 ? 3 : 2)); }
 
 template <int NT>
 __global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView m, SourceArgs a, int* counter,
@@ -607,6 +607,10 @@ int source_check_options(const ember_source_options* o) {
     EMBER_CHECK_ARG(o->bdf_reltol > 0 && o->bdf_abstol_momentum > 0 && o->bdf_abstol_energy > 0 &&
                         o->bdf_abstol_species > 0 && o->bdf_max_num_steps > 0,
                     "bad BDF tolerances");
+    bool width_ok = o->threads_per_point == 0;
+    for (int c : kQssThreadChoices) width_ok = width_ok || o->threads_per_point == c;
+    EMBER_CHECK_ARG(width_ok, "threads_per_point must be 0 or one of 32, 64, 96, 128, 160, 192, 256 (got %d)",
+                    o->threads_per_point);
     return EMBER_OK;
 }
 
@@ -615,6 +619,7 @@ SourceArgs make_source_args(const ember_source_options* o, int n, const double* 
                             int* stats) {
     SourceArgs a{};
     a.n = n;
+    a.threads = o->threads_per_point;
     a.state_in = state_in;
     a.split = split;
     a.dt = dt;
@@ -690,11 +695,20 @@ static int qss_scratch_nt(const MechView& m, const SourceArgs& a, size_t* bytes)
     return EMBER_OK;
 }
 
+int source_qss_threads(const MechView& m, const SourceArgs& a) {
+    if (a.threads) return a.threads;
+    if (m.qss_threads) return m.qss_threads;
+    return chem_threads_for(m.S);
+}
+
 int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes) {
-    switch (chem_threads_for(m.S)) {
+    switch (source_qss_threads(m, a)) {
+        case 32: return qss_scratch_nt<32>(m, a, bytes);
         case 64: return qss_scratch_nt<64>(m, a, bytes);
+        case 96: return qss_scratch_nt<96>(m, a, bytes);
         case 128: return qss_scratch_nt<128>(m, a, bytes);
         case 160: return qss_scratch_nt<160>(m, a, bytes);
+        case 192: return qss_scratch_nt<192>(m, a, bytes);
         default: return qss_scratch_nt<256>(m, a, bytes);
     }
 }
@@ -713,11 +727,20 @@ static int launch_qss_nt(const MechView& m, const SourceArgs& a, int* counter, S
     return EMBER_OK;
 }
 
+static int cuda_check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return EMBER_OK;
+    set_error("%s failed: %s", what, cudaGetErrorString(e));
+    return EMBER_ECUDA;
+}
+
 int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
-    switch (chem_threads_for(m.S)) {
+    switch (source_qss_threads(m, a)) {
+        case 32: return launch_qss_nt<32>(m, a, counter, sc, st);
         case 64: return launch_qss_nt<64>(m, a, counter, sc, st);
+        case 96: return launch_qss_nt<96>(m, a, counter, sc, st);
         case 128: return launch_qss_nt<128>(m, a, counter, sc, st);
         case 160: return launch_qss_nt<160>(m, a, counter, sc, st);
+        case 192: return launch_qss_nt<192>(m, a, counter, sc, st);
         default: return launch_qss_nt<256>(m, a, counter, sc, st);
     }
 }
@@ -771,6 +794,73 @@ extern "C" int ember_source_integrate(ember_mech m, int method, int n, const dou
             return EMBER_EFAIL;
         }
     }
+    return EMBER_OK;
+}
+
+extern "C" int ember_source_autotune(ember_mech m, int method, int n, const double* state_in,
+                                     const double* split_const, const double* dt, double t_start, const double* x,
+                                     const ember_source_options* opts, int* threads_out, double* ms_out, int mem,
+                                     void* stream) {
+    EMBER_CHECK_ARG(m != nullptr, "null mechanism");
+    EMBER_CHECK_ARG(method == EMBER_SOURCE_QSS || method == EMBER_SOURCE_BDF, "bad method %d", method);
+    EMBER_CHECK_ARG(n > 0, "autotuning needs at least one point");
+    EMBER_CHECK_ARG(state_in && dt && threads_out, "null state_in/dt/threads_out");
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_TRY(source_check_options(opts));
+    constexpr int kChoices = sizeof(kQssThreadChoices) / sizeof(kQssThreadChoices[0]);
+    static_assert(kChoices == EMBER_SOURCE_N_THREAD_CHOICES, "thread choices out of step with the header");
+    if (ms_out)
+        for (int i = 0; i < kChoices; ++i) ms_out[i] = 0.0;
+    if (method == EMBER_SOURCE_BDF) {
+        *threads_out = chem_threads_for(m->S);
+        return EMBER_OK;
+    }
+    EMBER_TRY(ensure_device());
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    const int nv = m->S + 2;
+    const double *d_in, *d_split, *d_dt, *d_x;
+    EMBER_TRY(stage_in(sc, state_in, size_t(n) * nv, mem, st, &d_in));
+    EMBER_TRY(stage_in(sc, split_const, size_t(n) * nv, mem, st, &d_split));
+    EMBER_TRY(stage_in(sc, dt, n, mem, st, &d_dt));
+    EMBER_TRY(stage_in(sc, x, n, mem, st, &d_x));
+    double* d_out = nullptr;
+    int *d_status = nullptr, *counter = nullptr;
+    EMBER_TRY(sc.alloc(&d_out, size_t(n) * nv));
+    EMBER_TRY(sc.alloc(&d_status, n));
+    EMBER_TRY(sc.alloc(&counter, 1));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    EMBER_CUDA_TRY(cudaEventCreate(&e0));
+    int rc = cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
+    int best = 0;
+    float best_ms = 0.0f;
+    for (int i = 0; i < kChoices && rc == EMBER_OK; ++i) {
+        ember_source_options o = *opts;
+        o.threads_per_point = kQssThreadChoices[i];
+        SourceArgs a = make_source_args(&o, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, nullptr);
+        float ms = 0.0f;
+        for (int rep = 0; rep < 2 && rc == EMBER_OK; ++rep) {  // the first run is untimed
+            rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), st), "cudaMemsetAsync");
+            if (rc == EMBER_OK) rc = cuda_check(cudaEventRecord(e0, st), "cudaEventRecord");
+            if (rc == EMBER_OK) rc = launch_source_qss(m->view, a, counter, sc, st);
+            if (rc == EMBER_OK) rc = cuda_check(cudaEventRecord(e1, st), "cudaEventRecord");
+            if (rc == EMBER_OK) rc = cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+            if (rc == EMBER_OK) rc = cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        }
+        if (rc != EMBER_OK) break;
+        if (ms_out) ms_out[i] = ms;
+        if (best == 0 || ms < best_ms) {
+            best = kQssThreadChoices[i];
+            best_ms = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    sc.release();
+    EMBER_TRY(rc);
+    EMBER_TRY(finish_call(EMBER_MEM_DEVICE, st));
+    m->view.qss_threads = best;
+    *threads_out = best;
     return EMBER_OK;
 }
 

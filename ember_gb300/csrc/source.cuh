@@ -12,6 +12,7 @@ namespace ember {
 // Flattened arguments of one source-term launch (device pointers).
 struct SourceArgs {
     int n;
+    int threads;              // QSS threads per point requested (0: the mechanism's tuned or default width)
     const double* state_in;   // [n][S+2]
     const double* split;      // [n][S+2] or null
     const double* dt;         // [n]
@@ -89,6 +90,8 @@ SourceArgs make_source_args(const ember_source_options* o, int n, const double* 
 int source_check_options(const ember_source_options* o);
 // Device bytes a launch above takes from its Scratch (for an arena sized up front).
 int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes);
+// Threads per point of the QSS kernel for these arguments (see threads_per_point).
+int source_qss_threads(const MechView& m, const SourceArgs& a);
 int source_bdf_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes);
 
 }  // namespace ember

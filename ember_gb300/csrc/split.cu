@@ -609,6 +609,9 @@ extern "C" int ember_split_create(ember_mech mech, int n_flames, const ember_dif
     auto* h = new ember_split_s;
     h->mech = mech;
     h->opt = *opts;
+    // the handle keeps the QSS width its scratch arena was sized for, even if
+    // the mechanism is tuned again later
+    if (opts->method == EMBER_SOURCE_QSS) h->opt.source.threads_per_point = source_qss_threads(mech->view, probe);
     h->n_flames = n_flames;
     h->n_vars = n_vars;
     h->nmax = nmax;

@@ -34,7 +34,7 @@ class SourceOptions(C.Structure):
         ("qss_iteration_count", C.c_int), ("qss_stability_check", C.c_int),
         ("bdf_reltol", C.c_double), ("bdf_abstol_momentum", C.c_double), ("bdf_abstol_energy", C.c_double),
         ("bdf_abstol_species", C.c_double), ("bdf_min_step", C.c_double), ("bdf_max_num_steps", C.c_int),
-        ("bdf_reserved", C.c_int),
+        ("threads_per_point", C.c_int),
         ("ignition_tstart", C.c_double), ("ignition_duration", C.c_double), ("ignition_energy", C.c_double),
         ("ignition_center", C.c_double), ("ignition_stddev", C.c_double),
     ]
@@ -52,6 +52,7 @@ class SourceOptions(C.Structure):
         o.bdf_abstol_species, o.bdf_min_step, o.bdf_max_num_steps = 1e-13, 1e-18, 1_000_000
         o.ignition_tstart, o.ignition_duration, o.ignition_energy = 0.0, 1e-3, 0.0
         o.ignition_center, o.ignition_stddev = 0.0, 1e-4
+        o.threads_per_point = 0  # the mechanism's autotuned width, else the default for its size
         for k, v in kw.items():
             if not hasattr(o, k):
                 raise AttributeError(k)
@@ -101,6 +102,31 @@ class GpuMechanism:
         out["cp_mass"] = cp
         out["density"] = rho
         return out
+
+
+THREAD_CHOICES = (32, 64, 96, 128, 160, 192, 256)
+
+
+def autotune(gmech: GpuMechanism, method: int, state, dt, opts: SourceOptions | None = None, split_const=None,
+             t_start: float = 0.0, x=None, stream=None):
+    """``ember_source_autotune``: time the QSS kernel at every width of
+    THREAD_CHOICES on these points, keep the fastest in the mechanism handle
+    (used by later calls whose threads_per_point is 0) and return
+    (width, {width: ms}). Host (numpy) arrays or torch CUDA tensors."""
+    opts = opts or SourceOptions.defaults()
+    mem = L.mem_of(state)
+    n = int(state.shape[0])
+    if mem == L.MEM_HOST:
+        state = np.ascontiguousarray(state, dtype=np.float64)
+        dt = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,)))
+        split_const = np.ascontiguousarray(split_const, dtype=np.float64) if split_const is not None else None
+        x = np.ascontiguousarray(x, dtype=np.float64) if x is not None else None
+    width = C.c_int(0)
+    ms = (C.c_double * len(THREAD_CHOICES))()
+    L.check(L.lib().ember_source_autotune(gmech.handle, method, n, L.ptr(state), L.ptr(split_const), L.ptr(dt),
+                                          float(t_start), L.ptr(x), C.byref(opts), C.byref(width), ms, mem,
+                                          L.stream_ptr(stream)), "ember_source_autotune")
+    return width.value, {c: ms[i] for i, c in enumerate(THREAD_CHOICES) if ms[i] > 0}
 
 
 def integrate_production_terms(gmech: GpuMechanism, method: int, state, dt, opts: SourceOptions | None = None,

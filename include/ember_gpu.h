@@ -290,6 +290,58 @@ int ember_gas_eval(ember_mech mech, int n_points, double pressure, int kinetics_
                    double* hk, double* cp_mass, double* density, int mem, void* stream);
 
 /* ======================================================================
+ * Thermo and transport properties of the flame state
+ *
+ * One call = FlameSolver::updateChemicalProperties (src/flameSolver.cpp:
+ * 652-699) for a batch of grid points with the default transport model
+ * "Approx" (ApproxMixTransport, src/chemistry0d.cpp:12-269): density, mean
+ * molecular weight, cp, partial molar cp and enthalpies; mixture-averaged
+ * thermal conductivity (0.5 (sum X_k lambda_k + 1 / sum X_k / lambda_k)),
+ * viscosity (Wilke's rule over the species whose mole fraction is at least
+ * `threshold`, ApproxMixTransport::viscosity / updateViscosity_T, 22-52 and
+ * 181-205) and the mass-based mixture diffusion coefficients times density
+ * (CanteraGas::getWeightedDiffusionCoefficientsMass, 583-591, over
+ * ApproxMixTransport::getMixDiffCoeffsMass, 98-139, whose sums run over all
+ * species for a major species and over the major species otherwise).
+ * threshold = 0 gives Cantera's plain mixture-averaged model ("Mix").
+ * Mole fractions are floored at 1e-20 for the transport sums, as Cantera's
+ * MixTransport does. Species properties come from polynomial fits in ln T
+ * (Cantera's non-CK fitting form):
+ *   sqrt(mu_k) = T^(1/4) P(ln T),  lambda_k = T^(1/2) P(ln T),
+ *   p D_jk     = T^(3/2) P(ln T)   (D at pressure p),
+ * P(x) = c0 + c1 x + c2 x^2 + c3 x^3 + c4 x^4. Thermal diffusion (Soret) is
+ * not computed: Ember turns it off for "Approx" (python/ember/input.py:377-383).
+ * ==================================================================== */
+typedef struct {
+    int n_species;
+    const double* visc_fit;   /* [S][5] mu_k in Pa s                                            */
+    const double* cond_fit;   /* [S][5] lambda_k in W/m/K                                       */
+    const double* diff_fit;   /* [S(S+1)/2][5] D_jk in m^2/s; pair j <= k at j S - j(j-1)/2 + k - j */
+} ember_transport_desc;
+
+typedef struct ember_transport_s* ember_transport;
+
+/* Upload the fits of a mechanism's species (n_species must match mech). */
+int ember_transport_create(ember_mech mech, const ember_transport_desc* desc, ember_transport* out);
+int ember_transport_destroy(ember_transport tr);
+
+/* Outputs of ember_transport_eval (point-major; any pointer may be NULL). */
+typedef struct {
+    double* density;       /* [n] kg/m^3                      (rho)     */
+    double* mean_mol_weight;/* [n] kg/kmol                    (Wmx)     */
+    double* cp_mass;       /* [n] J/kg/K                      (cp)      */
+    double* cp_species;    /* [n][S] partial molar cp J/kmol/K (cpSpec) */
+    double* h_species;     /* [n][S] partial molar h J/kmol   (hk)      */
+    double* conductivity;  /* [n] W/m/K                       (lambda)  */
+    double* viscosity;     /* [n] Pa s                        (mu)      */
+    double* rho_d;         /* [n][S] rho D_k kg/m/s           (rhoD)    */
+} ember_properties;
+
+/* T [n], Y [n][S] (normalised as setState_TPY: negative Y clipped, sum 1). */
+int ember_transport_eval(ember_transport tr, int n_points, double pressure, double threshold, const double* T,
+                         const double* Y, const ember_properties* out, int mem, void* stream);
+
+/* ======================================================================
  * Production (chemistry source term) stage
  *
  * One call = FlameSolver::integrateProductionTerms() for a batch of grid
@@ -329,7 +381,11 @@ typedef struct {
     /* CvodeTolerances (python/ember/input.py:733-745) */
     double bdf_reltol, bdf_abstol_momentum, bdf_abstol_energy, bdf_abstol_species, bdf_min_step;
     int bdf_max_num_steps;
-    int bdf_reserved;
+    /* threads per grid point of the QSS kernel (one CTA per point): 0 = the
+     * width ember_source_autotune chose for the mechanism, else the default
+     * for its size; or 32, 64, 96, 128, 160, 192, 256. Results do not depend
+     * on it (every reduction runs in one fixed 32-lane order). */
+    int threads_per_point;
     /* ignition source of SourceSystem::getQdotIgniter (src/sourceSystem.cpp:33-45);
      * ignition_energy == 0 disables it */
     double ignition_tstart, ignition_duration, ignition_energy, ignition_center, ignition_stddev;
@@ -347,6 +403,22 @@ int ember_source_integrate(ember_mech mech, int method, int n_points, const doub
                            const double* split_const, const double* dt, double t_start, const double* x,
                            const ember_source_options* opts, double* state_out, int* status, int* stats,
                            int mem, void* stream);
+
+/* Autotuner of the QSS launch width: integrates the given points (a sample of
+ * the workload; the same arguments as ember_source_integrate) once with every
+ * threads-per-point width of EMBER_SOURCE_THREAD_CHOICES, times each run on
+ * the stream with CUDA events (after one untimed run), and stores the fastest
+ * width in the mechanism handle, where calls whose threads_per_point is 0 pick
+ * it up. threads_out: the chosen width; ms_out: [EMBER_SOURCE_N_THREAD_CHOICES]
+ * milliseconds per width (0 where the width does not fit) or NULL. The BDF
+ * kernel has a single width per mechanism size: method EMBER_SOURCE_BDF
+ * returns it without timing. Integration results are identical for every
+ * width. */
+#define EMBER_SOURCE_N_THREAD_CHOICES 7
+#define EMBER_SOURCE_THREAD_CHOICES {32, 64, 96, 128, 160, 192, 256}
+int ember_source_autotune(ember_mech mech, int method, int n_points, const double* state_in, const double* split_const,
+                          const double* dt, double t_start, const double* x, const ember_source_options* opts,
+                          int* threads_out, double* ms_out, int mem, void* stream);
 
 /* Discrete adjoint of a BDF source-term integration (EMBER_SOURCE_BDF, same
  * arguments as ember_source_integrate): for phi = sum over points of

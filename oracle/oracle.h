@@ -91,7 +91,7 @@ typedef struct {
     int qss_iteration_count, qss_stability_check;
     double bdf_reltol, bdf_abstol_momentum, bdf_abstol_energy, bdf_abstol_species, bdf_min_step;
     int bdf_max_num_steps;
-    int bdf_reserved;
+    int threads_per_point; /* launch width of the GPU kernel; no effect here */
     double ignition_tstart, ignition_duration, ignition_energy, ignition_center, ignition_stddev;
 } oracle_source_options;
 
@@ -127,6 +127,12 @@ int oracle_bdf_point(const oracle_mech* m, oracle_ws* w, const oracle_source_opt
 void oracle_source_batch(const oracle_mech* m, int method, int n, const double* state_in, const double* split,
                          const double* dt, double t_start, const double* x, const oracle_source_options* o,
                          double* state_out, int* status, int* stats, int n_threads);
+
+/* ---- transport (oracle_transport.c) ------------------------------------- */
+void oracle_transport_eval(const oracle_mech* m, const double* visc_fit, const double* cond_fit,
+                           const double* diff_fit, int n, double p, double thr, const double* T, const double* Y,
+                           double* density, double* mean_mw, double* cp_mass, double* cp_species, double* h_species,
+                           double* conductivity, double* viscosity, double* rho_d);
 
 #ifdef __cplusplus
 }

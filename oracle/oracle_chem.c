@@ -118,21 +118,18 @@ static double oracle_exp10(double x) { return oracle_exp(x * 2.302585092994046);
 static double dmax(double a, double b) { return (a < b) ? b : a; } /* std::max */
 static double dmin(double a, double b) { return (b < a) ? b : a; } /* std::min */
 
-/* Threads per grid point of the GPU kernels for S species (the state
- * vector of S+2 values fits one pass): the width of the reduction order. */
+/* Width of the reduction order of the GPU kernels: 32 lanes, whatever the
+ * number of threads per grid point. */
 static int reduction_width(int S) {
-    const int n = S + 2;
-    if (n <= 64) return 64;
-    if (n <= 128) return 128;
-    if (n <= 160) return 160;
-    return 256;
+    (void)S;
+    return 32;
 }
 
 /* Sum of a[k] (b == NULL) or of a[k] * b[k] accumulated by fma, in the fixed
  * order of the GPU block reduction: element k goes to the partial sum of
- * thread k mod W (sequential in k); the W partials are folded into 32 as
- * p[l] + p[l+32] + p[l+64] + ... (in that order) and combined by an xor
- * butterfly. */
+ * lane k mod W (sequential in k; W = 32 for the kernels); the W partials are
+ * folded into 32 as p[l] + p[l+32] + p[l+64] + ... (in that order) and
+ * combined by an xor butterfly. */
 double oracle_block_sum(const double* a, const double* b, int n, int W);
 int oracle_reduction_width(int S) { return reduction_width(S); }
 #define block_sum oracle_block_sum

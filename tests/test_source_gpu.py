@@ -223,3 +223,40 @@ def test_empty_and_single_point_batches(pair_small, small_mech, method):
         one, ost, ostats = integrate_production_terms(g, m, st[j:j + 1], dt[j:j + 1], opts)
         assert np.array_equal(one[0], full[j]) and ost[0] == fst[j]
         assert np.array_equal(ostats[0], fstats[j])
+
+
+def test_qss_results_do_not_depend_on_the_launch_width(gpu_lib, big_mech):
+    # every reduction runs in one 32-lane order, so each width gives the
+    # oracle's bits
+    from ember_gb300.source import THREAD_CHOICES
+    g, o = GpuMechanism(big_mech), chem.OracleMech(big_mech)
+    st, dt = _states(big_mech, 40, seed=21)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_INTERP)
+    ro, rs, rst = o.integrate(chem.QSS, st, dt, opts)
+    for width in THREAD_CHOICES:
+        out, status, stats = integrate_production_terms(g, QSS, st, dt,
+                                                        SourceOptions.defaults(kinetics_model=KINETICS_INTERP,
+                                                                               threads_per_point=width))
+        np.testing.assert_array_equal(status, rs, err_msg=str(width))
+        assert np.array_equal(out, ro), (width, np.abs(out - ro).max())
+        np.testing.assert_array_equal(stats[:, :3], rst[:, :3], err_msg=str(width))
+
+
+def test_autotune_keeps_the_fastest_width_and_the_results(gpu_lib, small_mech):
+    from ember_gb300.source import THREAD_CHOICES, BDF, autotune
+    g, o = GpuMechanism(small_mech), chem.OracleMech(small_mech)
+    st, dt = _states(small_mech, 200, seed=22)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    width, ms = autotune(g, QSS, st, dt, opts)
+    assert width in THREAD_CHOICES and width in ms
+    assert set(ms) == set(THREAD_CHOICES) and all(v > 0 for v in ms.values())
+    assert ms[width] == min(ms.values())
+    out, status, _ = integrate_production_terms(g, QSS, st, dt, opts)  # threads_per_point 0: the tuned width
+    ro, rs, _ = o.integrate(chem.QSS, st, dt, opts)
+    np.testing.assert_array_equal(status, rs)
+    assert np.array_equal(out, ro)
+    # the BDF kernel has one width per mechanism size: returned untimed
+    bw, bms = autotune(g, BDF, st[:4], dt[:4], opts)
+    assert bw in THREAD_CHOICES and bms == {}
+    with pytest.raises(L.EmberGpuError):
+        integrate_production_terms(g, QSS, st, dt, SourceOptions.defaults(threads_per_point=48))
