@@ -47,7 +47,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="qss", choices=["qss", "bdf", "diffusion", "split", "adjoint"])
+    p.add_argument("--workload", default="qss", choices=["qss", "bdf", "diffusion", "split", "adjoint", "transport"])
     p.add_argument("--points", type=int, default=N_POINTS)
     p.add_argument("--kinetics", default="interp", choices=["interp", "standard"])
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
@@ -487,8 +487,11 @@ def run_ours_diffusion(args):
 SPLIT_METRIC = "ms per split step"
 SPLIT_DT = 2e-5
 SPLIT_WORKLOAD = ("C5 strain-sweep proxy: 32 seeded flame-like profiles (150-700 points), synthetic "
-                  "150-species/1000-reaction mechanism, balanced D-S-D split step (dt 2e-5 s; diffusion "
-                  "h rule, QSS source, interp kinetics), convection not integrated")
+                  "150-species/1000-reaction mechanism, FlameSolver step without convection: thermo and "
+                  "Approx transport (seeded kinetic-theory fits), B/D and cross terms from the step-start "
+                  "state, balanced D-S-D split step (dt 2e-5 s; diffusion h rule, QSS source, interp kinetics)")
+SPLIT_TRANSPORT_SEED = 1523
+SPLIT_THRESHOLD = 1e-5
 
 
 def split_inputs(rank: int):
@@ -513,11 +516,13 @@ def run_reference_split(args):
     n0 = g0[0].n_points
     nv = mech.n_vars
     st0, B0, D0 = state[:n0], B[:nv * n0], D[:nv * n0]
+    from ember_gb300.transport import synthetic_transport
+    tr = (synthetic_transport(mech, seed=SPLIT_TRANSPORT_SEED), SPLIT_THRESHOLD, True)
     for _ in range(args.warmup):
-        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, QSS, opts)
+        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, QSS, opts, transport=tr)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, QSS, opts)
+        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, QSS, opts, transport=tr)
     per_flame = (time.perf_counter() - t0) / args.steps
     # scaled to the 32-flame batch by points
     ms = 1e3 * per_flame * len(state) / n0
@@ -550,6 +555,9 @@ def run_ours_split(args):
     # QSS launch width tuned on the flames' start states over one step (before the solver takes it)
     width, tune_ms = autotune(gm, QSS, state, np.full(len(state), SPLIT_DT), opts)
     solver = FlameBatchSplitSolver(gm, grids, SPLIT_DT, method=QSS, source_options=opts)
+    from ember_gb300.transport import GpuTransport, synthetic_transport
+    tdata = synthetic_transport(mech, seed=SPLIT_TRANSPORT_SEED)
+    gtr = GpuTransport(gm, tdata)
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
@@ -557,6 +565,7 @@ def run_ours_split(args):
     _lib.check(_lib.lib().ember_probe_fp64_rate(0, C.byref(peak)), "probe")
     solver.set_state(0.0, state)
     solver.set_transport(B, D)
+    solver.set_transport_model(gtr, SPLIT_THRESHOLD, cross_terms=True)
     solver.step(args.warmup, graph=True, stream=stream)
     torch.cuda.synchronize()
     sampler = ClockSampler(local)
@@ -595,7 +604,8 @@ def run_ours_split(args):
     clocks = sampler.stop()
     ms = total_ms / args.steps
     n_vals = state.size
-    flops = src_flops / args.steps + 4 * roofline.tridiag_flops_per_point() * n_vals
+    flops = (src_flops / args.steps + 4 * roofline.tridiag_flops_per_point() * n_vals
+             + roofline.transport_point_flops(mech.n_species) * len(state))
     achieved = flops / (ms / 1e3) / 1e12
     line = {
         "metric": SPLIT_METRIC, "value": ms, "unit": "ms", "n_gpus": ws, "steps": args.steps,
@@ -607,13 +617,15 @@ def run_ours_split(args):
                    "threads_per_point": width, "autotune_ms": {str(k): round(v, 2) for k, v in tune_ms.items()}},
         "e2e": {"value": 1e3 * sum(e2e) / len(e2e), "unit": "ms", "h2d_bytes_per_step": int(state.nbytes),
                 "d2h_bytes_per_step": int(state.nbytes)},
-        # per step: begin, 2 x (transpose, 2 x (stage, failure count, delta), transpose back), stage dt,
+        # per step: transport, B/D, jCorr (flux, step size, 2 integrator kernels, failure count), 2 cross-term
+        # kernels; begin, 2 x (transpose, 2 x (stage, failure count, delta), transpose back), stage dt,
         # 3 work-order kernels + QSS, failure count, end, mass fractions, clock
-        "gpu_launches": 26 * args.steps,
+        "gpu_launches": 35 * args.steps,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / (peak.value / 1e12), "traffic": None,
                      "peak_source": "live DFMA throughput probe (ember_probe_fp64_rate)",
-                     "work_model": "QSS flops of the source stage (roofline.py) + 4 diffusion stages x 73 flops/value"},
+                     "work_model": "QSS flops of the source stage + 4 diffusion stages x 73 flops/value + transport and "
+                                   "cross terms per point (roofline.py)"},
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:
@@ -625,7 +637,8 @@ def run_ours_split(args):
         t0 = time.perf_counter()
         reps = 0
         while time.perf_counter() - t0 < args.cpu_seconds or reps == 0:
-            osplit.split_steps(om, grids[:1], state[:n0], 0.0, B[:nv * n0], D[:nv * n0], SPLIT_DT, 1, QSS, opts)
+            osplit.split_steps(om, grids[:1], state[:n0], 0.0, B[:nv * n0], D[:nv * n0], SPLIT_DT, 1, QSS, opts,
+                               transport=(tdata, SPLIT_THRESHOLD, True))
             reps += 1
         tcpu = (time.perf_counter() - t0) / reps
         threads = os.cpu_count() or 1
@@ -764,8 +777,143 @@ def run_ours_adjoint(args):
     return 0
 
 
+# ------------------------------------------------------ transport workload --
+
+TRANSPORT_METRIC = "transport property evaluations/s"
+TRANSPORT_POINTS = 16384
+TRANSPORT_WORKLOAD = ("updateChemicalProperties of 16384 seeded states (the C2 state distribution): thermo and "
+                      "Approx mixture-averaged transport (threshold 1e-5), synthetic 150-species mechanism with "
+                      "seeded kinetic-theory fits")
+
+
+def transport_inputs(rank: int):
+    from ember_gb300.mechanism import reactor_states, synthetic_mechanism
+    from ember_gb300.transport import synthetic_transport
+    mech = synthetic_mechanism(seed=MECH_SEED)
+    state, _ = reactor_states(mech, TRANSPORT_POINTS, seed=4096 + rank)
+    return mech, synthetic_transport(mech, seed=SPLIT_TRANSPORT_SEED), state
+
+
+def _transport_cpu_rate(mech, td, state, target_s: float):
+    from oracle import chem
+    om = chem.OracleMech(mech)
+    n, t = 8, 0.0
+    while True:
+        t0 = time.perf_counter()
+        chem.transport_eval(om, td, state[:n, 1], state[:n, 2:], 101325.0, SPLIT_THRESHOLD)
+        t = time.perf_counter() - t0
+        if t > target_s / 4 or n >= len(state):
+            return n / t, n, t
+        n = min(len(state), n * 4)
+
+
+def run_reference_transport(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    mech, td, state = transport_inputs(0)
+    rates = [_transport_cpu_rate(mech, td, state, args.cpu_seconds / max(args.steps, 1)) for _ in range(args.steps)]
+    rate = statistics.median(r[0] for r in rates)
+    print(json.dumps({
+        "impl": "reference", "metric": TRANSPORT_METRIC, "value": rate, "unit": "points/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * TRANSPORT_POINTS / rate,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": TRANSPORT_WORKLOAD, "points": TRANSPORT_POINTS},
+        "cpu_baseline": {"value": rate, "unit": "points/s", "cores": 1, "kind": "port",
+                         "sample": f"first {rates[0][1]} states per step, one thread"},
+        "e2e": {"value": rate, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+    return 0
+
+
+def run_ours_transport(args):
+    import ctypes as C
+    import numpy as np
+    import torch
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        torch.distributed.init_process_group("nccl")
+    from ember_gb300 import _lib, roofline
+    from ember_gb300.source import GpuMechanism
+    from ember_gb300.transport import GpuTransport
+    mech, td, state = transport_inputs(rank)
+    gm = GpuMechanism(mech)
+    gt = GpuTransport(gm, td)
+    dev = torch.device("cuda", local)
+    T_d = torch.as_tensor(np.ascontiguousarray(state[:, 1]), device=dev)
+    Y_d = torch.as_tensor(np.ascontiguousarray(state[:, 2:]), device=dev)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    peak = C.c_double()
+    _lib.check(_lib.lib().ember_probe_fp64_rate(0, C.byref(peak)), "probe")
+    for _ in range(args.warmup):
+        gt.eval(T_d, Y_d, threshold=SPLIT_THRESHOLD, stream=stream)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush.zero_()
+        starts[i].record(stream)
+        gt.eval(T_d, Y_d, threshold=SPLIT_THRESHOLD, stream=stream)
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    if ws > 1:
+        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    # end to end: host states in, properties out
+    T_h, Y_h = np.ascontiguousarray(state[:, 1]), np.ascontiguousarray(state[:, 2:])
+    e2e = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = gt.eval(T_h, Y_h, threshold=SPLIT_THRESHOLD)
+        e2e.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    ms = total_ms / args.steps
+    n = TRANSPORT_POINTS
+    flops = roofline.transport_point_flops(mech.n_species, cross_terms=False) * n
+    achieved = flops / (ms / 1e3) / 1e12
+    S = mech.n_species
+    line = {
+        "metric": TRANSPORT_METRIC, "value": ws * n / (ms / 1e3), "unit": "points/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded states and transport fits)",
+        "config": {"workload": TRANSPORT_WORKLOAD, "points": n, "n_species": S,
+                   "l2": "256 MB buffer written between timed iterations"},
+        "e2e": {"value": ws * n * len(e2e) / sum(e2e), "unit": "points/s",
+                "h2d_bytes_per_step": int(T_h.nbytes + Y_h.nbytes),
+                "d2h_bytes_per_step": int(sum(v.nbytes for v in out.values()))},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / (peak.value / 1e12), "traffic": None,
+                     "peak_source": "live DFMA throughput probe (ember_probe_fp64_rate)",
+                     "work_model": "roofline.transport_point_flops (all species major)"},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, ns, t = _transport_cpu_rate(mech, td, state, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": rate, "unit": "points/s", "cores": 1, "kind": "port",
+                                "sample": f"first {ns} states, {t:.1f} s on one thread"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
 def main():
     args = parse_args()
+    if args.workload == "transport":
+        return run_reference_transport(args) if args.impl == "reference" else run_ours_transport(args)
     if args.workload == "diffusion":
         return run_reference_diffusion(args) if args.impl == "reference" else run_ours_diffusion(args)
     if args.workload == "split":

@@ -84,6 +84,7 @@ def _declare(lib):
         "ember_transport_create": (C.c_int, [vp, vp, vp]),
         "ember_transport_destroy": (C.c_int, [vp]),
         "ember_transport_eval": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, vp, vp, vp, C.c_int, vp]),
+        "ember_split_set_transport_model": (C.c_int, [vp, vp, C.c_double, C.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -26,6 +26,7 @@
 // restatement bit for bit.
 #include "common.cuh"
 #include "source.cuh"
+#include "transport.cuh"
 #include "tridiag.cuh"
 
 #include <algorithm>
@@ -362,6 +363,141 @@ __global__ void k_sum_rows2(int64_t n_pts, int R, const double* __restrict__ a, 
     }
 }
 
+// ---- properties of the step start (FlameSolver::step) ------------------------
+
+// prepareIntegrators (src/flameSolver.cpp:156-172), not quasi-2D: B and D of
+// every (point, variable) in the variable-major layout of the diffusion stages.
+__global__ void k_bd_from_props(SplitTables tb, int S, const double* __restrict__ rho, const double* __restrict__ cp,
+                                const double* __restrict__ lam, const double* __restrict__ mu,
+                                const double* __restrict__ rhoD, double* __restrict__ B, double* __restrict__ D) {
+    const int64_t total = tb.n_pts * tb.n;
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t p = e / tb.n;
+        const int v = static_cast<int>(e - p * tb.n);
+        const int64_t q = vm_index(tb, p, v);
+        if (v == 0) {
+            B[q] = 1.0 / rho[p];
+            D[q] = mu[p];
+        } else if (v == 1) {
+            B[q] = 1.0 / (rho[p] * cp[p]);
+            D[q] = lam[p];
+        } else {
+            B[q] = 1.0 / rho[p];
+            D[q] = rhoD[p * S + (v - 2)];
+        }
+    }
+}
+
+// Point p's Fick flux of species k to the right, jFick(k, j) of
+// updateCrossTerms (src/flameSolver.cpp:555-556).
+__device__ __forceinline__ double fick_flux(const double* st, const double* rhoD, int n, int S, int64_t p, int k,
+                                            double hh) {
+    return (-0.5 * (rhoD[p * S + k] + rhoD[(p + 1) * S + k])) * ((st[(p + 1) * n + 2 + k] - st[p * n + 2 + k]) / hh);
+}
+
+// jCorr = -sum_k jFick (no thermal diffusion: jSoret = 0), jCorr[jj] = 0
+// (src/flameSolver.cpp:551-565), and the smoothing system's B = lambda/(rho cp)
+// (573-577). One thread per point.
+__global__ void k_jcorr_fick(int64_t n_pts, int n, int S, const int* __restrict__ pt_local,
+                             const int* __restrict__ pt_flame, const int* __restrict__ flame_npts,
+                             const double* __restrict__ x, const double* __restrict__ st,
+                             const double* __restrict__ rhoD, const double* __restrict__ lam,
+                             const double* __restrict__ rho, const double* __restrict__ cp, double* __restrict__ jcorr,
+                             double* __restrict__ jB) {
+    for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < n_pts; p += int64_t(gridDim.x) * blockDim.x) {
+        const int i = pt_local[p];
+        const int N = flame_npts[pt_flame[p]];
+        double jc = 0.0;
+        if (i < N - 1) {
+            const double hh = x[p + 1] - x[p];
+            for (int k = 0; k < S; ++k) jc = jc - fick_flux(st, rhoD, n, S, p, k, hh);
+        }
+        jcorr[p] = jc;
+        jB[p] = lam[p] / (rho[p] * cp[p]);
+    }
+}
+
+// Step size of the jCorr smoothing (src/flameSolver.cpp:579-582), one thread per flame.
+__global__ void k_jcorr_h(int n_flames, const int64_t* __restrict__ goff, const int* __restrict__ npts,
+                          const double* __restrict__ x, const double* __restrict__ jB, double mult, double gdt,
+                          double* __restrict__ h) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_flames) return;
+    const double* xf = x + goff[f];
+    const double* bf = jB + goff[f];
+    double dt = gdt;
+    for (int j = 1; j < npts[f] - 1; ++j) {
+        const double dlj = 0.5 * (xf[j + 1] - xf[j - 1]);
+        const double cand = ((mult * dlj) * dlj) / bf[j];
+        dt = (cand < dt) ? cand : dt;  // std::min(dt, cand)
+    }
+    h[f] = dt;
+}
+
+__device__ __forceinline__ double grid_pow(double v, int alpha) { return alpha == 0 ? 1.0 : (alpha == 1 ? v : pow(v, alpha)); }
+
+// Species cross terms dYdtCross and the heat-capacity flux sums sumcpj
+// (src/flameSolver.cpp:591-609, jSoret = 0); zero at the boundary points.
+__global__ void k_cross_species(int64_t n_pts, int n, int S, const int* __restrict__ pt_local,
+                                const int* __restrict__ pt_flame, const int* __restrict__ flame_npts,
+                                const ember_diffusion_grid* __restrict__ grids, const double* __restrict__ x,
+                                const double* __restrict__ st, const double* __restrict__ rhoD,
+                                const double* __restrict__ cpS, const double* __restrict__ W,
+                                const double* __restrict__ rho, const double* __restrict__ jcorr,
+                                double* __restrict__ sumcpj, double* __restrict__ cross) {
+    for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < n_pts; p += int64_t(gridDim.x) * blockDim.x) {
+        const int i = pt_local[p];
+        const int f = pt_flame[p];
+        const int N = flame_npts[f];
+        if (i == 0 || i == N - 1) {
+            for (int k = 0; k < S; ++k) cross[p * n + 2 + k] = 0.0;
+            sumcpj[p] = 0.0;
+            continue;
+        }
+        const int alpha = grids[f].alpha;
+        const double r = grid_pow(x[p], alpha);
+        const double rph = grid_pow(0.5 * (x[p] + x[p + 1]), alpha);
+        const double rphm = grid_pow(0.5 * (x[p - 1] + x[p]), alpha);
+        const double dlj = 0.5 * (x[p + 1] - x[p - 1]);
+        const double hh = x[p + 1] - x[p];
+        const double c = -0.5 / ((r * rho[p]) * dlj);
+        const double jc = jcorr[p], jcm = jcorr[p - 1];
+        double s = 0.0;
+        for (int k = 0; k < S; ++k) {
+            const double yk = st[p * n + 2 + k], yk1 = st[(p + 1) * n + 2 + k], ykm = st[(p - 1) * n + 2 + k];
+            cross[p * n + 2 + k] = c * ((rph * (yk + yk1)) * jc - (rphm * (ykm + yk)) * jcm);
+            const double F = fick_flux(st, rhoD, n, S, p, k, hh);
+            s = s + ((0.5 * (cpS[p * S + k] + cpS[(p + 1) * S + k])) / W[k]) * (F + ((0.5 * (yk + yk1)) * jc));
+        }
+        sumcpj[p] = s;
+    }
+}
+
+// Temperature cross term dTdtCross (src/flameSolver.cpp:610-612) with the
+// grid's centred first-derivative weights (src/grid.cpp:61-65); the U row
+// and the boundary points are zero.
+__global__ void k_cross_temperature(int64_t n_pts, int n, const int* __restrict__ pt_local,
+                                    const int* __restrict__ pt_flame, const int* __restrict__ flame_npts,
+                                    const double* __restrict__ x, const double* __restrict__ st,
+                                    const double* __restrict__ rho, const double* __restrict__ cp,
+                                    const double* __restrict__ sumcpj, double* __restrict__ cross) {
+    for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < n_pts; p += int64_t(gridDim.x) * blockDim.x) {
+        const int i = pt_local[p];
+        const int N = flame_npts[pt_flame[p]];
+        cross[p * n] = 0.0;
+        double dT = 0.0;
+        if (i > 0 && i < N - 1) {
+            const double hh = x[p + 1] - x[p], hm = x[p] - x[p - 1];
+            const double cfp = hm / (hh * (hh + hm));
+            const double cf = (hh - hm) / (hh * hm);
+            const double cfm = -hh / (hm * (hh + hm));
+            const double dTdx = (cfm * st[(p - 1) * n + 1] + cf * st[p * n + 1]) + cfp * st[(p + 1) * n + 1];
+            dT = ((-0.5 * (sumcpj[p] + sumcpj[p - 1])) * dTdx) / (cp[p] * rho[p]);
+        }
+        cross[p * n + 1] = dT;
+    }
+}
+
 int grid_for(int64_t n, int threads = 256) {
     return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>((n + threads - 1) / threads, 4096)));
 }
@@ -401,6 +537,17 @@ struct ember_split_s {
     void* src_arena = nullptr;
     size_t src_arena_bytes = 0;
     DiffusionWarpPlan plan;
+    // transport model (ember_split_set_transport_model): properties of the step start
+    ember_transport tr = nullptr;
+    double tr_threshold = 0.0;
+    int tr_cross = 0;
+    void* pblob = nullptr;
+    double *p_rho = nullptr, *p_cp = nullptr, *p_lam = nullptr, *p_mu = nullptr, *p_rhoD = nullptr, *p_cpS = nullptr;
+    double *jcorr = nullptr, *jB = nullptr, *jD = nullptr, *jsc = nullptr, *jh = nullptr, *sumcpj = nullptr;
+    double* jwork = nullptr;
+    DiffSysInfo* jinfo = nullptr;
+    ember_diffusion_grid* d_grids = nullptr;
+    int *jstatus = nullptr, *pt_local = nullptr, *pt_flame = nullptr;
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -470,6 +617,52 @@ int enqueue_diffusion_pair(ember_split h, double f0, double f1, double f2, cudaS
     return EMBER_OK;
 }
 
+// Start of FlameSolver::step (src/flameSolver.cpp): updateChemicalProperties
+// from the current state, prepareIntegrators' B and D and, with cross terms,
+// updateCrossTerms into ddt_cross.
+int enqueue_properties(ember_split h, cudaStream_t st) {
+    const SplitTables tb = h->tables();
+    const int n = h->n_vars, S = n - 2;
+    ember_properties pr{};
+    pr.density = h->p_rho;
+    pr.cp_mass = h->p_cp;
+    pr.conductivity = h->p_lam;
+    pr.viscosity = h->p_mu;
+    pr.rho_d = h->p_rhoD;
+    pr.cp_species = h->tr_cross ? h->p_cpS : nullptr;
+    EMBER_TRY(launch_transport(h->mech->view, h->tr->view, static_cast<int>(h->n_pts), h->opt.source.pressure,
+                               h->tr_threshold, h->state + 1, n, h->state + 2, n, pr, st));
+    k_bd_from_props<<<grid_for(h->n_vals), 256, 0, st>>>(tb, S, h->p_rho, h->p_cp, h->p_lam, h->p_mu, h->p_rhoD,
+                                                          h->B, h->D);
+    if (!h->tr_cross) return EMBER_OK;
+    const int gp = grid_for(h->n_pts);
+    k_jcorr_fick<<<gp, 256, 0, st>>>(h->n_pts, n, S, h->pt_local, h->pt_flame, h->flame_npts, h->x, h->state,
+                                      h->p_rhoD, h->p_lam, h->p_rho, h->p_cp, h->jcorr, h->jB);
+    k_jcorr_h<<<blocks_for(h->n_flames, 64), 64, 0, st>>>(h->n_flames, h->flame_goff, h->flame_npts, h->x, h->jB,
+                                                           h->opt.dt_multiplier, h->opt.dt, h->jh);
+    DiffusionView jv{};
+    jv.n_systems = h->n_flames;
+    jv.info = h->jinfo;
+    jv.x = h->x;
+    jv.B = h->jB;
+    jv.D = h->jD;
+    jv.split_const = h->jsc;
+    jv.h = h->jh;
+    jv.status = h->jstatus;
+    StageTime tm;
+    tm.t0 = 0.0;
+    tm.t1 = h->opt.dt;
+    EMBER_TRY(diffusion_serial_run(jv, h->jcorr, h->jwork, h->n_pts, h->nmax, tm, h->opt.dt_multiplier, h->opt.dt, st));
+    k_count_failures<<<blocks_for(h->n_flames, 256), 256, 0, st>>>(h->n_flames, h->jstatus, h->fails + 1);
+    k_cross_species<<<gp, 256, 0, st>>>(h->n_pts, n, S, h->pt_local, h->pt_flame, h->flame_npts, h->d_grids, h->x,
+                                         h->state, h->p_rhoD, h->p_cpS, h->mech->view.W, h->p_rho, h->jcorr,
+                                         h->sumcpj, h->ddt_cross);
+    k_cross_temperature<<<gp, 256, 0, st>>>(h->n_pts, n, h->pt_local, h->pt_flame, h->flame_npts, h->x, h->state,
+                                             h->p_rho, h->p_cp, h->sumcpj, h->ddt_cross);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
 // One split step, enqueued on `st` (kernel launches and device copies only).
 // What a taped step (the forward pass of ember_split_adjoint) keeps.
 struct StepTape {
@@ -484,6 +677,7 @@ int enqueue_step(ember_split h, cudaStream_t st, const StepTape* tape = nullptr)
     const SplitTables tb = h->tables();
     const int g = grid_for(h->n_vals);
     if (tape) EMBER_CUDA_TRY(cudaMemcpyAsync(tape->t_saved, h->t_dev, sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (h->tr) EMBER_TRY(enqueue_properties(h, st));
     k_split_begin<<<g, 256, 0, st>>>(tb, h->opt.balanced, h->ddt_diff, h->ddt_prod, h->ddt_cross, h->sc_diff,
                                      h->sc_diff_vm, h->sc_prod, h->delta_vm);
     // diffusion 1/4 and 2/4
@@ -526,6 +720,7 @@ void free_split(ember_split h) {
     if (h->graph) cudaGraphDestroy(h->graph);
     if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     cudaFree(h->blob);
+    cudaFree(h->pblob);
     delete h;
 }
 
@@ -723,6 +918,88 @@ extern "C" int ember_split_set_transport(ember_split h, const double* B, const d
     return finish_call(mem, st);
 }
 
+extern "C" int ember_split_set_transport_model(ember_split h, ember_transport tr, double threshold,
+                                               int cross_terms) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(!tr || tr->mech == h->mech, "the transport model belongs to another mechanism");
+    EMBER_CHECK_ARG(threshold >= 0 && threshold < 1, "threshold must be in [0, 1)");
+    EMBER_TRY(ensure_device());
+    // the captured graph (if any) has the old stage list
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->graph_exec = nullptr;
+    h->graph = nullptr;
+    EMBER_CUDA_TRY(cudaDeviceSynchronize());
+    cudaFree(h->pblob);
+    h->pblob = nullptr;
+    h->tr = nullptr;
+    if (!tr) return EMBER_OK;
+    const int64_t np = h->n_pts;
+    const int S = h->n_vars - 2, nf = h->n_flames;
+    auto bd = [](size_t c) { return Scratch::rounded(c * sizeof(double)); };
+    const size_t total = 4 * bd(np) + 2 * bd(size_t(np) * S) + 6 * bd(np) + bd(7 * size_t(np)) +
+                         Scratch::rounded(sizeof(DiffSysInfo) * nf) + Scratch::rounded(sizeof(ember_diffusion_grid) * nf) +
+                         Scratch::rounded(sizeof(int) * nf) + 2 * Scratch::rounded(sizeof(int) * np);
+    EMBER_CUDA_TRY(cudaMalloc(&h->pblob, total));
+    int rc = EMBER_OK;
+    {
+        Scratch a(nullptr, h->pblob, total);
+        auto carve = [&](auto** p, size_t c) {
+            if (rc == EMBER_OK) rc = a.alloc(p, c);
+        };
+        carve(&h->p_rho, np);
+        carve(&h->p_cp, np);
+        carve(&h->p_lam, np);
+        carve(&h->p_mu, np);
+        carve(&h->p_rhoD, size_t(np) * S);
+        carve(&h->p_cpS, size_t(np) * S);
+        carve(&h->jcorr, np);
+        carve(&h->jB, np);
+        carve(&h->jD, np);
+        carve(&h->jsc, np);
+        carve(&h->jh, np);
+        carve(&h->sumcpj, np);
+        carve(&h->jwork, 7 * size_t(np));
+        carve(&h->jinfo, nf);
+        carve(&h->d_grids, nf);
+        carve(&h->jstatus, nf);
+        carve(&h->pt_local, np);
+        carve(&h->pt_flame, np);
+    }
+    if (rc != EMBER_OK) return rc;
+    std::vector<DiffSysInfo> ji(nf);
+    std::vector<int> loc(np), fl(np);
+    std::vector<double> ones(np, 1.0);
+    for (int f = 0; f < nf; ++f) {
+        const ember_diffusion_grid& g = h->grids[f];
+        ji[f].off = h->h_goff[f];
+        ji[f].grid_off = h->h_goff[f];
+        ji[f].n = g.n_points;
+        ji[f].left_bc = g.left_bc;
+        ji[f].right_bc = g.right_bc;
+        ji[f].alpha = g.alpha;
+        for (int i = 0; i < g.n_points; ++i) {
+            loc[h->h_goff[f] + i] = i;
+            fl[h->h_goff[f] + i] = f;
+        }
+    }
+    cudaError_t e = cudaMemcpy(h->jinfo, ji.data(), sizeof(DiffSysInfo) * nf, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_grids, h->grids.data(), sizeof(ember_diffusion_grid) * nf,
+                                         cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->pt_local, loc.data(), sizeof(int) * np, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->pt_flame, fl.data(), sizeof(int) * np, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->jD, ones.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(h->jsc, 0, sizeof(double) * np);
+    if (e != cudaSuccess) {
+        set_error("ember_split_set_transport_model: %s", cudaGetErrorString(e));
+        return EMBER_ECUDA;
+    }
+    h->tr = tr;
+    h->tr_threshold = threshold;
+    h->tr_cross = cross_terms != 0;
+    return EMBER_OK;
+}
+
 extern "C" int ember_split_step(ember_split h, int n_steps, int use_graph, void* stream) {
     EMBER_TRY(check_split(h));
     EMBER_CHECK_ARG(n_steps >= 0, "n_steps must be >= 0");
@@ -846,6 +1123,7 @@ extern "C" int ember_split_adjoint(ember_split h, const double* w_heat_release, 
                                    double* lnk_bar, int mem, void* stream) {
     EMBER_TRY(check_split(h));
     EMBER_CHECK_ARG(h->opt.method == EMBER_SOURCE_BDF, "the split-step adjoint needs EMBER_SOURCE_BDF");
+    EMBER_CHECK_ARG(h->tr == nullptr, "the split-step adjoint holds B and D fixed: detach the transport model");
     EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
     EMBER_CHECK_ARG(w_heat_release || w_consumption_speed, "no objective weights");
     EMBER_CHECK_ARG(!w_consumption_speed || (rho_u && ju && jb), "consumption speed needs rho_u, ju and jb");

@@ -31,23 +31,9 @@
 
 #include "common.cuh"
 #include "source.cuh"
+#include "transport.cuh"
 
 namespace ember {
-
-constexpr double kMoleFractionFloor = 1e-20;  // Cantera's Tiny in MixTransport::update_C
-
-struct TransportView {
-    int S;
-    const double* visc;  // [S][5]
-    const double* cond;  // [S][5]
-    const double* diff;  // [P][5], P = S(S+1)/2
-    const double* w4;    // [P] (W_lo / W_hi)^(1/4)
-    const double* s8w1;  // [P] sqrt(8) * sqrt(1 + W_hi / W_lo)
-};
-
-__host__ __device__ inline int64_t pair_index(int S, int lo, int hi) {
-    return int64_t(lo) * S - int64_t(lo) * (lo - 1) / 2 + (hi - lo);
-}
 
 __device__ __forceinline__ double fit5(const double* c, double x1, double x2, double x3, double x4) {
     double r = c[0];
@@ -59,12 +45,6 @@ __device__ __forceinline__ double fit5(const double* c, double x1, double x2, do
 }
 
 }  // namespace ember
-
-struct ember_transport_s {
-    ember_mech mech = nullptr;
-    void* blob = nullptr;
-    ember::TransportView view{};
-};
 
 namespace ember {
 namespace {
@@ -86,7 +66,8 @@ __device__ __forceinline__ double wilke_phi(const TransportView& tv, const doubl
 
 template <int NT>
 __global__ void __launch_bounds__(NT) k_transport(MechView m, TransportView tv, int n, double p, double thr,
-                                                 const double* __restrict__ Tin, const double* __restrict__ Yin,
+                                                 const double* __restrict__ Tin, int64_t tstride,
+                                                 const double* __restrict__ Yin, int64_t ystride,
                                                  ember_properties out) {
     extern __shared__ double sm[];
     const int S = m.S;
@@ -101,8 +82,8 @@ __global__ void __launch_bounds__(NT) k_transport(MechView m, TransportView tv, 
     double* sk = lam + S;
     double* red = sk + S;
     for (int j = blockIdx.x; j < n; j += gridDim.x) {
-        const double T = Tin[j];
-        for (int k = t; k < S; k += NT) y[k] = Yin[size_t(j) * S + k];
+        const double T = Tin[j * tstride];
+        for (int k = t; k < S; k += NT) y[k] = Yin[j * ystride + k];
         const double lnT = em_log(T), rT = 1.0 / T;
         const double RT = kGasConstant * T;
         const double sqT = sqrt(T), t14 = sqrt(sqT), t15 = T * sqT;
@@ -178,7 +159,8 @@ __global__ void __launch_bounds__(NT) k_transport(MechView m, TransportView tv, 
 
 template <int NT>
 int launch_transport_nt(const MechView& m, const TransportView& tv, int n, double p, double thr, const double* T,
-                        const double* Y, const ember_properties& out, cudaStream_t st) {
+                        int64_t tstride, const double* Y, int64_t ystride, const ember_properties& out,
+                        cudaStream_t st) {
     const size_t smem = (size_t(8) * m.S + kRedDoubles) * sizeof(double);
     EMBER_CHECK_ARG(smem <= 227 * 1024, "too many species for the transport work area");
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_transport<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
@@ -187,7 +169,7 @@ int launch_transport_nt(const MechView& m, const TransportView& tv, int n, doubl
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     EMBER_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_transport<NT>, NT, smem));
     const int blocks = std::max(1, std::min(n, sms * std::max(per_sm, 1)));
-    k_transport<NT><<<blocks, NT, smem, st>>>(m, tv, n, p, thr, T, Y, out);
+    k_transport<NT><<<blocks, NT, smem, st>>>(m, tv, n, p, thr, T, tstride, Y, ystride, out);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }
@@ -195,12 +177,12 @@ int launch_transport_nt(const MechView& m, const TransportView& tv, int n, doubl
 }  // namespace
 
 int launch_transport(const MechView& m, const TransportView& tv, int n, double p, double thr, const double* T,
-                     const double* Y, const ember_properties& out, cudaStream_t st) {
+                     int64_t tstride, const double* Y, int64_t ystride, const ember_properties& out, cudaStream_t st) {
     switch (chem_threads_for(m.S)) {
-        case 64: return launch_transport_nt<64>(m, tv, n, p, thr, T, Y, out, st);
-        case 128: return launch_transport_nt<128>(m, tv, n, p, thr, T, Y, out, st);
-        case 160: return launch_transport_nt<160>(m, tv, n, p, thr, T, Y, out, st);
-        default: return launch_transport_nt<256>(m, tv, n, p, thr, T, Y, out, st);
+        case 64: return launch_transport_nt<64>(m, tv, n, p, thr, T, tstride, Y, ystride, out, st);
+        case 128: return launch_transport_nt<128>(m, tv, n, p, thr, T, tstride, Y, ystride, out, st);
+        case 160: return launch_transport_nt<160>(m, tv, n, p, thr, T, tstride, Y, ystride, out, st);
+        default: return launch_transport_nt<256>(m, tv, n, p, thr, T, tstride, Y, ystride, out, st);
     }
 }
 
@@ -291,7 +273,7 @@ extern "C" int ember_transport_eval(ember_transport tr, int n, double pressure, 
     EMBER_TRY(stage_buffer(sc, out->conductivity, n, mem, &d.conductivity));
     EMBER_TRY(stage_buffer(sc, out->viscosity, n, mem, &d.viscosity));
     EMBER_TRY(stage_buffer(sc, out->rho_d, size_t(n) * S, mem, &d.rho_d));
-    EMBER_TRY(launch_transport(tr->mech->view, tr->view, n, pressure, threshold, dT, dY, d, st));
+    EMBER_TRY(launch_transport(tr->mech->view, tr->view, n, pressure, threshold, dT, 1, dY, S, d, st));
     EMBER_TRY(stage_out(out->density, d.density, n, mem, st));
     EMBER_TRY(stage_out(out->mean_mol_weight, d.mean_mol_weight, n, mem, st));
     EMBER_TRY(stage_out(out->cp_mass, d.cp_mass, n, mem, st));

@@ -104,6 +104,17 @@ def tridiag_flops_per_point() -> float:
     return 12.0 + 5.0 + 8 * 7.0
 
 
+def transport_point_flops(n_species: int, cross_terms: bool = True) -> float:
+    """Thermo, "Approx" transport and cross terms of one grid point
+    (ember_transport_eval / the split step's property update), every species
+    major: per species the NASA7 cp and h (~20) and three fits (3 x 11); per
+    species pair the Wilke term (~10) and the binary diffusion fit plus the
+    two sums of the mixture coefficient (~15); the cross terms ~20 per
+    species (Fick flux twice, species and heat-capacity terms)."""
+    S = float(n_species)
+    return 53.0 * S + 10.0 * S * S + 15.0 * S * (S - 1.0) + (20.0 * S if cross_terms else 0.0)
+
+
 def tridiag_bytes_per_point() -> float:
     """B, D, split constant and y read, y written (8 bytes each)."""
     return 40.0

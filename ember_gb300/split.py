@@ -125,6 +125,15 @@ class FlameBatchSplitSolver:
         L.check(_lib().ember_split_set_transport(self._h, L.ptr(b), L.ptr(d), L.ptr(x), mem, L.stream_ptr(stream)),
                 "ember_split_set_transport")
 
+    def set_transport_model(self, transport=None, threshold: float = 1e-5, cross_terms: bool = True):
+        """ember_split_set_transport_model: B, D (and with cross_terms the
+        cross terms) from a GpuTransport at the start of every step; None
+        detaches."""
+        self._transport = transport  # keeps the handle alive
+        L.check(_lib().ember_split_set_transport_model(self._h, transport.handle if transport is not None else None,
+                                                       float(threshold), int(bool(cross_terms))),
+                "ember_split_set_transport_model")
+
     def step(self, n_steps: int = 1, graph: bool = False, stream=None):
         L.check(_lib().ember_split_step(self._h, int(n_steps), int(bool(graph)), L.stream_ptr(stream)),
                 "ember_split_step")

@@ -504,6 +504,22 @@ int ember_split_set_state(ember_split split, double t, const double* state, int 
 /* B, D: variable-major per flame; ddt_cross: point-major or NULL (zero). */
 int ember_split_set_transport(ember_split split, const double* B, const double* D, const double* ddt_cross,
                               int mem, void* stream);
+/* Attach a transport model (NULL detaches): every following step starts as
+ * FlameSolver::step does (src/flameSolver.cpp:130-154, 156-172, 551-617),
+ * from the state at the step start and on the device:
+ *   updateChemicalProperties  ember_transport_eval with `threshold`;
+ *   prepareIntegrators        B, D of every variable (1/rho and mu for U,
+ *                             1/(rho cp) and lambda for T, 1/rho and rho D_k
+ *                             for Y_k), replacing ember_split_set_transport's;
+ *   updateCrossTerms          (cross_terms != 0) Fick fluxes, the correction
+ *                             flux smoothed by a tridiagonal integration over
+ *                             [0, dt] (B = lambda/(rho cp), D = 1, the jCorr
+ *                             step-size rule), the species and temperature
+ *                             cross terms into ddt_cross. Thermal diffusion
+ *                             (Soret) is not included.
+ * The properties are part of the captured graph. The split-step adjoint holds
+ * B and D fixed and so requires no transport model. */
+int ember_split_set_transport_model(ember_split split, ember_transport tr, double threshold, int cross_terms);
 /* n_steps split steps, asynchronous on `stream`. */
 int ember_split_step(ember_split split, int n_steps, int use_graph, void* stream);
 int ember_split_get_state(ember_split split, double* state, double* t, int mem, void* stream);

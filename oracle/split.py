@@ -36,11 +36,99 @@ def correct_mass_fractions(state):
     state[:, 2:] = Yc * r[:, None]
 
 
+def step_properties(omech, tdata, grids, state, pressure, threshold, mult, gdt, cross_terms):
+    """Start of FlameSolver::step for a batch of flames: updateChemicalProperties
+    (src/flameSolver.cpp:652-699, thermo and "Approx" transport from
+    oracle_transport.c), prepareIntegrators' diffusion coefficients
+    (src/flameSolver.cpp:156-172: B = 1/rho, D = mu for U; 1/(rho cp), lambda
+    for T; 1/rho, rho D_k for Y_k) and, with cross_terms, updateCrossTerms
+    (src/flameSolver.cpp:551-617) without thermal diffusion: Fick fluxes,
+    the correction flux jCorr smoothed by a tridiagonal integration with
+    B = lambda/(rho cp), D = 1 over [0, globalTimestep], and the species and
+    temperature cross terms. Returns (B, D, ddt_cross) in the layouts of
+    split_steps."""
+    from oracle import chem
+    n_pts, n = state.shape
+    S = n - 2
+    props = chem.transport_eval(omech, tdata, state[:, 1], state[:, 2:], pressure, threshold)
+    rho, cp, lam, mu = props["density"], props["cp_mass"], props["conductivity"], props["viscosity"]
+    rhoD, cpS = props["rho_d"], props["cp_species"]
+    W = [float(w) for w in omech.mech.mol_weight]
+    offs = np.cumsum([0] + [g.n_points for g in grids])
+    B = np.empty(n_pts * n)
+    D = np.empty(n_pts * n)
+    for f in range(len(grids)):
+        a, b = offs[f], offs[f + 1]
+        N = b - a
+        base = a * n
+        B[base:base + N] = 1.0 / rho[a:b]
+        D[base:base + N] = mu[a:b]
+        B[base + N:base + 2 * N] = 1.0 / (rho[a:b] * cp[a:b])
+        D[base + N:base + 2 * N] = lam[a:b]
+        for k in range(S):
+            B[base + (2 + k) * N:base + (3 + k) * N] = 1.0 / rho[a:b]
+            D[base + (2 + k) * N:base + (3 + k) * N] = rhoD[a:b, k]
+    cross = np.zeros((n_pts, n))
+    if not cross_terms:
+        return B, D, cross
+    for f, g in enumerate(grids):
+        a, b = offs[f], offs[f + 1]
+        N = b - a
+        x = [float(v) for v in g.x]
+        Y = state[a:b, 2:]
+        T = state[a:b, 1]
+        rd = rhoD[a:b]
+        jc = [0.0] * N
+        for i in range(N - 1):
+            hh = x[i + 1] - x[i]
+            s = 0.0
+            for k in range(S):
+                F = (-0.5 * (rd[i, k] + rd[i + 1, k])) * ((Y[i + 1, k] - Y[i, k]) / hh)
+                s = s - F
+            jc[i] = s
+        jB = lam[a:b] / (rho[a:b] * cp[a:b])
+        h = gdt
+        for i in range(1, N - 1):
+            dlj = 0.5 * (x[i + 1] - x[i - 1])
+            cand = ((mult * dlj) * dlj) / jB[i]
+            h = cand if cand < h else h
+        jc = oracle.diffusion_system(g.x, jB, np.ones(N), np.array(jc), 0.0, gdt, split_const=np.zeros(N),
+                                     alpha=g.alpha, left_bc=g.left_bc, right_bc=g.right_bc, h=h, mult=mult, gdt=gdt)
+        jc = [float(v) for v in jc]
+        sumcpj = [0.0] * N
+        for i in range(1, N - 1):
+            r = x[i] ** g.alpha
+            rph = (0.5 * (x[i] + x[i + 1])) ** g.alpha
+            rphm = (0.5 * (x[i - 1] + x[i])) ** g.alpha
+            dlj = 0.5 * (x[i + 1] - x[i - 1])
+            hh = x[i + 1] - x[i]
+            c = -0.5 / ((r * float(rho[a + i])) * dlj)
+            s = 0.0
+            for k in range(S):
+                yk, yk1, ykm = float(Y[i, k]), float(Y[i + 1, k]), float(Y[i - 1, k])
+                cross[a + i, 2 + k] = c * ((rph * (yk + yk1)) * jc[i] - (rphm * (ykm + yk)) * jc[i - 1])
+                F = (-0.5 * (float(rd[i, k]) + float(rd[i + 1, k]))) * ((yk1 - yk) / hh)
+                s = s + ((0.5 * (float(cpS[a + i, k]) + float(cpS[a + i + 1, k]))) / W[k]) * (
+                    F + ((0.5 * (yk + yk1)) * jc[i]))
+            sumcpj[i] = s
+        for i in range(1, N - 1):
+            hh, hm = x[i + 1] - x[i], x[i] - x[i - 1]
+            cfp = hm / (hh * (hh + hm))
+            cf = (hh - hm) / (hh * hm)
+            cfm = -hh / (hm * (hh + hm))
+            dTdx = (cfm * float(T[i - 1]) + cf * float(T[i])) + cfp * float(T[i + 1])
+            cross[a + i, 1] = ((-0.5 * (sumcpj[i] + sumcpj[i - 1])) * dTdx) / (float(cp[a + i]) * float(rho[a + i]))
+    return B, D, cross
+
+
 def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cross=None, balanced=True,
-                mult=10.0, ddt=None):
+                mult=10.0, ddt=None, transport=None):
     """n_steps split steps of a batch of flames. state: point-major [n_pts, n]
-    (copied); B, D: variable-major per flame (flat). Returns (state, t,
-    ddt_diff, ddt_prod, source_status_of_last_step)."""
+    (copied); B, D: variable-major per flame (flat). transport: None, or
+    (TransportData, threshold, cross_terms): B, D (and the cross terms) are
+    then recomputed from the state at the start of every step
+    (step_properties). Returns (state, t, ddt_diff, ddt_prod,
+    source_status_of_last_step)."""
     state = np.array(state, dtype=np.float64, copy=True)
     n_pts, n = state.shape
     offs = np.cumsum([0] + [g.n_points for g in grids])
@@ -51,6 +139,11 @@ def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cro
     ddt_prod = np.zeros_like(state) if ddt is None else ddt[1].copy()
     status = None
     for _ in range(n_steps):
+        if transport is not None:
+            tdata, thr, with_cross = transport
+            B, D, c = step_properties(omech, tdata, grids, state, opts.pressure, thr, mult, dt, with_cross)
+            if with_cross:
+                cross = c
         if balanced:
             sc_diff = 0.5 * ((ddt_prod + cross) - ddt_diff)
             sc_prod = 0.5 * ((ddt_diff + cross) - ddt_prod)

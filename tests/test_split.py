@@ -128,3 +128,101 @@ def test_split_objectives_bitwise_vs_oracle(gpu_lib, mech):
     assert np.array_equal(q, rq)
     assert np.array_equal(hr, rhr) and np.array_equal(cs, rcs)
     assert (hr != 0).all()
+
+
+def _cross_numpy(om, td, grids, state, pressure, thr, mult, gdt):
+    """Vectorised restatement of updateCrossTerms (src/flameSolver.cpp:551-617,
+    no thermal diffusion) for checking oracle/split.py's loops."""
+    import oracle
+    from oracle import chem
+    props = chem.transport_eval(om, td, state[:, 1], state[:, 2:], pressure, thr)
+    n_pts, n = state.shape
+    cross = np.zeros((n_pts, n))
+    offs = np.cumsum([0] + [g.n_points for g in grids])
+    W = om.mech.mol_weight
+    for f, g in enumerate(grids):
+        a, b = offs[f], offs[f + 1]
+        N = b - a
+        x = np.asarray(g.x, float)
+        Y = state[a:b, 2:]
+        T = state[a:b, 1]
+        rd = props["rho_d"][a:b]
+        cs = props["cp_species"][a:b]
+        rho, cp, lam = props["density"][a:b], props["cp_mass"][a:b], props["conductivity"][a:b]
+        hh = np.diff(x)
+        jF = -0.5 * (rd[:-1] + rd[1:]) * (np.diff(Y, axis=0) / hh[:, None])
+        jc = np.append(-jF.sum(axis=1), 0.0)
+        jB = lam / (rho * cp)
+        dlj = 0.5 * (x[2:] - x[:-2])
+        h = min(gdt, (mult * dlj * dlj / jB[1:-1]).min())
+        jc = oracle.diffusion_system(x, jB, np.ones(N), jc, 0.0, gdt, split_const=np.zeros(N), alpha=g.alpha,
+                                     left_bc=g.left_bc, right_bc=g.right_bc, h=h, mult=mult, gdt=gdt)
+        r = x ** g.alpha
+        rph = (0.5 * (x[:-1] + x[1:])) ** g.alpha
+        i = np.arange(1, N - 1)
+        c = -0.5 / (r[i] * rho[i] * dlj)
+        dY = c[:, None] * (rph[i, None] * (Y[i] + Y[i + 1]) * jc[i, None]
+                           - rph[i - 1, None] * (Y[i - 1] + Y[i]) * jc[i - 1, None])
+        cross[a + 1:b - 1, 2:] = dY
+        s = np.zeros(N)
+        s[i] = (0.5 * (cs[i] + cs[i + 1]) / W * (jF[i] + 0.5 * (Y[i] + Y[i + 1]) * jc[i, None])).sum(axis=1)
+        hm = hh[:-1]
+        hp = hh[1:]
+        dTdx = (-hp / (hm * (hp + hm))) * T[:-2] + ((hp - hm) / (hp * hm)) * T[1:-1] + (hm / (hp * (hp + hm))) * T[2:]
+        cross[a + 1:b - 1, 1] = -0.5 * (s[i] + s[i - 1]) * dTdx / (cp[i] * rho[i])
+    return props, cross
+
+
+def test_oracle_step_properties_match_vectorised_restatement(mech):
+    from oracle.chem import OracleMech
+    from ember_gb300.transport import synthetic_transport
+    om = OracleMech(mech)
+    td = synthetic_transport(mech, seed=4)
+    grids, state, B, D, rho_u, ju, jb = _case(mech, n_flames=2, n_min=12, n_max=20)
+    Bo, Do, co = osplit.step_properties(om, td, grids, state, 101325.0, 1e-5, 10.0, 2e-6, True)
+    props, cr = _cross_numpy(om, td, grids, state, 101325.0, 1e-5, 10.0, 2e-6)
+    scale = np.abs(cr).max(axis=0)
+    np.testing.assert_allclose(co, cr, rtol=0, atol=1e-10 * scale.max())
+    assert np.abs(co[:, 2:]).max() > 0 and np.abs(co[:, 1]).max() > 0
+    assert (co[:, 0] == 0).all()
+    # B, D of the first flame's T and Y_0 rows
+    N = grids[0].n_points
+    np.testing.assert_array_equal(Bo[N:2 * N], 1.0 / (props["density"][:N] * props["cp_mass"][:N]))
+    np.testing.assert_array_equal(Do[2 * N:3 * N], props["rho_d"][:N, 0])
+    # a spatially uniform state has no cross terms
+    uni = np.repeat(state[N // 2][None, :], N, axis=0)
+    _, _, cu = osplit.step_properties(om, td, grids[:1], uni, 101325.0, 1e-5, 10.0, 2e-6, True)
+    assert (cu == 0).all()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cross", [False, True])
+def test_split_transport_model_bitwise_vs_oracle(gpu_lib, mech, cross):
+    from oracle.chem import OracleMech
+    from ember_gb300.transport import GpuTransport, synthetic_transport
+    td = synthetic_transport(mech, seed=4)
+    grids, state, B, D, rho_u, ju, jb = _case(mech, n_flames=2, n_min=10, n_max=16)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    dt = 2e-6
+    gm, s = _gpu_solver(mech, grids, dt, QSS, opts, L.DIFFUSION_SERIAL)
+    gt = GpuTransport(gm, td)
+    s.set_state(0.0, state)
+    s.set_transport(B * 0.0, D * 0.0)   # replaced by the model at every step
+    s.set_transport_model(gt, 1e-5, cross)
+    s.step(2)
+    out, t = s.state()
+    dd, dp = s.derivatives()
+    ref, rt, rdd, rdp, rst = osplit.split_steps(OracleMech(mech), grids, state, 0.0, B, D, dt, 2, QSS, opts,
+                                                transport=(td, 1e-5, cross))
+    assert t == rt
+    assert np.array_equal(out, ref), np.abs(out - ref).max()
+    assert np.array_equal(dd, rdd) and np.array_equal(dp, rdp)
+    assert s.failures()[1] == 0
+    # the captured graph replays the same step
+    gm2, s2 = _gpu_solver(mech, grids, dt, QSS, opts, L.DIFFUSION_SERIAL)
+    gt2 = GpuTransport(gm2, td)
+    s2.set_state(0.0, state)
+    s2.set_transport(B, D)
+    s2.set_transport_model(gt2, 1e-5, cross)
+    s2.step(2, graph=True)
+    assert np.array_equal(s2.state()[0], out)
