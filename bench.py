@@ -52,6 +52,9 @@ def parse_args():
     p.add_argument("--kinetics", default="interp", choices=["interp", "standard"])
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--mech", default="150", choices=["150", "53"],
+                   help="source workloads: the 150-species/1000-reaction mechanism or the GRI-3.0-sized "
+                        "53-species/325-reaction one")
     p.add_argument("--threads", type=int, default=0,
                    help="QSS threads per point; 0: ember_source_autotune picks it before the timed region")
     return p.parse_args()
@@ -118,9 +121,12 @@ def dist_info():
     return ws, rank, local
 
 
-def workload_inputs(n_points: int, rank: int):
+def workload_inputs(n_points: int, rank: int, mech_size: str = "150"):
     from ember_gb300.mechanism import synthetic_mechanism, reactor_states
-    mech = synthetic_mechanism(seed=MECH_SEED)
+    if mech_size == "53":
+        mech = synthetic_mechanism(n_species=53, n_reactions=325, seed=53325)
+    else:
+        mech = synthetic_mechanism(seed=MECH_SEED)
     state, dt = reactor_states(mech, n_points, seed=STATE_SEED + rank)
     return mech, state, dt
 
@@ -158,7 +164,7 @@ def run_reference(args):
         return 0
     from oracle import chem
     method = chem.QSS if args.workload == "qss" else chem.BDF
-    mech, state, dt = workload_inputs(args.points, 0)
+    mech, state, dt = workload_inputs(args.points, 0, args.mech)
     opts = source_options(args.kinetics, args.workload)
     threads = os.cpu_count() or 1
     om = chem.OracleMech(mech)
@@ -178,7 +184,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"C2 isolated source-term step, {args.workload.upper()}, {args.kinetics} kinetics, "
-                               f"synthetic 150-species/1000-reaction mechanism, {args.points} seeded states",
+                               f"synthetic {mech.n_species}-species/{mech.n_reactions}-reaction mechanism, {args.points} seeded states",
                    "sample_points_per_step": n},
         "cpu_baseline": {"value": value, "unit": "points/s", "cores": threads, "kind": "port",
                          "sample": f"{n} of the {args.points} states per step, all host threads"},
@@ -205,7 +211,7 @@ def run_ours(args):
 
     lib = _lib.lib()
     method = QSS if args.workload == "qss" else BDF
-    mech, state, dt = workload_inputs(args.points, rank)
+    mech, state, dt = workload_inputs(args.points, rank, args.mech)
     opts = source_options(args.kinetics, args.workload)
     gm = GpuMechanism(mech)
     dev = torch.device("cuda", local)
@@ -305,7 +311,7 @@ def run_ours(args):
     # DRAM bytes per launch from the ncu captures of the integration kernels
     # (150-species mechanism), scaled to this launch's points.
     per_point = roofline.QSS_DRAM_BYTES_PER_POINT if method == QSS else roofline.BDF_DRAM_BYTES_PER_POINT
-    traffic = per_point * args.points
+    traffic = per_point * args.points if args.mech == "150" else None
 
     line = {
         "metric": METRIC, "value": ws * args.points * args.steps / (total_ms / 1e3), "unit": "points/s",
@@ -313,7 +319,8 @@ def run_ours(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded mechanism and reactor states)",
         "config": {"workload": f"C2 isolated source-term step, {args.workload.upper()}, {args.kinetics} kinetics, "
-                               f"synthetic 150-species/1000-reaction mechanism, {args.points} seeded states per GPU",
+                               f"synthetic {mech.n_species}-species/{mech.n_reactions}-reaction mechanism, {args.points} seeded states "
+                               f"per GPU",
                    "points_per_gpu": args.points, "n_vars": mech.n_vars, "n_reactions": mech.n_reactions,
                    "l2": "256 MB buffer written between timed iterations", "parallelism": f"replicas x{ws}",
                    "failed_points": n_fail,
@@ -605,7 +612,8 @@ def run_ours_split(args):
     ms = total_ms / args.steps
     n_vals = state.size
     flops = (src_flops / args.steps + 4 * roofline.tridiag_flops_per_point() * n_vals
-             + roofline.transport_point_flops(mech.n_species) * len(state))
+             + float(np.sum(roofline.transport_point_flops(mech.n_species,
+                                                           major_counts(mech, state[:, 2:], SPLIT_THRESHOLD)))))
     achieved = flops / (ms / 1e3) / 1e12
     line = {
         "metric": SPLIT_METRIC, "value": ms, "unit": "ms", "n_gpus": ws, "steps": args.steps,
@@ -786,6 +794,15 @@ TRANSPORT_WORKLOAD = ("updateChemicalProperties of 16384 seeded states (the C2 s
                       "seeded kinetic-theory fits")
 
 
+def major_counts(mech, Y, threshold):
+    """Species per state whose mole fraction is at least the threshold."""
+    import numpy as np
+    y = np.maximum(np.asarray(Y, dtype=float), 0.0)
+    xw = y / mech.mol_weight[None, :]
+    X = xw / xw.sum(axis=1, keepdims=True)
+    return (np.maximum(X, 1e-20) >= threshold).sum(axis=1)
+
+
 def transport_inputs(rank: int):
     from ember_gb300.mechanism import reactor_states, synthetic_mechanism
     from ember_gb300.transport import synthetic_transport
@@ -880,7 +897,9 @@ def run_ours_transport(args):
     clocks = sampler.stop()
     ms = total_ms / args.steps
     n = TRANSPORT_POINTS
-    flops = roofline.transport_point_flops(mech.n_species, cross_terms=False) * n
+    flops = float(np.sum(roofline.transport_point_flops(mech.n_species, major_counts(mech, state[:, 2:],
+                                                                                     SPLIT_THRESHOLD),
+                                                         cross_terms=False)))
     achieved = flops / (ms / 1e3) / 1e12
     S = mech.n_species
     line = {
@@ -896,7 +915,7 @@ def run_ours_transport(args):
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / (peak.value / 1e12), "traffic": None,
                      "peak_source": "live DFMA throughput probe (ember_probe_fp64_rate)",
-                     "work_model": "roofline.transport_point_flops (all species major)"},
+                     "work_model": "roofline.transport_point_flops with each state's major-species count"},
         "clocks": clocks,
     }
     if rank == 0 and not args.no_cpu_baseline:

@@ -62,7 +62,9 @@ struct BdfSmem {
 
 template <int NT>
 struct BdfPoint {
-    MechView m;
+    // the kernel's __grid_constant__ parameter: read in place, never copied to the stack
+    const MechView& m;
+    __device__ explicit BdfPoint(const MechView& mv) : m(mv) {}
     ChemSmem w;
     BdfSmem v;
     const SourceArgs* a = nullptr;
@@ -842,14 +844,14 @@ __device__ int bdf_integrate(BdfPoint<NT>& P, double tf, double t_start, int* st
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT) k_source_bdf(MechView m, SourceArgs a, int* counter, const int* order,
+__global__ void __launch_bounds__(NT) k_source_bdf(const __grid_constant__ MechView m,
+                                                  const __grid_constant__ SourceArgs a, int* counter, const int* order,
                                                   double* kcache, double* jm, size_t jm_stride, int jm_mode) {
     extern __shared__ double smem[];
     __shared__ int next_point;
     const int n = m.S + 2;
-    BdfPoint<NT> P;
-    P.m = m;
-    bdf_carve(P, smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), jm + size_t(blockIdx.x) * jm_stride,
+    BdfPoint<NT> P(m);
+    bdf_carve(P, smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m), jm + size_t(blockIdx.x) * jm_stride,
               jm_mode);
     P.a = &a;
     P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
@@ -909,7 +911,7 @@ static int bdf_scratch_nt(const MechView& m, const SourceArgs& a, size_t* bytes)
     size_t per = 0;
     int blocks = 0;
     EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
-    *bytes = Scratch::rounded(sizeof(double) * size_t(blocks) * ChemSmem::global_doubles(m.R)) +
+    *bytes = Scratch::rounded(sizeof(double) * size_t(blocks) * ChemSmem::global_doubles(m)) +
              Scratch::rounded(sizeof(double) * size_t(blocks) * bdf_layout(m).global_doubles) +
              Scratch::rounded(sizeof(int) * 64) + Scratch::rounded(sizeof(int) * size_t(a.n));
     return EMBER_OK;
@@ -930,7 +932,7 @@ static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, S
     int blocks = 0;
     EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
     double *kcache = nullptr, *jm = nullptr;
-    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
+    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));
     const BdfLayout lay = bdf_layout(m);
     EMBER_TRY(sc.alloc(&jm, size_t(blocks) * lay.global_doubles));
     int* order = nullptr;
@@ -956,7 +958,9 @@ static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, S
 // transposed solve reuses the LU of I - gamma J. The gradient with respect to
 // ln(multiplier_i) of every reaction is accumulated per point.
 template <int NT>
-__global__ void __launch_bounds__(NT) k_source_bdf_adjoint(MechView m, SourceArgs a, int* counter, double* kcache,
+__global__ void __launch_bounds__(NT) k_source_bdf_adjoint(const __grid_constant__ MechView m,
+                                                          const __grid_constant__ SourceArgs a, int* counter,
+                                                          double* kcache,
                                                           double* jm, size_t jm_stride, int jm_mode,
                                                           const double* __restrict__ ybar_out,
                                                           double* __restrict__ ybar_in, double* __restrict__ pbar,
@@ -964,9 +968,8 @@ __global__ void __launch_bounds__(NT) k_source_bdf_adjoint(MechView m, SourceArg
     extern __shared__ double smem[];
     __shared__ int next_point;
     const int n = m.S + 2;
-    BdfPoint<NT> P;
-    P.m = m;
-    bdf_carve(P, smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), jm + size_t(blockIdx.x) * jm_stride,
+    BdfPoint<NT> P(m);
+    bdf_carve(P, smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m), jm + size_t(blockIdx.x) * jm_stride,
               jm_mode);
     P.a = &a;
     P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
@@ -1112,7 +1115,7 @@ static int launch_bdf_adjoint_nt(const MechView& m, const SourceArgs& a, int* co
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_bdf_adjoint<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         int(per)));
     double *kcache = nullptr, *jm = nullptr;
-    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
+    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));
     const BdfLayout lay = bdf_layout(m);
     EMBER_TRY(sc.alloc(&jm, size_t(blocks) * lay.global_doubles));
     k_source_bdf_adjoint<NT><<<blocks, NT, per, st>>>(m, a, counter, kcache, jm, lay.global_doubles, lay.mode,
@@ -1131,7 +1134,8 @@ static int launch_bdf_adjoint_nt(const MechView& m, const SourceArgs& a, int* co
 // Y_k cp_k/(R W_k); then the normalisation Y/sum(Y) is projected out. Also
 // d psi / d ln(multiplier_i) = gq * (-sum_k nu_ki h_k) r_i, per point.
 template <int NT>
-__global__ void __launch_bounds__(NT) k_objective_vjp(MechView m, SourceArgs a, int n_pts,
+__global__ void __launch_bounds__(NT) k_objective_vjp(const __grid_constant__ MechView m,
+                                                     const __grid_constant__ SourceArgs a, int n_pts,
                                                      const double* __restrict__ state, const double* __restrict__ gq,
                                                      const double* __restrict__ gcp, const double* __restrict__ gT,
                                                      int* counter, double* kcache, double* jm, size_t jm_stride, int jm_mode,
@@ -1139,9 +1143,8 @@ __global__ void __launch_bounds__(NT) k_objective_vjp(MechView m, SourceArgs a, 
     extern __shared__ double smem[];
     __shared__ int next_point;
     const int n = m.S + 2;
-    BdfPoint<NT> P;
-    P.m = m;
-    bdf_carve(P, smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), jm + size_t(blockIdx.x) * jm_stride,
+    BdfPoint<NT> P(m);
+    bdf_carve(P, smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m), jm + size_t(blockIdx.x) * jm_stride,
               jm_mode);
     P.a = &a;
     P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
@@ -1236,7 +1239,7 @@ static int launch_objective_vjp_nt(const MechView& m, const SourceArgs& a, int n
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_objective_vjp<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
     double *kcache = nullptr, *jm = nullptr;
     int* counter = nullptr;
-    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
+    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));
     const BdfLayout lay = bdf_layout(m);
     EMBER_TRY(sc.alloc(&jm, size_t(blocks) * lay.global_doubles));
     EMBER_TRY(sc.alloc(&counter, 1));

@@ -102,10 +102,9 @@ __device__ __forceinline__ int rinfo_tbslot(int r) { return (r >> 9) & 0x3fffff;
 // temperature-only per-reaction values in global memory.
 struct ChemSmem {
     double* c;     // [S] concentrations
-    double* ym;    // [S]
+    double* ym;    // [S] Y_k / W_k of the composition (chem_rates only)
     double* cpR;   // [S]
-    double* hRT;   // [S]
-    double* gRT;   // [S]
+    double* gRT;   // [S] g/RT of the temperature pass; shares ym's storage (used only before chem_rates)
     double* wq;    // [S] creation
     double* wd;    // [S] destruction
     double* wn;    // [S] net (only when the caller wants it; may alias wd otherwise)
@@ -113,10 +112,10 @@ struct ChemSmem {
     double* ropf;  // [R] (shared memory, or global when the point's matrices take the shared memory)
     double* ropr;  // [R]
     double* concm; // [n_tb]
-    double* fo_kinf;  // [n_fo]
-    double* fo_rkinf; // [n_fo] 1/(kinf + 1e-300)
-    double* fo_k0;    // [n_fo]
-    double* fo_lfc;   // [n_fo] log10 Fcent (Troe)
+    double* fo_kinf;  // global [n_fo]
+    double* fo_rkinf; // global [n_fo] 1/(kinf + 1e-300)
+    double* fo_k0;    // global [n_fo]
+    double* fo_lfc;   // global [n_fo] log10 Fcent (Troe)
     double* red;      // [kRedDoubles] reduction scratch
     double* fo_F;     // [n_fo] falloff F of the last composition (only when set; for Jacobians)
     double* fo_pr;    // [n_fo] reduced pressure Pr of the last composition (idem)
@@ -128,20 +127,21 @@ struct ChemSmem {
     // shared-memory doubles (with_net: a separate wn array; rop_smem: ropf and
     // ropr in shared memory)
     static __host__ __device__ size_t doubles(int S, int R, int n_tb, int n_fo, bool with_net, bool rop_smem = true) {
-        return size_t(with_net ? 9 : 8) * S + (rop_smem ? size_t(2) * R : 0) + n_tb + size_t(4) * n_fo + kRedDoubles;
+        (void)n_fo;
+        return size_t(with_net ? 7 : 6) * S + (rop_smem ? size_t(2) * R : 0) + n_tb + kRedDoubles;
     }
-    // global doubles per point slot
-    static __host__ __device__ size_t global_doubles(int R) { return size_t(2) * R; }
+    // global doubles per CTA slot: the temperature-only per-reaction values
+    static __host__ __device__ size_t global_doubles(int R, int n_fo) { return size_t(2) * R + size_t(4) * n_fo; }
+    static __host__ __device__ size_t global_doubles(const MechView& m) { return global_doubles(m.R, m.n_fo); }
 
     // rop_global: 2R doubles of global memory for ropf/ropr, or null (shared memory)
     __device__ void carve(double* base, double* gbase, const MechView& m, bool with_net, double* rop_global = nullptr) {
         const int S = m.S, R = m.R;
         c = base;
         ym = c + S;
+        gRT = ym;
         cpR = ym + S;
-        hRT = cpR + S;
-        gRT = hRT + S;
-        wq = gRT + S;
+        wq = cpR + S;
         wd = wq + S;
         hk = wd + S;
         wn = with_net ? hk + S : wd;
@@ -155,17 +155,17 @@ struct ChemSmem {
             p += 2 * R;
         }
         concm = p;
-        fo_kinf = concm + m.n_tb;
-        fo_rkinf = fo_kinf + m.n_fo;
-        fo_k0 = fo_rkinf + m.n_fo;
-        fo_lfc = fo_k0 + m.n_fo;
-        red = fo_lfc + m.n_fo;
+        red = concm + m.n_tb;
         fo_F = nullptr;
         fo_pr = nullptr;
         fo_dF = nullptr;
         mmw = 0.0;
         kfm = gbase;
         rkc = gbase + R;
+        fo_kinf = rkc + R;
+        fo_rkinf = fo_kinf + m.n_fo;
+        fo_k0 = fo_rkinf + m.n_fo;
+        fo_lfc = fo_k0 + m.n_fo;
     }
 };
 
@@ -238,7 +238,6 @@ __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem&
         double sp = fma(fma(fma(s[3], T, s[2]), T, s[1]), T, s[0]);
         double sr = fma(a[0], lnT, fma(sp, T, a[6]));
         w.cpR[k] = cp;
-        w.hRT[k] = hr;
         w.gRT[k] = hr - sr;
         w.hk[k] = hr * RT;  // updateThermo: h_k [J/kmol]
     }

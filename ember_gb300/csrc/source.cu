@@ -28,7 +28,7 @@ template <int NT>
 __global__ void __launch_bounds__(NT) k_build_tables(MechView m, double* work) {
     const int node = blockIdx.x;
     const size_t sd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, false);
-    double* base = work + size_t(node) * (sd + ChemSmem::global_doubles(m.R));
+    double* base = work + size_t(node) * (sd + ChemSmem::global_doubles(m));
     ChemSmem w;
     w.carve(base, base + sd, m, false);
     const double T = m.Tmin + ((double)node) / (m.nT - 1) * (m.Tmax - m.Tmin);
@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(NT) k_gas_eval(MechView m, int n, double p, in
                                                 double* hk, double* cp_mass, double* density) {
     extern __shared__ double smem[];
     ChemSmem w;
-    w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), m, true);
+    w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m), m, true);
     double* y = smem + ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true);
     for (int j = blockIdx.x; j < n; j += gridDim.x) {
         for (int k = threadIdx.x; k < m.S; k += NT) y[k] = Y[size_t(j) * m.S + k];
@@ -193,9 +193,9 @@ __global__ void k_order_scatter(const double* __restrict__ dt, int n, int* curso
 }
 
 // Resident CTAs per SM the register budget is sized for (none of the widths
-// spills): 5 for NT <= 128 (the shared-memory limit of the 150-species
-// mechanism), 4 for 160, 3 for 192, 2 for 256.
-constexpr int qss_min_blocks(int nt) { return nt <= 128 ? 5 : (nt <= 160 ? 4 : (nt <= 192 ? 3 : 2)); }
+// spills): 6 for NT <= 96 (the shared-memory limit of the 150-species
+// mechanism, 35 KB per point), 5 for 128, 4 for 160, 3 for 192, 2 for 256.
+constexpr int qss_min_blocks(int nt) { return nt <= 96 ? 6 : (nt <= 128 ? 5 : (nt <= 160 ? 4 : (nt <= 192 ? 3 : 2))); }
 
 template <int NT>
 __global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView m, SourceArgs a, int* counter,
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView 
     const size_t cd = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, false);
     SourceQssOde<NT> ode;
     ode.m = m;
-    ode.w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m.R), m, false);
+    ode.w.carve(smem, kcache + size_t(blockIdx.x) * ChemSmem::global_doubles(m), m, false);
     QssSmem v;
     v.carve(smem + cd, n, stab);
     ode.a = &a;
@@ -464,7 +464,7 @@ extern "C" int ember_mech_create(const ember_mech_desc* d, ember_mech* out) {
     if (e == cudaSuccess && R) {
         double* work = nullptr;
         e = cudaMalloc(&work, sizeof(double) * (ChemSmem::doubles(S, R, n_tb, n_fo, false) +
-                                                 ChemSmem::global_doubles(R)) * nT);
+                                                 ChemSmem::global_doubles(R, n_fo)) * nT);
         if (e == cudaSuccess) {
             switch (chem_threads_for(S)) {
                 case 64: k_build_tables<64><<<nT, 64>>>(v, work); break;
@@ -548,7 +548,7 @@ extern "C" int ember_gas_eval(ember_mech m, int n, double pressure, int model, i
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const int blocks = std::min(n, sms * 4);
     double* kcache = nullptr;
-    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m->R)));
+    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m->view)));
 #define EMBER_GAS_EVAL(NTV)                                                                                  \
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_gas_eval<NTV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per))); \
     k_gas_eval<NTV><<<blocks, NTV, per, st>>>(v, n, pressure, model, mode, dT, dY, kcache, c1, c2, c3, c4, c5, c6)
@@ -690,7 +690,7 @@ static int qss_scratch_nt(const MechView& m, const SourceArgs& a, size_t* bytes)
     size_t per = 0;
     int blocks = 0;
     EMBER_TRY(qss_config<NT>(m, a, &per, &blocks));
-    *bytes = Scratch::rounded(sizeof(double) * size_t(blocks) * ChemSmem::global_doubles(m.R)) +
+    *bytes = Scratch::rounded(sizeof(double) * size_t(blocks) * ChemSmem::global_doubles(m)) +
              Scratch::rounded(sizeof(int) * 64) + Scratch::rounded(sizeof(int) * size_t(a.n));
     return EMBER_OK;
 }
@@ -719,7 +719,7 @@ static int launch_qss_nt(const MechView& m, const SourceArgs& a, int* counter, S
     int blocks = 0;
     EMBER_TRY(qss_config<NT>(m, a, &per, &blocks));
     double* kcache = nullptr;
-    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m.R)));
+    EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));
     int* order = nullptr;
     EMBER_TRY(make_work_order(a, sc, st, &order));
     k_source_qss<NT><<<blocks, NT, per, st>>>(m, a, counter, order, kcache);

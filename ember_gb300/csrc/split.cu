@@ -417,21 +417,30 @@ __global__ void k_jcorr_fick(int64_t n_pts, int n, int S, const int* __restrict_
     }
 }
 
-// Step size of the jCorr smoothing (src/flameSolver.cpp:579-582), one thread per flame.
+// Step size of the jCorr smoothing (src/flameSolver.cpp:579-582), one warp
+// per flame. Every lane starts from dt and keeps the smaller candidate (a NaN
+// candidate is never taken, as in the reference's std::min(dt, cand)), so the
+// warp minimum equals the sequential one exactly.
 __global__ void k_jcorr_h(int n_flames, const int64_t* __restrict__ goff, const int* __restrict__ npts,
                           const double* __restrict__ x, const double* __restrict__ jB, double mult, double gdt,
                           double* __restrict__ h) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    const int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
     if (f >= n_flames) return;
     const double* xf = x + goff[f];
     const double* bf = jB + goff[f];
     double dt = gdt;
-    for (int j = 1; j < npts[f] - 1; ++j) {
+    for (int j = 1 + lane; j < npts[f] - 1; j += 32) {
         const double dlj = 0.5 * (xf[j + 1] - xf[j - 1]);
         const double cand = ((mult * dlj) * dlj) / bf[j];
-        dt = (cand < dt) ? cand : dt;  // std::min(dt, cand)
+        dt = (cand < dt) ? cand : dt;
     }
-    h[f] = dt;
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) {
+        const double o = __shfl_xor_sync(0xffffffffu, dt, off);
+        dt = (o < dt) ? o : dt;
+    }
+    if (lane == 0) h[f] = dt;
 }
 
 __device__ __forceinline__ double grid_pow(double v, int alpha) { return alpha == 0 ? 1.0 : (alpha == 1 ? v : pow(v, alpha)); }
@@ -546,6 +555,7 @@ struct ember_split_s {
     double *jcorr = nullptr, *jB = nullptr, *jD = nullptr, *jsc = nullptr, *jh = nullptr, *sumcpj = nullptr;
     double* jwork = nullptr;
     DiffSysInfo* jinfo = nullptr;
+    DiffusionWarpPlan jplan;  // jCorr systems (one per flame) with the warp-parallel algorithm
     ember_diffusion_grid* d_grids = nullptr;
     int *jstatus = nullptr, *pt_local = nullptr, *pt_flame = nullptr;
     cudaStream_t capture_stream = nullptr;
@@ -638,8 +648,9 @@ int enqueue_properties(ember_split h, cudaStream_t st) {
     const int gp = grid_for(h->n_pts);
     k_jcorr_fick<<<gp, 256, 0, st>>>(h->n_pts, n, S, h->pt_local, h->pt_flame, h->flame_npts, h->x, h->state,
                                       h->p_rhoD, h->p_lam, h->p_rho, h->p_cp, h->jcorr, h->jB);
-    k_jcorr_h<<<blocks_for(h->n_flames, 64), 64, 0, st>>>(h->n_flames, h->flame_goff, h->flame_npts, h->x, h->jB,
-                                                           h->opt.dt_multiplier, h->opt.dt, h->jh);
+    k_jcorr_h<<<blocks_for(int64_t(h->n_flames) * 32, 128), 128, 0, st>>>(h->n_flames, h->flame_goff, h->flame_npts,
+                                                                          h->x, h->jB, h->opt.dt_multiplier, h->opt.dt,
+                                                                          h->jh);
     DiffusionView jv{};
     jv.n_systems = h->n_flames;
     jv.info = h->jinfo;
@@ -652,7 +663,12 @@ int enqueue_properties(ember_split h, cudaStream_t st) {
     StageTime tm;
     tm.t0 = 0.0;
     tm.t1 = h->opt.dt;
-    EMBER_TRY(diffusion_serial_run(jv, h->jcorr, h->jwork, h->n_pts, h->nmax, tm, h->opt.dt_multiplier, h->opt.dt, st));
+    if (h->opt.diffusion_algorithm == EMBER_DIFFUSION_SERIAL) {
+        EMBER_TRY(diffusion_serial_run(jv, h->jcorr, h->jwork, h->n_pts, h->nmax, tm, h->opt.dt_multiplier, h->opt.dt,
+                                       st));
+    } else {
+        EMBER_TRY(diffusion_warp_run(h->jplan, jv, h->jcorr, tm, h->opt.dt_multiplier, h->opt.dt, st));
+    }
     k_count_failures<<<blocks_for(h->n_flames, 256), 256, 0, st>>>(h->n_flames, h->jstatus, h->fails + 1);
     k_cross_species<<<gp, 256, 0, st>>>(h->n_pts, n, S, h->pt_local, h->pt_flame, h->flame_npts, h->d_grids, h->x,
                                          h->state, h->p_rhoD, h->p_cpS, h->mech->view.W, h->p_rho, h->jcorr,
@@ -936,10 +952,27 @@ extern "C" int ember_split_set_transport_model(ember_split h, ember_transport tr
     if (!tr) return EMBER_OK;
     const int64_t np = h->n_pts;
     const int S = h->n_vars - 2, nf = h->n_flames;
+    std::vector<DiffSysInfo> ji(nf);
+    std::vector<int> loc(np), fl(np);
+    for (int f = 0; f < nf; ++f) {
+        const ember_diffusion_grid& g = h->grids[f];
+        ji[f].off = h->h_goff[f];
+        ji[f].grid_off = h->h_goff[f];
+        ji[f].n = g.n_points;
+        ji[f].left_bc = g.left_bc;
+        ji[f].right_bc = g.right_bc;
+        ji[f].alpha = g.alpha;
+        for (int i = 0; i < g.n_points; ++i) {
+            loc[h->h_goff[f] + i] = i;
+            fl[h->h_goff[f] + i] = f;
+        }
+    }
+    const bool serial = h->opt.diffusion_algorithm == EMBER_DIFFUSION_SERIAL;
     auto bd = [](size_t c) { return Scratch::rounded(c * sizeof(double)); };
-    const size_t total = 4 * bd(np) + 2 * bd(size_t(np) * S) + 6 * bd(np) + bd(7 * size_t(np)) +
-                         Scratch::rounded(sizeof(DiffSysInfo) * nf) + Scratch::rounded(sizeof(ember_diffusion_grid) * nf) +
-                         Scratch::rounded(sizeof(int) * nf) + 2 * Scratch::rounded(sizeof(int) * np);
+    const size_t total = 4 * bd(np) + 2 * bd(size_t(np) * S) + 6 * bd(np) + (serial ? bd(7 * size_t(np)) : 0) +
+                         (serial ? 0 : diffusion_warp_plan_bytes(ji, np)) + Scratch::rounded(sizeof(DiffSysInfo) * nf) +
+                         Scratch::rounded(sizeof(ember_diffusion_grid) * nf) + Scratch::rounded(sizeof(int) * nf) +
+                         2 * Scratch::rounded(sizeof(int) * np);
     EMBER_CUDA_TRY(cudaMalloc(&h->pblob, total));
     int rc = EMBER_OK;
     {
@@ -959,30 +992,16 @@ extern "C" int ember_split_set_transport_model(ember_split h, ember_transport tr
         carve(&h->jsc, np);
         carve(&h->jh, np);
         carve(&h->sumcpj, np);
-        carve(&h->jwork, 7 * size_t(np));
+        if (serial) carve(&h->jwork, 7 * size_t(np));
         carve(&h->jinfo, nf);
         carve(&h->d_grids, nf);
         carve(&h->jstatus, nf);
         carve(&h->pt_local, np);
         carve(&h->pt_flame, np);
+        if (rc == EMBER_OK && !serial) rc = diffusion_warp_plan_init(&h->jplan, ji, nf, 1, np, a, nullptr);
     }
     if (rc != EMBER_OK) return rc;
-    std::vector<DiffSysInfo> ji(nf);
-    std::vector<int> loc(np), fl(np);
     std::vector<double> ones(np, 1.0);
-    for (int f = 0; f < nf; ++f) {
-        const ember_diffusion_grid& g = h->grids[f];
-        ji[f].off = h->h_goff[f];
-        ji[f].grid_off = h->h_goff[f];
-        ji[f].n = g.n_points;
-        ji[f].left_bc = g.left_bc;
-        ji[f].right_bc = g.right_bc;
-        ji[f].alpha = g.alpha;
-        for (int i = 0; i < g.n_points; ++i) {
-            loc[h->h_goff[f] + i] = i;
-            fl[h->h_goff[f] + i] = f;
-        }
-    }
     cudaError_t e = cudaMemcpy(h->jinfo, ji.data(), sizeof(DiffSysInfo) * nf, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(h->d_grids, h->grids.data(), sizeof(ember_diffusion_grid) * nf,
                                          cudaMemcpyHostToDevice);
@@ -990,6 +1009,11 @@ extern "C" int ember_split_set_transport_model(ember_split h, ember_transport tr
     if (e == cudaSuccess) e = cudaMemcpy(h->pt_flame, fl.data(), sizeof(int) * np, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(h->jD, ones.data(), sizeof(double) * np, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(h->jsc, 0, sizeof(double) * np);
+    if (e == cudaSuccess && !serial) {
+        rc = diffusion_warp_geometry(h->jplan, h->jinfo, h->x, nullptr);
+        if (rc != EMBER_OK) return rc;
+        e = cudaDeviceSynchronize();
+    }
     if (e != cudaSuccess) {
         set_error("ember_split_set_transport_model: %s", cudaGetErrorString(e));
         return EMBER_ECUDA;

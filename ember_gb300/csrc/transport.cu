@@ -81,6 +81,8 @@ __global__ void __launch_bounds__(NT) k_transport(MechView m, TransportView tv, 
     double* lam = mu + S;
     double* sk = lam + S;
     double* red = sk + S;
+    int* rows = reinterpret_cast<int*>(red + kRedDoubles);  // [S]: major species, then the others (ascending)
+    __shared__ int s_nmaj;
     for (int j = blockIdx.x; j < n; j += gridDim.x) {
         const double T = Tin[j * tstride];
         for (int k = t; k < S; k += NT) y[k] = Yin[j * ystride + k];
@@ -111,29 +113,57 @@ __global__ void __launch_bounds__(NT) k_transport(MechView m, TransportView tv, 
         for (int k = t; k < S; k += NT) x[k] = dmaxr(ym[k] * mmw, kMoleFractionFloor);
         const double s1 = block_sum<NT>(red, S, [&](int k, double q) { return q + x[k] * lam[k]; });
         const double s2 = block_sum<NT>(red, S, [&](int k, double q) { return q + x[k] / lam[k]; });
-        // Wilke denominators of the major species
-        for (int k = t; k < S; k += NT) {
+        // Lists of the major species and of the others, each in species order
+        // (warp 0, ballot compaction), so that threads take rows of equal
+        // cost: a major row has S - 1 partners, any other row the K majors.
+        __syncthreads();
+        if (t < 32) {
+            const unsigned below = (1u << t) - 1u;
+            int nm = 0;
+            for (int b = 0; b < S; b += 32) {
+                const bool f = b + t < S && x[b + t] >= thr;
+                const unsigned bal = __ballot_sync(0xffffffffu, f);
+                if (f) rows[nm + __popc(bal & below)] = b + t;
+                nm += __popc(bal);
+            }
+            int no = nm;
+            for (int b = 0; b < S; b += 32) {
+                const bool f = b + t < S && !(x[b + t] >= thr);
+                const unsigned bal = __ballot_sync(0xffffffffu, f);
+                if (f) rows[no + __popc(bal & below)] = b + t;
+                no += __popc(bal);
+            }
+            if (t == 0) s_nmaj = nm;
+        }
+        __syncthreads();
+        const int K = s_nmaj;
+        // Wilke denominators of the major species (partners: the majors in order)
+        for (int r = t; r < K; r += NT) {
+            const int k = rows[r];
             double s = 0.0;
-            if (x[k] >= thr) {
-                for (int c = 0; c < S; ++c)
-                    if (x[c] >= thr) s = s + x[c] * wilke_phi(tv, sq, mu, m.W, k, c);
+            for (int ci = 0; ci < K; ++ci) {
+                const int c = rows[ci];
+                s = s + x[c] * wilke_phi(tv, sq, mu, m.W, k, c);
             }
             sk[k] = s;
         }
         const double vis = block_sum<NT>(red, S, [&](int k, double q) {
             return x[k] >= thr ? q + (x[k] * mu[k]) / sk[k] : q;
         });
-        // rho D_k
+        // rho D_k: a major species with every other one, the others with the majors
         if (out.rho_d) {
-            for (int k = t; k < S; k += NT) {
+            for (int r = t; r < S; r += NT) {
+                const int k = rows[r];
                 double d;
                 if (S == 1) {
                     d = (t15 * fit5(tv.diff, lnT, l2, l3, l4)) / p;
                 } else {
-                    const bool major = x[k] >= thr;
+                    const bool major = r < K;
+                    const int count = major ? S : K;
                     double a1 = 0.0, a2 = 0.0;
-                    for (int i = 0; i < S; ++i) {
-                        if (i == k || !(major || x[i] >= thr)) continue;
+                    for (int ii = 0; ii < count; ++ii) {
+                        const int i = major ? ii : rows[ii];
+                        if (i == k) continue;
                         const int64_t q = i < k ? pair_index(S, i, k) : pair_index(S, k, i);
                         const double bd = t15 * fit5(tv.diff + 5 * q, lnT, l2, l3, l4);
                         a1 = a1 + x[i] / bd;
@@ -161,7 +191,7 @@ template <int NT>
 int launch_transport_nt(const MechView& m, const TransportView& tv, int n, double p, double thr, const double* T,
                         int64_t tstride, const double* Y, int64_t ystride, const ember_properties& out,
                         cudaStream_t st) {
-    const size_t smem = (size_t(8) * m.S + kRedDoubles) * sizeof(double);
+    const size_t smem = (size_t(8) * m.S + kRedDoubles) * sizeof(double) + sizeof(int) * m.S;
     EMBER_CHECK_ARG(smem <= 227 * 1024, "too many species for the transport work area");
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_transport<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int dev = 0, sms = 0, per_sm = 0;

@@ -104,15 +104,19 @@ def tridiag_flops_per_point() -> float:
     return 12.0 + 5.0 + 8 * 7.0
 
 
-def transport_point_flops(n_species: int, cross_terms: bool = True) -> float:
+def transport_point_flops(n_species: int, n_major=None, cross_terms: bool = True):
     """Thermo, "Approx" transport and cross terms of one grid point
-    (ember_transport_eval / the split step's property update), every species
-    major: per species the NASA7 cp and h (~20) and three fits (3 x 11); per
-    species pair the Wilke term (~10) and the binary diffusion fit plus the
-    two sums of the mixture coefficient (~15); the cross terms ~20 per
-    species (Fick flux twice, species and heat-capacity terms)."""
+    (ember_transport_eval / the split step's property update) with n_major
+    species at or above the threshold (default: all; scalar or array): per
+    species the NASA7 cp and h (~20) and three fits (3 x 11); per major pair
+    the Wilke term (~10); per pair of the mixture diffusion sums (a major
+    species with every other, a minor one with the major ones) the binary
+    diffusion fit and the two sums (~15); the cross terms ~20 per species
+    (Fick flux twice, species and heat-capacity terms)."""
     S = float(n_species)
-    return 53.0 * S + 10.0 * S * S + 15.0 * S * (S - 1.0) + (20.0 * S if cross_terms else 0.0)
+    K = S if n_major is None else np.asarray(n_major, dtype=float)
+    pairs = K * (S - 1.0) + (S - K) * K
+    return 53.0 * S + 10.0 * K * K + 15.0 * pairs + (20.0 * S if cross_terms else 0.0)
 
 
 def tridiag_bytes_per_point() -> float:

@@ -226,3 +226,26 @@ def test_split_transport_model_bitwise_vs_oracle(gpu_lib, mech, cross):
     s2.set_transport_model(gt2, 1e-5, cross)
     s2.step(2, graph=True)
     assert np.array_equal(s2.state()[0], out)
+
+
+@pytest.mark.gpu
+def test_split_transport_model_parallel_diffusion_close_to_oracle(gpu_lib, mech):
+    # the warp-parallel integrator (diffusion stages and the jCorr smoothing)
+    # agrees with the reference's Thomas algorithm to rounding
+    from oracle.chem import OracleMech
+    from ember_gb300.transport import GpuTransport, synthetic_transport
+    td = synthetic_transport(mech, seed=4)
+    grids, state, B, D, rho_u, ju, jb = _case(mech, n_flames=2, n_min=40, n_max=90)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    gm, s = _gpu_solver(mech, grids, 2e-6, QSS, opts, L.DIFFUSION_PARALLEL)
+    gt = GpuTransport(gm, td)
+    s.set_state(0.0, state)
+    s.set_transport(B, D)
+    s.set_transport_model(gt, 1e-5, True)
+    s.step(2, graph=True)
+    out, _ = s.state()
+    ref, *_ = osplit.split_steps(OracleMech(mech), grids, state, 0.0, B, D, 2e-6, 2, QSS, opts,
+                                 transport=(td, 1e-5, True))
+    scale = np.abs(ref).max(axis=0)
+    err = (np.abs(out - ref) / np.where(scale > 0, scale, 1.0)).max()
+    assert err <= 1e-9, err
