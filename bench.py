@@ -55,6 +55,8 @@ def parse_args():
     p.add_argument("--mech", default="150", choices=["150", "53"],
                    help="source workloads: the 150-species/1000-reaction mechanism or the GRI-3.0-sized "
                         "53-species/325-reaction one")
+    p.add_argument("--source", default="qss", choices=["qss", "bdf"],
+                   help="split workload: source-term integrator (the C5 sweep names BDF)")
     p.add_argument("--threads", type=int, default=0,
                    help="QSS threads per point; 0: ember_source_autotune picks it before the timed region")
     return p.parse_args()
@@ -229,8 +231,10 @@ def run_ours(args):
 
     # launch width: autotuned on this batch (outside the timed region), or given
     tune_ms = {}
-    if method == QSS and args.threads == 0:
-        width, tune_ms = autotune(gm, QSS, st_d, dt_d, opts, stream=stream)
+    if args.threads == 0:
+        # QSS: the whole batch; BDF (12 candidates): its first 1024 points
+        k = args.points if method == QSS else min(args.points, 1024)
+        width, tune_ms = autotune(gm, method, st_d[:k], dt_d[:k], opts, stream=stream)
     else:
         width = args.threads
         opts.threads_per_point = width
@@ -501,11 +505,19 @@ SPLIT_TRANSPORT_SEED = 1523
 SPLIT_THRESHOLD = 1e-5
 
 
-def split_inputs(rank: int):
+def split_inputs(rank: int, mech_size: str = "150"):
     from ember_gb300.mechanism import synthetic_mechanism
     from ember_gb300.split import flame_batch
-    mech = synthetic_mechanism(seed=MECH_SEED)
+    if mech_size == "53":
+        mech = synthetic_mechanism(n_species=53, n_reactions=325, seed=53325)
+    else:
+        mech = synthetic_mechanism(seed=MECH_SEED)
     return (mech,) + flame_batch(mech, n_flames=32, n_min=150, n_max=700, seed=3232 + rank)
+
+
+def split_workload(args, mech) -> str:
+    return SPLIT_WORKLOAD.replace("150-species/1000-reaction", f"{mech.n_species}-species/{mech.n_reactions}-reaction") \
+        .replace("QSS source", f"{args.source.upper()} source")
 
 
 def run_reference_split(args):
@@ -514,9 +526,10 @@ def run_reference_split(args):
         return 0
     from oracle.chem import OracleMech
     from oracle import split as osplit
-    from ember_gb300.source import QSS
-    mech, grids, state, B, D, rho_u, ju, jb = split_inputs(0)
-    opts = source_options(args.kinetics, "qss")
+    from ember_gb300.source import QSS, BDF
+    mech, grids, state, B, D, rho_u, ju, jb = split_inputs(0, args.mech)
+    opts = source_options(args.kinetics, args.source)
+    method = QSS if args.source == "qss" else BDF
     om = OracleMech(mech)
     # bounded sample: the first flame, one split step per timed step
     g0 = grids[:1]
@@ -526,10 +539,10 @@ def run_reference_split(args):
     from ember_gb300.transport import synthetic_transport
     tr = (synthetic_transport(mech, seed=SPLIT_TRANSPORT_SEED), SPLIT_THRESHOLD, True)
     for _ in range(args.warmup):
-        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, QSS, opts, transport=tr)
+        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, method, opts, transport=tr)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, QSS, opts, transport=tr)
+        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, method, opts, transport=tr)
     per_flame = (time.perf_counter() - t0) / args.steps
     # scaled to the 32-flame batch by points
     ms = 1e3 * per_flame * len(state) / n0
@@ -538,7 +551,7 @@ def run_reference_split(args):
         "impl": "reference", "metric": SPLIT_METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": SPLIT_WORKLOAD, "points": int(len(state))},
+        "config": {"workload": split_workload(args, mech), "points": int(len(state))},
         "cpu_baseline": {"value": ms, "unit": "ms", "cores": threads, "kind": "port",
                          "sample": f"flame 0 ({n0} points) per step, scaled to {len(state)} points"},
         "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
@@ -554,14 +567,15 @@ def run_ours_split(args):
     if ws > 1:
         torch.distributed.init_process_group("nccl")
     from ember_gb300 import _lib, roofline
-    from ember_gb300.source import GpuMechanism, QSS, autotune
+    from ember_gb300.source import GpuMechanism, QSS, BDF, autotune
     from ember_gb300.split import FlameBatchSplitSolver
-    mech, grids, state, B, D, rho_u, ju, jb = split_inputs(rank)
-    opts = source_options(args.kinetics, "qss")
+    mech, grids, state, B, D, rho_u, ju, jb = split_inputs(rank, args.mech)
+    opts = source_options(args.kinetics, args.source)
+    method = QSS if args.source == "qss" else BDF
     gm = GpuMechanism(mech)
     # QSS launch width tuned on the flames' start states over one step (before the solver takes it)
-    width, tune_ms = autotune(gm, QSS, state, np.full(len(state), SPLIT_DT), opts)
-    solver = FlameBatchSplitSolver(gm, grids, SPLIT_DT, method=QSS, source_options=opts)
+    width, tune_ms = autotune(gm, method, state, np.full(len(state), SPLIT_DT), opts)
+    solver = FlameBatchSplitSolver(gm, grids, SPLIT_DT, method=method, source_options=opts)
     from ember_gb300.transport import GpuTransport, synthetic_transport
     tdata = synthetic_transport(mech, seed=SPLIT_TRANSPORT_SEED)
     gtr = GpuTransport(gm, tdata)
@@ -591,7 +605,11 @@ def run_ours_split(args):
         ends[i].record(stream)
         torch.cuda.synchronize()
         _, stats = solver.source_status()
-        src_flops += float(roofline.qss_point_flops(mech, opts.kinetics_model, stats[:, 0], stats[:, 1]).sum())
+        if method == QSS:
+            src_flops += float(roofline.qss_point_flops(mech, opts.kinetics_model, stats[:, 0], stats[:, 1]).sum())
+        else:
+            src_flops += float(roofline.bdf_point_flops(mech, opts.kinetics_model, stats[:, 0], stats[:, 1],
+                                                        stats[:, 3]).sum())
     total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     if ws > 1:
         t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
@@ -619,7 +637,7 @@ def run_ours_split(args):
         "metric": SPLIT_METRIC, "value": ms, "unit": "ms", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded flame-like profiles, synthetic transport)",
-        "config": {"workload": SPLIT_WORKLOAD, "points": int(len(state)), "flames": len(grids),
+        "config": {"workload": split_workload(args, mech), "points": int(len(state)), "flames": len(grids),
                    "points_per_s": len(state) / (ms / 1e3), "l2": "256 MB buffer written between timed steps",
                    "graph": True, "failed_source_points": n_fail_src, "failed_diffusion_systems": n_fail_diff,
                    "threads_per_point": width, "autotune_ms": {str(k): round(v, 2) for k, v in tune_ms.items()}},
@@ -645,7 +663,7 @@ def run_ours_split(args):
         t0 = time.perf_counter()
         reps = 0
         while time.perf_counter() - t0 < args.cpu_seconds or reps == 0:
-            osplit.split_steps(om, grids[:1], state[:n0], 0.0, B[:nv * n0], D[:nv * n0], SPLIT_DT, 1, QSS, opts,
+            osplit.split_steps(om, grids[:1], state[:n0], 0.0, B[:nv * n0], D[:nv * n0], SPLIT_DT, 1, method, opts,
                                transport=(tdata, SPLIT_THRESHOLD, True))
             reps += 1
         tcpu = (time.perf_counter() - t0) / reps

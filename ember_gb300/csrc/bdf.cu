@@ -465,15 +465,35 @@ struct BdfLayout {
 
 constexpr size_t kBdfSmemBudget = 225 * 1024;  // leaves room for the static shared arrays
 
-inline BdfLayout bdf_layout(const MechView& m) {
+// The layout of a mode, or mode -1 for the default: the first of
+// BDF_JM_SMEM, BDF_M_SMEM, BDF_JM_GLOBAL that fits. smem_bytes is 0 when the
+// requested mode does not fit.
+inline BdfLayout bdf_layout_of(const MechView& m, int mode) {
     const size_t n = size_t(m.S) + 2, nn = n * n;
     const size_t full = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(3) * m.n_fo + BdfSmem::doubles(int(n));
     const size_t lean = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true, false) + size_t(3) * m.n_fo +
                         BdfSmem::doubles(int(n), false);
-    if ((full + 2 * nn) * sizeof(double) <= kBdfSmemBudget) return {BDF_JM_SMEM, (full + 2 * nn) * sizeof(double), 0};
-    if ((lean + nn) * sizeof(double) <= kBdfSmemBudget)
-        return {BDF_M_SMEM, (lean + nn) * sizeof(double), nn + size_t(kQmax + 1) * n + size_t(2) * m.R};
-    return {BDF_JM_GLOBAL, full * sizeof(double), 2 * nn};
+    const BdfLayout both{BDF_JM_SMEM, (full + 2 * nn) * sizeof(double), 0};
+    const BdfLayout lu{BDF_M_SMEM, (lean + nn) * sizeof(double), nn + size_t(kQmax + 1) * n + size_t(2) * m.R};
+    const BdfLayout none{BDF_JM_GLOBAL, full * sizeof(double), 2 * nn};
+    const BdfLayout opts[3] = {both, lu, none};
+    for (const BdfLayout& l : opts) {
+        const bool fits = l.smem_bytes <= kBdfSmemBudget;
+        if (mode < 0 && fits) return l;
+        if (l.mode == mode) return fits ? l : BdfLayout{mode, 0, 0};
+    }
+    return none;
+}
+
+// The layout a launch uses: the one requested by the arguments or tuned for
+// the mechanism (1 + mode; when it fits), else the default.
+inline BdfLayout bdf_layout(const MechView& m, const SourceArgs& a) {
+    const int req = a.bdf_layout ? a.bdf_layout - 1 : (m.bdf_layout ? m.bdf_layout - 1 : -1);
+    if (req >= 0) {
+        const BdfLayout l = bdf_layout_of(m, req);
+        if (l.smem_bytes) return l;
+    }
+    return bdf_layout_of(m, -1);
 }
 
 // Carves one CTA's work areas: smem (dynamic shared memory), kc (its slice of
@@ -893,7 +913,7 @@ __global__ void __launch_bounds__(NT) k_source_bdf(const __grid_constant__ MechV
 // Dynamic shared memory and persistent grid size of the BDF kernel.
 template <int NT>
 static int bdf_config(const MechView& m, const SourceArgs& a, size_t* per_out, int* blocks_out) {
-    const size_t per = bdf_layout(m).smem_bytes;
+    const size_t per = bdf_layout(m, a).smem_bytes;
     EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the BDF shared-memory work area (%zu B)", per);
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_bdf<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
     int dev = 0, sms = 0, per_sm = 0;
@@ -912,13 +932,26 @@ static int bdf_scratch_nt(const MechView& m, const SourceArgs& a, size_t* bytes)
     int blocks = 0;
     EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
     *bytes = Scratch::rounded(sizeof(double) * size_t(blocks) * ChemSmem::global_doubles(m)) +
-             Scratch::rounded(sizeof(double) * size_t(blocks) * bdf_layout(m).global_doubles) +
+             Scratch::rounded(sizeof(double) * size_t(blocks) * bdf_layout(m, a).global_doubles) +
              Scratch::rounded(sizeof(int) * 64) + Scratch::rounded(sizeof(int) * size_t(a.n));
     return EMBER_OK;
 }
 
+int source_bdf_threads(const MechView& m, const SourceArgs& a) {
+    for (int c : kBdfThreadChoices)
+        if (a.threads == c) return c;
+    if (m.bdf_threads) return m.bdf_threads;
+    return chem_threads_for(m.S);
+}
+
+int source_bdf_layout(const MechView& m, const SourceArgs& a) { return 1 + bdf_layout(m, a).mode; }
+
+bool source_bdf_layout_fits(const MechView& m, int layout) {
+    return layout >= 1 && layout <= 3 && bdf_layout_of(m, layout - 1).smem_bytes != 0;
+}
+
 int source_bdf_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes) {
-    switch (chem_threads_for(m.S)) {
+    switch (source_bdf_threads(m, a)) {
         case 64: return bdf_scratch_nt<64>(m, a, bytes);
         case 128: return bdf_scratch_nt<128>(m, a, bytes);
         case 160: return bdf_scratch_nt<160>(m, a, bytes);
@@ -933,7 +966,7 @@ static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, S
     EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
     double *kcache = nullptr, *jm = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));
-    const BdfLayout lay = bdf_layout(m);
+    const BdfLayout lay = bdf_layout(m, a);
     EMBER_TRY(sc.alloc(&jm, size_t(blocks) * lay.global_doubles));
     int* order = nullptr;
     EMBER_TRY(make_work_order(a, sc, st, &order));
@@ -1116,7 +1149,7 @@ static int launch_bdf_adjoint_nt(const MechView& m, const SourceArgs& a, int* co
                                         int(per)));
     double *kcache = nullptr, *jm = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));
-    const BdfLayout lay = bdf_layout(m);
+    const BdfLayout lay = bdf_layout(m, a);
     EMBER_TRY(sc.alloc(&jm, size_t(blocks) * lay.global_doubles));
     k_source_bdf_adjoint<NT><<<blocks, NT, per, st>>>(m, a, counter, kcache, jm, lay.global_doubles, lay.mode,
                                                       ybar_out, ybar_in, pbar, adj_status);
@@ -1240,7 +1273,7 @@ static int launch_objective_vjp_nt(const MechView& m, const SourceArgs& a, int n
     double *kcache = nullptr, *jm = nullptr;
     int* counter = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));
-    const BdfLayout lay = bdf_layout(m);
+    const BdfLayout lay = bdf_layout(m, a);
     EMBER_TRY(sc.alloc(&jm, size_t(blocks) * lay.global_doubles));
     EMBER_TRY(sc.alloc(&counter, 1));
     EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
@@ -1253,7 +1286,7 @@ static int launch_objective_vjp_nt(const MechView& m, const SourceArgs& a, int n
 int launch_objective_vjp(const MechView& m, const SourceArgs& a, int n_pts, const double* state, const double* gq,
                          const double* gcp, const double* gT, double* ybar, double* pbar, Scratch& sc,
                          cudaStream_t st) {
-    switch (chem_threads_for(m.S)) {
+    switch (source_bdf_threads(m, a)) {
         case 64: return launch_objective_vjp_nt<64>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
         case 128: return launch_objective_vjp_nt<128>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
         case 160: return launch_objective_vjp_nt<160>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
@@ -1263,7 +1296,7 @@ int launch_objective_vjp(const MechView& m, const SourceArgs& a, int n_pts, cons
 
 int launch_source_bdf_adjoint(const MechView& m, const SourceArgs& a, int* counter, const double* ybar_out,
                               double* ybar_in, double* pbar, int* adj_status, Scratch& sc, cudaStream_t st) {
-    switch (chem_threads_for(m.S)) {
+    switch (source_bdf_threads(m, a)) {
         case 64: return launch_bdf_adjoint_nt<64>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
         case 128: return launch_bdf_adjoint_nt<128>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
         case 160: return launch_bdf_adjoint_nt<160>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
@@ -1272,7 +1305,7 @@ int launch_source_bdf_adjoint(const MechView& m, const SourceArgs& a, int* count
 }
 
 int launch_source_bdf(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
-    switch (chem_threads_for(m.S)) {
+    switch (source_bdf_threads(m, a)) {
         case 64: return launch_bdf_nt<64>(m, a, counter, sc, st);
         case 128: return launch_bdf_nt<128>(m, a, counter, sc, st);
         case 160: return launch_bdf_nt<160>(m, a, counter, sc, st);

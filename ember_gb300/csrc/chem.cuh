@@ -64,6 +64,8 @@ __host__ __device__ inline int chem_threads_for(int S) {
 struct MechView {
     int S, R, nT;
     int qss_threads;      // QSS launch width chosen by ember_source_autotune (0: none)
+    int bdf_threads;      // BDF launch width chosen by ember_source_autotune (0: none)
+    int bdf_layout;       // BDF matrix layout chosen by ember_source_autotune (0: by size, else 1 + layout)
     int n_tb, n_fo;       // reactions with [M] (three-body and falloff); falloff reactions
     double Tmin, Tmax;
     const double* W;      // [S]

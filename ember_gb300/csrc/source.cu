@@ -193,9 +193,12 @@ __global__ void k_order_scatter(const double* __restrict__ dt, int n, int* curso
 }
 
 // Resident CTAs per SM the register budget is sized for (none of the widths
-// spills): 6 for NT <= 96 (the shared-memory limit of the 150-species
-// mechanism, 35 KB per point), 5 for 128, 4 for 160, 3 for 192, 2 for 256.
-constexpr int qss_min_blocks(int nt) { return nt <= 96 ? 6 : (nt <= 128 ? 5 : (nt <= 160 ? 4 : (nt <= 192 ? 3 : 2))); }
+// spills): 16 for NT = 32 (one warp per point, for small mechanisms whose
+// passes are too short to hide barrier and shared-memory latency with a few
+// points per SM), 6 for NT <= 96 (the shared-memory limit of the
+// 150-species mechanism, 35 KB per point), 5 for 128, 4 for 160, 3 for 192,
+// 2 for 256.
+constexpr int qss_min_blocks(int nt) { return nt <= 32 ? 16 : (nt <= 96 ? 6 : (nt <= 128 ? 5 : (nt <= 160 ? 4 : (nt <= 192 ? 3 : 2)))); }
 
 template <int NT>
 __global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView m, SourceArgs a, int* counter,
@@ -811,10 +814,6 @@ extern "C" int ember_source_autotune(ember_mech m, int method, int n, const doub
     static_assert(kChoices == EMBER_SOURCE_N_THREAD_CHOICES, "thread choices out of step with the header");
     if (ms_out)
         for (int i = 0; i < kChoices; ++i) ms_out[i] = 0.0;
-    if (method == EMBER_SOURCE_BDF) {
-        *threads_out = chem_threads_for(m->S);
-        return EMBER_OK;
-    }
     EMBER_TRY(ensure_device());
     cudaStream_t st = as_stream(stream);
     Scratch sc(st);
@@ -832,26 +831,40 @@ extern "C" int ember_source_autotune(ember_mech m, int method, int n, const doub
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     EMBER_CUDA_TRY(cudaEventCreate(&e0));
     int rc = cuda_check(cudaEventCreate(&e1), "cudaEventCreate");
-    int best = 0;
+    int best = 0, best_layout = 0;
     float best_ms = 0.0f;
+    // QSS: every width; BDF: every width of kBdfThreadChoices x every matrix layout that fits
+    const bool bdf = method == EMBER_SOURCE_BDF;
     for (int i = 0; i < kChoices && rc == EMBER_OK; ++i) {
-        ember_source_options o = *opts;
-        o.threads_per_point = kQssThreadChoices[i];
-        SourceArgs a = make_source_args(&o, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, nullptr);
-        float ms = 0.0f;
-        for (int rep = 0; rep < 2 && rc == EMBER_OK; ++rep) {  // the first run is untimed
-            rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), st), "cudaMemsetAsync");
-            if (rc == EMBER_OK) rc = cuda_check(cudaEventRecord(e0, st), "cudaEventRecord");
-            if (rc == EMBER_OK) rc = launch_source_qss(m->view, a, counter, sc, st);
-            if (rc == EMBER_OK) rc = cuda_check(cudaEventRecord(e1, st), "cudaEventRecord");
-            if (rc == EMBER_OK) rc = cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
-            if (rc == EMBER_OK) rc = cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
-        }
-        if (rc != EMBER_OK) break;
-        if (ms_out) ms_out[i] = ms;
-        if (best == 0 || ms < best_ms) {
-            best = kQssThreadChoices[i];
-            best_ms = ms;
+        const int width = kQssThreadChoices[i];
+        bool valid = !bdf;
+        for (int c : kBdfThreadChoices) valid = valid || width == c;
+        if (!valid) continue;
+        for (int layout = bdf ? 1 : 0; layout <= (bdf ? 3 : 0) && rc == EMBER_OK; ++layout) {
+            if (bdf && !source_bdf_layout_fits(m->view, layout)) continue;
+            ember_source_options o = *opts;
+            o.threads_per_point = width;
+            SourceArgs a = make_source_args(&o, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, nullptr);
+            a.bdf_layout = layout;
+            float ms = 0.0f;
+            for (int rep = 0; rep < 2 && rc == EMBER_OK; ++rep) {  // the first run is untimed
+                Scratch work(st);  // the launch's work areas, freed after it on the stream
+                rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), st), "cudaMemsetAsync");
+                if (rc == EMBER_OK) rc = cuda_check(cudaEventRecord(e0, st), "cudaEventRecord");
+                if (rc == EMBER_OK)
+                    rc = bdf ? launch_source_bdf(m->view, a, counter, work, st)
+                             : launch_source_qss(m->view, a, counter, work, st);
+                if (rc == EMBER_OK) rc = cuda_check(cudaEventRecord(e1, st), "cudaEventRecord");
+                if (rc == EMBER_OK) rc = cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+                if (rc == EMBER_OK) rc = cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+            }
+            if (rc != EMBER_OK) break;
+            if (ms_out && (ms_out[i] == 0.0 || ms < ms_out[i])) ms_out[i] = ms;
+            if (best == 0 || ms < best_ms) {
+                best = width;
+                best_layout = layout;
+                best_ms = ms;
+            }
         }
     }
     cudaEventDestroy(e0);
@@ -859,7 +872,12 @@ extern "C" int ember_source_autotune(ember_mech m, int method, int n, const doub
     sc.release();
     EMBER_TRY(rc);
     EMBER_TRY(finish_call(EMBER_MEM_DEVICE, st));
-    m->view.qss_threads = best;
+    if (bdf) {
+        m->view.bdf_threads = best;
+        m->view.bdf_layout = best_layout;
+    } else {
+        m->view.qss_threads = best;
+    }
     *threads_out = best;
     return EMBER_OK;
 }

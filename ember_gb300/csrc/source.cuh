@@ -12,7 +12,8 @@ namespace ember {
 // Flattened arguments of one source-term launch (device pointers).
 struct SourceArgs {
     int n;
-    int threads;              // QSS threads per point requested (0: the mechanism's tuned or default width)
+    int threads;              // threads per point requested (0: the mechanism's tuned or default width)
+    int bdf_layout;           // BDF matrix layout requested (0: the mechanism's tuned one or by size, else 1 + layout)
     const double* state_in;   // [n][S+2]
     const double* split;      // [n][S+2] or null
     const double* dt;         // [n]
@@ -93,6 +94,13 @@ int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* byt
 // Threads per point of the QSS kernel for these arguments (see threads_per_point).
 int source_qss_threads(const MechView& m, const SourceArgs& a);
 int source_bdf_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes);
+// Threads per point and matrix layout (1 + BDF_* of bdf.cu) of the BDF kernel for these arguments.
+int source_bdf_threads(const MechView& m, const SourceArgs& a);
+int source_bdf_layout(const MechView& m, const SourceArgs& a);
+// Whether matrix layout 1 + mode fits the BDF kernel's shared memory for this mechanism.
+bool source_bdf_layout_fits(const MechView& m, int layout);
+// Launch widths of the BDF kernel.
+constexpr int kBdfThreadChoices[] = {64, 128, 160, 256};
 
 }  // namespace ember
 

@@ -519,6 +519,7 @@ using namespace ember;
 struct ember_split_s {
     ember_mech mech = nullptr;
     ember_split_options opt{};
+    int bdf_layout = 0;  // the BDF matrix layout the source arena was sized for (1 + mode)
     int n_flames = 0, n_vars = 0, nmax = 0;
     int64_t n_pts = 0, n_vals = 0;
     std::vector<ember_diffusion_grid> grids;
@@ -569,6 +570,7 @@ struct ember_split_s {
         SourceArgs a = make_source_args(&opt.source, static_cast<int>(n_pts), xD2, sc_prod, dtp, 0.0, x, state,
                                         src_status, src_stats);
         a.t_start_dev = t_dev;
+        a.bdf_layout = bdf_layout;
         return a;
     }
 
@@ -822,7 +824,12 @@ extern "C" int ember_split_create(ember_mech mech, int n_flames, const ember_dif
     h->opt = *opts;
     // the handle keeps the QSS width its scratch arena was sized for, even if
     // the mechanism is tuned again later
-    if (opts->method == EMBER_SOURCE_QSS) h->opt.source.threads_per_point = source_qss_threads(mech->view, probe);
+    if (opts->method == EMBER_SOURCE_QSS) {
+        h->opt.source.threads_per_point = source_qss_threads(mech->view, probe);
+    } else {
+        h->opt.source.threads_per_point = source_bdf_threads(mech->view, probe);
+        h->bdf_layout = source_bdf_layout(mech->view, probe);
+    }
     h->n_flames = n_flames;
     h->n_vars = n_vars;
     h->nmax = nmax;

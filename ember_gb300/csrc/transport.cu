@@ -21,9 +21,11 @@
 //               sum_i X_i W_i / D_ki), the sums over every species i != k for
 //               a major k, over the major ones otherwise (getMixDiffCoeffsMass,
 //               98-139).
-// Sums over species run in the fixed 32-lane order of block_sum; the
-// per-species sums over partners run sequentially in species order. No
-// automatic FMA contraction (--fmad=false): the CPU oracle repeats every
+// Sums over species, and a major species' diffusion sums over its S - 1
+// partners (one warp per species), run in the fixed 32-lane order of
+// block_sum: term m on lane m mod 32, sequential per lane, then an xor
+// butterfly; the other per-species sums run sequentially in species order.
+// No automatic FMA contraction (--fmad=false): the CPU oracle repeats every
 // operation.
 #include <algorithm>
 #include <cmath>
@@ -137,7 +139,8 @@ __global__ void __launch_bounds__(NT) k_transport(MechView m, TransportView tv, 
         }
         __syncthreads();
         const int K = s_nmaj;
-        // Wilke denominators of the major species (partners: the majors in order)
+        // Wilke denominators of the major species, one thread per species
+        // (partners: the K majors, sequentially in species order)
         for (int r = t; r < K; r += NT) {
             const int k = rows[r];
             double s = 0.0;
@@ -150,30 +153,44 @@ __global__ void __launch_bounds__(NT) k_transport(MechView m, TransportView tv, 
         const double vis = block_sum<NT>(red, S, [&](int k, double q) {
             return x[k] >= thr ? q + (x[k] * mu[k]) / sk[k] : q;
         });
-        // rho D_k: a major species with every other one, the others with the majors
+        // rho D_k. A minor species sums over the K majors: one thread per
+        // species, sequentially in species order. A major species sums over
+        // all S - 1 others: one warp per species, partner m (in species
+        // order) on lane m mod 32, the 32 partials combined by an xor
+        // butterfly (the order of block_sum).
         if (out.rho_d) {
-            for (int r = t; r < S; r += NT) {
-                const int k = rows[r];
-                double d;
-                if (S == 1) {
-                    d = (t15 * fit5(tv.diff, lnT, l2, l3, l4)) / p;
-                } else {
-                    const bool major = r < K;
-                    const int count = major ? S : K;
+            auto finish = [&](int k, double a1, double a2) {
+                a1 = a1 * p;
+                a2 = a2 * ((p * x[k]) / (mmw - m.W[k] * x[k]));
+                out.rho_d[size_t(j) * S + k] = (1.0 / (a1 + a2)) * rho;
+            };
+            auto pair_terms = [&](int k, int i, double& a1, double& a2) {
+                const int64_t q = i < k ? pair_index(S, i, k) : pair_index(S, k, i);
+                const double bd = t15 * fit5(tv.diff + 5 * q, lnT, l2, l3, l4);
+                a1 = a1 + x[i] / bd;
+                a2 = a2 + (x[i] * m.W[i]) / bd;
+            };
+            if (S == 1) {
+                if (t == 0) out.rho_d[size_t(j)] = ((t15 * fit5(tv.diff, lnT, l2, l3, l4)) / p) * rho;
+            } else {
+                for (int r = K + t; r < S; r += NT) {
+                    const int k = rows[r];
                     double a1 = 0.0, a2 = 0.0;
-                    for (int ii = 0; ii < count; ++ii) {
-                        const int i = major ? ii : rows[ii];
-                        if (i == k) continue;
-                        const int64_t q = i < k ? pair_index(S, i, k) : pair_index(S, k, i);
-                        const double bd = t15 * fit5(tv.diff + 5 * q, lnT, l2, l3, l4);
-                        a1 = a1 + x[i] / bd;
-                        a2 = a2 + (x[i] * m.W[i]) / bd;
-                    }
-                    a1 = a1 * p;
-                    a2 = a2 * ((p * x[k]) / (mmw - m.W[k] * x[k]));
-                    d = 1.0 / (a1 + a2);
+                    for (int ii = 0; ii < K; ++ii) pair_terms(k, rows[ii], a1, a2);
+                    finish(k, a1, a2);
                 }
-                out.rho_d[size_t(j) * S + k] = d * rho;
+                const int warp = t >> 5, lane = t & 31;
+                for (int r = warp; r < K; r += NT / 32) {
+                    const int k = rows[r];
+                    double a1 = 0.0, a2 = 0.0;
+                    for (int mi = lane; mi < S - 1; mi += 32) pair_terms(k, mi < k ? mi : mi + 1, a1, a2);
+#pragma unroll
+                    for (int off = 16; off >= 1; off >>= 1) {
+                        a1 = a1 + __shfl_xor_sync(0xffffffffu, a1, off);
+                        a2 = a2 + __shfl_xor_sync(0xffffffffu, a2, off);
+                    }
+                    if (lane == 0) finish(k, a1, a2);
+                }
             }
         }
         if (t == 0) {

@@ -89,13 +89,14 @@ def bdf_point_flops(mech: Mechanism, kinetics_model: int, steps, rhs_calls, jaco
 
 
 # DRAM bytes of one k_source_qss launch per integrated point, from the ncu
-# capture of 1216 points (dram__bytes_read.sum 4,974,848 + dram__bytes_write.sum
-# 488,448 bytes): state in and out plus the per-CTA rate-constant cache.
-QSS_DRAM_BYTES_PER_POINT = (4974848 + 488448) / 1216
-# The same for k_source_bdf with 152 variables, from the capture of 304 points
-# (493,865,984 + 1,199,238,656 bytes): the Jacobian and iteration matrix live in
-# global memory at this size and every factorisation streams them.
-BDF_DRAM_BYTES_PER_POINT = (493865984 + 1199238656) / 304
+# capture of the 4096-point step at 64 threads per point (dram__bytes_read.sum
+# 8,559,872 + dram__bytes_write.sum 823,552 bytes): state in and out plus the
+# per-CTA rate-constant cache.
+QSS_DRAM_BYTES_PER_POINT = (8559872 + 823552) / 4096
+# The same for k_source_bdf with 152 variables, from the capture of 152 points
+# (5,715,968 + 19,849,984 bytes): the LU factors in shared memory, the
+# Jacobian, rates of progress and saved Nordsieck array in a global slice.
+BDF_DRAM_BYTES_PER_POINT = (5715968 + 19849984) / 152
 
 
 def tridiag_flops_per_point() -> float:

@@ -381,10 +381,11 @@ typedef struct {
     /* CvodeTolerances (python/ember/input.py:733-745) */
     double bdf_reltol, bdf_abstol_momentum, bdf_abstol_energy, bdf_abstol_species, bdf_min_step;
     int bdf_max_num_steps;
-    /* threads per grid point of the QSS kernel (one CTA per point): 0 = the
-     * width ember_source_autotune chose for the mechanism, else the default
-     * for its size; or 32, 64, 96, 128, 160, 192, 256. Results do not depend
-     * on it (every reduction runs in one fixed 32-lane order). */
+    /* threads per grid point (one CTA per point): 0 = the width
+     * ember_source_autotune chose for the mechanism, else the default for its
+     * size; or 32, 64, 96, 128, 160, 192, 256 (QSS) / 64, 128, 160, 256 (BDF;
+     * other values give the mechanism's width). Results do not depend on it
+     * (every reduction runs in one fixed 32-lane order). */
     int threads_per_point;
     /* ignition source of SourceSystem::getQdotIgniter (src/sourceSystem.cpp:33-45);
      * ignition_energy == 0 disables it */
@@ -404,16 +405,17 @@ int ember_source_integrate(ember_mech mech, int method, int n_points, const doub
                            const ember_source_options* opts, double* state_out, int* status, int* stats,
                            int mem, void* stream);
 
-/* Autotuner of the QSS launch width: integrates the given points (a sample of
- * the workload; the same arguments as ember_source_integrate) once with every
- * threads-per-point width of EMBER_SOURCE_THREAD_CHOICES, times each run on
- * the stream with CUDA events (after one untimed run), and stores the fastest
- * width in the mechanism handle, where calls whose threads_per_point is 0 pick
- * it up. threads_out: the chosen width; ms_out: [EMBER_SOURCE_N_THREAD_CHOICES]
- * milliseconds per width (0 where the width does not fit) or NULL. The BDF
- * kernel has a single width per mechanism size: method EMBER_SOURCE_BDF
- * returns it without timing. Integration results are identical for every
- * width. */
+/* Autotuner of the source-term launch: integrates the given points (a sample
+ * of the workload; the same arguments as ember_source_integrate) once per
+ * candidate, times each run on the stream with CUDA events (after one untimed
+ * run), and stores the fastest candidate in the mechanism handle, where calls
+ * whose threads_per_point is 0 pick it up. QSS candidates: every width of
+ * EMBER_SOURCE_THREAD_CHOICES. BDF candidates: the widths 64, 128, 160, 256
+ * times every placement of the Jacobian and LU factors that fits (both in
+ * shared memory, the LU factors alone, neither). threads_out: the chosen
+ * width; ms_out: [EMBER_SOURCE_N_THREAD_CHOICES] milliseconds per width (the
+ * best placement for BDF; 0 for widths not tried) or NULL. Integration
+ * results are identical for every candidate. */
 #define EMBER_SOURCE_N_THREAD_CHOICES 7
 #define EMBER_SOURCE_THREAD_CHOICES {32, 64, 96, 128, 160, 192, 256}
 int ember_source_autotune(ember_mech mech, int method, int n_points, const double* state_in, const double* split_const,

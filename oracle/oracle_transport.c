@@ -23,8 +23,10 @@
  * (no reference test holds transport values).
  *
  * Operation order equals the GPU kernel's (ember_gb300/csrc/transport.cu):
- * sums over species in the 32-lane order of oracle_block_sum, sums over
- * partner species sequentially in species order, no FMA contraction.
+ * sums over species, and a major species' diffusion sums over its S - 1
+ * partners, in the 32-lane order of oracle_block_sum (term m on lane m mod 32,
+ * then the xor butterfly); the other per-species sums sequentially in species
+ * order; no FMA contraction.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -56,6 +58,16 @@ static double fit5(const double* c, double x1, double x2, double x3, double x4) 
 /* Sum over k of term[k] in the 32-lane order (term precomputed, plain adds). */
 static double lane_sum(const double* term, int n) { return oracle_block_sum(term, NULL, n, 32); }
 
+/* The xor butterfly that combines 32 lane partials (the GPU's warp shuffle). */
+static double butterfly(double* q) {
+    for (int off = 16; off >= 1; off >>= 1) {
+        double r[32];
+        for (int l = 0; l < 32; ++l) r[l] = q[l] + q[l ^ off];
+        memcpy(q, r, sizeof r);
+    }
+    return q[0];
+}
+
 static double wilke_phi(int S, const double* w4, const double* s8w1, const double* sq, const double* mu,
                         const double* W, int r, int c) {
     if (r >= c) {
@@ -84,6 +96,7 @@ void oracle_transport_eval(const oracle_mech* m, const double* visc_fit, const d
             s8w1[q] = sqrt(8.0) * sqrt(1.0 + m->W[hi] / m->W[lo]);
         }
     double* buf = (double*)malloc(sizeof(double) * 9 * S);
+    int* majors = (int*)malloc(sizeof(int) * (S > 0 ? S : 1));
     double *ym = buf, *cpR = ym + S, *x = cpR + S, *sq = x + S, *mu = sq + S, *lam = mu + S, *sk = lam + S,
            *term = sk + S, *term2 = term + S;
     for (int j = 0; j < n; ++j) {
@@ -121,12 +134,18 @@ void oracle_transport_eval(const oracle_mech* m, const double* visc_fit, const d
         }
         const double s1 = lane_sum(term, S);
         const double s2 = lane_sum(term2, S);
+        /* the major species, in order: every partner list below is a
+         * sequence whose term m goes to lane m mod 32 */
+        int K = 0;
+        for (int k = 0; k < S; ++k)
+            if (x[k] >= thr) majors[K++] = k;
         for (int k = 0; k < S; ++k) {
             double s = 0.0;
-            if (x[k] >= thr) {
-                for (int c = 0; c < S; ++c)
-                    if (x[c] >= thr) s = s + x[c] * wilke_phi(S, w4, s8w1, sq, mu, m->W, k, c);
-            }
+            if (x[k] >= thr)
+                for (int ci = 0; ci < K; ++ci) {
+                    const int c = majors[ci];
+                    s = s + x[c] * wilke_phi(S, w4, s8w1, sq, mu, m->W, k, c);
+                }
             sk[k] = s;
         }
         /* terms of the major species; the others add exact zeros (q + 0 == q for q != -0) */
@@ -138,15 +157,20 @@ void oracle_transport_eval(const oracle_mech* m, const double* visc_fit, const d
                 if (S == 1) {
                     d = (t15 * fit5(diff_fit, lnT, l2, l3, l4)) / p;
                 } else {
+                    /* a major species: term m of its S - 1 partners on lane m mod 32,
+                     * then the butterfly; a minor one: sequentially over the majors */
                     const int major = x[k] >= thr;
-                    double a1 = 0.0, a2 = 0.0;
-                    for (int i = 0; i < S; ++i) {
-                        if (i == k || !(major || x[i] >= thr)) continue;
+                    const int count = major ? S - 1 : K;
+                    double q1[32] = {0.0}, q2[32] = {0.0};
+                    for (int mi = 0; mi < count; ++mi) {
+                        const int i = major ? (mi < k ? mi : mi + 1) : majors[mi];
+                        const int lane = major ? mi % 32 : 0;
                         const long long q = i < k ? pair_index(S, i, k) : pair_index(S, k, i);
                         const double bd = t15 * fit5(diff_fit + 5 * q, lnT, l2, l3, l4);
-                        a1 = a1 + x[i] / bd;
-                        a2 = a2 + (x[i] * m->W[i]) / bd;
+                        q1[lane] = q1[lane] + x[i] / bd;
+                        q2[lane] = q2[lane] + (x[i] * m->W[i]) / bd;
                     }
+                    double a1 = major ? butterfly(q1) : q1[0], a2 = major ? butterfly(q2) : q2[0];
                     a1 = a1 * p;
                     a2 = a2 * ((p * x[k]) / (mmw - m->W[k] * x[k]));
                     d = 1.0 / (a1 + a2);
@@ -161,6 +185,7 @@ void oracle_transport_eval(const oracle_mech* m, const double* visc_fit, const d
         if (viscosity) viscosity[j] = vis;
     }
     free(buf);
+    free(majors);
     free(w4);
     free(s8w1);
 }

@@ -255,8 +255,31 @@ def test_autotune_keeps_the_fastest_width_and_the_results(gpu_lib, small_mech):
     ro, rs, _ = o.integrate(chem.QSS, st, dt, opts)
     np.testing.assert_array_equal(status, rs)
     assert np.array_equal(out, ro)
-    # the BDF kernel has one width per mechanism size: returned untimed
-    bw, bms = autotune(g, BDF, st[:4], dt[:4], opts)
-    assert bw in THREAD_CHOICES and bms == {}
+    # BDF: widths 64/128/160/256 x the matrix placements that fit
+    bw, bms = autotune(g, BDF, st[:16], dt[:16], opts)
+    assert bw in (64, 128, 160, 256) and set(bms) == {64, 128, 160, 256}
     with pytest.raises(L.EmberGpuError):
         integrate_production_terms(g, QSS, st, dt, SourceOptions.defaults(threads_per_point=48))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n_species,n_reactions,seed", [(40, 200, 7), (150, 1000, 150_1000)])
+def test_bdf_results_do_not_depend_on_width_or_matrix_placement(gpu_lib, n_species, n_reactions, seed):
+    # every BDF launch configuration the autotuner can pick gives the oracle's bits
+    import ctypes as C
+    from ember_gb300.source import BDF, autotune
+    m = synthetic_mechanism(n_species=n_species, n_reactions=n_reactions, seed=seed)
+    g, o = GpuMechanism(m), chem.OracleMech(m)
+    st, dt = _states(m, 12, seed=23)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    ro, rs, rst = o.integrate(chem.BDF, st, dt, opts)
+    for width in (64, 128, 160, 256):
+        out, status, stats = integrate_production_terms(g, BDF, st, dt,
+                                                        SourceOptions.defaults(kinetics_model=KINETICS_STANDARD,
+                                                                               threads_per_point=width))
+        np.testing.assert_array_equal(status, rs, err_msg=str(width))
+        assert np.array_equal(out, ro), (width, np.abs(out - ro).max())
+    # the placement the autotuner keeps (it tries every one that fits)
+    autotune(g, BDF, st, dt, opts)
+    out, status, _ = integrate_production_terms(g, BDF, st, dt, opts)
+    assert np.array_equal(out, ro)
