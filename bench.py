@@ -55,6 +55,8 @@ def parse_args():
     p.add_argument("--mech", default="150", choices=["150", "53"],
                    help="source workloads: the 150-species/1000-reaction mechanism or the GRI-3.0-sized "
                         "53-species/325-reaction one")
+    p.add_argument("--no-plain", action="store_true",
+                   help="split workload: skip the plain per-flame GPU path measured beside the batched step")
     p.add_argument("--source", default="qss", choices=["qss", "bdf"],
                    help="split workload: source-term integrator (the C5 sweep names BDF)")
     p.add_argument("--threads", type=int, default=0,
@@ -232,9 +234,8 @@ def run_ours(args):
     # launch width: autotuned on this batch (outside the timed region), or given
     tune_ms = {}
     if args.threads == 0:
-        # QSS: the whole batch; BDF (12 candidates): its first 1024 points
-        k = args.points if method == QSS else min(args.points, 1024)
-        width, tune_ms = autotune(gm, method, st_d[:k], dt_d[:k], opts, stream=stream)
+        # on the whole batch: a sample's makespan need not rank the candidates as the batch's does
+        width, tune_ms = autotune(gm, method, st_d, dt_d, opts, stream=stream)
     else:
         width = args.threads
         opts.threads_per_point = width
@@ -628,6 +629,26 @@ def run_ours_split(args):
         e2e.append(time.perf_counter() - t0)
     clocks = sampler.stop()
     ms = total_ms / args.steps
+    # the plain per-flame GPU path beside it: one solver per flame, stream launches, flames one after another
+    plain_ms = 0.0
+    if not args.no_plain:
+        nv = mech.n_vars
+        off = np.cumsum([0] + [g.n_points for g in grids])
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        for f in range(len(grids)):
+            a, b = off[f], off[f + 1]
+            one = FlameBatchSplitSolver(gm, grids[f:f + 1], SPLIT_DT, method=method, source_options=opts)
+            one.set_state(0.0, state[a:b])
+            one.set_transport(B[a * nv:b * nv], D[a * nv:b * nv])
+            one.set_transport_model(gtr, SPLIT_THRESHOLD, cross_terms=True)
+            one.step(args.warmup, graph=False, stream=stream)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            one.step(args.steps, graph=False, stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            plain_ms += e0.elapsed_time(e1) / args.steps
+            del one
     n_vals = state.size
     flops = (src_flops / args.steps + 4 * roofline.tridiag_flops_per_point() * n_vals
              + float(np.sum(roofline.transport_point_flops(mech.n_species,
@@ -640,7 +661,9 @@ def run_ours_split(args):
         "config": {"workload": split_workload(args, mech), "points": int(len(state)), "flames": len(grids),
                    "points_per_s": len(state) / (ms / 1e3), "l2": "256 MB buffer written between timed steps",
                    "graph": True, "failed_source_points": n_fail_src, "failed_diffusion_systems": n_fail_diff,
-                   "threads_per_point": width, "autotune_ms": {str(k): round(v, 2) for k, v in tune_ms.items()}},
+                   "threads_per_point": width, "autotune_ms": {str(k): round(v, 2) for k, v in tune_ms.items()},
+                   "plain_per_flame_ms": plain_ms if not args.no_plain else None,
+                   "batched_vs_plain_per_flame": plain_ms / ms if not args.no_plain else None},
         "e2e": {"value": 1e3 * sum(e2e) / len(e2e), "unit": "ms", "h2d_bytes_per_step": int(state.nbytes),
                 "d2h_bytes_per_step": int(state.nbytes)},
         # per step: transport, B/D, jCorr (flux, step size, 2 integrator kernels, failure count), 2 cross-term

@@ -28,10 +28,18 @@ namespace ember {
 
 constexpr int kQmax = 5;
 
+// Rows of a Nordsieck-type array stored contiguously: a[j] is row j (n
+// values). Row addresses are computed, so no pointer table sits on the stack.
+struct ZArr {
+    double* base = nullptr;
+    int n = 0;
+    __device__ double* operator[](int j) const { return base + size_t(j) * n; }
+};
+
 // Shared-memory vectors of the BDF integrator (n entries each).
 struct BdfSmem {
-    double* z[kQmax + 2];   // Nordsieck array z_0..z_{q+1}
-    double* zs[kQmax + 1];  // saved array for step retries
+    ZArr z;   // Nordsieck array z_0..z_{q+1}
+    ZArr zs;  // saved array for step retries
     double *acor, *acorp, *ewt, *y, *ft, *bb, *f0, *ycopy, *f1;
     int* piv;
     // shared-memory doubles (zs_smem: the saved array in shared memory)
@@ -41,11 +49,13 @@ struct BdfSmem {
     // zs_global: (kQmax + 1) n doubles of global memory for zs, or null
     __device__ void carve(double* base, int n, double* zs_global = nullptr) {
         double* p = base;
-        for (int j = 0; j <= kQmax + 1; ++j, p += n) z[j] = p;
+        z = ZArr{p, n};
+        p += size_t(kQmax + 2) * n;
         if (zs_global) {
-            for (int j = 0; j <= kQmax; ++j) zs[j] = zs_global + size_t(j) * n;
+            zs = ZArr{zs_global, n};
         } else {
-            for (int j = 0; j <= kQmax; ++j, p += n) zs[j] = p;
+            zs = ZArr{p, n};
+            p += size_t(kQmax + 1) * n;
         }
         acor = p; p += n;
         acorp = p; p += n;
@@ -550,7 +560,7 @@ __device__ int bdf_integrate(BdfPoint<NT>& P, double tf, double t_start, int* st
     auto set_ewt = [&](const double* vec) {
         for (int i = tid; i < n; i += NT) v.ewt[i] = 1.0 / (rtol * fabs(vec[i]) + P.atol(i));
     };
-    auto copy_z = [&](double* const* dst, double* const* src, int q) {
+    auto copy_z = [&](const ZArr& dst, const ZArr& src, int q) {
         for (int j = 0; j <= q; ++j)
             for (int i = tid; i < n; i += NT) dst[j][i] = src[j][i];
     };
@@ -864,7 +874,7 @@ __device__ int bdf_integrate(BdfPoint<NT>& P, double tf, double t_start, int* st
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NT) k_source_bdf(const __grid_constant__ MechView m,
+__global__ void __maxnreg__(168) k_source_bdf(const __grid_constant__ MechView m,
                                                   const __grid_constant__ SourceArgs a, int* counter, const int* order,
                                                   double* kcache, double* jm, size_t jm_stride, int jm_mode) {
     extern __shared__ double smem[];
@@ -991,7 +1001,7 @@ static int launch_bdf_nt(const MechView& m, const SourceArgs& a, int* counter, S
 // transposed solve reuses the LU of I - gamma J. The gradient with respect to
 // ln(multiplier_i) of every reaction is accumulated per point.
 template <int NT>
-__global__ void __launch_bounds__(NT) k_source_bdf_adjoint(const __grid_constant__ MechView m,
+__global__ void __maxnreg__(168) k_source_bdf_adjoint(const __grid_constant__ MechView m,
                                                           const __grid_constant__ SourceArgs a, int* counter,
                                                           double* kcache,
                                                           double* jm, size_t jm_stride, int jm_mode,
@@ -1008,7 +1018,7 @@ __global__ void __launch_bounds__(NT) k_source_bdf_adjoint(const __grid_constant
     P.cachedT = __longlong_as_double(0x7ff8000000000000LL);
     P.tape = nullptr;
     BdfSmem& v = P.v;
-    double* const* zb = v.z;  // adjoint of the Nordsieck array
+    const ZArr zb = v.z;  // adjoint of the Nordsieck array
     const int tid = threadIdx.x;
     const double t_start = a.t_start_dev ? *a.t_start_dev : a.t_start;
     for (;;) {
@@ -1167,7 +1177,7 @@ static int launch_bdf_adjoint_nt(const MechView& m, const SourceArgs& a, int* co
 // Y_k cp_k/(R W_k); then the normalisation Y/sum(Y) is projected out. Also
 // d psi / d ln(multiplier_i) = gq * (-sum_k nu_ki h_k) r_i, per point.
 template <int NT>
-__global__ void __launch_bounds__(NT) k_objective_vjp(const __grid_constant__ MechView m,
+__global__ void __maxnreg__(168) k_objective_vjp(const __grid_constant__ MechView m,
                                                      const __grid_constant__ SourceArgs a, int n_pts,
                                                      const double* __restrict__ state, const double* __restrict__ gq,
                                                      const double* __restrict__ gcp, const double* __restrict__ gT,
