@@ -210,7 +210,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
     from ember_gb300 import _lib
     from ember_gb300 import roofline
-    from ember_gb300.source import GpuMechanism, integrate_production_terms, autotune, QSS, BDF, STATS_WIDTH
+    from ember_gb300.source import GpuMechanism, integrate_production_terms, autotune, tuning, QSS, BDF, STATS_WIDTH
     import ctypes as C
 
     lib = _lib.lib()
@@ -332,7 +332,8 @@ def run_ours(args):
                    "mean_steps_per_point": float(stats[:, 0].mean()),
                    "mean_rhs_calls_per_point": float(stats[:, 1].mean()),
                    "threads_per_point": width or "default for the mechanism size",
-                   "autotune_ms": {str(k): round(v, 2) for k, v in tune_ms.items()}},
+                   "autotune_ms": {str(k): round(v, 2) for k, v in tune_ms.items()},
+                   "tuning": tuning(gm)},
         "e2e": {"value": ws * args.points * args.steps / e2e_s, "unit": "points/s",
                 "h2d_bytes_per_step": int(state.nbytes + dt.nbytes),
                 "d2h_bytes_per_step": int(state.nbytes + status_h.numpy().nbytes + stats_h.numpy().nbytes)},
@@ -568,7 +569,7 @@ def run_ours_split(args):
     if ws > 1:
         torch.distributed.init_process_group("nccl")
     from ember_gb300 import _lib, roofline
-    from ember_gb300.source import GpuMechanism, QSS, BDF, autotune
+    from ember_gb300.source import GpuMechanism, QSS, BDF, autotune, tuning
     from ember_gb300.split import FlameBatchSplitSolver
     mech, grids, state, B, D, rho_u, ju, jb = split_inputs(rank, args.mech)
     opts = source_options(args.kinetics, args.source)
@@ -617,15 +618,15 @@ def run_ours_split(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     n_fail_src, n_fail_diff = solver.failures()
-    # end to end: host state in, one step, host state out
+    # end to end: the last step's state in from the host, one step, the state out to the host
     e2e = []
-    host = np.array(state)
+    host, _ = solver.state()
     for _ in range(args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        solver.set_state(0.0, host)
+        solver.load_state(host)
         solver.step(1, graph=True)
-        out, _ = solver.state()
+        host, _ = solver.state()
         e2e.append(time.perf_counter() - t0)
     clocks = sampler.stop()
     ms = total_ms / args.steps
@@ -662,6 +663,7 @@ def run_ours_split(args):
                    "points_per_s": len(state) / (ms / 1e3), "l2": "256 MB buffer written between timed steps",
                    "graph": True, "failed_source_points": n_fail_src, "failed_diffusion_systems": n_fail_diff,
                    "threads_per_point": width, "autotune_ms": {str(k): round(v, 2) for k, v in tune_ms.items()},
+                   "tuning": tuning(gm),
                    "plain_per_flame_ms": plain_ms if not args.no_plain else None,
                    "batched_vs_plain_per_flame": plain_ms / ms if not args.no_plain else None},
         "e2e": {"value": 1e3 * sum(e2e) / len(e2e), "unit": "ms", "h2d_bytes_per_step": int(state.nbytes),

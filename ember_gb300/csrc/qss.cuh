@@ -49,6 +49,15 @@ struct QssStats {
     int steps, gcount, rcount;
 };
 
+// Integrator state between two steps, for suspending a point after a number
+// of steps and resuming it later (in another launch, with another CTA width):
+// everything the step loop carries from one step to the next.
+struct QssResume {
+    double tn, dt;
+    int steps, gcount, rcount, started;
+};
+constexpr int kQssSuspended = -31;
+
 __device__ __forceinline__ double rsign(double x) { return (x > 0) ? 1.0 : (x < 0) ? -1.0 : 0.0; }
 
 // Pade numerator / denominator of the QSS predictor and corrector.
@@ -58,9 +67,13 @@ __device__ __forceinline__ double pade_an(double r) { return fma(r, fma(r, 11.0 
 
 // enforce(i): whether component i is limited to ymin(i) (QssIntegrator::enforce_ymin / ymin).
 // red: block reduction scratch (kMaxChemThreads + 2 doubles).
+// step_cap > 0: stop before step step_cap + 1 (counted from the first step
+// of the point, across resumptions), save the loop state in *rs and return
+// kQssSuspended. rs with started set: continue from that state.
 template <int NT, class Ode, class Enforce, class Ymin>
 __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, const QssParams& P, Enforce enforce,
-                                                   Ymin ymin, double tf, double tstart, double* red, QssStats& st) {
+                                                   Ymin ymin, double tf, double tstart, double* red, QssStats& st,
+                                                   int step_cap = 0, QssResume* rs = nullptr) {
     const int t0 = threadIdx.x;
     const double tfd = 1.000008;
     const bool stab_on = P.stability_check != 0;
@@ -78,10 +91,23 @@ __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, 
     double tn = 0.0, ts = 0.0, dt = 0.0;
     bool first = true;
     int gcount = 0, rcount = 0, steps = 0;
+    if (rs && rs->started) {
+        tn = rs->tn;
+        dt = rs->dt;
+        first = false;
+        steps = rs->steps;
+        gcount = rs->gcount;
+        rcount = rs->rcount;
+    }
     int ret = 0;
     while (tfd * tn < tf) {
         if (steps >= P.max_steps) {
             ret = -20;
+            break;
+        }
+        if (step_cap > 0 && steps >= step_cap) {
+            ret = kQssSuspended;
+            if (rs && t0 == 0) *rs = QssResume{tn, dt, steps, gcount, rcount, 1};
             break;
         }
         ++steps;

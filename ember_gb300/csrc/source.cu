@@ -225,16 +225,18 @@ __global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView 
     P.stability_check = a.qss_stability_check;
     P.max_steps = a.max_steps;
     const int tid = threadIdx.x;
+    // the points of this launch: the work order, or the suspended points being resumed
+    const int n_work = a.resuming ? *a.susp_n : a.n;
     for (;;) {
         if (tid == 0) {
             const int slot = atomicAdd(counter, 1);
-            next_point = slot < a.n ? order[slot] : a.n;
+            next_point = slot < n_work ? (a.resuming ? a.susp_list[slot] : order[slot]) : a.n;
         }
         __syncthreads();
         const int j = next_point;
         __syncthreads();
         if (j >= a.n) break;
-        const double* yin = a.state_in + size_t(j) * n;
+        const double* yin = (a.resuming ? a.state_out : a.state_in) + size_t(j) * n;
         for (int i = tid; i < n; i += NT) v.y[i] = yin[i];
         ode.split = a.split ? a.split + size_t(j) * n : nullptr;
         ode.x = a.x ? a.x[j] : 0.0;
@@ -242,8 +244,11 @@ __global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView 
         ode.rrho = 1.0;
         ode.rrc = 1.0;
         QssStats st;
+        QssResume rs{};
+        if (a.resuming) rs = a.resume[j];
         int ret = qss_integrate_block<NT>(ode, v, n, P, EnforceNotMomentum(), SourceYmin{a.qss_minval}, a.dt[j],
-                                          a.t_start_dev ? *a.t_start_dev : a.t_start, ode.w.red, st);
+                                          a.t_start_dev ? *a.t_start_dev : a.t_start, ode.w.red, st, a.step_cap,
+                                          a.resume ? &rs : nullptr);
         int nonfinite = 0;
         double* yout = a.state_out + size_t(j) * n;
         for (int i = tid; i < n; i += NT) {
@@ -254,6 +259,10 @@ __global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView 
         nonfinite = __syncthreads_or(nonfinite);
         if (ret == 0 && nonfinite) ret = -21;
         if (tid == 0) {
+            if (ret == kQssSuspended) {
+                a.resume[j] = rs;
+                a.susp_list[atomicAdd(a.susp_n, 1)] = j;
+            }
             a.status[j] = ret;
             if (a.stats) {
                 a.stats[4 * size_t(j) + 0] = st.steps;
@@ -610,10 +619,17 @@ int source_check_options(const ember_source_options* o) {
     EMBER_CHECK_ARG(o->bdf_reltol > 0 && o->bdf_abstol_momentum > 0 && o->bdf_abstol_energy > 0 &&
                         o->bdf_abstol_species > 0 && o->bdf_max_num_steps > 0,
                     "bad BDF tolerances");
-    bool width_ok = o->threads_per_point == 0;
-    for (int c : kQssThreadChoices) width_ok = width_ok || o->threads_per_point == c;
+    bool width_ok = o->threads_per_point == 0, tail_ok = o->qss_tail_threads == 0;
+    for (int c : kQssThreadChoices) {
+        width_ok = width_ok || o->threads_per_point == c;
+        tail_ok = tail_ok || o->qss_tail_threads == c;
+    }
     EMBER_CHECK_ARG(width_ok, "threads_per_point must be 0 or one of 32, 64, 96, 128, 160, 192, 256 (got %d)",
                     o->threads_per_point);
+    EMBER_CHECK_ARG(tail_ok && o->qss_tail_steps >= -1, "bad QSS two-pass schedule (%d steps, %d threads)",
+                    o->qss_tail_steps, o->qss_tail_threads);
+    EMBER_CHECK_ARG(o->qss_tail_steps <= 0 || o->qss_stability_check == 0,
+                    "the QSS two-pass schedule cannot be combined with the stability check");
     return EMBER_OK;
 }
 
@@ -653,6 +669,8 @@ SourceArgs make_source_args(const ember_source_options* o, int n, const double* 
     a.ign_energy = o->ignition_energy;
     a.ign_center = o->ignition_center;
     a.ign_stddev = o->ignition_stddev;
+    a.tail_steps = o->qss_tail_steps;
+    a.tail_threads = o->qss_tail_threads;
     return a;
 }
 
@@ -698,14 +716,27 @@ static int qss_scratch_nt(const MechView& m, const SourceArgs& a, size_t* bytes)
     return EMBER_OK;
 }
 
+// The two-pass schedule of a launch: the requested one (tail_steps < 0: one
+// pass), else the mechanism's.
+static void qss_tail_config(const MechView& m, const SourceArgs& a, int* steps, int* threads) {
+    *steps = a.tail_steps ? a.tail_steps : m.qss_tail_steps;
+    *threads = a.tail_steps ? a.tail_threads : m.qss_tail_threads;
+    if (*threads == 0) *threads = 256;
+    if (*steps < 0 || a.qss_stability_check) *steps = 0;
+}
+
+void source_qss_tail(const MechView& m, const SourceArgs& a, int* steps, int* threads) {
+    qss_tail_config(m, a, steps, threads);
+}
+
 int source_qss_threads(const MechView& m, const SourceArgs& a) {
     if (a.threads) return a.threads;
     if (m.qss_threads) return m.qss_threads;
     return chem_threads_for(m.S);
 }
 
-int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes) {
-    switch (source_qss_threads(m, a)) {
+static int qss_scratch_width(const MechView& m, const SourceArgs& a, int width, size_t* bytes) {
+    switch (width) {
         case 32: return qss_scratch_nt<32>(m, a, bytes);
         case 64: return qss_scratch_nt<64>(m, a, bytes);
         case 96: return qss_scratch_nt<96>(m, a, bytes);
@@ -714,6 +745,19 @@ int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* byt
         case 192: return qss_scratch_nt<192>(m, a, bytes);
         default: return qss_scratch_nt<256>(m, a, bytes);
     }
+}
+
+int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes) {
+    EMBER_TRY(qss_scratch_width(m, a, source_qss_threads(m, a), bytes));
+    int tail_steps = 0, tail_threads = 0;
+    qss_tail_config(m, a, &tail_steps, &tail_threads);
+    if (tail_steps) {
+        size_t second = 0;
+        EMBER_TRY(qss_scratch_width(m, a, tail_threads, &second));
+        *bytes += second + Scratch::rounded(sizeof(QssResume) * size_t(a.n)) +
+                  Scratch::rounded(sizeof(int) * size_t(a.n)) + Scratch::rounded(sizeof(int));
+    }
+    return EMBER_OK;
 }
 
 template <int NT>
@@ -730,14 +774,9 @@ static int launch_qss_nt(const MechView& m, const SourceArgs& a, int* counter, S
     return EMBER_OK;
 }
 
-static int cuda_check(cudaError_t e, const char* what) {
-    if (e == cudaSuccess) return EMBER_OK;
-    set_error("%s failed: %s", what, cudaGetErrorString(e));
-    return EMBER_ECUDA;
-}
-
-int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
-    switch (source_qss_threads(m, a)) {
+static int launch_qss_width(const MechView& m, const SourceArgs& a, int width, int* counter, Scratch& sc,
+                            cudaStream_t st) {
+    switch (width) {
         case 32: return launch_qss_nt<32>(m, a, counter, sc, st);
         case 64: return launch_qss_nt<64>(m, a, counter, sc, st);
         case 96: return launch_qss_nt<96>(m, a, counter, sc, st);
@@ -746,6 +785,37 @@ int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, Scra
         case 192: return launch_qss_nt<192>(m, a, counter, sc, st);
         default: return launch_qss_nt<256>(m, a, counter, sc, st);
     }
+}
+
+static int cuda_check(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return EMBER_OK;
+    set_error("%s failed: %s", what, cudaGetErrorString(e));
+    return EMBER_ECUDA;
+}
+
+// One launch over all points, or the two-pass schedule: every point runs at
+// the chosen width for at most tail_steps steps; the points still running are
+// suspended (their state in state_out and a QssResume each) and continued,
+// after the others, by a second launch at tail_threads threads per point. A
+// point's steps and arithmetic are the same either way; only where and when
+// they run changes. The suspended-point count stays on the device, so both
+// passes can be captured in a graph.
+int launch_source_qss(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
+    int tail_steps = 0, tail_threads = 0;
+    qss_tail_config(m, a, &tail_steps, &tail_threads);
+    if (tail_steps == 0) return launch_qss_width(m, a, source_qss_threads(m, a), counter, sc, st);
+    SourceArgs a1 = a;
+    a1.step_cap = tail_steps;
+    EMBER_TRY(sc.alloc(&a1.resume, size_t(a.n)));
+    EMBER_TRY(sc.alloc(&a1.susp_list, size_t(a.n)));
+    EMBER_TRY(sc.alloc(&a1.susp_n, 1));
+    EMBER_CUDA_TRY(cudaMemsetAsync(a1.susp_n, 0, sizeof(int), st));
+    EMBER_TRY(launch_qss_width(m, a1, source_qss_threads(m, a), counter, sc, st));
+    SourceArgs a2 = a1;
+    a2.step_cap = 0;
+    a2.resuming = 1;
+    EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
+    return launch_qss_width(m, a2, tail_threads, counter, sc, st);
 }
 
 }  // namespace ember
@@ -844,6 +914,7 @@ extern "C" int ember_source_autotune(ember_mech m, int method, int n, const doub
             if (bdf && !source_bdf_layout_fits(m->view, layout)) continue;
             ember_source_options o = *opts;
             o.threads_per_point = width;
+            o.qss_tail_steps = -1;  // one pass while the widths are compared
             SourceArgs a = make_source_args(&o, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, nullptr);
             a.bdf_layout = layout;
             float ms = 0.0f;
@@ -867,11 +938,64 @@ extern "C" int ember_source_autotune(ember_mech m, int method, int n, const doub
             }
         }
     }
+    // QSS: two-pass schedules around the best width, the cap at the 50th / 75th /
+    // 90th percentile of the points' step counts, the tail on 128 or 256 threads
+    int best_tail = 0, best_tail_threads = 0;
+    if (!bdf && rc == EMBER_OK && !opts->qss_stability_check) {
+        int* d_stats = nullptr;
+        rc = sc.alloc(&d_stats, size_t(n) * EMBER_STATS_WIDTH);
+        ember_source_options o = *opts;
+        o.threads_per_point = best;
+        o.qss_tail_steps = -1;
+        SourceArgs a = make_source_args(&o, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, d_stats);
+        if (rc == EMBER_OK) {
+            Scratch work(st);
+            rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), st), "cudaMemsetAsync");
+            if (rc == EMBER_OK) rc = launch_source_qss(m->view, a, counter, work, st);
+        }
+        std::vector<int> stats(size_t(n) * EMBER_STATS_WIDTH);
+        if (rc == EMBER_OK)
+            rc = cuda_check(cudaMemcpyAsync(stats.data(), d_stats, sizeof(int) * stats.size(), cudaMemcpyDeviceToHost, st),
+                            "cudaMemcpyAsync");
+        if (rc == EMBER_OK) rc = cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+        std::vector<int> steps(n);
+        for (int j = 0; j < n; ++j) steps[j] = stats[size_t(j) * EMBER_STATS_WIDTH];
+        std::sort(steps.begin(), steps.end());
+        for (double pct : {0.5, 0.75, 0.9}) {
+            const int cap = std::max(1, steps[std::min(n - 1, int(pct * n))]);
+            for (int tw : {128, 256}) {
+                if (rc != EMBER_OK) break;
+                ember_source_options ot = o;
+                ot.qss_tail_steps = cap;
+                ot.qss_tail_threads = tw;
+                SourceArgs at = make_source_args(&ot, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, nullptr);
+                float ms = 0.0f;
+                for (int rep = 0; rep < 2 && rc == EMBER_OK; ++rep) {
+                    Scratch work(st);
+                    rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), st), "cudaMemsetAsync");
+                    if (rc == EMBER_OK) rc = cuda_check(cudaEventRecord(e0, st), "cudaEventRecord");
+                    if (rc == EMBER_OK) rc = launch_source_qss(m->view, at, counter, work, st);
+                    if (rc == EMBER_OK) rc = cuda_check(cudaEventRecord(e1, st), "cudaEventRecord");
+                    if (rc == EMBER_OK) rc = cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+                    if (rc == EMBER_OK) rc = cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+                }
+                if (rc == EMBER_OK && ms < best_ms) {
+                    best_ms = ms;
+                    best_tail = cap;
+                    best_tail_threads = tw;
+                }
+            }
+        }
+    }
     cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     sc.release();
     EMBER_TRY(rc);
     EMBER_TRY(finish_call(EMBER_MEM_DEVICE, st));
+    if (!bdf) {
+        m->view.qss_tail_steps = best_tail;
+        m->view.qss_tail_threads = best_tail_threads;
+    }
     if (bdf) {
         m->view.bdf_threads = best;
         m->view.bdf_layout = best_layout;
@@ -879,6 +1003,21 @@ extern "C" int ember_source_autotune(ember_mech m, int method, int n, const doub
         m->view.qss_threads = best;
     }
     *threads_out = best;
+    return EMBER_OK;
+}
+
+extern "C" int ember_mech_get_tuning(ember_mech m, int* qss_threads, int* qss_tail_steps, int* qss_tail_threads,
+                                     int* bdf_threads, int* bdf_layout) {
+    EMBER_CHECK_ARG(m != nullptr, "null mechanism");
+    if (qss_threads) *qss_threads = m->view.qss_threads;
+    if (qss_tail_steps) *qss_tail_steps = m->view.qss_tail_steps;
+    if (qss_tail_threads) *qss_tail_threads = m->view.qss_tail_threads;
+    if (bdf_threads) *bdf_threads = m->view.bdf_threads;
+    if (bdf_layout) {
+        // BdfLayout modes (bdf.cu): 0 global, 1 both in shared memory, 2 LU only -> 3, 1, 2
+        const int l = m->view.bdf_layout;
+        *bdf_layout = l == 0 ? 0 : (l == 1 ? 3 : (l == 2 ? 1 : 2));
+    }
     return EMBER_OK;
 }
 

@@ -37,6 +37,15 @@ struct SourceArgs {
     double* tape;
     int64_t tape_stride;
     int tape_cap;
+    // QSS two-pass schedule (see launch_source_qss): suspend after step_cap
+    // steps into resume[j], listing the point in susp_list; a resuming launch
+    // takes its points from work_list (susp_n of them) and continues them.
+    int step_cap;
+    int resuming;
+    QssResume* resume;
+    int* susp_list;
+    int* susp_n;
+    int tail_steps, tail_threads;  // requested (0: the mechanism's tuned values)
 };
 
 // Tape header: accepted steps recorded, order after the last step, t after
@@ -93,6 +102,8 @@ int source_check_options(const ember_source_options* o);
 int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes);
 // Threads per point of the QSS kernel for these arguments (see threads_per_point).
 int source_qss_threads(const MechView& m, const SourceArgs& a);
+// Two-pass schedule of the QSS kernel for these arguments (steps 0: one pass).
+void source_qss_tail(const MechView& m, const SourceArgs& a, int* steps, int* threads);
 int source_bdf_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes);
 // Threads per point and matrix layout (1 + BDF_* of bdf.cu) of the BDF kernel for these arguments.
 int source_bdf_threads(const MechView& m, const SourceArgs& a);

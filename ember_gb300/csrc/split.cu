@@ -826,6 +826,10 @@ extern "C" int ember_split_create(ember_mech mech, int n_flames, const ember_dif
     // the mechanism is tuned again later
     if (opts->method == EMBER_SOURCE_QSS) {
         h->opt.source.threads_per_point = source_qss_threads(mech->view, probe);
+        int tail_steps = 0, tail_threads = 0;
+        source_qss_tail(mech->view, probe, &tail_steps, &tail_threads);
+        h->opt.source.qss_tail_steps = tail_steps ? tail_steps : -1;
+        h->opt.source.qss_tail_threads = tail_steps ? tail_threads : 0;
     } else {
         h->opt.source.threads_per_point = source_bdf_threads(mech->view, probe);
         h->bdf_layout = source_bdf_layout(mech->view, probe);
@@ -924,6 +928,14 @@ extern "C" int ember_split_set_state(ember_split h, double t, const double* stat
     // the host value of t must outlive the copy
     EMBER_CUDA_TRY(cudaStreamSynchronize(st));
     return EMBER_OK;
+}
+
+extern "C" int ember_split_load_state(ember_split h, const double* state, int mem, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(state != nullptr, "null state");
+    cudaStream_t st = as_stream(stream);
+    EMBER_TRY(copy_to_device(h->state, state, size_t(h->n_vals), mem, st));
+    return finish_call(mem, st);
 }
 
 extern "C" int ember_split_set_transport(ember_split h, const double* B, const double* D, const double* ddt_cross,

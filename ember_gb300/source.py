@@ -37,6 +37,7 @@ class SourceOptions(C.Structure):
         ("threads_per_point", C.c_int),
         ("ignition_tstart", C.c_double), ("ignition_duration", C.c_double), ("ignition_energy", C.c_double),
         ("ignition_center", C.c_double), ("ignition_stddev", C.c_double),
+        ("qss_tail_steps", C.c_int), ("qss_tail_threads", C.c_int),
     ]
 
     @classmethod
@@ -53,6 +54,7 @@ class SourceOptions(C.Structure):
         o.ignition_tstart, o.ignition_duration, o.ignition_energy = 0.0, 1e-3, 0.0
         o.ignition_center, o.ignition_stddev = 0.0, 1e-4
         o.threads_per_point = 0  # the mechanism's autotuned width, else the default for its size
+        o.qss_tail_steps, o.qss_tail_threads = 0, 0  # the mechanism's autotuned schedule, else one pass
         for k, v in kw.items():
             if not hasattr(o, k):
                 raise AttributeError(k)
@@ -127,6 +129,14 @@ def autotune(gmech: GpuMechanism, method: int, state, dt, opts: SourceOptions | 
                                           float(t_start), L.ptr(x), C.byref(opts), C.byref(width), ms, mem,
                                           L.stream_ptr(stream)), "ember_source_autotune")
     return width.value, {c: ms[i] for i, c in enumerate(THREAD_CHOICES) if ms[i] > 0}
+
+
+def tuning(gmech: GpuMechanism) -> dict:
+    """The launch configuration ember_source_autotune stored in the mechanism."""
+    v = [C.c_int() for _ in range(5)]
+    L.check(L.lib().ember_mech_get_tuning(gmech.handle, *(C.byref(x) for x in v)), "ember_mech_get_tuning")
+    keys = ("qss_threads", "qss_tail_steps", "qss_tail_threads", "bdf_threads", "bdf_layout")
+    return {k: x.value for k, x in zip(keys, v)}
 
 
 def integrate_production_terms(gmech: GpuMechanism, method: int, state, dt, opts: SourceOptions | None = None,

@@ -117,6 +117,11 @@ class FlameBatchSplitSolver:
         a, mem = self._arr(state, (self.n_points, self.n_vars))
         L.check(_lib().ember_split_set_state(self._h, float(t), L.ptr(a), mem, None), "ember_split_set_state")
 
+    def load_state(self, state, stream=None):
+        """ember_split_load_state: new state values, same time and split history."""
+        a, mem = self._arr(state, (self.n_points, self.n_vars))
+        L.check(_lib().ember_split_load_state(self._h, L.ptr(a), mem, L.stream_ptr(stream)), "ember_split_load_state")
+
     def set_transport(self, B, D, ddt_cross=None, stream=None):
         n = self.n_points * self.n_vars
         b, mem = self._arr(B, (n,))

@@ -390,6 +390,13 @@ typedef struct {
     /* ignition source of SourceSystem::getQdotIgniter (src/sourceSystem.cpp:33-45);
      * ignition_energy == 0 disables it */
     double ignition_tstart, ignition_duration, ignition_energy, ignition_center, ignition_stddev;
+    /* QSS two-pass schedule: 0 = the mechanism's tuned schedule (none unless
+     * ember_source_autotune found one faster). qss_tail_steps > 0: points
+     * still running after that many steps are suspended and resumed, after
+     * the others, on CTAs of qss_tail_threads threads (0: 256), so that the
+     * stiffest points finish sooner. Results do not depend on it. Not with
+     * qss_stability_check. */
+    int qss_tail_steps, qss_tail_threads;
 } ember_source_options;
 
 /* Fill `opts` with the reference's defaults (pressure 1 atm, interp kinetics). */
@@ -421,6 +428,13 @@ int ember_source_integrate(ember_mech mech, int method, int n_points, const doub
 int ember_source_autotune(ember_mech mech, int method, int n_points, const double* state_in, const double* split_const,
                           const double* dt, double t_start, const double* x, const ember_source_options* opts,
                           int* threads_out, double* ms_out, int mem, void* stream);
+
+/* The launch configuration stored in the mechanism by ember_source_autotune
+ * (0 where none was chosen): QSS width, QSS two-pass steps and tail width,
+ * BDF width, BDF matrix placement (1: J and LU in shared memory, 2: LU
+ * only, 3: neither). */
+int ember_mech_get_tuning(ember_mech mech, int* qss_threads, int* qss_tail_steps, int* qss_tail_threads,
+                          int* bdf_threads, int* bdf_layout);
 
 /* Discrete adjoint of a BDF source-term integration (EMBER_SOURCE_BDF, same
  * arguments as ember_source_integrate): for phi = sum over points of
@@ -503,6 +517,10 @@ int ember_split_destroy(ember_split split);
 /* State at time t; resets the time derivatives (and so the split
  * constants of the next step) and the failure counters. */
 int ember_split_set_state(ember_split split, double t, const double* state, int mem, void* stream);
+/* Replace the state values only: the time, the time derivatives (the next
+ * step's split constants) and the failure counters are kept, as when a caller
+ * that holds the state on the host hands back the state of the last step. */
+int ember_split_load_state(ember_split split, const double* state, int mem, void* stream);
 /* B, D: variable-major per flame; ddt_cross: point-major or NULL (zero). */
 int ember_split_set_transport(ember_split split, const double* B, const double* D, const double* ddt_cross,
                               int mem, void* stream);

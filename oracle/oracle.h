@@ -93,6 +93,7 @@ typedef struct {
     int bdf_max_num_steps;
     int threads_per_point; /* launch width of the GPU kernel; no effect here */
     double ignition_tstart, ignition_duration, ignition_energy, ignition_center, ignition_stddev;
+    int qss_tail_steps, qss_tail_threads; /* GPU schedule; no effect here */
 } oracle_source_options;
 
 /* QSS integrator on any q/d right-hand side (QssOde::odefun). */

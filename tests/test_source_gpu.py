@@ -283,3 +283,30 @@ def test_bdf_results_do_not_depend_on_width_or_matrix_placement(gpu_lib, n_speci
     autotune(g, BDF, st, dt, opts)
     out, status, _ = integrate_production_terms(g, BDF, st, dt, opts)
     assert np.array_equal(out, ro)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("big", [False, True])
+def test_qss_two_pass_schedule_gives_the_same_bits(gpu_lib, small_mech, big_mech, big):
+    # points suspended after a few steps and resumed on wider CTAs reproduce
+    # the one-pass integration (and the oracle) exactly, statistics included
+    from ember_gb300.source import autotune, tuning
+    m = big_mech if big else small_mech
+    g, o = GpuMechanism(m), chem.OracleMech(m)
+    st, dt = _states(m, 40, seed=31)
+    base = dict(kinetics_model=KINETICS_INTERP)
+    ro, rs, rst = o.integrate(chem.QSS, st, dt, SourceOptions.defaults(**base))
+    for cap, tw in ((1, 256), (5, 128), (20, 32)):
+        out, status, stats = integrate_production_terms(
+            g, QSS, st, dt, SourceOptions.defaults(qss_tail_steps=cap, qss_tail_threads=tw, **base))
+        np.testing.assert_array_equal(status, rs, err_msg=str(cap))
+        assert np.array_equal(out, ro), (cap, np.abs(out - ro).max())
+        np.testing.assert_array_equal(stats[:, :3], rst[:, :3])
+    # whatever schedule the autotuner keeps
+    autotune(g, QSS, st, dt, SourceOptions.defaults(**base))
+    t = tuning(g)
+    assert t["qss_threads"] in (32, 64, 96, 128, 160, 192, 256)
+    out, status, _ = integrate_production_terms(g, QSS, st, dt, SourceOptions.defaults(**base))
+    assert np.array_equal(out, ro)
+    with pytest.raises(L.EmberGpuError):
+        integrate_production_terms(g, QSS, st, dt, SourceOptions.defaults(qss_tail_steps=5, qss_stability_check=1))

@@ -249,3 +249,23 @@ def test_split_transport_model_parallel_diffusion_close_to_oracle(gpu_lib, mech)
     scale = np.abs(ref).max(axis=0)
     err = (np.abs(out - ref) / np.where(scale > 0, scale, 1.0)).max()
     assert err <= 1e-9, err
+
+
+@pytest.mark.gpu
+def test_load_state_keeps_time_and_split_history(gpu_lib, mech):
+    grids, state, B, D, rho_u, ju, jb = _case(mech, n_flames=2, n_min=12, n_max=20)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    gm, a = _gpu_solver(mech, grids, 2e-6, QSS, opts, L.DIFFUSION_SERIAL)
+    a.set_state(0.0, state)
+    a.set_transport(B, D)
+    a.step(2)
+    _, b = _gpu_solver(mech, grids, 2e-6, QSS, opts, L.DIFFUSION_SERIAL)
+    b.set_state(0.0, state)
+    b.set_transport(B, D)
+    b.step(1)
+    mid, _ = b.state()
+    b.load_state(mid)   # a host round trip of the state between steps
+    b.step(1)
+    (sa, ta), (sb, tb) = a.state(), b.state()
+    assert ta == tb and np.array_equal(sa, sb)
+    assert all(np.array_equal(x, y) for x, y in zip(a.derivatives(), b.derivatives()))
