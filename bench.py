@@ -125,6 +125,17 @@ def dist_info():
     return ws, rank, local
 
 
+def max_over_ranks(value: float, ws: int, device) -> float:
+    """The largest value over the ranks (each rank's timed total; replicas
+    finish when the slowest does)."""
+    if ws <= 1:
+        return value
+    import torch
+    t = torch.tensor([value], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload_inputs(n_points: int, rank: int, mech_size: str = "150"):
     from ember_gb300.mechanism import synthetic_mechanism, reactor_states
     if mech_size == "53":
@@ -268,10 +279,7 @@ def run_ours(args):
     wall = time.perf_counter() - w0
     kernel_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = sum(kernel_ms)
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, ws, dev)
 
     # end to end through the public API with pinned host buffers (copies inside the call)
     st_h = torch.as_tensor(state).pin_memory()
@@ -295,10 +303,7 @@ def run_ours(args):
         step_host()
         e2e_times.append(time.perf_counter() - t0)
     e2e_s = sum(e2e_times)
-    if ws > 1:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(e2e_s, ws, dev)
     clocks = sampler.stop()
 
     status = status_d.cpu().numpy()
@@ -441,10 +446,7 @@ def run_ours_diffusion(args):
         ends[i].record(stream)
     torch.cuda.synchronize()
     total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, ws, dev)
     # end to end with host arrays (copies inside the call)
     Yh = Y.copy()
     e2e = []
@@ -613,10 +615,7 @@ def run_ours_split(args):
             src_flops += float(roofline.bdf_point_flops(mech, opts.kinetics_model, stats[:, 0], stats[:, 1],
                                                         stats[:, 3]).sum())
     total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, ws, dev)
     n_fail_src, n_fail_diff = solver.failures()
     # end to end: the last step's state in from the host, one step, the state out to the host
     e2e = []
@@ -924,10 +923,7 @@ def run_ours_transport(args):
         ends[i].record(stream)
     torch.cuda.synchronize()
     total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    if ws > 1:
-        t = torch.tensor([total_ms], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, ws, dev)
     # end to end: host states in, properties out
     T_h, Y_h = np.ascontiguousarray(state[:, 1]), np.ascontiguousarray(state[:, 2:])
     e2e = []
