@@ -119,15 +119,16 @@ def qss_cesium(y0, tf, epsmin, itermax=5, epsmax=20.0, dtmin=1e-15, dtmax=1e300,
     return y, r, stats
 
 
-def transport_eval(om: OracleMech, data, T, Y, pressure=101325.0, threshold=1e-5):
+def transport_eval(om: OracleMech, data, T, Y, pressure=101325.0, threshold=1e-5, n_threads=1):
     """The oracle's thermo and mixture-averaged transport properties
     (oracle_transport.c) of the states T [n], Y [n, S], with the fits of a
-    ember_gb300.transport.TransportData."""
+    ember_gb300.transport.TransportData; n_threads > 1 splits the points."""
     l = _lib()
     if not getattr(l, "_transport_declared", False):
         vp = C.c_void_p
-        l.oracle_transport_eval.argtypes = [vp, vp, vp, vp, C.c_int, C.c_double, C.c_double, vp, vp] + [vp] * 8
-        l.oracle_transport_eval.restype = None
+        l.oracle_transport_eval_threads.argtypes = ([vp, vp, vp, vp, C.c_int, C.c_double, C.c_double, vp, vp]
+                                                    + [vp] * 8 + [C.c_int])
+        l.oracle_transport_eval_threads.restype = None
         l._transport_declared = True
     T = np.ascontiguousarray(np.atleast_1d(T), dtype=np.float64)
     n, S = T.size, om.S
@@ -136,7 +137,8 @@ def transport_eval(om: OracleMech, data, T, Y, pressure=101325.0, threshold=1e-5
     out = {"density": np.empty(n), "mean_mol_weight": np.empty(n), "cp_mass": np.empty(n),
            "cp_species": np.empty((n, S)), "h_species": np.empty((n, S)), "conductivity": np.empty(n),
            "viscosity": np.empty(n), "rho_d": np.empty((n, S))}
-    l.oracle_transport_eval(om._h, *(_p(f) for f in fits), n, float(pressure), float(threshold), _p(T), _p(Y),
-                            *(_p(out[k]) for k in ("density", "mean_mol_weight", "cp_mass", "cp_species",
-                                                   "h_species", "conductivity", "viscosity", "rho_d")))
+    l.oracle_transport_eval_threads(om._h, *(_p(f) for f in fits), n, float(pressure), float(threshold), _p(T),
+                                    _p(Y), *(_p(out[k]) for k in ("density", "mean_mol_weight", "cp_mass",
+                                                                  "cp_species", "h_species", "conductivity",
+                                                                  "viscosity", "rho_d")), int(n_threads))
     return out

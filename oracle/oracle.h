@@ -134,6 +134,11 @@ void oracle_transport_eval(const oracle_mech* m, const double* visc_fit, const d
                            const double* diff_fit, int n, double p, double thr, const double* T, const double* Y,
                            double* density, double* mean_mw, double* cp_mass, double* cp_species, double* h_species,
                            double* conductivity, double* viscosity, double* rho_d);
+void oracle_transport_eval_threads(const oracle_mech* m, const double* visc_fit, const double* cond_fit,
+                                   const double* diff_fit, int n, double p, double thr, const double* T,
+                                   const double* Y, double* density, double* mean_mw, double* cp_mass,
+                                   double* cp_species, double* h_species, double* conductivity, double* viscosity,
+                                   double* rho_d, int n_threads);
 
 #ifdef __cplusplus
 }

@@ -189,3 +189,49 @@ void oracle_transport_eval(const oracle_mech* m, const double* visc_fit, const d
     free(w4);
     free(s8w1);
 }
+
+/* ---- threaded batch (CPU baseline): contiguous ranges of points per thread */
+
+#include <pthread.h>
+
+typedef struct {
+    const oracle_mech* m;
+    const double *visc, *cond, *diff, *T, *Y;
+    double p, thr;
+    int j0, j1;
+    double *density, *mean_mw, *cp_mass, *cp_species, *h_species, *conductivity, *viscosity, *rho_d;
+} transport_job;
+
+static void* transport_worker(void* arg) {
+    const transport_job* J = (const transport_job*)arg;
+    const int S = J->m->S, j0 = J->j0, n = J->j1 - J->j0;
+#define OFF1(a) ((a) ? (a) + j0 : NULL)
+#define OFFS(a) ((a) ? (a) + (size_t)j0 * S : NULL)
+    oracle_transport_eval(J->m, J->visc, J->cond, J->diff, n, J->p, J->thr, J->T + j0, J->Y + (size_t)j0 * S,
+                          OFF1(J->density), OFF1(J->mean_mw), OFF1(J->cp_mass), OFFS(J->cp_species),
+                          OFFS(J->h_species), OFF1(J->conductivity), OFF1(J->viscosity), OFFS(J->rho_d));
+#undef OFF1
+#undef OFFS
+    return NULL;
+}
+
+void oracle_transport_eval_threads(const oracle_mech* m, const double* visc_fit, const double* cond_fit,
+                                   const double* diff_fit, int n, double p, double thr, const double* T,
+                                   const double* Y, double* density, double* mean_mw, double* cp_mass,
+                                   double* cp_species, double* h_species, double* conductivity, double* viscosity,
+                                   double* rho_d, int n_threads) {
+    if (n_threads < 1) n_threads = 1;
+    if (n_threads > n) n_threads = n > 0 ? n : 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * n_threads);
+    transport_job* jobs = (transport_job*)malloc(sizeof(transport_job) * n_threads);
+    for (int t = 0; t < n_threads; ++t) {
+        transport_job J = {m, visc_fit, cond_fit, diff_fit, T, Y, p, thr, (int)((long long)n * t / n_threads),
+                           (int)((long long)n * (t + 1) / n_threads), density, mean_mw, cp_mass, cp_species,
+                           h_species, conductivity, viscosity, rho_d};
+        jobs[t] = J;
+        pthread_create(&th[t], NULL, transport_worker, &jobs[t]);
+    }
+    for (int t = 0; t < n_threads; ++t) pthread_join(th[t], NULL);
+    free(jobs);
+    free(th);
+}

@@ -154,3 +154,12 @@ def test_gpu_transport_device_memory_and_gas_eval_agree(gpu_lib, mech, tdata):
     np.testing.assert_array_equal(host["cp_mass"], ge["cp_mass"])
     np.testing.assert_array_equal(host["h_species"], ge["hk"])
     assert g.eval(T[:0], Y[:0])["density"].shape == (0,)
+
+
+def test_oracle_threads_give_the_same_bits(mech, tdata):
+    T, Y = _states(mech, 23, seed=8)
+    om = chem.OracleMech(mech)
+    one = chem.transport_eval(om, tdata, T, Y, 101325.0, 1e-5, n_threads=1)
+    many = chem.transport_eval(om, tdata, T, Y, 101325.0, 1e-5, n_threads=5)
+    for k in KEYS:
+        assert np.array_equal(one[k], many[k], equal_nan=True), k
