@@ -854,15 +854,21 @@ def transport_inputs(rank: int):
 
 
 def _transport_cpu_rate(mech, td, state, target_s: float, threads: int = 1):
+    """States/s of the threaded oracle: a growing prefix of the states, then
+    repeats of all of them, until the sample takes a quarter of target_s."""
     from oracle import chem
     om = chem.OracleMech(mech)
-    n, t = 8 * threads, 0.0
+    n = 8 * threads
     while True:
-        t0 = time.perf_counter()
-        chem.transport_eval(om, td, state[:n, 1], state[:n, 2:], 101325.0, SPLIT_THRESHOLD, n_threads=threads)
-        t = time.perf_counter() - t0
+        reps, t0 = 0, time.perf_counter()
+        while True:
+            chem.transport_eval(om, td, state[:n, 1], state[:n, 2:], 101325.0, SPLIT_THRESHOLD, n_threads=threads)
+            reps += 1
+            t = time.perf_counter() - t0
+            if n < len(state) or t > target_s / 4:
+                break
         if t > target_s / 4 or n >= len(state):
-            return n / t, n, t
+            return n * reps / t, n * reps, t
         n = min(len(state), n * 4)
 
 
@@ -881,7 +887,7 @@ def run_reference_transport(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": TRANSPORT_WORKLOAD, "points": TRANSPORT_POINTS},
         "cpu_baseline": {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
-                         "sample": f"first {rates[0][1]} states per step, {threads} threads"},
+                         "sample": f"{rates[0][1]} state evaluations per step, {threads} threads"},
         "e2e": {"value": rate, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
     return 0
 
@@ -963,7 +969,7 @@ def run_ours_transport(args):
         threads = os.cpu_count() or 1
         rate, ns, t = _transport_cpu_rate(mech, td, state, args.cpu_seconds, threads)
         line["cpu_baseline"] = {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
-                                "sample": f"first {ns} states, {t:.1f} s on {threads} threads"}
+                                "sample": f"{ns} state evaluations, {t:.1f} s on {threads} threads"}
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:

@@ -86,7 +86,7 @@ def _declare(lib):
         "ember_transport_eval": (C.c_int, [vp, C.c_int, C.c_double, C.c_double, vp, vp, vp, C.c_int, vp]),
         "ember_split_set_transport_model": (C.c_int, [vp, vp, C.c_double, C.c_int]),
         "ember_split_load_state": (C.c_int, [vp, vp, C.c_int, vp]),
-        "ember_mech_get_tuning": (C.c_int, [vp, vp, vp, vp, vp, vp]),
+        "ember_mech_get_tuning": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

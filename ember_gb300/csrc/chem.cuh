@@ -67,6 +67,7 @@ struct MechView {
     int bdf_threads;      // BDF launch width chosen by ember_source_autotune (0: none)
     int bdf_layout;       // BDF matrix layout chosen by ember_source_autotune (0: by size, else 1 + layout)
     int qss_tail_steps, qss_tail_threads;  // QSS two-pass schedule chosen by ember_source_autotune (0: none)
+    int qss_chunk;        // QSS work-queue granularity chosen by ember_source_autotune (0: 1)
     int n_tb, n_fo;       // reactions with [M] (three-body and falloff); falloff reactions
     double Tmin, Tmax;
     const double* W;      // [S]

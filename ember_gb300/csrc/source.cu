@@ -226,11 +226,19 @@ __global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView 
     P.max_steps = a.max_steps;
     const int tid = threadIdx.x;
     // the points of this launch: the work order, or the suspended points being resumed
+    // Queue granularity: a CTA claims `chunk` consecutive slots of the order per atomic.
     const int n_work = a.resuming ? *a.susp_n : a.n;
+    const int chunk = a.queue_chunk > 1 ? a.queue_chunk : 1;
+    int slot = 0, left = 0;  // thread 0's current claim
     for (;;) {
         if (tid == 0) {
-            const int slot = atomicAdd(counter, 1);
+            if (left == 0) {
+                slot = atomicAdd(counter, chunk);
+                left = chunk;
+            }
             next_point = slot < n_work ? (a.resuming ? a.susp_list[slot] : order[slot]) : a.n;
+            ++slot;
+            --left;
         }
         __syncthreads();
         const int j = next_point;
@@ -671,6 +679,7 @@ SourceArgs make_source_args(const ember_source_options* o, int n, const double* 
     a.ign_stddev = o->ignition_stddev;
     a.tail_steps = o->qss_tail_steps;
     a.tail_threads = o->qss_tail_threads;
+    a.queue_chunk = 0;  // the mechanism's tuned granularity
     return a;
 }
 
@@ -761,7 +770,9 @@ int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* byt
 }
 
 template <int NT>
-static int launch_qss_nt(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
+static int launch_qss_nt(const MechView& m, const SourceArgs& a_in, int* counter, Scratch& sc, cudaStream_t st) {
+    SourceArgs a = a_in;
+    if (a.queue_chunk == 0) a.queue_chunk = m.qss_chunk > 0 ? m.qss_chunk : 1;
     size_t per = 0;
     int blocks = 0;
     EMBER_TRY(qss_config<NT>(m, a, &per, &blocks));
@@ -987,6 +998,31 @@ extern "C" int ember_source_autotune(ember_mech m, int method, int n, const doub
             }
         }
     }
+    // QSS: queue granularity (slots claimed per atomic) with the best width and schedule
+    int best_chunk = 1;
+    for (int chunk : {2, 4}) {
+        if (bdf || rc != EMBER_OK) break;
+        ember_source_options o = *opts;
+        o.threads_per_point = best;
+        o.qss_tail_steps = best_tail ? best_tail : -1;
+        o.qss_tail_threads = best_tail_threads;
+        SourceArgs a = make_source_args(&o, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, nullptr);
+        a.queue_chunk = chunk;
+        float ms = 0.0f;
+        for (int rep = 0; rep < 2 && rc == EMBER_OK; ++rep) {
+            Scratch work(st);
+            rc = cuda_check(cudaMemsetAsync(counter, 0, sizeof(int), st), "cudaMemsetAsync");
+            if (rc == EMBER_OK) rc = cuda_check(cudaEventRecord(e0, st), "cudaEventRecord");
+            if (rc == EMBER_OK) rc = launch_source_qss(m->view, a, counter, work, st);
+            if (rc == EMBER_OK) rc = cuda_check(cudaEventRecord(e1, st), "cudaEventRecord");
+            if (rc == EMBER_OK) rc = cuda_check(cudaEventSynchronize(e1), "cudaEventSynchronize");
+            if (rc == EMBER_OK) rc = cuda_check(cudaEventElapsedTime(&ms, e0, e1), "cudaEventElapsedTime");
+        }
+        if (rc == EMBER_OK && ms < best_ms) {
+            best_ms = ms;
+            best_chunk = chunk;
+        }
+    }
     cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     sc.release();
@@ -995,6 +1031,7 @@ extern "C" int ember_source_autotune(ember_mech m, int method, int n, const doub
     if (!bdf) {
         m->view.qss_tail_steps = best_tail;
         m->view.qss_tail_threads = best_tail_threads;
+        m->view.qss_chunk = best_chunk;
     }
     if (bdf) {
         m->view.bdf_threads = best;
@@ -1007,11 +1044,12 @@ extern "C" int ember_source_autotune(ember_mech m, int method, int n, const doub
 }
 
 extern "C" int ember_mech_get_tuning(ember_mech m, int* qss_threads, int* qss_tail_steps, int* qss_tail_threads,
-                                     int* bdf_threads, int* bdf_layout) {
+                                     int* qss_chunk, int* bdf_threads, int* bdf_layout) {
     EMBER_CHECK_ARG(m != nullptr, "null mechanism");
     if (qss_threads) *qss_threads = m->view.qss_threads;
     if (qss_tail_steps) *qss_tail_steps = m->view.qss_tail_steps;
     if (qss_tail_threads) *qss_tail_threads = m->view.qss_tail_threads;
+    if (qss_chunk) *qss_chunk = m->view.qss_chunk;
     if (bdf_threads) *bdf_threads = m->view.bdf_threads;
     if (bdf_layout) {
         // BdfLayout modes (bdf.cu): 0 global, 1 both in shared memory, 2 LU only -> 3, 1, 2

@@ -46,6 +46,7 @@ struct SourceArgs {
     int* susp_list;
     int* susp_n;
     int tail_steps, tail_threads;  // requested (0: the mechanism's tuned values)
+    int queue_chunk;               // work-queue slots claimed per atomic (0: the mechanism's tuned value)
 };
 
 // Tape header: accepted steps recorded, order after the last step, t after

@@ -133,9 +133,9 @@ def autotune(gmech: GpuMechanism, method: int, state, dt, opts: SourceOptions | 
 
 def tuning(gmech: GpuMechanism) -> dict:
     """The launch configuration ember_source_autotune stored in the mechanism."""
-    v = [C.c_int() for _ in range(5)]
+    v = [C.c_int() for _ in range(6)]
     L.check(L.lib().ember_mech_get_tuning(gmech.handle, *(C.byref(x) for x in v)), "ember_mech_get_tuning")
-    keys = ("qss_threads", "qss_tail_steps", "qss_tail_threads", "bdf_threads", "bdf_layout")
+    keys = ("qss_threads", "qss_tail_steps", "qss_tail_threads", "qss_chunk", "bdf_threads", "bdf_layout")
     return {k: x.value for k, x in zip(keys, v)}
 
 

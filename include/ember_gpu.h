@@ -421,8 +421,10 @@ int ember_source_integrate(ember_mech mech, int method, int n_points, const doub
  * times every placement of the Jacobian and LU factors that fits (both in
  * shared memory, the LU factors alone, neither). threads_out: the chosen
  * width; ms_out: [EMBER_SOURCE_N_THREAD_CHOICES] milliseconds per width (the
- * best placement for BDF; 0 for widths not tried) or NULL. Integration
- * results are identical for every candidate. */
+ * best placement for BDF; 0 for widths not tried) or NULL. For QSS it then
+ * tries two-pass schedules and work-queue granularities of 2 and 4 points
+ * per claim with the best width. Integration results are identical for
+ * every candidate. */
 #define EMBER_SOURCE_N_THREAD_CHOICES 7
 #define EMBER_SOURCE_THREAD_CHOICES {32, 64, 96, 128, 160, 192, 256}
 int ember_source_autotune(ember_mech mech, int method, int n_points, const double* state_in, const double* split_const,
@@ -430,11 +432,13 @@ int ember_source_autotune(ember_mech mech, int method, int n_points, const doubl
                           int* threads_out, double* ms_out, int mem, void* stream);
 
 /* The launch configuration stored in the mechanism by ember_source_autotune
- * (0 where none was chosen): QSS width, QSS two-pass steps and tail width,
- * BDF width, BDF matrix placement (1: J and LU in shared memory, 2: LU
- * only, 3: neither). */
+ * (0 where none was chosen): QSS width, QSS two-pass steps and tail width, QSS
+ * work-queue granularity (points a CTA claims per atomic), BDF width, BDF
+ * matrix placement (1: J and LU in shared memory, 2: LU only, 3: neither).
+ * ember_source_autotune changes the mechanism handle: do not call it while
+ * other threads launch work with the same mechanism. */
 int ember_mech_get_tuning(ember_mech mech, int* qss_threads, int* qss_tail_steps, int* qss_tail_threads,
-                          int* bdf_threads, int* bdf_layout);
+                          int* qss_chunk, int* bdf_threads, int* bdf_layout);
 
 /* Discrete adjoint of a BDF source-term integration (EMBER_SOURCE_BDF, same
  * arguments as ember_source_integrate): for phi = sum over points of

@@ -52,7 +52,7 @@ def test_bad_arguments_are_rejected_without_device():
     assert lib.ember_transport_eval(None, 1, 101325.0, 1e-5, None, None, None, 0, None) == _lib.EINVAL
     assert lib.ember_split_load_state(None, None, 0, None) == _lib.EINVAL
     assert lib.ember_split_set_transport_model(None, None, 1e-5, 1) == _lib.EINVAL
-    assert lib.ember_mech_get_tuning(None, None, None, None, None, None) == _lib.EINVAL
+    assert lib.ember_mech_get_tuning(None, None, None, None, None, None, None) == _lib.EINVAL
     assert lib.ember_source_autotune(None, 0, 1, None, None, None, 0.0, None, None, None, None, 0, None) \
         == _lib.EINVAL
 
