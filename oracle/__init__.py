@@ -2,7 +2,7 @@
 
 ctypes binding of the plain-C restatement in this folder (liboracle.so). Only
 tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import it,
-and only as the checker; the product package never does.
+and only to compare the GPU results with; the product package never does.
 """
 from __future__ import annotations
 

@@ -1,7 +1,7 @@
 /*
  * CPU ORACLE -- test infrastructure only. Never linked into, or called by,
  * the product library; only tests/, the smoke check and bench.py's CPU
- * baseline load it, as the checker.
+ * baseline load it, to compare the GPU results with.
  *
  * Plain-C restatement of the reference's tridiagonal integrator and
  * diffusion matrix:
