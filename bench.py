@@ -57,6 +57,9 @@ def parse_args():
                         "53-species/325-reaction one")
     p.add_argument("--no-plain", action="store_true",
                    help="split workload: skip the plain per-flame GPU path measured beside the batched step")
+    p.add_argument("--split-dt", type=float, default=0.0,
+                   help="split workload: global time step (0: 2e-5 s; the GRI-sized BDF case needs 5e-6 s on the "
+                        "seeded profiles)")
     p.add_argument("--source", default="qss", choices=["qss", "bdf"],
                    help="split workload: source-term integrator (the C5 sweep names BDF)")
     p.add_argument("--threads", type=int, default=0,
@@ -521,7 +524,7 @@ def split_inputs(rank: int, mech_size: str = "150"):
 
 def split_workload(args, mech) -> str:
     return SPLIT_WORKLOAD.replace("150-species/1000-reaction", f"{mech.n_species}-species/{mech.n_reactions}-reaction") \
-        .replace("QSS source", f"{args.source.upper()} source")
+        .replace("QSS source", f"{args.source.upper()} source").replace("dt 2e-5 s", f"dt {args.split_dt or SPLIT_DT:g} s")
 
 
 def run_reference_split(args):
@@ -534,6 +537,7 @@ def run_reference_split(args):
     mech, grids, state, B, D, rho_u, ju, jb = split_inputs(0, args.mech)
     opts = source_options(args.kinetics, args.source)
     method = QSS if args.source == "qss" else BDF
+    split_dt = args.split_dt or SPLIT_DT
     om = OracleMech(mech)
     # bounded sample: the first flame, one split step per timed step
     g0 = grids[:1]
@@ -543,10 +547,10 @@ def run_reference_split(args):
     from ember_gb300.transport import synthetic_transport
     tr = (synthetic_transport(mech, seed=SPLIT_TRANSPORT_SEED), SPLIT_THRESHOLD, True)
     for _ in range(args.warmup):
-        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, method, opts, transport=tr)
+        osplit.split_steps(om, g0, st0, 0.0, B0, D0, split_dt, 1, method, opts, transport=tr)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        osplit.split_steps(om, g0, st0, 0.0, B0, D0, SPLIT_DT, 1, method, opts, transport=tr)
+        osplit.split_steps(om, g0, st0, 0.0, B0, D0, split_dt, 1, method, opts, transport=tr)
     per_flame = (time.perf_counter() - t0) / args.steps
     # scaled to the 32-flame batch by points
     ms = 1e3 * per_flame * len(state) / n0
@@ -576,10 +580,11 @@ def run_ours_split(args):
     mech, grids, state, B, D, rho_u, ju, jb = split_inputs(rank, args.mech)
     opts = source_options(args.kinetics, args.source)
     method = QSS if args.source == "qss" else BDF
+    split_dt = args.split_dt or SPLIT_DT
     gm = GpuMechanism(mech)
     # QSS launch width tuned on the flames' start states over one step (before the solver takes it)
-    width, tune_ms = autotune(gm, method, state, np.full(len(state), SPLIT_DT), opts)
-    solver = FlameBatchSplitSolver(gm, grids, SPLIT_DT, method=method, source_options=opts)
+    width, tune_ms = autotune(gm, method, state, np.full(len(state), split_dt), opts)
+    solver = FlameBatchSplitSolver(gm, grids, split_dt, method=method, source_options=opts)
     from ember_gb300.transport import GpuTransport, synthetic_transport
     tdata = synthetic_transport(mech, seed=SPLIT_TRANSPORT_SEED)
     gtr = GpuTransport(gm, tdata)
@@ -637,7 +642,7 @@ def run_ours_split(args):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         for f in range(len(grids)):
             a, b = off[f], off[f + 1]
-            one = FlameBatchSplitSolver(gm, grids[f:f + 1], SPLIT_DT, method=method, source_options=opts)
+            one = FlameBatchSplitSolver(gm, grids[f:f + 1], split_dt, method=method, source_options=opts)
             one.set_state(0.0, state[a:b])
             one.set_transport(B[a * nv:b * nv], D[a * nv:b * nv])
             one.set_transport_model(gtr, SPLIT_THRESHOLD, cross_terms=True)
@@ -687,7 +692,7 @@ def run_ours_split(args):
         t0 = time.perf_counter()
         reps = 0
         while time.perf_counter() - t0 < args.cpu_seconds or reps == 0:
-            osplit.split_steps(om, grids[:1], state[:n0], 0.0, B[:nv * n0], D[:nv * n0], SPLIT_DT, 1, method, opts,
+            osplit.split_steps(om, grids[:1], state[:n0], 0.0, B[:nv * n0], D[:nv * n0], split_dt, 1, method, opts,
                                transport=(tdata, SPLIT_THRESHOLD, True))
             reps += 1
         tcpu = (time.perf_counter() - t0) / reps
