@@ -962,6 +962,7 @@ bool source_bdf_layout_fits(const MechView& m, int layout) {
 
 int source_bdf_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes) {
     switch (source_bdf_threads(m, a)) {
+        case 32: return bdf_scratch_nt<32>(m, a, bytes);
         case 64: return bdf_scratch_nt<64>(m, a, bytes);
         case 128: return bdf_scratch_nt<128>(m, a, bytes);
         case 160: return bdf_scratch_nt<160>(m, a, bytes);
@@ -1297,6 +1298,7 @@ int launch_objective_vjp(const MechView& m, const SourceArgs& a, int n_pts, cons
                          const double* gcp, const double* gT, double* ybar, double* pbar, Scratch& sc,
                          cudaStream_t st) {
     switch (source_bdf_threads(m, a)) {
+        case 32: return launch_objective_vjp_nt<32>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
         case 64: return launch_objective_vjp_nt<64>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
         case 128: return launch_objective_vjp_nt<128>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
         case 160: return launch_objective_vjp_nt<160>(m, a, n_pts, state, gq, gcp, gT, ybar, pbar, sc, st);
@@ -1307,6 +1309,7 @@ int launch_objective_vjp(const MechView& m, const SourceArgs& a, int n_pts, cons
 int launch_source_bdf_adjoint(const MechView& m, const SourceArgs& a, int* counter, const double* ybar_out,
                               double* ybar_in, double* pbar, int* adj_status, Scratch& sc, cudaStream_t st) {
     switch (source_bdf_threads(m, a)) {
+        case 32: return launch_bdf_adjoint_nt<32>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
         case 64: return launch_bdf_adjoint_nt<64>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
         case 128: return launch_bdf_adjoint_nt<128>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
         case 160: return launch_bdf_adjoint_nt<160>(m, a, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
@@ -1316,6 +1319,7 @@ int launch_source_bdf_adjoint(const MechView& m, const SourceArgs& a, int* count
 
 int launch_source_bdf(const MechView& m, const SourceArgs& a, int* counter, Scratch& sc, cudaStream_t st) {
     switch (source_bdf_threads(m, a)) {
+        case 32: return launch_bdf_nt<32>(m, a, counter, sc, st);
         case 64: return launch_bdf_nt<64>(m, a, counter, sc, st);
         case 128: return launch_bdf_nt<128>(m, a, counter, sc, st);
         case 160: return launch_bdf_nt<160>(m, a, counter, sc, st);

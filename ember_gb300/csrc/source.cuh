@@ -112,7 +112,7 @@ int source_bdf_layout(const MechView& m, const SourceArgs& a);
 // Whether matrix layout 1 + mode fits the BDF kernel's shared memory for this mechanism.
 bool source_bdf_layout_fits(const MechView& m, int layout);
 // Launch widths of the BDF kernel.
-constexpr int kBdfThreadChoices[] = {64, 128, 160, 256};
+constexpr int kBdfThreadChoices[] = {32, 64, 128, 160, 256};
 
 }  // namespace ember
 

@@ -383,7 +383,7 @@ typedef struct {
     int bdf_max_num_steps;
     /* threads per grid point (one CTA per point): 0 = the width
      * ember_source_autotune chose for the mechanism, else the default for its
-     * size; or 32, 64, 96, 128, 160, 192, 256 (QSS) / 64, 128, 160, 256 (BDF;
+     * size; or 32, 64, 96, 128, 160, 192, 256 (QSS) / 32, 64, 128, 160, 256 (BDF;
      * other values give the mechanism's width). Results do not depend on it
      * (every reduction runs in one fixed 32-lane order). */
     int threads_per_point;
@@ -417,7 +417,7 @@ int ember_source_integrate(ember_mech mech, int method, int n_points, const doub
  * candidate, times each run on the stream with CUDA events (after one untimed
  * run), and stores the fastest candidate in the mechanism handle, where calls
  * whose threads_per_point is 0 pick it up. QSS candidates: every width of
- * EMBER_SOURCE_THREAD_CHOICES. BDF candidates: the widths 64, 128, 160, 256
+ * EMBER_SOURCE_THREAD_CHOICES. BDF candidates: the widths 32, 64, 128, 160, 256
  * times every placement of the Jacobian and LU factors that fits (both in
  * shared memory, the LU factors alone, neither). threads_out: the chosen
  * width; ms_out: [EMBER_SOURCE_N_THREAD_CHOICES] milliseconds per width (the

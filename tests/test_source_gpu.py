@@ -255,9 +255,9 @@ def test_autotune_keeps_the_fastest_width_and_the_results(gpu_lib, small_mech):
     ro, rs, _ = o.integrate(chem.QSS, st, dt, opts)
     np.testing.assert_array_equal(status, rs)
     assert np.array_equal(out, ro)
-    # BDF: widths 64/128/160/256 x the matrix placements that fit
+    # BDF: widths 32/64/128/160/256 x the matrix placements that fit
     bw, bms = autotune(g, BDF, st[:16], dt[:16], opts)
-    assert bw in (64, 128, 160, 256) and set(bms) == {64, 128, 160, 256}
+    assert bw in (32, 64, 128, 160, 256) and set(bms) == {32, 64, 128, 160, 256}
     with pytest.raises(L.EmberGpuError):
         integrate_production_terms(g, QSS, st, dt, SourceOptions.defaults(threads_per_point=48))
 
@@ -273,7 +273,7 @@ def test_bdf_results_do_not_depend_on_width_or_matrix_placement(gpu_lib, n_speci
     st, dt = _states(m, 12, seed=23)
     opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
     ro, rs, rst = o.integrate(chem.BDF, st, dt, opts)
-    for width in (64, 128, 160, 256):
+    for width in (32, 64, 128, 160, 256):
         out, status, stats = integrate_production_terms(g, BDF, st, dt,
                                                         SourceOptions.defaults(kinetics_model=KINETICS_STANDARD,
                                                                                threads_per_point=width))
