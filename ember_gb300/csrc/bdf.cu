@@ -282,74 +282,122 @@ struct BdfPoint {
     // multipliers a_ik * (1/a_kk)). Returns 0, or k+1 when column k has no
     // usable pivot: all zeros, or a NaN anywhere in it (then no row index is
     // chosen at all, so nothing is swapped or read out of range).
+    // Partial-pivot search of column k over rows k..n-1: the largest |entry|
+    // (ties to the lowest row); writes v.piv[k]. Returns 0, or k + 1 when the
+    // column holds a NaN or its largest entry is zero (singular).
+    __device__ int lu_pivot(int k, double* sbest, int* sidx, int& s_p, double& s_best) {
+        const int tid = threadIdx.x;
+        const double* colk = M + size_t(k) * n;
+        double best = -1.0;
+        int bi = n;
+        int has_nan = 0;
+        for (int i = k + tid; i < n; i += NT) {
+            const double vv = fabs(colk[i]);
+            if (vv != vv) has_nan = 1;
+            if (vv > best) {
+                best = vv;
+                bi = i;
+            }
+        }
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) {
+            const double ob = __shfl_xor_sync(0xffffffffu, best, off);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+            if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+            }
+        }
+        if (lane_id() == 0) {
+            sbest[tid >> 5] = best;
+            sidx[tid >> 5] = bi;
+        }
+        const int col_nan = __syncthreads_or(has_nan);
+        if (col_nan) return k + 1;
+        if (tid == 0) {
+            double b = sbest[0];
+            int pp = sidx[0];
+            for (int q = 1; q < NT / 32; ++q)
+                if (sbest[q] > b || (sbest[q] == b && sidx[q] < pp)) {
+                    b = sbest[q];
+                    pp = sidx[q];
+                }
+            s_p = pp;
+            s_best = b;
+            v.piv[k] = pp;
+        }
+        __syncthreads();
+        if (s_best == 0.0) return k + 1;
+        return 0;
+    }
+
+    // Swap rows k and p over every column.
+    __device__ void lu_swap(int k, int p) {
+        if (p == k) return;
+        for (int j = threadIdx.x; j < n; j += NT) {
+            double* a1 = M + size_t(j) * n + k;
+            double* a2 = M + size_t(j) * n + p;
+            const double tt = *a1;
+            *a1 = *a2;
+            *a2 = tt;
+        }
+    }
+
+    // In-place LU with partial pivoting (CVODE's dense getrf): M = P^-1 L U,
+    // two columns per pass over the trailing matrix. For columns k, k+1:
+    // pivot, swap and scale column k; bring column k+1 up to date with step k
+    // and pivot, swap and scale it (the swap may precede step k's update of the
+    // other rows: that update is row by row); update row k+1 with step k; then
+    // every trailing element gets step k's and step k+1's multiply-add in that
+    // order, the operations and order of the one-column algorithm. Returns 0 or
+    // the 1-based column found singular.
     __device__ int lu_factor() {
         const int tid = threadIdx.x;
+        const int warp = tid >> 5, lane = tid & 31;
         __shared__ double sbest[32];
         __shared__ int sidx[32];
         __shared__ int s_p;
         __shared__ double s_best;
-        for (int k = 0; k < n; ++k) {
+        for (int k = 0; k < n; k += 2) {
             double* colk = M + size_t(k) * n;
-            double best = -1.0;
-            int bi = n;
-            int has_nan = 0;
-            for (int i = k + tid; i < n; i += NT) {
-                const double vv = fabs(colk[i]);
-                if (vv != vv) has_nan = 1;
-                if (vv > best) {
-                    best = vv;
-                    bi = i;
-                }
-            }
-#pragma unroll
-            for (int off = 16; off >= 1; off >>= 1) {
-                const double ob = __shfl_xor_sync(0xffffffffu, best, off);
-                const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-                if (ob > best || (ob == best && oi < bi)) {
-                    best = ob;
-                    bi = oi;
-                }
-            }
-            if (lane_id() == 0) {
-                sbest[tid >> 5] = best;
-                sidx[tid >> 5] = bi;
-            }
-            const int col_nan = __syncthreads_or(has_nan);
-            if (col_nan) return k + 1;
-            if (tid == 0) {
-                double b = sbest[0];
-                int p = sidx[0];
-                for (int q = 1; q < NT / 32; ++q)
-                    if (sbest[q] > b || (sbest[q] == b && sidx[q] < p)) {
-                        b = sbest[q];
-                        p = sidx[q];
-                    }
-                s_p = p;
-                s_best = b;
-                v.piv[k] = p;
-            }
-            __syncthreads();
-            const int p = s_p;
-            if (s_best == 0.0) return k + 1;
-            if (p != k)
-                for (int j = tid; j < n; j += NT) {
-                    double* a1 = M + size_t(j) * n + k;
-                    double* a2 = M + size_t(j) * n + p;
-                    const double tt = *a1;
-                    *a1 = *a2;
-                    *a2 = tt;
-                }
+            int sing = lu_pivot(k, sbest, sidx, s_p, s_best);
+            if (sing) return sing;
+            lu_swap(k, s_p);
             __syncthreads();
             const double r = 1.0 / colk[k];
             for (int i = k + 1 + tid; i < n; i += NT) colk[i] = colk[i] * r;
             __syncthreads();
-            // trailing update a_ij -= l_i a_kj: one warp per column, lanes over rows
+            const int k1 = k + 1;
+            if (k1 >= n) break;
+            // column k+1 under step k
+            double* colk1 = M + size_t(k1) * n;
             {
-                const int warp = tid >> 5, lane = tid & 31;
-                for (int j = k + 1 + warp; j < n; j += NT / 32) {
-                    double* colj = M + size_t(j) * n;
-                    const double akj = colj[k];
-                    for (int i = k + 1 + lane; i < n; i += 32) colj[i] = fma(-colk[i], akj, colj[i]);
+                const double akj = colk1[k];
+                for (int i = k1 + tid; i < n; i += NT) colk1[i] = fma(-colk[i], akj, colk1[i]);
+            }
+            __syncthreads();
+            sing = lu_pivot(k1, sbest, sidx, s_p, s_best);
+            if (sing) return sing;
+            lu_swap(k1, s_p);
+            __syncthreads();
+            const double r1 = 1.0 / colk1[k1];
+            for (int i = k1 + 1 + tid; i < n; i += NT) colk1[i] = colk1[i] * r1;
+            // row k+1 of the trailing columns under step k
+            {
+                const double lk1 = colk[k1];
+                for (int j = k1 + 1 + tid; j < n; j += NT) {
+                    double* a = M + size_t(j) * n;
+                    a[k1] = fma(-lk1, a[k], a[k1]);
+                }
+            }
+            __syncthreads();
+            // trailing update with both steps: one warp per column, lanes over rows
+            for (int j = k1 + 1 + warp; j < n; j += NT / 32) {
+                double* colj = M + size_t(j) * n;
+                const double akj = colj[k], ak1j = colj[k1];
+                for (int i = k1 + 1 + lane; i < n; i += 32) {
+                    double a = fma(-colk[i], akj, colj[i]);
+                    colj[i] = fma(-colk1[i], ak1j, a);
                 }
             }
             __syncthreads();
