@@ -344,13 +344,16 @@ struct BdfPoint {
     }
 
     // In-place LU with partial pivoting (CVODE's dense getrf): M = P^-1 L U,
-    // two columns per pass over the trailing matrix. For columns k, k+1:
-    // pivot, swap and scale column k; bring column k+1 up to date with step k
-    // and pivot, swap and scale it (the swap may precede step k's update of the
-    // other rows: that update is row by row); update row k+1 with step k; then
-    // every trailing element gets step k's and step k+1's multiply-add in that
-    // order, the operations and order of the one-column algorithm. Returns 0 or
-    // the 1-based column found singular.
+    // kLuPanel columns per pass over the trailing matrix. Within a panel,
+    // column c first receives the multiply-adds of the panel's earlier steps
+    // (in step order), then is pivoted, swapped (whole rows: the updates still
+    // pending for a row go with it) and scaled. After the panel, each pivot
+    // row's trailing entries receive the earlier panel steps in order, and every
+    // other trailing element receives all the panel's steps in order: per
+    // element the operations and their order are those of the one-column
+    // algorithm, so the factors are the same bits. Returns 0 or the 1-based
+    // column found singular.
+    static constexpr int kLuPanel = 4;
     __device__ int lu_factor() {
         const int tid = threadIdx.x;
         const int warp = tid >> 5, lane = tid & 31;
@@ -358,46 +361,47 @@ struct BdfPoint {
         __shared__ int sidx[32];
         __shared__ int s_p;
         __shared__ double s_best;
-        for (int k = 0; k < n; k += 2) {
-            double* colk = M + size_t(k) * n;
-            int sing = lu_pivot(k, sbest, sidx, s_p, s_best);
-            if (sing) return sing;
-            lu_swap(k, s_p);
-            __syncthreads();
-            const double r = 1.0 / colk[k];
-            for (int i = k + 1 + tid; i < n; i += NT) colk[i] = colk[i] * r;
-            __syncthreads();
-            const int k1 = k + 1;
-            if (k1 >= n) break;
-            // column k+1 under step k
-            double* colk1 = M + size_t(k1) * n;
-            {
-                const double akj = colk1[k];
-                for (int i = k1 + tid; i < n; i += NT) colk1[i] = fma(-colk[i], akj, colk1[i]);
+        for (int k = 0; k < n; k += kLuPanel) {
+            const int kend = min(k + kLuPanel, n);
+            for (int c = k; c < kend; ++c) {
+                double* colc = M + size_t(c) * n;
+                for (int t = k; t < c; ++t) {
+                    const double atc = colc[t];
+                    const double* colt = M + size_t(t) * n;
+                    for (int i = t + 1 + tid; i < n; i += NT) colc[i] = fma(-colt[i], atc, colc[i]);
+                    __syncthreads();
+                }
+                const int sing = lu_pivot(c, sbest, sidx, s_p, s_best);
+                if (sing) return sing;
+                lu_swap(c, s_p);
+                __syncthreads();
+                const double r = 1.0 / colc[c];
+                for (int i = c + 1 + tid; i < n; i += NT) colc[i] = colc[i] * r;
+                __syncthreads();
             }
-            __syncthreads();
-            sing = lu_pivot(k1, sbest, sidx, s_p, s_best);
-            if (sing) return sing;
-            lu_swap(k1, s_p);
-            __syncthreads();
-            const double r1 = 1.0 / colk1[k1];
-            for (int i = k1 + 1 + tid; i < n; i += NT) colk1[i] = colk1[i] * r1;
-            // row k+1 of the trailing columns under step k
-            {
-                const double lk1 = colk[k1];
-                for (int j = k1 + 1 + tid; j < n; j += NT) {
-                    double* a = M + size_t(j) * n;
-                    a[k1] = fma(-lk1, a[k], a[k1]);
+            if (kend >= n) break;
+            // pivot rows k+1..kend-1 of the trailing columns: the earlier panel steps, in order
+            for (int j = kend + tid; j < n; j += NT) {
+                double* colj = M + size_t(j) * n;
+                for (int r = k + 1; r < kend; ++r) {
+                    double a = colj[r];
+                    for (int t = k; t < r; ++t) a = fma(-M[size_t(t) * n + r], colj[t], a);
+                    colj[r] = a;
                 }
             }
             __syncthreads();
-            // trailing update with both steps: one warp per column, lanes over rows
-            for (int j = k1 + 1 + warp; j < n; j += NT / 32) {
+            // the other trailing elements: every panel step, in order; one warp per column
+            for (int j = kend + warp; j < n; j += NT / 32) {
                 double* colj = M + size_t(j) * n;
-                const double akj = colj[k], ak1j = colj[k1];
-                for (int i = k1 + 1 + lane; i < n; i += 32) {
-                    double a = fma(-colk[i], akj, colj[i]);
-                    colj[i] = fma(-colk1[i], ak1j, a);
+                double u[kLuPanel];
+#pragma unroll
+                for (int t = 0; t < kLuPanel; ++t) u[t] = (k + t < kend) ? colj[k + t] : 0.0;
+                for (int i = kend + lane; i < n; i += 32) {
+                    double a = colj[i];
+#pragma unroll
+                    for (int t = 0; t < kLuPanel; ++t)
+                        if (k + t < kend) a = fma(-M[size_t(k + t) * n + i], u[t], a);
+                    colj[i] = a;
                 }
             }
             __syncthreads();
