@@ -353,7 +353,7 @@ struct BdfPoint {
     // element the operations and their order are those of the one-column
     // algorithm, so the factors are the same bits. Returns 0 or the 1-based
     // column found singular.
-    static constexpr int kLuPanel = 4;
+    static constexpr int kLuPanel = 8;
     __device__ int lu_factor() {
         const int tid = threadIdx.x;
         const int warp = tid >> 5, lane = tid & 31;
