@@ -93,10 +93,11 @@ def bdf_point_flops(mech: Mechanism, kinetics_model: int, steps, rhs_calls, jaco
 # 8,559,872 + dram__bytes_write.sum 823,552 bytes): state in and out plus the
 # per-CTA rate-constant cache.
 QSS_DRAM_BYTES_PER_POINT = (8559872 + 823552) / 4096
-# The same for k_source_bdf with 152 variables, from the capture of 152 points
-# (5,715,968 + 19,849,984 bytes): the LU factors in shared memory, the
-# Jacobian, rates of progress and saved Nordsieck array in a global slice.
-BDF_DRAM_BYTES_PER_POINT = (5715968 + 19849984) / 152
+# The same for k_source_bdf with 152 variables, from the capture of 608 points
+# at 128 threads (5,883,392 + 14,031,104 bytes): the LU factors in shared
+# memory, the Jacobian, rates of progress and saved Nordsieck array in a
+# global slice.
+BDF_DRAM_BYTES_PER_POINT = (5883392 + 14031104) / 608
 
 
 def tridiag_flops_per_point() -> float:
