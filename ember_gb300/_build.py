@@ -20,7 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Translation units whose arithmetic must match the CPU oracle operation by
 # operation: no automatic multiply-add contraction (explicit fma() only).
 FILE_FLAGS = {"source.cu": ["--fmad=false"], "bdf.cu": ["--fmad=false"], "split.cu": ["--fmad=false"],
-              "transport.cu": ["--fmad=false"]}
+              "transport.cu": ["--fmad=false"], "convection.cu": ["--fmad=false"]}
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 

@@ -87,6 +87,8 @@ def _declare(lib):
         "ember_split_set_transport_model": (C.c_int, [vp, vp, C.c_double, C.c_int]),
         "ember_split_load_state": (C.c_int, [vp, vp, C.c_int, vp]),
         "ember_mech_get_tuning": (C.c_int, [vp, vp, vp, vp, vp, vp, vp]),
+        "ember_convection_integrate": (C.c_int, [C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                                 C.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

@@ -1,0 +1,924 @@
+// Convection stage of the split step for a batch of flames:
+// ConvectionSystemSplit::integrateToTime (src/convectionSystem.cpp:588-627).
+//
+//   k_conv_prepare   one CTA per flame: grid metrics, the initial mean
+//                    molecular weight W from the mass fractions and the W
+//                    split constant (src/convectionSystem.cpp:485-511, 572-586)
+//   k_conv_utw       one warp per flame: the UTW system
+//                    (ConvectionSystemUTW::f, src/convectionSystem.cpp:14-130)
+//                    integrated to the stage end with a stop time, V / rho
+//                    recorded after every step (src/convectionSystem.cpp:592-611)
+//   k_conv_species   one warp per (flame, species): ConvectionSystemY::f
+//                    (src/convectionSystem.cpp:307-359) with v(t) interpolated
+//                    from that record (ConvectionSystemY::update_v, 372-398),
+//                    integrated past the stage end and interpolated back
+//
+// Both integrations use the Adams method (variable order 1..12, Nordsieck
+// form) with a diagonal difference-quotient Jacobian: the reference runs
+// CVODE's Adams method with a zero-bandwidth banded Jacobian
+// (src/convectionSystem.cpp:467-478, 663-676). Every vector operation is
+// lane-strided over one warp; weighted norms are summed with term i on lane
+// i mod 32 and an xor butterfly; the continuity integral runs on lane 0 in
+// point order. The Nordsieck arrays and the per-system vectors live in a
+// global work slice per system (40 vectors). Compiled with --fmad=false, the
+// results are bitwise those of the CPU restatement.
+#include <cstdint>
+
+#include "common.cuh"
+#include "emath.cuh"
+
+namespace ember {
+namespace {
+
+constexpr int QA = 12;
+constexpr int kWorkVectors = 2 * (QA + 2) + 12;
+constexpr double kGasConstant = 6.02214076e26 * 1.380649e-23;
+
+__device__ __forceinline__ double dmaxc(double a, double b) { return (a < b) ? b : a; }
+__device__ __forceinline__ double dminc(double a, double b) { return (b < a) ? b : a; }
+__device__ __forceinline__ double cpow_(double x, double e) { return em_exp(e * em_log(x)); }
+__device__ __forceinline__ int lane_of() { return threadIdx.x & 31; }
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = v + __shfl_xor_sync(0xffffffffu, v, off);
+    return v;
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) v = dmaxc(v, __shfl_xor_sync(0xffffffffu, v, off));
+    return v;
+}
+
+// sqrt(sum (v_i ewt_i)^2 / n), term i on lane i mod 32
+__device__ double wrms_w(const double* v, const double* ewt, int n) {
+    double p = 0.0;
+    for (int i = lane_of(); i < n; i += 32) {
+        const double t = v[i] * ewt[i];
+        p = fma(t, t, p);
+    }
+    return sqrt(warp_sum(p) / n);
+}
+
+struct AdamsConst {
+    double g[QA + 2];
+    __device__ AdamsConst() {
+        g[0] = 1.0;
+        for (int j = 1; j <= QA + 1; ++j) {
+            double s = 0.0;
+            for (int i = 0; i < j; ++i) s = s + g[i] / (double)(j + 1 - i);
+            g[j] = 1.0 - s;
+        }
+    }
+};
+
+__device__ void adams_l(int q, double* l) {
+    double p[QA + 2];
+    for (int j = 0; j <= QA + 1; ++j) {
+        p[j] = 0.0;
+        l[j] = 0.0;
+    }
+    p[0] = 1.0;
+    for (int i = 1; i <= q - 1; ++i) {
+        for (int j = i; j >= 1; --j) p[j] = p[j - 1] + (double)i * p[j];
+        p[0] = (double)i * p[0];
+    }
+    double q0 = 0.0;
+    for (int j = 0; j < q; ++j) {
+        const double tj = p[j] / (double)(j + 1);
+        q0 = (j % 2 == 0) ? q0 + tj : q0 - tj;
+    }
+    l[0] = 1.0;
+    for (int j = 0; j < q; ++j) l[j + 1] = (p[j] / (double)(j + 1)) / q0;
+}
+
+// One warp integrates y' = f(t, y) from t0 to tf (tstop: the last step ends
+// on tf; else past tf, then interpolated). `wk` holds kWorkVectors * n
+// doubles. Same operations, in the same order, as the CPU restatement.
+template <class Sys>
+__device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t0, double tf, int tstop,
+                          double hmin, int max_steps, int* stats) {
+    const int n = s.n, lane = lane_of();
+    auto Z = [&](int j) { return wk + size_t(j) * n; };
+    auto ZS = [&](int j) { return wk + size_t(QA + 2 + j) * n; };
+    double* b0 = wk + size_t(2 * (QA + 2)) * n;
+    double *acor = b0, *acorp = b0 + n, *ewt = b0 + 2 * size_t(n), *y = b0 + 3 * size_t(n);
+    double *ft = b0 + 4 * size_t(n), *bb = b0 + 5 * size_t(n), *tmp = b0 + 6 * size_t(n);
+    double *f0 = b0 + 7 * size_t(n), *ycopy = b0 + 8 * size_t(n), *f1 = b0 + 9 * size_t(n);
+    double *jd = b0 + 10 * size_t(n), *md = b0 + 11 * size_t(n);
+    const double uround = 2.220446049250313e-16;
+    const AdamsConst C;
+    const double* g = C.g;
+    int nst = 0, nfe = 0, nje = 0, nfail = 0, status = 0;
+#define VLOOP for (int i = lane; i < n; i += 32)
+#define SET_EWT(v) VLOOP ewt[i] = 1.0 / (rtol * fabs((v)[i]) + s.atol(i));
+#define COPY_COLS(dst, src)                                  \
+    for (int j = 0; j <= q; ++j) {                           \
+        double* d_ = dst(j);                                 \
+        const double* s_ = src(j);                           \
+        VLOOP d_[i] = s_[i];                                 \
+    }
+#define RESCALE(eta_)                                        \
+    {                                                        \
+        double sc_ = (eta_);                                 \
+        for (int j = 1; j <= q; ++j) {                       \
+            double* zj_ = Z(j);                              \
+            VLOOP zj_[i] *= sc_;                             \
+            sc_ *= (eta_);                                   \
+        }                                                    \
+    }
+
+    VLOOP Z(0)[i] = yio[i];
+    s.f(t0, Z(0), f0);
+    nfe++;
+    SET_EWT(Z(0));
+    double t = t0;
+    const double tdist = tf - t0;
+    double hub = 0.1 * tdist;
+    double rmax = 0.0;
+    VLOOP rmax = dmaxc(rmax, fabs(f0[i]) / (0.1 * fabs(Z(0)[i]) + s.atol(i)));
+    rmax = warp_max(rmax);
+    if (rmax * hub > 1.0) hub = 1.0 / rmax;
+    const double hlb = 100.0 * uround * dmaxc(fabs(t0), fabs(tf));
+    double hg = sqrt(hlb * hub);
+    double h;
+    if (hub > hlb) {
+        for (int it = 0; it < 4; ++it) {
+            VLOOP ycopy[i] = fma(hg, f0[i], Z(0)[i]);
+            s.f(t0 + hg, ycopy, f1);
+            nfe++;
+            VLOOP tmp[i] = (f1[i] - f0[i]) / hg;
+            const double ydd = wrms_w(tmp, ewt, n);
+            const double hnew = (ydd * hub * hub > 2.0) ? sqrt(2.0 / ydd) : sqrt(hg * hub);
+            const double ratio = hnew / hg;
+            hg = hnew;
+            if (ratio > 0.5 && ratio < 2.0) break;
+        }
+        h = dminc(dmaxc(0.5 * hg, hlb), hub);
+    } else {
+        h = hlb;
+    }
+    if (h < hmin) h = hmin;
+    VLOOP Z(1)[i] = h * f0[i];
+
+    int q = 1, qwait = 2, nstlp = 0, nstlj = 0, have_m = 0, have_acorp = 0, qsave = 0;
+    double gammap = 0.0, crate = 1.0, etamax = 10000.0, acnrm = 0.0, hsave = 0.0;
+    double l[QA + 2];
+
+    while (t < tf) {
+        if (nst >= max_steps) {
+            status = -11;
+            break;
+        }
+        if (tstop && t + h > tf) {
+            const double eta = (tf - t) / h;
+            RESCALE(eta);
+            h = tf - t;
+        }
+        COPY_COLS(ZS, Z);
+        int ncf = 0, nef = 0, convfail_bad_j = 0, force_setup = !have_m;
+        double dsm = 0.0;
+        for (;;) {
+            for (int k = 1; k <= q; ++k)
+                for (int j = q; j >= k; --j) {
+                    double* a = Z(j - 1);
+                    const double* b = Z(j);
+                    VLOOP a[i] += b[i];
+                }
+            const double tn = t + h;
+            adams_l(q, l);
+            const double cq = fabs(g[q] - g[q - 1]) / g[q - 1];
+            const double gamma = h / l[1];
+            const double tq4 = 0.1 / cq;
+            int jcur = 0;
+            const double gamrat0 = have_m ? gamma / gammap : 1.0;
+            bool fail_conv = false;
+            if (force_setup || nst >= nstlp + 20 || fabs(gamrat0 - 1.0) > 0.3) {
+                const int jbad = (nst == 0) || (nst >= nstlj + 51) || convfail_bad_j || !have_m;
+                if (jbad) {
+                    s.f(tn, Z(0), ft);
+                    nfe++;
+                    const double fnorm = wrms_w(ft, ewt, n);
+                    const double srur = sqrt(uround);
+                    const double min_inc = (fnorm != 0.0) ? (1000.0 * fabs(h) * uround * n * fnorm) : 1.0;
+                    VLOOP {
+                        const double inc = dmaxc(srur * fabs(Z(0)[i]), min_inc / ewt[i]);
+                        bb[i] = inc;
+                        ycopy[i] = Z(0)[i] + inc;
+                    }
+                    s.f(tn, ycopy, f1);
+                    nfe++;
+                    VLOOP jd[i] = (f1[i] - ft[i]) / bb[i];
+                    nje++;
+                    nstlj = nst;
+                    jcur = 1;
+                }
+                int sing = 0;
+                VLOOP {
+                    md[i] = 1.0 - gamma * jd[i];
+                    if (md[i] == 0.0) sing = 1;
+                }
+                sing = __any_sync(0xffffffffu, sing);
+                gammap = gamma;
+                nstlp = nst;
+                crate = 1.0;
+                have_m = !sing;
+                force_setup = 0;
+                convfail_bad_j = 0;
+                if (sing) fail_conv = true;
+            }
+            if (!fail_conv) {
+                const double gamrat = gamma / gammap;
+                VLOOP {
+                    acor[i] = 0.0;
+                    y[i] = Z(0)[i];
+                }
+                double delp = 0.0, del = 0.0;
+                int converged = 0;
+                const double rl1 = 1.0 / l[1];
+                for (int mit = 0; mit < 3; ++mit) {
+                    s.f(tn, y, ft);
+                    nfe++;
+                    const double* z1 = Z(1);
+                    VLOOP bb[i] = (gamma * ft[i] - fma(rl1, z1[i], acor[i])) / md[i];
+                    if (gamrat != 1.0) {
+                        const double sc = 2.0 / (1.0 + gamrat);
+                        VLOOP bb[i] *= sc;
+                    }
+                    del = wrms_w(bb, ewt, n);
+                    const double* z0 = Z(0);
+                    VLOOP {
+                        acor[i] += bb[i];
+                        y[i] = z0[i] + acor[i];
+                    }
+                    if (mit > 0) crate = dmaxc(0.3 * crate, del / delp);
+                    const double dcon = del * dminc(1.0, crate) / tq4;
+                    if (dcon <= 1.0) {
+                        acnrm = (mit == 0) ? del : wrms_w(acor, ewt, n);
+                        converged = 1;
+                        break;
+                    }
+                    if (mit >= 1 && del > 2.0 * delp) break;
+                    delp = del;
+                }
+                if (!converged) fail_conv = true;
+            }
+            if (!fail_conv) {
+                dsm = acnrm * cq;
+                if (dsm <= 1.0) break;
+                nef++;
+                nfail++;
+                COPY_COLS(Z, ZS);
+                if (nef >= 7 || h <= hmin * 1.0000000000000002) {
+                    status = -13;
+                    goto done;
+                }
+                double eta;
+                if (nef <= 3) {
+                    eta = 1.0 / (cpow_(6.0 * dsm, 1.0 / (q + 1)) + 1e-6);
+                    eta = dmaxc(0.1, dmaxc(eta, hmin / h));
+                    if (nef >= 2) eta = dminc(eta, 0.2);
+                    RESCALE(eta);
+                    h *= eta;
+                } else {
+                    eta = dmaxc(0.1, hmin / h);
+                    h *= eta;
+                    q = 1;
+                    s.f(t, Z(0), ft);
+                    nfe++;
+                    VLOOP Z(1)[i] = h * ft[i];
+                }
+                qwait = q + 1;
+                have_acorp = 0;
+                etamax = 1.0;
+                COPY_COLS(ZS, Z);
+                continue;
+            }
+            // convergence failure
+            COPY_COLS(Z, ZS);
+            nfail++;
+            if (!jcur && have_m) {
+                force_setup = 1;
+                convfail_bad_j = 1;
+                continue;
+            }
+            ncf++;
+            if (ncf >= 10 || h <= hmin * 1.0000000000000002) {
+                status = -14;
+                goto done;
+            }
+            {
+                const double eta = dmaxc(0.25, hmin / h);
+                RESCALE(eta);
+                h *= eta;
+                qwait = q + 1;
+                have_acorp = 0;
+                etamax = 1.0;
+                force_setup = 1;
+                COPY_COLS(ZS, Z);
+            }
+        }
+        // accepted step
+        nst++;
+        {
+            const double tnew = t + h;
+            t = (tstop && (tnew >= tf || tf - tnew <= 100.0 * uround * (fabs(tnew) + fabs(h)))) ? tf : tnew;
+        }
+        for (int j = 0; j <= q; ++j) {
+            double* zj = Z(j);
+            const double lj = l[j];
+            VLOOP zj[i] = fma(lj, acor[i], zj[i]);
+        }
+        SET_EWT(Z(0));
+        s.on_step(t);
+        {
+            const double etaq = 1.0 / (cpow_(6.0 * dsm, 1.0 / (q + 1)) + 1e-6);
+            double eta = etaq;
+            int qnew = q;
+            qwait--;
+            if (qwait == 0) {
+                double etaqm1 = 0.0, etaqp1 = 0.0;
+                if (q > 1) {
+                    double fact = 1.0;
+                    for (int i = 2; i <= q; ++i) fact *= i;
+                    const double ddn = wrms_w(Z(q), ewt, n) * (fabs(g[q - 1] - g[q - 2]) * fact);
+                    etaqm1 = 1.0 / (cpow_(6.0 * ddn, 1.0 / q) + 1e-6);
+                }
+                if (q < QA && have_acorp && qsave == q) {
+                    const double cc = cpow_(h / hsave, (double)(q + 1));
+                    VLOOP tmp[i] = fma(-cc, acorp[i], acor[i]);
+                    const double dup = wrms_w(tmp, ewt, n) * (fabs(g[q + 1] - g[q]) / g[q - 1]);
+                    etaqp1 = 1.0 / (cpow_(10.0 * dup, 1.0 / (q + 2)) + 1e-6);
+                }
+                if (etaq >= etaqm1 && etaq >= etaqp1) {
+                    eta = etaq;
+                } else if (etaqm1 >= etaqp1) {
+                    eta = etaqm1;
+                    qnew = q - 1;
+                } else {
+                    eta = etaqp1;
+                    qnew = q + 1;
+                }
+                qwait = 2;
+            } else if (qwait == 1 && q < QA) {
+                VLOOP acorp[i] = acor[i];
+                hsave = h;
+                qsave = q;
+                have_acorp = 1;
+            }
+            if (etamax <= 1.0) {
+                eta = 1.0;
+                qnew = q;
+            } else if (eta < 1.5 && qnew == q) {
+                eta = 1.0;
+            } else {
+                eta = dminc(eta, etamax);
+                if (h * eta < hmin) eta = hmin / h;
+            }
+            if (qnew > q) {
+                double fact = 1.0;
+                for (int i = 2; i <= q + 1; ++i) fact *= i;
+                const double c = -1.0 / (g[q - 1] * fact);
+                double* zq1 = Z(q + 1);
+                VLOOP zq1[i] = acor[i] * c;
+            }
+            if (qnew != q) {
+                q = qnew;
+                qwait = q + 1;
+                have_acorp = 0;
+            }
+            if (eta != 1.0) {
+                RESCALE(eta);
+                h *= eta;
+            }
+            etamax = 10.0;
+        }
+    }
+    {
+        const double sv = (tf - t) / h;
+        VLOOP {
+            double v = Z(q)[i];
+            for (int j = q - 1; j >= 0; --j) v = fma(v, sv, Z(j)[i]);
+            yio[i] = v;
+        }
+    }
+done:
+    if (status != 0) {
+        const double* z0 = Z(0);
+        VLOOP yio[i] = z0[i];
+    }
+    __syncwarp();
+    if (stats) {
+        stats[0] = nst;
+        stats[1] = nfe;
+        stats[2] = nfail;
+        stats[3] = nje;
+    }
+    return status;
+#undef VLOOP
+#undef SET_EWT
+#undef COPY_COLS
+#undef RESCALE
+}
+
+// ---- per-flame data -------------------------------------------------------
+
+struct ConvFlame {
+    ember_convection_flame f;
+    int64_t p0;      // first point of the flame in the concatenated point arrays
+    int64_t v0;      // first value of the flame in the variable-major state arrays
+    int64_t utw_wk;  // UTW work slice (kWorkVectors * 3N doubles + 3N y + 6N scratch)
+    int64_t hist;    // first recorded time of the flame (max_history per flame)
+    int64_t histv;   // first recorded value of the flame (max_history * N per flame)
+};
+
+struct ConvArgs {
+    int n_flames, S;
+    const ConvFlame* flames;
+    const double* W;
+    const double* x;
+    const double* y_left;
+    const double* drhodt;
+    const double* split;
+    double* state;
+    double* wk_utw;
+    double* wk_spec;     // kWorkVectors * N per (flame, species) system, at spec_off
+    const int64_t* spec_off;
+    double* hist_t;
+    double* hist_v;
+    int* n_hist;
+    int* status;         // n_flames * (1 + S)
+    int* stats;          // n_flames * 4 or null
+    double t0, tf, reltol, abstol_u, abstol_t, abstol_y, min_step;
+    int max_steps, max_history;
+};
+
+__device__ __forceinline__ double center_volume(const double* x, int alpha) {
+    return alpha == 0 ? x[1] : (x[1] * x[1]) / 2.0;
+}
+
+// per-flame scratch inside the UTW slice, after the work vectors
+struct UtwView {
+    double *y3, *hh, *rph, *Wm, *sW, *rho, *rV, *V;
+};
+
+__device__ UtwView utw_view(const ConvArgs& a, const ConvFlame& F) {
+    const int N = F.f.n_points;
+    double* base = a.wk_utw + F.utw_wk + size_t(kWorkVectors) * 3 * N;
+    UtwView v;
+    v.y3 = base;
+    v.hh = base + 3 * size_t(N);
+    v.rph = v.hh + N;
+    v.Wm = v.rph + N;
+    v.sW = v.Wm + N;
+    v.rho = v.sW + N;
+    v.rV = v.rho + N;
+    v.V = v.rV + N;
+    return v;
+}
+
+__global__ void k_conv_prepare(const __grid_constant__ ConvArgs a) {
+    const ConvFlame& F = a.flames[blockIdx.x];
+    const int N = F.f.n_points, S = a.S;
+    const double* x = a.x + F.p0;
+    const double* st = a.state + F.v0;
+    const double* sc = a.split + F.v0;
+    UtwView u = utw_view(a, F);
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        // rph[N-1]: the radius factor at the last point, for the continuity
+        // conditions that read one half point past the grid
+        if (j < N - 1) {
+            u.hh[j] = x[j + 1] - x[j];
+            const double xm = 0.5 * (x[j] + x[j + 1]);
+            u.rph[j] = F.f.alpha == 0 ? 1.0 : xm;
+        } else {
+            u.hh[j] = 0.0;
+            u.rph[j] = F.f.alpha == 0 ? 1.0 : x[j];
+        }
+        double ysum = 0.0;
+        for (int k = 0; k < S; ++k) ysum = ysum + dmaxc(st[size_t(2 + k) * N + j], 0.0);
+        const double rnorm = 1.0 / ysum;
+        double acc = 0.0;
+        for (int k = 0; k < S; ++k) acc = acc + (dmaxc(st[size_t(2 + k) * N + j], 0.0) * rnorm) / a.W[k];
+        const double wm = 1.0 / acc;
+        u.Wm[j] = wm;
+        double sw = 0.0;
+        for (int k = 0; k < S; ++k) sw = sw + sc[size_t(2 + k) * N + j] / a.W[k];
+        u.sW[j] = sw;
+        u.y3[3 * j + 0] = st[j];
+        u.y3[3 * j + 1] = st[size_t(N) + j];
+        u.y3[3 * j + 2] = wm;
+    }
+}
+
+struct UtwSys {
+    int n;
+    const ConvArgs* a;
+    const ember_convection_flame* fl;
+    const double *x, *drhodt, *sU, *sT;
+    UtwView u;
+    double* ht;
+    double* hv;
+    int n_history, overflow, max_history;
+
+    __device__ double atol(int i) const {
+        const int c = i % 3;
+        return c == 0 ? a->abstol_u : (c == 1 ? a->abstol_t : 20.0 * a->abstol_y);
+    }
+
+    __device__ void f_(double t, const double* y, double* ydot) {
+        const int N = fl->n_points, jj = N - 1, jc = fl->j_cont, lane = lane_of();
+        const double beta = fl->beta;
+        const double *hh = u.hh, *rph = u.rph, *sW = u.sW;
+        double *rho = u.rho, *rV = u.rV, *V = u.V;
+        __syncwarp();
+        for (int j = lane; j < N; j += 32) rho[j] = (fl->pressure * y[3 * j + 2]) / (kGasConstant * y[3 * j + 1]);
+        __syncwarp();
+        if (lane == 0) {
+#define U_(j) y[3 * (j) + 0]
+#define T_(j) y[3 * (j) + 1]
+#define MFLUX(j) ((hh[j] * rph[j]) * (drhodt[j] + (rho[j] * beta) * U_(j)))
+            if (fl->continuity_bc == EMBER_CONTINUITY_LEFT) {
+                rV[0] = fl->rv_zero;
+                for (int j = 0; j < N - 1; ++j) rV[j + 1] = rV[j] - MFLUX(j);
+            } else if (fl->continuity_bc == EMBER_CONTINUITY_ZERO) {
+                int j = jc;
+                double dVdx0 = -rph[j] * (drhodt[j] - (rho[j] * beta) * U_(j));
+                if (jc != 0)
+                    dVdx0 = 0.5 * dVdx0 - (0.5 * rph[j - 1]) * (drhodt[j - 1] + (rho[j - 1] * beta) * U_(j - 1));
+                rV[j] = (x[j] - fl->x_vzero) * dVdx0;
+                for (j = jc; j < jj; ++j) rV[j + 1] = rV[j] - MFLUX(j);
+                if (jc != 0) {
+                    j = jc - 1;
+                    rV[j] = (x[j] - fl->x_vzero) * dVdx0;
+                    for (j = jc - 1; j > 0; --j) rV[j - 1] = rV[j] + MFLUX(j - 1);
+                }
+            } else {
+                if (fl->continuity_bc == EMBER_CONTINUITY_TEMP) {
+                    const int j = jc;
+                    if (j == 0 || sT[j] / (T_(j + 1) - T_(j)) < 0)
+                        rV[j] = (((rph[j] * rho[j]) * sT[j]) * hh[j]) / (T_(j + 1) - T_(j));
+                    else
+                        rV[j] = (((rph[j - 1] * rho[j]) * sT[j]) * hh[j - 1]) / (T_(j) - T_(j - 1));
+                } else {
+                    rV[jc] = fl->rv_cont;
+                }
+                for (int j = jc; j < N - 1; ++j) rV[j + 1] = rV[j] - MFLUX(j);
+                for (int j = jc; j > 0; --j)
+                    rV[j - 1] = rV[j] + (hh[j - 1] * rph[j]) * (drhodt[j] + (rho[j] * beta) * U_(j));
+            }
+#undef MFLUX
+#undef T_
+#undef U_
+        }
+        __syncwarp();
+        for (int j = lane; j < N; j += 32) V[j] = (j == 0 || fl->alpha == 0) ? rV[j] : rV[j] / x[j];
+        __syncwarp();
+        double aa, dadt;
+        {
+            const double a0 = fl->strain_initial, a1 = fl->strain_final, T0 = fl->strain_t0, Dt = fl->strain_dt;
+            aa = (t <= T0) ? a0 : (t >= T0 + Dt) ? a1 : a0 + ((a1 - a0) * (t - T0)) / Dt;
+            dadt = (t >= T0 && t < T0 + Dt) ? (a1 - a0) / Dt : 0.0;
+        }
+        const double K = dadt / beta + (aa * aa) / (beta * beta);
+        const bool cv = fl->left_bc == EMBER_BC_CONTROL_VOLUME || fl->left_bc == EMBER_BC_WALL_FLUX;
+        const bool right_fixed = rV[jj] < 0 || fl->right_bc == EMBER_BC_FIXED_VALUE;
+        for (int j = lane; j < N; j += 32) {
+            const double Uj = y[3 * j + 0], Tj = y[3 * j + 1], Wj = y[3 * j + 2];
+            const double strain_term = (fl->rhou / rho[j]) * K;
+            if (j == 0) {
+                ydot[0] = (sU[0] - Uj * Uj) + strain_term;
+                if (cv) {
+                    const double cvol = center_volume(x, fl->alpha);
+                    const double rvm = dmaxc(rV[0], 0.0);
+                    ydot[1] = (-rvm * (Tj - fl->t_left)) / (rho[0] * cvol) + sT[0];
+                    ydot[2] = (-rvm * (Wj - fl->w_left)) / (rho[0] * cvol) - (Wj * Wj) * sW[0];
+                } else {
+                    ydot[1] = sT[0];
+                    ydot[2] = -((Wj * Wj) * sW[0]);
+                }
+            } else if (j < jj) {
+                double dT, dU, dW;
+                if (rV[j] < 0) {
+                    dT = (y[3 * (j + 1) + 1] - Tj) / hh[j];
+                    dU = (y[3 * (j + 1) + 0] - Uj) / hh[j];
+                    dW = (y[3 * (j + 1) + 2] - Wj) / hh[j];
+                } else {
+                    dT = (Tj - y[3 * (j - 1) + 1]) / hh[j - 1];
+                    dU = (Uj - y[3 * (j - 1) + 0]) / hh[j - 1];
+                    dW = (Wj - y[3 * (j - 1) + 2]) / hh[j - 1];
+                }
+                ydot[3 * j + 0] = (((-V[j] * dU) / rho[j] - Uj * Uj) + strain_term) + sU[j];
+                ydot[3 * j + 1] = (-V[j] * dT) / rho[j] + sT[j];
+                ydot[3 * j + 2] = (-V[j] * dW) / rho[j] - (Wj * Wj) * sW[j];
+            } else if (right_fixed) {
+                ydot[3 * jj + 0] = (sU[jj] - Uj * Uj) + strain_term;
+                ydot[3 * jj + 1] = sT[jj];
+                ydot[3 * jj + 2] = -((Wj * Wj) * sW[jj]);
+            } else {
+                const double hl = hh[jj - 1];
+                ydot[3 * jj + 0] =
+                    ((sU[jj] - ((V[jj] * (Uj - y[3 * (jj - 1) + 0])) / hl) / rho[jj]) - Uj * Uj) + strain_term;
+                ydot[3 * jj + 1] = sT[jj] - ((V[jj] * (Tj - y[3 * (jj - 1) + 1])) / hl) / rho[jj];
+                ydot[3 * jj + 2] = -((Wj * Wj) * sW[jj]) - ((V[jj] * (Wj - y[3 * (jj - 1) + 2])) / hl) / rho[jj];
+            }
+        }
+        __syncwarp();
+    }
+    __device__ void f(double t, const double* y, double* ydot) { f_(t, y, ydot); }
+
+    __device__ void record(double t) {
+        if (n_history >= max_history) {
+            overflow = 1;
+            return;
+        }
+        const int N = fl->n_points;
+        if (lane_of() == 0) ht[n_history] = t;
+        double* v = hv + size_t(n_history) * N;
+        for (int j = lane_of(); j < N; j += 32) v[j] = u.V[j] / u.rho[j];
+        __syncwarp();
+        n_history++;
+    }
+    __device__ void on_step(double t) { record(t); }
+};
+
+__global__ void __launch_bounds__(32) k_conv_utw(const __grid_constant__ ConvArgs a) {
+    const int fi = blockIdx.x;
+    const ConvFlame& F = a.flames[fi];
+    const int N = F.f.n_points;
+    UtwSys s;
+    s.n = 3 * N;
+    s.a = &a;
+    s.fl = &F.f;
+    s.x = a.x + F.p0;
+    s.drhodt = a.drhodt + F.p0;
+    s.sU = a.split + F.v0;
+    s.sT = a.split + F.v0 + N;
+    s.u = utw_view(a, F);
+    s.ht = a.hist_t + F.hist;
+    s.hv = a.hist_v + F.histv;
+    s.n_history = 0;
+    s.overflow = 0;
+    s.max_history = a.max_history;
+    double* wk = a.wk_utw + F.utw_wk;
+    // the record starts with V / rho of the initial state
+    s.f(a.t0, s.u.y3, wk);
+    s.record(a.t0);
+    int st[4];
+    int rc = adams_warp(s, wk, s.u.y3, a.reltol, a.t0, a.tf, 1, a.min_step, a.max_steps, st);
+    if (s.overflow) rc = -20;
+    double* state = a.state + F.v0;
+    for (int j = lane_of(); j < N; j += 32) {
+        state[j] = s.u.y3[3 * j + 0];
+        state[size_t(N) + j] = s.u.y3[3 * j + 1];
+    }
+    if (lane_of() == 0) {
+        a.status[size_t(fi) * (1 + a.S)] = rc;
+        a.n_hist[fi] = s.n_history;
+        if (a.stats) {
+            a.stats[4 * fi + 0] = st[0];
+            a.stats[4 * fi + 1] = st[1];
+        }
+    }
+}
+
+struct SpecSys {
+    int n;
+    const ConvArgs* a;
+    const ember_convection_flame* fl;
+    const double *x, *hh, *split;
+    double y_left;
+    int H;
+    const double *ht, *hv;
+
+    __device__ double atol(int) const { return a->abstol_y; }
+
+    __device__ void f_(double t, const double* y, double* ydot) {
+        const int N = n, jj = N - 1, lane = lane_of();
+        __syncwarp();
+        // ConvectionSystemY::update_v: [lower_bound(t), next], moved back at the end
+        int iL = -1;
+        double s = 0.0;
+        if (H > 1) {
+            int lo = 0, hi = H;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (ht[mid] < t)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            iL = lo;
+            if (iL == H) iL--;
+            if (iL + 1 == H) iL--;
+            s = (t - ht[iL]) / (ht[iL + 1] - ht[iL]);
+        }
+        const double* vL = hv + size_t(iL < 0 ? 0 : iL) * N;
+        const double* vR = iL < 0 ? vL : vL + N;
+        auto VV = [&](int j) { return iL < 0 ? vL[j] : vL[j] * (1 - s) + vR[j] * s; };
+        const bool cv = fl->left_bc == EMBER_BC_CONTROL_VOLUME || fl->left_bc == EMBER_BC_WALL_FLUX;
+        for (int j = lane; j < N; j += 32) {
+            const double v = VV(j);
+            if (j == 0) {
+                if (cv) {
+                    const double cvol = center_volume(x, fl->alpha);
+                    const double rvm = dmaxc(v, 0.0);
+                    ydot[0] = (-rvm * (y[0] - y_left)) / cvol + split[0];
+                } else {
+                    ydot[0] = split[0];
+                }
+            } else if (j < jj) {
+                const double dYdx = (v < 0) ? (y[j + 1] - y[j]) / hh[j] : (y[j] - y[j - 1]) / hh[j - 1];
+                ydot[j] = -v * dYdx + split[j];
+            } else if (v < 0 || fl->right_bc == EMBER_BC_FIXED_VALUE) {
+                ydot[jj] = split[jj];
+            } else {
+                ydot[jj] = split[jj] - (v * (y[jj] - y[jj - 1])) / hh[jj - 1];
+            }
+        }
+        __syncwarp();
+    }
+    __device__ void f(double t, const double* y, double* ydot) { f_(t, y, ydot); }
+    __device__ void on_step(double) {}
+};
+
+__global__ void __launch_bounds__(32) k_conv_species(const __grid_constant__ ConvArgs a) {
+    const int sys = blockIdx.x;
+    const int fi = sys / a.S, k = sys % a.S;
+    const ConvFlame& F = a.flames[fi];
+    const int N = F.f.n_points;
+    int* status = a.status + size_t(fi) * (1 + a.S);
+    const int utw_rc = status[0];
+    if (utw_rc != 0) {
+        if (lane_of() == 0) status[1 + k] = utw_rc;
+        return;
+    }
+    SpecSys s;
+    s.n = N;
+    s.a = &a;
+    s.fl = &F.f;
+    s.x = a.x + F.p0;
+    s.hh = utw_view(a, F).hh;
+    s.split = a.split + F.v0 + size_t(2 + k) * N;
+    s.y_left = a.y_left[size_t(fi) * a.S + k];
+    s.H = a.n_hist[fi];
+    s.ht = a.hist_t + F.hist;
+    s.hv = a.hist_v + F.histv;
+    int st[4];
+    double* y = a.state + F.v0 + size_t(2 + k) * N;
+    const int rc = adams_warp(s, a.wk_spec + a.spec_off[sys], y, a.reltol, a.t0, a.tf, 0, a.min_step,
+                              a.max_steps, st);
+    if (lane_of() == 0) {
+        status[1 + k] = rc;
+        if (a.stats) {
+            atomicAdd(&a.stats[4 * fi + 2], st[0]);
+            atomicAdd(&a.stats[4 * fi + 3], st[1]);
+        }
+    }
+}
+
+}  // namespace
+}  // namespace ember
+
+using namespace ember;
+
+extern "C" int ember_convection_integrate(int n_flames, const ember_convection_flame* flames, int n_species,
+                                          const double* mol_weight, const double* x, const double* y_left,
+                                          const double* drhodt, const double* split_const, double* state,
+                                          const ember_convection_options* opts, int* status, int* stats, int mem,
+                                          void* stream) {
+    EMBER_CHECK_ARG(n_flames >= 0, "n_flames must be >= 0");
+    EMBER_CHECK_ARG(n_flames == 0 || (flames && mol_weight && x && y_left && drhodt && split_const && state && opts),
+                    "null argument");
+    EMBER_CHECK_ARG(n_species >= 1, "n_species must be >= 1");
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    if (n_flames == 0) return EMBER_OK;
+    EMBER_CHECK_ARG(opts->t_end > opts->t_start, "t_end must be > t_start");
+    EMBER_CHECK_ARG(opts->reltol > 0 && opts->abstol_u > 0 && opts->abstol_t > 0 && opts->abstol_y > 0,
+                    "tolerances must be positive");
+    EMBER_CHECK_ARG(opts->max_steps > 0 && opts->max_history >= 2, "max_steps > 0 and max_history >= 2 required");
+    EMBER_CHECK_ARG(opts->min_step >= 0, "min_step must be >= 0");
+    const int S = n_species, nv = S + 2;
+    std::vector<ConvFlame> hf(n_flames);
+    std::vector<int64_t> spec_off(size_t(n_flames) * S);
+    int64_t P = 0, V = 0, WU = 0, WS = 0, HS = 0, HV = 0;
+    for (int f = 0; f < n_flames; ++f) {
+        const ember_convection_flame& g = flames[f];
+        const int N = g.n_points;
+        EMBER_CHECK_ARG(N >= 3, "flame %d: n_points must be >= 3", f);
+        EMBER_CHECK_ARG(g.alpha == 0 || g.alpha == 1, "flame %d: alpha must be 0 or 1", f);
+        EMBER_CHECK_ARG(g.left_bc >= EMBER_BC_FIXED_VALUE && g.left_bc <= EMBER_BC_WALL_FLUX,
+                        "flame %d: bad left boundary condition %d", f, g.left_bc);
+        EMBER_CHECK_ARG(g.continuity_bc >= EMBER_CONTINUITY_LEFT && g.continuity_bc <= EMBER_CONTINUITY_TEMP,
+                        "flame %d: bad continuity boundary condition %d", f, g.continuity_bc);
+        EMBER_CHECK_ARG(g.continuity_bc == EMBER_CONTINUITY_LEFT || (g.j_cont >= 0 && g.j_cont < N),
+                        "flame %d: j_cont out of range", f);
+        EMBER_CHECK_ARG(g.continuity_bc != EMBER_CONTINUITY_TEMP || g.j_cont < N - 1,
+                        "flame %d: the temperature continuity point needs a right neighbour", f);
+        EMBER_CHECK_ARG(g.beta > 0 && g.pressure > 0, "flame %d: beta and pressure must be positive", f);
+        EMBER_CHECK_ARG(g.strain_dt >= 0, "flame %d: strain_dt must be >= 0", f);
+        hf[f].f = g;
+        hf[f].p0 = P;
+        hf[f].v0 = V;
+        hf[f].utw_wk = WU;
+        hf[f].hist = HS;
+        hf[f].histv = HV;
+        for (int k = 0; k < S; ++k) {
+            spec_off[size_t(f) * S + k] = WS;
+            WS += int64_t(kWorkVectors) * N;
+        }
+        P += N;
+        V += int64_t(nv) * N;
+        WU += int64_t(kWorkVectors) * 3 * N + 3 * int64_t(N) + 8 * int64_t(N);
+        HS += int64_t(opts->max_history);
+        HV += int64_t(opts->max_history) * N;
+    }
+    EMBER_TRY(ensure_device());
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    const double *dW, *dx, *dyl, *ddr, *dsp;
+    EMBER_TRY(stage_in(sc, mol_weight, size_t(S), mem, st, &dW));
+    EMBER_TRY(stage_in(sc, x, size_t(P), mem, st, &dx));
+    EMBER_TRY(stage_in(sc, y_left, size_t(n_flames) * S, mem, st, &dyl));
+    EMBER_TRY(stage_in(sc, drhodt, size_t(P), mem, st, &ddr));
+    EMBER_TRY(stage_in(sc, split_const, size_t(V), mem, st, &dsp));
+    double* dstate = nullptr;
+    EMBER_TRY(stage_buffer(sc, state, size_t(V), mem, &dstate));
+    if (mem == EMBER_MEM_HOST)
+        EMBER_CUDA_TRY(cudaMemcpyAsync(dstate, state, size_t(V) * sizeof(double), cudaMemcpyHostToDevice, st));
+    int* dstatus = nullptr;
+    EMBER_TRY(sc.alloc(&dstatus, size_t(n_flames) * (1 + S)));
+    int* dstats = nullptr;
+    if (stats) {
+        EMBER_TRY(sc.alloc(&dstats, size_t(n_flames) * 4));
+        EMBER_CUDA_TRY(cudaMemsetAsync(dstats, 0, size_t(n_flames) * 4 * sizeof(int), st));
+    }
+    ConvFlame* dflames = nullptr;
+    int64_t* dspec = nullptr;
+    double *wku = nullptr, *wks = nullptr, *ht = nullptr, *hv = nullptr;
+    int* nh = nullptr;
+    EMBER_TRY(sc.alloc(&dflames, size_t(n_flames)));
+    EMBER_TRY(sc.alloc(&dspec, spec_off.size()));
+    EMBER_TRY(sc.alloc(&wku, size_t(WU)));
+    EMBER_TRY(sc.alloc(&wks, size_t(WS)));
+    EMBER_TRY(sc.alloc(&ht, size_t(HS)));
+    EMBER_TRY(sc.alloc(&hv, size_t(HV)));
+    EMBER_TRY(sc.alloc(&nh, size_t(n_flames)));
+    EMBER_CUDA_TRY(cudaMemcpyAsync(dflames, hf.data(), hf.size() * sizeof(ConvFlame), cudaMemcpyHostToDevice, st));
+    EMBER_CUDA_TRY(
+        cudaMemcpyAsync(dspec, spec_off.data(), spec_off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    ConvArgs a{};
+    a.n_flames = n_flames;
+    a.S = S;
+    a.flames = dflames;
+    a.W = dW;
+    a.x = dx;
+    a.y_left = dyl;
+    a.drhodt = ddr;
+    a.split = dsp;
+    a.state = dstate;
+    a.wk_utw = wku;
+    a.wk_spec = wks;
+    a.spec_off = dspec;
+    a.hist_t = ht;
+    a.hist_v = hv;
+    a.n_hist = nh;
+    a.status = dstatus;
+    a.stats = dstats;
+    a.t0 = opts->t_start;
+    a.tf = opts->t_end;
+    a.reltol = opts->reltol;
+    a.abstol_u = opts->abstol_u;
+    a.abstol_t = opts->abstol_t;
+    a.abstol_y = opts->abstol_y;
+    a.min_step = opts->min_step;
+    a.max_steps = opts->max_steps;
+    a.max_history = opts->max_history;
+    k_conv_prepare<<<n_flames, 128, 0, st>>>(a);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    k_conv_utw<<<n_flames, 32, 0, st>>>(a);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    k_conv_species<<<n_flames * S, 32, 0, st>>>(a);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    EMBER_TRY(stage_out(state, dstate, size_t(V), mem, st));
+    if (status) {
+        if (mem == EMBER_MEM_HOST)
+            EMBER_CUDA_TRY(cudaMemcpyAsync(status, dstatus, size_t(n_flames) * (1 + S) * sizeof(int),
+                                           cudaMemcpyDeviceToHost, st));
+        else
+            EMBER_CUDA_TRY(cudaMemcpyAsync(status, dstatus, size_t(n_flames) * (1 + S) * sizeof(int),
+                                           cudaMemcpyDeviceToDevice, st));
+    }
+    if (stats) {
+        if (mem == EMBER_MEM_HOST)
+            EMBER_CUDA_TRY(
+                cudaMemcpyAsync(stats, dstats, size_t(n_flames) * 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        else
+            EMBER_CUDA_TRY(
+                cudaMemcpyAsync(stats, dstats, size_t(n_flames) * 4 * sizeof(int), cudaMemcpyDeviceToDevice, st));
+    }
+    const int rc = finish_call(mem, st);
+    sc.release();
+    return rc;
+}

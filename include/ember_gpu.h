@@ -222,6 +222,82 @@ int ember_diffusion_integrate_noalloc(int n_flames, const ember_diffusion_grid* 
                                       const ember_diffusion_options* opts, int* status, void* stream);
 
 /* ======================================================================
+ * Convection stage
+ *
+ * One call = ConvectionSystemSplit::integrateToTime for a batch of flames
+ * (src/convectionSystem.cpp:588-627, with setState 485-511 and
+ * setSplitConstants 572-586): per flame the UTW system
+ * (ConvectionSystemUTW::f, src/convectionSystem.cpp:14-130: continuity
+ * integral for rV from the continuity point, upwinded convection of U, T and
+ * the mean molecular weight W, strain-rate source of U) is integrated from
+ * t_start to t_end, stopping on t_end, and V / rho is recorded after every
+ * step; then every species system (ConvectionSystemY::f, 307-359, upwinded
+ * convection of Y_k) is integrated to t_end with v(t) interpolated from that
+ * record as ConvectionSystemY::update_v does (372-398). The reference runs
+ * CVODE's Adams method with a zero-bandwidth difference-quotient Jacobian for
+ * both (src/convectionSystem.cpp:467-478, 663-676); this library runs an own
+ * variable-order (1..12) Adams-Moulton integrator with a diagonal
+ * difference-quotient Jacobian (same step and order control as its BDF).
+ *
+ * Layout: flame f has n_points N_f; x and drhodt are concatenated over
+ * flames; state and split_const are variable-major per flame (U, T, Y_0 ..
+ * Y_{S-1}; element (v, j) at var_offset_f + v*N_f + j, as for the diffusion
+ * stage); y_left holds S mass fractions per flame. U, T and Y are replaced by
+ * the stage's result; W is not part of the state (the reference keeps it
+ * inside the convection system).
+ * ==================================================================== */
+#define EMBER_CONTINUITY_LEFT  0   /* fixedLeft: rV[0] = rv_zero                      */
+#define EMBER_CONTINUITY_RIGHT 1   /* fixedRight: rV[j_cont] = rv_cont, j_cont = N-1  */
+#define EMBER_CONTINUITY_ZERO  2   /* stagnationPoint: V = 0 at x_vzero               */
+#define EMBER_CONTINUITY_QDOT  3   /* fixedQdot: rV[j_cont] = rv_cont                 */
+#define EMBER_CONTINUITY_TEMP  4   /* fixedTemperature: dT/dt = 0 at j_cont           */
+
+typedef struct {
+    int n_points;          /* N_f >= 3                                                */
+    int left_bc;           /* EMBER_BC_FIXED_VALUE / ZERO_GRADIENT / CONTROL_VOLUME / WALL_FLUX */
+    int right_bc;          /* EMBER_BC_FIXED_VALUE, else outflow when V > 0 there     */
+    int alpha;             /* 0 planar, 1 cylindrical                                 */
+    int continuity_bc;     /* EMBER_CONTINUITY_*                                      */
+    int j_cont;            /* jContBC (ignored for LEFT)                              */
+    double beta;           /* grid.beta                                               */
+    double x_vzero;        /* xVzero (ZERO)                                           */
+    double rv_zero;        /* rVzero (LEFT)                                           */
+    double rv_cont;        /* rV[jContBC] carried into the stage (RIGHT, QDOT): the
+                              reference's f() leaves it as it was                    */
+    double t_left;         /* Tleft                                                   */
+    double w_left;         /* Wleft, mean molecular weight at the left boundary       */
+    double rhou;           /* unburned density                                        */
+    double pressure;       /* Pa                                                      */
+    double strain_initial, strain_final, strain_t0, strain_dt;  /* a(t): LinearFunction
+                              (src/scalarFunction.cpp:12-22); equal initial and final
+                              values give a constant strain rate                     */
+} ember_convection_flame;
+
+typedef struct {
+    double t_start, t_end;   /* tStageStart, tStageEnd                                */
+    double reltol;           /* integratorRelTol (1e-6)                               */
+    double abstol_u;         /* integratorMomentumAbsTol (1e-7)                       */
+    double abstol_t;         /* integratorEnergyAbsTol (1e-8)                         */
+    double abstol_y;         /* integratorSpeciesAbsTol (1e-13); W uses 20 times it   */
+    double min_step;         /* minStep (1e-16)                                       */
+    int max_steps;           /* per system                                            */
+    int max_history;         /* recorded V / rho per flame: UTW steps + 1             */
+} ember_convection_options;
+
+/* status: n_flames * (1 + S) ints, may be NULL: per flame the UTW status
+ * then one per species (0 ok; -11 too many steps, -13 error-test failures,
+ * -14 convergence failures, -20 record full; a failed UTW integration marks
+ * its species with its own status and leaves them unchanged). stats:
+ * n_flames * 4 ints or NULL: UTW steps, UTW right-hand sides, species steps
+ * and right-hand sides summed over species. Per-flame structs and opts are
+ * host memory; every array is in the `mem` space. */
+int ember_convection_integrate(int n_flames, const ember_convection_flame* flames, int n_species,
+                               const double* mol_weight, const double* x, const double* y_left,
+                               const double* drhodt, const double* split_const, double* state,
+                               const ember_convection_options* opts, int* status, int* stats, int mem,
+                               void* stream);
+
+/* ======================================================================
  * Mechanism tables
  *
  * A gas-phase mechanism compiled once into structure-of-arrays device

@@ -140,6 +140,40 @@ void oracle_transport_eval_threads(const oracle_mech* m, const double* visc_fit,
                                    double* cp_species, double* h_species, double* conductivity, double* viscosity,
                                    double* rho_d, int n_threads);
 
+/* ---- convection stage (oracle_convection.c) ------------------------------ */
+#define ORACLE_BC_FIXED_VALUE 0
+#define ORACLE_BC_ZERO_GRADIENT 1
+#define ORACLE_BC_CONTROL_VOLUME 2
+#define ORACLE_BC_WALL_FLUX 3
+#define ORACLE_CONT_LEFT 0
+#define ORACLE_CONT_RIGHT 1
+#define ORACLE_CONT_ZERO 2
+#define ORACLE_CONT_QDOT 3
+#define ORACLE_CONT_TEMP 4
+typedef struct {
+    int n_points, left_bc, right_bc, alpha, continuity_bc, j_cont;
+    double beta, x_vzero, rv_zero, rv_cont, t_left, w_left, rhou, pressure;
+    double strain_initial, strain_final, strain_t0, strain_dt;
+} oracle_conv_flame;
+typedef struct {
+    double reltol, abstol_u, abstol_t, abstol_y, min_step;
+    int max_steps, max_history;
+} oracle_conv_options;
+void oracle_adams_gammas(double* g);
+void oracle_adams_l(int q, double* l);
+void oracle_convection_grid(int N, const double* x, int alpha, double* hh, double* rph);
+void oracle_convection_prepare(int N, int S, const double* W, const double* state, const double* split,
+                               double* Wmx, double* sW);
+void oracle_convection_utw_rhs(const oracle_conv_flame* fl, const double* x, const double* hh, const double* rph,
+                               double t, const double* y, const double* drhodt, const double* sU,
+                               const double* sT, const double* sW, double* ydot, double* rho, double* rV,
+                               double* V);
+int oracle_convection_interval(const double* ht, int H, double t, double* s);
+int oracle_convection_flame(const oracle_conv_flame* fl, int S, const double* W, const double* x,
+                            const double* y_left, double t0, double tf, const double* drhodt, const double* split,
+                            double* state, const oracle_conv_options* o, int* status, int* stats,
+                            int* n_history_out, double* hist_t_out, double* hist_v_out);
+
 #ifdef __cplusplus
 }
 #endif
