@@ -47,7 +47,8 @@ def parse_args():
     p.add_argument("--steps", type=int, default=10)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--workload", default="qss", choices=["qss", "bdf", "diffusion", "split", "adjoint", "transport"])
+    p.add_argument("--workload", default="qss", choices=["qss", "bdf", "diffusion", "split", "adjoint", "transport",
+                                                             "convection"])
     p.add_argument("--points", type=int, default=N_POINTS)
     p.add_argument("--kinetics", default="interp", choices=["interp", "standard"])
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
@@ -982,11 +983,181 @@ def run_ours_transport(args):
         torch.distributed.destroy_process_group()
     return 0
 
+# ------------------------------------------------------------ convection --
+
+CONV_METRIC = "convection-stage points/s"
+CONV_DT = 1e-5
+CONV_WORKLOAD = ("convection stage (ConvectionSystemSplit::integrateToTime) of 32 seeded strained-flame profiles "
+                 "(150-700 points, strain rates 100-2000 1/s), synthetic 53-species mechanism: per flame the UTW "
+                 "system and 53 species systems, Adams integrators, one stage of 1e-5 s (half the 2e-5 s global "
+                 "step)")
+
+
+def convection_inputs(rank: int):
+    from ember_gb300.convection import convection_batch
+    from ember_gb300.mechanism import synthetic_mechanism
+    mech = synthetic_mechanism(n_species=53, n_reactions=325, seed=53_325)
+    return mech, convection_batch(mech, n_flames=32, n_min=150, n_max=700, seed=3232 + rank, split_scale=0.1,
+                                  drhodt_scale=0.1)
+
+
+def _convection_cpu_rate(mech, b, target_s: float, threads: int):
+    """Points/s of the oracle over whole flames, one flame per thread (ctypes
+    releases the interpreter lock), on a growing prefix of the flames."""
+    from concurrent.futures import ThreadPoolExecutor
+    from ember_gb300.convection import ConvectionOptions
+    from oracle import convection as oc
+    S = mech.n_species
+    opts = ConvectionOptions()
+    offs, voffs = [0], [0]
+    for fl in b.flames:
+        offs.append(offs[-1] + fl.n_points)
+        voffs.append(voffs[-1] + (S + 2) * fl.n_points)
+
+    def one(f):
+        fl = b.flames[f]
+        p0, p1, v0, v1 = offs[f], offs[f + 1], voffs[f], voffs[f + 1]
+        oc.convection_flame(fl, mech.mol_weight, b.x[p0:p1], b.y_left[f], b.drhodt[p0:p1], b.split_const[v0:v1],
+                            b.state[v0:v1], 0.0, CONV_DT, opts)
+        return fl.n_points
+
+    n = min(len(b.flames), threads)
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        while True:
+            t0 = time.perf_counter()
+            pts = sum(ex.map(one, range(n)))
+            t = time.perf_counter() - t0
+            if t > target_s / 4 or n >= len(b.flames):
+                return pts / t, n, t
+            n = min(len(b.flames), n * 2)
+
+
+def run_reference_convection(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return 0
+    mech, b = convection_inputs(0)
+    threads = os.cpu_count() or 1
+    rates = [_convection_cpu_rate(mech, b, args.cpu_seconds / max(args.steps, 1), threads)
+             for _ in range(args.steps)]
+    rate = statistics.median(r[0] for r in rates)
+    total = sum(fl.n_points for fl in b.flames)
+    print(json.dumps({
+        "impl": "reference", "metric": CONV_METRIC, "value": rate, "unit": "points/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / rate, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": CONV_WORKLOAD, "flames": len(b.flames), "points": total},
+        "cpu_baseline": {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
+                         "sample": f"first {rates[0][1]} flames per step, one flame per thread, {threads} threads"},
+        "e2e": {"value": rate, "unit": "points/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+    return 0
+
+
+def run_ours_convection(args):
+    import ctypes as C
+    import numpy as np
+    import torch
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        torch.distributed.init_process_group("nccl")
+    from ember_gb300 import _lib, roofline
+    from ember_gb300.convection import ConvectionOptions, integrate_convection_terms
+    mech, b = convection_inputs(rank)
+    S = mech.n_species
+    dev = torch.device("cuda", local)
+    opts = ConvectionOptions()
+    x_d, yl_d, dr_d, sc_d = (torch.as_tensor(np.ascontiguousarray(a), device=dev)
+                             for a in (b.x, b.y_left, b.drhodt, b.split_const))
+    W_d = torch.as_tensor(mech.mol_weight, device=dev)
+    init_d = torch.as_tensor(b.state, device=dev)
+    work = init_d.clone()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    peak = C.c_double()
+    _lib.check(_lib.lib().ember_probe_fp64_rate(0, C.byref(peak)), "probe")
+
+    def stage():
+        return integrate_convection_terms(b.flames, W_d, x_d, yl_d, dr_d, sc_d, work, 0.0, CONV_DT, opts,
+                                          stream=stream)
+
+
+    for _ in range(args.warmup):
+        work.copy_(init_d)
+        stage()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for i in range(args.steps):
+        work.copy_(init_d)
+        flush.zero_()
+        starts[i].record(stream)
+        _, status, stats = stage()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    total_ms = max_over_ranks(total_ms, ws, dev)
+    status = status.cpu().numpy()
+    stats = stats.cpu().numpy()
+    # end to end: host arrays in, the state back on the host
+    e2e = []
+    for _ in range(args.steps):
+        st_h = b.state.copy()
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        integrate_convection_terms(b.flames, mech.mol_weight, b.x, b.y_left, b.drhodt, b.split_const, st_h, 0.0,
+                                   CONV_DT, opts)
+        e2e.append(time.perf_counter() - t0)
+    clocks = sampler.stop()
+    ms = total_ms / args.steps
+    npts = int(sum(fl.n_points for fl in b.flames))
+    Ns = np.array([fl.n_points for fl in b.flames], dtype=float)
+    flops = float(np.sum(roofline.convection_flame_flops(Ns, stats)))
+    achieved = flops / (ms / 1e3) / 1e12
+    h2d = b.state.nbytes + b.split_const.nbytes + b.x.nbytes + b.drhodt.nbytes + b.y_left.nbytes
+    line = {
+        "metric": CONV_METRIC, "value": ws * npts / (ms / 1e3), "unit": "points/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded strained-flame profiles)",
+        "config": {"workload": CONV_WORKLOAD, "flames": len(b.flames), "points": npts, "n_species": S,
+                   "failed_systems": int((status != 0).sum()),
+                   "mean_utw_steps": float(stats[:, 0].mean()),
+                   "mean_species_steps": float(stats[:, 2].sum() / (S * len(b.flames))),
+                   "l2": "256 MB buffer written between timed iterations"},
+        "e2e": {"value": ws * npts * len(e2e) / sum(e2e), "unit": "points/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(b.state.nbytes)},
+        "gpu_launches": 3 * args.steps,
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
+                     "frac": achieved / (peak.value / 1e12), "traffic": None,
+                     "peak_source": "live DFMA throughput probe (ember_probe_fp64_rate)",
+                     "work_model": "roofline.convection_flame_flops over the measured step and RHS counts"},
+        "clocks": clocks,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, nf, t = _convection_cpu_rate(mech, b, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
+                                "sample": f"first {nf} flames, one flame per thread, {t:.1f} s on {threads} threads"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
 
 def main():
     args = parse_args()
     if args.workload == "transport":
         return run_reference_transport(args) if args.impl == "reference" else run_ours_transport(args)
+    if args.workload == "convection":
+        return run_reference_convection(args) if args.impl == "reference" else run_ours_convection(args)
     if args.workload == "diffusion":
         return run_reference_diffusion(args) if args.impl == "reference" else run_ours_diffusion(args)
     if args.workload == "split":

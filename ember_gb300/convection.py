@@ -4,7 +4,7 @@ a batch of flames -- the UTW system (continuity, upwinded convection of U, T
 and the mean molecular weight) stepped to the stage end with V / rho recorded
 after every step, then one convection system per species with v(t)
 interpolated from that record. Adams integrators with a diagonal
-difference-quotient Jacobian, one warp per system.
+difference-quotient Jacobian, one 256-thread CTA per system.
 
 ``convection_batch`` builds a seeded flame-like batch (the strained-flame
 profiles of ``split.flame_batch`` with a strained-flow velocity profile).
@@ -36,7 +36,7 @@ class ConvectionFlameC(C.Structure):
 class ConvectionOptionsC(C.Structure):
     _fields_ = [("t_start", C.c_double), ("t_end", C.c_double), ("reltol", C.c_double), ("abstol_u", C.c_double),
                 ("abstol_t", C.c_double), ("abstol_y", C.c_double), ("min_step", C.c_double),
-                ("max_steps", C.c_int), ("max_history", C.c_int)]
+                ("max_steps", C.c_int), ("max_history", C.c_int), ("species_threads", C.c_int)]
 
 
 @dataclass
@@ -75,6 +75,7 @@ class ConvectionOptions:
     min_step: float = 1e-16     # SundialsCvode::minStep as set by setState
     max_steps: int = 100000
     max_history: int = 4096
+    species_threads: int = 0    # CTA width of a species system: 0 or 32 (one warp)
 
 
 def mean_molecular_weight(Y, W):
@@ -106,7 +107,7 @@ def integrate_convection_terms(flames, mol_weight, x, y_left, drhodt, split_cons
     mem = L.mem_of(state)
     arr = (ConvectionFlameC * max(nf, 1))(*[f.as_c() for f in flames])
     o = ConvectionOptionsC(float(t_start), float(t_end), opts.reltol, opts.abstol_u, opts.abstol_t, opts.abstol_y,
-                           opts.min_step, int(opts.max_steps), int(opts.max_history))
+                           opts.min_step, int(opts.max_steps), int(opts.max_history), int(opts.species_threads))
     if mem == L.MEM_HOST:
         conv = lambda a: np.ascontiguousarray(a, dtype=np.float64)  # noqa: E731
         W, x, y_left, drhodt, split_const = map(conv, (mol_weight, x, y_left, drhodt, split_const))

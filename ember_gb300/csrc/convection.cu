@@ -4,11 +4,11 @@
 //   k_conv_prepare   one CTA per flame: grid metrics, the initial mean
 //                    molecular weight W from the mass fractions and the W
 //                    split constant (src/convectionSystem.cpp:485-511, 572-586)
-//   k_conv_utw       one warp per flame: the UTW system
+//   k_conv_utw       one CTA per flame: the UTW system
 //                    (ConvectionSystemUTW::f, src/convectionSystem.cpp:14-130)
 //                    integrated to the stage end with a stop time, V / rho
 //                    recorded after every step (src/convectionSystem.cpp:592-611)
-//   k_conv_species   one warp per (flame, species): ConvectionSystemY::f
+//   k_conv_species   one CTA per (flame, species): ConvectionSystemY::f
 //                    (src/convectionSystem.cpp:307-359) with v(t) interpolated
 //                    from that record (ConvectionSystemY::update_v, 372-398),
 //                    integrated past the stage end and interpolated back
@@ -16,13 +16,18 @@
 // Both integrations use the Adams method (variable order 1..12, Nordsieck
 // form) with a diagonal difference-quotient Jacobian: the reference runs
 // CVODE's Adams method with a zero-bandwidth banded Jacobian
-// (src/convectionSystem.cpp:467-478, 663-676). Every vector operation is
-// lane-strided over one warp; weighted norms are summed with term i on lane
-// i mod 32 and an xor butterfly; the continuity integral runs on lane 0 in
-// point order. The Nordsieck arrays and the per-system vectors live in a
-// global work slice per system (40 vectors). Compiled with --fmad=false, the
-// results are bitwise those of the CPU restatement.
+// (src/convectionSystem.cpp:467-478, 663-676). A CTA owns one system (256
+// threads for a UTW system, one warp for a species system, whose integrator
+// control is scalar work every warp of a CTA would repeat); thread t of NT
+// owns elements t, t + NT, ..., and every operation on the Nordsieck columns
+// of an element is one pass; weighted norms are summed in NT slots (term i in
+// slot i mod NT) folded in slot order. The continuity
+// integral runs on one thread in point order over increments computed in
+// parallel. The Nordsieck arrays and the per-system vectors live in a global
+// work slice per system (40 vectors). Compiled with --fmad=false, the results
+// are bitwise those of the CPU restatement.
 #include <cstdint>
+#include <type_traits>
 
 #include "common.cuh"
 #include "emath.cuh"
@@ -37,7 +42,12 @@ constexpr double kGasConstant = 6.02214076e26 * 1.380649e-23;
 __device__ __forceinline__ double dmaxc(double a, double b) { return (a < b) ? b : a; }
 __device__ __forceinline__ double dminc(double a, double b) { return (b < a) ? b : a; }
 __device__ __forceinline__ double cpow_(double x, double e) { return em_exp(e * em_log(x)); }
-__device__ __forceinline__ int lane_of() { return threadIdx.x & 31; }
+
+// Threads of a UTW system's CTA and of a species system's CTA: the control
+// of an integrator is scalar work every warp of a CTA repeats, and a species
+// system is short (its points), so it gets one warp.
+constexpr int kNT = 256;
+constexpr int kNTSpecies = 32;
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -45,20 +55,56 @@ __device__ __forceinline__ double warp_sum(double v) {
     return v;
 }
 
-__device__ __forceinline__ double warp_max(double v) {
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) v = dmaxc(v, __shfl_xor_sync(0xffffffffu, v, off));
-    return v;
+// Norms are summed in NT slots, one per thread of the CTA: element i goes to
+// slot i mod NT (each slot in increasing i), the slots are folded into 32 in
+// slot order, then an xor butterfly. The CPU restatement sums in the same
+// order with the same slot count.
+constexpr int kRed = 2 * 256 + 2;  // shared doubles of the reductions (NT <= 256)
+
+// Apply f(i, acc0, acc1) to every element of this thread and return both sums
+// to every thread; red: kRed doubles of shared memory.
+template <int NT, class F>
+__device__ void slot_pass(int n, double* red, F&& f, double& s0, double& s1) {
+    const int t = threadIdx.x;
+    double a0 = 0.0, a1 = 0.0;
+    for (int i = t; i < n; i += NT) f(i, a0, a1);
+    __syncthreads();
+    red[t] = a0;
+    red[NT + t] = a1;
+    __syncthreads();
+    if (t < 32) {
+        double v0 = red[t], v1 = red[NT + t];
+        for (int w = 1; w < NT / 32; ++w) {
+            v0 = v0 + red[t + 32 * w];
+            v1 = v1 + red[NT + t + 32 * w];
+        }
+        v0 = warp_sum(v0);
+        v1 = warp_sum(v1);
+        if (t == 0) {
+            red[2 * NT] = v0;
+            red[2 * NT + 1] = v1;
+        }
+    }
+    __syncthreads();
+    s0 = red[2 * NT];
+    s1 = red[2 * NT + 1];
 }
 
-// sqrt(sum (v_i ewt_i)^2 / n), term i on lane i mod 32
-__device__ double wrms_w(const double* v, const double* ewt, int n) {
-    double p = 0.0;
-    for (int i = lane_of(); i < n; i += 32) {
-        const double t = v[i] * ewt[i];
-        p = fma(t, t, p);
+template <int NT>
+__device__ double block_max(double v, double* red) {
+    const int t = threadIdx.x;
+    __syncthreads();
+    red[t] = v;
+    __syncthreads();
+    if (t < 32) {
+        double m = red[t];
+        for (int w = 1; w < NT / 32; ++w) m = dmaxc(m, red[t + 32 * w]);
+#pragma unroll
+        for (int off = 16; off >= 1; off >>= 1) m = dmaxc(m, __shfl_xor_sync(0xffffffffu, m, off));
+        if (t == 0) red[2 * NT] = m;
     }
-    return sqrt(warp_sum(p) / n);
+    __syncthreads();
+    return red[2 * NT];
 }
 
 struct AdamsConst {
@@ -93,52 +139,105 @@ __device__ void adams_l(int q, double* l) {
     for (int j = 0; j < q; ++j) l[j + 1] = (p[j] / (double)(j + 1)) / q0;
 }
 
-// One warp integrates y' = f(t, y) from t0 to tf (tstop: the last step ends
-// on tf; else past tf, then interpolated). `wk` holds kWorkVectors * n
-// doubles. Same operations, in the same order, as the CPU restatement.
-template <class Sys>
-__device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t0, double tf, int tstop,
-                          double hmin, int max_steps, int* stats) {
-    const int n = s.n, lane = lane_of();
+// Block-uniform coefficients, in shared memory: the Adams constants g, the
+// corrector's l and the column factors scj of the last rescaling.
+struct AdamsShared {
+    double g[QA + 2], l[QA + 2], scj[QA + 2];
+};
+
+// scj[j] = eta^j as the running product eta, eta*eta, ... (scj[0] = 1);
+// thread 0 writes once every thread is done with the previous factors,
+// everyone reads after the second barrier
+__device__ __forceinline__ void powers(double eta, int q, double* scj) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        scj[0] = 1.0;
+        double sc = eta;
+        for (int j = 1; j <= q; ++j) {
+            scj[j] = sc;
+            sc *= eta;
+        }
+    }
+    __syncthreads();
+}
+
+// Call f with std::integral_constant<int, q> (1 <= q <= QA): the per-element
+// loops over the Nordsieck columns are unrolled for the current order.
+template <class F>
+__device__ __forceinline__ void with_q(int q, F&& f) {
+    switch (q) {
+        case 1: f(std::integral_constant<int, 1>{}); break;
+        case 2: f(std::integral_constant<int, 2>{}); break;
+        case 3: f(std::integral_constant<int, 3>{}); break;
+        case 4: f(std::integral_constant<int, 4>{}); break;
+        case 5: f(std::integral_constant<int, 5>{}); break;
+        case 6: f(std::integral_constant<int, 6>{}); break;
+        case 7: f(std::integral_constant<int, 7>{}); break;
+        case 8: f(std::integral_constant<int, 8>{}); break;
+        case 9: f(std::integral_constant<int, 9>{}); break;
+        case 10: f(std::integral_constant<int, 10>{}); break;
+        case 11: f(std::integral_constant<int, 11>{}); break;
+        default: f(std::integral_constant<int, 12>{}); break;
+    }
+}
+
+// One CTA of NT threads integrates y' = f(t, y) from t0 to tf (tstop: the
+// last step ends on tf; else past tf, then interpolated). `wk` holds
+// kWorkVectors * n doubles. Per element, the same operations in the same
+// order as the CPU restatement; the Nordsieck columns of an element are
+// handled together in one pass.
+template <int NT, class Sys>
+__device__ int adams_block(Sys& s, double* wk, double* yio, double rtol, double t0, double tf, int tstop,
+                           double hmin, int max_steps, int* stats, double* red, AdamsShared& sh) {
+    const int n = s.n, tid = threadIdx.x;
     auto Z = [&](int j) { return wk + size_t(j) * n; };
     auto ZS = [&](int j) { return wk + size_t(QA + 2 + j) * n; };
     double* b0 = wk + size_t(2 * (QA + 2)) * n;
     double *acor = b0, *acorp = b0 + n, *ewt = b0 + 2 * size_t(n), *y = b0 + 3 * size_t(n);
-    double *ft = b0 + 4 * size_t(n), *bb = b0 + 5 * size_t(n), *tmp = b0 + 6 * size_t(n);
+    double *ft = b0 + 4 * size_t(n), *bb = b0 + 5 * size_t(n);
     double *f0 = b0 + 7 * size_t(n), *ycopy = b0 + 8 * size_t(n), *f1 = b0 + 9 * size_t(n);
     double *jd = b0 + 10 * size_t(n), *md = b0 + 11 * size_t(n);
     const double uround = 2.220446049250313e-16;
-    const AdamsConst C;
-    const double* g = C.g;
+    if (tid == 0) {
+        const AdamsConst C;
+        for (int j = 0; j <= QA + 1; ++j) sh.g[j] = C.g[j];
+    }
+    __syncthreads();
+    const double* g = sh.g;
+    double* scj = sh.scj;
+    double* l = sh.l;
     int nst = 0, nfe = 0, nje = 0, nfail = 0, status = 0;
-#define VLOOP for (int i = lane; i < n; i += 32)
-#define SET_EWT(v) VLOOP ewt[i] = 1.0 / (rtol * fabs((v)[i]) + s.atol(i));
-#define COPY_COLS(dst, src)                                  \
-    for (int j = 0; j <= q; ++j) {                           \
-        double* d_ = dst(j);                                 \
-        const double* s_ = src(j);                           \
-        VLOOP d_[i] = s_[i];                                 \
-    }
-#define RESCALE(eta_)                                        \
-    {                                                        \
-        double sc_ = (eta_);                                 \
-        for (int j = 1; j <= q; ++j) {                       \
-            double* zj_ = Z(j);                              \
-            VLOOP zj_[i] *= sc_;                             \
-            sc_ *= (eta_);                                   \
-        }                                                    \
-    }
+#define VLOOP for (int i = tid; i < n; i += NT)
+    // restore from the saved columns (restore != 0), rescale column j by
+    // scj[j] (rescale != 0), save into the saved columns (save != 0)
+    auto cols = [&](int q, bool restore, bool rescale, bool save) {
+        with_q(q, [&](auto qc) {
+            constexpr int Q = decltype(qc)::value;
+            VLOOP {
+#pragma unroll
+                for (int j = 0; j <= Q; ++j) {
+                    double v = restore ? ZS(j)[i] : Z(j)[i];
+                    if (rescale && j >= 1) v *= scj[j];
+                    if (restore || rescale) Z(j)[i] = v;
+                    if (save) ZS(j)[i] = v;
+                }
+            }
+        });
+    };
+    double sa, sb;
 
     VLOOP Z(0)[i] = yio[i];
     s.f(t0, Z(0), f0);
     nfe++;
-    SET_EWT(Z(0));
+    double rmax = 0.0;
+    VLOOP {
+        ewt[i] = 1.0 / (rtol * fabs(Z(0)[i]) + s.atol(i));
+        rmax = dmaxc(rmax, fabs(f0[i]) / (0.1 * fabs(Z(0)[i]) + s.atol(i)));
+    }
+    rmax = block_max<NT>(rmax, red);
     double t = t0;
     const double tdist = tf - t0;
     double hub = 0.1 * tdist;
-    double rmax = 0.0;
-    VLOOP rmax = dmaxc(rmax, fabs(f0[i]) / (0.1 * fabs(Z(0)[i]) + s.atol(i)));
-    rmax = warp_max(rmax);
     if (rmax * hub > 1.0) hub = 1.0 / rmax;
     const double hlb = 100.0 * uround * dmaxc(fabs(t0), fabs(tf));
     double hg = sqrt(hlb * hub);
@@ -148,8 +247,11 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
             VLOOP ycopy[i] = fma(hg, f0[i], Z(0)[i]);
             s.f(t0 + hg, ycopy, f1);
             nfe++;
-            VLOOP tmp[i] = (f1[i] - f0[i]) / hg;
-            const double ydd = wrms_w(tmp, ewt, n);
+            slot_pass<NT>(n, red, [&](int i, double& p, double&) {
+                const double tv = ((f1[i] - f0[i]) / hg) * ewt[i];
+                p = fma(tv, tv, p);
+            }, sa, sb);
+            const double ydd = sqrt(sa / n);
             const double hnew = (ydd * hub * hub > 2.0) ? sqrt(2.0 / ydd) : sqrt(hg * hub);
             const double ratio = hnew / hg;
             hg = hnew;
@@ -164,7 +266,6 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
 
     int q = 1, qwait = 2, nstlp = 0, nstlj = 0, have_m = 0, have_acorp = 0, qsave = 0;
     double gammap = 0.0, crate = 1.0, etamax = 10000.0, acnrm = 0.0, hsave = 0.0;
-    double l[QA + 2];
 
     while (t < tf) {
         if (nst >= max_steps) {
@@ -172,22 +273,34 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
             break;
         }
         if (tstop && t + h > tf) {
-            const double eta = (tf - t) / h;
-            RESCALE(eta);
+            powers((tf - t) / h, q, scj);
+            cols(q, false, true, true);
             h = tf - t;
+        } else {
+            cols(q, false, false, true);
         }
-        COPY_COLS(ZS, Z);
         int ncf = 0, nef = 0, convfail_bad_j = 0, force_setup = !have_m;
         double dsm = 0.0;
         for (;;) {
-            for (int k = 1; k <= q; ++k)
-                for (int j = q; j >= k; --j) {
-                    double* a = Z(j - 1);
-                    const double* b = Z(j);
-                    VLOOP a[i] += b[i];
+            // predict (Pascal triangle on each element's columns)
+            with_q(q, [&](auto qc) {
+                constexpr int Q = decltype(qc)::value;
+                VLOOP {
+                    double v[Q + 1];
+#pragma unroll
+                    for (int j = 0; j <= Q; ++j) v[j] = Z(j)[i];
+#pragma unroll
+                    for (int k = 1; k <= Q; ++k)
+#pragma unroll
+                        for (int j = Q; j >= k; --j) v[j - 1] += v[j];
+#pragma unroll
+                    for (int j = 0; j <= Q; ++j) Z(j)[i] = v[j];
                 }
+            });
             const double tn = t + h;
-            adams_l(q, l);
+            __syncthreads();  // every thread is done with the previous l
+            if (tid == 0) adams_l(q, l);
+            __syncthreads();
             const double cq = fabs(g[q] - g[q - 1]) / g[q - 1];
             const double gamma = h / l[1];
             const double tq4 = 0.1 / cq;
@@ -196,10 +309,15 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
             bool fail_conv = false;
             if (force_setup || nst >= nstlp + 20 || fabs(gamrat0 - 1.0) > 0.3) {
                 const int jbad = (nst == 0) || (nst >= nstlj + 51) || convfail_bad_j || !have_m;
+                int sing = 0;
                 if (jbad) {
                     s.f(tn, Z(0), ft);
                     nfe++;
-                    const double fnorm = wrms_w(ft, ewt, n);
+                    slot_pass<NT>(n, red, [&](int i, double& p, double&) {
+                        const double tv = ft[i] * ewt[i];
+                        p = fma(tv, tv, p);
+                    }, sa, sb);
+                    const double fnorm = sqrt(sa / n);
                     const double srur = sqrt(uround);
                     const double min_inc = (fnorm != 0.0) ? (1000.0 * fabs(h) * uround * n * fnorm) : 1.0;
                     VLOOP {
@@ -209,17 +327,21 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
                     }
                     s.f(tn, ycopy, f1);
                     nfe++;
-                    VLOOP jd[i] = (f1[i] - ft[i]) / bb[i];
+                    VLOOP {
+                        jd[i] = (f1[i] - ft[i]) / bb[i];
+                        md[i] = 1.0 - gamma * jd[i];
+                        if (md[i] == 0.0) sing = 1;
+                    }
                     nje++;
                     nstlj = nst;
                     jcur = 1;
+                } else {
+                    VLOOP {
+                        md[i] = 1.0 - gamma * jd[i];
+                        if (md[i] == 0.0) sing = 1;
+                    }
                 }
-                int sing = 0;
-                VLOOP {
-                    md[i] = 1.0 - gamma * jd[i];
-                    if (md[i] == 0.0) sing = 1;
-                }
-                sing = __any_sync(0xffffffffu, sing);
+                sing = __syncthreads_or(sing);
                 gammap = gamma;
                 nstlp = nst;
                 crate = 1.0;
@@ -237,25 +359,26 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
                 double delp = 0.0, del = 0.0;
                 int converged = 0;
                 const double rl1 = 1.0 / l[1];
+                const double scg = 2.0 / (1.0 + gamrat);
                 for (int mit = 0; mit < 3; ++mit) {
                     s.f(tn, y, ft);
                     nfe++;
-                    const double* z1 = Z(1);
-                    VLOOP bb[i] = (gamma * ft[i] - fma(rl1, z1[i], acor[i])) / md[i];
-                    if (gamrat != 1.0) {
-                        const double sc = 2.0 / (1.0 + gamrat);
-                        VLOOP bb[i] *= sc;
-                    }
-                    del = wrms_w(bb, ewt, n);
-                    const double* z0 = Z(0);
-                    VLOOP {
-                        acor[i] += bb[i];
-                        y[i] = z0[i] + acor[i];
-                    }
+                    slot_pass<NT>(n, red, [&](int i, double& p0, double& p1) {
+                        double b = (gamma * ft[i] - fma(rl1, Z(1)[i], acor[i])) / md[i];
+                        if (gamrat != 1.0) b *= scg;
+                        const double tv = b * ewt[i];
+                        p0 = fma(tv, tv, p0);
+                        const double a = acor[i] + b;
+                        acor[i] = a;
+                        y[i] = Z(0)[i] + a;
+                        const double ta = a * ewt[i];
+                        p1 = fma(ta, ta, p1);
+                    }, sa, sb);
+                    del = sqrt(sa / n);
                     if (mit > 0) crate = dmaxc(0.3 * crate, del / delp);
                     const double dcon = del * dminc(1.0, crate) / tq4;
                     if (dcon <= 1.0) {
-                        acnrm = (mit == 0) ? del : wrms_w(acor, ewt, n);
+                        acnrm = (mit == 0) ? del : sqrt(sb / n);
                         converged = 1;
                         break;
                     }
@@ -269,68 +392,78 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
                 if (dsm <= 1.0) break;
                 nef++;
                 nfail++;
-                COPY_COLS(Z, ZS);
                 if (nef >= 7 || h <= hmin * 1.0000000000000002) {
+                    cols(q, true, false, false);
                     status = -13;
                     goto done;
                 }
-                double eta;
                 if (nef <= 3) {
-                    eta = 1.0 / (cpow_(6.0 * dsm, 1.0 / (q + 1)) + 1e-6);
+                    double eta = 1.0 / (cpow_(6.0 * dsm, 1.0 / (q + 1)) + 1e-6);
                     eta = dmaxc(0.1, dmaxc(eta, hmin / h));
                     if (nef >= 2) eta = dminc(eta, 0.2);
-                    RESCALE(eta);
+                    powers(eta, q, scj);
+                    cols(q, true, true, true);
                     h *= eta;
                 } else {
-                    eta = dmaxc(0.1, hmin / h);
+                    cols(q, true, false, false);
+                    const double eta = dmaxc(0.1, hmin / h);
                     h *= eta;
                     q = 1;
                     s.f(t, Z(0), ft);
                     nfe++;
                     VLOOP Z(1)[i] = h * ft[i];
+                    cols(q, false, false, true);
                 }
                 qwait = q + 1;
                 have_acorp = 0;
                 etamax = 1.0;
-                COPY_COLS(ZS, Z);
                 continue;
             }
             // convergence failure
-            COPY_COLS(Z, ZS);
             nfail++;
             if (!jcur && have_m) {
+                cols(q, true, false, false);
                 force_setup = 1;
                 convfail_bad_j = 1;
                 continue;
             }
             ncf++;
             if (ncf >= 10 || h <= hmin * 1.0000000000000002) {
+                cols(q, true, false, false);
                 status = -14;
                 goto done;
             }
             {
                 const double eta = dmaxc(0.25, hmin / h);
-                RESCALE(eta);
+                powers(eta, q, scj);
+                cols(q, true, true, true);
                 h *= eta;
                 qwait = q + 1;
                 have_acorp = 0;
                 etamax = 1.0;
                 force_setup = 1;
-                COPY_COLS(ZS, Z);
             }
         }
-        // accepted step
+        // accepted step: Nordsieck update, weights, the correction saved for the order test
         nst++;
         {
             const double tnew = t + h;
             t = (tstop && (tnew >= tf || tf - tnew <= 100.0 * uround * (fabs(tnew) + fabs(h)))) ? tf : tnew;
         }
-        for (int j = 0; j <= q; ++j) {
-            double* zj = Z(j);
-            const double lj = l[j];
-            VLOOP zj[i] = fma(lj, acor[i], zj[i]);
-        }
-        SET_EWT(Z(0));
+        const bool save_acorp = (qwait - 1 == 1) && q < QA;
+        with_q(q, [&](auto qc) {
+            constexpr int Q = decltype(qc)::value;
+            double lr[Q + 1];
+#pragma unroll
+            for (int j = 0; j <= Q; ++j) lr[j] = l[j];
+            VLOOP {
+                const double a = acor[i];
+#pragma unroll
+                for (int j = 0; j <= Q; ++j) Z(j)[i] = fma(lr[j], a, Z(j)[i]);
+                ewt[i] = 1.0 / (rtol * fabs(Z(0)[i]) + s.atol(i));
+                if (save_acorp) acorp[i] = a;
+            }
+        });
         s.on_step(t);
         {
             const double etaq = 1.0 / (cpow_(6.0 * dsm, 1.0 / (q + 1)) + 1e-6);
@@ -339,16 +472,30 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
             qwait--;
             if (qwait == 0) {
                 double etaqm1 = 0.0, etaqp1 = 0.0;
-                if (q > 1) {
+                const bool lower = q > 1, upper = q < QA && have_acorp && qsave == q;
+                const double cc = upper ? cpow_(h / hsave, (double)(q + 1)) : 0.0;
+                if (lower || upper) {
+                    const double* zq = Z(q);
+                    slot_pass<NT>(n, red, [&](int i, double& p0, double& p1) {
+                        const double e = ewt[i];
+                        if (lower) {
+                            const double tv = zq[i] * e;
+                            p0 = fma(tv, tv, p0);
+                        }
+                        if (upper) {
+                            const double tv = fma(-cc, acorp[i], acor[i]) * e;
+                            p1 = fma(tv, tv, p1);
+                        }
+                    }, sa, sb);
+                }
+                if (lower) {
                     double fact = 1.0;
                     for (int i = 2; i <= q; ++i) fact *= i;
-                    const double ddn = wrms_w(Z(q), ewt, n) * (fabs(g[q - 1] - g[q - 2]) * fact);
+                    const double ddn = sqrt(sa / n) * (fabs(g[q - 1] - g[q - 2]) * fact);
                     etaqm1 = 1.0 / (cpow_(6.0 * ddn, 1.0 / q) + 1e-6);
                 }
-                if (q < QA && have_acorp && qsave == q) {
-                    const double cc = cpow_(h / hsave, (double)(q + 1));
-                    VLOOP tmp[i] = fma(-cc, acorp[i], acor[i]);
-                    const double dup = wrms_w(tmp, ewt, n) * (fabs(g[q + 1] - g[q]) / g[q - 1]);
+                if (upper) {
+                    const double dup = sqrt(sb / n) * (fabs(g[q + 1] - g[q]) / g[q - 1]);
                     etaqp1 = 1.0 / (cpow_(10.0 * dup, 1.0 / (q + 2)) + 1e-6);
                 }
                 if (etaq >= etaqm1 && etaq >= etaqp1) {
@@ -362,7 +509,6 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
                 }
                 qwait = 2;
             } else if (qwait == 1 && q < QA) {
-                VLOOP acorp[i] = acor[i];
                 hsave = h;
                 qsave = q;
                 have_acorp = 1;
@@ -376,21 +522,39 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
                 eta = dminc(eta, etamax);
                 if (h * eta < hmin) eta = hmin / h;
             }
-            if (qnew > q) {
+            const bool grow = qnew > q;
+            double cnew = 0.0;
+            if (grow) {
                 double fact = 1.0;
                 for (int i = 2; i <= q + 1; ++i) fact *= i;
-                const double c = -1.0 / (g[q - 1] * fact);
-                double* zq1 = Z(q + 1);
-                VLOOP zq1[i] = acor[i] * c;
+                cnew = -1.0 / (g[q - 1] * fact);
             }
+            const int qold = q;
             if (qnew != q) {
                 q = qnew;
                 qwait = q + 1;
                 have_acorp = 0;
             }
-            if (eta != 1.0) {
-                RESCALE(eta);
-                h *= eta;
+            if (grow || eta != 1.0) {
+                powers(eta, q, scj);
+                const bool resc = eta != 1.0;
+                if (grow) {
+                    double* zn = Z(qold + 1);
+                    VLOOP zn[i] = acor[i] * cnew;
+                }
+                if (resc) {
+                    with_q(q, [&](auto qc) {
+                        constexpr int Q = decltype(qc)::value;
+                        double sr[Q + 1];
+#pragma unroll
+                        for (int j = 1; j <= Q; ++j) sr[j] = scj[j];
+                        VLOOP {
+#pragma unroll
+                            for (int j = 1; j <= Q; ++j) Z(j)[i] *= sr[j];
+                        }
+                    });
+                }
+                if (resc) h *= eta;
             }
             etamax = 10.0;
         }
@@ -405,10 +569,9 @@ __device__ int adams_warp(Sys& s, double* wk, double* yio, double rtol, double t
     }
 done:
     if (status != 0) {
-        const double* z0 = Z(0);
-        VLOOP yio[i] = z0[i];
+        VLOOP yio[i] = Z(0)[i];
     }
-    __syncwarp();
+    __syncthreads();
     if (stats) {
         stats[0] = nst;
         stats[1] = nfe;
@@ -417,9 +580,6 @@ done:
     }
     return status;
 #undef VLOOP
-#undef SET_EWT
-#undef COPY_COLS
-#undef RESCALE
 }
 
 // ---- per-flame data -------------------------------------------------------
@@ -452,7 +612,11 @@ struct ConvArgs {
     int* stats;          // n_flames * 4 or null
     double t0, tf, reltol, abstol_u, abstol_t, abstol_y, min_step;
     int max_steps, max_history;
+    // allocated sizes (doubles), for the kernels' own checks of their slices
+    int64_t wk_utw_n, wk_spec_n, hist_n, histv_n, dyn_n;
 };
+
+constexpr int kStatusBadSlice = -30;  // a work slice outside its allocation: nothing was touched
 
 __device__ __forceinline__ double center_volume(const double* x, int alpha) {
     return alpha == 0 ? x[1] : (x[1] * x[1]) / 2.0;
@@ -460,8 +624,9 @@ __device__ __forceinline__ double center_volume(const double* x, int alpha) {
 
 // per-flame scratch inside the UTW slice, after the work vectors
 struct UtwView {
-    double *y3, *hh, *rph, *Wm, *sW, *rho, *rV, *V;
+    double *y3, *hh, *rph, *Wm, *sW, *rho, *rV, *V, *m, *mb;
 };
+constexpr int kUtwScratch = 13;  // doubles per point after the work vectors
 
 __device__ UtwView utw_view(const ConvArgs& a, const ConvFlame& F) {
     const int N = F.f.n_points;
@@ -475,12 +640,22 @@ __device__ UtwView utw_view(const ConvArgs& a, const ConvFlame& F) {
     v.rho = v.sW + N;
     v.rV = v.rho + N;
     v.V = v.rV + N;
+    v.m = v.V + N;
+    v.mb = v.m + N;
     return v;
+}
+
+__device__ __forceinline__ bool utw_slice_ok(const ConvArgs& a, const ConvFlame& F) {
+    const int64_t N = F.f.n_points;
+    return F.utw_wk >= 0 && F.utw_wk + (int64_t(kWorkVectors) * 3 + kUtwScratch) * N <= a.wk_utw_n &&
+           F.hist >= 0 && F.hist + a.max_history <= a.hist_n && F.histv >= 0 &&
+           F.histv + int64_t(a.max_history) * N <= a.histv_n;
 }
 
 __global__ void k_conv_prepare(const __grid_constant__ ConvArgs a) {
     const ConvFlame& F = a.flames[blockIdx.x];
     const int N = F.f.n_points, S = a.S;
+    if (!utw_slice_ok(a, F)) return;
     const double* x = a.x + F.p0;
     const double* st = a.state + F.v0;
     const double* sc = a.split + F.v0;
@@ -518,6 +693,7 @@ struct UtwSys {
     const ember_convection_flame* fl;
     const double *x, *drhodt, *sU, *sT;
     UtwView u;
+    double *sm_m, *sm_mb, *sm_rV;  // shared memory, N each: the increments and rV
     double* ht;
     double* hv;
     int n_history, overflow, max_history;
@@ -527,54 +703,82 @@ struct UtwSys {
         return c == 0 ? a->abstol_u : (c == 1 ? a->abstol_t : 20.0 * a->abstol_y);
     }
 
-    __device__ void f_(double t, const double* y, double* ydot) {
-        const int N = fl->n_points, jj = N - 1, jc = fl->j_cont, lane = lane_of();
+    // ConvectionSystemUTW::f: the per-point increments of the continuity
+    // integral in parallel, the integral itself on thread 0 in point order,
+    // then V and the derivatives in parallel.
+    __device__ void f(double t, const double* y, double* ydot) {
+        const int N = fl->n_points, jj = N - 1, jc = fl->j_cont, tid = threadIdx.x;
         const double beta = fl->beta;
         const double *hh = u.hh, *rph = u.rph, *sW = u.sW;
-        double *rho = u.rho, *rV = u.rV, *V = u.V;
-        __syncwarp();
-        for (int j = lane; j < N; j += 32) rho[j] = (fl->pressure * y[3 * j + 2]) / (kGasConstant * y[3 * j + 1]);
-        __syncwarp();
-        if (lane == 0) {
-#define U_(j) y[3 * (j) + 0]
-#define T_(j) y[3 * (j) + 1]
-#define MFLUX(j) ((hh[j] * rph[j]) * (drhodt[j] + (rho[j] * beta) * U_(j)))
+        double *rho = u.rho, *V = u.V, *m = sm_m, *mb = sm_mb, *rV = sm_rV;
+        const bool backward_own = fl->continuity_bc == EMBER_CONTINUITY_RIGHT ||
+                                  fl->continuity_bc == EMBER_CONTINUITY_QDOT ||
+                                  fl->continuity_bc == EMBER_CONTINUITY_TEMP;
+        __syncthreads();
+        for (int j = tid; j < N; j += kNT) {
+            const double r = (fl->pressure * y[3 * j + 2]) / (kGasConstant * y[3 * j + 1]);
+            rho[j] = r;
+            const double flux = drhodt[j] + (r * beta) * y[3 * j + 0];
+            if (j < N - 1) m[j] = (hh[j] * rph[j]) * flux;
+            if (backward_own && j >= 1) mb[j] = (hh[j - 1] * rph[j]) * flux;
+        }
+        __syncthreads();
+        if (tid == 0) {
             if (fl->continuity_bc == EMBER_CONTINUITY_LEFT) {
-                rV[0] = fl->rv_zero;
-                for (int j = 0; j < N - 1; ++j) rV[j + 1] = rV[j] - MFLUX(j);
+                double r = fl->rv_zero;
+                rV[0] = r;
+#pragma unroll 8
+                for (int j = 0; j < N - 1; ++j) {
+                    r = r - m[j];
+                    rV[j + 1] = r;
+                }
             } else if (fl->continuity_bc == EMBER_CONTINUITY_ZERO) {
                 int j = jc;
-                double dVdx0 = -rph[j] * (drhodt[j] - (rho[j] * beta) * U_(j));
+                double dVdx0 = -rph[j] * (drhodt[j] - (rho[j] * beta) * y[3 * j + 0]);
                 if (jc != 0)
-                    dVdx0 = 0.5 * dVdx0 - (0.5 * rph[j - 1]) * (drhodt[j - 1] + (rho[j - 1] * beta) * U_(j - 1));
-                rV[j] = (x[j] - fl->x_vzero) * dVdx0;
-                for (j = jc; j < jj; ++j) rV[j + 1] = rV[j] - MFLUX(j);
+                    dVdx0 = 0.5 * dVdx0 -
+                            (0.5 * rph[j - 1]) * (drhodt[j - 1] + (rho[j - 1] * beta) * y[3 * (j - 1) + 0]);
+                double r = (x[j] - fl->x_vzero) * dVdx0;
+                rV[j] = r;
+                for (j = jc; j < jj; ++j) {
+                    r = r - m[j];
+                    rV[j + 1] = r;
+                }
                 if (jc != 0) {
                     j = jc - 1;
-                    rV[j] = (x[j] - fl->x_vzero) * dVdx0;
-                    for (j = jc - 1; j > 0; --j) rV[j - 1] = rV[j] + MFLUX(j - 1);
+                    r = (x[j] - fl->x_vzero) * dVdx0;
+                    rV[j] = r;
+                    for (j = jc - 1; j > 0; --j) {
+                        r = r + m[j - 1];
+                        rV[j - 1] = r;
+                    }
                 }
             } else {
+                double r;
                 if (fl->continuity_bc == EMBER_CONTINUITY_TEMP) {
                     const int j = jc;
-                    if (j == 0 || sT[j] / (T_(j + 1) - T_(j)) < 0)
-                        rV[j] = (((rph[j] * rho[j]) * sT[j]) * hh[j]) / (T_(j + 1) - T_(j));
+                    const double Tj = y[3 * j + 1], Tn = y[3 * (j + 1) + 1];
+                    if (j == 0 || sT[j] / (Tn - Tj) < 0)
+                        r = (((rph[j] * rho[j]) * sT[j]) * hh[j]) / (Tn - Tj);
                     else
-                        rV[j] = (((rph[j - 1] * rho[j]) * sT[j]) * hh[j - 1]) / (T_(j) - T_(j - 1));
+                        r = (((rph[j - 1] * rho[j]) * sT[j]) * hh[j - 1]) / (Tj - y[3 * (j - 1) + 1]);
                 } else {
-                    rV[jc] = fl->rv_cont;
+                    r = fl->rv_cont;
                 }
-                for (int j = jc; j < N - 1; ++j) rV[j + 1] = rV[j] - MFLUX(j);
-                for (int j = jc; j > 0; --j)
-                    rV[j - 1] = rV[j] + (hh[j - 1] * rph[j]) * (drhodt[j] + (rho[j] * beta) * U_(j));
+                rV[jc] = r;
+                const double r0 = r;
+                for (int j = jc; j < N - 1; ++j) {
+                    r = r - m[j];
+                    rV[j + 1] = r;
+                }
+                r = r0;
+                for (int j = jc; j > 0; --j) {
+                    r = r + mb[j];
+                    rV[j - 1] = r;
+                }
             }
-#undef MFLUX
-#undef T_
-#undef U_
         }
-        __syncwarp();
-        for (int j = lane; j < N; j += 32) V[j] = (j == 0 || fl->alpha == 0) ? rV[j] : rV[j] / x[j];
-        __syncwarp();
+        __syncthreads();
         double aa, dadt;
         {
             const double a0 = fl->strain_initial, a1 = fl->strain_final, T0 = fl->strain_t0, Dt = fl->strain_dt;
@@ -583,17 +787,21 @@ struct UtwSys {
         }
         const double K = dadt / beta + (aa * aa) / (beta * beta);
         const bool cv = fl->left_bc == EMBER_BC_CONTROL_VOLUME || fl->left_bc == EMBER_BC_WALL_FLUX;
-        const bool right_fixed = rV[jj] < 0 || fl->right_bc == EMBER_BC_FIXED_VALUE;
-        for (int j = lane; j < N; j += 32) {
+        const double rVjj = rV[jj];
+        const bool right_fixed = rVjj < 0 || fl->right_bc == EMBER_BC_FIXED_VALUE;
+        for (int j = tid; j < N; j += kNT) {
+            const double Vj = (j == 0 || fl->alpha == 0) ? rV[j] : rV[j] / x[j];
+            V[j] = Vj;
             const double Uj = y[3 * j + 0], Tj = y[3 * j + 1], Wj = y[3 * j + 2];
-            const double strain_term = (fl->rhou / rho[j]) * K;
+            const double rj = rho[j];
+            const double strain_term = (fl->rhou / rj) * K;
             if (j == 0) {
                 ydot[0] = (sU[0] - Uj * Uj) + strain_term;
                 if (cv) {
                     const double cvol = center_volume(x, fl->alpha);
                     const double rvm = dmaxc(rV[0], 0.0);
-                    ydot[1] = (-rvm * (Tj - fl->t_left)) / (rho[0] * cvol) + sT[0];
-                    ydot[2] = (-rvm * (Wj - fl->w_left)) / (rho[0] * cvol) - (Wj * Wj) * sW[0];
+                    ydot[1] = (-rvm * (Tj - fl->t_left)) / (rj * cvol) + sT[0];
+                    ydot[2] = (-rvm * (Wj - fl->w_left)) / (rj * cvol) - (Wj * Wj) * sW[0];
                 } else {
                     ydot[1] = sT[0];
                     ydot[2] = -((Wj * Wj) * sW[0]);
@@ -609,9 +817,9 @@ struct UtwSys {
                     dU = (Uj - y[3 * (j - 1) + 0]) / hh[j - 1];
                     dW = (Wj - y[3 * (j - 1) + 2]) / hh[j - 1];
                 }
-                ydot[3 * j + 0] = (((-V[j] * dU) / rho[j] - Uj * Uj) + strain_term) + sU[j];
-                ydot[3 * j + 1] = (-V[j] * dT) / rho[j] + sT[j];
-                ydot[3 * j + 2] = (-V[j] * dW) / rho[j] - (Wj * Wj) * sW[j];
+                ydot[3 * j + 0] = (((-Vj * dU) / rj - Uj * Uj) + strain_term) + sU[j];
+                ydot[3 * j + 1] = (-Vj * dT) / rj + sT[j];
+                ydot[3 * j + 2] = (-Vj * dW) / rj - (Wj * Wj) * sW[j];
             } else if (right_fixed) {
                 ydot[3 * jj + 0] = (sU[jj] - Uj * Uj) + strain_term;
                 ydot[3 * jj + 1] = sT[jj];
@@ -619,34 +827,43 @@ struct UtwSys {
             } else {
                 const double hl = hh[jj - 1];
                 ydot[3 * jj + 0] =
-                    ((sU[jj] - ((V[jj] * (Uj - y[3 * (jj - 1) + 0])) / hl) / rho[jj]) - Uj * Uj) + strain_term;
-                ydot[3 * jj + 1] = sT[jj] - ((V[jj] * (Tj - y[3 * (jj - 1) + 1])) / hl) / rho[jj];
-                ydot[3 * jj + 2] = -((Wj * Wj) * sW[jj]) - ((V[jj] * (Wj - y[3 * (jj - 1) + 2])) / hl) / rho[jj];
+                    ((sU[jj] - ((Vj * (Uj - y[3 * (jj - 1) + 0])) / hl) / rj) - Uj * Uj) + strain_term;
+                ydot[3 * jj + 1] = sT[jj] - ((Vj * (Tj - y[3 * (jj - 1) + 1])) / hl) / rj;
+                ydot[3 * jj + 2] = -((Wj * Wj) * sW[jj]) - ((Vj * (Wj - y[3 * (jj - 1) + 2])) / hl) / rj;
             }
         }
-        __syncwarp();
+        __syncthreads();
     }
-    __device__ void f(double t, const double* y, double* ydot) { f_(t, y, ydot); }
 
+    // V / rho of the last right-hand side, recorded with the time
     __device__ void record(double t) {
         if (n_history >= max_history) {
             overflow = 1;
             return;
         }
         const int N = fl->n_points;
-        if (lane_of() == 0) ht[n_history] = t;
+        if (threadIdx.x == 0) ht[n_history] = t;
         double* v = hv + size_t(n_history) * N;
-        for (int j = lane_of(); j < N; j += 32) v[j] = u.V[j] / u.rho[j];
-        __syncwarp();
+        for (int j = threadIdx.x; j < N; j += kNT) v[j] = u.V[j] / u.rho[j];
         n_history++;
     }
     __device__ void on_step(double t) { record(t); }
 };
 
-__global__ void __launch_bounds__(32) k_conv_utw(const __grid_constant__ ConvArgs a) {
+__global__ void __launch_bounds__(kNT, 2) k_conv_utw(const __grid_constant__ ConvArgs a) {
+    __shared__ double red[kRed];
+    __shared__ AdamsShared sh;
+    extern __shared__ double dyn[];  // 3 * max n_points
     const int fi = blockIdx.x;
     const ConvFlame& F = a.flames[fi];
     const int N = F.f.n_points;
+    if (!utw_slice_ok(a, F) || 3 * int64_t(N) > a.dyn_n) {
+        if (threadIdx.x == 0) {
+            a.status[size_t(fi) * (1 + a.S)] = kStatusBadSlice;
+            a.n_hist[fi] = 0;
+        }
+        return;
+    }
     UtwSys s;
     s.n = 3 * N;
     s.a = &a;
@@ -656,6 +873,9 @@ __global__ void __launch_bounds__(32) k_conv_utw(const __grid_constant__ ConvArg
     s.sU = a.split + F.v0;
     s.sT = a.split + F.v0 + N;
     s.u = utw_view(a, F);
+    s.sm_m = dyn;
+    s.sm_mb = dyn + N;
+    s.sm_rV = dyn + 2 * N;
     s.ht = a.hist_t + F.hist;
     s.hv = a.hist_v + F.histv;
     s.n_history = 0;
@@ -666,14 +886,14 @@ __global__ void __launch_bounds__(32) k_conv_utw(const __grid_constant__ ConvArg
     s.f(a.t0, s.u.y3, wk);
     s.record(a.t0);
     int st[4];
-    int rc = adams_warp(s, wk, s.u.y3, a.reltol, a.t0, a.tf, 1, a.min_step, a.max_steps, st);
+    int rc = adams_block<kNT>(s, wk, s.u.y3, a.reltol, a.t0, a.tf, 1, a.min_step, a.max_steps, st, red, sh);
     if (s.overflow) rc = -20;
     double* state = a.state + F.v0;
-    for (int j = lane_of(); j < N; j += 32) {
+    for (int j = threadIdx.x; j < N; j += kNT) {
         state[j] = s.u.y3[3 * j + 0];
         state[size_t(N) + j] = s.u.y3[3 * j + 1];
     }
-    if (lane_of() == 0) {
+    if (threadIdx.x == 0) {
         a.status[size_t(fi) * (1 + a.S)] = rc;
         a.n_hist[fi] = s.n_history;
         if (a.stats) {
@@ -683,6 +903,7 @@ __global__ void __launch_bounds__(32) k_conv_utw(const __grid_constant__ ConvArg
     }
 }
 
+template <int NT>
 struct SpecSys {
     int n;
     const ConvArgs* a;
@@ -690,14 +911,15 @@ struct SpecSys {
     const double *x, *hh, *split;
     double y_left;
     int H;
-    const double *ht, *hv;
+    const double *ht, *hv;  // ht: the record's times, in shared memory when they fit
 
     __device__ double atol(int) const { return a->abstol_y; }
 
-    __device__ void f_(double t, const double* y, double* ydot) {
-        const int N = n, jj = N - 1, lane = lane_of();
-        __syncwarp();
-        // ConvectionSystemY::update_v: [lower_bound(t), next], moved back at the end
+    // ConvectionSystemY::f with v(t) from ConvectionSystemY::update_v: the
+    // interval [lower_bound(t), next], moved back by one at the end of the record
+    __device__ void f(double t, const double* y, double* ydot) {
+        const int N = n, jj = N - 1;
+        __syncthreads();
         int iL = -1;
         double s = 0.0;
         if (H > 1) {
@@ -716,10 +938,9 @@ struct SpecSys {
         }
         const double* vL = hv + size_t(iL < 0 ? 0 : iL) * N;
         const double* vR = iL < 0 ? vL : vL + N;
-        auto VV = [&](int j) { return iL < 0 ? vL[j] : vL[j] * (1 - s) + vR[j] * s; };
         const bool cv = fl->left_bc == EMBER_BC_CONTROL_VOLUME || fl->left_bc == EMBER_BC_WALL_FLUX;
-        for (int j = lane; j < N; j += 32) {
-            const double v = VV(j);
+        for (int j = threadIdx.x; j < N; j += NT) {
+            const double v = iL < 0 ? vL[j] : vL[j] * (1 - s) + vR[j] * s;
             if (j == 0) {
                 if (cv) {
                     const double cvol = center_volume(x, fl->alpha);
@@ -737,13 +958,18 @@ struct SpecSys {
                 ydot[jj] = split[jj] - (v * (y[jj] - y[jj - 1])) / hh[jj - 1];
             }
         }
-        __syncwarp();
+        __syncthreads();
     }
-    __device__ void f(double t, const double* y, double* ydot) { f_(t, y, ydot); }
     __device__ void on_step(double) {}
 };
 
-__global__ void __launch_bounds__(32) k_conv_species(const __grid_constant__ ConvArgs a) {
+constexpr int kHistShared = 512;
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 12) k_conv_species(const __grid_constant__ ConvArgs a) {
+    __shared__ double red[kRed];
+    __shared__ AdamsShared sh;
+    __shared__ double ht_s[kHistShared];
     const int sys = blockIdx.x;
     const int fi = sys / a.S, k = sys % a.S;
     const ConvFlame& F = a.flames[fi];
@@ -751,10 +977,16 @@ __global__ void __launch_bounds__(32) k_conv_species(const __grid_constant__ Con
     int* status = a.status + size_t(fi) * (1 + a.S);
     const int utw_rc = status[0];
     if (utw_rc != 0) {
-        if (lane_of() == 0) status[1 + k] = utw_rc;
+        if (threadIdx.x == 0) status[1 + k] = utw_rc;
         return;
     }
-    SpecSys s;
+    const int H = a.n_hist[fi];
+    if (a.spec_off[sys] < 0 || a.spec_off[sys] + int64_t(kWorkVectors) * N > a.wk_spec_n || H < 1 ||
+        H > a.max_history) {
+        if (threadIdx.x == 0) status[1 + k] = kStatusBadSlice;
+        return;
+    }
+    SpecSys<NT> s;
     s.n = N;
     s.a = &a;
     s.fl = &F.f;
@@ -762,14 +994,19 @@ __global__ void __launch_bounds__(32) k_conv_species(const __grid_constant__ Con
     s.hh = utw_view(a, F).hh;
     s.split = a.split + F.v0 + size_t(2 + k) * N;
     s.y_left = a.y_left[size_t(fi) * a.S + k];
-    s.H = a.n_hist[fi];
+    s.H = H;
     s.ht = a.hist_t + F.hist;
+    if (s.H <= kHistShared) {
+        for (int i = threadIdx.x; i < s.H; i += NT) ht_s[i] = s.ht[i];
+        __syncthreads();
+        s.ht = ht_s;
+    }
     s.hv = a.hist_v + F.histv;
     int st[4];
     double* y = a.state + F.v0 + size_t(2 + k) * N;
-    const int rc = adams_warp(s, a.wk_spec + a.spec_off[sys], y, a.reltol, a.t0, a.tf, 0, a.min_step,
-                              a.max_steps, st);
-    if (lane_of() == 0) {
+    const int rc = adams_block<NT>(s, a.wk_spec + a.spec_off[sys], y, a.reltol, a.t0, a.tf, 0, a.min_step,
+                               a.max_steps, st, red, sh);
+    if (threadIdx.x == 0) {
         status[1 + k] = rc;
         if (a.stats) {
             atomicAdd(&a.stats[4 * fi + 2], st[0]);
@@ -799,14 +1036,19 @@ extern "C" int ember_convection_integrate(int n_flames, const ember_convection_f
                     "tolerances must be positive");
     EMBER_CHECK_ARG(opts->max_steps > 0 && opts->max_history >= 2, "max_steps > 0 and max_history >= 2 required");
     EMBER_CHECK_ARG(opts->min_step >= 0, "min_step must be >= 0");
+    EMBER_CHECK_ARG(opts->species_threads == 0 || opts->species_threads == kNTSpecies,
+                    "species_threads must be 0 or 32");
     const int S = n_species, nv = S + 2;
     std::vector<ConvFlame> hf(n_flames);
     std::vector<int64_t> spec_off(size_t(n_flames) * S);
     int64_t P = 0, V = 0, WU = 0, WS = 0, HS = 0, HV = 0;
+    int max_points = 0;
     for (int f = 0; f < n_flames; ++f) {
         const ember_convection_flame& g = flames[f];
         const int N = g.n_points;
-        EMBER_CHECK_ARG(N >= 3, "flame %d: n_points must be >= 3", f);
+        EMBER_CHECK_ARG(N >= 3 && N <= EMBER_CONVECTION_MAX_POINTS, "flame %d: n_points must be in [3, %d]", f,
+                        EMBER_CONVECTION_MAX_POINTS);
+        max_points = N > max_points ? N : max_points;
         EMBER_CHECK_ARG(g.alpha == 0 || g.alpha == 1, "flame %d: alpha must be 0 or 1", f);
         EMBER_CHECK_ARG(g.left_bc >= EMBER_BC_FIXED_VALUE && g.left_bc <= EMBER_BC_WALL_FLUX,
                         "flame %d: bad left boundary condition %d", f, g.left_bc);
@@ -830,7 +1072,7 @@ extern "C" int ember_convection_integrate(int n_flames, const ember_convection_f
         }
         P += N;
         V += int64_t(nv) * N;
-        WU += int64_t(kWorkVectors) * 3 * N + 3 * int64_t(N) + 8 * int64_t(N);
+        WU += int64_t(kWorkVectors) * 3 * N + int64_t(kUtwScratch) * N;
         HS += int64_t(opts->max_history);
         HV += int64_t(opts->max_history) * N;
     }
@@ -895,11 +1137,18 @@ extern "C" int ember_convection_integrate(int n_flames, const ember_convection_f
     a.min_step = opts->min_step;
     a.max_steps = opts->max_steps;
     a.max_history = opts->max_history;
+    a.wk_utw_n = WU;
+    a.wk_spec_n = WS;
+    a.hist_n = HS;
+    a.histv_n = HV;
+    a.dyn_n = 3 * int64_t(max_points);
     k_conv_prepare<<<n_flames, 128, 0, st>>>(a);
     EMBER_CUDA_TRY(cudaGetLastError());
-    k_conv_utw<<<n_flames, 32, 0, st>>>(a);
+    const size_t utw_smem = size_t(3) * max_points * sizeof(double);
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_conv_utw, cudaFuncAttributeMaxDynamicSharedMemorySize, int(utw_smem)));
+    k_conv_utw<<<n_flames, kNT, utw_smem, st>>>(a);
     EMBER_CUDA_TRY(cudaGetLastError());
-    k_conv_species<<<n_flames * S, 32, 0, st>>>(a);
+    k_conv_species<kNTSpecies><<<n_flames * S, kNTSpecies, 0, st>>>(a);
     EMBER_CUDA_TRY(cudaGetLastError());
     EMBER_TRY(stage_out(state, dstate, size_t(V), mem, st));
     if (status) {

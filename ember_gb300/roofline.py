@@ -124,3 +124,17 @@ def transport_point_flops(n_species: int, n_major=None, cross_terms: bool = True
 def tridiag_bytes_per_point() -> float:
     """B, D, split constant and y read, y written (8 bytes each)."""
     return 40.0
+
+
+def convection_flame_flops(n_points, stats):
+    """Flops of one convection stage per flame from its counters (stats rows:
+    UTW steps, UTW right-hand sides, species steps and right-hand sides
+    summed over species). A UTW right-hand side costs about 30 flops per point
+    (density, continuity increment, V, three upwinded differences and the
+    three derivatives with the strain term), a species one about 8 (the
+    interpolated v, one upwinded difference, the derivative); an Adams step
+    about 35 per value (prediction, on average 1.5 Newton corrections with
+    their norms, the Nordsieck update, weights, the error and order tests)."""
+    N = np.asarray(n_points, dtype=float)
+    st = np.asarray(stats, dtype=float).reshape(-1, 4)
+    return st[:, 1] * 30.0 * N + st[:, 0] * 35.0 * 3.0 * N + st[:, 3] * 8.0 * N + st[:, 2] * 35.0 * N

@@ -252,8 +252,11 @@ int ember_diffusion_integrate_noalloc(int n_flames, const ember_diffusion_grid* 
 #define EMBER_CONTINUITY_QDOT  3   /* fixedQdot: rV[j_cont] = rv_cont                 */
 #define EMBER_CONTINUITY_TEMP  4   /* fixedTemperature: dT/dt = 0 at j_cont           */
 
+/* Largest flame: the continuity integral of a flame is staged in shared memory. */
+#define EMBER_CONVECTION_MAX_POINTS 8192
+
 typedef struct {
-    int n_points;          /* N_f >= 3                                                */
+    int n_points;          /* 3 <= N_f <= EMBER_CONVECTION_MAX_POINTS                 */
     int left_bc;           /* EMBER_BC_FIXED_VALUE / ZERO_GRADIENT / CONTROL_VOLUME / WALL_FLUX */
     int right_bc;          /* EMBER_BC_FIXED_VALUE, else outflow when V > 0 there     */
     int alpha;             /* 0 planar, 1 cylindrical                                 */
@@ -282,6 +285,7 @@ typedef struct {
     double min_step;         /* minStep (1e-16)                                       */
     int max_steps;           /* per system                                            */
     int max_history;         /* recorded V / rho per flame: UTW steps + 1             */
+    int species_threads;     /* CTA width of a species system: 0 or 32 (one warp)     */
 } ember_convection_options;
 
 /* status: n_flames * (1 + S) ints, may be NULL: per flame the UTW status

@@ -22,8 +22,9 @@
  * variable-order (1..12) Nordsieck restatement of the published method (the
  * step and order control of the BDF integrator in oracle_bdf.c with the
  * Adams-Moulton coefficients), not SUNDIALS source: parity with CVODE itself
- * is unpinned; accuracy is checked against scipy. Norms are summed in the GPU
- * warp's 32-lane order so that the GPU reproduces every bit.
+ * is unpinned; accuracy is checked against scipy. Norms are summed in the
+ * order of the GPU CTA that integrates the system (256 slots for UTW, 32 for
+ * a species) so that the GPU reproduces every bit.
  */
 #include <math.h>
 #include <stdlib.h>
@@ -84,13 +85,16 @@ struct adams_sys {
     void (*f)(adams_sys*, double t, const double* y, double* ydot);
     void (*on_step)(adams_sys*, double t); /* after every accepted step, or NULL */
     int n;
+    int W; /* slots of the norms' partial sums: the GPU CTA width (UTW 256, species 32) */
 };
 
-/* Weighted RMS norm in the 32-lane order of the GPU warp. */
-static double wrms_c(const double* v, const double* ewt, int n, double* tmp) {
+/* Weighted RMS norm in the GPU's order: term i in slot i mod W (each slot in
+ * increasing i), the slots folded into 32 in slot order, an xor butterfly. */
+static double wrms_w(const double* v, const double* ewt, int n, double* tmp, int W) {
     for (int i = 0; i < n; ++i) tmp[i] = v[i] * ewt[i];
-    return sqrt(oracle_block_sum(tmp, tmp, n, 32) / n);
+    return sqrt(oracle_block_sum(tmp, tmp, n, W) / n);
 }
+#define wrms_c(v, ewt, n, tmp) wrms_w(v, ewt, n, tmp, s->W)
 
 /* Integrate y' = f(t, y) from t0 to tf. tstop != 0: never step past tf (the
  * last step ends on tf; one-step mode with a stop time); else step past tf
@@ -661,7 +665,7 @@ int oracle_convection_flame(const oracle_conv_flame* fl, int S, const double* W,
         at3[3 * j + 2] = 20.0 * o->abstol_y;
         atN[j] = o->abstol_y;
     }
-    utw_ctx uc = {{utw_f, utw_on_step, 3 * N}, fl, N, x, hh, rph, drhodt, split, split + N, sW,
+    utw_ctx uc = {{utw_f, utw_on_step, 3 * N, 256}, fl, N, x, hh, rph, drhodt, split, split + N, sW,
                   rho, rV, V, o->max_history, 0, 0, ht, hv};
     /* the record starts with V / rho of the initial state */
     oracle_convection_utw_rhs(fl, x, hh, rph, t0, y3, drhodt, split, split + N, sW, yd3, rho, rV, V);
@@ -688,7 +692,7 @@ int oracle_convection_flame(const oracle_conv_flame* fl, int S, const double* W,
             status[1 + k] = rc;
             continue;
         }
-        spec_ctx sc = {{spec_f, NULL, N}, fl, N, x, hh, split + (size_t)(2 + k) * N, y_left[k], uc.n_history, ht, hv};
+        spec_ctx sc = {{spec_f, NULL, N, 32}, fl, N, x, hh, split + (size_t)(2 + k) * N, y_left[k], uc.n_history, ht, hv};
         int sst[4] = {0, 0, 0, 0};
         status[1 + k] =
             adams_integrate(&sc.base, state + (size_t)(2 + k) * N, atN, o->reltol, t0, tf, 0, o->min_step,

@@ -346,6 +346,10 @@ def test_gpu_convection_device_memory_and_overflow(gpu_lib, mech):
                                            1e-3, 1e-3 + 5e-6, opts)
     assert np.array_equal(dev.cpu().numpy(), host)
     assert np.array_equal(s2.cpu().numpy(), s1) and np.array_equal(t2.cpu().numpy(), t1)
+    st = b.state.copy()
+    integrate_convection_terms(b.flames, mech.mol_weight, b.x, b.y_left, b.drhodt, b.split_const, st, 1e-3,
+                               1e-3 + 5e-6, ConvectionOptions(species_threads=32))
+    assert np.array_equal(st, host)
     # a record too short for the UTW steps: every system of the flame reports it, nothing faults
     small = ConvectionOptions(max_history=3)
     st = b.state.copy()
