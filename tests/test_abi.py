@@ -55,6 +55,9 @@ def test_bad_arguments_are_rejected_without_device():
     assert lib.ember_mech_get_tuning(None, None, None, None, None, None, None) == _lib.EINVAL
     assert lib.ember_source_autotune(None, 0, 1, None, None, None, 0.0, None, None, None, None, 0, None) \
         == _lib.EINVAL
+    assert lib.ember_convection_integrate(1, None, 10, None, None, None, None, None, None, None, None, None, 0,
+                                          None) == _lib.EINVAL
+    assert "null" in _lib.last_error()
 
 
 def test_no_device_is_reported_not_crashed():
