@@ -140,9 +140,11 @@ __device__ void adams_l(int q, double* l) {
 }
 
 // Block-uniform coefficients, in shared memory: the Adams constants g, the
-// corrector's l and the column factors scj of the last rescaling.
+// corrector's l for every order (row q) with its error constant, and the
+// column factors scj of the last rescaling.
 struct AdamsShared {
-    double g[QA + 2], l[QA + 2], scj[QA + 2];
+    double g[QA + 2], scj[QA + 2];
+    double ltab[QA + 1][QA + 2], cqtab[QA + 1];
 };
 
 // scj[j] = eta^j as the running product eta, eta*eta, ... (scj[0] = 1);
@@ -201,11 +203,15 @@ __device__ int adams_block(Sys& s, double* wk, double* yio, double rtol, double 
     if (tid == 0) {
         const AdamsConst C;
         for (int j = 0; j <= QA + 1; ++j) sh.g[j] = C.g[j];
+        for (int q = 1; q <= QA; ++q) {
+            adams_l(q, sh.ltab[q]);
+            sh.cqtab[q] = fabs(C.g[q] - C.g[q - 1]) / C.g[q - 1];
+        }
     }
     __syncthreads();
     const double* g = sh.g;
     double* scj = sh.scj;
-    double* l = sh.l;
+    const double* l = sh.ltab[1];
     int nst = 0, nfe = 0, nje = 0, nfail = 0, status = 0;
 #define VLOOP for (int i = tid; i < n; i += NT)
     // restore from the saved columns (restore != 0), rescale column j by
@@ -298,10 +304,8 @@ __device__ int adams_block(Sys& s, double* wk, double* yio, double rtol, double 
                 }
             });
             const double tn = t + h;
-            __syncthreads();  // every thread is done with the previous l
-            if (tid == 0) adams_l(q, l);
-            __syncthreads();
-            const double cq = fabs(g[q] - g[q - 1]) / g[q - 1];
+            l = sh.ltab[q];
+            const double cq = sh.cqtab[q];
             const double gamma = h / l[1];
             const double tq4 = 0.1 / cq;
             int jcur = 0;
