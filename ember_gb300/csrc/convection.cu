@@ -30,6 +30,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "convection.cuh"
 #include "emath.cuh"
 
 namespace ember {
@@ -586,41 +587,18 @@ done:
 #undef VLOOP
 }
 
-// ---- per-flame data -------------------------------------------------------
+constexpr int kStatusBadSlice = -30;
 
-struct ConvFlame {
-    ember_convection_flame f;
-    int64_t p0;      // first point of the flame in the concatenated point arrays
-    int64_t v0;      // first value of the flame in the variable-major state arrays
-    int64_t utw_wk;  // UTW work slice (kWorkVectors * 3N doubles + 3N y + 6N scratch)
-    int64_t hist;    // first recorded time of the flame (max_history per flame)
-    int64_t histv;   // first recorded value of the flame (max_history * N per flame)
-};
-
-struct ConvArgs {
-    int n_flames, S;
-    const ConvFlame* flames;
-    const double* W;
-    const double* x;
-    const double* y_left;
-    const double* drhodt;
-    const double* split;
-    double* state;
-    double* wk_utw;
-    double* wk_spec;     // kWorkVectors * N per (flame, species) system, at spec_off
-    const int64_t* spec_off;
-    double* hist_t;
-    double* hist_v;
-    int* n_hist;
-    int* status;         // n_flames * (1 + S)
-    int* stats;          // n_flames * 4 or null
-    double t0, tf, reltol, abstol_u, abstol_t, abstol_y, min_step;
-    int max_steps, max_history;
-    // allocated sizes (doubles), for the kernels' own checks of their slices
-    int64_t wk_utw_n, wk_spec_n, hist_n, histv_n, dyn_n;
-};
-
-constexpr int kStatusBadSlice = -30;  // a work slice outside its allocation: nothing was touched
+__device__ __forceinline__ void stage_times(const ConvArgs& a, double& t0, double& tf) {
+    if (a.t_dev) {
+        const double t = *a.t_dev;
+        t0 = (a.f0 == 0.0) ? t : t + a.f0 * a.dt;
+        tf = t + a.f1 * a.dt;
+    } else {
+        t0 = a.t0;
+        tf = a.tf;
+    }
+}  // a work slice outside its allocation: nothing was touched
 
 __device__ __forceinline__ double center_volume(const double* x, int alpha) {
     return alpha == 0 ? x[1] : (x[1] * x[1]) / 2.0;
@@ -886,11 +864,13 @@ __global__ void __launch_bounds__(kNT, 2) k_conv_utw(const __grid_constant__ Con
     s.overflow = 0;
     s.max_history = a.max_history;
     double* wk = a.wk_utw + F.utw_wk;
+    double t0, tf;
+    stage_times(a, t0, tf);
     // the record starts with V / rho of the initial state
-    s.f(a.t0, s.u.y3, wk);
-    s.record(a.t0);
+    s.f(t0, s.u.y3, wk);
+    s.record(t0);
     int st[4];
-    int rc = adams_block<kNT>(s, wk, s.u.y3, a.reltol, a.t0, a.tf, 1, a.min_step, a.max_steps, st, red, sh);
+    int rc = adams_block<kNT>(s, wk, s.u.y3, a.reltol, t0, tf, 1, a.min_step, a.max_steps, st, red, sh);
     if (s.overflow) rc = -20;
     double* state = a.state + F.v0;
     for (int j = threadIdx.x; j < N; j += kNT) {
@@ -1008,8 +988,10 @@ __global__ void __launch_bounds__(NT, 12) k_conv_species(const __grid_constant__
     s.hv = a.hist_v + F.histv;
     int st[4];
     double* y = a.state + F.v0 + size_t(2 + k) * N;
-    const int rc = adams_block<NT>(s, a.wk_spec + a.spec_off[sys], y, a.reltol, a.t0, a.tf, 0, a.min_step,
-                               a.max_steps, st, red, sh);
+    double t0, tf;
+    stage_times(a, t0, tf);
+    const int rc = adams_block<NT>(s, a.wk_spec + a.spec_off[sys], y, a.reltol, t0, tf, 0, a.min_step,
+                                   a.max_steps, st, red, sh);
     if (threadIdx.x == 0) {
         status[1 + k] = rc;
         if (a.stats) {
@@ -1024,6 +1006,136 @@ __global__ void __launch_bounds__(NT, 12) k_conv_species(const __grid_constant__
 
 using namespace ember;
 
+namespace ember {
+
+int conv_plan_layout(ConvPlan& p, int n_flames, const ember_convection_flame* flames, int S,
+                     const ember_convection_options* opts) {
+    EMBER_CHECK_ARG(opts->reltol > 0 && opts->abstol_u > 0 && opts->abstol_t > 0 && opts->abstol_y > 0,
+                    "tolerances must be positive");
+    EMBER_CHECK_ARG(opts->max_steps > 0 && opts->max_history >= 2, "max_steps > 0 and max_history >= 2 required");
+    EMBER_CHECK_ARG(opts->min_step >= 0, "min_step must be >= 0");
+    EMBER_CHECK_ARG(opts->species_threads == 0 || opts->species_threads == kNTSpecies,
+                    "species_threads must be 0 or 32");
+    const int nv = S + 2;
+    p = ConvPlan{};
+    p.n_flames = n_flames;
+    p.S = S;
+    p.hf.resize(n_flames);
+    p.spec_off.resize(size_t(n_flames) * S);
+    for (int f = 0; f < n_flames; ++f) {
+        const ember_convection_flame& g = flames[f];
+        const int N = g.n_points;
+        EMBER_CHECK_ARG(N >= 3 && N <= EMBER_CONVECTION_MAX_POINTS, "flame %d: n_points must be in [3, %d]", f,
+                        EMBER_CONVECTION_MAX_POINTS);
+        p.max_points = N > p.max_points ? N : p.max_points;
+        EMBER_CHECK_ARG(g.alpha == 0 || g.alpha == 1, "flame %d: alpha must be 0 or 1", f);
+        EMBER_CHECK_ARG(g.left_bc >= EMBER_BC_FIXED_VALUE && g.left_bc <= EMBER_BC_WALL_FLUX,
+                        "flame %d: bad left boundary condition %d", f, g.left_bc);
+        EMBER_CHECK_ARG(g.continuity_bc >= EMBER_CONTINUITY_LEFT && g.continuity_bc <= EMBER_CONTINUITY_TEMP,
+                        "flame %d: bad continuity boundary condition %d", f, g.continuity_bc);
+        EMBER_CHECK_ARG(g.continuity_bc == EMBER_CONTINUITY_LEFT || (g.j_cont >= 0 && g.j_cont < N),
+                        "flame %d: j_cont out of range", f);
+        EMBER_CHECK_ARG(g.continuity_bc != EMBER_CONTINUITY_TEMP || g.j_cont < N - 1,
+                        "flame %d: the temperature continuity point needs a right neighbour", f);
+        EMBER_CHECK_ARG(g.beta > 0 && g.pressure > 0, "flame %d: beta and pressure must be positive", f);
+        EMBER_CHECK_ARG(g.strain_dt >= 0, "flame %d: strain_dt must be >= 0", f);
+        ConvFlame& c = p.hf[f];
+        c.f = g;
+        c.p0 = p.P;
+        c.v0 = p.V;
+        c.utw_wk = p.WU;
+        c.hist = p.HS;
+        c.histv = p.HV;
+        for (int k = 0; k < S; ++k) {
+            p.spec_off[size_t(f) * S + k] = p.WS;
+            p.WS += int64_t(kWorkVectors) * N;
+        }
+        p.P += N;
+        p.V += int64_t(nv) * N;
+        p.WU += int64_t(kWorkVectors) * 3 * N + int64_t(kUtwScratch) * N;
+        p.HS += int64_t(opts->max_history);
+        p.HV += int64_t(opts->max_history) * N;
+    }
+    ConvArgs& a = p.a;
+    a.n_flames = n_flames;
+    a.S = S;
+    a.t0 = opts->t_start;
+    a.tf = opts->t_end;
+    a.reltol = opts->reltol;
+    a.abstol_u = opts->abstol_u;
+    a.abstol_t = opts->abstol_t;
+    a.abstol_y = opts->abstol_y;
+    a.min_step = opts->min_step;
+    a.max_steps = opts->max_steps;
+    a.max_history = opts->max_history;
+    a.wk_utw_n = p.WU;
+    a.wk_spec_n = p.WS;
+    a.hist_n = p.HS;
+    a.histv_n = p.HV;
+    a.dyn_n = 3 * int64_t(p.max_points);
+    return EMBER_OK;
+}
+
+size_t conv_plan_bytes(const ConvPlan& p, bool with_stats) {
+    const size_t nf = size_t(p.n_flames);
+    size_t b = Scratch::rounded(nf * (1 + p.S) * sizeof(int));
+    if (with_stats) b += Scratch::rounded(nf * 4 * sizeof(int));
+    b += Scratch::rounded(nf * sizeof(ConvFlame)) + Scratch::rounded(p.spec_off.size() * sizeof(int64_t));
+    b += Scratch::rounded(size_t(p.WU) * sizeof(double)) + Scratch::rounded(size_t(p.WS) * sizeof(double));
+    b += Scratch::rounded(size_t(p.HS) * sizeof(double)) + Scratch::rounded(size_t(p.HV) * sizeof(double));
+    b += Scratch::rounded(nf * sizeof(int));
+    return b;
+}
+
+int conv_plan_alloc(ConvPlan& p, Scratch& sc, bool with_stats, cudaStream_t st) {
+    ConvArgs& a = p.a;
+    const size_t nf = size_t(p.n_flames);
+    int* status = nullptr;
+    int* stats = nullptr;
+    ConvFlame* dflames = nullptr;
+    int64_t* dspec = nullptr;
+    double *wku = nullptr, *wks = nullptr, *ht = nullptr, *hv = nullptr;
+    int* nh = nullptr;
+    EMBER_TRY(sc.alloc(&status, nf * (1 + p.S)));
+    if (with_stats) EMBER_TRY(sc.alloc(&stats, nf * 4));
+    EMBER_TRY(sc.alloc(&dflames, nf));
+    EMBER_TRY(sc.alloc(&dspec, p.spec_off.size()));
+    EMBER_TRY(sc.alloc(&wku, size_t(p.WU)));
+    EMBER_TRY(sc.alloc(&wks, size_t(p.WS)));
+    EMBER_TRY(sc.alloc(&ht, size_t(p.HS)));
+    EMBER_TRY(sc.alloc(&hv, size_t(p.HV)));
+    EMBER_TRY(sc.alloc(&nh, nf));
+    EMBER_CUDA_TRY(cudaMemcpyAsync(dflames, p.hf.data(), nf * sizeof(ConvFlame), cudaMemcpyHostToDevice, st));
+    EMBER_CUDA_TRY(
+        cudaMemcpyAsync(dspec, p.spec_off.data(), p.spec_off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    a.status = status;
+    a.stats = stats;
+    a.flames = dflames;
+    a.spec_off = dspec;
+    a.wk_utw = wku;
+    a.wk_spec = wks;
+    a.hist_t = ht;
+    a.hist_v = hv;
+    a.n_hist = nh;
+    const size_t utw_smem = size_t(3) * p.max_points * sizeof(double);
+    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_conv_utw, cudaFuncAttributeMaxDynamicSharedMemorySize, int(utw_smem)));
+    return EMBER_OK;
+}
+
+int conv_launch(const ConvPlan& p, const ConvArgs& a, cudaStream_t st) {
+    if (a.stats) EMBER_CUDA_TRY(cudaMemsetAsync(a.stats, 0, size_t(p.n_flames) * 4 * sizeof(int), st));
+    k_conv_prepare<<<p.n_flames, 128, 0, st>>>(a);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    const size_t utw_smem = size_t(3) * p.max_points * sizeof(double);
+    k_conv_utw<<<p.n_flames, kNT, utw_smem, st>>>(a);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    k_conv_species<kNTSpecies><<<p.n_flames * p.S, kNTSpecies, 0, st>>>(a);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
+}  // namespace ember
+
 extern "C" int ember_convection_integrate(int n_flames, const ember_convection_flame* flames, int n_species,
                                           const double* mol_weight, const double* x, const double* y_left,
                                           const double* drhodt, const double* split_const, double* state,
@@ -1036,141 +1148,28 @@ extern "C" int ember_convection_integrate(int n_flames, const ember_convection_f
     EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
     if (n_flames == 0) return EMBER_OK;
     EMBER_CHECK_ARG(opts->t_end > opts->t_start, "t_end must be > t_start");
-    EMBER_CHECK_ARG(opts->reltol > 0 && opts->abstol_u > 0 && opts->abstol_t > 0 && opts->abstol_y > 0,
-                    "tolerances must be positive");
-    EMBER_CHECK_ARG(opts->max_steps > 0 && opts->max_history >= 2, "max_steps > 0 and max_history >= 2 required");
-    EMBER_CHECK_ARG(opts->min_step >= 0, "min_step must be >= 0");
-    EMBER_CHECK_ARG(opts->species_threads == 0 || opts->species_threads == kNTSpecies,
-                    "species_threads must be 0 or 32");
-    const int S = n_species, nv = S + 2;
-    std::vector<ConvFlame> hf(n_flames);
-    std::vector<int64_t> spec_off(size_t(n_flames) * S);
-    int64_t P = 0, V = 0, WU = 0, WS = 0, HS = 0, HV = 0;
-    int max_points = 0;
-    for (int f = 0; f < n_flames; ++f) {
-        const ember_convection_flame& g = flames[f];
-        const int N = g.n_points;
-        EMBER_CHECK_ARG(N >= 3 && N <= EMBER_CONVECTION_MAX_POINTS, "flame %d: n_points must be in [3, %d]", f,
-                        EMBER_CONVECTION_MAX_POINTS);
-        max_points = N > max_points ? N : max_points;
-        EMBER_CHECK_ARG(g.alpha == 0 || g.alpha == 1, "flame %d: alpha must be 0 or 1", f);
-        EMBER_CHECK_ARG(g.left_bc >= EMBER_BC_FIXED_VALUE && g.left_bc <= EMBER_BC_WALL_FLUX,
-                        "flame %d: bad left boundary condition %d", f, g.left_bc);
-        EMBER_CHECK_ARG(g.continuity_bc >= EMBER_CONTINUITY_LEFT && g.continuity_bc <= EMBER_CONTINUITY_TEMP,
-                        "flame %d: bad continuity boundary condition %d", f, g.continuity_bc);
-        EMBER_CHECK_ARG(g.continuity_bc == EMBER_CONTINUITY_LEFT || (g.j_cont >= 0 && g.j_cont < N),
-                        "flame %d: j_cont out of range", f);
-        EMBER_CHECK_ARG(g.continuity_bc != EMBER_CONTINUITY_TEMP || g.j_cont < N - 1,
-                        "flame %d: the temperature continuity point needs a right neighbour", f);
-        EMBER_CHECK_ARG(g.beta > 0 && g.pressure > 0, "flame %d: beta and pressure must be positive", f);
-        EMBER_CHECK_ARG(g.strain_dt >= 0, "flame %d: strain_dt must be >= 0", f);
-        hf[f].f = g;
-        hf[f].p0 = P;
-        hf[f].v0 = V;
-        hf[f].utw_wk = WU;
-        hf[f].hist = HS;
-        hf[f].histv = HV;
-        for (int k = 0; k < S; ++k) {
-            spec_off[size_t(f) * S + k] = WS;
-            WS += int64_t(kWorkVectors) * N;
-        }
-        P += N;
-        V += int64_t(nv) * N;
-        WU += int64_t(kWorkVectors) * 3 * N + int64_t(kUtwScratch) * N;
-        HS += int64_t(opts->max_history);
-        HV += int64_t(opts->max_history) * N;
-    }
+    const int S = n_species;
+    ConvPlan p;
+    EMBER_TRY(conv_plan_layout(p, n_flames, flames, S, opts));
     EMBER_TRY(ensure_device());
     cudaStream_t st = as_stream(stream);
     Scratch sc(st);
-    const double *dW, *dx, *dyl, *ddr, *dsp;
-    EMBER_TRY(stage_in(sc, mol_weight, size_t(S), mem, st, &dW));
-    EMBER_TRY(stage_in(sc, x, size_t(P), mem, st, &dx));
-    EMBER_TRY(stage_in(sc, y_left, size_t(n_flames) * S, mem, st, &dyl));
-    EMBER_TRY(stage_in(sc, drhodt, size_t(P), mem, st, &ddr));
-    EMBER_TRY(stage_in(sc, split_const, size_t(V), mem, st, &dsp));
-    double* dstate = nullptr;
-    EMBER_TRY(stage_buffer(sc, state, size_t(V), mem, &dstate));
+    ConvArgs& a = p.a;
+    EMBER_TRY(stage_in(sc, mol_weight, size_t(S), mem, st, &a.W));
+    EMBER_TRY(stage_in(sc, x, size_t(p.P), mem, st, &a.x));
+    EMBER_TRY(stage_in(sc, y_left, size_t(n_flames) * S, mem, st, &a.y_left));
+    EMBER_TRY(stage_in(sc, drhodt, size_t(p.P), mem, st, &a.drhodt));
+    EMBER_TRY(stage_in(sc, split_const, size_t(p.V), mem, st, &a.split));
+    EMBER_TRY(stage_buffer(sc, state, size_t(p.V), mem, &a.state));
     if (mem == EMBER_MEM_HOST)
-        EMBER_CUDA_TRY(cudaMemcpyAsync(dstate, state, size_t(V) * sizeof(double), cudaMemcpyHostToDevice, st));
-    int* dstatus = nullptr;
-    EMBER_TRY(sc.alloc(&dstatus, size_t(n_flames) * (1 + S)));
-    int* dstats = nullptr;
-    if (stats) {
-        EMBER_TRY(sc.alloc(&dstats, size_t(n_flames) * 4));
-        EMBER_CUDA_TRY(cudaMemsetAsync(dstats, 0, size_t(n_flames) * 4 * sizeof(int), st));
-    }
-    ConvFlame* dflames = nullptr;
-    int64_t* dspec = nullptr;
-    double *wku = nullptr, *wks = nullptr, *ht = nullptr, *hv = nullptr;
-    int* nh = nullptr;
-    EMBER_TRY(sc.alloc(&dflames, size_t(n_flames)));
-    EMBER_TRY(sc.alloc(&dspec, spec_off.size()));
-    EMBER_TRY(sc.alloc(&wku, size_t(WU)));
-    EMBER_TRY(sc.alloc(&wks, size_t(WS)));
-    EMBER_TRY(sc.alloc(&ht, size_t(HS)));
-    EMBER_TRY(sc.alloc(&hv, size_t(HV)));
-    EMBER_TRY(sc.alloc(&nh, size_t(n_flames)));
-    EMBER_CUDA_TRY(cudaMemcpyAsync(dflames, hf.data(), hf.size() * sizeof(ConvFlame), cudaMemcpyHostToDevice, st));
-    EMBER_CUDA_TRY(
-        cudaMemcpyAsync(dspec, spec_off.data(), spec_off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
-    ConvArgs a{};
-    a.n_flames = n_flames;
-    a.S = S;
-    a.flames = dflames;
-    a.W = dW;
-    a.x = dx;
-    a.y_left = dyl;
-    a.drhodt = ddr;
-    a.split = dsp;
-    a.state = dstate;
-    a.wk_utw = wku;
-    a.wk_spec = wks;
-    a.spec_off = dspec;
-    a.hist_t = ht;
-    a.hist_v = hv;
-    a.n_hist = nh;
-    a.status = dstatus;
-    a.stats = dstats;
-    a.t0 = opts->t_start;
-    a.tf = opts->t_end;
-    a.reltol = opts->reltol;
-    a.abstol_u = opts->abstol_u;
-    a.abstol_t = opts->abstol_t;
-    a.abstol_y = opts->abstol_y;
-    a.min_step = opts->min_step;
-    a.max_steps = opts->max_steps;
-    a.max_history = opts->max_history;
-    a.wk_utw_n = WU;
-    a.wk_spec_n = WS;
-    a.hist_n = HS;
-    a.histv_n = HV;
-    a.dyn_n = 3 * int64_t(max_points);
-    k_conv_prepare<<<n_flames, 128, 0, st>>>(a);
-    EMBER_CUDA_TRY(cudaGetLastError());
-    const size_t utw_smem = size_t(3) * max_points * sizeof(double);
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_conv_utw, cudaFuncAttributeMaxDynamicSharedMemorySize, int(utw_smem)));
-    k_conv_utw<<<n_flames, kNT, utw_smem, st>>>(a);
-    EMBER_CUDA_TRY(cudaGetLastError());
-    k_conv_species<kNTSpecies><<<n_flames * S, kNTSpecies, 0, st>>>(a);
-    EMBER_CUDA_TRY(cudaGetLastError());
-    EMBER_TRY(stage_out(state, dstate, size_t(V), mem, st));
-    if (status) {
-        if (mem == EMBER_MEM_HOST)
-            EMBER_CUDA_TRY(cudaMemcpyAsync(status, dstatus, size_t(n_flames) * (1 + S) * sizeof(int),
-                                           cudaMemcpyDeviceToHost, st));
-        else
-            EMBER_CUDA_TRY(cudaMemcpyAsync(status, dstatus, size_t(n_flames) * (1 + S) * sizeof(int),
-                                           cudaMemcpyDeviceToDevice, st));
-    }
-    if (stats) {
-        if (mem == EMBER_MEM_HOST)
-            EMBER_CUDA_TRY(
-                cudaMemcpyAsync(stats, dstats, size_t(n_flames) * 4 * sizeof(int), cudaMemcpyDeviceToHost, st));
-        else
-            EMBER_CUDA_TRY(
-                cudaMemcpyAsync(stats, dstats, size_t(n_flames) * 4 * sizeof(int), cudaMemcpyDeviceToDevice, st));
-    }
+        EMBER_CUDA_TRY(cudaMemcpyAsync(a.state, state, size_t(p.V) * sizeof(double), cudaMemcpyHostToDevice, st));
+    EMBER_TRY(conv_plan_alloc(p, sc, stats != nullptr, st));
+    EMBER_TRY(conv_launch(p, a, st));
+    EMBER_TRY(stage_out(state, a.state, size_t(p.V), mem, st));
+    const cudaMemcpyKind kind = mem == EMBER_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    if (status)
+        EMBER_CUDA_TRY(cudaMemcpyAsync(status, a.status, size_t(n_flames) * (1 + S) * sizeof(int), kind, st));
+    if (stats) EMBER_CUDA_TRY(cudaMemcpyAsync(stats, a.stats, size_t(n_flames) * 4 * sizeof(int), kind, st));
     const int rc = finish_call(mem, st);
     sc.release();
     return rc;

@@ -25,6 +25,7 @@
 // so with the serial diffusion algorithm the step reproduces the CPU
 // restatement bit for bit.
 #include "common.cuh"
+#include "convection.cuh"
 #include "source.cuh"
 #include "transport.cuh"
 #include "tridiag.cuh"
@@ -86,20 +87,35 @@ __global__ void k_diff_accumulate(int64_t n_vals, const double* __restrict__ yv,
 
 // Start of a step (SplitSolver::step, src/splitSolver.cpp:38-46): split
 // constants from the previous step's time derivatives, deltaDiff = 0.
-// Balanced splitting of the two integrated operators gives each half of the
-// total rate: c_D = (f_S + f_X - f_D) / 2, c_S = (f_D + f_X - f_S) / 2; the
-// plain Strang variant uses c_D = f_X, c_S = 0.
+// Without convection, balanced splitting of the two integrated operators
+// gives each half of the total rate: c_D = (f_S + f_X - f_D) / 2,
+// c_S = (f_D + f_X - f_S) / 2. With convection (ddt_conv set) the reference's
+// three-operator constants: c_D = (f_S + f_C + f_X - 3 f_D) / 4,
+// c_C = (f_S + f_D + f_X - 3 f_C) / 4, c_S = (f_C + f_D + f_X - f_S) / 2.
+// The plain Strang variant uses c_D = f_X and zero for the others.
 __global__ void k_split_begin(SplitTables tb, int balanced, const double* __restrict__ ddt_diff,
                               const double* __restrict__ ddt_prod, const double* __restrict__ ddt_cross,
                               double* __restrict__ sc_diff, double* __restrict__ sc_diff_vm,
-                              double* __restrict__ sc_prod, double* __restrict__ delta_diff_vm) {
+                              double* __restrict__ sc_prod, double* __restrict__ delta_diff_vm,
+                              const double* __restrict__ ddt_conv, double* __restrict__ sc_conv,
+                              double* __restrict__ sc_conv_vm, double* __restrict__ delta_conv_vm) {
     const int64_t total = tb.n_pts * tb.n;
     for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
         const int64_t p = e / tb.n;
         const int v = static_cast<int>(e - p * tb.n);
         const double fx = ddt_cross ? ddt_cross[e] : 0.0;
-        double cd, cs;
-        if (balanced) {
+        double cd, cs, cc = 0.0;
+        if (ddt_conv) {
+            const double fd = ddt_diff[e], fs = ddt_prod[e], fc = ddt_conv[e];
+            if (balanced) {
+                cd = 0.25 * (((fs + fc) + fx) - 3.0 * fd);
+                cc = 0.25 * (((fs + fd) + fx) - 3.0 * fc);
+                cs = 0.5 * (((fc + fd) + fx) - fs);
+            } else {
+                cd = fx;
+                cs = 0.0;
+            }
+        } else if (balanced) {
             cd = 0.5 * ((ddt_prod[e] + fx) - ddt_diff[e]);
             cs = 0.5 * ((ddt_diff[e] + fx) - ddt_prod[e]);
         } else {
@@ -111,6 +127,44 @@ __global__ void k_split_begin(SplitTables tb, int balanced, const double* __rest
         sc_diff_vm[q] = cd;
         sc_prod[e] = cs;
         delta_diff_vm[q] = 0.0;
+        if (ddt_conv) {
+            sc_conv[e] = cc;
+            sc_conv_vm[q] = cc;
+            delta_conv_vm[q] = 0.0;
+        }
+    }
+}
+
+// FlameSolver::prepareIntegrators' density derivative for the convection
+// stage (src/flameSolver.cpp:208-212): ddt = ddtConv + ddtDiff + ddtProd
+// (+ ddtCross when balanced), drho/dt = -rho (ddt_T / T + W sum_k ddt_Yk / W_k),
+// with rho and the mean molecular weight W of the step-start state (mass
+// fractions clipped at zero and normalised, sums in species order).
+__global__ void k_density_derivative(int64_t n_pts, int n, int balanced, double pressure,
+                                     const double* __restrict__ W, const double* __restrict__ state,
+                                     const double* __restrict__ ddt_conv, const double* __restrict__ ddt_diff,
+                                     const double* __restrict__ ddt_prod, const double* __restrict__ ddt_cross,
+                                     double* __restrict__ drhodt) {
+    const double R = 6.02214076e26 * 1.380649e-23;
+    for (int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; p < n_pts; p += int64_t(gridDim.x) * blockDim.x) {
+        const double* s = state + p * n;
+        const int64_t e0 = p * n;
+        double ysum = 0.0;
+        for (int k = 2; k < n; ++k) ysum = ysum + (s[k] < 0.0 ? 0.0 : s[k]);
+        const double rnorm = 1.0 / ysum;
+        double acc = 0.0;
+        for (int k = 2; k < n; ++k) acc = acc + ((s[k] < 0.0 ? 0.0 : s[k]) * rnorm) / W[k - 2];
+        const double wmx = 1.0 / acc;
+        const double T = s[1];
+        const double rho = (pressure * wmx) / (R * T);
+        auto ddt = [&](int64_t e) {
+            double d = (ddt_conv[e] + ddt_diff[e]) + ddt_prod[e];
+            if (balanced && ddt_cross) d = d + ddt_cross[e];
+            return d;
+        };
+        double tmp = 0.0;
+        for (int k = 2; k < n; ++k) tmp = tmp + ddt(e0 + k) / W[k - 2];
+        drhodt[p] = -rho * (ddt(e0 + 1) / T + tmp * wmx);
     }
 }
 
@@ -127,7 +181,8 @@ __global__ void k_stage_dt(int64_t n_pts, const double* __restrict__ t_dev, doub
 __global__ void k_split_end(SplitTables tb, double dt, const double* __restrict__ xS, const double* __restrict__ xD2,
                             const double* __restrict__ delta_diff_vm, const double* __restrict__ sc_diff,
                             const double* __restrict__ sc_prod, double* __restrict__ ddt_diff,
-                            double* __restrict__ ddt_prod) {
+                            double* __restrict__ ddt_prod, const double* __restrict__ delta_conv_vm,
+                            const double* __restrict__ sc_conv, double* __restrict__ ddt_conv) {
     const int64_t total = tb.n_pts * tb.n;
     for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < total; e += int64_t(gridDim.x) * blockDim.x) {
         const int64_t p = e / tb.n;
@@ -135,6 +190,7 @@ __global__ void k_split_end(SplitTables tb, double dt, const double* __restrict_
         const double delta_prod = xS[e] - xD2[e];
         ddt_diff[e] = delta_diff_vm[vm_index(tb, p, v)] / dt - sc_diff[e];
         ddt_prod[e] = delta_prod / dt - sc_prod[e];
+        if (ddt_conv) ddt_conv[e] = delta_conv_vm[vm_index(tb, p, v)] / dt - sc_conv[e];
     }
 }
 
@@ -559,6 +615,12 @@ struct ember_split_s {
     DiffusionWarpPlan jplan;  // jCorr systems (one per flame) with the warp-parallel algorithm
     ember_diffusion_grid* d_grids = nullptr;
     int *jstatus = nullptr, *pt_local = nullptr, *pt_flame = nullptr;
+    // convection stage (ember_split_set_convection): D C D S D C D
+    bool conv = false;
+    ConvPlan cplan;
+    void* cblob = nullptr;
+    double *ddt_conv = nullptr, *sc_conv = nullptr, *sc_conv_vm = nullptr, *delta_conv_vm = nullptr;
+    double *drhodt = nullptr, *y_left = nullptr;
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -601,6 +663,39 @@ int copy_to_device(double* dst, const double* src, size_t n, int mem, cudaStream
     EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
     EMBER_CUDA_TRY(cudaMemcpyAsync(dst, src, n * sizeof(double),
                                    mem == EMBER_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, st));
+    return EMBER_OK;
+}
+
+// One diffusion stage on the variable-major copy, its change added to deltaDiff.
+int enqueue_diffusion_stage(ember_split h, double f0, double f1, cudaStream_t st) {
+    const DiffusionView dv = h->diffusion_view(h->diff_status);
+    StageTime tm;
+    tm.t_dev = h->t_dev;
+    tm.f0 = f0;
+    tm.f1 = f1;
+    tm.dt = h->opt.dt;
+    if (h->opt.diffusion_algorithm == EMBER_DIFFUSION_PARALLEL) {
+        EMBER_TRY(diffusion_warp_run(h->plan, dv, h->yv, tm, h->opt.dt_multiplier, h->opt.dt, st));
+    } else {
+        EMBER_TRY(diffusion_serial_run(dv, h->yv, h->serial_work, h->n_vals, h->nmax, tm, h->opt.dt_multiplier,
+                                       h->opt.dt, st));
+    }
+    k_count_failures<<<grid_for(dv.n_systems), 256, 0, st>>>(dv.n_systems, h->diff_status, h->fails + 1);
+    k_diff_accumulate<<<grid_for(h->n_vals), 256, 0, st>>>(h->n_vals, h->yv, h->ystart, h->delta_vm);
+    return EMBER_OK;
+}
+
+// One convection stage (SplitSolver::_integrateConvectionTerms,
+// src/splitSolver.cpp:106-121) on the variable-major copy, from t + f0 dt to
+// t + f1 dt of the device clock, its change added to deltaConv.
+int enqueue_convection_stage(ember_split h, double f0, double f1, cudaStream_t st) {
+    ConvArgs a = h->cplan.a;
+    a.f0 = f0;
+    a.f1 = f1;
+    EMBER_TRY(conv_launch(h->cplan, a, st));
+    const int ns = h->n_flames * (1 + h->cplan.S);
+    k_count_failures<<<grid_for(ns), 256, 0, st>>>(ns, a.status, h->fails + 1);
+    k_diff_accumulate<<<grid_for(h->n_vals), 256, 0, st>>>(h->n_vals, h->yv, h->ystart, h->delta_conv_vm);
     return EMBER_OK;
 }
 
@@ -696,10 +791,24 @@ int enqueue_step(ember_split h, cudaStream_t st, const StepTape* tape = nullptr)
     const int g = grid_for(h->n_vals);
     if (tape) EMBER_CUDA_TRY(cudaMemcpyAsync(tape->t_saved, h->t_dev, sizeof(double), cudaMemcpyDeviceToDevice, st));
     if (h->tr) EMBER_TRY(enqueue_properties(h, st));
+    if (h->conv)
+        k_density_derivative<<<grid_for(h->n_pts), 256, 0, st>>>(h->n_pts, h->n_vars, h->opt.balanced,
+                                                                 h->opt.source.pressure, h->mech->view.W, h->state,
+                                                                 h->ddt_conv, h->ddt_diff, h->ddt_prod, h->ddt_cross,
+                                                                 h->drhodt);
     k_split_begin<<<g, 256, 0, st>>>(tb, h->opt.balanced, h->ddt_diff, h->ddt_prod, h->ddt_cross, h->sc_diff,
-                                     h->sc_diff_vm, h->sc_prod, h->delta_vm);
-    // diffusion 1/4 and 2/4
-    EMBER_TRY(enqueue_diffusion_pair(h, 0.0, 0.25, 0.5, st));
+                                     h->sc_diff_vm, h->sc_prod, h->delta_vm, h->conv ? h->ddt_conv : nullptr,
+                                     h->sc_conv, h->sc_conv_vm, h->delta_conv_vm);
+    if (h->conv) {
+        // diffusion 1/4, convection 1/2, diffusion 2/4 (src/splitSolver.cpp:68-70)
+        k_to_varmajor<<<g, 256, 0, st>>>(tb, h->state, h->yv, h->ystart);
+        EMBER_TRY(enqueue_diffusion_stage(h, 0.0, 0.25, st));
+        EMBER_TRY(enqueue_convection_stage(h, 0.0, 0.5, st));
+        EMBER_TRY(enqueue_diffusion_stage(h, 0.25, 0.5, st));
+    } else {
+        // diffusion 1/4 and 2/4
+        EMBER_TRY(enqueue_diffusion_pair(h, 0.0, 0.25, 0.5, st));
+    }
     k_to_pointmajor<<<g, 256, 0, st>>>(tb, h->yv, h->state, h->xD2);
     // source term over the whole step
     k_stage_dt<<<grid_for(h->n_pts), 256, 0, st>>>(h->n_pts, h->t_dev, h->opt.dt, h->dtp);
@@ -720,11 +829,19 @@ int enqueue_step(ember_split h, cudaStream_t st, const StepTape* tape = nullptr)
     }
     k_count_failures<<<grid_for(h->n_pts), 256, 0, st>>>(static_cast<int>(h->n_pts), h->src_status, h->fails);
     EMBER_CUDA_TRY(cudaMemcpyAsync(h->xS, h->state, sizeof(double) * h->n_vals, cudaMemcpyDeviceToDevice, st));
-    // diffusion 3/4 and 4/4
-    EMBER_TRY(enqueue_diffusion_pair(h, 0.5, 0.75, 1.0, st));
+    if (h->conv) {
+        // diffusion 3/4, convection 2/2, diffusion 4/4 (src/splitSolver.cpp:72-74)
+        k_to_varmajor<<<g, 256, 0, st>>>(tb, h->state, h->yv, h->ystart);
+        EMBER_TRY(enqueue_diffusion_stage(h, 0.5, 0.75, st));
+        EMBER_TRY(enqueue_convection_stage(h, 0.5, 1.0, st));
+        EMBER_TRY(enqueue_diffusion_stage(h, 0.75, 1.0, st));
+    } else {
+        // diffusion 3/4 and 4/4
+        EMBER_TRY(enqueue_diffusion_pair(h, 0.5, 0.75, 1.0, st));
+    }
     k_to_pointmajor<<<g, 256, 0, st>>>(tb, h->yv, h->state, nullptr);
     k_split_end<<<g, 256, 0, st>>>(tb, h->opt.dt, h->xS, h->xD2, h->delta_vm, h->sc_diff, h->sc_prod, h->ddt_diff,
-                                   h->ddt_prod);
+                                   h->ddt_prod, h->delta_conv_vm, h->sc_conv, h->conv ? h->ddt_conv : nullptr);
     if (tape) EMBER_CUDA_TRY(cudaMemcpyAsync(tape->xF, h->state, sizeof(double) * h->n_vals, cudaMemcpyDeviceToDevice, st));
     k_correct_mass_fractions<<<grid_for(h->n_pts, 128), 128, 0, st>>>(h->n_pts, h->n_vars, h->state);
     k_advance_clock<<<1, 32, 0, st>>>(h->t_dev, h->opt.dt);
@@ -739,6 +856,7 @@ void free_split(ember_split h) {
     if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
     cudaFree(h->blob);
     cudaFree(h->pblob);
+    cudaFree(h->cblob);
     delete h;
 }
 
@@ -924,6 +1042,7 @@ extern "C" int ember_split_set_state(ember_split h, double t, const double* stat
     EMBER_CUDA_TRY(cudaMemcpyAsync(h->t_dev, &t, sizeof(double), cudaMemcpyHostToDevice, st));
     EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_diff, 0, sizeof(double) * h->n_vals, st));
     EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_prod, 0, sizeof(double) * h->n_vals, st));
+    if (h->conv) EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_conv, 0, sizeof(double) * h->n_vals, st));
     EMBER_CUDA_TRY(cudaMemsetAsync(h->fails, 0, 2 * sizeof(unsigned long long), st));
     // the host value of t must outlive the copy
     EMBER_CUDA_TRY(cudaStreamSynchronize(st));
@@ -951,6 +1070,64 @@ extern "C" int ember_split_set_transport(ember_split h, const double* B, const d
         EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_cross, 0, sizeof(double) * h->n_vals, st));
     }
     return finish_call(mem, st);
+}
+
+extern "C" int ember_split_set_convection(ember_split h, const ember_convection_flame* flames,
+                                         const double* y_left, const ember_convection_options* opts) {
+    EMBER_TRY(check_split(h));
+    EMBER_TRY(ensure_device());
+    // the captured graph (if any) has the old stage list
+    if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->graph_exec = nullptr;
+    h->graph = nullptr;
+    EMBER_CUDA_TRY(cudaDeviceSynchronize());
+    cudaFree(h->cblob);
+    h->cblob = nullptr;
+    h->conv = false;
+    if (!flames) return EMBER_OK;
+    EMBER_CHECK_ARG(y_left != nullptr && opts != nullptr, "null y_left or options");
+    const int S = h->n_vars - 2;
+    for (int f = 0; f < h->n_flames; ++f) {
+        EMBER_CHECK_ARG(flames[f].n_points == h->grids[f].n_points, "flame %d: n_points %d differs from the grid's %d",
+                        f, flames[f].n_points, h->grids[f].n_points);
+        EMBER_CHECK_ARG(flames[f].alpha == h->grids[f].alpha, "flame %d: alpha differs from the grid's", f);
+    }
+    ConvPlan p;
+    EMBER_TRY(conv_plan_layout(p, h->n_flames, flames, S, opts));
+    const size_t nv = size_t(h->n_vals);
+    const size_t bytes = conv_plan_bytes(p, false) + 4 * Scratch::rounded(nv * sizeof(double)) +
+                         Scratch::rounded(size_t(h->n_pts) * sizeof(double)) +
+                         Scratch::rounded(size_t(h->n_flames) * S * sizeof(double));
+    cudaError_t e = cudaMalloc(&h->cblob, bytes);
+    if (e != cudaSuccess) {
+        h->cblob = nullptr;
+        set_error("ember_split_set_convection: cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? EMBER_ENOMEM : EMBER_ECUDA;
+    }
+    Scratch a(nullptr, h->cblob, bytes);
+    EMBER_TRY(a.alloc(&h->ddt_conv, nv));
+    EMBER_TRY(a.alloc(&h->sc_conv, nv));
+    EMBER_TRY(a.alloc(&h->sc_conv_vm, nv));
+    EMBER_TRY(a.alloc(&h->delta_conv_vm, nv));
+    EMBER_TRY(a.alloc(&h->drhodt, size_t(h->n_pts)));
+    EMBER_TRY(a.alloc(&h->y_left, size_t(h->n_flames) * S));
+    EMBER_TRY(conv_plan_alloc(p, a, false, nullptr));
+    EMBER_CUDA_TRY(cudaMemcpy(h->y_left, y_left, sizeof(double) * h->n_flames * S, cudaMemcpyHostToDevice));
+    EMBER_CUDA_TRY(cudaMemset(h->ddt_conv, 0, sizeof(double) * nv));
+    EMBER_CUDA_TRY(cudaDeviceSynchronize());
+    ConvArgs& c = p.a;
+    c.W = h->mech->view.W;
+    c.x = h->x;
+    c.y_left = h->y_left;
+    c.drhodt = h->drhodt;
+    c.split = h->sc_conv_vm;
+    c.state = h->yv;
+    c.t_dev = h->t_dev;
+    c.dt = h->opt.dt;
+    h->cplan = std::move(p);
+    h->conv = true;
+    return EMBER_OK;
 }
 
 extern "C" int ember_split_set_transport_model(ember_split h, ember_transport tr, double threshold,
@@ -1167,6 +1344,7 @@ extern "C" int ember_split_adjoint(ember_split h, const double* w_heat_release, 
     EMBER_TRY(check_split(h));
     EMBER_CHECK_ARG(h->opt.method == EMBER_SOURCE_BDF, "the split-step adjoint needs EMBER_SOURCE_BDF");
     EMBER_CHECK_ARG(h->tr == nullptr, "the split-step adjoint holds B and D fixed: detach the transport model");
+    EMBER_CHECK_ARG(!h->conv, "the split-step adjoint covers D-S-D: detach the convection stage");
     EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
     EMBER_CHECK_ARG(w_heat_release || w_consumption_speed, "no objective weights");
     EMBER_CHECK_ARG(!w_consumption_speed || (rho_u && ju && jb), "consumption speed needs rho_u, ju and jb");

@@ -42,6 +42,7 @@ def _declare(lib):
         "ember_split_failures": (C.c_int, [vp, vp, vp, vp]),
         "ember_split_objectives": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, C.c_int, vp]),
         "ember_split_adjoint": (C.c_int, [vp, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, C.c_int, vp]),
+        "ember_split_set_convection": (C.c_int, [vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -138,6 +139,23 @@ class FlameBatchSplitSolver:
         L.check(_lib().ember_split_set_transport_model(self._h, transport.handle if transport is not None else None,
                                                        float(threshold), int(bool(cross_terms))),
                 "ember_split_set_transport_model")
+
+    def set_convection(self, flames=None, y_left=None, opts=None):
+        """ember_split_set_convection: every step becomes D C D S D C D with
+        the convection stage of ``flames`` (ember_gb300.convection.
+        ConvectionFlame, one per flame; y_left [n_flames, S]; opts a
+        ConvectionOptions); None detaches."""
+        if flames is None:
+            L.check(_lib().ember_split_set_convection(self._h, None, None, None), "ember_split_set_convection")
+            return
+        from .convection import ConvectionFlameC, ConvectionOptions, ConvectionOptionsC
+        opts = opts or ConvectionOptions()
+        arr = (ConvectionFlameC * len(flames))(*[f.as_c() for f in flames])
+        o = ConvectionOptionsC(0.0, 0.0, opts.reltol, opts.abstol_u, opts.abstol_t, opts.abstol_y, opts.min_step,
+                               int(opts.max_steps), int(opts.max_history), int(opts.species_threads))
+        yl = np.ascontiguousarray(y_left, dtype=np.float64)
+        L.check(_lib().ember_split_set_convection(self._h, C.addressof(arr), yl.ctypes.data, C.byref(o)),
+                "ember_split_set_convection")
 
     def step(self, n_steps: int = 1, graph: bool = False, stream=None):
         L.check(_lib().ember_split_step(self._h, int(n_steps), int(bool(graph)), L.stream_ptr(stream)),

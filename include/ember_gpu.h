@@ -624,6 +624,21 @@ int ember_split_set_transport(ember_split split, const double* B, const double* 
  * The properties are part of the captured graph. The split-step adjoint holds
  * B and D fixed and so requires no transport model. */
 int ember_split_set_transport_model(ember_split split, ember_transport tr, double threshold, int cross_terms);
+
+/* Add the convection stage to every split step: the step becomes the
+ * reference's D(1/4) C(1/2) D(1/4) S D(1/4) C(1/2) D(1/4)
+ * (SplitSolver::integrateSplitTerms, src/splitSolver.cpp:60-76) with the
+ * three-operator balanced split constants (38-46) and the convection stage's
+ * density derivative from the step's time derivatives (FlameSolver::
+ * prepareIntegrators, src/flameSolver.cpp:208-213). flames: one per flame
+ * of the handle (n_points and alpha as its grid); y_left: S mass fractions
+ * per flame; opts: tolerances and limits of ember_convection_integrate
+ * (t_start, t_end unused). flames == NULL detaches the stage. Host memory;
+ * the handle keeps its own copies and a fixed workspace, so the stage is part
+ * of the captured step graph. The split-step adjoint covers D-S-D only and
+ * refuses a handle with the stage attached. */
+int ember_split_set_convection(ember_split split, const ember_convection_flame* flames, const double* y_left,
+                               const ember_convection_options* opts);
 /* n_steps split steps, asynchronous on `stream`. */
 int ember_split_step(ember_split split, int n_steps, int use_graph, void* stream);
 int ember_split_get_state(ember_split split, double* state, double* t, int mem, void* stream);

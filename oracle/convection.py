@@ -43,7 +43,20 @@ def _lib():
     l.oracle_convection_interval.restype = i
     l.oracle_convection_flame.argtypes = [vp, i, vp, vp, vp, d, d, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     l.oracle_convection_flame.restype = i
+    l.oracle_convection_drhodt.argtypes = [i, i, i, d, vp, vp, vp, vp, vp, vp, vp]
+    l.oracle_convection_drhodt.restype = None
     return l
+
+
+def density_derivative(state, W, pressure, ddt_conv, ddt_diff, ddt_prod, ddt_cross, balanced):
+    """drho/dt per point of point-major arrays (prepareIntegrators)."""
+    state = np.ascontiguousarray(state, dtype=np.float64)
+    n_pts, n = state.shape
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (W, ddt_conv, ddt_diff, ddt_prod, ddt_cross)]
+    out = np.zeros(n_pts)
+    _lib().oracle_convection_drhodt(n_pts, n, int(bool(balanced)), float(pressure), _p(arrs[0]), _p(state),
+                                    _p(arrs[1]), _p(arrs[2]), _p(arrs[3]), _p(arrs[4]), _p(out))
+    return out
 
 
 def _p(a):

@@ -169,6 +169,9 @@ void oracle_convection_utw_rhs(const oracle_conv_flame* fl, const double* x, con
                                const double* sT, const double* sW, double* ydot, double* rho, double* rV,
                                double* V);
 int oracle_convection_interval(const double* ht, int H, double t, double* s);
+void oracle_convection_drhodt(int n_pts, int n, int balanced, double pressure, const double* W, const double* state,
+                              const double* ddt_conv, const double* ddt_diff, const double* ddt_prod,
+                              const double* ddt_cross, double* drhodt);
 int oracle_convection_flame(const oracle_conv_flame* fl, int S, const double* W, const double* x,
                             const double* y_left, double t0, double tf, const double* drhodt, const double* split,
                             double* state, const oracle_conv_options* o, int* status, int* stats,

@@ -717,3 +717,35 @@ int oracle_convection_flame(const oracle_conv_flame* fl, int S, const double* W,
     free(hv);
     return rc;
 }
+
+static double ddt_sum(size_t e, int balanced, const double* c, const double* d, const double* p, const double* x) {
+    double v = (c[e] + d[e]) + p[e];
+    if (balanced && x) v = v + x[e];
+    return v;
+}
+
+/* FlameSolver::prepareIntegrators' density derivative for the convection
+ * stage (src/flameSolver.cpp:208-212), point-major [n_pts][n] arrays:
+ * ddt = ddtConv + ddtDiff + ddtProd (+ ddtCross when balanced),
+ * drho/dt = -rho (ddt_T / T + W sum_k ddt_Yk / W_k) with rho and the mean
+ * molecular weight W of the state (mass fractions clipped at zero and
+ * normalised; sums in species order). */
+void oracle_convection_drhodt(int n_pts, int n, int balanced, double pressure, const double* W, const double* state,
+                              const double* ddt_conv, const double* ddt_diff, const double* ddt_prod,
+                              const double* ddt_cross, double* drhodt) {
+    for (int p = 0; p < n_pts; ++p) {
+        const double* s = state + (size_t)p * n;
+        const size_t e0 = (size_t)p * n;
+        double ysum = 0.0;
+        for (int k = 2; k < n; ++k) ysum = ysum + (s[k] < 0.0 ? 0.0 : s[k]);
+        const double rnorm = 1.0 / ysum;
+        double acc = 0.0;
+        for (int k = 2; k < n; ++k) acc = acc + ((s[k] < 0.0 ? 0.0 : s[k]) * rnorm) / W[k - 2];
+        const double wmx = 1.0 / acc;
+        const double T = s[1];
+        const double rho = (pressure * wmx) / (GAS_CONSTANT * T);
+        double tmp = 0.0;
+        for (int k = 2; k < n; ++k) tmp = tmp + ddt_sum(e0 + k, balanced, ddt_conv, ddt_diff, ddt_prod, ddt_cross) / W[k - 2];
+        drhodt[p] = -rho * (ddt_sum(e0 + 1, balanced, ddt_conv, ddt_diff, ddt_prod, ddt_cross) / T + tmp * wmx);
+    }
+}

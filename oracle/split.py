@@ -5,8 +5,11 @@ operation order, built from the oracle's diffusion systems (oracle_tridiag.c)
 and source-term integrators (oracle_chem.c / oracle_bdf.c):
 
   SplitSolver::step / integrateSplitTerms / calculateTimeDerivatives
-      src/splitSolver.cpp:27-121 (convection stages not integrated; the
-      two-operator balanced split constants of the device split step)
+      src/splitSolver.cpp:27-121: D-S-D with the two-operator balanced
+      split constants of the device split step, or, with a convection stage
+      (oracle_convection.c), the reference's D C D S D C D with its
+      three-operator constants and prepareIntegrators' density derivative
+      (src/flameSolver.cpp:208-213)
   FlameSolver::setDiffusionSolverState / integrateDiffusionTerms
       src/flameSolver.cpp:702-718, 838-854
   FlameSolver::setProductionSolverState / integrateProductionTerms
@@ -122,13 +125,15 @@ def step_properties(omech, tdata, grids, state, pressure, threshold, mult, gdt, 
 
 
 def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cross=None, balanced=True,
-                mult=10.0, ddt=None, transport=None):
+                mult=10.0, ddt=None, transport=None, convection=None):
     """n_steps split steps of a batch of flames. state: point-major [n_pts, n]
     (copied); B, D: variable-major per flame (flat). transport: None, or
     (TransportData, threshold, cross_terms): B, D (and the cross terms) are
     then recomputed from the state at the start of every step
-    (step_properties). Returns (state, t, ddt_diff, ddt_prod,
-    source_status_of_last_step)."""
+    (step_properties). convection: None, or (flames, y_left, options) of
+    the convection stage (ConvectionFlame-like objects, [n_flames, S], a
+    ConvectionOptions): the step is then D C D S D C D. Returns (state, t,
+    ddt_diff, ddt_prod, source_status_of_last_step)."""
     state = np.array(state, dtype=np.float64, copy=True)
     n_pts, n = state.shape
     offs = np.cumsum([0] + [g.n_points for g in grids])
@@ -137,6 +142,8 @@ def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cro
     cross = np.zeros_like(state) if ddt_cross is None else np.asarray(ddt_cross, dtype=np.float64).reshape(n_pts, n)
     ddt_diff = np.zeros_like(state) if ddt is None else ddt[0].copy()
     ddt_prod = np.zeros_like(state) if ddt is None else ddt[1].copy()
+    ddt_conv = np.zeros_like(state)
+    W = np.asarray(omech.mech.mol_weight, dtype=np.float64)
     status = None
     for _ in range(n_steps):
         if transport is not None:
@@ -144,13 +151,40 @@ def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cro
             B, D, c = step_properties(omech, tdata, grids, state, opts.pressure, thr, mult, dt, with_cross)
             if with_cross:
                 cross = c
-        if balanced:
+        if convection is not None:
+            from oracle import convection as oconv
+            drhodt = oconv.density_derivative(state, W, opts.pressure, ddt_conv, ddt_diff, ddt_prod, cross, balanced)
+            if balanced:
+                sc_diff = 0.25 * (((ddt_prod + ddt_conv) + cross) - 3.0 * ddt_diff)
+                sc_conv = 0.25 * (((ddt_prod + ddt_diff) + cross) - 3.0 * ddt_conv)
+                sc_prod = 0.5 * (((ddt_conv + ddt_diff) + cross) - ddt_prod)
+            else:
+                sc_diff = cross.copy()
+                sc_conv = np.zeros_like(state)
+                sc_prod = np.zeros_like(state)
+        elif balanced:
             sc_diff = 0.5 * ((ddt_prod + cross) - ddt_diff)
             sc_prod = 0.5 * ((ddt_diff + cross) - ddt_prod)
         else:
             sc_diff = cross.copy()
             sc_prod = np.zeros_like(state)
         delta = np.zeros_like(state)
+        delta_conv = np.zeros_like(state)
+
+        def convection_stage(f0, f1):
+            from oracle import convection as oconv
+            cflames, y_left, copts = convection
+            t0 = t if f0 == 0.0 else t + f0 * dt
+            t1 = t + f1 * dt
+            for f, g in enumerate(grids):
+                a, b = offs[f], offs[f + 1]
+                y0 = state[a:b].T.copy()
+                y1, _, _, _, _ = oconv.convection_flame(cflames[f], W, xs[a:b], y_left[f], drhodt[a:b],
+                                                        sc_conv[a:b].T.copy().reshape(-1), y0.reshape(-1), t0, t1,
+                                                        copts)
+                y1 = y1.reshape(y0.shape)
+                delta_conv[a:b] = delta_conv[a:b] + (y1 - y0).T
+                state[a:b] = y1.T
 
         def diffusion(f0, f1):
             t0 = t if f0 == 0.0 else t + f0 * dt
@@ -168,6 +202,8 @@ def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cro
                     state[a:b, v] = y1
 
         diffusion(0.0, 0.25)
+        if convection is not None:
+            convection_stage(0.0, 0.5)
         diffusion(0.25, 0.5)
         xD2 = state.copy()
         dtp = np.full(n_pts, (t + dt) - t)
@@ -175,9 +211,13 @@ def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cro
         state[:] = out
         xS = state.copy()
         diffusion(0.5, 0.75)
+        if convection is not None:
+            convection_stage(0.5, 1.0)
         diffusion(0.75, 1.0)
         ddt_diff = delta / dt - sc_diff
         ddt_prod = (xS - xD2) / dt - sc_prod
+        if convection is not None:
+            ddt_conv = delta_conv / dt - sc_conv
         correct_mass_fractions(state)
         t = t + dt
     return state, t, ddt_diff, ddt_prod, status

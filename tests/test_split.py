@@ -269,3 +269,71 @@ def test_load_state_keeps_time_and_split_history(gpu_lib, mech):
     (sa, ta), (sb, tb) = a.state(), b.state()
     assert ta == tb and np.array_equal(sa, sb)
     assert all(np.array_equal(x, y) for x, y in zip(a.derivatives(), b.derivatives()))
+
+
+def _convection_case(mech, n_flames=2, n_min=12, n_max=18, seed=5):
+    """A split case with the convection stage: the strained-flow velocity
+    U = a sqrt(rho_u / rho), inflow through the left boundary."""
+    from ember_gb300.convection import ConvectionFlame, mean_molecular_weight
+    from ember_gb300.split import mixture_properties
+    grids, state, B, D, rho_u, ju, jb = _case(mech, n_flames=n_flames, n_min=n_min, n_max=n_max, seed=seed)
+    state = state.copy()
+    rho, _ = mixture_properties(mech, state)
+    flames, y_left = [], []
+    p = 0
+    for f, g in enumerate(grids):
+        N = g.n_points
+        a = 200.0 + 300.0 * f
+        state[p:p + N, 0] = a * np.sqrt(rho_u[f] / rho[p:p + N])
+        y0 = state[p, 2:].copy()
+        flames.append(ConvectionFlame(n_points=N, left_bc=g.left_bc, right_bc=g.right_bc, alpha=g.alpha,
+                                      rv_zero=0.4 * rho_u[f], t_left=float(state[p, 1]),
+                                      w_left=float(mean_molecular_weight(y0, mech.mol_weight)[0]),
+                                      rhou=float(rho_u[f]), strain_initial=a, strain_final=a))
+        y_left.append(y0)
+        p += N
+    return grids, state, B, D, flames, np.array(y_left)
+
+
+def test_oracle_split_with_convection_runs_the_full_sequence(mech):
+    from oracle.chem import OracleMech
+    from ember_gb300.convection import ConvectionOptions
+    grids, state, B, D, flames, y_left = _convection_case(mech)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    om = OracleMech(mech)
+    conv = (flames, y_left, ConvectionOptions())
+    out, t, dd, dp, st = osplit.split_steps(om, grids, state, 0.0, B, D, 2e-6, 2, QSS, opts, convection=conv)
+    assert t == 4e-6 and np.isfinite(out).all()
+    np.testing.assert_allclose(out[:, 2:].sum(axis=1), 1.0, rtol=0, atol=1e-12)
+    ref, *_ = osplit.split_steps(om, grids, state, 0.0, B, D, 2e-6, 2, QSS, opts)
+    assert not np.array_equal(out[:, 0], ref[:, 0])      # the convection stage moved U
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("graph", [False, True])
+def test_split_with_convection_bitwise_vs_oracle(gpu_lib, mech, graph):
+    from oracle.chem import OracleMech
+    from ember_gb300.convection import ConvectionOptions
+    grids, state, B, D, flames, y_left = _convection_case(mech)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    dt = 2e-6
+    copts = ConvectionOptions()
+    gm, s = _gpu_solver(mech, grids, dt, QSS, opts, L.DIFFUSION_SERIAL)
+    s.set_state(1e-3, state)
+    s.set_transport(B, D)
+    s.set_convection(flames, y_left, copts)
+    s.step(3, graph=graph)
+    out, t = s.state()
+    dd, dp = s.derivatives()
+    ref, rt, rdd, rdp, rst = osplit.split_steps(OracleMech(mech), grids, state, 1e-3, B, D, dt, 3, QSS, opts,
+                                                convection=(flames, y_left, copts))
+    assert t == rt
+    assert np.array_equal(out, ref), np.abs(out - ref).max()
+    assert np.array_equal(dd, rdd) and np.array_equal(dp, rdp)
+    assert s.failures()[1] == 0
+    # detached: the step is D-S-D again
+    s.set_convection(None)
+    s.set_state(1e-3, state)
+    s.step(1)
+    ref2, *_ = osplit.split_steps(OracleMech(mech), grids, state, 1e-3, B, D, dt, 1, QSS, opts)
+    assert np.array_equal(s.state()[0], ref2)
