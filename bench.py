@@ -61,6 +61,8 @@ def parse_args():
     p.add_argument("--split-dt", type=float, default=0.0,
                    help="split workload: global time step (0: 2e-5 s; the GRI-sized BDF case needs 5e-6 s on the "
                         "seeded profiles)")
+    p.add_argument("--convection", action="store_true",
+                   help="split workload: the reference's full D C D S D C D step with the convection stage")
     p.add_argument("--source", default="qss", choices=["qss", "bdf"],
                    help="split workload: source-term integrator (the C5 sweep names BDF)")
     p.add_argument("--threads", type=int, default=0,
@@ -525,8 +527,39 @@ def split_inputs(rank: int, mech_size: str = "150"):
 
 
 def split_workload(args, mech) -> str:
-    return SPLIT_WORKLOAD.replace("150-species/1000-reaction", f"{mech.n_species}-species/{mech.n_reactions}-reaction") \
+    w = SPLIT_WORKLOAD.replace("150-species/1000-reaction", f"{mech.n_species}-species/{mech.n_reactions}-reaction") \
         .replace("QSS source", f"{args.source.upper()} source").replace("dt 2e-5 s", f"dt {args.split_dt or SPLIT_DT:g} s")
+    if args.convection:
+        w = w.replace("FlameSolver step without convection", "FlameSolver step with convection") \
+            .replace("balanced D-S-D split step", "balanced D-C-D-S-D-C-D split step (three-operator split constants)")
+        w += ("; convection: strain rates 100-2000 1/s log-spaced over the flames, U = a sqrt(rho_u/rho), inflow "
+              "through the left boundary")
+    return w
+
+
+def split_convection(mech, grids, state, rho_u):
+    """Convection parameters for the split workload: U = a sqrt(rho_u / rho)
+    (written into ``state``), strain rates log-spaced 100-2000 1/s, the
+    continuity integral from the left with inflow rho_u * 0.4 m/s."""
+    import numpy as np
+    from ember_gb300.convection import BC_CONTROL_VOLUME, ConvectionFlame, mean_molecular_weight
+    from ember_gb300.split import mixture_properties
+    rho, _ = mixture_properties(mech, state)
+    strains = np.geomspace(100.0, 2000.0, len(grids))
+    flames, y_left = [], []
+    p = 0
+    for f, g in enumerate(grids):
+        N = g.n_points
+        a = float(strains[f])
+        state[p:p + N, 0] = a * np.sqrt(rho_u[f] / rho[p:p + N])
+        y0 = state[p, 2:].copy()
+        flames.append(ConvectionFlame(n_points=N, left_bc=g.left_bc, right_bc=g.right_bc, alpha=g.alpha,
+                                      rv_zero=0.4 * float(rho_u[f]), t_left=float(state[p, 1]),
+                                      w_left=float(mean_molecular_weight(y0, mech.mol_weight)[0]),
+                                      rhou=float(rho_u[f]), strain_initial=a, strain_final=a))
+        y_left.append(y0)
+        p += N
+    return flames, np.array(y_left)
 
 
 def run_reference_split(args):
@@ -541,6 +574,11 @@ def run_reference_split(args):
     method = QSS if args.source == "qss" else BDF
     split_dt = args.split_dt or SPLIT_DT
     om = OracleMech(mech)
+    conv = None
+    if args.convection:
+        from ember_gb300.convection import ConvectionOptions
+        cflames, y_left = split_convection(mech, grids, state, rho_u)
+        conv = (cflames[:1], y_left[:1], ConvectionOptions())
     # bounded sample: the first flame, one split step per timed step
     g0 = grids[:1]
     n0 = g0[0].n_points
@@ -549,10 +587,10 @@ def run_reference_split(args):
     from ember_gb300.transport import synthetic_transport
     tr = (synthetic_transport(mech, seed=SPLIT_TRANSPORT_SEED), SPLIT_THRESHOLD, True)
     for _ in range(args.warmup):
-        osplit.split_steps(om, g0, st0, 0.0, B0, D0, split_dt, 1, method, opts, transport=tr)
+        osplit.split_steps(om, g0, st0, 0.0, B0, D0, split_dt, 1, method, opts, transport=tr, convection=conv)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        osplit.split_steps(om, g0, st0, 0.0, B0, D0, split_dt, 1, method, opts, transport=tr)
+        osplit.split_steps(om, g0, st0, 0.0, B0, D0, split_dt, 1, method, opts, transport=tr, convection=conv)
     per_flame = (time.perf_counter() - t0) / args.steps
     # scaled to the 32-flame batch by points
     ms = 1e3 * per_flame * len(state) / n0
@@ -563,7 +601,9 @@ def run_reference_split(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": split_workload(args, mech), "points": int(len(state))},
         "cpu_baseline": {"value": ms, "unit": "ms", "cores": threads, "kind": "port",
-                         "sample": f"flame 0 ({n0} points) per step, scaled to {len(state)} points"},
+                         "sample": f"flame 0 ({n0} points) per step, scaled to {len(state)} points"
+                                   + ("; flame 0 has the lowest strain rate, so its convection stages take the "
+                                      "fewest steps" if args.convection else "")},
         "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
     return 0
 
@@ -583,6 +623,11 @@ def run_ours_split(args):
     opts = source_options(args.kinetics, args.source)
     method = QSS if args.source == "qss" else BDF
     split_dt = args.split_dt or SPLIT_DT
+    cflames = y_left = copts = None
+    if args.convection:
+        from ember_gb300.convection import ConvectionOptions
+        cflames, y_left = split_convection(mech, grids, state, rho_u)
+        copts = ConvectionOptions()
     gm = GpuMechanism(mech)
     # QSS launch width tuned on the flames' start states over one step (before the solver takes it)
     width, tune_ms = autotune(gm, method, state, np.full(len(state), split_dt), opts)
@@ -598,6 +643,8 @@ def run_ours_split(args):
     solver.set_state(0.0, state)
     solver.set_transport(B, D)
     solver.set_transport_model(gtr, SPLIT_THRESHOLD, cross_terms=True)
+    if args.convection:
+        solver.set_convection(cflames, y_left, copts)
     solver.step(args.warmup, graph=True, stream=stream)
     torch.cuda.synchronize()
     sampler = ClockSampler(local)
@@ -648,6 +695,8 @@ def run_ours_split(args):
             one.set_state(0.0, state[a:b])
             one.set_transport(B[a * nv:b * nv], D[a * nv:b * nv])
             one.set_transport_model(gtr, SPLIT_THRESHOLD, cross_terms=True)
+            if args.convection:
+                one.set_convection(cflames[f:f + 1], y_left[f:f + 1], copts)
             one.step(args.warmup, graph=False, stream=stream)
             torch.cuda.synchronize()
             e0.record(stream)
@@ -677,7 +726,9 @@ def run_ours_split(args):
         # per step: transport, B/D, jCorr (flux, step size, 2 integrator kernels, failure count), 2 cross-term
         # kernels; begin, 2 x (transpose, 2 x (stage, failure count, delta), transpose back), stage dt,
         # 3 work-order kernels + QSS, failure count, end, mass fractions, clock
-        "gpu_launches": 35 * args.steps,
+        # with the convection stage: the density derivative, and per half 3 convection kernels, failure
+        # count and delta (the diffusion pairs become single stages around it, same launches)
+        "gpu_launches": (46 if args.convection else 35) * args.steps,
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak.value / 1e12, "unit": "TFLOP/s",
                      "frac": achieved / (peak.value / 1e12), "traffic": None,
                      "peak_source": "live DFMA throughput probe (ember_probe_fp64_rate)",
@@ -695,13 +746,16 @@ def run_ours_split(args):
         reps = 0
         while time.perf_counter() - t0 < args.cpu_seconds or reps == 0:
             osplit.split_steps(om, grids[:1], state[:n0], 0.0, B[:nv * n0], D[:nv * n0], split_dt, 1, method, opts,
-                               transport=(tdata, SPLIT_THRESHOLD, True))
+                               transport=(tdata, SPLIT_THRESHOLD, True),
+                               convection=(cflames[:1], y_left[:1], copts) if args.convection else None)
             reps += 1
         tcpu = (time.perf_counter() - t0) / reps
         threads = os.cpu_count() or 1
         line["cpu_baseline"] = {"value": 1e3 * tcpu * len(state) / n0, "unit": "ms", "cores": threads,
                                 "kind": "port",
-                                "sample": f"flame 0 ({n0} points) x{reps} on {threads} threads, scaled by points"}
+                                "sample": f"flame 0 ({n0} points) x{reps} on {threads} threads, scaled by points"
+                                          + ("; flame 0 has the lowest strain rate, so its convection stages take "
+                                             "the fewest steps" if args.convection else "")}
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:
