@@ -359,3 +359,26 @@ def test_gpu_convection_device_memory_and_overflow(gpu_lib, mech):
     np.testing.assert_array_equal(s3, rs)
     assert (s3 == -20).any()
     assert np.array_equal(st, ref)
+
+
+@pytest.mark.parametrize("balanced", [True, False])
+def test_density_derivative_matches_numpy_restatement(mech, balanced):
+    """prepareIntegrators' drho/dt (src/flameSolver.cpp:208-212) from the
+    four time derivatives and the state, as the split step computes it."""
+    rng = np.random.default_rng(31)
+    S, W = mech.n_species, mech.mol_weight
+    n_pts = 17
+    state = np.empty((n_pts, S + 2))
+    state[:, 0] = rng.uniform(0, 500, n_pts)
+    state[:, 1] = rng.uniform(300, 2500, n_pts)
+    Y = rng.uniform(0, 1, (n_pts, S))
+    Y[3, 2] = -1e-4                                     # clipped
+    state[:, 2:] = Y / Y.sum(axis=1, keepdims=True)
+    ddt = [rng.standard_normal((n_pts, S + 2)) * 1e3 for _ in range(4)]
+    got = oc.density_derivative(state, W, 101325.0, *ddt, balanced)
+    yc = np.maximum(state[:, 2:], 0.0)
+    wmx = 1.0 / ((yc / yc.sum(axis=1, keepdims=True)) / W[None, :]).sum(axis=1)
+    rho = 101325.0 * wmx / (GAS_CONSTANT * state[:, 1])
+    tot = ddt[0] + ddt[1] + ddt[2] + (ddt[3] if balanced else 0.0)
+    exp = -rho * (tot[:, 1] / state[:, 1] + (tot[:, 2:] / W[None, :]).sum(axis=1) * wmx)
+    np.testing.assert_allclose(got, exp, rtol=1e-12)
