@@ -124,6 +124,26 @@ def step_properties(omech, tdata, grids, state, pressure, threshold, mult, gdt, 
     return B, D, cross
 
 
+def split_constants(ddt_diff, ddt_prod, cross, balanced, ddt_conv=None):
+    """SplitSolver::step's split constants (src/splitSolver.cpp:38-46):
+    (sc_diff, sc_prod, sc_conv). Without convection (ddt_conv None) the
+    two-operator balanced constants of the device split step; with it the
+    reference's three-operator ones. sc_conv is None without convection."""
+    if ddt_conv is not None:
+        if balanced:
+            sc_diff = 0.25 * (((ddt_prod + ddt_conv) + cross) - 3.0 * ddt_diff)
+            sc_conv = 0.25 * (((ddt_prod + ddt_diff) + cross) - 3.0 * ddt_conv)
+            sc_prod = 0.5 * (((ddt_conv + ddt_diff) + cross) - ddt_prod)
+        else:
+            sc_diff = cross.copy()
+            sc_conv = np.zeros_like(cross)
+            sc_prod = np.zeros_like(cross)
+        return sc_diff, sc_prod, sc_conv
+    if balanced:
+        return 0.5 * ((ddt_prod + cross) - ddt_diff), 0.5 * ((ddt_diff + cross) - ddt_prod), None
+    return cross.copy(), np.zeros_like(cross), None
+
+
 def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cross=None, balanced=True,
                 mult=10.0, ddt=None, transport=None, convection=None):
     """n_steps split steps of a batch of flames. state: point-major [n_pts, n]
@@ -154,20 +174,8 @@ def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cro
         if convection is not None:
             from oracle import convection as oconv
             drhodt = oconv.density_derivative(state, W, opts.pressure, ddt_conv, ddt_diff, ddt_prod, cross, balanced)
-            if balanced:
-                sc_diff = 0.25 * (((ddt_prod + ddt_conv) + cross) - 3.0 * ddt_diff)
-                sc_conv = 0.25 * (((ddt_prod + ddt_diff) + cross) - 3.0 * ddt_conv)
-                sc_prod = 0.5 * (((ddt_conv + ddt_diff) + cross) - ddt_prod)
-            else:
-                sc_diff = cross.copy()
-                sc_conv = np.zeros_like(state)
-                sc_prod = np.zeros_like(state)
-        elif balanced:
-            sc_diff = 0.5 * ((ddt_prod + cross) - ddt_diff)
-            sc_prod = 0.5 * ((ddt_diff + cross) - ddt_prod)
-        else:
-            sc_diff = cross.copy()
-            sc_prod = np.zeros_like(state)
+        sc_diff, sc_prod, sc_conv = split_constants(ddt_diff, ddt_prod, cross, balanced,
+                                                    ddt_conv if convection is not None else None)
         delta = np.zeros_like(state)
         delta_conv = np.zeros_like(state)
 

@@ -337,3 +337,24 @@ def test_split_with_convection_bitwise_vs_oracle(gpu_lib, mech, graph):
     s.step(1)
     ref2, *_ = osplit.split_steps(OracleMech(mech), grids, state, 1e-3, B, D, dt, 1, QSS, opts)
     assert np.array_equal(s.state()[0], ref2)
+
+
+@pytest.mark.parametrize("with_convection", [False, True])
+def test_balanced_split_constants_add_up_to_the_cross_rate(with_convection):
+    """Balanced splitting redistributes the rates between the operators: the
+    split constants of all operators sum to the cross-term rate (two operators:
+    c_D + c_S = f_X; three: c_D + c_C + c_S = f_X), and each operator's
+    constant plus its own rate is the same total rate share."""
+    rng = np.random.default_rng(7)
+    shape = (13, 9)
+    fd, fs, fc, fx = (rng.standard_normal(shape) * 1e3 for _ in range(4))
+    sd, ss, sc = osplit.split_constants(fd, fs, fx, True, fc if with_convection else None)
+    total = sd + ss + (sc if with_convection else 0.0)
+    np.testing.assert_allclose(total, fx, rtol=0, atol=1e-9)
+    if with_convection:
+        rate = (fd + fs + fc + fx) / 4.0
+        np.testing.assert_allclose(sd + fd, rate, atol=1e-9)
+        np.testing.assert_allclose(sc + fc, rate, atol=1e-9)
+        np.testing.assert_allclose(ss + fs, 2.0 * rate, atol=1e-9)
+    sd, ss, sc = osplit.split_constants(fd, fs, fx, False, fc if with_convection else None)
+    np.testing.assert_array_equal(sd, fx)
