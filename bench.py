@@ -65,6 +65,8 @@ def parse_args():
                    help="split workload: the reference's full D C D S D C D step with the convection stage")
     p.add_argument("--source", default="qss", choices=["qss", "bdf"],
                    help="split workload: source-term integrator (the C5 sweep names BDF)")
+    p.add_argument("--no-secondary", action="store_true",
+                   help="qss workload: skip the secondary figures (BDF, diffusion, split steps, adjoint)")
     p.add_argument("--threads", type=int, default=0,
                    help="QSS threads per point; 0: ember_source_autotune picks it before the timed region")
     return p.parse_args()
@@ -158,7 +160,9 @@ def source_options(kinetics: str, method: str):
 
 
 def cpu_sample_rate(mech, state, dt, opts, method: int, target_s: float, threads: int):
-    """Points/s of the CPU oracle on a bounded sample of the workload."""
+    """Points/s of the CPU oracle on a bounded sample of the workload: the
+    first n states, n grown until one pass takes a quarter of target_s.
+    Returns (rate, n, seconds, (state_out, status, stats) of those n states)."""
     from oracle import chem
     om = chem.OracleMech(mech)
     n = 16
@@ -172,9 +176,61 @@ def cpu_sample_rate(mech, state, dt, opts, method: int, target_s: float, threads
         n = min(len(state), int(n * max(2.0, min(8.0, 0.3 * target_s / max(t, 1e-3)))))
     # one more pass at the final sample size for the figure
     t0 = time.perf_counter()
-    om.integrate(method, state[:n], dt[:n], opts, n_threads=threads)
+    res = om.integrate(method, state[:n], dt[:n], opts, n_threads=threads)
     t = time.perf_counter() - t0
-    return n / t, n, t
+    return n / t, n, t, res
+
+
+def source_parity(out, status, stats, ref_out, ref_status, ref_stats) -> dict:
+    """Agreement of a source-term batch with the oracle on the same states:
+    points equal bit for bit, the largest relative error of T and of the
+    mass fractions above 1e-14, the largest |sum Y - 1| of both results
+    (the integrators do not renormalise), and status / counter mismatches."""
+    import numpy as np
+    g, r = np.asarray(out, dtype=np.float64), np.asarray(ref_out, dtype=np.float64)
+    n = min(len(g), len(r))
+    g, r = g[:n], r[:n]
+    with np.errstate(divide="ignore", invalid="ignore"):
+        rel_t = np.abs(g[:, 1] - r[:, 1]) / np.abs(r[:, 1])
+        yr, yg = r[:, 2:], g[:, 2:]
+        big = np.abs(yr) > 1e-14
+        rel_y = np.where(big, np.abs(yg - yr) / np.where(big, np.abs(yr), 1.0), 0.0)
+    return {
+        "against": "oracle (FP64 CPU restatement of the reference path), same seeded states",
+        "n_compared": int(n),
+        "n_bitwise": int(np.all(g.view(np.int64) == r.view(np.int64), axis=1).sum()),
+        "max_rel_err_T": float(np.nanmax(rel_t)) if n else 0.0,
+        "max_rel_err_Y_above_1e-14": float(np.nanmax(rel_y)) if n else 0.0,
+        "max_abs_sumY_minus_1": float(np.abs(yg.sum(axis=1) - 1.0).max()) if n else 0.0,
+        "max_abs_sumY_minus_1_oracle": float(np.abs(yr.sum(axis=1) - 1.0).max()) if n else 0.0,
+        "status_mismatches": int((np.asarray(status)[:n] != np.asarray(ref_status)[:n]).sum()),
+        "counter_mismatches": int(np.any(np.asarray(stats)[:n] != np.asarray(ref_stats)[:n], axis=1).sum()),
+        "failed_points_oracle": int((np.asarray(ref_status)[:n] != 0).sum()),
+    }
+
+
+def field_parity(rows, ref_rows, tol=None) -> dict:
+    """Agreement of per-variable rows (list of 1-D arrays, GPU and oracle):
+    rows equal bit for bit and the largest error relative to the row's
+    largest |value| (the tolerance form of the tridiagonal path). With
+    tol = [(rtol, atol) per row], also the largest |error| / (rtol |ref| +
+    atol): the error in units of an integrator's own tolerance."""
+    import numpy as np
+    worst, same, worst_tol = 0.0, 0, 0.0
+    for r, (a, b) in enumerate(zip(rows, ref_rows)):
+        a, b = np.asarray(a), np.asarray(b)
+        same += int(np.array_equal(a, b))
+        scale = float(np.abs(b).max())
+        err = float(np.abs(a - b).max())
+        worst = max(worst, err / scale if scale > 0 else err)
+        if tol is not None:
+            rt, at = tol[r]
+            worst_tol = max(worst_tol, float((np.abs(a - b) / (rt * np.abs(b) + at)).max()))
+    out = {"against": "oracle (FP64 CPU restatement of the reference path), same seeded inputs",
+           "n_compared": len(rows), "n_bitwise": same, "max_err_rel_to_row_max": worst}
+    if tol is not None:
+        out["max_err_in_tolerance_units"] = worst_tol
+    return out
 
 
 # ------------------------------------------------------- reference arm --
@@ -190,7 +246,7 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     om = chem.OracleMech(mech)
     # size one step's sample to ~args.cpu_seconds/2 of host work
-    rate, n, t = cpu_sample_rate(mech, state, dt, opts, method, args.cpu_seconds / 2, threads)
+    rate, n, t, _ = cpu_sample_rate(mech, state, dt, opts, method, args.cpu_seconds / 2, threads)
     for _ in range(args.warmup):
         om.integrate(method, state[:n], dt[:n], opts, n_threads=threads)
     times = []
@@ -221,10 +277,6 @@ def run_ours(args):
     import numpy as np
     import torch
     ws, rank, local = dist_info()
-    torch.cuda.set_device(local)
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
     from ember_gb300 import _lib
     from ember_gb300 import roofline
     from ember_gb300.source import GpuMechanism, integrate_production_terms, autotune, tuning, QSS, BDF, STATS_WIDTH
@@ -358,16 +410,16 @@ def run_ours(args):
         "wall_s_timed_region": wall,
     }
     if rank == 0 and not args.no_cpu_baseline:
-        from oracle import chem
         threads = os.cpu_count() or 1
-        rate, n, t = cpu_sample_rate(mech, state, dt, opts, method, args.cpu_seconds, threads)
+        rate, n, t, ref = cpu_sample_rate(mech, state, dt, opts, method, args.cpu_seconds, threads)
         line["cpu_baseline"] = {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
                                 "sample": f"first {n} of the {args.points} states, {t:.1f} s on {threads} threads"}
-    if rank == 0:
-        print(json.dumps(line))
-    if ws > 1:
-        torch.distributed.destroy_process_group()
-    return 0
+        if n < args.points:  # the rest of the batch, for the parity figures only (not timed)
+            from oracle import chem
+            rest = chem.OracleMech(mech).integrate(method, state[n:], dt[n:], opts, n_threads=threads)
+            ref = tuple(np.concatenate([a, b]) for a, b in zip(ref, rest))
+        line["parity"] = source_parity(out_d.cpu().numpy(), status, stats, *ref)
+    return line
 
 
 # ------------------------------------------------- diffusion workload (C3) --
@@ -411,9 +463,6 @@ def run_ours_diffusion(args):
     import torch
     import ctypes as C
     ws, rank, local = dist_info()
-    torch.cuda.set_device(local)
-    if ws > 1:
-        torch.distributed.init_process_group("nccl")
     from ember_gb300 import _lib, roofline
     from ember_gb300.diffusion import integrate_diffusion_terms
     lib = _lib.lib()
@@ -491,17 +540,24 @@ def run_ours_diffusion(args):
         threads = os.cpu_count() or 1
         t0 = time.perf_counter()
         reps = 0
-        while time.perf_counter() - t0 < args.cpu_seconds:
-            oracle.diffusion_batch(grids, B, D, S, Y, 0.0, 1e-5, h=h, n_threads=threads)
+        ref = None
+        while time.perf_counter() - t0 < args.cpu_seconds or reps == 0:
+            ref = oracle.diffusion_batch(grids, B, D, S, Y, 0.0, 1e-5, h=h, n_threads=threads)
             reps += 1
         tcpu = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": n_vals * reps / tcpu, "unit": "values/s", "cores": threads, "kind": "port",
                                 "sample": f"the whole workload x{reps}, {tcpu:.1f} s on {threads} threads"}
-    if rank == 0:
-        print(json.dumps(line))
-    if ws > 1:
-        torch.distributed.destroy_process_group()
-    return 0
+        gy = Yd.cpu().numpy()
+        rows, ref_rows, p = [], [], 0
+        nv = Y.size // sum(g.n_points for g in grids)
+        for g in grids:
+            for _ in range(nv):
+                rows.append(gy[p:p + g.n_points])
+                ref_rows.append(ref[p:p + g.n_points])
+                p += g.n_points
+        line["parity"] = field_parity(rows, ref_rows)
+        line["parity"]["tolerance"] = "1e-12 of each system's largest |y| (warp-parallel Thomas vs the sequential order)"
+    return line
 
 
 # ------------------------------------------------ split-step workload (C5) --
@@ -613,9 +669,6 @@ def run_ours_split(args):
     import numpy as np
     import torch
     ws, rank, local = dist_info()
-    torch.cuda.set_device(local)
-    if ws > 1:
-        torch.distributed.init_process_group("nccl")
     from ember_gb300 import _lib, roofline
     from ember_gb300.source import GpuMechanism, QSS, BDF, autotune, tuning
     from ember_gb300.split import FlameBatchSplitSolver
@@ -756,11 +809,37 @@ def run_ours_split(args):
                                 "sample": f"flame 0 ({n0} points) x{reps} on {threads} threads, scaled by points"
                                           + ("; flame 0 has the lowest strain rate, so its convection stages take "
                                              "the fewest steps" if args.convection else "")}
-    if rank == 0:
-        print(json.dumps(line))
-    if ws > 1:
-        torch.distributed.destroy_process_group()
-    return 0
+        # parity: one step of the batched solver from the start state, against the oracle's step of
+        # the first, middle and last flame (flames are independent, so a subset steps as in the batch)
+        solver.set_state(0.0, state)
+        solver.step(1, graph=True, stream=stream)
+        torch.cuda.synchronize()
+        gpu_state, _ = solver.state()
+        sel = sorted({0, len(grids) // 2, len(grids) - 1})
+        off = np.cumsum([0] + [g.n_points for g in grids])
+        pick = lambda a, per: np.concatenate([a[off[f] * per:off[f + 1] * per] for f in sel])
+        ref_state, _, _, _, _ = osplit.split_steps(
+            om, [grids[f] for f in sel], pick(state.reshape(-1), nv).reshape(-1, nv), 0.0, pick(B, nv), pick(D, nv),
+            split_dt, 1, method, opts, transport=(tdata, SPLIT_THRESHOLD, True),
+            convection=([cflames[f] for f in sel], y_left[sel], copts) if args.convection else None)
+        rows, ref_rows, tol, p = [], [], [], 0
+        for f in sel:
+            a, b = off[f], off[f + 1]
+            for v in range(nv):
+                rows.append(gpu_state[a:b, v])
+                ref_rows.append(ref_state[p:p + (b - a), v])
+                atol = (opts.bdf_abstol_momentum, opts.bdf_abstol_energy)[v] if v < 2 else opts.bdf_abstol_species
+                tol.append((opts.bdf_reltol, atol))
+            p += b - a
+        line["parity"] = field_parity(rows, ref_rows, tol if method == BDF else None)
+        if method == BDF:
+            line["parity"]["tolerance"] = ("BDF: |error| / (reltol |y| + abstol) with the source options' CVODE "
+                                           "tolerances (reltol 1e-6; abstol 1e-7 U, 1e-8 T, 1e-13 Y)")
+        line["parity"].update({"flames_compared": sel, "steps": 1,
+                               "note": "warp-parallel diffusion (rounding-level differences from the sequential "
+                                       "order) feeding the source stage; the serial algorithm is bitwise "
+                                       "(tests/test_split.py)"})
+    return line
 
 
 # ---------------------------------------------------- adjoint workload (C4) --
@@ -814,9 +893,6 @@ def run_ours_adjoint(args):
     import numpy as np
     import torch
     ws, rank, local = dist_info()
-    torch.cuda.set_device(local)
-    if ws > 1:
-        torch.distributed.init_process_group("nccl")
     from ember_gb300.source import GpuMechanism, BDF
     from ember_gb300.split import FlameBatchSplitSolver
     mech, grids, state, B, D, rho_u, ju, jb = adjoint_inputs(rank)
@@ -881,11 +957,14 @@ def run_ours_adjoint(args):
         line["cpu_baseline"] = {"value": 2.0 * mech.n_reactions, "unit": "x", "cores": threads, "kind": "port",
                                 "sample": f"central differences on the CPU split step: 2 x {mech.n_reactions} "
                                           f"forward steps of {1e3 * tcpu:.0f} ms each ({threads} threads)"}
-    if rank == 0:
-        print(json.dumps(line))
-    if ws > 1:
-        torch.distributed.destroy_process_group()
-    return 0
+        ref_state, _, _, _, _ = osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, BDF, opts)
+        _, rhr, rcs = osplit.objectives(om, grids, ref_state, opts.pressure, opts.kinetics_model, rho_u, ju, jb)
+        line["parity"] = {"against": "oracle split step and objectives (FP64 CPU restatement), same start state",
+                          "heat_release_rel_err": float(abs(hr[0] - rhr[0]) / abs(rhr[0])),
+                          "consumption_speed_rel_err": float(abs(cs[0] - rcs[0]) / abs(rcs[0])),
+                          "note": "forward objectives of the taped step; the gradients are checked against "
+                                  "central differences of the oracle in tests/test_adjoint.py"}
+    return line
 
 
 # ------------------------------------------------------ transport workload --
@@ -958,9 +1037,6 @@ def run_ours_transport(args):
     import numpy as np
     import torch
     ws, rank, local = dist_info()
-    torch.cuda.set_device(local)
-    if ws > 1:
-        torch.distributed.init_process_group("nccl")
     from ember_gb300 import _lib, roofline
     from ember_gb300.source import GpuMechanism
     from ember_gb300.transport import GpuTransport
@@ -1031,11 +1107,7 @@ def run_ours_transport(args):
         rate, ns, t = _transport_cpu_rate(mech, td, state, args.cpu_seconds, threads)
         line["cpu_baseline"] = {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
                                 "sample": f"{ns} state evaluations, {t:.1f} s on {threads} threads"}
-    if rank == 0:
-        print(json.dumps(line))
-    if ws > 1:
-        torch.distributed.destroy_process_group()
-    return 0
+    return line
 
 # ------------------------------------------------------------ convection --
 
@@ -1112,9 +1184,6 @@ def run_ours_convection(args):
     import numpy as np
     import torch
     ws, rank, local = dist_info()
-    torch.cuda.set_device(local)
-    if ws > 1:
-        torch.distributed.init_process_group("nccl")
     from ember_gb300 import _lib, roofline
     from ember_gb300.convection import ConvectionOptions, integrate_convection_terms
     mech, b = convection_inputs(rank)
@@ -1199,28 +1268,71 @@ def run_ours_convection(args):
         rate, nf, t = _convection_cpu_rate(mech, b, args.cpu_seconds, threads)
         line["cpu_baseline"] = {"value": rate, "unit": "points/s", "cores": threads, "kind": "port",
                                 "sample": f"first {nf} flames, one flame per thread, {t:.1f} s on {threads} threads"}
-    if rank == 0:
-        print(json.dumps(line))
-    if ws > 1:
-        torch.distributed.destroy_process_group()
-    return 0
+    return line
+
+
+# ------------------------------------------------------ secondary figures --
+
+# The other parts of the headline metric ("ms per split step; adjoint/forward
+# cost") and the other configurations, measured in the same default run beside
+# the headline: (workload overrides, timed steps, CPU-sample seconds).
+SECONDARY = (
+    ("bdf", {"workload": "bdf", "mech": "150"}, 5, 4.0),
+    ("diffusion", {"workload": "diffusion"}, 10, 2.0),
+    ("split_bdf53", {"workload": "split", "mech": "53", "source": "bdf", "split_dt": 5e-6}, 3, 4.0),
+    ("split_qss150", {"workload": "split", "mech": "150", "source": "qss", "split_dt": 0.0}, 5, 4.0),
+    ("adjoint", {"workload": "adjoint"}, 3, 1.0),
+)
+
+RUNNERS = {}
+
+
+def run_secondary(args) -> dict:
+    """Each secondary workload at its own configuration, with W >= 3 warm-up
+    steps and a few timed steps; every entry carries its own roofline,
+    cpu_baseline, parity and clocks."""
+    out = {}
+    for name, over, steps, cpu_s in SECONDARY:
+        a = argparse.Namespace(**vars(args))
+        for k, v in over.items():
+            setattr(a, k, v)
+        a.steps = min(args.steps, steps)
+        a.warmup = max(3, min(args.warmup, 3))
+        a.cpu_seconds = min(args.cpu_seconds, cpu_s)
+        a.threads = 0
+        a.convection = False
+        a.no_plain = False
+        t0 = time.perf_counter()
+        line = RUNNERS[a.workload](a)
+        line["wall_s"] = round(time.perf_counter() - t0, 2)
+        out[name] = line
+    return out
 
 
 def main():
     args = parse_args()
-    if args.workload == "transport":
-        return run_reference_transport(args) if args.impl == "reference" else run_ours_transport(args)
-    if args.workload == "convection":
-        return run_reference_convection(args) if args.impl == "reference" else run_ours_convection(args)
-    if args.workload == "diffusion":
-        return run_reference_diffusion(args) if args.impl == "reference" else run_ours_diffusion(args)
-    if args.workload == "split":
-        return run_reference_split(args) if args.impl == "reference" else run_ours_split(args)
-    if args.workload == "adjoint":
-        return run_reference_adjoint(args) if args.impl == "reference" else run_ours_adjoint(args)
     if args.impl == "reference":
-        return run_reference(args)
-    return run_ours(args)
+        ref = {"transport": run_reference_transport, "convection": run_reference_convection,
+               "diffusion": run_reference_diffusion, "split": run_reference_split, "adjoint": run_reference_adjoint}
+        return ref.get(args.workload, run_reference)(args)
+    import torch
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        torch.distributed.init_process_group("nccl")
+    RUNNERS.update({"qss": run_ours, "bdf": run_ours, "transport": run_ours_transport,
+                    "convection": run_ours_convection, "diffusion": run_ours_diffusion, "split": run_ours_split,
+                    "adjoint": run_ours_adjoint})
+    try:
+        line = RUNNERS[args.workload](args)
+        if args.workload == "qss" and not args.no_secondary:
+            line["secondary"] = run_secondary(args)
+        if rank == 0:
+            print(json.dumps(line))
+    finally:
+        if ws > 1:
+            torch.distributed.destroy_process_group()
+    return 0
 
 
 if __name__ == "__main__":
