@@ -977,7 +977,7 @@ template <int NT>
 static int bdf_config(const MechView& m, const SourceArgs& a, size_t* per_out, int* blocks_out) {
     const size_t per = bdf_layout(m, a).smem_bytes;
     EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the BDF shared-memory work area (%zu B)", per);
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_bdf<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
+    EMBER_TRY(raise_dynamic_smem(reinterpret_cast<const void*>(k_source_bdf<NT>), per));
     int dev = 0, sms = 0, per_sm = 0;
     EMBER_CUDA_TRY(cudaGetDevice(&dev));
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -1208,8 +1208,7 @@ static int launch_bdf_adjoint_nt(const MechView& m, const SourceArgs& a, int* co
     size_t per = 0;
     int blocks = 0;
     EMBER_TRY(bdf_config<NT>(m, a, &per, &blocks));
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_bdf_adjoint<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        int(per)));
+    EMBER_TRY(raise_dynamic_smem(reinterpret_cast<const void*>(k_source_bdf_adjoint<NT>), per));
     double *kcache = nullptr, *jm = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));
     const BdfLayout lay = bdf_layout(m, a);
@@ -1332,7 +1331,7 @@ static int launch_objective_vjp_nt(const MechView& m, const SourceArgs& a, int n
     SourceArgs b = a;
     b.n = n_pts;
     EMBER_TRY(bdf_config<NT>(m, b, &per, &blocks));
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_objective_vjp<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
+    EMBER_TRY(raise_dynamic_smem(reinterpret_cast<const void*>(k_objective_vjp<NT>), per));
     double *kcache = nullptr, *jm = nullptr;
     int* counter = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));

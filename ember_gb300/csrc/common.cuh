@@ -45,13 +45,19 @@ const std::string& last_error();
 
 inline cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
 
-// Make sure the calling thread has a usable device; keeps the default
-// memory pool from returning freed blocks to the driver so that the
-// stream-ordered scratch allocations below are cheap after the first call.
+// Make sure the calling thread has a usable device.
 int ensure_device();
 
-// Stream-ordered device scratch (cudaMallocAsync / cudaFreeAsync on the
-// call's stream). Freed when the object goes out of scope; the free is
+// The library's own stream-ordered memory pool of the current device (freed
+// blocks are kept for reuse; the default pool is not touched).
+int scratch_pool(cudaMemPool_t* pool);
+
+// Raise (never lower) a kernel's dynamic shared memory limit on the current
+// device to `bytes`.
+int raise_dynamic_smem(const void* func, size_t bytes);
+
+// Stream-ordered device scratch (allocated from the library's pool with
+// cudaMallocFromPoolAsync, freed with cudaFreeAsync on the call's stream). Freed when the object goes out of scope; the free is
 // ordered after every kernel already queued on that stream.
 //
 // Arena mode (the second constructor): allocations are carved in order out of
@@ -87,9 +93,11 @@ public:
             return EMBER_OK;
         }
         void* q = nullptr;
-        cudaError_t e = cudaMallocAsync(&q, bytes, stream_);
+        cudaMemPool_t pool = nullptr;
+        EMBER_TRY(scratch_pool(&pool));
+        cudaError_t e = cudaMallocFromPoolAsync(&q, bytes, pool, stream_);
         if (e != cudaSuccess) {
-            set_error("cudaMallocAsync(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+            set_error("cudaMallocFromPoolAsync(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
             return (e == cudaErrorMemoryAllocation) ? EMBER_ENOMEM : EMBER_ECUDA;
         }
         ptrs_.push_back(q);

@@ -1118,7 +1118,7 @@ int conv_plan_alloc(ConvPlan& p, Scratch& sc, bool with_stats, cudaStream_t st) 
     a.hist_v = hv;
     a.n_hist = nh;
     const size_t utw_smem = size_t(3) * p.max_points * sizeof(double);
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_conv_utw, cudaFuncAttributeMaxDynamicSharedMemorySize, int(utw_smem)));
+    EMBER_TRY(raise_dynamic_smem(reinterpret_cast<const void*>(k_conv_utw), utw_smem));
     return EMBER_OK;
 }
 

@@ -570,7 +570,7 @@ extern "C" int ember_gas_eval(ember_mech m, int n, double pressure, int model, i
     double* kcache = nullptr;
     EMBER_TRY(sc.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m->view)));
 #define EMBER_GAS_EVAL(NTV)                                                                                  \
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_gas_eval<NTV>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per))); \
+    EMBER_TRY(raise_dynamic_smem(reinterpret_cast<const void*>(k_gas_eval<NTV>), per)); \
     k_gas_eval<NTV><<<blocks, NTV, per, st>>>(v, n, pressure, model, mode, dT, dY, kcache, c1, c2, c3, c4, c5, c6)
     switch (NTh) {
         case 64: EMBER_GAS_EVAL(64); break;
@@ -702,7 +702,7 @@ template <int NT>
 static int qss_config(const MechView& m, const SourceArgs& a, size_t* per_out, int* blocks_out) {
     const size_t per = qss_smem_doubles(m, a.qss_stability_check != 0) * sizeof(double);
     EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the QSS shared-memory work area (%zu B)", per);
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_qss<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(per)));
+    EMBER_TRY(raise_dynamic_smem(reinterpret_cast<const void*>(k_source_qss<NT>), per));
     EMBER_CUDA_TRY(cudaFuncSetAttribute(k_source_qss<NT>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                         int(cudaSharedmemCarveoutMaxShared)));
     int dev = 0, sms = 0, per_sm = 0;

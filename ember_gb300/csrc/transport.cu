@@ -210,7 +210,7 @@ int launch_transport_nt(const MechView& m, const TransportView& tv, int n, doubl
                         cudaStream_t st) {
     const size_t smem = (size_t(8) * m.S + kRedDoubles) * sizeof(double) + sizeof(int) * m.S;
     EMBER_CHECK_ARG(smem <= 227 * 1024, "too many species for the transport work area");
-    EMBER_CUDA_TRY(cudaFuncSetAttribute(k_transport<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    EMBER_TRY(raise_dynamic_smem(reinterpret_cast<const void*>(k_transport<NT>), smem));
     int dev = 0, sms = 0, per_sm = 0;
     EMBER_CUDA_TRY(cudaGetDevice(&dev));
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
