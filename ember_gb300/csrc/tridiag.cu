@@ -620,6 +620,36 @@ int noalloc_scratch(void** out) {
     return EMBER_OK;
 }
 
+// The per-system descriptors are built on the device from per-flame records
+// passed by value as kernel parameters (copied with the launch), so the call
+// needs neither a host buffer nor a host-to-device copy.
+constexpr int kNoAllocFlamesPerLaunch = 256;
+
+struct NoAllocFlame {
+    int n, left_bc, right_bc, alpha;
+    int64_t grid_off, val_off;
+};
+
+struct NoAllocFlames {
+    int first, count, n_vars;
+    NoAllocFlame f[kNoAllocFlamesPerLaunch];
+};
+
+__global__ void k_noalloc_info(const __grid_constant__ NoAllocFlames c, ember::DiffSysInfo* __restrict__ info) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= c.count * c.n_vars) return;
+    const int fl = t / c.n_vars, v = t - fl * c.n_vars;
+    const NoAllocFlame& g = c.f[fl];
+    ember::DiffSysInfo s;
+    s.n = g.n;
+    s.left_bc = g.left_bc;
+    s.right_bc = g.right_bc;
+    s.alpha = g.alpha;
+    s.grid_off = g.grid_off;
+    s.off = g.val_off + int64_t(v) * g.n;
+    info[int64_t(c.first + fl) * c.n_vars + v] = s;
+}
+
 }  // namespace
 
 extern "C" int ember_diffusion_integrate_noalloc(int n_flames, const ember_diffusion_grid* grids, int n_vars,
@@ -634,7 +664,6 @@ extern "C" int ember_diffusion_integrate_noalloc(int n_flames, const ember_diffu
                     "ember_diffusion_integrate_noalloc: %lld systems exceed the maximum of %d "
                     "(use ember_diffusion_integrate)",
                     (long long)n_sys, EMBER_NOALLOC_MAX_SYSTEMS);
-    std::vector<DiffSysInfo> info(n_sys);
     int64_t n_pts = 0, n_vals = 0;
     int nmax = 0;
     for (int f = 0; f < n_flames; ++f) {
@@ -645,15 +674,6 @@ extern "C" int ember_diffusion_integrate_noalloc(int n_flames, const ember_diffu
                             g.right_bc == EMBER_BC_FLOATING,
                         "flame %d: bad right_bc %d", f, g.right_bc);
         EMBER_CHECK_ARG(g.alpha >= 0, "flame %d: bad alpha %d", f, g.alpha);
-        for (int v = 0; v < n_vars; ++v) {
-            DiffSysInfo& s = info[int64_t(f) * n_vars + v];
-            s.n = g.n_points;
-            s.left_bc = g.left_bc;
-            s.right_bc = g.right_bc;
-            s.alpha = g.alpha;
-            s.grid_off = n_pts;
-            s.off = n_vals + int64_t(v) * g.n_points;
-        }
         n_pts += g.n_points;
         n_vals += int64_t(n_vars) * g.n_points;
         nmax = std::max(nmax, g.n_points);
@@ -673,7 +693,23 @@ extern "C" int ember_diffusion_integrate_noalloc(int n_flames, const ember_diffu
     DiffSysInfo* d_info = reinterpret_cast<DiffSysInfo*>(p + kNoAllocWorkBytes);
     int* d_status = reinterpret_cast<int*>(p + kNoAllocWorkBytes + kNoAllocInfoBytes);
     cudaStream_t st = as_stream(stream);
-    EMBER_CUDA_TRY(cudaMemcpyAsync(d_info, info.data(), sizeof(DiffSysInfo) * n_sys, cudaMemcpyHostToDevice, st));
+    {
+        NoAllocFlames c;
+        int64_t pts = 0, vals = 0;
+        for (int f0 = 0; f0 < n_flames; f0 += kNoAllocFlamesPerLaunch) {
+            c.first = f0;
+            c.count = std::min(kNoAllocFlamesPerLaunch, n_flames - f0);
+            c.n_vars = n_vars;
+            for (int i = 0; i < c.count; ++i) {
+                const ember_diffusion_grid& g = grids[f0 + i];
+                c.f[i] = NoAllocFlame{g.n_points, g.left_bc, g.right_bc, g.alpha, pts, vals};
+                pts += g.n_points;
+                vals += int64_t(n_vars) * g.n_points;
+            }
+            k_noalloc_info<<<blocks_for(int64_t(c.count) * n_vars, 128), 128, 0, st>>>(c, d_info);
+            EMBER_CUDA_TRY(cudaGetLastError());
+        }
+    }
 
     DiffusionView dv;
     dv.n_systems = static_cast<int>(n_sys);

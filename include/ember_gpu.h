@@ -205,9 +205,10 @@ int ember_diffusion_adjoint(int n_flames, const ember_diffusion_grid* grids, int
  * sized for EMBER_NOALLOC_MAX_VALUES values (n_vars x total points) and
  * EMBER_NOALLOC_MAX_SYSTEMS (flame, variable) systems, about 28.3 MiB that
  * every GPU which loads the library keeps until the process exits. Larger
- * problems are rejected with EMBER_EINVAL. The call allocates nothing: no
- * cudaMalloc, cudaFree or allocating library routine.
- * The first call on a device looks up the array's device address
+ * problems are rejected with EMBER_EINVAL. The call makes no device
+ * allocation (no cudaMalloc, cudaFree or allocating library routine) and no
+ * host heap allocation: the per-system descriptors are built on the device
+ * from kernel parameters. The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress); make that first call before any stream capture.
  * Every call uses the same array: calls whose kernels can overlap on the GPU
  * (other streams, other host threads) race and corrupt each other's results;

@@ -68,6 +68,35 @@ def test_noalloc_matches_allocating_entry_point_twice():
         np.testing.assert_allclose(out, ref, rtol=1e-12, atol=0.0, err_msg=f"call {call + 1}")
 
 
+def test_noalloc_call_leaves_device_memory_unchanged():
+    # a warm call (the array's address already looked up, the kernels loaded)
+    # changes neither the device's free memory nor torch's pools
+    torch = pytest.importorskip("torch")
+    lib = L.lib()
+    grids, n_vars, x, B, D, S, Y = _case(303)
+    dev = lambda a: torch.as_tensor(a, device="cuda")
+    xd, Bd, Dd, Sd, Yd = dev(x), dev(B), dev(D), dev(S), dev(Y.copy())
+    status = torch.zeros(len(grids) * n_vars, dtype=torch.int32, device="cuda")
+    garr = (L.DiffusionGrid * len(grids))(*grids)
+    opts = L.DiffusionOptions(0.0, 1e-5, 10.0, 2e-5, None, None, None, L.DIFFUSION_SERIAL)
+
+    def call():
+        rc = lib.ember_diffusion_integrate_noalloc(len(grids), garr, n_vars, xd.data_ptr(), Bd.data_ptr(),
+                                                   Dd.data_ptr(), Sd.data_ptr(), Yd.data_ptr(), C.byref(opts),
+                                                   status.data_ptr(), None)
+        torch.cuda.synchronize()
+        assert rc == L.OK, L.last_error()
+
+    call()
+    free0, _ = torch.cuda.mem_get_info()
+    reserved0 = torch.cuda.memory_reserved()
+    call()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_reserved() == reserved0
+    assert (status.cpu().numpy() == 0).all()
+
+
 def test_noalloc_rejects_oversized_problem():
     lib = L.lib()
     n_vars = 8
