@@ -20,7 +20,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Translation units whose arithmetic must match the CPU oracle operation by
 # operation: no automatic multiply-add contraction (explicit fma() only).
 FILE_FLAGS = {"source.cu": ["--fmad=false"], "bdf.cu": ["--fmad=false"], "split.cu": ["--fmad=false"],
-              "transport.cu": ["--fmad=false"], "convection.cu": ["--fmad=false"]}
+              "transport.cu": ["--fmad=false"], "convection.cu": ["--fmad=false"],
+              # host code: the same rounding on x86-64 and aarch64 (no contraction into FMA)
+              "grid.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "include")]
 
@@ -34,6 +36,7 @@ def nvcc() -> str:
 
 def _deps() -> list[str]:
     return sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cuh")) +
+                  glob.glob(os.path.join(CSRC, "*.cpp")) +
                   glob.glob(os.path.join(ROOT, "include", "*.h")))
 
 
@@ -51,10 +54,10 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     flags = NVCC_FLAGS + ARCH + (extra_flags or [])
-    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
+    sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cpp")))
 
     def compile_one(src: str) -> str:
-        obj = os.path.join(BUILD, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(BUILD, os.path.splitext(os.path.basename(src))[0] + ".o")
         cmd = [cc, "-c", src, "-o", obj] + flags + FILE_FLAGS.get(os.path.basename(src), [])
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:

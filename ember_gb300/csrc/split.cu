@@ -609,6 +609,9 @@ struct ember_split_s {
     int tr_cross = 0;
     void* pblob = nullptr;
     double *p_rho = nullptr, *p_cp = nullptr, *p_lam = nullptr, *p_mu = nullptr, *p_rhoD = nullptr, *p_cpS = nullptr;
+    // true once a step has run with the transport model attached: p_cp then holds the c_p of the
+    // last step's property update, which the consumption speed divides by (as FlameSolver's cp)
+    bool props_valid = false;
     double *jcorr = nullptr, *jB = nullptr, *jD = nullptr, *jsc = nullptr, *jh = nullptr, *sumcpj = nullptr;
     double* jwork = nullptr;
     DiffSysInfo* jinfo = nullptr;
@@ -1044,6 +1047,7 @@ extern "C" int ember_split_set_state(ember_split h, double t, const double* stat
     EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_prod, 0, sizeof(double) * h->n_vals, st));
     if (h->conv) EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_conv, 0, sizeof(double) * h->n_vals, st));
     EMBER_CUDA_TRY(cudaMemsetAsync(h->fails, 0, 2 * sizeof(unsigned long long), st));
+    h->props_valid = false;
     // the host value of t must outlive the copy
     EMBER_CUDA_TRY(cudaStreamSynchronize(st));
     return EMBER_OK;
@@ -1092,6 +1096,11 @@ extern "C" int ember_split_set_convection(ember_split h, const ember_convection_
         EMBER_CHECK_ARG(flames[f].n_points == h->grids[f].n_points, "flame %d: n_points %d differs from the grid's %d",
                         f, flames[f].n_points, h->grids[f].n_points);
         EMBER_CHECK_ARG(flames[f].alpha == h->grids[f].alpha, "flame %d: alpha differs from the grid's", f);
+        // one gas pressure for the whole step, as the reference's single CanteraGas: the density
+        // derivative and the transport model use the source options' pressure
+        EMBER_CHECK_ARG(flames[f].pressure == h->opt.source.pressure,
+                        "flame %d: pressure %g differs from the split options' %g", f, flames[f].pressure,
+                        h->opt.source.pressure);
     }
     ConvPlan p;
     EMBER_TRY(conv_plan_layout(p, h->n_flames, flames, S, opts));
@@ -1145,6 +1154,7 @@ extern "C" int ember_split_set_transport_model(ember_split h, ember_transport tr
     cudaFree(h->pblob);
     h->pblob = nullptr;
     h->tr = nullptr;
+    h->props_valid = false;
     if (!tr) return EMBER_OK;
     const int64_t np = h->n_pts;
     const int S = h->n_vars - 2, nf = h->n_flames;
@@ -1224,6 +1234,7 @@ extern "C" int ember_split_step(ember_split h, int n_steps, int use_graph, void*
     EMBER_TRY(check_split(h));
     EMBER_CHECK_ARG(n_steps >= 0, "n_steps must be >= 0");
     cudaStream_t st = as_stream(stream);
+    if (h->tr && n_steps > 0) h->props_valid = true;
     if (!use_graph) {
         for (int k = 0; k < n_steps; ++k) EMBER_TRY(enqueue_step(h, st));
         return EMBER_OK;
@@ -1262,6 +1273,21 @@ extern "C" int ember_split_get_derivatives(ember_split h, double* ddt_diff, doub
     const cudaMemcpyKind kind = mem == EMBER_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     if (ddt_diff) EMBER_CUDA_TRY(cudaMemcpyAsync(ddt_diff, h->ddt_diff, sizeof(double) * h->n_vals, kind, st));
     if (ddt_prod) EMBER_CUDA_TRY(cudaMemcpyAsync(ddt_prod, h->ddt_prod, sizeof(double) * h->n_vals, kind, st));
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_split_set_derivatives(ember_split h, const double* ddt_diff, const double* ddt_prod,
+                                           const double* ddt_conv, int mem, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(ddt_diff && ddt_prod, "null ddt_diff or ddt_prod");
+    EMBER_CHECK_ARG(!ddt_conv || h->conv, "ddt_conv given but no convection stage is attached");
+    cudaStream_t st = as_stream(stream);
+    EMBER_TRY(copy_to_device(h->ddt_diff, ddt_diff, size_t(h->n_vals), mem, st));
+    EMBER_TRY(copy_to_device(h->ddt_prod, ddt_prod, size_t(h->n_vals), mem, st));
+    if (h->conv) {
+        if (ddt_conv) EMBER_TRY(copy_to_device(h->ddt_conv, ddt_conv, size_t(h->n_vals), mem, st));
+        else EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_conv, 0, sizeof(double) * h->n_vals, st));
+    }
     return finish_call(mem, st);
 }
 
@@ -1325,7 +1351,11 @@ extern "C" int ember_split_objectives(ember_split h, const double* rho_u, const 
     EMBER_TRY(ember_gas_eval(h->mech, static_cast<int>(h->n_pts), h->opt.source.pressure,
                              h->opt.source.kinetics_model, EMBER_STATE_NORMALIZED, T, Y, nullptr, nullptr, net, hk,
                              cp, nullptr, EMBER_MEM_DEVICE, stream));
-    k_qdot<<<grid_for(h->n_pts, 128), 128, 0, st>>>(h->n_pts, S, net, hk, cp, q, qcp);
+    // qdot of the current state; q/cp with the c_p of the last property update when the transport
+    // model ran one (FlameSolver::getConsumptionSpeed divides by the cp of updateChemicalProperties,
+    // src/flameSolver.cpp:956-961), else with the current state's
+    const double* cp_sc = (h->tr && h->props_valid) ? h->p_cp : cp;
+    k_qdot<<<grid_for(h->n_pts, 128), 128, 0, st>>>(h->n_pts, S, net, hk, cp_sc, q, qcp);
     if (hr || cs)
         k_flame_objectives<<<blocks_for(h->n_flames, 64), 64, 0, st>>>(h->n_flames, h->flame_npts, h->flame_goff, h->x,
                                                                         q, qcp, T, d_rho, d_ju, d_jb, work, hr, cs);

@@ -38,6 +38,7 @@ def _declare(lib):
         "ember_split_step": (C.c_int, [vp, C.c_int, C.c_int, vp]),
         "ember_split_get_state": (C.c_int, [vp, vp, vp, C.c_int, vp]),
         "ember_split_get_derivatives": (C.c_int, [vp, vp, vp, C.c_int, vp]),
+        "ember_split_set_derivatives": (C.c_int, [vp, vp, vp, vp, C.c_int, vp]),
         "ember_split_source_status": (C.c_int, [vp, vp, vp, C.c_int, vp]),
         "ember_split_failures": (C.c_int, [vp, vp, vp, vp]),
         "ember_split_objectives": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, C.c_int, vp]),
@@ -179,6 +180,16 @@ class FlameBatchSplitSolver:
                 "get_derivatives")
         return dd, dp
 
+    def set_derivatives(self, ddt_diff, ddt_prod, ddt_conv=None):
+        """ember_split_set_derivatives: the time derivatives behind the next
+        step's split constants (e.g. interpolated onto a new grid)."""
+        shape = (self.n_points, self.n_vars)
+        dd, mem = self._arr(ddt_diff, shape)
+        dp, _ = self._arr(ddt_prod, shape)
+        dc = self._arr(ddt_conv, shape)[0] if ddt_conv is not None else None
+        L.check(_lib().ember_split_set_derivatives(self._h, L.ptr(dd), L.ptr(dp), L.ptr(dc), mem, None),
+                "ember_split_set_derivatives")
+
     def source_status(self):
         st = np.empty(self.n_points, dtype=np.int32)
         stats = np.empty((self.n_points, STATS_WIDTH), dtype=np.int32)
@@ -191,40 +202,71 @@ class FlameBatchSplitSolver:
         L.check(_lib().ember_split_failures(self._h, C.addressof(a), C.addressof(b), None), "failures")
         return a.value, b.value
 
-    def objectives(self, rho_u=None, ju=None, jb=None):
+    def objectives(self, rho_u=None, ju=None, jb=None, device=None):
         """(qdot [n_points], heat release rate [n_flames], consumption speed
-        [n_flames] or None) of the current state."""
+        [n_flames] or None) of the current state. With ``device`` (a torch
+        device) the inputs may be tensors there and the outputs are tensors
+        on it, with no host round trip."""
         nf = len(self.grids)
-        q = np.empty(self.n_points)
-        hr = np.empty(nf)
-        cs = np.empty(nf) if rho_u is not None else None
-        r = np.ascontiguousarray(rho_u, dtype=np.float64) if rho_u is not None else None
-        a = np.ascontiguousarray(ju, dtype=np.int32) if ju is not None else None
-        b = np.ascontiguousarray(jb, dtype=np.int32) if jb is not None else None
-        L.check(_lib().ember_split_objectives(self._h, L.ptr(r), L.ptr(a), L.ptr(b), q.ctypes.data, hr.ctypes.data,
-                                              L.ptr(cs), L.MEM_HOST, None), "objectives")
+        if device is not None:
+            import torch
+            f64 = lambda v: torch.as_tensor(v, dtype=torch.float64, device=device).contiguous() \
+                if v is not None else None
+            i32 = lambda v: torch.as_tensor(v, dtype=torch.int32, device=device).contiguous() \
+                if v is not None else None
+            q = torch.empty(self.n_points, dtype=torch.float64, device=device)
+            hr = torch.empty(nf, dtype=torch.float64, device=device)
+            cs = torch.empty(nf, dtype=torch.float64, device=device) if rho_u is not None else None
+            r, a, b, mem = f64(rho_u), i32(ju), i32(jb), L.MEM_DEVICE
+        else:
+            q = np.empty(self.n_points)
+            hr = np.empty(nf)
+            cs = np.empty(nf) if rho_u is not None else None
+            r = np.ascontiguousarray(rho_u, dtype=np.float64) if rho_u is not None else None
+            a = np.ascontiguousarray(ju, dtype=np.int32) if ju is not None else None
+            b = np.ascontiguousarray(jb, dtype=np.int32) if jb is not None else None
+            mem = L.MEM_HOST
+        L.check(_lib().ember_split_objectives(self._h, L.ptr(r), L.ptr(a), L.ptr(b), L.ptr(q), L.ptr(hr),
+                                              L.ptr(cs), mem, None), "objectives")
         return q, hr, cs
 
     def adjoint(self, w_heat_release=None, w_consumption_speed=None, rho_u=None, ju=None, jb=None,
-                tape_cap: int = 0):
+                tape_cap: int = 0, device=None):
         """One split step from the current state and the gradient of
         J = sum_f w_heat_release[f] Q_f + w_consumption_speed[f] S_c,f at its end
         with respect to the state at its start and ln(multiplier) of every
         reaction (``ember_split_adjoint``; BDF source). Returns (Q, S_c or None,
-        d J / d state [n_points, S+2], d J / d ln multiplier [R])."""
+        d J / d state [n_points, S+2], d J / d ln multiplier [R]); with
+        ``device`` (a torch device) as tensors there, computed without a host
+        round trip."""
         nf = len(self.grids)
-        f64 = lambda v: np.ascontiguousarray(v, dtype=np.float64) if v is not None else None
-        i32 = lambda v: np.ascontiguousarray(v, dtype=np.int32) if v is not None else None
-        wq, ws, r = f64(w_heat_release), f64(w_consumption_speed), f64(rho_u)
-        a, b = i32(ju), i32(jb)
-        hr = np.empty(nf)
-        cs = np.empty(nf) if ws is not None else None
-        sbar = np.empty((self.n_points, self.n_vars))
-        lbar = np.empty(max(self.gmech.mech.n_reactions, 1))
+        R = self.gmech.mech.n_reactions
+        if device is not None:
+            import torch
+            f64 = lambda v: torch.as_tensor(v, dtype=torch.float64, device=device).contiguous() \
+                if v is not None else None
+            i32 = lambda v: torch.as_tensor(v, dtype=torch.int32, device=device).contiguous() \
+                if v is not None else None
+            wq, ws, r, a, b = f64(w_heat_release), f64(w_consumption_speed), f64(rho_u), i32(ju), i32(jb)
+            hr = torch.empty(nf, dtype=torch.float64, device=device)
+            cs = torch.empty(nf, dtype=torch.float64, device=device) if ws is not None else None
+            sbar = torch.empty((self.n_points, self.n_vars), dtype=torch.float64, device=device)
+            lbar = torch.empty(max(R, 1), dtype=torch.float64, device=device)
+            mem = L.MEM_DEVICE
+        else:
+            f64 = lambda v: np.ascontiguousarray(v, dtype=np.float64) if v is not None else None
+            i32 = lambda v: np.ascontiguousarray(v, dtype=np.int32) if v is not None else None
+            wq, ws, r = f64(w_heat_release), f64(w_consumption_speed), f64(rho_u)
+            a, b = i32(ju), i32(jb)
+            hr = np.empty(nf)
+            cs = np.empty(nf) if ws is not None else None
+            sbar = np.empty((self.n_points, self.n_vars))
+            lbar = np.empty(max(R, 1))
+            mem = L.MEM_HOST
         L.check(_lib().ember_split_adjoint(self._h, L.ptr(wq), L.ptr(ws), L.ptr(r), L.ptr(a), L.ptr(b), int(tape_cap),
-                                           hr.ctypes.data, L.ptr(cs), sbar.ctypes.data, lbar.ctypes.data, L.MEM_HOST,
-                                           None), "ember_split_adjoint")
-        return hr, cs, sbar, lbar[:self.gmech.mech.n_reactions]
+                                           L.ptr(hr), L.ptr(cs), L.ptr(sbar), L.ptr(lbar), mem, None),
+                "ember_split_adjoint")
+        return hr, cs, sbar, lbar[:R]
 
 
 def mixture_properties(mech: Mechanism, state, pressure: float = 101325.0):

@@ -645,6 +645,12 @@ int ember_split_step(ember_split split, int n_steps, int use_graph, void* stream
 int ember_split_get_state(ember_split split, double* state, double* t, int mem, void* stream);
 /* ddtDiff and ddtProd of the last step, point-major. */
 int ember_split_get_derivatives(ember_split split, double* ddt_diff, double* ddt_prod, int mem, void* stream);
+/* Replace the time derivatives that set the next step's split constants
+ * (point-major; ddt_conv only with the convection stage attached, NULL =
+ * zero), as FlameSolver does after a regrid: ddtDiff, ddtProd and ddtConv
+ * interpolated onto the new grid (src/flameSolver.cpp:331-336). */
+int ember_split_set_derivatives(ember_split split, const double* ddt_diff, const double* ddt_prod,
+                                const double* ddt_conv, int mem, void* stream);
 /* Source-stage status [n_points] and stats [n_points][EMBER_STATS_WIDTH] of the last step. */
 int ember_split_source_status(ember_split split, int* status, int* stats, int mem, void* stream);
 /* Failed source points and diffusion systems summed over the steps since
@@ -676,6 +682,69 @@ int ember_split_objectives(ember_split split, const double* rho_u, const int* ju
 int ember_split_adjoint(ember_split split, const double* w_heat_release, const double* w_consumption_speed,
                         const double* rho_u, const int* ju, const int* jb, int tape_cap, double* heat_release,
                         double* consumption_speed, double* state_bar, double* lnk_bar, int mem, void* stream);
+
+/* ======================================================================
+ * Adaptive grid of a flame (host code; needs no device)
+ *
+ * The regrid block of FlameSolver::finishStep (src/flameSolver.cpp:279-352)
+ * with the rules of OneDimGrid (src/grid.cpp): boundary regrid (regrid /
+ * regridUnstrained, src/grid.cpp:721-838: points added at a boundary that is
+ * not flat to boundary_tol, removed while it is flat to boundary_tol_rm),
+ * the damping values interpolated onto the new grid, then interior
+ * adaptation (adapt, src/grid.cpp:77-359: insertion by the vtol / dvtol /
+ * damping / grid_max / uniformity criteria, then removal with rm_tol of
+ * margin). Inserted points take the natural cubic spline value of every row
+ * (mathUtils::splines); boundary points repeat the boundary value.
+ * After a change the caller re-creates its split handle on the new grids
+ * (the step graph is captured for fixed sizes) and hands back the state
+ * and time derivatives interpolated here.
+ * ==================================================================== */
+typedef struct {
+    double vtol;                        /* Grid.vtol (0.12)                           */
+    double dvtol;                       /* Grid.dvtol (0.2)                           */
+    double absvtol;                     /* Grid.absvtol (1e-8)                        */
+    double rm_tol;                      /* Grid.rmTol (0.6)                           */
+    double uniformity_tol;              /* Grid.uniformityTol (2.5)                   */
+    double grid_min, grid_max;          /* Grid.gridMin (5e-7), gridMax (2e-4) m      */
+    double damp_const;                  /* Grid.dampConst (7)                         */
+    double center_grid_min;             /* Grid.centerGridMin (1e-4) m                */
+    double boundary_tol;                /* Grid.boundaryTol (5e-5)                    */
+    double boundary_tol_rm;             /* Grid.boundaryTolRm (1e-5)                  */
+    double unstrained_downstream_width; /* Grid.unstrainedDownstreamWidth (5)         */
+    int add_point_count;                /* Grid.addPointCount (3)                     */
+    int fixed_burned_val;               /* General.fixedBurnedVal (1)                 */
+    int unburned_left;                  /* General.unburnedLeft (1)                   */
+    int fixed_left_loc;                 /* General.fixedLeftLocation (0)              */
+    int twin_flame, cylindrical_flame;  /* General.twinFlame, curvedFlame (0, 0)      */
+    int left_bc, right_bc;              /* EMBER_BC_* of the flame's grid             */
+} ember_grid_options;
+
+typedef struct ember_grid_s* ember_grid;
+
+/* The reference's defaults (python/ember/input.py, classes Grid and General). */
+int ember_grid_options_default(ember_grid_options* opts);
+/* A grid of n_points >= 3 strictly increasing coordinates x (copied).
+ * Replaces: OneDimGrid with setOptions (src/grid.cpp:9-41). */
+int ember_grid_create(const ember_grid_options* opts, int n_points, const double* x, ember_grid* out);
+int ember_grid_destroy(ember_grid grid);
+/* One regrid of the current grid. rows: n_rows rows of the current number of
+ * points each (row-major; the first n_adapt drive the criteria: FlameSolver
+ * passes the state rows U, T, Y_k, followed by the rows of ddtConv, ddtDiff
+ * and ddtProd, which are only carried along). damp_val: the damping length
+ * per point (ember_grid_damping). boundaries != 0 moves the domain ends first:
+ * with strain_rate != 0 by the flatness criteria (regrid), with strain_rate
+ * == 0 from qdot (regridUnstrained; qdot: per point). Returns the new number
+ * of points and whether the grid changed; ember_grid_get reads the result. */
+int ember_grid_regrid(ember_grid grid, int n_rows, int n_adapt, const double* rows, const double* damp_val,
+                      const double* qdot, double strain_rate, int boundaries, int* n_points_out, int* updated);
+/* The grid after the last regrid: x and rows (n_rows rows of the new number
+ * of points; either may be NULL) and the unburned / burned boundary indices. */
+int ember_grid_get(ember_grid grid, double* x, double* rows, int* ju, int* jb);
+/* Damping length per point as FlameSolver computes it before a regrid
+ * (src/flameSolver.cpp:292-303): sqrt(min(mu, lambda/cp, rho D_k > 0) /
+ * max(|rho a|, 1e-100)); rho_d point-major [n][S]. */
+int ember_grid_damping(int n_points, int n_species, const double* mu, const double* conductivity, const double* cp,
+                       const double* rho_d, const double* rho, double strain_rate, double* damp_val);
 
 #ifdef __cplusplus
 }

@@ -39,7 +39,7 @@ def correct_mass_fractions(state):
     state[:, 2:] = Yc * r[:, None]
 
 
-def step_properties(omech, tdata, grids, state, pressure, threshold, mult, gdt, cross_terms):
+def step_properties(omech, tdata, grids, state, pressure, threshold, mult, gdt, cross_terms, props_out=None):
     """Start of FlameSolver::step for a batch of flames: updateChemicalProperties
     (src/flameSolver.cpp:652-699, thermo and "Approx" transport from
     oracle_transport.c), prepareIntegrators' diffusion coefficients
@@ -49,11 +49,13 @@ def step_properties(omech, tdata, grids, state, pressure, threshold, mult, gdt, 
     the correction flux jCorr smoothed by a tridiagonal integration with
     B = lambda/(rho cp), D = 1 over [0, globalTimestep], and the species and
     temperature cross terms. Returns (B, D, ddt_cross) in the layouts of
-    split_steps."""
+    split_steps; the properties go into props_out (a dict) when given."""
     from oracle import chem
     n_pts, n = state.shape
     S = n - 2
     props = chem.transport_eval(omech, tdata, state[:, 1], state[:, 2:], pressure, threshold)
+    if props_out is not None:
+        props_out.update(props)
     rho, cp, lam, mu = props["density"], props["cp_mass"], props["conductivity"], props["viscosity"]
     rhoD, cpS = props["rho_d"], props["cp_species"]
     W = [float(w) for w in omech.mech.mol_weight]
@@ -145,15 +147,18 @@ def split_constants(ddt_diff, ddt_prod, cross, balanced, ddt_conv=None):
 
 
 def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cross=None, balanced=True,
-                mult=10.0, ddt=None, transport=None, convection=None):
+                mult=10.0, ddt=None, transport=None, convection=None, props_out=None):
     """n_steps split steps of a batch of flames. state: point-major [n_pts, n]
     (copied); B, D: variable-major per flame (flat). transport: None, or
     (TransportData, threshold, cross_terms): B, D (and the cross terms) are
     then recomputed from the state at the start of every step
     (step_properties). convection: None, or (flames, y_left, options) of
     the convection stage (ConvectionFlame-like objects, [n_flames, S], a
-    ConvectionOptions): the step is then D C D S D C D. Returns (state, t,
-    ddt_diff, ddt_prod, source_status_of_last_step)."""
+    ConvectionOptions): the step is then D C D S D C D. ddt: None, or the
+    time derivatives (ddt_diff, ddt_prod[, ddt_conv]) of the previous step.
+    Returns (state, t,
+    ddt_diff, ddt_prod, source_status_of_last_step); with a transport model
+    the last step's properties go into props_out (a dict) when given."""
     state = np.array(state, dtype=np.float64, copy=True)
     n_pts, n = state.shape
     offs = np.cumsum([0] + [g.n_points for g in grids])
@@ -162,13 +167,14 @@ def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cro
     cross = np.zeros_like(state) if ddt_cross is None else np.asarray(ddt_cross, dtype=np.float64).reshape(n_pts, n)
     ddt_diff = np.zeros_like(state) if ddt is None else ddt[0].copy()
     ddt_prod = np.zeros_like(state) if ddt is None else ddt[1].copy()
-    ddt_conv = np.zeros_like(state)
+    ddt_conv = np.zeros_like(state) if ddt is None or len(ddt) < 3 or ddt[2] is None else ddt[2].copy()
     W = np.asarray(omech.mech.mol_weight, dtype=np.float64)
     status = None
     for _ in range(n_steps):
         if transport is not None:
             tdata, thr, with_cross = transport
-            B, D, c = step_properties(omech, tdata, grids, state, opts.pressure, thr, mult, dt, with_cross)
+            B, D, c = step_properties(omech, tdata, grids, state, opts.pressure, thr, mult, dt, with_cross,
+                                      props_out)
             if with_cross:
                 cross = c
         if convection is not None:
@@ -260,12 +266,15 @@ def spline_integral(x, y):
     return total
 
 
-def objectives(omech, grids, state, pressure, kinetics_model, rho_u=None, ju=None, jb=None):
-    """(qdot, heat release per flame, consumption speed per flame or None)."""
+def objectives(omech, grids, state, pressure, kinetics_model, rho_u=None, ju=None, jb=None, cp=None):
+    """(qdot, heat release per flame, consumption speed per flame or None).
+    The consumption speed divides qdot by cp: that of the last property
+    update when given (FlameSolver's cp array, src/flameSolver.cpp:956-961),
+    else the current state's."""
     from ember_gb300.source import STATE_NORMALIZED
     g = omech.gas_eval(state[:, 1], state[:, 2:], pressure=pressure, model=kinetics_model, mode=STATE_NORMALIZED)
     qdot = -_seq_sum(g["net"] * g["hk"], axis=1)
-    qcp = qdot / g["cp_mass"]
+    qcp = qdot / (g["cp_mass"] if cp is None else np.asarray(cp, dtype=np.float64))
     offs = np.cumsum([0] + [gr.n_points for gr in grids])
     hr = np.array([spline_integral(gr.x, qdot[offs[f]:offs[f + 1]]) for f, gr in enumerate(grids)])
     cs = None
