@@ -10,8 +10,9 @@
 // Polynomial coefficients are the reciprocal factorials 1/n! and 2/(2k+1)
 // rounded to the nearest double; ln2 is split into its nearest double and
 // the nearest double of the remainder. Both functions are accurate to about
-// 1-2 ulp; tests compare them with the C library on the CPU and with CUDA's
-// exp/log on the GPU.
+// 1-2 ulp against the C library's exp/log (checked on the CPU restatement,
+// which runs the same operation sequence); on the GPU they give the CPU
+// restatement's bits, which every chemistry parity test exercises.
 #pragma once
 
 #include <cstdint>

@@ -1,7 +1,8 @@
 """Regenerate the golden fixtures in this folder from the reference sources.
 
-Run in a container where the reference checkout is mounted (default
-/root/reference, or pass its path). It is never run by the tests.
+Run where a checkout of the reference is available, with its path as the
+only argument:  python tests/golden/make_golden.py <reference checkout>.
+It is never run by the tests.
 
 Fixtures written:
   tridiag_bdf.json  -- the reference's tridiagonal golden table, both as
@@ -68,7 +69,7 @@ def parse_cesium(ref: str):
     }
 
 
-def main(ref: str = "/root/reference") -> None:
+def main(ref: str) -> None:
     bdf = load_bdf(ref)
     y0 = np.array([0, 0.5, 2.0, 1.0, 0])
     k = np.array([0, 0, 0, 0.2, 0.4])
@@ -91,4 +92,6 @@ def main(ref: str = "/root/reference") -> None:
 
 
 if __name__ == "__main__":
-    main(*sys.argv[1:])
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])

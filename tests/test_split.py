@@ -130,6 +130,36 @@ def test_split_objectives_bitwise_vs_oracle(gpu_lib, mech):
     assert (hr != 0).all()
 
 
+@pytest.mark.gpu
+def test_consumption_speed_uses_the_property_update_cp(gpu_lib, mech):
+    # with the transport model the step starts with a property update, and the
+    # consumption speed divides by that cp (FlameSolver::getConsumptionSpeed)
+    from oracle.chem import OracleMech
+    from ember_gb300.transport import GpuTransport, synthetic_transport
+    td = synthetic_transport(mech, seed=4)
+    grids, state, B, D, rho_u, ju, jb = _case(mech, n_flames=2, n_min=12, n_max=20)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    gm, s = _gpu_solver(mech, grids, 2e-6, QSS, opts, L.DIFFUSION_SERIAL)
+    gt = GpuTransport(gm, td)
+    s.set_state(0.0, state)
+    s.set_transport(B, D)
+    s.set_transport_model(gt, 1e-5, True)
+    s.step(2)
+    out, _ = s.state()
+    q, hr, cs = s.objectives(rho_u, ju, jb)
+    om = OracleMech(mech)
+    props = {}
+    ref, *_ = osplit.split_steps(om, grids, state, 0.0, B, D, 2e-6, 2, QSS, opts, transport=(td, 1e-5, True),
+                                 props_out=props)
+    assert np.array_equal(out, ref)
+    rq, rhr, rcs = osplit.objectives(om, grids, ref, opts.pressure, opts.kinetics_model, rho_u, ju, jb,
+                                     cp=props["cp_mass"])
+    assert np.array_equal(q, rq) and np.array_equal(hr, rhr)
+    assert np.array_equal(cs, rcs)
+    _, _, cs_now = osplit.objectives(om, grids, ref, opts.pressure, opts.kinetics_model, rho_u, ju, jb)
+    assert not np.array_equal(cs, cs_now)   # the start-of-step cp differs from the end state's
+
+
 def _cross_numpy(om, td, grids, state, pressure, thr, mult, gdt):
     """Vectorised restatement of updateCrossTerms (src/flameSolver.cpp:551-617,
     no thermal diffusion) for checking oracle/split.py's loops."""
@@ -337,6 +367,89 @@ def test_split_with_convection_bitwise_vs_oracle(gpu_lib, mech, graph):
     s.step(1)
     ref2, *_ = osplit.split_steps(OracleMech(mech), grids, state, 1e-3, B, D, dt, 1, QSS, opts)
     assert np.array_equal(s.state()[0], ref2)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("algorithm", [L.DIFFUSION_SERIAL, L.DIFFUSION_PARALLEL], ids=["serial", "parallel"])
+def test_split_with_convection_and_transport_model_vs_oracle(gpu_lib, mech, algorithm):
+    # the configuration the split benchmark runs: D C D S D C D with the device
+    # transport model and cross terms (properties, B/D, jCorr smoothing) at the
+    # start of every step; the serial diffusion algorithm is bitwise. With the
+    # warp-parallel one the rounding-level differences reach the convection
+    # stage, whose adaptive Adams integrator (reltol 1e-6) can then take other
+    # steps: the two agree within the convection tolerances, |error| <=
+    # reltol |y| + abstol per variable (measured: 5e-5 of a variable's largest
+    # value, for a minor species near its abstol)
+    from oracle.chem import OracleMech
+    from ember_gb300.convection import ConvectionOptions
+    from ember_gb300.transport import GpuTransport, synthetic_transport
+    td = synthetic_transport(mech, seed=4)
+    grids, state, B, D, flames, y_left = _convection_case(mech)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    # this small synthetic mechanism runs away within a few steps of 2e-6 s
+    # (points fail at the QSS dtmin, on the GPU as in the oracle); two steps
+    # of 5e-7 s stay clear of that
+    dt = 5e-7
+    copts = ConvectionOptions()
+    gm, s = _gpu_solver(mech, grids, dt, QSS, opts, algorithm)
+    gt = GpuTransport(gm, td)
+    s.set_state(0.0, state)
+    s.set_transport(B, D)
+    s.set_transport_model(gt, 1e-5, True)
+    s.set_convection(flames, y_left, copts)
+    s.step(2, graph=True)
+    out, t = s.state()
+    ref, rt, _, _, rst = osplit.split_steps(OracleMech(mech), grids, state, 0.0, B, D, dt, 2, QSS, opts,
+                                            transport=(td, 1e-5, True), convection=(flames, y_left, copts))
+    assert t == rt
+    assert (rst == 0).all()
+    assert s.failures() == (0, 0)
+    if algorithm == L.DIFFUSION_SERIAL:
+        assert np.array_equal(out, ref), np.abs(out - ref).max()
+    else:
+        atol = np.full(out.shape[1], copts.abstol_y)
+        atol[0], atol[1] = copts.abstol_u, copts.abstol_t
+        units = np.abs(out - ref) / (copts.reltol * np.abs(ref) + atol)
+        assert units.max() <= 1.0, units.max()
+
+
+@pytest.mark.gpu
+def test_captured_step_survives_a_later_call_for_smaller_flames(gpu_lib, mech):
+    # the UTW kernel stages 3N doubles of shared memory per flame; a later
+    # convection call for small flames must not lower the kernel's limit
+    # below what a captured step of a 2100-point flame (50 KB) needs
+    from ember_gb300.convection import ConvectionOptions, convection_batch, integrate_convection_terms
+    grids, state, B, D, flames, y_left = _convection_case(mech, n_flames=1, n_min=2100, n_max=2100)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    copts = ConvectionOptions()
+    gm, s = _gpu_solver(mech, grids, 2e-7, QSS, opts, L.DIFFUSION_PARALLEL)
+    s.set_state(0.0, state)
+    s.set_transport(B, D)
+    s.set_convection(flames, y_left, copts)
+    s.step(1, graph=True)
+    cb = convection_batch(mech, n_flames=2, n_min=40, n_max=60, seed=17)
+    integrate_convection_terms(cb.flames, mech.mol_weight, cb.x, cb.y_left, cb.drhodt, cb.split_const,
+                               cb.state.copy(), 0.0, 1e-6, copts)
+    s.step(1, graph=True)   # replays the captured step
+    out, t = s.state()
+    gm2, r = _gpu_solver(mech, grids, 2e-7, QSS, opts, L.DIFFUSION_PARALLEL)
+    r.set_state(0.0, state)
+    r.set_transport(B, D)
+    r.set_convection(flames, y_left, copts)
+    r.step(2)
+    assert np.array_equal(out, r.state()[0])
+
+
+@pytest.mark.gpu
+def test_split_rejects_convection_flames_at_another_pressure(gpu_lib, mech):
+    # the reference has one gas pressure for every stage of the step
+    from ember_gb300.convection import ConvectionOptions
+    grids, state, B, D, flames, y_left = _convection_case(mech)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    gm, s = _gpu_solver(mech, grids, 2e-6, QSS, opts, L.DIFFUSION_SERIAL)
+    flames[1].pressure = 2.0 * opts.pressure
+    with pytest.raises(L.EmberGpuError):
+        s.set_convection(flames, y_left, ConvectionOptions())
 
 
 @pytest.mark.parametrize("with_convection", [False, True])
