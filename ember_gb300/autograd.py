@@ -21,28 +21,47 @@ def _np(t):
 
 
 class SplitStepObjectives(torch.autograd.Function):
+    """Inputs on a CUDA device stay there: the multipliers, the start state,
+    the objectives and both gradients go through the library's device
+    pointers without a host round trip; CPU tensors go through host arrays."""
+
     @staticmethod
     def forward(ctx, state0, ln_mult, solver, t0, rho_u, ju, jb, tape_cap):
-        solver.gmech.set_multipliers(np.exp(_np(ln_mult)))
-        solver.set_state(float(t0), _np(state0))
-        solver.step(1)
-        _, hr, cs = solver.objectives(rho_u, ju, jb)
+        dev = state0.device if state0.is_cuda else None
+        if dev is not None:
+            solver.gmech.set_multipliers(torch.exp(ln_mult.detach().to(dev, torch.float64)).contiguous())
+            solver.set_state(float(t0), state0.detach().to(torch.float64).contiguous())
+            solver.step(1)
+            _, hr, cs = solver.objectives(rho_u, ju, jb, device=dev)
+            out = torch.cat([hr, cs])
+        else:
+            solver.gmech.set_multipliers(np.exp(_np(ln_mult)))
+            solver.set_state(float(t0), _np(state0))
+            solver.step(1)
+            _, hr, cs = solver.objectives(rho_u, ju, jb)
+            out = torch.as_tensor(np.concatenate([hr, cs]), dtype=torch.float64)
         ctx.solver, ctx.t0, ctx.rho_u, ctx.ju, ctx.jb, ctx.tape_cap = solver, t0, rho_u, ju, jb, tape_cap
         ctx.save_for_backward(state0, ln_mult)
-        return torch.as_tensor(np.concatenate([hr, cs]), dtype=torch.float64, device=state0.device)
+        return out
 
     @staticmethod
     def backward(ctx, grad):
         state0, ln_mult = ctx.saved_tensors
         solver = ctx.solver
         nf = len(solver.grids)
+        if state0.is_cuda:
+            dev = state0.device
+            g = grad.detach().to(dev, torch.float64).contiguous()
+            solver.gmech.set_multipliers(torch.exp(ln_mult.detach().to(dev, torch.float64)).contiguous())
+            solver.set_state(float(ctx.t0), state0.detach().to(torch.float64).contiguous())
+            _, _, sbar, lbar = solver.adjoint(g[:nf], g[nf:], ctx.rho_u, ctx.ju, ctx.jb, ctx.tape_cap, device=dev)
+            return (sbar.reshape(state0.shape), lbar.to(ln_mult.device), None, None, None, None, None, None)
         g = _np(grad)
         solver.gmech.set_multipliers(np.exp(_np(ln_mult)))
         solver.set_state(float(ctx.t0), _np(state0))
         _, _, sbar, lbar = solver.adjoint(g[:nf], g[nf:], ctx.rho_u, ctx.ju, ctx.jb, ctx.tape_cap)
-        dev = state0.device
-        return (torch.as_tensor(sbar, device=dev).reshape(state0.shape), torch.as_tensor(lbar, device=dev),
-                None, None, None, None, None, None)
+        return (torch.as_tensor(sbar).reshape(state0.shape), torch.as_tensor(lbar), None, None, None, None, None,
+                None)
 
 
 def split_step_objectives(solver, state0, ln_mult, t0, rho_u, ju, jb, tape_cap: int = 0):

@@ -872,6 +872,10 @@ __global__ void __launch_bounds__(kNT, 2) k_conv_utw(const __grid_constant__ Con
     int st[4];
     int rc = adams_block<kNT>(s, wk, s.u.y3, a.reltol, t0, tf, 1, a.min_step, a.max_steps, st, red, sh);
     if (s.overflow) rc = -20;
+    // rV of the last right-hand side (V is already in the slice): the next
+    // step's continuity point reads both, as the reference reads its members
+    __syncthreads();
+    for (int j = threadIdx.x; j < N; j += kNT) s.u.rV[j] = s.sm_rV[j];
     double* state = a.state + F.v0;
     for (int j = threadIdx.x; j < N; j += kNT) {
         state[j] = s.u.y3[3 * j + 0];
@@ -1119,6 +1123,101 @@ int conv_plan_alloc(ConvPlan& p, Scratch& sc, bool with_stats, cudaStream_t st) 
     a.n_hist = nh;
     const size_t utw_smem = size_t(3) * p.max_points * sizeof(double);
     EMBER_TRY(raise_dynamic_smem(reinterpret_cast<const void*>(k_conv_utw), utw_smem));
+    return EMBER_OK;
+}
+
+// ConvectionSystemUTW::updateContinuityBoundaryCondition
+// (src/convectionSystem.cpp:196-277), run at the start of every split step
+// but the first after the stage is attached or the state set (*ready == 0:
+// the caller's values stand, as the reference's first update reads its
+// initial V): the continuity point from the step-start temperature (state,
+// point-major), the heat release rate (qdot, fixedQdot only) and V of the
+// UTW system's last right-hand side; x_vzero for the stagnation-point
+// condition; rv_cont = rV[j_cont] of that evaluation for fixedRight and
+// fixedQdot, whose right-hand side never writes that entry. One thread per
+// flame (sequential searches as the reference's).
+__global__ void k_conv_continuity(const __grid_constant__ ConvArgs a, ConvFlame* flames, const int* ready,
+                                  const double* __restrict__ state, int n_vars, const double* __restrict__ qdot) {
+    const int fi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fi >= a.n_flames || *ready == 0) return;
+    ConvFlame& F = flames[fi];
+    if (!utw_slice_ok(a, F)) return;
+    ember_convection_flame& fl = F.f;
+    const int N = fl.n_points, jj = N - 1;
+    const double* x = a.x + F.p0;
+    const UtwView u = utw_view(a, F);
+    const double* V = u.V;
+    auto T = [&](int j) { return state[(F.p0 + j) * n_vars + 1]; };
+    auto sgn = [](double v) { return v > 0 ? 1 : (v < 0 ? -1 : 0); };
+    int jc = fl.j_cont;
+    switch (fl.continuity_bc) {
+        case EMBER_CONTINUITY_LEFT: jc = 0; break;
+        case EMBER_CONTINUITY_RIGHT: jc = jj; break;
+        case EMBER_CONTINUITY_QDOT: {
+            jc = 0;
+            double qmax = 0.0;
+            for (int j = 0; j < N; ++j) {
+                const double q = qdot[F.p0 + j];
+                if (q > qmax) {
+                    qmax = q;
+                    jc = j;
+                }
+            }
+            break;
+        }
+        case EMBER_CONTINUITY_ZERO: {
+            int js = jj;
+            if (x[jj] > fl.x_vzero)
+                for (int j = 0; j < N; ++j)
+                    if (x[j] > fl.x_vzero) {
+                        js = j;
+                        break;
+                    }
+            jc = js;
+            for (int i = 1; js + i <= jj || js >= i; ++i) {
+                if (js + i <= jj && sgn(V[js + i]) != sgn(V[js])) {
+                    jc = js + i;
+                    break;
+                }
+                if (js >= i && sgn(V[js - i]) != sgn(V[js])) {
+                    jc = js - i + 1;
+                    break;
+                }
+            }
+            if (jc == 0) fl.x_vzero = x[0] - V[0] * (x[1] - x[0]) / (V[1] - V[0]);
+            else if (jc == jj) fl.x_vzero = x[jj] - V[jj] * (x[jj] - x[jj - 1]) / (V[jj] - V[jj - 1]);
+            else fl.x_vzero = x[jc] - V[jc] * (x[jc] - x[jc - 1]) / (V[jc] - V[jc - 1]);
+            break;
+        }
+        default: {  // fixedTemperature: the first crossing of the mid temperature
+            double tmax = T(0), tmin = T(0);
+            for (int j = 1; j < N; ++j) {
+                tmax = fmax(tmax, T(j));
+                tmin = fmin(tmin, T(j));
+            }
+            const double tmid = 0.5 * (tmax + tmin);
+            jc = 0;
+            for (int j = 1; j < N; ++j)
+                if ((T(j) - tmid) * (T(j - 1) - tmid) <= 0) {
+                    jc = j;
+                    break;
+                }
+            break;
+        }
+    }
+    fl.j_cont = jc;
+    if (fl.continuity_bc == EMBER_CONTINUITY_RIGHT || fl.continuity_bc == EMBER_CONTINUITY_QDOT) fl.rv_cont = u.rV[jc];
+}
+
+__global__ void k_conv_ready(int* ready) { *ready = 1; }
+
+int conv_continuity_launch(const ConvPlan& p, const ConvArgs& a, const int* ready, const double* state, int n_vars,
+                           const double* qdot, cudaStream_t st) {
+    k_conv_continuity<<<blocks_for(p.n_flames, 32), 32, 0, st>>>(a, const_cast<ConvFlame*>(a.flames), ready, state,
+                                                                 n_vars, qdot);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    k_conv_ready<<<1, 1, 0, st>>>(const_cast<int*>(ready));
+    EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }
 

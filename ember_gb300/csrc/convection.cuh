@@ -65,5 +65,10 @@ size_t conv_plan_bytes(const ConvPlan& p, bool with_stats);
 // The three kernels on `st` with arguments `a` (the plan's, inputs and
 // times set by the caller).
 int conv_launch(const ConvPlan& p, const ConvArgs& a, cudaStream_t st);
+// The continuity point of every flame at the start of a split step (after
+// the first since *ready was cleared; then sets *ready): state point-major
+// with n_vars per point; qdot per point or null (needed for fixedQdot).
+int conv_continuity_launch(const ConvPlan& p, const ConvArgs& a, const int* ready, const double* state, int n_vars,
+                           const double* qdot, cudaStream_t st);
 
 }  // namespace ember

@@ -589,6 +589,51 @@ extern "C" int ember_gas_eval(ember_mech m, int n, double pressure, int model, i
     return finish_call(mem, st);
 }
 
+namespace ember {
+
+// Thermo and rates of n contiguous states (T [n], Y [n][S] on the device)
+// into caller-provided buffers, with a caller-provided rate-constant cache of
+// gas_eval_cache_doubles(m, n) doubles: no allocation, so it can be captured
+// into a graph.
+// CTAs of the capturable gas evaluation (one rate-constant cache slot each):
+// the same count when the cache is sized and when the kernel is launched.
+static int gas_eval_blocks(int n) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                   cudaSuccess)
+        sms = 152;
+    return std::max(1, std::min(n, sms * 4));
+}
+
+size_t gas_eval_cache_doubles(const MechView& v, int n) {
+    return size_t(gas_eval_blocks(n)) * ChemSmem::global_doubles(v);
+}
+
+int launch_gas_eval(const MechView& v, int n, double pressure, int model, int mode, const double* T, const double* Y,
+                    double* kcache, double* net, double* hk, double* cp_mass, cudaStream_t st) {
+    if (n <= 0) return EMBER_OK;
+    const int S = v.S;
+    const int NTh = chem_threads_for(S);
+    const size_t per = (ChemSmem::doubles(S, v.R, v.n_tb, v.n_fo, true) + S) * sizeof(double);
+    EMBER_CHECK_ARG(per <= 227 * 1024, "mechanism too large for the shared-memory work area (%zu B)", per);
+    const int blocks = gas_eval_blocks(n);
+#define EMBER_GAS_EVAL(NTV)                                                                 \
+    EMBER_TRY(raise_dynamic_smem(reinterpret_cast<const void*>(k_gas_eval<NTV>), per)); \
+    k_gas_eval<NTV><<<blocks, NTV, per, st>>>(v, n, pressure, model, mode, T, Y, kcache, nullptr, nullptr, net, hk, \
+                                              cp_mass, nullptr)
+    switch (NTh) {
+        case 64: EMBER_GAS_EVAL(64); break;
+        case 128: EMBER_GAS_EVAL(128); break;
+        case 160: EMBER_GAS_EVAL(160); break;
+        default: EMBER_GAS_EVAL(256); break;
+    }
+#undef EMBER_GAS_EVAL
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
+
+}  // namespace ember
+
 extern "C" int ember_source_options_default(ember_source_options* o) {
     EMBER_CHECK_ARG(o != nullptr, "null options");
     *o = ember_source_options{};

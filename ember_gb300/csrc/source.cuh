@@ -99,6 +99,10 @@ SourceArgs make_source_args(const ember_source_options* o, int n, const double* 
                             const double* dt, double t_start, const double* x, double* state_out, int* status,
                             int* stats);
 int source_check_options(const ember_source_options* o);
+// Rates and thermo of n states into caller buffers (no allocation; capturable).
+size_t gas_eval_cache_doubles(const MechView& v, int n);
+int launch_gas_eval(const MechView& v, int n, double pressure, int model, int mode, const double* T, const double* Y,
+                    double* kcache, double* net, double* hk, double* cp_mass, cudaStream_t st);
 // Device bytes a launch above takes from its Scratch (for an arena sized up front).
 int source_qss_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes);
 // Threads per point of the QSS kernel for these arguments (see threads_per_point).

@@ -624,6 +624,12 @@ struct ember_split_s {
     void* cblob = nullptr;
     double *ddt_conv = nullptr, *sc_conv = nullptr, *sc_conv_vm = nullptr, *delta_conv_vm = nullptr;
     double *drhodt = nullptr, *y_left = nullptr;
+    // the continuity point moved every step: a flag cleared at attach and set_state (the first step
+    // keeps the caller's values), and for fixedQdot the start state's heat release rate
+    int* conv_ready = nullptr;
+    bool conv_qdot = false;
+    double *cq_T = nullptr, *cq_Y = nullptr, *cq_net = nullptr, *cq_hk = nullptr, *cq_cp = nullptr,
+           *cq_q = nullptr, *cq_qcp = nullptr, *cq_cache = nullptr;
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -794,11 +800,25 @@ int enqueue_step(ember_split h, cudaStream_t st, const StepTape* tape = nullptr)
     const int g = grid_for(h->n_vals);
     if (tape) EMBER_CUDA_TRY(cudaMemcpyAsync(tape->t_saved, h->t_dev, sizeof(double), cudaMemcpyDeviceToDevice, st));
     if (h->tr) EMBER_TRY(enqueue_properties(h, st));
-    if (h->conv)
+    if (h->conv) {
         k_density_derivative<<<grid_for(h->n_pts), 256, 0, st>>>(h->n_pts, h->n_vars, h->opt.balanced,
                                                                  h->opt.source.pressure, h->mech->view.W, h->state,
                                                                  h->ddt_conv, h->ddt_diff, h->ddt_prod, h->ddt_cross,
                                                                  h->drhodt);
+        // updateContinuityBoundaryCondition (prepareIntegrators, src/flameSolver.cpp:215), with the start
+        // state's qdot for fixedQdot (calculateQdot after the previous step)
+        if (h->conv_qdot) {
+            const int S = h->n_vars - 2;
+            k_gather_TY<<<grid_for(h->n_pts * S), 256, 0, st>>>(h->n_pts, h->n_vars, h->state, h->cq_T, h->cq_Y);
+            EMBER_TRY(launch_gas_eval(h->mech->view, static_cast<int>(h->n_pts), h->opt.source.pressure,
+                                      h->opt.source.kinetics_model, EMBER_STATE_NORMALIZED, h->cq_T, h->cq_Y,
+                                      h->cq_cache, h->cq_net, h->cq_hk, h->cq_cp, st));
+            k_qdot<<<grid_for(h->n_pts, 128), 128, 0, st>>>(h->n_pts, S, h->cq_net, h->cq_hk, h->cq_cp, h->cq_q,
+                                                            h->cq_qcp);
+        }
+        EMBER_TRY(conv_continuity_launch(h->cplan, h->cplan.a, h->conv_ready, h->state, h->n_vars,
+                                         h->conv_qdot ? h->cq_q : nullptr, st));
+    }
     k_split_begin<<<g, 256, 0, st>>>(tb, h->opt.balanced, h->ddt_diff, h->ddt_prod, h->ddt_cross, h->sc_diff,
                                      h->sc_diff_vm, h->sc_prod, h->delta_vm, h->conv ? h->ddt_conv : nullptr,
                                      h->sc_conv, h->sc_conv_vm, h->delta_conv_vm);
@@ -1045,7 +1065,10 @@ extern "C" int ember_split_set_state(ember_split h, double t, const double* stat
     EMBER_CUDA_TRY(cudaMemcpyAsync(h->t_dev, &t, sizeof(double), cudaMemcpyHostToDevice, st));
     EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_diff, 0, sizeof(double) * h->n_vals, st));
     EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_prod, 0, sizeof(double) * h->n_vals, st));
-    if (h->conv) EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_conv, 0, sizeof(double) * h->n_vals, st));
+    if (h->conv) {
+        EMBER_CUDA_TRY(cudaMemsetAsync(h->ddt_conv, 0, sizeof(double) * h->n_vals, st));
+        EMBER_CUDA_TRY(cudaMemsetAsync(h->conv_ready, 0, sizeof(int), st));
+    }
     EMBER_CUDA_TRY(cudaMemsetAsync(h->fails, 0, 2 * sizeof(unsigned long long), st));
     h->props_valid = false;
     // the host value of t must outlive the copy
@@ -1105,9 +1128,19 @@ extern "C" int ember_split_set_convection(ember_split h, const ember_convection_
     ConvPlan p;
     EMBER_TRY(conv_plan_layout(p, h->n_flames, flames, S, opts));
     const size_t nv = size_t(h->n_vals);
+    bool any_qdot = false;
+    for (int f = 0; f < h->n_flames; ++f) any_qdot = any_qdot || flames[f].continuity_bc == EMBER_CONTINUITY_QDOT;
+    const size_t np = size_t(h->n_pts);
+    const size_t cache = gas_eval_cache_doubles(h->mech->view, static_cast<int>(h->n_pts));
+    // fixedQdot: T, cp, qdot, qdot/cp per point; Y, net rates, hk per point and species; the rate cache
+    const size_t qdot_bytes = any_qdot ? 3 * Scratch::rounded(np * S * sizeof(double)) +
+                                             4 * Scratch::rounded(np * sizeof(double)) +
+                                             Scratch::rounded(cache * sizeof(double))
+                                       : 0;
     const size_t bytes = conv_plan_bytes(p, false) + 4 * Scratch::rounded(nv * sizeof(double)) +
                          Scratch::rounded(size_t(h->n_pts) * sizeof(double)) +
-                         Scratch::rounded(size_t(h->n_flames) * S * sizeof(double));
+                         Scratch::rounded(size_t(h->n_flames) * S * sizeof(double)) + Scratch::rounded(sizeof(int)) +
+                         qdot_bytes;
     cudaError_t e = cudaMalloc(&h->cblob, bytes);
     if (e != cudaSuccess) {
         h->cblob = nullptr;
@@ -1121,6 +1154,19 @@ extern "C" int ember_split_set_convection(ember_split h, const ember_convection_
     EMBER_TRY(a.alloc(&h->delta_conv_vm, nv));
     EMBER_TRY(a.alloc(&h->drhodt, size_t(h->n_pts)));
     EMBER_TRY(a.alloc(&h->y_left, size_t(h->n_flames) * S));
+    EMBER_TRY(a.alloc(&h->conv_ready, 1));
+    h->conv_qdot = any_qdot;
+    if (any_qdot) {
+        EMBER_TRY(a.alloc(&h->cq_T, np));
+        EMBER_TRY(a.alloc(&h->cq_Y, np * S));
+        EMBER_TRY(a.alloc(&h->cq_net, np * S));
+        EMBER_TRY(a.alloc(&h->cq_hk, np * S));
+        EMBER_TRY(a.alloc(&h->cq_cp, np));
+        EMBER_TRY(a.alloc(&h->cq_q, np));
+        EMBER_TRY(a.alloc(&h->cq_qcp, np));
+        EMBER_TRY(a.alloc(&h->cq_cache, cache));
+    }
+    EMBER_CUDA_TRY(cudaMemset(h->conv_ready, 0, sizeof(int)));
     EMBER_TRY(conv_plan_alloc(p, a, false, nullptr));
     EMBER_CUDA_TRY(cudaMemcpy(h->y_left, y_left, sizeof(double) * h->n_flames * S, cudaMemcpyHostToDevice));
     EMBER_CUDA_TRY(cudaMemset(h->ddt_conv, 0, sizeof(double) * nv));

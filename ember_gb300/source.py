@@ -88,8 +88,14 @@ class GpuMechanism:
             pass
 
     def set_multipliers(self, mult=None):
-        m = np.ascontiguousarray(mult, dtype=np.float64) if mult is not None else None
-        L.check(L.lib().ember_mech_set_multipliers(self._h, L.ptr(m), L.MEM_HOST, None), "set_multipliers")
+        """Per-reaction rate multipliers (numpy, or a torch CUDA tensor used in
+        place); None resets them to 1."""
+        if mult is not None and L.mem_of(mult) == L.MEM_DEVICE:
+            m, mem = mult.contiguous(), L.MEM_DEVICE
+        else:
+            m = np.ascontiguousarray(mult, dtype=np.float64) if mult is not None else None
+            mem = L.MEM_HOST
+        L.check(L.lib().ember_mech_set_multipliers(self._h, L.ptr(m), mem, None), "set_multipliers")
 
     def gas_eval(self, T, Y, pressure=101325.0, model=KINETICS_STANDARD, mode=STATE_NORMALIZED):
         S = self.mech.n_species

@@ -636,7 +636,12 @@ int ember_split_set_transport_model(ember_split split, ember_transport tr, doubl
  * per flame; opts: tolerances and limits of ember_convection_integrate
  * (t_start, t_end unused). flames == NULL detaches the stage. Host memory;
  * the handle keeps its own copies and a fixed workspace, so the stage is part
- * of the captured step graph. The split-step adjoint covers D-S-D only and
+ * of the captured step graph. The flames' continuity points (j_cont, x_vzero,
+ * rv_cont) are the caller's for the first step after this call or
+ * ember_split_set_state; at the start of every later step they are updated on
+ * the device as ConvectionSystemUTW::updateContinuityBoundaryCondition does
+ * (src/convectionSystem.cpp:196-277), from the step-start temperature, its
+ * heat release rate (fixedQdot) and V / rV of the last UTW evaluation. The split-step adjoint covers D-S-D only and
  * refuses a handle with the stage attached. */
 int ember_split_set_convection(ember_split split, const ember_convection_flame* flames, const double* y_left,
                                const ember_convection_options* opts);

@@ -41,7 +41,7 @@ def _lib():
     l.oracle_convection_utw_rhs.restype = None
     l.oracle_convection_interval.argtypes = [vp, i, d, vp]
     l.oracle_convection_interval.restype = i
-    l.oracle_convection_flame.argtypes = [vp, i, vp, vp, vp, d, d, vp, vp, vp, vp, vp, vp, vp, vp, vp]
+    l.oracle_convection_flame.argtypes = [vp, i, vp, vp, vp, d, d, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]
     l.oracle_convection_flame.restype = i
     l.oracle_convection_drhodt.argtypes = [i, i, i, d, vp, vp, vp, vp, vp, vp, vp]
     l.oracle_convection_drhodt.restype = None
@@ -102,10 +102,11 @@ def interval(ht, t):
     return i, s.value
 
 
-def convection_flame(fl, W, x, y_left, drhodt, split, state, t0, tf, opts):
+def convection_flame(fl, W, x, y_left, drhodt, split, state, t0, tf, opts, last=None):
     """One flame's stage: state (variable-major (S+2) x N) is copied and the
     result returned with (status [1+S], stats [4], history times, history
-    values [H, N])."""
+    values [H, N]). ``last``: a dict that receives V and rV of the UTW
+    system's last right-hand side evaluation ("V", "rV")."""
     N = fl.n_points
     S = len(W)
     st = np.array(state, dtype=np.float64).reshape(-1).copy()
@@ -118,9 +119,12 @@ def convection_flame(fl, W, x, y_left, drhodt, split, state, t0, tf, opts):
                           int(opts.max_steps), int(opts.max_history))
     arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (W, x, y_left, drhodt, split)]
     f = flame_struct(fl)
+    vl, rvl = np.zeros(N), np.zeros(N)
     _lib().oracle_convection_flame(C.byref(f), S, _p(arrs[0]), _p(arrs[1]), _p(arrs[2]), float(t0), float(tf),
                                    _p(arrs[3]), _p(arrs[4]), _p(st), C.byref(o), _p(status), _p(stats), C.byref(H),
-                                   _p(ht), _p(hv))
+                                   _p(ht), _p(hv), _p(vl), _p(rvl))
+    if last is not None:
+        last["V"], last["rV"] = vl, rvl
     h = H.value
     return st, status, stats, ht[:h].copy(), hv[:h * N].reshape(h, N).copy()
 

@@ -175,7 +175,8 @@ void oracle_convection_drhodt(int n_pts, int n, int balanced, double pressure, c
 int oracle_convection_flame(const oracle_conv_flame* fl, int S, const double* W, const double* x,
                             const double* y_left, double t0, double tf, const double* drhodt, const double* split,
                             double* state, const oracle_conv_options* o, int* status, int* stats,
-                            int* n_history_out, double* hist_t_out, double* hist_v_out);
+                            int* n_history_out, double* hist_t_out, double* hist_v_out,
+                            double* v_last, double* rv_last);
 
 #ifdef __cplusplus
 }

@@ -639,7 +639,8 @@ void oracle_convection_prepare(int N, int S, const double* W, const double* stat
 int oracle_convection_flame(const oracle_conv_flame* fl, int S, const double* W, const double* x,
                             const double* y_left, double t0, double tf, const double* drhodt, const double* split,
                             double* state, const oracle_conv_options* o, int* status, int* stats,
-                            int* n_history_out, double* hist_t_out, double* hist_v_out) {
+                            int* n_history_out, double* hist_t_out, double* hist_v_out, double* v_last,
+                            double* rv_last) {
     const int N = fl->n_points;
     double* hh = (double*)calloc((size_t)N, sizeof(double));
     double* rph = (double*)calloc((size_t)N, sizeof(double));
@@ -684,6 +685,10 @@ int oracle_convection_flame(const oracle_conv_flame* fl, int S, const double* W,
         state[j] = y3[3 * j + 0];
         state[(size_t)N + j] = y3[3 * j + 1];
     }
+    /* V and rV of the last right-hand side evaluation (ConvectionSystemUTW's
+       members after the stage: the next step's continuity point reads them) */
+    if (v_last) memcpy(v_last, V, sizeof(double) * N);
+    if (rv_last) memcpy(rv_last, rV, sizeof(double) * N);
     if (n_history_out) *n_history_out = uc.n_history;
     if (hist_t_out) memcpy(hist_t_out, ht, sizeof(double) * uc.n_history);
     if (hist_v_out) memcpy(hist_v_out, hv, sizeof(double) * (size_t)uc.n_history * N);

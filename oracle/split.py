@@ -126,6 +126,63 @@ def step_properties(omech, tdata, grids, state, pressure, threshold, mult, gdt, 
     return B, D, cross
 
 
+def _sign(v):
+    return 1 if v > 0 else (-1 if v < 0 else 0)
+
+
+def continuity_point(fl, x, T, qdot, V, rV):
+    """ConvectionSystemUTW::updateContinuityBoundaryCondition
+    (src/convectionSystem.cpp:196-277) at the start of a step: the continuity
+    point j_cont of the flame's condition from the step-start temperature, its
+    heat release rate and V of the UTW system's last evaluation; x_vzero for
+    the stagnation-point condition; and rv_cont, the value rV[j_cont] keeps
+    (the reference's right-hand side never writes it for the fixedRight and
+    fixedQdot conditions). Updates fl in place."""
+    N = len(x)
+    jj = N - 1
+    bc = fl.continuity_bc
+    if bc == 0:        # fixedLeft
+        jc = 0
+    elif bc == 1:      # fixedRight
+        jc = jj
+    elif bc == 3:      # fixedQdot: the first maximum of positive qdot
+        jc, qmax = 0, 0.0
+        for j in range(N):
+            if qdot[j] > qmax:
+                qmax, jc = qdot[j], j
+    elif bc == 2:      # stagnationPoint: the sign change of V nearest the old x_vzero
+        if x[jj] > fl.x_vzero:
+            js = next(j for j in range(N) if x[j] > fl.x_vzero)
+        else:
+            js = jj
+        jc = js
+        i = 1
+        while js + i <= jj or js >= i:
+            if js + i <= jj and _sign(V[js + i]) != _sign(V[js]):
+                jc = js + i
+                break
+            if js >= i and _sign(V[js - i]) != _sign(V[js]):
+                jc = js - i + 1
+                break
+            i += 1
+        if jc == 0:
+            fl.x_vzero = x[0] - V[0] * (x[1] - x[0]) / (V[1] - V[0])
+        elif jc == jj:
+            fl.x_vzero = x[jj] - V[jj] * (x[jj] - x[jj - 1]) / (V[jj] - V[jj - 1])
+        else:
+            fl.x_vzero = x[jc] - V[jc] * (x[jc] - x[jc - 1]) / (V[jc] - V[jc - 1])
+    else:              # fixedTemperature: the first crossing of the mid temperature
+        Tmid = 0.5 * (max(T) + min(T))
+        jc = 0
+        for j in range(1, N):
+            if (T[j] - Tmid) * (T[j - 1] - Tmid) <= 0:
+                jc = j
+                break
+    fl.j_cont = jc
+    if bc in (1, 3):
+        fl.rv_cont = float(rV[jc])
+
+
 def split_constants(ddt_diff, ddt_prod, cross, balanced, ddt_conv=None):
     """SplitSolver::step's split constants (src/splitSolver.cpp:38-46):
     (sc_diff, sc_prod, sc_conv). Without convection (ddt_conv None) the
@@ -170,7 +227,13 @@ def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cro
     ddt_conv = np.zeros_like(state) if ddt is None or len(ddt) < 3 or ddt[2] is None else ddt[2].copy()
     W = np.asarray(omech.mech.mol_weight, dtype=np.float64)
     status = None
-    for _ in range(n_steps):
+    if convection is not None:
+        import copy
+        # the flames' continuity points move every step after the first
+        # (continuity_point); the caller's objects are left as given
+        convection = ([copy.copy(f) for f in convection[0]],) + tuple(convection[1:])
+        last_eval = [None] * len(grids)
+    for step_no in range(n_steps):
         if transport is not None:
             tdata, thr, with_cross = transport
             B, D, c = step_properties(omech, tdata, grids, state, opts.pressure, thr, mult, dt, with_cross,
@@ -180,6 +243,15 @@ def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cro
         if convection is not None:
             from oracle import convection as oconv
             drhodt = oconv.density_derivative(state, W, opts.pressure, ddt_conv, ddt_diff, ddt_prod, cross, balanced)
+            if step_no > 0:
+                qdot = None
+                if any(f.continuity_bc == 3 for f in convection[0]):
+                    qdot, _, _ = objectives(omech, grids, state, opts.pressure, opts.kinetics_model)
+                for f, g in enumerate(grids):
+                    a, b = offs[f], offs[f + 1]
+                    ev = last_eval[f]
+                    continuity_point(convection[0][f], xs[a:b], state[a:b, 1],
+                                     None if qdot is None else qdot[a:b], ev["V"], ev["rV"])
         sc_diff, sc_prod, sc_conv = split_constants(ddt_diff, ddt_prod, cross, balanced,
                                                     ddt_conv if convection is not None else None)
         delta = np.zeros_like(state)
@@ -193,9 +265,10 @@ def split_steps(omech, grids, state, t, B, D, dt, n_steps, method, opts, ddt_cro
             for f, g in enumerate(grids):
                 a, b = offs[f], offs[f + 1]
                 y0 = state[a:b].T.copy()
+                last_eval[f] = {}
                 y1, _, _, _, _ = oconv.convection_flame(cflames[f], W, xs[a:b], y_left[f], drhodt[a:b],
                                                         sc_conv[a:b].T.copy().reshape(-1), y0.reshape(-1), t0, t1,
-                                                        copts)
+                                                        copts, last=last_eval[f])
                 y1 = y1.reshape(y0.shape)
                 delta_conv[a:b] = delta_conv[a:b] + (y1 - y0).T
                 state[a:b] = y1.T

@@ -161,3 +161,97 @@ def test_split_step_gradients_match_central_differences_of_the_oracle(gpu_lib):
         fd = (J(state, mp) - J(state, mm)) / 2e-3
         assert abs(g_lnk[i] - fd) <= 2e-3 * abs(fd), (i, g_lnk[i], fd)
     om.set_multipliers(None)
+
+
+def test_split_step_adjoint_at_the_c4_size(gpu_lib):
+    # The C4 configuration: one 400-point flame-like profile of the 53-species /
+    # 325-reaction mechanism, one balanced D-S-D split step of 2e-5 s with the
+    # BDF source; J = Q + 1e3 S_c. Gradients of the discrete adjoint against
+    # central differences of the oracle for 20 random reactions and 20 random
+    # state entries (T and mass fractions above 1e-6).
+    #
+    # Step size of the differences: the benchmark spec names 1e-6 in ln A, but the
+    # adaptive integrator's step-size decisions make J noisy at the level of
+    # its tolerance (|J| = 3.8e5; at reltol 1e-10 the central differences of one
+    # reaction vary from 405 to -0.24 between h = 1e-6 and 1e-3, and most
+    # reactions' true sensitivities here are below 0.1). The test therefore uses
+    # reltol 1e-10 and h = 1e-3 (noise about 0.02), and holds each gradient to
+    # 2e-3 of the difference quotient plus 1e-4 of the largest gradient.
+    from oracle import split as osplit
+    from oracle.chem import OracleMech
+    from ember_gb300 import _lib as L
+    from ember_gb300.source import GpuMechanism
+    from ember_gb300.split import FlameBatchSplitSolver, flame_batch
+    mech = synthetic_mechanism(n_species=53, n_reactions=325, seed=53325)   # the benchmark's C4 inputs
+    grids, state, B, D, rho_u, ju, jb = flame_batch(mech, n_flames=1, n_min=400, n_max=400, seed=4000)
+    rt = 1e-10
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD, bdf_reltol=rt, bdf_abstol_momentum=rt,
+                                  bdf_abstol_energy=rt, bdf_abstol_species=rt * 1e-6)
+    dt = 2e-5
+    gm = GpuMechanism(mech)
+    solver = FlameBatchSplitSolver(gm, grids, dt, method=BDF, source_options=opts,
+                                   diffusion_algorithm=L.DIFFUSION_SERIAL)
+    solver.set_state(0.0, state)
+    solver.set_transport(B, D)
+    hr, cs, g_state, g_lnk = solver.adjoint(np.ones(1), np.full(1, 1e3), rho_u, ju, jb, tape_cap=8192)
+    om = OracleMech(mech)
+    R = mech.n_reactions
+
+    def J(st, mult=None):
+        om.set_multipliers(mult)
+        y, _, _, _, status = osplit.split_steps(om, grids, st, 0.0, B, D, dt, 1, BDF, opts)
+        assert (status == 0).all()
+        _, q, c = osplit.objectives(om, grids, y, opts.pressure, opts.kinetics_model, rho_u, ju, jb)
+        return q[0] + 1e3 * c[0]
+
+    # the taped forward step is the oracle's step
+    assert hr[0] + 1e3 * cs[0] == J(state)
+    rng = np.random.default_rng(2024)
+    gmax = np.abs(g_lnk).max()
+    assert gmax > 0
+    for i in rng.choice(R, 20, replace=False):
+        mp, mm = np.ones(R), np.ones(R)
+        mp[i], mm[i] = np.exp(1e-3), np.exp(-1e-3)
+        fd = (J(state, mp) - J(state, mm)) / 2e-3
+        assert abs(g_lnk[i] - fd) <= 2e-3 * abs(fd) + 1e-4 * gmax, (i, g_lnk[i], fd, gmax)
+    om.set_multipliers(None)
+    pts = rng.choice(len(state), 20, replace=False)
+    for p in pts:
+        ks = [1] + [2 + k for k in np.flatnonzero(state[p, 2:] > 1e-6)]
+        k = int(rng.choice(ks))
+        hstep = 1e-4 * abs(state[p, k])
+        e = np.zeros_like(state)
+        e[p, k] = hstep
+        fd = (J(state + e) - J(state - e)) / (2 * hstep)
+        scale = np.abs(g_state[:, k]).max()
+        assert abs(g_state[p, k] - fd) <= 2e-3 * abs(fd) + 1e-4 * scale, (p, k, g_state[p, k], fd, scale)
+
+
+def test_autograd_on_cuda_tensors_matches_the_host_path(gpu_lib):
+    # CUDA inputs stay on the device (multipliers, state, objectives, gradients
+    # through device pointers); the numbers are those of the host path
+    torch = pytest.importorskip("torch")
+    from ember_gb300 import _lib as L
+    from ember_gb300.autograd import split_step_objectives
+    from ember_gb300.source import GpuMechanism
+    from ember_gb300.split import FlameBatchSplitSolver, flame_batch
+    mech = synthetic_mechanism(n_species=20, n_reactions=60, seed=3)
+    grids, state, B, D, rho_u, ju, jb = flame_batch(mech, n_flames=2, n_min=10, n_max=12, seed=5, width=2e-3,
+                                                    thickness=3e-4, T_b=1500.0)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    gm = GpuMechanism(mech)
+    solver = FlameBatchSplitSolver(gm, grids, 1e-6, method=BDF, source_options=opts,
+                                   diffusion_algorithm=L.DIFFUSION_SERIAL)
+    solver.set_transport(B, D)
+    w = np.array([1.0, -0.5, 2e3, 1e3])
+    res = []
+    for dev in ("cpu", "cuda"):
+        s0 = torch.tensor(state, dtype=torch.float64, device=dev, requires_grad=True)
+        lk = torch.zeros(mech.n_reactions, dtype=torch.float64, device=dev, requires_grad=True)
+        out = split_step_objectives(solver, s0, lk, 0.0, rho_u, ju, jb, 4096)
+        assert out.device.type == dev
+        (out * torch.as_tensor(w, device=dev)).sum().backward()
+        assert s0.grad.device.type == dev and lk.grad.device.type == dev
+        res.append((out.detach().cpu().numpy(), s0.grad.cpu().numpy(), lk.grad.cpu().numpy()))
+    for a, b in zip(*res):
+        np.testing.assert_array_equal(a, b)

@@ -414,6 +414,51 @@ def test_split_with_convection_and_transport_model_vs_oracle(gpu_lib, mech, algo
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("bc", ["temperature", "stagnation", "qdot", "right"])
+def test_continuity_point_moves_every_step_like_the_oracle(gpu_lib, mech, bc):
+    # updateContinuityBoundaryCondition at the start of every step after the
+    # first: the continuity point follows the mid-temperature crossing, the
+    # stagnation point of V, the heat-release peak; rV[j_cont] is carried from
+    # the last evaluation (fixedRight, fixedQdot). Start values deliberately
+    # off, so that the update moves them; bitwise against the oracle, stream
+    # launches and graph replay.
+    from oracle.chem import OracleMech
+    from ember_gb300.convection import CONT_QDOT, CONT_RIGHT, CONT_TEMP, CONT_ZERO, ConvectionOptions
+    grids, state, B, D, flames, y_left = _convection_case(mech)
+    for fl, g in zip(flames, grids):
+        N = g.n_points
+        if bc == "temperature":
+            fl.continuity_bc, fl.j_cont = CONT_TEMP, 1
+        elif bc == "stagnation":
+            fl.continuity_bc, fl.j_cont, fl.x_vzero = CONT_ZERO, 2, float(g.x[2])
+        elif bc == "qdot":
+            fl.continuity_bc, fl.j_cont, fl.rv_cont = CONT_QDOT, 1, 0.1
+        else:
+            fl.continuity_bc, fl.j_cont, fl.rv_cont = CONT_RIGHT, N - 1, -0.05
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    dt = 5e-7
+    copts = ConvectionOptions()
+    ref, rt, *_ = osplit.split_steps(OracleMech(mech), grids, state, 0.0, B, D, dt, 3, QSS, opts,
+                                     convection=(flames, y_left, copts))
+    for graph in (False, True):
+        gm, s = _gpu_solver(mech, grids, dt, QSS, opts, L.DIFFUSION_SERIAL)
+        s.set_state(0.0, state)
+        s.set_transport(B, D)
+        s.set_convection(flames, y_left, copts)
+        s.step(3, graph=graph)
+        out, t = s.state()
+        assert t == rt
+        assert np.array_equal(out, ref), (graph, np.abs(out - ref).max())
+    if bc == "temperature":
+        # the start value was not the crossing: the update moved it
+        from copy import copy
+        fl = copy(flames[0])
+        n0 = grids[0].n_points
+        osplit.continuity_point(fl, grids[0].x, state[:n0, 1], None, None, None)
+        assert fl.j_cont != 1
+
+
+@pytest.mark.gpu
 def test_captured_step_survives_a_later_call_for_smaller_flames(gpu_lib, mech):
     # the UTW kernel stages 3N doubles of shared memory per flame; a later
     # convection call for small flames must not lower the kernel's limit
