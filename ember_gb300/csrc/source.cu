@@ -591,10 +591,6 @@ extern "C" int ember_gas_eval(ember_mech m, int n, double pressure, int model, i
 
 namespace ember {
 
-// Thermo and rates of n contiguous states (T [n], Y [n][S] on the device)
-// into caller-provided buffers, with a caller-provided rate-constant cache of
-// gas_eval_cache_doubles(m, n) doubles: no allocation, so it can be captured
-// into a graph.
 // CTAs of the capturable gas evaluation (one rate-constant cache slot each):
 // the same count when the cache is sized and when the kernel is launched.
 static int gas_eval_blocks(int n) {
@@ -605,6 +601,10 @@ static int gas_eval_blocks(int n) {
     return std::max(1, std::min(n, sms * 4));
 }
 
+// Thermo and rates of n contiguous states (T [n], Y [n][S] on the device)
+// into caller-provided buffers, with a caller-provided rate-constant cache of
+// gas_eval_cache_doubles(m, n) doubles: no allocation, so it can be captured
+// into a graph.
 size_t gas_eval_cache_doubles(const MechView& v, int n) {
     return size_t(gas_eval_blocks(n)) * ChemSmem::global_doubles(v);
 }
