@@ -664,6 +664,13 @@ def run_reference_split(args):
     return 0
 
 
+def _flame_ranges(sizes):
+    """(first, end) point of each flame of a batch with these point counts."""
+    import numpy as np
+    off = np.cumsum([0] + list(sizes))
+    return [(int(off[i]), int(off[i + 1])) for i in range(len(sizes))]
+
+
 def run_ours_split(args):
     import ctypes as C
     import numpy as np
@@ -837,6 +844,25 @@ def run_ours_split(args):
             p += b - a
         adaptive = method == BDF or args.convection
         line["parity"] = field_parity(rows, ref_rows, tol if adaptive else None)
+        # the same flames through the serial diffusion algorithm (the reference's sequential
+        # Thomas order): the rest of the step is then bitwise the oracle's
+        ser = FlameBatchSplitSolver(gm, [grids[f] for f in sel], split_dt, method=method, source_options=opts,
+                                    diffusion_algorithm=_lib.DIFFUSION_SERIAL)
+        ser.set_state(0.0, pick(state.reshape(-1), nv).reshape(-1, nv))
+        ser.set_transport(pick(B, nv), pick(D, nv))
+        ser.set_transport_model(gtr, SPLIT_THRESHOLD, cross_terms=True)
+        if args.convection:
+            ser.set_convection([cflames[f] for f in sel], y_left[sel], copts)
+        ser.step(1, graph=False, stream=stream)
+        torch.cuda.synchronize()
+        ser_state, _ = ser.state()
+        ranges = _flame_ranges([grids[f].n_points for f in sel])
+        line["parity"]["serial_diffusion"] = {
+            "n_compared": len(ranges) * nv,
+            "n_bitwise": int(sum(np.array_equal(ser_state[a:b, v], ref_state[a:b, v]) for a, b in ranges
+                                 for v in range(nv))),
+            "max_abs_err": float(np.abs(ser_state - ref_state).max())}
+        del ser
         if args.convection:
             line["parity"]["tolerance"] = ("|error| / (reltol |y| + abstol) with the convection stage's tolerances "
                                            "(reltol 1e-6; abstol 1e-7 U, 1e-8 T, 1e-13 Y): rounding-level "
@@ -845,9 +871,10 @@ def run_ours_split(args):
             line["parity"]["tolerance"] = ("BDF: |error| / (reltol |y| + abstol) with the source options' CVODE "
                                            "tolerances (reltol 1e-6; abstol 1e-7 U, 1e-8 T, 1e-13 Y)")
         line["parity"].update({"flames_compared": sel, "steps": 1,
-                               "note": "warp-parallel diffusion (rounding-level differences from the sequential "
-                                       "order) feeding the source stage; the serial algorithm is bitwise "
-                                       "(tests/test_split.py)"})
+                               "note": "the product path runs warp-parallel diffusion (rounding-level differences "
+                                       "from the sequential order, which the adaptive integrators after it can "
+                                       "amplify up to their tolerances); serial_diffusion: the same flames and step "
+                                       "with the sequential algorithm"})
     return line
 
 

@@ -41,10 +41,11 @@ struct BdfSmem {
     ZArr z;   // Nordsieck array z_0..z_{q+1}
     ZArr zs;  // saved array for step retries
     double *acor, *acorp, *ewt, *y, *ft, *bb, *f0, *ycopy, *f1;
+    double* rdiag;  // 1 / pivot of each column of the LU factors
     int* piv;
     // shared-memory doubles (zs_smem: the saved array in shared memory)
     static __host__ __device__ size_t doubles(int n, bool zs_smem = true) {
-        return size_t(zs_smem ? 2 * kQmax + 3 + 9 : kQmax + 2 + 9) * n + (n + 1) / 2;
+        return size_t(zs_smem ? 2 * kQmax + 3 + 10 : kQmax + 2 + 10) * n + (n + 1) / 2;
     }
     // zs_global: (kQmax + 1) n doubles of global memory for zs, or null
     __device__ void carve(double* base, int n, double* zs_global = nullptr) {
@@ -66,6 +67,7 @@ struct BdfSmem {
         f0 = p; p += n;
         ycopy = p; p += n;
         f1 = p; p += n;
+        rdiag = p; p += n;
         piv = reinterpret_cast<int*>(p);
     }
 };
@@ -99,7 +101,7 @@ struct BdfPoint {
             cachedT = T;
         }
         double rho_c, cp_c;
-        chem_rates<NT>(m, w, a->pressure, STATE_NO_NORM, T, y + 2, rho_c, cp_c, true);
+        chem_rates<NT>(m, w, a->pressure, STATE_NO_NORM, T, y + 2, rho_c, cp_c, true, false);
         const double *wn = w.wn, *hk = w.hk;
         double qd = -block_sum<NT>(w.red, S, [&](int k, double p) { return fma(wn[k], hk[k], p); });
         qd = qd + igniter(*a, t, x);
@@ -278,132 +280,155 @@ struct BdfPoint {
         __syncthreads();
     }
 
-    // LU with partial pivoting of column-major M (first maximum as pivot;
-    // multipliers a_ik * (1/a_kk)). Returns 0, or k+1 when column k has no
-    // usable pivot: all zeros, or a NaN anywhere in it (then no row index is
-    // chosen at all, so nothing is swapped or read out of range).
-    // Partial-pivot search of column k over rows k..n-1: the largest |entry|
-    // (ties to the lowest row); writes v.piv[k]. Returns 0, or k + 1 when the
-    // column holds a NaN or its largest entry is zero (singular).
-    __device__ int lu_pivot(int k, double* sbest, int* sidx, int& s_p, double& s_best) {
-        const int tid = threadIdx.x;
-        const double* colk = M + size_t(k) * n;
-        double best = -1.0;
-        int bi = n;
-        int has_nan = 0;
-        for (int i = k + tid; i < n; i += NT) {
-            const double vv = fabs(colk[i]);
-            if (vv != vv) has_nan = 1;
-            if (vv > best) {
-                best = vv;
-                bi = i;
+    // In-place LU with partial pivoting (CVODE's dense getrf, first maximum
+    // of |a_ik| as pivot, multipliers a_ik * (1/a_kk)): M = P^-1 L U, in
+    // panels of kLuPanel columns with one panel of lookahead. While warp 0
+    // brings the next panel up to date and factors it (its row interchanges
+    // applied to its own columns only), the other warps, and warp 0 when it is
+    // done, apply the current panel's steps to the rest of the trailing matrix;
+    // then every thread applies the next panel's interchanges to the columns
+    // outside it. Each element still receives the one-column algorithm's
+    // operations in its order (an interchange only relabels rows, and the
+    // columns a panel's interchanges reach later have by then received exactly
+    // the updates that preceded the interchange), so the factors are the same
+    // bits. Pivot searches compare |a_ik| through the bit pattern (integer
+    // order = numeric order for doubles with the sign cleared, a NaN above
+    // +inf), which keeps them off the FP64 pipe. Returns 0, or k + 1 when
+    // column k has no usable pivot (all zeros, or a NaN anywhere in it).
+    static constexpr int kLuPanel = 8;
+    static constexpr int kLuGroup = 16;  // trailing columns per task of a warp
+
+    // Panel [k0, k1) by the calling warp alone.
+    __device__ int lu_panel_warp(int k0, int k1) {
+        const int lane = threadIdx.x & 31;
+        const long long kInf = 0x7ff0000000000000LL;
+        for (int c = k0; c < k1; ++c) {
+            double* colc = M + size_t(c) * n;
+            for (int t = k0; t < c; ++t) {
+                const double atc = colc[t];
+                const double* colt = M + size_t(t) * n;
+                for (int i = t + 1 + lane; i < n; i += 32) colc[i] = fma(-colt[i], atc, colc[i]);
+                __syncwarp();
             }
-        }
-#pragma unroll
-        for (int off = 16; off >= 1; off >>= 1) {
-            const double ob = __shfl_xor_sync(0xffffffffu, best, off);
-            const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-            if (ob > best || (ob == best && oi < bi)) {
-                best = ob;
-                bi = oi;
-            }
-        }
-        if (lane_id() == 0) {
-            sbest[tid >> 5] = best;
-            sidx[tid >> 5] = bi;
-        }
-        const int col_nan = __syncthreads_or(has_nan);
-        if (col_nan) return k + 1;
-        if (tid == 0) {
-            double b = sbest[0];
-            int pp = sidx[0];
-            for (int q = 1; q < NT / 32; ++q)
-                if (sbest[q] > b || (sbest[q] == b && sidx[q] < pp)) {
-                    b = sbest[q];
-                    pp = sidx[q];
+            long long best = -1;
+            int bi = n;
+            int has_nan = 0;
+            for (int i = c + lane; i < n; i += 32) {
+                const long long vv = __double_as_longlong(colc[i]) & 0x7fffffffffffffffLL;
+                if (vv > kInf) has_nan = 1;
+                if (vv > best) {
+                    best = vv;
+                    bi = i;
                 }
-            s_p = pp;
-            s_best = b;
-            v.piv[k] = pp;
+            }
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) {
+                const long long ob = __shfl_xor_sync(0xffffffffu, best, off);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+                if (ob > best || (ob == best && oi < bi)) {
+                    best = ob;
+                    bi = oi;
+                }
+            }
+            if (__any_sync(0xffffffffu, has_nan)) return c + 1;
+            if (best == 0) return c + 1;
+            if (lane == 0) v.piv[c] = bi;
+            if (bi != c && lane < k1 - k0) {
+                double* colj = M + size_t(k0 + lane) * n;
+                const double tt = colj[c];
+                colj[c] = colj[bi];
+                colj[bi] = tt;
+            }
+            __syncwarp();
+            const double r = 1.0 / colc[c];
+            if (lane == 0) v.rdiag[c] = r;
+            for (int i = c + 1 + lane; i < n; i += 32) colc[i] = colc[i] * r;
+            __syncwarp();
         }
-        __syncthreads();
-        if (s_best == 0.0) return k + 1;
         return 0;
     }
 
-    // Swap rows k and p over every column.
-    __device__ void lu_swap(int k, int p) {
-        if (p == k) return;
+    // Panel [k, kend)'s steps on columns [j0, j1) (j1 - j0 <= 32) by the
+    // calling warp: the pivot rows k+1..kend-1 (a lane per column, the earlier
+    // panel steps in order), then every other row (lanes over rows, all the
+    // panel's steps in order).
+    __device__ void lu_panel_update(int k, int kend, int j0, int j1) {
+        const int lane = threadIdx.x & 31;
+        if (j0 + lane < j1) {
+            double* colj = M + size_t(j0 + lane) * n;
+            for (int r = k + 1; r < kend; ++r) {
+                double a = colj[r];
+                for (int t = k; t < r; ++t) a = fma(-M[size_t(t) * n + r], colj[t], a);
+                colj[r] = a;
+            }
+        }
+        __syncwarp();
+        for (int j = j0; j < j1; ++j) {
+            double* colj = M + size_t(j) * n;
+            double u[kLuPanel];
+#pragma unroll
+            for (int t = 0; t < kLuPanel; ++t) u[t] = (k + t < kend) ? colj[k + t] : 0.0;
+            for (int i = kend + lane; i < n; i += 32) {
+                double a = colj[i];
+#pragma unroll
+                for (int t = 0; t < kLuPanel; ++t)
+                    if (k + t < kend) a = fma(-M[size_t(k + t) * n + i], u[t], a);
+                colj[i] = a;
+            }
+        }
+        __syncwarp();
+    }
+
+    // The row interchanges of panel [k0, k1), in pivot order, on every column outside it.
+    __device__ void lu_deferred_swaps(int k0, int k1) {
         for (int j = threadIdx.x; j < n; j += NT) {
-            double* a1 = M + size_t(j) * n + k;
-            double* a2 = M + size_t(j) * n + p;
-            const double tt = *a1;
-            *a1 = *a2;
-            *a2 = tt;
+            if (j >= k0 && j < k1) continue;
+            double* colj = M + size_t(j) * n;
+            for (int c = k0; c < k1; ++c) {
+                const int p = v.piv[c];
+                if (p != c) {
+                    const double tt = colj[c];
+                    colj[c] = colj[p];
+                    colj[p] = tt;
+                }
+            }
         }
     }
 
-    // In-place LU with partial pivoting (CVODE's dense getrf): M = P^-1 L U,
-    // kLuPanel columns per pass over the trailing matrix. Within a panel,
-    // column c first receives the multiply-adds of the panel's earlier steps
-    // (in step order), then is pivoted, swapped (whole rows: the updates still
-    // pending for a row go with it) and scaled. After the panel, each pivot
-    // row's trailing entries receive the earlier panel steps in order, and every
-    // other trailing element receives all the panel's steps in order: per
-    // element the operations and their order are those of the one-column
-    // algorithm, so the factors are the same bits. Returns 0 or the 1-based
-    // column found singular.
-    static constexpr int kLuPanel = 8;
     __device__ int lu_factor() {
         const int tid = threadIdx.x;
         const int warp = tid >> 5, lane = tid & 31;
-        __shared__ double sbest[32];
-        __shared__ int sidx[32];
-        __shared__ int s_p;
-        __shared__ double s_best;
-        for (int k = 0; k < n; k += kLuPanel) {
-            const int kend = min(k + kLuPanel, n);
-            for (int c = k; c < kend; ++c) {
-                double* colc = M + size_t(c) * n;
-                for (int t = k; t < c; ++t) {
-                    const double atc = colc[t];
-                    const double* colt = M + size_t(t) * n;
-                    for (int i = t + 1 + tid; i < n; i += NT) colc[i] = fma(-colt[i], atc, colc[i]);
-                    __syncthreads();
-                }
-                const int sing = lu_pivot(c, sbest, sidx, s_p, s_best);
-                if (sing) return sing;
-                lu_swap(c, s_p);
-                __syncthreads();
-                const double r = 1.0 / colc[c];
-                for (int i = c + 1 + tid; i < n; i += NT) colc[i] = colc[i] * r;
-                __syncthreads();
+        __shared__ int s_sing, s_next;
+        const int k1 = min(kLuPanel, n);
+        if (warp == 0) {
+            const int sg = lu_panel_warp(0, k1);
+            if (lane == 0) s_sing = sg;
+        }
+        __syncthreads();
+        if (s_sing) return s_sing;
+        lu_deferred_swaps(0, k1);
+        if (tid == 0) s_next = 0;
+        __syncthreads();
+        for (int k = 0; k + kLuPanel < n; k += kLuPanel) {
+            const int kend = k + kLuPanel;
+            const int k2e = min(kend + kLuPanel, n);
+            if (warp == 0) {
+                lu_panel_update(k, kend, kend, k2e);
+                const int sg = lu_panel_warp(kend, k2e);
+                if (lane == 0) s_sing = sg;
             }
-            if (kend >= n) break;
-            // pivot rows k+1..kend-1 of the trailing columns: the earlier panel steps, in order
-            for (int j = kend + tid; j < n; j += NT) {
-                double* colj = M + size_t(j) * n;
-                for (int r = k + 1; r < kend; ++r) {
-                    double a = colj[r];
-                    for (int t = k; t < r; ++t) a = fma(-M[size_t(t) * n + r], colj[t], a);
-                    colj[r] = a;
-                }
+            for (;;) {
+                int g = 0;
+                if (lane == 0) g = atomicAdd(&s_next, 1);
+                g = __shfl_sync(0xffffffffu, g, 0);
+                const int j0 = k2e + g * kLuGroup;
+                if (j0 >= n) break;
+                lu_panel_update(k, kend, j0, min(j0 + kLuGroup, n));
             }
             __syncthreads();
-            // the other trailing elements: every panel step, in order; one warp per column
-            for (int j = kend + warp; j < n; j += NT / 32) {
-                double* colj = M + size_t(j) * n;
-                double u[kLuPanel];
-#pragma unroll
-                for (int t = 0; t < kLuPanel; ++t) u[t] = (k + t < kend) ? colj[k + t] : 0.0;
-                for (int i = kend + lane; i < n; i += 32) {
-                    double a = colj[i];
-#pragma unroll
-                    for (int t = 0; t < kLuPanel; ++t)
-                        if (k + t < kend) a = fma(-M[size_t(k + t) * n + i], u[t], a);
-                    colj[i] = a;
-                }
-            }
+            if (s_sing) return s_sing;
+            lu_deferred_swaps(kend, k2e);
+            if (tid == 0) s_next = 0;
             __syncthreads();
         }
         return 0;
@@ -417,7 +442,7 @@ struct BdfPoint {
         if (threadIdx.x < 32) {
             const int lane = threadIdx.x;
             for (int k = 0; k < n; ++k) {
-                const double zk = b[k] / M[size_t(k) * n + k];
+                const double zk = b[k] * v.rdiag[k];
                 __syncwarp();
                 if (lane == 0) b[k] = zk;
                 for (int j = k + 1 + lane; j < n; j += 32) b[j] = fma(-M[size_t(j) * n + k], zk, b[j]);
@@ -499,7 +524,7 @@ struct BdfPoint {
             }
             for (int k = n - 1; k >= 0; --k) {
                 const double* colk = M + size_t(k) * n;
-                const double bk = b[k] / colk[k];
+                const double bk = b[k] * v.rdiag[k];
                 __syncwarp();
                 if (lane == 0) b[k] = bk;
                 for (int i = lane; i < k; i += 32) b[i] = fma(-colk[i], bk, b[i]);

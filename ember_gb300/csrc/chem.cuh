@@ -230,8 +230,18 @@ __device__ __forceinline__ int unpack_hi(int v) { return (v >> 16) & 0xffff; }
 template <int NT>
 __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem& w, double T, int use_tables) {
     const int t = threadIdx.x;
-    const double lnT = em_log(T), rT = 1.0 / T;
     const double RT = kGasConstant * T;
+    const bool in_table = use_tables && T >= m.Tmin && T <= m.Tmax;
+    // ln(RT/p0) only for the formulas of 1/Kc (not needed with the tables);
+    // evaluated next to ln T, the two independent chains overlap
+    double lnT, lnRTp = 0.0;
+    if (in_table) {
+        lnT = em_log(T);
+    } else {
+        lnT = em_log(T);
+        lnRTp = em_log(RT / kOneAtm);
+    }
+    const double rT = 1.0 / T;
     for (int k = t; k < m.S; k += NT) {
         const int r = (T <= m.tmid[k]) ? 0 : 1;
         const double* a = m.nasa + 14 * k + 7 * r;
@@ -246,8 +256,6 @@ __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem&
         w.hk[k] = hr * RT;  // updateThermo: h_k [J/kmol]
     }
     __syncthreads();
-    const double lnRTp = em_log(RT / kOneAtm);
-    const bool in_table = use_tables && T >= m.Tmin && T <= m.Tmax;
     int n = 0;
     double dT = 0.0;
     if (in_table) {
@@ -311,10 +319,14 @@ __device__ __forceinline__ void chem_rate_constants(const MechView& m, ChemSmem&
 // Composition part of the state setter (setState_TPY or NoNorm), rates of
 // progress, production rates and thermo outputs at (T, Y). Rate constants
 // must be current for T (chem_rate_constants). Y is in shared memory.
-// Returns rho and cp_mass on every thread. Ends with a barrier.
+// Returns rho and cp_mass on every thread. Ends with a barrier. want_net:
+// also the net production rates (wn); want_qd: the creation and destruction
+// rates (wq, wd). The sums are independent, so skipping one leaves the
+// others' bits unchanged.
 template <int NT>
 __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, double p, int mode, double T,
-                                           const double* Y, double& rho_out, double& cp_out, bool want_net) {
+                                           const double* Y, double& rho_out, double& cp_out, bool want_net,
+                                           bool want_qd = true) {
     const int S = m.S;
     const int t = threadIdx.x;
     if (mode == STATE_NORMALIZED) {
@@ -403,18 +415,24 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
             const int nr = (ent >> 28) & 0xf;
             const double f = w.ropf[i], r = w.ropr[i];
             if (np == 1 && nr == 0) {
-                q = q + f;
-                d = d + r;
+                if (want_qd) {
+                    q = q + f;
+                    d = d + r;
+                }
                 if (want_net) nt = nt + (f - r);
             } else if (np == 0 && nr == 1) {
-                q = q + r;
-                d = d + f;
+                if (want_qd) {
+                    q = q + r;
+                    d = d + f;
+                }
                 if (want_net) nt = nt - (f - r);
             } else {
-                for (int o = 0; o < np; ++o) q = q + f;
-                for (int o = 0; o < nr; ++o) q = q + r;
-                for (int o = 0; o < nr; ++o) d = d + f;
-                for (int o = 0; o < np; ++o) d = d + r;
+                if (want_qd) {
+                    for (int o = 0; o < np; ++o) q = q + f;
+                    for (int o = 0; o < nr; ++o) q = q + r;
+                    for (int o = 0; o < nr; ++o) d = d + f;
+                    for (int o = 0; o < np; ++o) d = d + r;
+                }
                 if (want_net) {
                     const double net = f - r;
                     for (int o = 0; o < np; ++o) nt = nt + net;
@@ -422,8 +440,10 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
                 }
             }
         }
-        w.wq[k] = q;
-        w.wd[k] = d;
+        if (want_qd) {
+            w.wq[k] = q;
+            w.wd[k] = d;
+        }
         if (want_net) w.wn[k] = nt;
     }
     cp_out = (kGasConstant * cpsum) / mmw;

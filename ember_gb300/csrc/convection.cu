@@ -738,10 +738,12 @@ struct UtwSys {
             } else {
                 double r;
                 if (fl->continuity_bc == EMBER_CONTINUITY_TEMP) {
+                    // at the last point (where the per-step update can put the
+                    // temperature crossing) only the backward difference exists
                     const int j = jc;
-                    const double Tj = y[3 * j + 1], Tn = y[3 * (j + 1) + 1];
-                    if (j == 0 || sT[j] / (Tn - Tj) < 0)
-                        r = (((rph[j] * rho[j]) * sT[j]) * hh[j]) / (Tn - Tj);
+                    const double Tj = y[3 * j + 1];
+                    if (j == 0 || (j < jj && sT[j] / (y[3 * (j + 1) + 1] - Tj) < 0))
+                        r = (((rph[j] * rho[j]) * sT[j]) * hh[j]) / (y[3 * (j + 1) + 1] - Tj);
                     else
                         r = (((rph[j - 1] * rho[j]) * sT[j]) * hh[j - 1]) / (Tj - y[3 * (j - 1) + 1]);
                 } else {
@@ -1039,8 +1041,6 @@ int conv_plan_layout(ConvPlan& p, int n_flames, const ember_convection_flame* fl
                         "flame %d: bad continuity boundary condition %d", f, g.continuity_bc);
         EMBER_CHECK_ARG(g.continuity_bc == EMBER_CONTINUITY_LEFT || (g.j_cont >= 0 && g.j_cont < N),
                         "flame %d: j_cont out of range", f);
-        EMBER_CHECK_ARG(g.continuity_bc != EMBER_CONTINUITY_TEMP || g.j_cont < N - 1,
-                        "flame %d: the temperature continuity point needs a right neighbour", f);
         EMBER_CHECK_ARG(g.beta > 0 && g.pressure > 0, "flame %d: beta and pressure must be positive", f);
         EMBER_CHECK_ARG(g.strain_dt >= 0, "flame %d: strain_dt must be >= 0", f);
         ConvFlame& c = p.hf[f];

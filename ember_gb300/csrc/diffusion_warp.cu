@@ -25,25 +25,37 @@
 //    where the reference's own rounding error reaches 1e-11.
 //  * forward sweep d_i = rho_i - alpha_i d_{i-1} and back substitution
 //    y_i = d_i - c'_i y_{i+1} are affine in the value entering the chunk: a
-//    lane sweeps its chunk from zero, a warp scan of the affine maps gives the
+//    lane sweeps its chunk from zero, a scan of the affine maps gives the
 //    entering values, and the next pass adds G_i * carry (forward) or
 //    H_i * carry (backward), G and H being the chunk's running products of
 //    -alpha and -c'. That correction rides along with the following sweep, so
 //    a sub-step is two passes over the chunk and five FP64 operations a point.
 //
-// FP64 throughput, not memory, bounds this kernel on GB300 (about 2 FP64
-// lanes per clock per SM), so the work per point is kept small: the geometric
-// factors of the rows (0.5 / (dlj r^alpha) and r_{j+1/2}^alpha / hh) are
-// computed once per grid point and shared by the variables of a flame; 1/den
-// is computed once per factorisation and folded into alpha = a/den,
-// c' = c/den, e = -s/den and kappa = -k/den; a sub-step then costs one fma
-// for the right-hand side, one per sweep and one per carry correction.
+// FP64 throughput bounds this kernel on GB300: each SM sub-partition issues
+// one FP64 warp instruction per 64 cycles whatever the number of active lanes
+// (about 1.7 FP64 lanes per clock per SM), so the work per point is kept
+// small: the geometric factors of the rows (0.5 / (dlj r^alpha) and
+// r_{j+1/2}^alpha / hh) are computed once per grid point and shared by the
+// variables of a flame; 1/den is computed once per factorisation and folded
+// into alpha = a/den, c' = c/den, e = -s/den and kappa = -k/den; a sub-step
+// then costs one fma for the right-hand side, one per sweep and one per carry
+// correction.
 //
-// Workspace: per system, ceil(N/32) rows of 8 slots x 32 lanes (alpha, c', e,
-// kappa, G, H, state, y_prev), point j of lane l at row j, so that the 32
-// lanes of a warp touch one contiguous 256-byte segment per slot. A
-// persistent grid (a few warps per SM) takes systems largest first from an
-// atomic counter, which keeps the live workspace inside L2.
+// Lane groups: a system of N points is split over G = 1, 2, 4 or 8 warps (the
+// fewest that give each lane at most kPointsPerLane points), so that a lane's
+// chunk, its sequential chain and the scan overhead per point stay about the
+// same for every N. The warps of a group combine their scans through shared
+// memory and a named barrier (bar.sync 1+group, 32 G threads). A CTA of eight
+// warps takes one task at a time from an atomic counter: one system of eight
+// warps, or two of four, four of two, eight of one, largest systems first.
+// With short chunks the live workspace of the resident warps (about
+// kPointsPerLane x 64 bytes per lane) stays inside L2, which the 16 passes
+// over it per stage need: with one warp per system the chunks of the largest
+// systems were 125 points long and the live workspace spilled to DRAM.
+//
+// Workspace: per system, m = ceil(N / 32G) rows of 8 slots x 32G lanes
+// (alpha, c', e, kappa, G, H, state, y_prev), point j of a lane at row j, so
+// that the 32 lanes of a warp touch one contiguous 256-byte segment per slot.
 #include "common.cuh"
 #include "tridiag.cuh"
 
@@ -58,12 +70,15 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kSlots = 8;
+constexpr int kCtaWarps = 8;  // warps per CTA (one task)
+constexpr int kTaskInts = 1 + kCtaWarps;
 enum : int { S_ALPHA = 0, S_CP = 1, S_E = 2, S_KAPPA = 3, S_G = 4, S_H = 5, S_W = 6, S_YP = 7 };
 
 struct WarpDiffView {
     int n_systems;
+    int n_tasks;
     const DiffSysInfo* info;
-    const int* order;         // systems, largest first
+    const int* tasks;         // [n_tasks][1 + kCtaWarps]: G, then 8/G systems (-1: none), largest first
     const int64_t* ws_off;    // first workspace double of each system
     const double* x;
     const double2* geo;       // per grid point: (0.5 / (dlj r^alpha), r_{j+1/2}^alpha / hh)
@@ -117,13 +132,33 @@ __device__ __forceinline__ void normalize(double& m11, double& m12, double& m21,
 __device__ __forceinline__ double shfl_up(double v, int o) { return __shfl_up_sync(kFull, v, o); }
 __device__ __forceinline__ double shfl_down(double v, int o) { return __shfl_down_sync(kFull, v, o); }
 
-// One system as seen by one lane.
+// One system as seen by one lane of its group.
 struct LaneChunk {
     int N, i0, cnt;       // global index of the chunk's first point, points in the chunk
+    int stride;           // lanes of the group (32 G)
     int64_t base;         // workspace offset of row 0, this lane
     __device__ double& at(double* ws, int j, int slot) const {
-        return ws[base + (int64_t(j) * kSlots + slot) * 32];
+        return ws[base + (int64_t(j) * kSlots + slot) * stride];
     }
+};
+
+// The warps of one system. Shared memory: 8 doubles per warp of the CTA,
+// sh[w * 8 + ...]: [0..3] chunk-matrix totals and reductions, [4] forward
+// totals, [5] backward totals, [6] forward slope total, [7] backward slope
+// total of warp w.
+struct Group {
+    int G;       // warps
+    int wl;      // this warp's index in the group
+    int lane;
+    int w0;      // the group's first warp in the CTA
+    int bar;     // named barrier id
+    double* sh;  // the CTA's shared slots
+    __device__ void sync() const {
+        if (G > 1) asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(G * 32) : "memory");
+        else __syncwarp();
+    }
+    __device__ double* slot(int j) const { return sh + (w0 + j) * 8; }
+    __device__ double* mine() const { return slot(wl); }
 };
 
 // Row i of A and k_i as (a_i, c_i, x_i = -(a_i + b_i + c_i), k_i): interior
@@ -202,15 +237,23 @@ __device__ void rows_and_moebius(const RowCtx& r, const LaneChunk& ch, double* w
     normalize(m11, m12, m21, m22);
 }
 
-// Factorisation of (A - shift I) for one warp; srhs is the factor of y in the
+// The carried scan coefficients of a factorisation: per level the slope
+// before it (warp Kogge-Stone), and the lane's inclusive slopes from the
+// warp's start (forward) and to the warp's end (backward).
+struct ScanCoef {
+    double pf[5], pb[5];
+    double pin, qin;
+};
+
+// Factorisation of (A - shift I) for one group; srhs is the factor of y in the
 // right-hand side (-8/h for BDF1 sub-steps, -2/h for BDF2). Leaves alpha, c',
-// e, kappa, G, H in the workspace and returns the scan coefficients of the
-// forward (pf) and backward (pb) affine maps.
-__device__ void factorize(const RowCtx& r, const LaneChunk& ch, double* ws, int lane, double shift, double srhs,
-                          double (&pf)[5], double (&pb)[5]) {
+// e, kappa, G, H in the workspace and returns the scan coefficients.
+__device__ void factorize(const RowCtx& r, const LaneChunk& ch, double* ws, const Group& gr, double shift,
+                          double srhs, ScanCoef& sc) {
+    const int lane = gr.lane;
     double m11, m12, m21, m22;
     rows_and_moebius(r, ch, ws, shift, m11, m12, m21, m22);
-    // Inclusive scan of the chunk matrices, later chunks on the left.
+    // Inclusive scan of the chunk matrices over the warp, later chunks on the left.
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const double u11 = shfl_up(m11, o), u12 = shfl_up(m12, o), u21 = shfl_up(m21, o), u22 = shfl_up(m22, o);
@@ -224,10 +267,50 @@ __device__ void factorize(const RowCtx& r, const LaneChunk& ch, double* ws, int 
             normalize(m11, m12, m21, m22);
         }
     }
-    // u entering the chunk: the exclusive prefix applied to u = 1 (lu_c = 0).
-    const double e11 = shfl_up(m11, 1), e12 = shfl_up(m12, 1);
-    const double e21 = shfl_up(m21, 1), e22 = shfl_up(m22, 1);
-    double u = lane == 0 ? 1.0 : (e11 + e12) / (e21 + e22);
+    // Product of the earlier warps' totals, E = T_{wl-1} ... T_0.
+    double e11 = 1.0, e12 = 0.0, e21 = 0.0, e22 = 1.0;
+    if (gr.G > 1) {
+        if (lane == 31) {
+            double* q = gr.mine();
+            q[0] = m11;
+            q[1] = m12;
+            q[2] = m21;
+            q[3] = m22;
+        }
+        gr.sync();
+        for (int j = 0; j < gr.wl; ++j) {
+            const double* q = gr.slot(j);
+            const double r11 = fma(q[0], e11, q[1] * e21), r12 = fma(q[0], e12, q[1] * e22);
+            const double r21 = fma(q[2], e11, q[3] * e21), r22 = fma(q[2], e12, q[3] * e22);
+            e11 = r11;
+            e12 = r12;
+            e21 = r21;
+            e22 = r22;
+            normalize(e11, e12, e21, e22);
+        }
+    }
+    // u entering the chunk: the exclusive prefix (the previous lane's
+    // inclusive product times E; E alone for lane 0) applied to u = 1.
+    double x11 = shfl_up(m11, 1), x12 = shfl_up(m12, 1);
+    double x21 = shfl_up(m21, 1), x22 = shfl_up(m22, 1);
+    double p11, p12, p21, p22;
+    if (lane == 0) {
+        p11 = e11;
+        p12 = e12;
+        p21 = e21;
+        p22 = e22;
+    } else if (gr.wl == 0) {
+        p11 = x11;
+        p12 = x12;
+        p21 = x21;
+        p22 = x22;
+    } else {
+        p11 = fma(x11, e11, x12 * e21);
+        p12 = fma(x11, e12, x12 * e22);
+        p21 = fma(x21, e11, x22 * e21);
+        p22 = fma(x21, e12, x22 * e22);
+    }
+    double u = (lane == 0 && gr.wl == 0) ? 1.0 : (p11 + p12) / (p21 + p22);
 
     // Pass F: the recurrence itself, with the per-point coefficients.
     double G = 1.0;
@@ -256,11 +339,22 @@ __device__ void factorize(const RowCtx& r, const LaneChunk& ch, double* ws, int 
     double P = G, Q = H;
 #pragma unroll
     for (int lev = 0, o = 1; lev < 5; ++lev, o <<= 1) {
-        pf[lev] = P;
-        pb[lev] = Q;
+        sc.pf[lev] = P;
+        sc.pb[lev] = Q;
         const double tp = shfl_up(P, o), tq = shfl_down(Q, o);
         if (lane >= o) P *= tp;
         if (lane + o < 32) Q *= tq;
+    }
+    sc.pin = P;
+    sc.qin = Q;
+    if (gr.G > 1) {
+        // the warp's slope totals for the other warps' carries (read after
+        // the next sub-step's barrier)
+        const double pt = __shfl_sync(kFull, P, 31), qt = __shfl_sync(kFull, Q, 0);
+        if (lane == 0) {
+            gr.mine()[6] = pt;
+            gr.mine()[7] = qt;
+        }
     }
 }
 
@@ -268,8 +362,9 @@ __device__ void factorize(const RowCtx& r, const LaneChunk& ch, double* ws, int 
 // holds the back substitution of the previous sub-step without its carry,
 // i.e. y_j = state_j + H_j * cb; on exit likewise with the new cb.
 template <bool kBdf2>
-__device__ __forceinline__ void substep(const LaneChunk& ch, double* ws, int lane, const double (&pf)[5],
-                                        const double (&pb)[5], double& cb) {
+__device__ __forceinline__ void substep(const LaneChunk& ch, double* ws, const Group& gr, const ScanCoef& sc,
+                                        double& cb) {
+    const int lane = gr.lane;
     double d = 0.0;
 #pragma unroll 4
     for (int j = 0; j < ch.cnt; ++j) {
@@ -286,10 +381,17 @@ __device__ __forceinline__ void substep(const LaneChunk& ch, double* ws, int lan
 #pragma unroll
     for (int lev = 0, o = 1; lev < 5; ++lev, o <<= 1) {
         const double t = shfl_up(d, o);
-        if (lane >= o) d = fma(pf[lev], t, d);
+        if (lane >= o) d = fma(sc.pf[lev], t, d);
+    }
+    double cw = 0.0;  // value entering the warp
+    if (gr.G > 1) {
+        if (lane == 31) gr.mine()[4] = d;
+        gr.sync();
+        for (int j = 0; j < gr.wl; ++j) cw = fma(gr.slot(j)[6], cw, gr.slot(j)[4]);
+        d = fma(sc.pin, cw, d);
     }
     double cf = shfl_up(d, 1);
-    if (lane == 0) cf = 0.0;
+    if (lane == 0) cf = cw;
     double yv = 0.0;
 #pragma unroll 4
     for (int j = ch.cnt - 1; j >= 0; --j) {
@@ -300,10 +402,17 @@ __device__ __forceinline__ void substep(const LaneChunk& ch, double* ws, int lan
 #pragma unroll
     for (int lev = 0, o = 1; lev < 5; ++lev, o <<= 1) {
         const double t = shfl_down(yv, o);
-        if (lane + o < 32) yv = fma(pb[lev], t, yv);
+        if (lane + o < 32) yv = fma(sc.pb[lev], t, yv);
+    }
+    double cr = 0.0;  // value entering the warp from the right
+    if (gr.G > 1) {
+        if (lane == 0) gr.mine()[5] = yv;
+        gr.sync();
+        for (int j = gr.G - 1; j > gr.wl; --j) cr = fma(gr.slot(j)[7], cr, gr.slot(j)[5]);
+        yv = fma(sc.qin, cr, yv);
     }
     cb = shfl_down(yv, 1);
-    if (lane == 31) cb = 0.0;
+    if (lane == 31) cb = cr;
 }
 
 __device__ __forceinline__ void apply_carry(const LaneChunk& ch, double* ws, double& cb) {
@@ -311,157 +420,239 @@ __device__ __forceinline__ void apply_carry(const LaneChunk& ch, double* ws, dou
     cb = 0.0;
 }
 
-__global__ void __launch_bounds__(128) k_diffusion_warp(WarpDiffView v) {
-    const int lane = threadIdx.x & 31;
-    for (;;) {
-        unsigned int next = 0;
-        if (lane == 0) next = atomicAdd(v.counter, 1u);
-        next = __shfl_sync(kFull, next, 0);
-        if (next >= static_cast<unsigned int>(v.n_systems)) return;
-        const int s = v.order[next];
-        const DiffSysInfo info = v.info[s];
-        const int N = info.n;
-        const int m = (N + 31) / 32;
-        LaneChunk ch;
-        ch.N = N;
-        ch.i0 = min(lane * m, N);
-        ch.cnt = min(N - ch.i0, m);
-        ch.base = v.ws_off[s] + lane;
+// One system by one group of warps.
+__device__ void run_system(const WarpDiffView& v, int s, const Group& gr) {
+    const int lane = gr.lane;
+    const DiffSysInfo info = v.info[s];
+    const int N = info.n;
+    const int L = 32 * gr.G;
+    const int gl = gr.wl * 32 + lane;
+    const int m = (N + L - 1) / L;
+    LaneChunk ch;
+    ch.N = N;
+    ch.i0 = min(gl * m, N);
+    ch.cnt = min(N - ch.i0, m);
+    ch.stride = L;
+    ch.base = v.ws_off[s] + gl;
 
-        RowCtx r;
-        r.N = N;
-        r.alpha = info.alpha;
-        r.left_bc = info.left_bc;
-        r.right_bc = info.right_bc;
-        r.x = v.x + info.grid_off;
-        r.geo = v.geo + info.grid_off;
-        r.B = v.B + info.off;
-        r.D = v.D + info.off;
-        r.S = v.split_const ? v.split_const + info.off : nullptr;
-        r.wall_const = v.wall_const ? v.wall_const[s] : 0.0;
-        r.y_inf = v.y_inf ? v.y_inf[s] : 0.0;
+    RowCtx r;
+    r.N = N;
+    r.alpha = info.alpha;
+    r.left_bc = info.left_bc;
+    r.right_bc = info.right_bc;
+    r.x = v.x + info.grid_off;
+    r.geo = v.geo + info.grid_off;
+    r.B = v.B + info.off;
+    r.D = v.D + info.off;
+    r.S = v.split_const ? v.split_const + info.off : nullptr;
+    r.wall_const = v.wall_const ? v.wall_const[s] : 0.0;
+    r.y_inf = v.y_inf ? v.y_inf[s] : 0.0;
 
-        // Step size: explicit, or min(mult * min_j dlj^2 / (B_j D_j), gdt)
-        // with the reference's rounding (a minimum does not depend on order).
-        double h;
-        if (v.h) {
-            h = v.h[s];
-        } else {
-            double mn = 0.0;
-            bool have = false;
-            for (int j = 0; j < ch.cnt; ++j) {
-                const int i = ch.i0 + j;
-                if (i < 1 || i > N - 2) continue;
-                const double dlj = __dmul_rn(0.5, __dsub_rn(r.x[i + 1], r.x[i - 1]));
-                const double q = __ddiv_rn(__dmul_rn(dlj, dlj), __dmul_rn(r.B[i], r.D[i]));
-                if (!have || q < mn) mn = q;
-                have = true;
-            }
+    // Step size: explicit, or min(mult * min_j dlj^2 / (B_j D_j), gdt)
+    // with the reference's rounding (a minimum does not depend on order).
+    double h;
+    if (v.h) {
+        h = v.h[s];
+    } else {
+        double mn = 0.0;
+        bool have = false;
+        for (int j = 0; j < ch.cnt; ++j) {
+            const int i = ch.i0 + j;
+            if (i < 1 || i > N - 2) continue;
+            const double dlj = __dmul_rn(0.5, __dsub_rn(r.x[i + 1], r.x[i - 1]));
+            const double q = __ddiv_rn(__dmul_rn(dlj, dlj), __dmul_rn(r.B[i], r.D[i]));
+            if (!have || q < mn) mn = q;
+            have = true;
+        }
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const double t = __shfl_xor_sync(kFull, mn, o);
-                const bool th = __shfl_xor_sync(kFull, have, o);
+        for (int o = 16; o > 0; o >>= 1) {
+            const double t = __shfl_xor_sync(kFull, mn, o);
+            const bool th = __shfl_xor_sync(kFull, have, o);
+            if (th && (!have || t < mn)) mn = t;
+            have = have || th;
+        }
+        if (gr.G > 1) {
+            if (lane == 0) {
+                gr.mine()[0] = mn;
+                gr.mine()[1] = have ? 1.0 : 0.0;
+            }
+            gr.sync();
+            for (int j = 0; j < gr.G; ++j) {
+                const double t = gr.slot(j)[0];
+                const bool th = gr.slot(j)[1] != 0.0;
                 if (th && (!have || t < mn)) mn = t;
                 have = have || th;
             }
-            const double hm = __dmul_rn(v.mult, mn);
-            h = v.gdt < hm ? v.gdt : hm;
+            gr.sync();  // the slots are reused by the factorisation
         }
-        // Integrator::integrateToTime step rounding.
-        double t0, t1;
-        v.tm.get(t0, t1);
-        const double q = __dadd_rn(__ddiv_rn(__dsub_rn(t1, t0), h), 1e-5);
-        if (!(h > 0.0) || !(q < 2147483647.0)) {
-            if (lane == 0 && v.status) v.status[s] = TRI_BAD_STEP;
-            continue;
-        }
-        const int n_steps = q >= 1.0 ? static_cast<int>(q) : 1;
-        h = __ddiv_rn(__dsub_rn(t1, t0), static_cast<double>(n_steps));
+        const double hm = __dmul_rn(v.mult, mn);
+        h = v.gdt < hm ? v.gdt : hm;
+    }
+    // Integrator::integrateToTime step rounding.
+    double t0, t1;
+    v.tm.get(t0, t1);
+    const double q = __dadd_rn(__ddiv_rn(__dsub_rn(t1, t0), h), 1e-5);
+    if (!(h > 0.0) || !(q < 2147483647.0)) {
+        if (gl == 0 && v.status) v.status[s] = TRI_BAD_STEP;
+        return;
+    }
+    const int n_steps = q >= 1.0 ? static_cast<int>(q) : 1;
+    h = __ddiv_rn(__dsub_rn(t1, t0), static_cast<double>(n_steps));
 
-        double* y = v.y + info.off;
-        for (int j = 0; j < ch.cnt; ++j) {
-            const double y0 = y[ch.i0 + j];
-            ch.at(v.ws, j, S_W) = y0;
-            if (n_steps > 1) ch.at(v.ws, j, S_YP) = y0;
+    double* y = v.y + info.off;
+    for (int j = 0; j < ch.cnt; ++j) {
+        const double y0 = y[ch.i0 + j];
+        ch.at(v.ws, j, S_W) = y0;
+        if (n_steps > 1) ch.at(v.ws, j, S_YP) = y0;
+    }
+    ScanCoef sc;
+    double cb = 0.0;
+    // First step: 8 BDF1 sub-steps of h/8 with one factorisation.
+    factorize(r, ch, v.ws, gr, 8.0 / h, -8.0 / h, sc);
+    for (int sub = 0; sub < 8; ++sub) substep<false>(ch, v.ws, gr, sc, cb);
+    // Later steps: BDF2 with (A - 3/(2h) I).
+    if (n_steps > 1) {
+        apply_carry(ch, v.ws, cb);
+        factorize(r, ch, v.ws, gr, 1.5 / h, -2.0 / h, sc);
+        for (int step = 1; step < n_steps; ++step) substep<true>(ch, v.ws, gr, sc, cb);
+    }
+    bool finite = true;
+    for (int j = 0; j < ch.cnt; ++j) {
+        const double yv = fma(ch.at(v.ws, j, S_H), cb, ch.at(v.ws, j, S_W));
+        y[ch.i0 + j] = yv;
+        finite = finite && isfinite(yv);
+    }
+    bool all_finite = __all_sync(kFull, finite);
+    if (gr.G > 1) {
+        if (lane == 0) gr.mine()[4] = all_finite ? 1.0 : 0.0;
+        gr.sync();
+        for (int j = 0; j < gr.G; ++j) all_finite = all_finite && gr.slot(j)[4] != 0.0;
+    }
+    if (gl == 0 && v.status) v.status[s] = all_finite ? TRI_OK : TRI_NONFINITE;
+}
+
+__global__ void __launch_bounds__(32 * kCtaWarps, 2) k_diffusion_warp(const __grid_constant__ WarpDiffView v) {
+    __shared__ double sh[kCtaWarps * 8];
+    __shared__ int s_task;
+    const int warp = threadIdx.x >> 5;
+    for (;;) {
+        if (threadIdx.x == 0) s_task = static_cast<int>(atomicAdd(v.counter, 1u));
+        __syncthreads();
+        const int task = s_task;
+        if (task >= v.n_tasks) return;
+        const int* t = v.tasks + int64_t(task) * kTaskInts;
+        const int G = t[0];
+        const int g = warp / G;
+        const int s = t[1 + g];
+        if (s >= 0) {
+            Group gr;
+            gr.G = G;
+            gr.wl = warp - g * G;
+            gr.lane = threadIdx.x & 31;
+            gr.w0 = g * G;
+            gr.bar = 1 + g;
+            gr.sh = sh;
+            run_system(v, s, gr);
         }
-        double pf[5], pb[5];
-        double cb = 0.0;
-        // First step: 8 BDF1 sub-steps of h/8 with one factorisation.
-        factorize(r, ch, v.ws, lane, 8.0 / h, -8.0 / h, pf, pb);
-        for (int sub = 0; sub < 8; ++sub) substep<false>(ch, v.ws, lane, pf, pb, cb);
-        // Later steps: BDF2 with (A - 3/(2h) I).
-        if (n_steps > 1) {
-            apply_carry(ch, v.ws, cb);
-            factorize(r, ch, v.ws, lane, 1.5 / h, -2.0 / h, pf, pb);
-            for (int step = 1; step < n_steps; ++step) substep<true>(ch, v.ws, lane, pf, pb, cb);
-        }
-        bool finite = true;
-        for (int j = 0; j < ch.cnt; ++j) {
-            const double yv = fma(ch.at(v.ws, j, S_H), cb, ch.at(v.ws, j, S_W));
-            y[ch.i0 + j] = yv;
-            finite = finite && isfinite(yv);
-        }
-        const bool all_finite = __all_sync(kFull, finite);
-        if (lane == 0 && v.status) v.status[s] = all_finite ? TRI_OK : TRI_NONFINITE;
+        __syncthreads();  // every group done with the shared slots and s_task
     }
 }
 
-// Resident warps per SM of the persistent grid (EMBER_DIFFUSION_WARPS_PER_SM
-// overrides). Fewer warps keep more of the workspace in L2, more warps hide
-// more latency; on the 64-flame, 55-variable batch (N 100-4000) 12 was best.
-int warps_per_sm() {
-    static int w = [] {
-        const char* e = std::getenv("EMBER_DIFFUSION_WARPS_PER_SM");
-        int v = e ? std::atoi(e) : 0;
-        return (v >= 1 && v <= 64) ? v : 12;  // 4: 3.22 ms, 8: 2.24, 12: 1.75, 16: 1.83 on the 64-flame batch
-    }();
-    return w;
+// Tuning knobs (environment, read once): EMBER_DIFFUSION_POINTS_PER_LANE
+// (chunk length that sets the group size; default 24) and
+// EMBER_DIFFUSION_CTAS_PER_SM (resident CTAs of eight warps; default 2).
+int env_int(const char* name, int lo, int hi, int dflt) {
+    const char* e = std::getenv(name);
+    const int v = e ? std::atoi(e) : 0;
+    return (v >= lo && v <= hi) ? v : dflt;
+}
+int points_per_lane() {
+    static int p = env_int("EMBER_DIFFUSION_POINTS_PER_LANE", 1, 4096, 24);
+    return p;
+}
+int ctas_per_sm() {
+    static int c = env_int("EMBER_DIFFUSION_CTAS_PER_SM", 1, 8, 2);
+    return c;
+}
+
+// Warps of the group of a system of n points.
+int group_warps(int n) {
+    const int per_warp = 32 * points_per_lane();
+    const int need = (n + per_warp - 1) / per_warp;
+    return need <= 1 ? 1 : need <= 2 ? 2 : need <= 4 ? 4 : kCtaWarps;
+}
+
+int64_t system_doubles(int n) {
+    const int L = 32 * group_warps(n);
+    return int64_t(kSlots) * L * ((n + L - 1) / L);
+}
+
+// Tasks, largest systems first: per group size, systems by descending n,
+// 8/G to a task.
+std::vector<int> make_tasks(const std::vector<DiffSysInfo>& info) {
+    const int n_sys = static_cast<int>(info.size());
+    std::vector<int> order(n_sys);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return info[a].n > info[b].n; });
+    std::vector<int> tasks;
+    int cur_g = 0, filled = 0;
+    for (int s : order) {
+        const int G = group_warps(info[s].n);
+        if (G != cur_g || filled == kCtaWarps / G) {
+            tasks.push_back(G);
+            for (int k = 0; k < kCtaWarps; ++k) tasks.push_back(-1);
+            cur_g = G;
+            filled = 0;
+        }
+        tasks[tasks.size() - kCtaWarps + filled] = s;
+        ++filled;
+    }
+    return tasks;
 }
 
 }  // namespace
 
 size_t diffusion_warp_plan_bytes(const std::vector<DiffSysInfo>& info, int64_t n_pts) {
     int64_t total = 0;
-    for (const DiffSysInfo& d : info) total += int64_t(kSlots) * 32 * ((d.n + 31) / 32);
+    for (const DiffSysInfo& d : info) total += system_doubles(d.n);
     const size_t n_sys = info.size();
+    const size_t n_task_ints = make_tasks(info).size();
     return Scratch::rounded(sizeof(double) * size_t(total)) + Scratch::rounded(sizeof(double2) * size_t(n_pts)) +
-           Scratch::rounded(sizeof(int64_t) * n_sys) + Scratch::rounded(sizeof(int) * n_sys) +
+           Scratch::rounded(sizeof(int64_t) * n_sys) + Scratch::rounded(sizeof(int) * n_task_ints) +
            Scratch::rounded(sizeof(unsigned int));
 }
 
 int diffusion_warp_plan_init(DiffusionWarpPlan* p, const std::vector<DiffSysInfo>& info, int n_flames, int n_vars,
                              int64_t n_pts, Scratch& sc, cudaStream_t st) {
     const int n_sys = static_cast<int>(info.size());
-    // Workspace offsets and the largest-first order.
     std::vector<int64_t> off(n_sys);
     int64_t total = 0;
     int nmax = 0;
     for (int s = 0; s < n_sys; ++s) {
         off[s] = total;
-        total += int64_t(kSlots) * 32 * ((info[s].n + 31) / 32);
+        total += system_doubles(info[s].n);
         nmax = std::max(nmax, info[s].n);
     }
-    std::vector<int> order(n_sys);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return info[a].n > info[b].n; });
+    const std::vector<int> tasks = make_tasks(info);
 
     p->n_sys = n_sys;
     p->n_flames = n_flames;
     p->n_vars = n_vars;
     p->n_pts = n_pts;
     p->nmax = nmax;
+    p->n_tasks = static_cast<int>(tasks.size() / kTaskInts);
     EMBER_TRY(sc.alloc(&p->ws, size_t(total)));
     EMBER_TRY(sc.alloc(&p->geo, size_t(n_pts)));
     EMBER_TRY(sc.alloc(&p->ws_off, size_t(n_sys)));
-    EMBER_TRY(sc.alloc(&p->order, size_t(n_sys)));
+    EMBER_TRY(sc.alloc(&p->tasks, tasks.size()));
     EMBER_TRY(sc.alloc(&p->counter, 1));
     EMBER_CUDA_TRY(cudaMemcpyAsync(p->ws_off, off.data(), sizeof(int64_t) * n_sys, cudaMemcpyHostToDevice, st));
-    EMBER_CUDA_TRY(cudaMemcpyAsync(p->order, order.data(), sizeof(int) * n_sys, cudaMemcpyHostToDevice, st));
+    EMBER_CUDA_TRY(cudaMemcpyAsync(p->tasks, tasks.data(), sizeof(int) * tasks.size(), cudaMemcpyHostToDevice, st));
 
     int dev = 0, sms = 0;
     EMBER_CUDA_TRY(cudaGetDevice(&dev));
     EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    p->warps = std::min<int64_t>(n_sys, int64_t(sms) * warps_per_sm());
+    p->blocks = static_cast<int>(std::min<int64_t>(p->n_tasks, int64_t(sms) * ctas_per_sm()));
     return EMBER_OK;
 }
 
@@ -474,11 +665,13 @@ int diffusion_warp_geometry(const DiffusionWarpPlan& p, const DiffSysInfo* d_inf
 
 int diffusion_warp_run(const DiffusionWarpPlan& p, const DiffusionView& dv, double* y, const StageTime& tm,
                        double mult, double gdt, cudaStream_t st) {
+    if (p.n_tasks == 0) return EMBER_OK;
     EMBER_CUDA_TRY(cudaMemsetAsync(p.counter, 0, sizeof(unsigned int), st));
     WarpDiffView v;
     v.n_systems = p.n_sys;
+    v.n_tasks = p.n_tasks;
     v.info = dv.info;
-    v.order = p.order;
+    v.tasks = p.tasks;
     v.ws_off = p.ws_off;
     v.x = dv.x;
     v.geo = p.geo;
@@ -495,7 +688,7 @@ int diffusion_warp_run(const DiffusionWarpPlan& p, const DiffusionView& dv, doub
     v.tm = tm;
     v.mult = mult;
     v.gdt = gdt;
-    k_diffusion_warp<<<blocks_for(p.warps * 32, 128), 128, 0, st>>>(v);
+    k_diffusion_warp<<<p.blocks, 32 * kCtaWarps, 0, st>>>(v);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }

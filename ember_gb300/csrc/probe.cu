@@ -1,7 +1,12 @@
 // Device throughput probes used as roofline denominators: the FP64 FMA pipe
-// (DFMA) and the FP64 tensor path (DMMA m8n8k4). Both run a fixed amount of
-// independent work on every SM and are timed with CUDA events.
+// (DFMA) and the FP64 tensor path (DMMA m8n8k4), both run as a fixed amount
+// of independent work on every SM and timed with CUDA events; and the issue
+// cost of single FP64 warp instructions (clock64 per CTA), which shows how
+// the pipe is shared between warps and lanes.
 #include "common.cuh"
+
+#include <algorithm>
+#include <vector>
 
 namespace ember {
 
@@ -34,9 +39,88 @@ __global__ void k_probe_dmma(double* out, int iters) {
     if (c0 + c1 + c2 + c3 == 1234.5) out[0] = c0;
 }
 
+// Issue cost of FP64 warp instructions: one CTA of `warps` warps per SM,
+// lanes below `active` running `iters` x CHAINS operations (MODE 0: DFMA,
+// 1: DADD, 2: DMUL, 3: division), clocked per CTA with clock64.
+template <int CHAINS, int MODE>
+__global__ void k_probe_issue(double* sink, long long* cyc, int iters, int active) {
+    const int lane = threadIdx.x & 31;
+    double acc[CHAINS];
+#pragma unroll
+    for (int c = 0; c < CHAINS; ++c) acc[c] = 1.0 + threadIdx.x * 1e-3 + c;
+    const double s = 0.999999;
+    __syncthreads();
+    long long t0;
+    asm volatile("mov.u64 %0, %%clock64;" : "=l"(t0));
+    if (lane < active) {
+        for (int i = 0; i < iters; ++i) {
+#pragma unroll
+            for (int c = 0; c < CHAINS; ++c) {
+                if (MODE == 0) acc[c] = fma(acc[c], s, 0.25);
+                else if (MODE == 1) acc[c] = acc[c] + s;
+                else if (MODE == 2) acc[c] = acc[c] * s;
+                else acc[c] = s / acc[c];
+            }
+        }
+    }
+    __syncthreads();
+    long long t1;
+    asm volatile("mov.u64 %0, %%clock64;" : "=l"(t1));
+    double r = 0.0;
+#pragma unroll
+    for (int c = 0; c < CHAINS; ++c) r += acc[c];
+    if (r == 1234.5) sink[0] = r;
+    if (threadIdx.x == 0) cyc[blockIdx.x] = t1 - t0;
+}
+
 }  // namespace ember
 
 using namespace ember;
+
+extern "C" int ember_probe_fp64_issue(int op, int chains, int warps, int active_lanes, double* cycles_per_inst) {
+    EMBER_CHECK_ARG(cycles_per_inst != nullptr, "null output");
+    EMBER_CHECK_ARG(op >= 0 && op <= 3, "op must be 0 (DFMA), 1 (DADD), 2 (DMUL) or 3 (division)");
+    EMBER_CHECK_ARG(chains == 1 || chains == 8, "chains must be 1 or 8");
+    EMBER_CHECK_ARG(warps >= 1 && warps <= 32, "warps must be 1..32");
+    EMBER_CHECK_ARG(active_lanes >= 1 && active_lanes <= 32, "active_lanes must be 1..32");
+    EMBER_TRY(ensure_device());
+    int dev = 0, sms = 0;
+    EMBER_CUDA_TRY(cudaGetDevice(&dev));
+    EMBER_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    double* sink = nullptr;
+    long long* cyc = nullptr;
+    EMBER_CUDA_TRY(cudaMalloc(&sink, sizeof(double)));
+    if (cudaMalloc(&cyc, sizeof(long long) * sms) != cudaSuccess) {
+        cudaFree(sink);
+        set_error("probe: no device memory");
+        return EMBER_ECUDA;
+    }
+    const int iters = op == 3 ? 256 : 1024;
+    void (*kern)(double*, long long*, int, int) = nullptr;
+    switch (op * 2 + (chains == 8)) {
+        case 0: kern = k_probe_issue<1, 0>; break;
+        case 1: kern = k_probe_issue<8, 0>; break;
+        case 2: kern = k_probe_issue<1, 1>; break;
+        case 3: kern = k_probe_issue<8, 1>; break;
+        case 4: kern = k_probe_issue<1, 2>; break;
+        case 5: kern = k_probe_issue<8, 2>; break;
+        case 6: kern = k_probe_issue<1, 3>; break;
+        default: kern = k_probe_issue<8, 3>; break;
+    }
+    for (int rep = 0; rep < 2; ++rep) kern<<<sms, warps * 32>>>(sink, cyc, iters, active_lanes);
+    cudaError_t err = cudaDeviceSynchronize();
+    std::vector<long long> h(sms);
+    if (err == cudaSuccess) err = cudaMemcpy(h.data(), cyc, sizeof(long long) * sms, cudaMemcpyDeviceToHost);
+    cudaFree(sink);
+    cudaFree(cyc);
+    if (err != cudaSuccess) {
+        set_error("probe kernel failed: %s", cudaGetErrorString(err));
+        return EMBER_ECUDA;
+    }
+    std::sort(h.begin(), h.end());
+    *cycles_per_inst = double(h[sms / 2]) / (double(iters) * chains);
+    return EMBER_OK;
+}
 
 extern "C" int ember_probe_fp64_rate(int kind, double* flops_per_second) {
     EMBER_CHECK_ARG(flops_per_second != nullptr, "null output");

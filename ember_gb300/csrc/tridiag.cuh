@@ -367,15 +367,16 @@ __device__ __forceinline__ double diffusion_step_size(int N, const double* x, co
 
 // Warp-parallel diffusion stage (diffusion_warp.cu). A plan holds the
 // per-system workspace, the geometric factors of every grid point, the
-// largest-first order and the work counter of one batch of flames.
+// largest-first task list (systems packed onto the warps of a CTA) and the
+// work counter of one batch of flames.
 struct DiffusionWarpPlan {
     int n_sys = 0, n_flames = 0, n_vars = 0, nmax = 0;
     int64_t n_pts = 0;
-    int64_t warps = 0;
+    int n_tasks = 0, blocks = 0;
     double* ws = nullptr;
     double2* geo = nullptr;
     int64_t* ws_off = nullptr;
-    int* order = nullptr;
+    int* tasks = nullptr;
     unsigned int* counter = nullptr;
 };
 
@@ -388,7 +389,7 @@ size_t diffusion_warp_plan_bytes(const std::vector<DiffSysInfo>& info, int64_t n
 // Geometric factors of every grid point (x: all flames' coordinates).
 int diffusion_warp_geometry(const DiffusionWarpPlan& p, const DiffSysInfo* d_info, const double* x, cudaStream_t st);
 // One stage: rows, step size and integration of every system of `dv`, with
-// one warp per system; `y` (device, variable-major per flame) in place.
+// one to eight warps per system; `y` (device, variable-major per flame) in place.
 int diffusion_warp_run(const DiffusionWarpPlan& p, const DiffusionView& dv, double* y, const StageTime& tm,
                        double mult, double gdt, cudaStream_t st);
 

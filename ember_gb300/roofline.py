@@ -138,3 +138,45 @@ def convection_flame_flops(n_points, stats):
     N = np.asarray(n_points, dtype=float)
     st = np.asarray(stats, dtype=float).reshape(-1, 4)
     return st[:, 1] * 30.0 * N + st[:, 0] * 35.0 * 3.0 * N + st[:, 3] * 8.0 * N + st[:, 2] * 35.0 * N
+
+
+# (name, op, chains, warps per SM, active lanes) of the FP64 issue probe
+FP64_ISSUE_CASES = (
+    ("DFMA latency, 1 warp", 0, 1, 1, 32),
+    ("DFMA latency, 1 warp, 1 lane", 0, 1, 1, 1),
+    ("DADD latency, 1 warp", 1, 1, 1, 32),
+    ("DMUL latency, 1 warp", 2, 1, 1, 32),
+    ("division latency, 1 warp", 3, 1, 1, 32),
+    ("DFMA issue, 1 warp/SM", 0, 8, 1, 32),
+    ("DFMA issue, 2 warps/SM", 0, 8, 2, 32),
+    ("DFMA issue, 4 warps/SM", 0, 8, 4, 32),
+    ("DFMA issue, 8 warps/SM", 0, 8, 8, 32),
+    ("DFMA issue, 16 warps/SM", 0, 8, 16, 32),
+    ("DFMA issue, 8 warps/SM, 1 lane", 0, 8, 8, 1),
+    ("DFMA issue, 8 warps/SM, 8 lanes", 0, 8, 8, 8),
+    ("DFMA issue, 8 warps/SM, 16 lanes", 0, 8, 8, 16),
+    ("DADD issue, 8 warps/SM", 1, 8, 8, 32),
+    ("DMUL issue, 8 warps/SM", 2, 8, 8, 32),
+    ("division issue, 8 warps/SM", 3, 8, 8, 32),
+)
+
+
+def fp64_issue_table():
+    """ember_probe_fp64_issue over FP64_ISSUE_CASES on the current device:
+    [(name, warps per SM, active lanes, cycles per instruction per warp,
+    SM cycles per warp instruction, FP64 lane operations per SM cycle)]."""
+    import ctypes as C
+    from . import _lib as L
+    rows = []
+    for name, op, chains, warps, lanes in FP64_ISSUE_CASES:
+        c = C.c_double()
+        L.check(L.lib().ember_probe_fp64_issue(op, chains, warps, lanes, C.byref(c)), "probe")
+        per_sm = c.value / warps
+        rows.append((name, warps, lanes, c.value, per_sm, lanes / per_sm))
+    return rows
+
+
+if __name__ == "__main__":
+    print(f"{'case':36s} {'warps':>5s} {'lanes':>5s} {'cyc/inst/warp':>13s} {'SM cyc/inst':>11s} {'lane ops/SM cyc':>15s}")
+    for name, w, ln, c, s, r in fp64_issue_table():
+        print(f"{name:36s} {w:5d} {ln:5d} {c:13.1f} {s:11.2f} {r:15.3f}")

@@ -71,6 +71,13 @@ int ember_device_count(void);
  * (the reference has no GPU code). */
 int ember_probe_fp64_rate(int kind, double* flops_per_second);
 
+/* Cycles per FP64 warp instruction as seen by one warp: one CTA of `warps`
+ * warps on every SM, the first `active_lanes` lanes of each warp running
+ * `chains` (1: a dependent chain, latency; 8: independent chains, issue
+ * rate) of op 0 (DFMA), 1 (DADD), 2 (DMUL) or 3 (division); the median over
+ * SMs. No reference counterpart. */
+int ember_probe_fp64_issue(int op, int chains, int warps, int active_lanes, double* cycles_per_inst);
+
 /* ======================================================================
  * Batched tridiagonal integrator
  *

@@ -467,7 +467,10 @@ void oracle_convection_utw_rhs(const oracle_conv_flame* fl, const double* x, con
     } else {
         if (fl->continuity_bc == ORACLE_CONT_TEMP) {
             const int j = jc;
-            if (j == 0 || sT[j] / (T_(j + 1) - T_(j)) < 0)
+            /* at the last point (where the update can put the temperature
+               crossing) only the backward difference exists; the reference
+               reads T[jj + 1] there */
+            if (j == 0 || (j < jj && sT[j] / (T_(j + 1) - T_(j)) < 0))
                 rV[j] = (((rph[j] * rho[j]) * sT[j]) * hh[j]) / (T_(j + 1) - T_(j));
             else
                 rV[j] = (((rph[j - 1] * rho[j]) * sT[j]) * hh[j - 1]) / (T_(j) - T_(j - 1));

@@ -147,10 +147,14 @@ def test_split_step_gradients_match_central_differences_of_the_oracle(gpu_lib):
     _, hr_ref, cs_ref = osplit.objectives(om, grids, y_ref, opts.pressure, opts.kinetics_model, rho_u, ju, jb)
     assert np.array_equal(out.detach().numpy(), np.concatenate([hr_ref, cs_ref]))
     n0 = grids[0].n_points
-    # state entries away from Y = 0, where the clipping of setState_TPY makes J one-sided
+    # state entries away from Y = 0, where the clipping of setState_TPY makes J one-sided.
+    # Difference step 1e-3 of the entry: below it the adaptive integrator's
+    # step-size decisions make the quotients noisy (for (4, 2): -8.0542e5,
+    # -8.0549e5, -8.0447e5, -8.0706e5, -8.1672e5 at 1e-3, 3e-4, 1e-4, 3e-5,
+    # 1e-5 of the entry), while at 1e-3 and 3e-4 they agree to 1e-4.
     for (p, k) in [(3, 1), (n0 + 5, 1), (4, 2), (n0 + 6, 3), (2, 4), (n0 - 2, 5)]:
         assert state[p, k] > 1e-6
-        hstep = 1e-4 * max(abs(state[p, k]), 1e-6)
+        hstep = 1e-3 * max(abs(state[p, k]), 1e-6)
         e = np.zeros_like(state)
         e[p, k] = hstep
         fd = (J(state + e) - J(state - e)) / (2 * hstep)
@@ -215,11 +219,16 @@ def test_split_step_adjoint_at_the_c4_size(gpu_lib):
         fd = (J(state, mp) - J(state, mm)) / 2e-3
         assert abs(g_lnk[i] - fd) <= 2e-3 * abs(fd) + 1e-4 * gmax, (i, g_lnk[i], fd, gmax)
     om.set_multipliers(None)
+    # State entries: steps of 1e-3 of the entry. Smaller steps reach the
+    # integrator's step-size noise: for entry (294, 3) the quotients are
+    # -63482, -63466, -63496, -63508 at 1e-2, 3e-3, 1e-3, 3e-4 of the entry,
+    # then -63017, -63949, -59702 at 1e-4, 3e-5, 1e-5 (and the noisy ones
+    # differ between hosts).
     pts = rng.choice(len(state), 20, replace=False)
     for p in pts:
         ks = [1] + [2 + k for k in np.flatnonzero(state[p, 2:] > 1e-6)]
         k = int(rng.choice(ks))
-        hstep = 1e-4 * abs(state[p, k])
+        hstep = 1e-3 * abs(state[p, k])
         e = np.zeros_like(state)
         e[p, k] = hstep
         fd = (J(state + e) - J(state - e)) / (2 * hstep)

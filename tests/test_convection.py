@@ -96,7 +96,8 @@ def _numpy_utw(fl, x, t, U, T, Wm, drhodt, sU, sT, sW):
                 rV[j - 1] = rV[j] + m[j - 1]
     else:
         if fl.continuity_bc == CONT_TEMP:
-            if jc == 0 or sT[jc] / (T[jc + 1] - T[jc]) < 0:
+            # at the last point only the backward difference exists
+            if jc == 0 or (jc < jj and sT[jc] / (T[jc + 1] - T[jc]) < 0):
                 rV[jc] = rph[jc] * rho[jc] * sT[jc] * hh[jc] / (T[jc + 1] - T[jc])
             else:
                 rV[jc] = rph[jc - 1] * rho[jc] * sT[jc] * hh[jc - 1] / (T[jc] - T[jc - 1])
@@ -157,6 +158,7 @@ CASES = [
     dict(continuity_bc=CONT_ZERO, j_cont=39, x_vzero=1e-3, alpha=1),
     dict(continuity_bc=CONT_TEMP, j_cont=20),
     dict(continuity_bc=CONT_TEMP, j_cont=0),
+    dict(continuity_bc=CONT_TEMP, j_cont=39),   # the last point: backward difference only
     dict(continuity_bc=CONT_RIGHT, j_cont=39, rv_cont=-0.4),
     dict(continuity_bc=CONT_QDOT, j_cont=11, rv_cont=0.1, alpha=1, left_bc=BC_ZERO_GRADIENT),
 ]
