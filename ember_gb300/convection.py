@@ -21,6 +21,8 @@ from .mechanism import GAS_CONSTANT, Mechanism
 
 BC_FIXED_VALUE, BC_ZERO_GRADIENT, BC_CONTROL_VOLUME, BC_WALL_FLUX = 0, 1, 2, 3
 CONT_LEFT, CONT_RIGHT, CONT_ZERO, CONT_QDOT, CONT_TEMP = 0, 1, 2, 3, 4
+STRAIN_LINEAR, STRAIN_CHEBYSHEV = 0, 1
+CHEBYSHEV_MAX = 16
 STATUS_RECORD_FULL = -20
 
 
@@ -30,7 +32,8 @@ class ConvectionFlameC(C.Structure):
                 ("beta", C.c_double), ("x_vzero", C.c_double), ("rv_zero", C.c_double), ("rv_cont", C.c_double),
                 ("t_left", C.c_double), ("w_left", C.c_double), ("rhou", C.c_double), ("pressure", C.c_double),
                 ("strain_initial", C.c_double), ("strain_final", C.c_double), ("strain_t0", C.c_double),
-                ("strain_dt", C.c_double)]
+                ("strain_dt", C.c_double), ("strain_type", C.c_int), ("n_cheb", C.c_int), ("cheb_t0", C.c_double),
+                ("cheb_t1", C.c_double), ("cheb", C.c_double * CHEBYSHEV_MAX)]
 
 
 class ConvectionOptionsC(C.Structure):
@@ -61,9 +64,25 @@ class ConvectionFlame:
     strain_final: float = 100.0
     strain_t0: float = 0.0
     strain_dt: float = 0.0
+    # ChebyshevFunction (strain_type STRAIN_CHEBYSHEV): the interval mapped
+    # onto [-1, 1] and the coefficients (setCoefficients(2 + n, {t0, t1, c...}))
+    strain_type: int = STRAIN_LINEAR
+    cheb_t0: float = 0.0
+    cheb_t1: float = 1.0
+    cheb: tuple = ()
+
+    @property
+    def n_cheb(self) -> int:
+        return len(self.cheb)
 
     def as_c(self) -> ConvectionFlameC:
-        return ConvectionFlameC(**{f.name: getattr(self, f.name) for f in fields(self)})
+        if len(self.cheb) > CHEBYSHEV_MAX:
+            raise ValueError(f"at most {CHEBYSHEV_MAX} Chebyshev coefficients")
+        kw = {f.name: getattr(self, f.name) for f in fields(self) if f.name != "cheb"}
+        c = [float(v) for v in self.cheb]
+        kw["n_cheb"] = len(c)
+        kw["cheb"] = (C.c_double * CHEBYSHEV_MAX)(*(c + [0.0] * (CHEBYSHEV_MAX - len(c))))
+        return ConvectionFlameC(**kw)
 
 
 @dataclass

@@ -669,6 +669,43 @@ __global__ void k_conv_prepare(const __grid_constant__ ConvArgs a) {
     }
 }
 
+
+// a(t) and da/dt of a flame's strain function: LinearFunction
+// (src/scalarFunction.cpp:12-22) or ChebyshevFunction (:31-87), with the
+// reference's padding (fewer than two coefficients count as zeros) and its
+// derivative recurrence, which weights coefficient i by i U_i(x) (the loop
+// advances the U recurrence before using it; T'_i = i U_{i-1}).
+__device__ __forceinline__ void conv_strain(const ember_convection_flame& fl, double t, double& a, double& dadt) {
+    if (fl.strain_type == EMBER_STRAIN_CHEBYSHEV) {
+        const int n = fl.n_cheb < 2 ? 2 : fl.n_cheb;
+        auto c = [&](int i) { return i < fl.n_cheb ? fl.cheb[i] : 0.0; };
+        const double x = (2 * (t - fl.cheb_t0)) / (fl.cheb_t1 - fl.cheb_t0) - 1;
+        double cm = 1, cn = x;
+        double y = c(0) + x * c(1);
+        for (int i = 2; i < n; ++i) {
+            const double cp = (2 * x) * cn - cm;
+            y += cp * c(i);
+            cm = cn;
+            cn = cp;
+        }
+        a = y;
+        cm = 1;
+        cn = 2 * x;
+        double dydx = c(1);
+        for (int i = 2; i < n; ++i) {
+            const double cp = (2 * x) * cn - cm;
+            dydx += (static_cast<double>(i) * cp) * c(i);
+            cm = cn;
+            cn = cp;
+        }
+        dadt = dydx * (2.0 / (fl.cheb_t1 - fl.cheb_t0));
+        return;
+    }
+    const double a0 = fl.strain_initial, a1 = fl.strain_final, T0 = fl.strain_t0, Dt = fl.strain_dt;
+    a = (t <= T0) ? a0 : (t >= T0 + Dt) ? a1 : a0 + ((a1 - a0) * (t - T0)) / Dt;
+    dadt = (t >= T0 && t < T0 + Dt) ? (a1 - a0) / Dt : 0.0;
+}
+
 struct UtwSys {
     int n;
     const ConvArgs* a;
@@ -764,11 +801,7 @@ struct UtwSys {
         }
         __syncthreads();
         double aa, dadt;
-        {
-            const double a0 = fl->strain_initial, a1 = fl->strain_final, T0 = fl->strain_t0, Dt = fl->strain_dt;
-            aa = (t <= T0) ? a0 : (t >= T0 + Dt) ? a1 : a0 + ((a1 - a0) * (t - T0)) / Dt;
-            dadt = (t >= T0 && t < T0 + Dt) ? (a1 - a0) / Dt : 0.0;
-        }
+        conv_strain(*fl, t, aa, dadt);
         const double K = dadt / beta + (aa * aa) / (beta * beta);
         const bool cv = fl->left_bc == EMBER_BC_CONTROL_VOLUME || fl->left_bc == EMBER_BC_WALL_FLUX;
         const double rVjj = rV[jj];
@@ -1043,6 +1076,12 @@ int conv_plan_layout(ConvPlan& p, int n_flames, const ember_convection_flame* fl
                         "flame %d: j_cont out of range", f);
         EMBER_CHECK_ARG(g.beta > 0 && g.pressure > 0, "flame %d: beta and pressure must be positive", f);
         EMBER_CHECK_ARG(g.strain_dt >= 0, "flame %d: strain_dt must be >= 0", f);
+        EMBER_CHECK_ARG(g.strain_type == EMBER_STRAIN_LINEAR || g.strain_type == EMBER_STRAIN_CHEBYSHEV,
+                        "flame %d: bad strain function type %d", f, g.strain_type);
+        EMBER_CHECK_ARG(g.strain_type != EMBER_STRAIN_CHEBYSHEV ||
+                            (g.n_cheb >= 0 && g.n_cheb <= EMBER_CHEBYSHEV_MAX && g.cheb_t1 != g.cheb_t0),
+                        "flame %d: Chebyshev strain needs 0..%d coefficients and cheb_t1 != cheb_t0", f,
+                        EMBER_CHEBYSHEV_MAX);
         ConvFlame& c = p.hf[f];
         c.f = g;
         c.p0 = p.P;
@@ -1210,6 +1249,23 @@ __global__ void k_conv_continuity(const __grid_constant__ ConvArgs a, ConvFlame*
 }
 
 __global__ void k_conv_ready(int* ready) { *ready = 1; }
+
+// V of every flame's UTW system at its last right-hand side evaluation into
+// out (point-major across flames), one CTA per flame.
+__global__ void k_conv_velocity(const __grid_constant__ ConvArgs a, double* out) {
+    const int fi = blockIdx.x;
+    if (fi >= a.n_flames) return;
+    const ConvFlame& F = a.flames[fi];
+    if (!utw_slice_ok(a, F)) return;
+    const UtwView u = utw_view(a, F);
+    for (int j = threadIdx.x; j < F.f.n_points; j += blockDim.x) out[F.p0 + j] = u.V[j];
+}
+
+int conv_velocity_launch(const ConvPlan& p, const ConvArgs& a, double* out, cudaStream_t st) {
+    k_conv_velocity<<<p.n_flames, 128, 0, st>>>(a, out);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    return EMBER_OK;
+}
 
 int conv_continuity_launch(const ConvPlan& p, const ConvArgs& a, const int* ready, const double* state, int n_vars,
                            const double* qdot, cudaStream_t st) {

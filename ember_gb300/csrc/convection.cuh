@@ -68,6 +68,8 @@ int conv_launch(const ConvPlan& p, const ConvArgs& a, cudaStream_t st);
 // The continuity point of every flame at the start of a split step (after
 // the first since *ready was cleared; then sets *ready): state point-major
 // with n_vars per point; qdot per point or null (needed for fixedQdot).
+// V of the UTW systems' last right-hand side evaluation, point-major across flames.
+int conv_velocity_launch(const ConvPlan& p, const ConvArgs& a, double* out, cudaStream_t st);
 int conv_continuity_launch(const ConvPlan& p, const ConvArgs& a, const int* ready, const double* state, int n_vars,
                            const double* qdot, cudaStream_t st);
 

@@ -630,6 +630,7 @@ struct ember_split_s {
     bool conv_qdot = false;
     double *cq_T = nullptr, *cq_Y = nullptr, *cq_net = nullptr, *cq_hk = nullptr, *cq_cp = nullptr,
            *cq_q = nullptr, *cq_qcp = nullptr, *cq_cache = nullptr;
+    double* strain_stage = nullptr;  // [n_flames][2 + EMBER_CHEBYSHEV_MAX]: ember_split_set_strain's staging
     cudaStream_t capture_stream = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t graph_exec = nullptr;
@@ -1140,7 +1141,7 @@ extern "C" int ember_split_set_convection(ember_split h, const ember_convection_
     const size_t bytes = conv_plan_bytes(p, false) + 4 * Scratch::rounded(nv * sizeof(double)) +
                          Scratch::rounded(size_t(h->n_pts) * sizeof(double)) +
                          Scratch::rounded(size_t(h->n_flames) * S * sizeof(double)) + Scratch::rounded(sizeof(int)) +
-                         qdot_bytes;
+                         qdot_bytes + Scratch::rounded(size_t(h->n_flames) * (2 + EMBER_CHEBYSHEV_MAX) * sizeof(double));
     cudaError_t e = cudaMalloc(&h->cblob, bytes);
     if (e != cudaSuccess) {
         h->cblob = nullptr;
@@ -1155,6 +1156,7 @@ extern "C" int ember_split_set_convection(ember_split h, const ember_convection_
     EMBER_TRY(a.alloc(&h->drhodt, size_t(h->n_pts)));
     EMBER_TRY(a.alloc(&h->y_left, size_t(h->n_flames) * S));
     EMBER_TRY(a.alloc(&h->conv_ready, 1));
+    EMBER_TRY(a.alloc(&h->strain_stage, size_t(h->n_flames) * (2 + EMBER_CHEBYSHEV_MAX)));
     h->conv_qdot = any_qdot;
     if (any_qdot) {
         EMBER_TRY(a.alloc(&h->cq_T, np));
@@ -1182,6 +1184,48 @@ extern "C" int ember_split_set_convection(ember_split h, const ember_convection_
     c.dt = h->opt.dt;
     h->cplan = std::move(p);
     h->conv = true;
+    return EMBER_OK;
+}
+
+
+namespace ember {
+namespace {
+// The strain function of every flame becomes the Chebyshev series staged in
+// stage[f][0..1] (t0, t1) and stage[f][2..2+n) (coefficients).
+__global__ void k_set_strain(ConvFlame* flames, int n_flames, int n, const double* __restrict__ stage) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_flames) return;
+    ember_convection_flame& fl = flames[f].f;
+    const double* c = stage + size_t(f) * (2 + EMBER_CHEBYSHEV_MAX);
+    fl.strain_type = EMBER_STRAIN_CHEBYSHEV;
+    fl.n_cheb = n;
+    fl.cheb_t0 = c[0];
+    fl.cheb_t1 = c[1];
+    for (int i = 0; i < EMBER_CHEBYSHEV_MAX; ++i) fl.cheb[i] = i < n ? c[2 + i] : 0.0;
+}
+}  // namespace
+}  // namespace ember
+
+extern "C" int ember_split_set_strain(ember_split h, int n_coeffs, const double* coeffs, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(h->conv, "no convection stage attached (ember_split_set_convection)");
+    EMBER_CHECK_ARG(n_coeffs >= 0 && n_coeffs <= EMBER_CHEBYSHEV_MAX, "n_coeffs must be 0..%d", EMBER_CHEBYSHEV_MAX);
+    EMBER_CHECK_ARG(coeffs != nullptr, "null coefficients");
+    const int w = 2 + n_coeffs, ws = 2 + EMBER_CHEBYSHEV_MAX;
+    std::vector<double> stage(size_t(h->n_flames) * ws, 0.0);
+    for (int f = 0; f < h->n_flames; ++f) {
+        const double* c = coeffs + size_t(f) * w;
+        EMBER_CHECK_ARG(c[1] != c[0], "flame %d: t1 equals t0", f);
+        for (int i = 0; i < w; ++i) stage[size_t(f) * ws + i] = c[i];
+    }
+    cudaStream_t st = as_stream(stream);
+    EMBER_CUDA_TRY(cudaMemcpyAsync(h->strain_stage, stage.data(), sizeof(double) * stage.size(),
+                                   cudaMemcpyHostToDevice, st));
+    k_set_strain<<<blocks_for(h->n_flames, 64), 64, 0, st>>>(const_cast<ConvFlame*>(h->cplan.a.flames), h->n_flames,
+                                                             n_coeffs, h->strain_stage);
+    EMBER_CUDA_TRY(cudaGetLastError());
+    // the staging vector is a host buffer: the copy must be done before it goes away
+    EMBER_CUDA_TRY(cudaStreamSynchronize(st));
     return EMBER_OK;
 }
 
@@ -1319,6 +1363,33 @@ extern "C" int ember_split_get_derivatives(ember_split h, double* ddt_diff, doub
     const cudaMemcpyKind kind = mem == EMBER_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
     if (ddt_diff) EMBER_CUDA_TRY(cudaMemcpyAsync(ddt_diff, h->ddt_diff, sizeof(double) * h->n_vals, kind, st));
     if (ddt_prod) EMBER_CUDA_TRY(cudaMemcpyAsync(ddt_prod, h->ddt_prod, sizeof(double) * h->n_vals, kind, st));
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_split_get_convection_derivative(ember_split h, double* ddt_conv, int mem, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_CHECK_ARG(h->conv, "no convection stage attached");
+    EMBER_CHECK_ARG(ddt_conv != nullptr, "null ddt_conv");
+    cudaStream_t st = as_stream(stream);
+    const cudaMemcpyKind kind = mem == EMBER_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    EMBER_CUDA_TRY(cudaMemcpyAsync(ddt_conv, h->ddt_conv, sizeof(double) * h->n_vals, kind, st));
+    return finish_call(mem, st);
+}
+
+extern "C" int ember_split_get_velocity(ember_split h, double* V, int mem, void* stream) {
+    EMBER_TRY(check_split(h));
+    EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
+    EMBER_CHECK_ARG(h->conv, "no convection stage attached");
+    EMBER_CHECK_ARG(V != nullptr, "null V");
+    cudaStream_t st = as_stream(stream);
+    Scratch sc(st);
+    double* dv = V;
+    if (mem == EMBER_MEM_HOST) EMBER_TRY(sc.alloc(&dv, size_t(h->n_pts)));
+    EMBER_TRY(conv_velocity_launch(h->cplan, h->cplan.a, dv, st));
+    if (mem == EMBER_MEM_HOST)
+        EMBER_CUDA_TRY(cudaMemcpyAsync(V, dv, sizeof(double) * h->n_pts, cudaMemcpyDeviceToHost, st));
+    sc.release();
     return finish_call(mem, st);
 }
 

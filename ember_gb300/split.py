@@ -12,6 +12,7 @@ C ABI). Convection is not integrated (its rate can enter through
 """
 from __future__ import annotations
 
+import copy
 import ctypes as C
 
 import numpy as np
@@ -44,6 +45,9 @@ def _declare(lib):
         "ember_split_objectives": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, C.c_int, vp]),
         "ember_split_adjoint": (C.c_int, [vp, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, C.c_int, vp]),
         "ember_split_set_convection": (C.c_int, [vp, vp, vp, vp]),
+        "ember_split_set_strain": (C.c_int, [vp, C.c_int, vp, vp]),
+        "ember_split_get_convection_derivative": (C.c_int, [vp, vp, C.c_int, vp]),
+        "ember_split_get_velocity": (C.c_int, [vp, vp, C.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -148,6 +152,7 @@ class FlameBatchSplitSolver:
         ConvectionOptions); None detaches."""
         if flames is None:
             L.check(_lib().ember_split_set_convection(self._h, None, None, None), "ember_split_set_convection")
+            self._convection = None
             return
         from .convection import ConvectionFlameC, ConvectionOptions, ConvectionOptionsC
         opts = opts or ConvectionOptions()
@@ -157,6 +162,23 @@ class FlameBatchSplitSolver:
         yl = np.ascontiguousarray(y_left, dtype=np.float64)
         L.check(_lib().ember_split_set_convection(self._h, C.addressof(arr), yl.ctypes.data, C.byref(o)),
                 "ember_split_set_convection")
+        # the handle's view of the flames' strain functions, for the output writers (copies: the
+        # caller's objects are left as given)
+        self._convection = [copy.copy(f) for f in flames]
+
+    def set_strain_chebyshev(self, coeffs, stream=None):
+        """ember_split_set_strain: per flame a row {t0, t1, c_0, ..., c_{n-1}}
+        (the ChebyshevFunction coefficients of [t0, t1]); from the next step
+        every flame's strain rate is that series."""
+        c = np.ascontiguousarray(coeffs, dtype=np.float64)
+        if c.ndim != 2 or c.shape[0] != len(self.grids) or c.shape[1] < 2:
+            raise ValueError("coeffs must be [n_flames, 2 + n]")
+        L.check(_lib().ember_split_set_strain(self._h, c.shape[1] - 2, c.ctypes.data, L.stream_ptr(stream)),
+                "ember_split_set_strain")
+        from .convection import STRAIN_CHEBYSHEV
+        for fl, row in zip(getattr(self, "_convection", None) or [], c):
+            fl.strain_type, fl.cheb_t0, fl.cheb_t1, fl.cheb = STRAIN_CHEBYSHEV, float(row[0]), float(row[1]), \
+                tuple(float(v) for v in row[2:])
 
     def step(self, n_steps: int = 1, graph: bool = False, stream=None):
         L.check(_lib().ember_split_step(self._h, int(n_steps), int(bool(graph)), L.stream_ptr(stream)),
@@ -179,6 +201,19 @@ class FlameBatchSplitSolver:
         L.check(_lib().ember_split_get_derivatives(self._h, dd.ctypes.data, dp.ctypes.data, L.MEM_HOST, None),
                 "get_derivatives")
         return dd, dp
+
+    def convection_derivative(self):
+        """ddtConv of the last step (convection stage attached)."""
+        dc = np.empty((self.n_points, self.n_vars))
+        L.check(_lib().ember_split_get_convection_derivative(self._h, dc.ctypes.data, L.MEM_HOST, None),
+                "get_convection_derivative")
+        return dc
+
+    def velocity(self):
+        """V per point at the UTW systems' last evaluation (convection stage attached)."""
+        v = np.empty(self.n_points)
+        L.check(_lib().ember_split_get_velocity(self._h, v.ctypes.data, L.MEM_HOST, None), "get_velocity")
+        return v
 
     def set_derivatives(self, ddt_diff, ddt_prod, ddt_conv=None):
         """ember_split_set_derivatives: the time derivatives behind the next

@@ -263,6 +263,11 @@ int ember_diffusion_integrate_noalloc(int n_flames, const ember_diffusion_grid* 
 /* Largest flame: the continuity integral of a flame is staged in shared memory. */
 #define EMBER_CONVECTION_MAX_POINTS 8192
 
+/* Strain-rate function a(t) of a flame (src/scalarFunction.h). */
+#define EMBER_STRAIN_LINEAR    0   /* LinearFunction: strain_initial/final/t0/dt          */
+#define EMBER_STRAIN_CHEBYSHEV 1   /* ChebyshevFunction: cheb_t0, cheb_t1, cheb[n_cheb]   */
+#define EMBER_CHEBYSHEV_MAX    16  /* coefficients per flame                              */
+
 typedef struct {
     int n_points;          /* 3 <= N_f <= EMBER_CONVECTION_MAX_POINTS                 */
     int left_bc;           /* EMBER_BC_FIXED_VALUE / ZERO_GRADIENT / CONTROL_VOLUME / WALL_FLUX */
@@ -282,6 +287,13 @@ typedef struct {
     double strain_initial, strain_final, strain_t0, strain_dt;  /* a(t): LinearFunction
                               (src/scalarFunction.cpp:12-22); equal initial and final
                               values give a constant strain rate                     */
+    int strain_type;       /* EMBER_STRAIN_LINEAR (the fields above) or
+                              EMBER_STRAIN_CHEBYSHEV (the fields below)               */
+    int n_cheb;            /* Chebyshev coefficients in cheb (0..EMBER_CHEBYSHEV_MAX):
+                              ChebyshevFunction::setCoefficients(2 + n_cheb, {cheb_t0,
+                              cheb_t1, cheb...}) (src/scalarFunction.cpp:31-49)        */
+    double cheb_t0, cheb_t1;  /* the interval mapped onto [-1, 1]                      */
+    double cheb[EMBER_CHEBYSHEV_MAX];
 } ember_convection_flame;
 
 typedef struct {
@@ -652,11 +664,30 @@ int ember_split_set_transport_model(ember_split split, ember_transport tr, doubl
  * refuses a handle with the stage attached. */
 int ember_split_set_convection(ember_split split, const ember_convection_flame* flames, const double* y_left,
                                const ember_convection_options* opts);
+/* The strain rate of every flame becomes a Chebyshev series, as
+ * FlameSolver's strainfunc after ChebyshevFunction::setCoefficients
+ * (src/scalarFunction.cpp:31-49), which the Python layer calls before each
+ * step with the series fitted over [tNow, tNow + dt]
+ * (python/ember/_ember.pyx:521-531). coeffs: host, per flame 2 + n_coeffs
+ * values {t0, t1, c_0 .. c_{n_coeffs-1}} (0 <= n_coeffs <=
+ * EMBER_CHEBYSHEV_MAX). Needs the convection stage attached; takes effect
+ * from the next step, captured graph included (the flames' records are
+ * updated in device memory). Returns when the update is done on `stream`. */
+int ember_split_set_strain(ember_split split, int n_coeffs, const double* coeffs, void* stream);
 /* n_steps split steps, asynchronous on `stream`. */
 int ember_split_step(ember_split split, int n_steps, int use_graph, void* stream);
 int ember_split_get_state(ember_split split, double* state, double* t, int mem, void* stream);
 /* ddtDiff and ddtProd of the last step, point-major. */
 int ember_split_get_derivatives(ember_split split, double* ddt_diff, double* ddt_prod, int mem, void* stream);
+/* ddtConv of the last step, point-major (convection stage attached): with
+ * ember_split_get_derivatives, the three derivatives FlameSolver carries
+ * through a regrid (src/flameSolver.cpp:300-340). */
+int ember_split_get_convection_derivative(ember_split split, double* ddt_conv, int mem, void* stream);
+/* The mass flux V of every point at the UTW system's last right-hand side
+ * evaluation (convectionSystem.utwSystem.V; meaningful after a step),
+ * point-major: what FlameSolver interpolates onto a new grid for rVzero and
+ * the next continuity update (src/flameSolver.cpp:287-290, 336-338). */
+int ember_split_get_velocity(ember_split split, double* V, int mem, void* stream);
 /* Replace the time derivatives that set the next step's split constants
  * (point-major; ddt_conv only with the convection stage attached, NULL =
  * zero), as FlameSolver does after a regrid: ddtDiff, ddtProd and ddtConv

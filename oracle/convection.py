@@ -16,7 +16,8 @@ class OracleConvFlame(C.Structure):
                 ("beta", C.c_double), ("x_vzero", C.c_double), ("rv_zero", C.c_double), ("rv_cont", C.c_double),
                 ("t_left", C.c_double), ("w_left", C.c_double), ("rhou", C.c_double), ("pressure", C.c_double),
                 ("strain_initial", C.c_double), ("strain_final", C.c_double), ("strain_t0", C.c_double),
-                ("strain_dt", C.c_double)]
+                ("strain_dt", C.c_double), ("strain_type", C.c_int), ("n_cheb", C.c_int), ("cheb_t0", C.c_double),
+                ("cheb_t1", C.c_double), ("cheb", C.c_double * 16)]
 
 
 class OracleConvOptions(C.Structure):
@@ -29,6 +30,8 @@ def _lib():
     import oracle
     l = oracle.lib()
     vp, d, i = C.c_void_p, C.c_double, C.c_int
+    l.oracle_convection_strain.argtypes = [vp, d, vp, vp]
+    l.oracle_convection_strain.restype = None
     l.oracle_adams_gammas.argtypes = [vp]
     l.oracle_adams_gammas.restype = None
     l.oracle_adams_l.argtypes = [i, vp]
@@ -65,7 +68,18 @@ def _p(a):
 
 def flame_struct(params) -> OracleConvFlame:
     """From any object with the ConvectionFlame attributes."""
-    return OracleConvFlame(**{n: getattr(params, n) for n, _ in OracleConvFlame._fields_})
+    kw = {n: getattr(params, n) for n, _ in OracleConvFlame._fields_ if n != "cheb"}
+    c = list(getattr(params, "cheb", ()) or ())
+    kw["cheb"] = (C.c_double * 16)(*(c + [0.0] * (16 - len(c))))
+    return OracleConvFlame(**kw)
+
+
+def strain(params, t):
+    """(a, da/dt) of a flame's strain function at t (oracle_convection_strain)."""
+    a, d = C.c_double(), C.c_double()
+    f = flame_struct(params)
+    _lib().oracle_convection_strain(C.byref(f), float(t), C.byref(a), C.byref(d))
+    return a.value, d.value
 
 
 def adams_gammas():

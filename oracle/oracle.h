@@ -154,11 +154,15 @@ typedef struct {
     int n_points, left_bc, right_bc, alpha, continuity_bc, j_cont;
     double beta, x_vzero, rv_zero, rv_cont, t_left, w_left, rhou, pressure;
     double strain_initial, strain_final, strain_t0, strain_dt;
+    int strain_type, n_cheb;          /* 0 linear, 1 Chebyshev (cheb_t0, cheb_t1, cheb[n_cheb]) */
+    double cheb_t0, cheb_t1;
+    double cheb[16];
 } oracle_conv_flame;
 typedef struct {
     double reltol, abstol_u, abstol_t, abstol_y, min_step;
     int max_steps, max_history;
 } oracle_conv_options;
+void oracle_convection_strain(const oracle_conv_flame* fl, double t, double* a, double* dadt);
 void oracle_adams_gammas(double* g);
 void oracle_adams_l(int q, double* l);
 void oracle_convection_grid(int N, const double* x, int alpha, double* hh, double* rph);

@@ -423,7 +423,39 @@ done:
 
 static double center_volume(const double* x, int alpha) { return alpha == 0 ? x[1] : (x[1] * x[1]) / 2.0; }
 
-static void strain(const oracle_conv_flame* fl, double t, double* a, double* dadt) {
+/* a(t) and da/dt: LinearFunction (src/scalarFunction.cpp:12-22), or
+   ChebyshevFunction (src/scalarFunction.cpp:31-87) with its coefficient
+   padding (fewer than two coefficients count as zeros) and its derivative
+   recurrence, which weights coefficient i by i U_i(x) (the reference's loop
+   advances the U recurrence before using it; T'_i = i U_{i-1}). */
+void oracle_convection_strain(const oracle_conv_flame* fl, double t, double* a, double* dadt) {
+    if (fl->strain_type == 1) {
+        double c[16];
+        int n = fl->n_cheb;
+        for (int i = 0; i < 16; ++i) c[i] = i < n ? fl->cheb[i] : 0.0;
+        if (n < 2) n = 2;
+        const double x = (2 * (t - fl->cheb_t0)) / (fl->cheb_t1 - fl->cheb_t0) - 1;
+        double cm = 1, cn = x;
+        double y = c[0] + x * c[1];
+        for (int i = 2; i < n; ++i) {
+            const double cp = (2 * x) * cn - cm;
+            y += cp * c[i];
+            cm = cn;
+            cn = cp;
+        }
+        *a = y;
+        cm = 1;
+        cn = 2 * x;
+        double dydx = c[1];
+        for (int i = 2; i < n; ++i) {
+            const double cp = (2 * x) * cn - cm;
+            dydx += ((double)i * cp) * c[i];
+            cm = cn;
+            cn = cp;
+        }
+        *dadt = dydx * (2.0 / (fl->cheb_t1 - fl->cheb_t0));
+        return;
+    }
     const double a0 = fl->strain_initial, a1 = fl->strain_final, T0 = fl->strain_t0, Dt = fl->strain_dt;
     *a = (t <= T0) ? a0 : (t >= T0 + Dt) ? a1 : a0 + ((a1 - a0) * (t - T0)) / Dt;
     *dadt = (t >= T0 && t < T0 + Dt) ? (a1 - a0) / Dt : 0.0;
@@ -485,7 +517,7 @@ void oracle_convection_utw_rhs(const oracle_conv_flame* fl, const double* x, con
     V[0] = rV[0];
     for (int j = 1; j < N; ++j) V[j] = fl->alpha == 0 ? rV[j] : rV[j] / x[j];
     double a, dadt;
-    strain(fl, t, &a, &dadt);
+    oracle_convection_strain(fl, t, &a, &dadt);
     const double K = dadt / beta + (a * a) / (beta * beta);
     /* left boundary */
     ydot[0] = (sU[0] - U_(0) * U_(0)) + (fl->rhou / rho[0]) * K;

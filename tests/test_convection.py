@@ -12,12 +12,13 @@ from fractions import Fraction
 import bisect
 
 import numpy as np
+import numpy.polynomial.chebyshev as npcheb
 import pytest
 
 from oracle import convection as oc
 from ember_gb300.convection import (BC_CONTROL_VOLUME, BC_FIXED_VALUE, BC_WALL_FLUX, BC_ZERO_GRADIENT, CONT_LEFT,
-                                    CONT_QDOT, CONT_RIGHT, CONT_TEMP, CONT_ZERO, ConvectionFlame, ConvectionOptions,
-                                    convection_batch, mean_molecular_weight)
+                                    CONT_QDOT, CONT_RIGHT, CONT_TEMP, CONT_ZERO, STRAIN_CHEBYSHEV, ConvectionFlame,
+                                    ConvectionOptions, convection_batch, mean_molecular_weight)
 from ember_gb300.mechanism import GAS_CONSTANT, synthetic_mechanism
 
 
@@ -68,6 +69,49 @@ def test_adams_l_gives_backward_euler_and_trapezoid():
 
 # ---- the UTW right-hand side ------------------------------------------------
 
+def _numpy_strain(fl, t):
+    """LinearFunction, or ChebyshevFunction through numpy's Chebyshev series
+    for a(t) and the closed form U_i(cos th) = sin((i+1) th) / sin th for the
+    reference's derivative sum c_1 + sum_{i>=2} i U_i(x) c_i."""
+    if fl.strain_type == STRAIN_CHEBYSHEV:
+        c = np.array(list(fl.cheb) + [0.0] * max(0, 2 - len(fl.cheb)))
+        x = 2 * (t - fl.cheb_t0) / (fl.cheb_t1 - fl.cheb_t0) - 1
+        a = npcheb.chebval(x, c)
+        th = np.arccos(np.clip(x, -1, 1))
+        U = [np.sin((i + 1) * th) / np.sin(th) for i in range(len(c))]
+        d = c[1] + sum(i * U[i] * c[i] for i in range(2, len(c)))
+        return a, d * 2.0 / (fl.cheb_t1 - fl.cheb_t0)
+    if t <= fl.strain_t0:
+        a = fl.strain_initial
+    elif t >= fl.strain_t0 + fl.strain_dt:
+        a = fl.strain_final
+    else:
+        a = fl.strain_initial + (fl.strain_final - fl.strain_initial) * (t - fl.strain_t0) / fl.strain_dt
+    dadt = (fl.strain_final - fl.strain_initial) / fl.strain_dt \
+        if fl.strain_t0 <= t < fl.strain_t0 + fl.strain_dt else 0.0
+    return a, dadt
+
+
+def test_chebyshev_strain_matches_the_series():
+    # ChebyshevFunction (src/scalarFunction.cpp:31-87): a(t) is the series;
+    # da/dt follows the reference's recurrence (coefficient i weighted by
+    # i U_i, where T'_i = i U_{i-1}); fewer than two coefficients are padded
+    from ember_gb300.output import strain as out_strain
+    rng = np.random.default_rng(7)
+    for n in (0, 1, 2, 5, 16):
+        fl = ConvectionFlame(n_points=5, strain_type=STRAIN_CHEBYSHEV, cheb_t0=1e-3, cheb_t1=1.2e-3,
+                             cheb=tuple(rng.standard_normal(n) * 100.0))
+        for t in np.linspace(1e-3, 1.2e-3, 7)[1:-1]:
+            a, d = oc.strain(fl, t)
+            ea, ed = _numpy_strain(fl, t)
+            assert a == pytest.approx(ea, rel=1e-12, abs=1e-9)
+            assert d == pytest.approx(ed, rel=1e-10, abs=1e-6)
+            assert out_strain(fl, t) == (a, d)       # the output writer's restatement: same bits
+    # one coefficient: a constant strain, as LinearFunction's
+    fl = ConvectionFlame(n_points=5, strain_type=STRAIN_CHEBYSHEV, cheb_t0=0.0, cheb_t1=1.0, cheb=(350.0,))
+    assert oc.strain(fl, 0.3) == (350.0, 0.0)
+
+
 def _numpy_utw(fl, x, t, U, T, Wm, drhodt, sU, sT, sW):
     """Independent vectorised restatement of ConvectionSystemUTW::f."""
     N = len(x)
@@ -110,14 +154,7 @@ def _numpy_utw(fl, x, t, U, T, Wm, drhodt, sU, sT, sW):
     V = rV.copy()
     if fl.alpha:
         V[1:] = rV[1:] / x[1:]
-    if t <= fl.strain_t0:
-        a = fl.strain_initial
-    elif t >= fl.strain_t0 + fl.strain_dt:
-        a = fl.strain_final
-    else:
-        a = fl.strain_initial + (fl.strain_final - fl.strain_initial) * (t - fl.strain_t0) / fl.strain_dt
-    dadt = (fl.strain_final - fl.strain_initial) / fl.strain_dt \
-        if fl.strain_t0 <= t < fl.strain_t0 + fl.strain_dt else 0.0
+    a, dadt = _numpy_strain(fl, t)
     src = fl.rhou / rho * (dadt / fl.beta + a * a / fl.beta ** 2)
     dU, dT, dW = np.zeros(N), np.zeros(N), np.zeros(N)
     fwd = rV[1:jj] < 0
@@ -161,6 +198,8 @@ CASES = [
     dict(continuity_bc=CONT_TEMP, j_cont=39),   # the last point: backward difference only
     dict(continuity_bc=CONT_RIGHT, j_cont=39, rv_cont=-0.4),
     dict(continuity_bc=CONT_QDOT, j_cont=11, rv_cont=0.1, alpha=1, left_bc=BC_ZERO_GRADIENT),
+    dict(continuity_bc=CONT_LEFT, rv_zero=0.3, strain_type=STRAIN_CHEBYSHEV, cheb_t0=0.0, cheb_t1=5e-5,
+         cheb=(300.0, 120.0, -40.0, 15.0)),
 ]
 
 

@@ -516,3 +516,56 @@ def test_balanced_split_constants_add_up_to_the_cross_rate(with_convection):
         np.testing.assert_allclose(ss + fs, 2.0 * rate, atol=1e-9)
     sd, ss, sc = osplit.split_constants(fd, fs, fx, False, fc if with_convection else None)
     np.testing.assert_array_equal(sd, fx)
+
+
+@pytest.mark.gpu
+def test_split_with_chebyshev_strain_vs_oracle(gpu_lib, mech):
+    # ember_split_set_strain: every flame's strain rate becomes a Chebyshev
+    # series (the reference's strainfunc after setCoefficients); bitwise
+    # against the oracle with the same series attached from the start, and
+    # an update between captured-graph replays reaches the graph
+    from dataclasses import replace
+    from oracle.chem import OracleMech
+    from ember_gb300.convection import STRAIN_CHEBYSHEV, ConvectionOptions
+    grids, state, B, D, flames, y_left = _convection_case(mech)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    dt = 5e-7
+    copts = ConvectionOptions()
+    coeffs = np.array([[0.0, 3 * dt, a, 0.3 * a, -0.1 * a, 0.05 * a] for a in (200.0, 500.0)])
+    cheb = [replace(fl, strain_type=STRAIN_CHEBYSHEV, cheb_t0=c[0], cheb_t1=c[1], cheb=tuple(c[2:]))
+            for fl, c in zip(flames, coeffs)]
+    ref, rt, *_ = osplit.split_steps(OracleMech(mech), grids, state, 0.0, B, D, dt, 3, QSS, opts,
+                                     convection=(cheb, y_left, copts))
+    outs = {}
+    for graph in (False, True):
+        gm, s = _gpu_solver(mech, grids, dt, QSS, opts, L.DIFFUSION_SERIAL)
+        s.set_state(0.0, state)
+        s.set_transport(B, D)
+        s.set_convection(flames, y_left, copts)
+        s.set_strain_chebyshev(coeffs)
+        s.step(3, graph=graph)
+        out, t = s.state()
+        assert t == rt
+        assert np.array_equal(out, ref), (graph, np.abs(out - ref).max())
+        # linear strain for one captured step, then the series
+        s.set_state(0.0, state)
+        s.set_convection(flames, y_left, copts)
+        s.step(1, graph=graph)
+        s.set_strain_chebyshev(coeffs)
+        s.step(2, graph=graph)
+        outs[graph] = s.state()[0]
+    assert np.array_equal(outs[False], outs[True])
+    assert not np.array_equal(outs[False], ref)
+    # a one-coefficient series is a constant strain: LinearFunction's bits
+    const = np.array([[0.0, 3 * dt, fl.strain_initial] for fl in flames])
+    res = []
+    for use_cheb in (False, True):
+        gm, s = _gpu_solver(mech, grids, dt, QSS, opts, L.DIFFUSION_SERIAL)
+        s.set_state(0.0, state)
+        s.set_transport(B, D)
+        s.set_convection(flames, y_left, copts)
+        if use_cheb:
+            s.set_strain_chebyshev(const)
+        s.step(2)
+        res.append(s.state()[0])
+    assert np.array_equal(res[0], res[1])
