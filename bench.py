@@ -48,7 +48,7 @@ def parse_args():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--workload", default="qss", choices=["qss", "bdf", "diffusion", "split", "adjoint", "transport",
-                                                             "convection"])
+                                                             "convection", "sweep"])
     p.add_argument("--points", type=int, default=N_POINTS)
     p.add_argument("--kinetics", default="interp", choices=["interp", "standard"])
     p.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU baseline sample")
@@ -67,6 +67,8 @@ def parse_args():
                    help="split workload: source-term integrator (the C5 sweep names BDF)")
     p.add_argument("--no-secondary", action="store_true",
                    help="qss workload: skip the secondary figures (BDF, diffusion, split steps, adjoint)")
+    p.add_argument("--regrid-interval", type=int, default=20,
+                   help="sweep workload: steps between regrids (regridStepInterval)")
     p.add_argument("--threads", type=int, default=0,
                    help="QSS threads per point; 0: ember_source_autotune picks it before the timed region")
     return p.parse_args()
@@ -1328,6 +1330,78 @@ SECONDARY = (
 RUNNERS = {}
 
 
+# ------------------------------------------- strain sweep run (C5 loop) --
+
+SWEEP_METRIC = "ms per split step with regrids and termination tests"
+
+
+def run_ours_sweep(args):
+    """The C5 proxy through FlameBatchRun: split steps of the 32-flame batch
+    with FlameSolver's loop around them (heat release and consumption speed
+    recorded every step, termination tests every 10 steps, a regrid of every
+    flame every --regrid-interval steps with the batch rebuilt on the new
+    grids and its graph captured again). The timed region is the whole loop,
+    host work included."""
+    import numpy as np
+    import torch
+    ws, rank, local = dist_info()
+    from ember_gb300.source import GpuMechanism, QSS, BDF, autotune, tuning
+    from ember_gb300.sweep import FlameBatchRun, TerminationOptions
+    from ember_gb300.transport import GpuTransport, synthetic_transport
+    mech, grids, state, B, D, rho_u, ju, jb = split_inputs(rank, args.mech)
+    opts = source_options(args.kinetics, args.source)
+    method = QSS if args.source == "qss" else BDF
+    split_dt = args.split_dt or SPLIT_DT
+    conv = None
+    if args.convection:
+        from ember_gb300.convection import ConvectionOptions
+        flames, y_left = split_convection(mech, grids, state, rho_u)
+        conv = (flames, y_left, ConvectionOptions())
+    gm = GpuMechanism(mech)
+    width, tune_ms = autotune(gm, method, state, np.full(len(state), split_dt), opts)
+    gtr = GpuTransport(gm, synthetic_transport(mech, seed=SPLIT_TRANSPORT_SEED))
+    term = TerminationOptions(regrid_step_interval=args.regrid_interval)
+    strains = list(np.geomspace(100.0, 2000.0, len(grids)))
+    run = FlameBatchRun(gm, gtr, grids, state, split_dt, rho_u, method=method, source_options=opts,
+                        threshold=SPLIT_THRESHOLD, convection=conv, strain_rates=strains, termination=term)
+    run.run(args.warmup)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    rebuilds0, steps0 = run.n_rebuilds, run.n_steps
+    t0 = time.perf_counter()
+    run.run(args.steps)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    steps = run.n_steps - steps0
+    ms = 1e3 * wall / max(steps, 1)
+    recs = run.records
+    sc_last = [r.Sc[-1] for r in recs]
+    n_pts = [r.n_points[-1] for r in recs]
+    line = {
+        "metric": SWEEP_METRIC, "value": ms, "unit": "ms", "n_gpus": ws, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded flame-like profiles, synthetic transport)",
+        "config": {"workload": split_workload(args, mech) + f"; FlameSolver loop: regrid every {args.regrid_interval} "
+                               "steps, termination test every 10", "flames": len(grids),
+                   "threads_per_point": width, "tuning": tuning(gm),
+                   "rebuilds_in_timed_region": run.n_rebuilds - rebuilds0,
+                   "points_at_end": int(sum(n_pts)), "points_per_flame_at_end": [int(n) for n in n_pts],
+                   "consumption_speed_at_end": sc_last,
+                   "terminated": [r.terminated for r in recs],
+                   "heat_release_rms_variation": [r.rms_rel for r in recs],
+                   "timing": "wall clock around the whole loop (host regrid and rebuilds included), after "
+                             f"{args.warmup} untimed steps"},
+        "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                "note": "the loop is driven from the host API; the state stays on the device between regrids"},
+        "gpu_launches": None,
+        "clocks": clocks,
+    }
+    return line
+
+
 def run_secondary(args) -> dict:
     """Each secondary workload at its own configuration, with W >= 3 warm-up
     steps and a few timed steps; every entry carries its own roofline,
@@ -1354,7 +1428,8 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         ref = {"transport": run_reference_transport, "convection": run_reference_convection,
-               "diffusion": run_reference_diffusion, "split": run_reference_split, "adjoint": run_reference_adjoint}
+               "diffusion": run_reference_diffusion, "split": run_reference_split, "sweep": run_reference_split,
+               "adjoint": run_reference_adjoint}
         return ref.get(args.workload, run_reference)(args)
     import torch
     ws, rank, local = dist_info()
@@ -1363,7 +1438,7 @@ def main():
         torch.distributed.init_process_group("nccl")
     RUNNERS.update({"qss": run_ours, "bdf": run_ours, "transport": run_ours_transport,
                     "convection": run_ours_convection, "diffusion": run_ours_diffusion, "split": run_ours_split,
-                    "adjoint": run_ours_adjoint})
+                    "adjoint": run_ours_adjoint, "sweep": run_ours_sweep})
     try:
         line = RUNNERS[args.workload](args)
         if args.workload == "qss" and not args.no_secondary:

@@ -43,9 +43,10 @@ struct BdfSmem {
     double *acor, *acorp, *ewt, *y, *ft, *bb, *f0, *ycopy, *f1;
     double* rdiag;  // 1 / pivot of each column of the LU factors
     int* piv;
+    int* perm;      // the row interchanges composed: after them, row i holds original row perm[i]
     // shared-memory doubles (zs_smem: the saved array in shared memory)
     static __host__ __device__ size_t doubles(int n, bool zs_smem = true) {
-        return size_t(zs_smem ? 2 * kQmax + 3 + 10 : kQmax + 2 + 10) * n + (n + 1) / 2;
+        return size_t(zs_smem ? 2 * kQmax + 3 + 10 : kQmax + 2 + 10) * n + 2 * ((n + 1) / 2);
     }
     // zs_global: (kQmax + 1) n doubles of global memory for zs, or null
     __device__ void carve(double* base, int n, double* zs_global = nullptr) {
@@ -69,6 +70,7 @@ struct BdfSmem {
         f1 = p; p += n;
         rdiag = p; p += n;
         piv = reinterpret_cast<int*>(p);
+        perm = piv + 2 * ((n + 1) / 2);
     }
 };
 
@@ -431,7 +433,24 @@ struct BdfPoint {
             if (tid == 0) s_next = 0;
             __syncthreads();
         }
+        lu_compose_interchanges();
         return 0;
+    }
+
+    // v.perm from v.piv (the interchanges applied in order to the identity),
+    // so that a solve gathers its right-hand side in one pass.
+    __device__ void lu_compose_interchanges() {
+        if (threadIdx.x == 0) {
+            int* pm = v.perm;
+            for (int i = 0; i < n; ++i) pm[i] = i;
+            for (int k = 0; k < n; ++k) {
+                const int p = v.piv[k];
+                const int t = pm[k];
+                pm[k] = pm[p];
+                pm[p] = t;
+            }
+        }
+        __syncthreads();
     }
 
     // Solve M^T w = b in place with the factors and pivots of lu_factor
@@ -500,10 +519,73 @@ struct BdfPoint {
         }
     }
 
-    // Forward and back substitution with the factors, by the first warp
-    // (warp barriers instead of block barriers between the n steps).
+    // Forward and back substitution with the factors, by the first warp, with
+    // the right-hand side in its registers (lane l holds rows l, l + 32, ...):
+    // the row interchanges as one gather through v.perm, then per column a
+    // shuffle broadcast and one fma per row held (L unit lower), and per
+    // column the product with the pivot reciprocal then the updates above
+    // (U). Each element receives the same operations in the same order as
+    // SUNDIALS' dense getrs with fused multiply-adds.
+    static constexpr int kSolveRegRows = 8;  // n <= 256
     __device__ void lu_solve(double* b) {
         __syncthreads();
+        if (n > 32 * kSolveRegRows) {
+            lu_solve_smem(b);
+            return;
+        }
+        if (threadIdx.x < 32) {
+            const int lane = threadIdx.x;
+            double r[kSolveRegRows];
+#pragma unroll
+            for (int j = 0; j < kSolveRegRows; ++j) {
+                const int i = 32 * j + lane;
+                r[j] = i < n ? b[v.perm[i]] : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < kSolveRegRows; ++j) {
+                if (32 * j < n) {
+                    const int kend = min(32, n - 32 * j);
+                    for (int kk = 0; kk < kend; ++kk) {
+                        const int k = 32 * j + kk;
+                        const double bk = __shfl_sync(0xffffffffu, r[j], kk);
+                        const double* colk = M + size_t(k) * n;
+#pragma unroll
+                        for (int jj = j; jj < kSolveRegRows; ++jj) {
+                            if (32 * jj >= n) break;  // uniform: no issue slots for rows beyond n
+                            const int i = 32 * jj + lane;
+                            if (i > k && i < n) r[jj] = fma(-colk[i], bk, r[jj]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = kSolveRegRows - 1; j >= 0; --j) {
+                if (32 * j < n) {
+                    const int kend = min(32, n - 32 * j);
+                    for (int kk = kend - 1; kk >= 0; --kk) {
+                        const int k = 32 * j + kk;
+                        const double bk = __shfl_sync(0xffffffffu, r[j], kk) * v.rdiag[k];
+                        if (lane == kk) r[j] = bk;
+                        const double* colk = M + size_t(k) * n;
+#pragma unroll
+                        for (int jj = 0; jj <= j; ++jj) {
+                            const int i = 32 * jj + lane;
+                            if (i < k) r[jj] = fma(-colk[i], bk, r[jj]);
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < kSolveRegRows; ++j) {
+                const int i = 32 * j + lane;
+                if (i < n) b[i] = r[j];
+            }
+        }
+        __syncthreads();
+    }
+
+    // The same in shared memory, for n > 256.
+    __device__ void lu_solve_smem(double* b) {
         if (threadIdx.x < 32) {
             const int lane = threadIdx.x;
             if (lane == 0)
@@ -541,8 +623,11 @@ struct BdfPoint {
 //                 (M is read by every Newton solve, J once per matrix update);
 //                 to make room, the rates of progress and the saved Nordsieck
 //                 array move to that slice as well;
-//   BDF_JM_GLOBAL both in the global slice.
-enum : int { BDF_JM_GLOBAL = 0, BDF_JM_SMEM = 1, BDF_M_SMEM = 2 };
+//   BDF_JM_GLOBAL both in the global slice;
+//   BDF_M_ROP_SMEM M and the rates of progress in shared memory, J and the
+//                 saved Nordsieck array in the global slice (more points per
+//                 SM than BDF_JM_SMEM, the species sums still on chip).
+enum : int { BDF_JM_GLOBAL = 0, BDF_JM_SMEM = 1, BDF_M_SMEM = 2, BDF_M_ROP_SMEM = 3 };
 
 struct BdfLayout {
     int mode;
@@ -560,10 +645,13 @@ inline BdfLayout bdf_layout_of(const MechView& m, int mode) {
     const size_t full = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(3) * m.n_fo + BdfSmem::doubles(int(n));
     const size_t lean = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true, false) + size_t(3) * m.n_fo +
                         BdfSmem::doubles(int(n), false);
+    const size_t mrop_smem = ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true) + size_t(3) * m.n_fo +
+                             BdfSmem::doubles(int(n), false) + nn;
     const BdfLayout both{BDF_JM_SMEM, (full + 2 * nn) * sizeof(double), 0};
     const BdfLayout lu{BDF_M_SMEM, (lean + nn) * sizeof(double), nn + size_t(kQmax + 1) * n + size_t(2) * m.R};
     const BdfLayout none{BDF_JM_GLOBAL, full * sizeof(double), 2 * nn};
-    const BdfLayout opts[3] = {both, lu, none};
+    const BdfLayout mrop{BDF_M_ROP_SMEM, mrop_smem * sizeof(double), nn + size_t(kQmax + 1) * n};
+    const BdfLayout opts[4] = {both, lu, none, mrop};
     for (const BdfLayout& l : opts) {
         const bool fits = l.smem_bytes <= kBdfSmemBudget;
         if (mode < 0 && fits) return l;
@@ -590,17 +678,18 @@ __device__ __forceinline__ void bdf_carve(BdfPoint<NT>& P, double* smem, double*
     const MechView& m = P.m;
     const int n = m.S + 2;
     const size_t nn = size_t(n) * n;
-    const bool lean = mode == BDF_M_SMEM;
+    const bool lean = mode == BDF_M_SMEM;            // rates of progress and saved Nordsieck array global
+    const bool zs_global = lean || mode == BDF_M_ROP_SMEM;
     P.w.carve(smem, kc, m, true, lean ? g + nn + size_t(kQmax + 1) * n : nullptr);
     P.w.fo_F = smem + ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, true, !lean);
     P.w.fo_pr = P.w.fo_F + m.n_fo;
     P.w.fo_dF = P.w.fo_pr + m.n_fo;
-    P.v.carve(P.w.fo_dF + m.n_fo, n, lean ? g + nn : nullptr);
-    double* after = P.w.fo_dF + m.n_fo + BdfSmem::doubles(n, !lean);
+    P.v.carve(P.w.fo_dF + m.n_fo, n, zs_global ? g + nn : nullptr);
+    double* after = P.w.fo_dF + m.n_fo + BdfSmem::doubles(n, !zs_global);
     if (mode == BDF_JM_SMEM) {
         P.J = after;
         P.M = after + nn;
-    } else if (lean) {
+    } else if (zs_global) {
         P.J = g;
         P.M = after;
     } else {
@@ -1034,7 +1123,7 @@ int source_bdf_threads(const MechView& m, const SourceArgs& a) {
 int source_bdf_layout(const MechView& m, const SourceArgs& a) { return 1 + bdf_layout(m, a).mode; }
 
 bool source_bdf_layout_fits(const MechView& m, int layout) {
-    return layout >= 1 && layout <= 3 && bdf_layout_of(m, layout - 1).smem_bytes != 0;
+    return layout >= 1 && layout <= 4 && bdf_layout_of(m, layout - 1).smem_bytes != 0;
 }
 
 int source_bdf_scratch_bytes(const MechView& m, const SourceArgs& a, size_t* bytes) {

@@ -41,7 +41,8 @@ __global__ void k_probe_dmma(double* out, int iters) {
 
 // Issue cost of FP64 warp instructions: one CTA of `warps` warps per SM,
 // lanes below `active` running `iters` x CHAINS operations (MODE 0: DFMA,
-// 1: DADD, 2: DMUL, 3: division), clocked per CTA with clock64.
+// 1: DADD, 2: DMUL, 3: division, 4: fmax, 5: compare-and-select), clocked
+// per CTA with clock64.
 template <int CHAINS, int MODE>
 __global__ void k_probe_issue(double* sink, long long* cyc, int iters, int active) {
     const int lane = threadIdx.x & 31;
@@ -59,7 +60,9 @@ __global__ void k_probe_issue(double* sink, long long* cyc, int iters, int activ
                 if (MODE == 0) acc[c] = fma(acc[c], s, 0.25);
                 else if (MODE == 1) acc[c] = acc[c] + s;
                 else if (MODE == 2) acc[c] = acc[c] * s;
-                else acc[c] = s / acc[c];
+                else if (MODE == 3) acc[c] = s / acc[c];
+                else if (MODE == 4) acc[c] = fmax(acc[c] - s, s * 0.5);
+                else acc[c] = (acc[c] < s) ? acc[c] + s : acc[c] - s;
             }
         }
     }
@@ -79,7 +82,8 @@ using namespace ember;
 
 extern "C" int ember_probe_fp64_issue(int op, int chains, int warps, int active_lanes, double* cycles_per_inst) {
     EMBER_CHECK_ARG(cycles_per_inst != nullptr, "null output");
-    EMBER_CHECK_ARG(op >= 0 && op <= 3, "op must be 0 (DFMA), 1 (DADD), 2 (DMUL) or 3 (division)");
+    EMBER_CHECK_ARG(op >= 0 && op <= 5,
+                    "op must be 0 (DFMA), 1 (DADD), 2 (DMUL), 3 (division), 4 (fmax + DADD) or 5 (compare + DADD)");
     EMBER_CHECK_ARG(chains == 1 || chains == 8, "chains must be 1 or 8");
     EMBER_CHECK_ARG(warps >= 1 && warps <= 32, "warps must be 1..32");
     EMBER_CHECK_ARG(active_lanes >= 1 && active_lanes <= 32, "active_lanes must be 1..32");
@@ -105,7 +109,11 @@ extern "C" int ember_probe_fp64_issue(int op, int chains, int warps, int active_
         case 4: kern = k_probe_issue<1, 2>; break;
         case 5: kern = k_probe_issue<8, 2>; break;
         case 6: kern = k_probe_issue<1, 3>; break;
-        default: kern = k_probe_issue<8, 3>; break;
+        case 7: kern = k_probe_issue<8, 3>; break;
+        case 8: kern = k_probe_issue<1, 4>; break;
+        case 9: kern = k_probe_issue<8, 4>; break;
+        case 10: kern = k_probe_issue<1, 5>; break;
+        default: kern = k_probe_issue<8, 5>; break;
     }
     for (int rep = 0; rep < 2; ++rep) kern<<<sms, warps * 32>>>(sink, cyc, iters, active_lanes);
     cudaError_t err = cudaDeviceSynchronize();

@@ -681,6 +681,7 @@ int source_check_options(const ember_source_options* o) {
                     o->threads_per_point);
     EMBER_CHECK_ARG(tail_ok && o->qss_tail_steps >= -1, "bad QSS two-pass schedule (%d steps, %d threads)",
                     o->qss_tail_steps, o->qss_tail_threads);
+    EMBER_CHECK_ARG(o->bdf_layout >= 0 && o->bdf_layout <= 4, "bdf_layout must be 0..4 (got %d)", o->bdf_layout);
     EMBER_CHECK_ARG(o->qss_tail_steps <= 0 || o->qss_stability_check == 0,
                     "the QSS two-pass schedule cannot be combined with the stability check");
     return EMBER_OK;
@@ -724,6 +725,8 @@ SourceArgs make_source_args(const ember_source_options* o, int n, const double* 
     a.ign_stddev = o->ignition_stddev;
     a.tail_steps = o->qss_tail_steps;
     a.tail_threads = o->qss_tail_threads;
+    // public placement code -> 1 + BdfLayout mode (bdf.cu)
+    a.bdf_layout = o->bdf_layout == 1 ? 2 : o->bdf_layout == 2 ? 3 : o->bdf_layout == 3 ? 1 : o->bdf_layout == 4 ? 4 : 0;
     a.queue_chunk = 0;  // the mechanism's tuned granularity
     return a;
 }
@@ -966,7 +969,7 @@ extern "C" int ember_source_autotune(ember_mech m, int method, int n, const doub
         bool valid = !bdf;
         for (int c : kBdfThreadChoices) valid = valid || width == c;
         if (!valid) continue;
-        for (int layout = bdf ? 1 : 0; layout <= (bdf ? 3 : 0) && rc == EMBER_OK; ++layout) {
+        for (int layout = bdf ? 1 : 0; layout <= (bdf ? 4 : 0) && rc == EMBER_OK; ++layout) {
             if (bdf && !source_bdf_layout_fits(m->view, layout)) continue;
             ember_source_options o = *opts;
             o.threads_per_point = width;
@@ -1097,9 +1100,10 @@ extern "C" int ember_mech_get_tuning(ember_mech m, int* qss_threads, int* qss_ta
     if (qss_chunk) *qss_chunk = m->view.qss_chunk;
     if (bdf_threads) *bdf_threads = m->view.bdf_threads;
     if (bdf_layout) {
-        // BdfLayout modes (bdf.cu): 0 global, 1 both in shared memory, 2 LU only -> 3, 1, 2
+        // BdfLayout modes (bdf.cu): 0 global, 1 both in shared memory, 2 LU only, 3 LU and rates of
+        // progress -> 3, 1, 2, 4
         const int l = m->view.bdf_layout;
-        *bdf_layout = l == 0 ? 0 : (l == 1 ? 3 : (l == 2 ? 1 : 2));
+        *bdf_layout = l == 0 ? 0 : (l == 1 ? 3 : (l == 2 ? 1 : (l == 3 ? 2 : 4)));
     }
     return EMBER_OK;
 }

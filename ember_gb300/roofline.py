@@ -158,6 +158,8 @@ FP64_ISSUE_CASES = (
     ("DADD issue, 8 warps/SM", 1, 8, 8, 32),
     ("DMUL issue, 8 warps/SM", 2, 8, 8, 32),
     ("division issue, 8 warps/SM", 3, 8, 8, 32),
+    ("fmax + DADD issue, 8 warps/SM", 4, 8, 8, 32),
+    ("compare-select + DADD issue, 8 warps/SM", 5, 8, 8, 32),
 )
 
 

@@ -37,7 +37,7 @@ class SourceOptions(C.Structure):
         ("threads_per_point", C.c_int),
         ("ignition_tstart", C.c_double), ("ignition_duration", C.c_double), ("ignition_energy", C.c_double),
         ("ignition_center", C.c_double), ("ignition_stddev", C.c_double),
-        ("qss_tail_steps", C.c_int), ("qss_tail_threads", C.c_int),
+        ("qss_tail_steps", C.c_int), ("qss_tail_threads", C.c_int), ("bdf_layout", C.c_int),
     ]
 
     @classmethod
@@ -55,6 +55,7 @@ class SourceOptions(C.Structure):
         o.ignition_center, o.ignition_stddev = 0.0, 1e-4
         o.threads_per_point = 0  # the mechanism's autotuned width, else the default for its size
         o.qss_tail_steps, o.qss_tail_threads = 0, 0  # the mechanism's autotuned schedule, else one pass
+        o.bdf_layout = 0  # the mechanism's autotuned matrix placement, else the first that fits
         for k, v in kw.items():
             if not hasattr(o, k):
                 raise AttributeError(k)

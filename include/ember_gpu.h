@@ -74,8 +74,9 @@ int ember_probe_fp64_rate(int kind, double* flops_per_second);
 /* Cycles per FP64 warp instruction as seen by one warp: one CTA of `warps`
  * warps on every SM, the first `active_lanes` lanes of each warp running
  * `chains` (1: a dependent chain, latency; 8: independent chains, issue
- * rate) of op 0 (DFMA), 1 (DADD), 2 (DMUL) or 3 (division); the median over
- * SMs. No reference counterpart. */
+ * rate) of op 0 (DFMA), 1 (DADD), 2 (DMUL), 3 (division), 4 (fmax and a
+ * DADD) or 5 (a compare, a DADD and a select); the median over SMs. No
+ * reference counterpart. */
 int ember_probe_fp64_issue(int op, int chains, int warps, int active_lanes, double* cycles_per_inst);
 
 /* ======================================================================
@@ -497,6 +498,11 @@ typedef struct {
      * stiffest points finish sooner. Results do not depend on it. Not with
      * qss_stability_check. */
     int qss_tail_steps, qss_tail_threads;
+    /* BDF placement of the Jacobian and LU factors (codes of
+     * ember_mech_get_tuning: 1 both in shared memory, 2 LU only, 3 neither,
+     * 4 LU and the rates of progress); 0: the mechanism's tuned placement,
+     * else the first that fits. Results do not depend on it. */
+    int bdf_layout;
 } ember_source_options;
 
 /* Fill `opts` with the reference's defaults (pressure 1 atm, interp kinetics). */
@@ -534,7 +540,8 @@ int ember_source_autotune(ember_mech mech, int method, int n_points, const doubl
 /* The launch configuration stored in the mechanism by ember_source_autotune
  * (0 where none was chosen): QSS width, QSS two-pass steps and tail width, QSS
  * work-queue granularity (points a CTA claims per atomic), BDF width, BDF
- * matrix placement (1: J and LU in shared memory, 2: LU only, 3: neither).
+ * matrix placement (1: J and LU in shared memory, 2: LU only, 3: neither,
+ * 4: LU and the rates of progress).
  * ember_source_autotune changes the mechanism handle: do not call it while
  * other threads launch work with the same mechanism. */
 int ember_mech_get_tuning(ember_mech mech, int* qss_threads, int* qss_tail_steps, int* qss_tail_threads,
