@@ -64,7 +64,7 @@ def test_batch_run_regrids_and_terminates(gpu_lib, with_convection):
         flames, y_left, p = [], [], 0
         for f, g in enumerate(grids):
             N = g.n_points
-            a = 200.0 + 300.0 * f
+            a = 200.0 + 100.0 * f
             state[p:p + N, 0] = a * np.sqrt(rho_u[f] / rho[p:p + N])
             y0 = state[p, 2:].copy()
             flames.append(ConvectionFlame(n_points=N, left_bc=g.left_bc, right_bc=g.right_bc, alpha=g.alpha,
@@ -76,17 +76,24 @@ def test_batch_run_regrids_and_terminates(gpu_lib, with_convection):
         conv = (flames, np.array(y_left), ConvectionOptions())
     gm = GpuMechanism(mech)
     gt = GpuTransport(gm, td)
-    # no tolerance at first (nothing terminates), regrids every second step
-    term = TerminationOptions(tolerance=0.0, abstol=0.0, steady_period=4 * dt, terminate_step_interval=3,
-                              regrid_step_interval=2)
+    # No tolerance at first (nothing terminates), regrids every second step.
+    # The seeded profiles are not converged flames. With the convection stage
+    # attached, their first step after a regrid stays bounded, but the
+    # convection systems of a flame fail within two steps of the second regrid
+    # (the oracle, stepped through the same sequence of split steps and
+    # regrids, fails in the same steps). The convection variant therefore
+    # regrids once and terminates at the step after it.
+    n_first = 2 if with_convection else 4
+    term = TerminationOptions(tolerance=0.0, abstol=0.0, steady_period=(1.5 if with_convection else 4.0) * dt,
+                              terminate_step_interval=3, regrid_step_interval=2)
     run = FlameBatchRun(gm, gt, grids, state, dt, rho_u, method=QSS,
                         source_options=SourceOptions.defaults(kinetics_model=KINETICS_STANDARD),
                         convection=conv, strain_rates=[200.0, 500.0], termination=term,
                         diffusion_algorithm=L.DIFFUSION_SERIAL)
-    recs = run.run(4)
-    assert run.n_steps == 4 and len(recs[0].t) == 4
+    recs = run.run(n_first)
+    assert run.n_steps == n_first and len(recs[0].t) == n_first
     assert run.n_rebuilds >= 1                      # the regrids changed the grids
-    assert recs[0].n_points[-1] != grids[0].n_points or recs[1].n_points[-1] != grids[1].n_points
+    assert run.grids[0].n_points != grids[0].n_points or run.grids[1].n_points != grids[1].n_points
     # an absolute tolerance that any variation meets: both flames terminate at the next test
     run.termination.abstol = 1e30
     recs = run.run(6)
