@@ -17,7 +17,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SOURCES = ["oracle_tridiag.c", "oracle_chem.c", "oracle_bdf.c", "oracle_testode.c", "oracle_transport.c",
-           "oracle_convection.c"]
+           "oracle_convection.c", "oracle_qss_adjoint.c"]
 TARGET = os.path.join(HERE, "liboracle.so")
 
 

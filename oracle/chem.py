@@ -28,6 +28,8 @@ def declare(l):
     l.oracle_gas_eval.restype = None
     l.oracle_source_batch.argtypes = [vp, i, i, vp, vp, vp, d, vp, vp, vp, vp, vp, i]
     l.oracle_source_batch.restype = None
+    l.oracle_qss_adjoint_batch.argtypes = [vp, i, vp, vp, vp, d, vp, vp, vp, vp, vp, vp, vp, vp, i]
+    l.oracle_qss_adjoint_batch.restype = None
     l.oracle_exp.argtypes = [d]
     l.oracle_exp.restype = d
     l.oracle_log.argtypes = [d]
@@ -91,6 +93,28 @@ class OracleMech:
         _lib().oracle_source_batch(self._h, method, n, _p(state), _p(sc), _p(dt), float(t_start), _p(xx),
                                    C.addressof(opts), _p(out), _p(status), _p(stats), int(nt))
         return out, status, stats
+
+
+def qss_adjoint(om: OracleMech, state, dt, opts, state_bar, split_const=None, t_start=0.0, x=None, n_threads=None):
+    """Discrete adjoint of the QSS integration of a batch of points
+    (oracle_qss_adjoint.c): for phi = sum state_bar . state_out, returns
+    (state_out, d phi / d state_in, d phi / d ln(multiplier) per point
+    [n, R], status, steps)."""
+    state = np.ascontiguousarray(state, dtype=np.float64)
+    n = state.shape[0]
+    dt = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,)))
+    sc = np.ascontiguousarray(split_const, dtype=np.float64) if split_const is not None else None
+    xx = np.ascontiguousarray(x, dtype=np.float64) if x is not None else None
+    bar = np.ascontiguousarray(np.broadcast_to(state_bar, state.shape), dtype=np.float64)
+    out = np.empty_like(state)
+    ybar = np.zeros_like(state)
+    pbar = np.zeros((n, om.R))
+    status = np.zeros(n, dtype=np.int32)
+    steps = np.zeros(n, dtype=np.int32)
+    nt = n_threads or os.cpu_count() or 1
+    _lib().oracle_qss_adjoint_batch(om._h, n, _p(state), _p(sc), _p(dt), float(t_start), _p(xx), C.addressof(opts),
+                                    _p(bar), _p(out), _p(ybar), _p(pbar), _p(status), _p(steps), int(nt))
+    return out, ybar, pbar, status, steps
 
 
 def exp(x):

@@ -125,6 +125,17 @@ int oracle_qss_point(const oracle_mech* m, oracle_ws* w, const oracle_source_opt
                      const double* split, double tf, double t_start, double x, int* stats);
 int oracle_bdf_point(const oracle_mech* m, oracle_ws* w, const oracle_source_options* o, double* y,
                      const double* split, double tf, double t_start, double x, int* stats);
+/* Sum over species in the GPU block reductions' order (oracle_chem.c). */
+double oracle_block_sum(const double* a, const double* b, int n, int W);
+int oracle_reduction_width(int S);
+/* Discrete adjoint of the QSS source-term integration (oracle_qss_adjoint.c). */
+int oracle_qss_adjoint_point(const oracle_mech* m, oracle_ws* w, const oracle_source_options* o, const double* y_in,
+                             const double* split, double tf, double t_start, double x, const double* ybar_out,
+                             double* y_out, double* ybar_in, double* pbar, int* n_steps);
+void oracle_qss_adjoint_batch(const oracle_mech* m, int n, const double* state_in, const double* split,
+                              const double* dt, double t_start, const double* x, const oracle_source_options* o,
+                              const double* ybar_out, double* state_out, double* ybar_in, double* pbar, int* status,
+                              int* steps, int n_threads);
 void oracle_source_batch(const oracle_mech* m, int method, int n, const double* state_in, const double* split,
                          const double* dt, double t_start, const double* x, const oracle_source_options* o,
                          double* state_out, int* status, int* stats, int n_threads);
