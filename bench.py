@@ -64,7 +64,7 @@ def parse_args():
     p.add_argument("--convection", action="store_true",
                    help="split workload: the reference's full D C D S D C D step with the convection stage")
     p.add_argument("--source", default="qss", choices=["qss", "bdf"],
-                   help="split workload: source-term integrator (the C5 sweep names BDF)")
+                   help="split and adjoint workloads: source-term integrator (the C5 sweep names BDF)")
     p.add_argument("--no-secondary", action="store_true",
                    help="qss workload: skip the secondary figures (BDF, diffusion, split steps, adjoint)")
     p.add_argument("--regrid-interval", type=int, default=20,
@@ -885,8 +885,15 @@ def run_ours_split(args):
 ADJ_METRIC = "adjoint/forward cost"
 ADJ_DT = 2e-5
 ADJ_WORKLOAD = ("C4 proxy: one flame-like profile of 400 points, synthetic 53-species/325-reaction mechanism "
-                "(GRI-3.0 sizes), balanced D-S-D split step (dt 2e-5 s, BDF source with CVODE default tolerances), "
+                "(GRI-3.0 sizes), balanced D-S-D split step (dt 2e-5 s, {src}), "
                 "gradient of heat release + consumption speed w.r.t. the start state and ln A of every reaction")
+ADJ_SOURCES = {"bdf": "BDF source with CVODE default tolerances",
+               "qss": "QSS source (the reference's default integrator) with its default options"}
+
+
+def adjoint_method(args):
+    from ember_gb300.source import BDF, QSS
+    return BDF if args.source == "bdf" else QSS
 
 
 def adjoint_inputs(rank: int):
@@ -902,15 +909,15 @@ def run_reference_adjoint(args):
         return 0
     from oracle.chem import OracleMech
     from oracle import split as osplit
-    from ember_gb300.source import BDF
+    method = adjoint_method(args)
     mech, grids, state, B, D, rho_u, ju, jb = adjoint_inputs(0)
-    opts = source_options(args.kinetics, "bdf")
+    opts = source_options(args.kinetics, args.source)
     om = OracleMech(mech)
     for _ in range(args.warmup):
-        osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, BDF, opts)
+        osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, method, opts)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, BDF, opts)
+        osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, method, opts)
     fwd = (time.perf_counter() - t0) / args.steps
     # the reference has no adjoint: central differences need 2 forward steps per ln A
     ratio = 2.0 * mech.n_reactions
@@ -919,7 +926,7 @@ def run_reference_adjoint(args):
         "impl": "reference", "metric": ADJ_METRIC, "value": ratio, "unit": "x", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * fwd * ratio, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": ADJ_WORKLOAD, "forward_ms": 1e3 * fwd,
+        "config": {"workload": ADJ_WORKLOAD.format(src=ADJ_SOURCES[args.source]), "forward_ms": 1e3 * fwd,
                    "gradient_method": "central differences of the CPU split step (2 steps per ln A)"},
         "cpu_baseline": {"value": ratio, "unit": "x", "cores": threads, "kind": "port",
                          "sample": f"one forward split step of the 400-point flame, {1e3 * fwd:.1f} ms"},
@@ -931,12 +938,13 @@ def run_ours_adjoint(args):
     import numpy as np
     import torch
     ws, rank, local = dist_info()
-    from ember_gb300.source import GpuMechanism, BDF
+    from ember_gb300.source import GpuMechanism
     from ember_gb300.split import FlameBatchSplitSolver
+    method = adjoint_method(args)
     mech, grids, state, B, D, rho_u, ju, jb = adjoint_inputs(rank)
-    opts = source_options(args.kinetics, "bdf")
+    opts = source_options(args.kinetics, args.source)
     gm = GpuMechanism(mech)
-    solver = FlameBatchSplitSolver(gm, grids, ADJ_DT, method=BDF, source_options=opts)
+    solver = FlameBatchSplitSolver(gm, grids, ADJ_DT, method=method, source_options=opts)
     solver.set_transport(B, D)
     stream = torch.cuda.current_stream()
     wq, wsc = np.ones(1), np.ones(1)
@@ -976,7 +984,8 @@ def run_ours_adjoint(args):
         "metric": ADJ_METRIC, "value": adj_ms / fwd_ms, "unit": "x", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": adj_ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded flame-like profile, synthetic transport)",
-        "config": {"workload": ADJ_WORKLOAD, "forward_ms": fwd_ms, "adjoint_ms": adj_ms,
+        "config": {"workload": ADJ_WORKLOAD.format(src=ADJ_SOURCES[args.source]), "forward_ms": fwd_ms,
+                   "adjoint_ms": adj_ms,
                    "gradients": int(state.size + mech.n_reactions), "heat_release": float(hr[0]),
                    "consumption_speed": float(cs[0])},
         "e2e": {"value": adj_ms / fwd_ms, "unit": "x", "h2d_bytes_per_step": int(state.nbytes),
@@ -989,13 +998,13 @@ def run_ours_adjoint(args):
         from oracle import split as osplit
         om = OracleMech(mech)
         t0 = time.perf_counter()
-        osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, BDF, opts)
+        osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, method, opts)
         tcpu = time.perf_counter() - t0
         threads = os.cpu_count() or 1
         line["cpu_baseline"] = {"value": 2.0 * mech.n_reactions, "unit": "x", "cores": threads, "kind": "port",
                                 "sample": f"central differences on the CPU split step: 2 x {mech.n_reactions} "
                                           f"forward steps of {1e3 * tcpu:.0f} ms each ({threads} threads)"}
-        ref_state, _, _, _, _ = osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, BDF, opts)
+        ref_state, _, _, _, _ = osplit.split_steps(om, grids, state, 0.0, B, D, ADJ_DT, 1, method, opts)
         _, rhr, rcs = osplit.objectives(om, grids, ref_state, opts.pressure, opts.kinetics_model, rho_u, ju, jb)
         line["parity"] = {"against": "oracle split step and objectives (FP64 CPU restatement), same start state",
                           "heat_release_rel_err": float(abs(hr[0] - rhr[0]) / abs(rhr[0])),
@@ -1324,7 +1333,8 @@ SECONDARY = (
     # failed points from step 4 and 30-280 times the integrator steps by step 10), at 5e-6 s they do not
     ("split_conv53", {"workload": "split", "mech": "53", "source": "qss", "split_dt": 5e-6, "convection": True},
      3, 4.0),
-    ("adjoint", {"workload": "adjoint"}, 3, 1.0),
+    ("adjoint", {"workload": "adjoint", "source": "bdf"}, 3, 1.0),
+    ("adjoint_qss", {"workload": "adjoint", "source": "qss"}, 3, 1.0),
 )
 
 RUNNERS = {}

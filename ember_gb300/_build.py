@@ -20,6 +20,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # Translation units whose arithmetic must match the CPU oracle operation by
 # operation: no automatic multiply-add contraction (explicit fma() only).
 FILE_FLAGS = {"source.cu": ["--fmad=false"], "bdf.cu": ["--fmad=false"], "split.cu": ["--fmad=false"],
+              "qss_adjoint.cu": ["--fmad=false"],
               "transport.cu": ["--fmad=false"], "convection.cu": ["--fmad=false"],
               # host code: the same rounding on x86-64 and aarch64 (no contraction into FMA)
               "grid.cpp": ["-Xcompiler", "-ffp-contract=off"]}

@@ -80,6 +80,8 @@ def _declare(lib):
                                              C.c_int, vp]),
         "ember_source_adjoint": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp, C.c_int, vp, vp, vp, vp,
                                            C.c_int, vp]),
+        "ember_source_adjoint_qss": (C.c_int, [vp, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp, C.c_int, vp, vp, vp,
+                                               vp, C.c_int, vp]),
         "ember_source_autotune": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp, vp, C.c_int,
                                             vp]),
         "ember_transport_create": (C.c_int, [vp, vp, vp]),

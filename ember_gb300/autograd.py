@@ -6,8 +6,8 @@ multipliers exp(ln_mult) and returns the heat release rate Q_f and the
 consumption speed S_c,f of every flame (FlameSolver::getHeatReleaseRate /
 getConsumptionSpeed after the step). Its backward pass is the hand-written
 discrete adjoint of the step (``ember_split_adjoint``): the forward step is
-recomputed from the saved start state with a tape of the BDF source stage,
-and the gradients with respect to the start state and to ln(multiplier) of
+recomputed from the saved start state with a tape of the source stage (BDF
+or QSS), and the gradients with respect to the start state and to ln(multiplier) of
 every reaction are returned.
 """
 from __future__ import annotations

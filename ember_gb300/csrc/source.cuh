@@ -94,6 +94,17 @@ int launch_objective_vjp(const MechView& m, const SourceArgs& a, int n_pts, cons
 // lnk_bar_points: per point ([n][R], or null: scratch).
 int source_bdf_adjoint_run(const MechView& m, SourceArgs a, int tape_cap, const double* ybar_out, double* ybar_in,
                            double* lnk_bar, double* lnk_bar_points, int* adj_status, Scratch& sc, cudaStream_t st);
+// Discrete adjoint of a QSS launch (qss_adjoint.cu): the forward integration
+// of every point again (state_out, status as the forward kernel's) with a
+// per-CTA tape of at most tape_cap step starts, then the backward pass: ybar_in
+// [n][S+2] and, per point, pbar [n][R]; adj_status [n]: 0, the forward status,
+// -30 (tape full), -33 (more than 32 attempts in a step).
+int launch_source_qss_adjoint(const MechView& m, const SourceArgs& a, int tape_cap, int* counter,
+                              const double* ybar_out, double* ybar_in, double* pbar, int* adj_status, Scratch& sc,
+                              cudaStream_t st);
+int source_qss_adjoint_run(const MechView& m, const SourceArgs& a, int tape_cap, const double* ybar_out,
+                           double* ybar_in, double* lnk_bar, double* lnk_bar_points, int* adj_status, Scratch& sc,
+                           cudaStream_t st);
 // SourceArgs from the public options (source.cu).
 SourceArgs make_source_args(const ember_source_options* o, int n, const double* state_in, const double* split,
                             const double* dt, double t_start, const double* x, double* state_out, int* status,

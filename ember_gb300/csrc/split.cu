@@ -1489,26 +1489,30 @@ extern "C" int ember_split_adjoint(ember_split h, const double* w_heat_release, 
                                    double* heat_release, double* consumption_speed, double* state_bar,
                                    double* lnk_bar, int mem, void* stream) {
     EMBER_TRY(check_split(h));
-    EMBER_CHECK_ARG(h->opt.method == EMBER_SOURCE_BDF, "the split-step adjoint needs EMBER_SOURCE_BDF");
+    const bool qss = h->opt.method == EMBER_SOURCE_QSS;
+    EMBER_CHECK_ARG(!qss || h->opt.source.qss_stability_check == 0,
+                    "the split-step adjoint with the QSS source needs qss_stability_check = 0");
     EMBER_CHECK_ARG(h->tr == nullptr, "the split-step adjoint holds B and D fixed: detach the transport model");
     EMBER_CHECK_ARG(!h->conv, "the split-step adjoint covers D-S-D: detach the convection stage");
     EMBER_CHECK_ARG(mem == EMBER_MEM_HOST || mem == EMBER_MEM_DEVICE, "bad mem flag %d", mem);
     EMBER_CHECK_ARG(w_heat_release || w_consumption_speed, "no objective weights");
     EMBER_CHECK_ARG(!w_consumption_speed || (rho_u && ju && jb), "consumption speed needs rho_u, ju and jb");
     EMBER_CHECK_ARG(tape_cap >= 0 && tape_cap <= (1 << 20), "bad tape_cap %d", tape_cap);
-    if (tape_cap == 0) tape_cap = 1024;
+    if (tape_cap == 0) tape_cap = qss ? 4096 : 1024;
     cudaStream_t st = as_stream(stream);
     Scratch sc(st);
     const MechView& m = h->mech->view;
     const int n = h->n_vars, S = m.S, R = std::max(m.R, 1);
     const int64_t np = h->n_pts, nv = h->n_vals;
     const int nf = h->n_flames;
-    // ---- forward: one taped step, then the objectives
+    // ---- forward: one taped step, then the objectives (the QSS adjoint
+    // replays the source stage from its input, kept in xD2, with a tape of
+    // its own)
     StepTape tape{};
-    tape.cap = tape_cap;
-    tape.stride = bdf_tape_doubles(n, tape_cap);
+    tape.cap = qss ? 0 : tape_cap;
+    tape.stride = qss ? 0 : bdf_tape_doubles(n, tape_cap);
     EMBER_TRY(sc.alloc(&tape.t_saved, 1));
-    EMBER_TRY(sc.alloc(&tape.buf, size_t(np) * tape.stride));
+    if (!qss) EMBER_TRY(sc.alloc(&tape.buf, size_t(np) * tape.stride));
     EMBER_TRY(sc.alloc(&tape.xF, size_t(nv)));
     EMBER_TRY(enqueue_step(h, st, &tape));
     double *T, *Y, *net, *hk, *cp, *q, *qcp, *work, *hr, *cs;
@@ -1590,7 +1594,15 @@ extern "C" int ember_split_adjoint(ember_split h, const double* w_heat_release, 
         int* counter = nullptr;
         EMBER_TRY(sc.alloc(&counter, 1));
         EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
-        EMBER_TRY(launch_source_bdf_adjoint(m, a, counter, ybar, ybar2, prow_src, adj_status, sc, st));
+        if (qss) {
+            // the replayed forward writes its end states into scratch, not into the step's state
+            EMBER_TRY(sc.alloc(&a.state_out, size_t(nv)));
+            a.status = nullptr;
+            a.stats = nullptr;
+            EMBER_TRY(launch_source_qss_adjoint(m, a, tape_cap, counter, ybar, ybar2, prow_src, adj_status, sc, st));
+        } else {
+            EMBER_TRY(launch_source_bdf_adjoint(m, a, counter, ybar, ybar2, prow_src, adj_status, sc, st));
+        }
         EMBER_CUDA_TRY(cudaMemcpyAsync(ybar, ybar2, sizeof(double) * nv, cudaMemcpyDeviceToDevice, st));
         k_count_failures<<<grid_for(np), 256, 0, st>>>(static_cast<int>(np), adj_status, h->fails);
     }

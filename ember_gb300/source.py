@@ -179,11 +179,11 @@ def integrate_production_terms(gmech: GpuMechanism, method: int, state, dt, opts
 
 
 def source_adjoint(gmech: GpuMechanism, state, dt, opts: SourceOptions, state_bar, split_const=None, t_start=0.0,
-                   x=None, tape_cap: int = 0):
-    """Discrete adjoint of a BDF source-term integration
-    (``ember_source_adjoint``): for phi = sum(state_bar * state_out), returns
-    (state_out, status, d phi / d state, d phi / d ln(multiplier) per reaction).
-    Host (numpy) arrays."""
+                   x=None, tape_cap: int = 0, method: int = BDF):
+    """Discrete adjoint of a source-term integration (``ember_source_adjoint``
+    for BDF, ``ember_source_adjoint_qss`` for QSS): for phi = sum(state_bar *
+    state_out), returns (state_out, status, d phi / d state, d phi / d
+    ln(multiplier) per reaction). Host (numpy) arrays."""
     state = np.ascontiguousarray(state, dtype=np.float64)
     n = state.shape[0]
     dt = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, dtype=np.float64), (n,)))
@@ -194,9 +194,10 @@ def source_adjoint(gmech: GpuMechanism, state, dt, opts: SourceOptions, state_ba
     status = np.zeros(n, dtype=np.int32)
     gin = np.empty_like(state)
     glnk = np.zeros(max(gmech.mech.n_reactions, 1))
-    rc = L.lib().ember_source_adjoint(gmech.handle, n, L.ptr(state), L.ptr(sc), L.ptr(dt), float(t_start), L.ptr(xx),
-                                      C.byref(opts), L.ptr(bar), int(tape_cap), L.ptr(out), L.ptr(status),
-                                      L.ptr(gin), L.ptr(glnk), L.MEM_HOST, None)
+    name = "ember_source_adjoint_qss" if method == QSS else "ember_source_adjoint"
+    rc = getattr(L.lib(), name)(gmech.handle, n, L.ptr(state), L.ptr(sc), L.ptr(dt), float(t_start), L.ptr(xx),
+                                C.byref(opts), L.ptr(bar), int(tape_cap), L.ptr(out), L.ptr(status),
+                                L.ptr(gin), L.ptr(glnk), L.MEM_HOST, None)
     if rc not in (L.OK, L.EFAIL):
-        L.check(rc, "ember_source_adjoint")
+        L.check(rc, name)
     return out, status, gin, glnk[:gmech.mech.n_reactions]

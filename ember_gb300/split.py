@@ -270,7 +270,7 @@ class FlameBatchSplitSolver:
         """One split step from the current state and the gradient of
         J = sum_f w_heat_release[f] Q_f + w_consumption_speed[f] S_c,f at its end
         with respect to the state at its start and ln(multiplier) of every
-        reaction (``ember_split_adjoint``; BDF source). Returns (Q, S_c or None,
+        reaction (``ember_split_adjoint``; BDF or QSS source). Returns (Q, S_c or None,
         d J / d state [n_points, S+2], d J / d ln multiplier [R]); with
         ``device`` (a torch device) as tensors there, computed without a host
         round trip."""

@@ -564,6 +564,31 @@ int ember_source_adjoint(ember_mech mech, int n_points, const double* state_in, 
                          const double* state_bar, int tape_cap, double* state_out, int* status,
                          double* state_in_bar, double* lnk_bar, int mem, void* stream);
 
+/* Discrete adjoint of a QSS source-term integration (EMBER_SOURCE_QSS, the
+ * reference's default integrator; same arguments as ember_source_adjoint).
+ * For phi = sum over points of state_bar . state_out, returns state_in_bar =
+ * d phi / d state_in [n_points][nVars] and lnk_bar = d phi / d
+ * ln(multiplier_i) of every reaction [n_reactions], summed over points (or
+ * NULL). The integration is differentiated as it runs: every attempt of every
+ * step (a retried attempt's predictor uses the rejected attempt's corrector
+ * rates), the step sizes as functions of the state (getInitialStepSize, the
+ * error-estimate rule dt (1/sqrt(eps) + 0.005), the clip to the end time),
+ * the right-hand side analytically in the mass fractions and by a forward
+ * difference in T; accept / reject decisions are held fixed. Finite
+ * differences of the adaptive forward map agree with it to their own noise
+ * at the reference's default tolerances. Needs qss_stability_check = 0 and
+ * qss_iteration_count 1-4. tape_cap: step starts kept per point (0: 4096).
+ * There is no counterpart in the reference (QssIntegrator runs forward
+ * only); it serves the gradients of FlameSolver's objectives
+ * (src/flameSolver.cpp:926-961) with the QSS source
+ * (src/qssintegrator.cpp:58-265, src/sourceSystem.cpp:403-531).
+ * status: as ember_source_integrate, or -30 (tape full), -33 (more than 32
+ * attempts in one step). */
+int ember_source_adjoint_qss(ember_mech mech, int n_points, const double* state_in, const double* split_const,
+                             const double* dt, double t_start, const double* x, const ember_source_options* opts,
+                             const double* state_bar, int tape_cap, double* state_out, int* status,
+                             double* state_in_bar, double* lnk_bar, int mem, void* stream);
+
 /* Known-answer self-test of the device QSS integrator: integrates the
  * CHEMEQ2 cesium relaxation problem of the reference's QSS test
  * (test/old/test_qssintegrator.cpp:11-83) from y7 (7 values, in/out) over
@@ -720,12 +745,13 @@ int ember_split_objectives(ember_split split, const double* rho_u, const int* ju
  *   J = sum_f w_heat_release[f] Q_f + w_consumption_speed[f] S_c,f
  * at the end of that step (either weight array may be NULL) with respect to
  * the state at its start (state_bar, point-major) and to ln(multiplier) of
- * every reaction (lnk_bar [n_reactions]). Needs EMBER_SOURCE_BDF. Backward
- * pass: the objectives' gradient at the end state (spline weights of
- * mathUtils::integrate, the analytic Jacobian of qdot and cp), the
- * mass-fraction correction, the transposed diffusion stages, the discrete
- * adjoint of the BDF source stage (see ember_source_adjoint; tape_cap
- * accepted steps per point, 0: 1024), the first two diffusion stages. The
+ * every reaction (lnk_bar [n_reactions]). Backward pass: the objectives'
+ * gradient at the end state (spline weights of mathUtils::integrate, the
+ * analytic Jacobian of qdot and cp), the mass-fraction correction, the
+ * transposed diffusion stages, the discrete adjoint of the source stage (BDF:
+ * see ember_source_adjoint, tape_cap accepted steps per point, 0: 1024; QSS:
+ * see ember_source_adjoint_qss, tape_cap step starts per point, 0: 4096,
+ * needs qss_stability_check = 0), the first two diffusion stages. The
  * split constants of the step are held fixed (they come from the previous
  * step's time derivatives). Q_f and S_c,f of the step are returned in
  * heat_release / consumption_speed when given. */

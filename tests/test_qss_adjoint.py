@@ -68,3 +68,88 @@ def test_oracle_qss_adjoint_matches_central_differences():
         fd = (phi(st, mp) - phi(st, mm)) / 2e-6
         assert abs(g[i] - fd) <= 1e-5 * abs(fd) + 1e-7 * np.abs(g).max(), (i, g[i], fd)
     om.set_multipliers(None)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kinetics", [KINETICS_STANDARD, KINETICS_INTERP])
+def test_gpu_qss_adjoint_matches_the_oracle_adjoint(gpu_lib, kinetics):
+    # the device adjoint (its forward replay and its backward pass) against
+    # the CPU restatement, with split constants and the igniter on
+    from oracle import chem
+    from ember_gb300.source import GpuMechanism, integrate_production_terms, source_adjoint
+    mech, st, dt, opts, bar = _case(kinetics, n=8, seed=12)
+    opts.ignition_energy, opts.ignition_duration, opts.ignition_stddev = 2e6, 1.0, 5e-4
+    rng = np.random.default_rng(3)
+    sc = rng.normal(scale=1e-2, size=st.shape) * np.abs(st).clip(1e-3)
+    sc[:, 1] = rng.normal(scale=2e3, size=len(st))
+    x = rng.uniform(-1e-3, 1e-3, size=len(st))
+    gm = GpuMechanism(mech)
+    out, status, g_state, g_lnk = source_adjoint(gm, st, dt, opts, bar, split_const=sc, x=x, method=QSS)
+    om = chem.OracleMech(mech)
+    ref_out, ref_g, ref_p, ref_status, _ = chem.qss_adjoint(om, st, dt, opts, bar, split_const=sc, x=x)
+    assert (status == 0).all() and (ref_status == 0).all()
+    assert np.array_equal(out, ref_out)                  # the replayed forward pass is the integrator's
+    fwd, fstatus, _ = integrate_production_terms(gm, QSS, st, dt, opts, split_const=sc, x=x)
+    assert np.array_equal(out, np.asarray(fwd))
+    np.testing.assert_allclose(g_state, ref_g, rtol=1e-9, atol=1e-12 * np.abs(ref_g).max())
+    ref_lnk = ref_p.sum(axis=0)
+    np.testing.assert_allclose(g_lnk, ref_lnk, rtol=1e-9, atol=1e-12 * np.abs(ref_lnk).max())
+
+
+@pytest.mark.gpu
+def test_split_step_qss_gradients_match_central_differences_of_the_oracle(gpu_lib):
+    # Heat release and consumption speed after one balanced D-S-D split step
+    # with the QSS source at its default options (serial diffusion): the
+    # discrete adjoint of the step through torch.autograd against central
+    # differences of the oracle's step, perturbations 1e-6.
+    torch = pytest.importorskip("torch")
+    from oracle import split as osplit
+    from oracle.chem import OracleMech
+    from ember_gb300 import _lib as L
+    from ember_gb300.autograd import split_step_objectives
+    from ember_gb300.source import GpuMechanism
+    from ember_gb300.split import FlameBatchSplitSolver, flame_batch
+    mech = synthetic_mechanism(n_species=20, n_reactions=60, seed=3)
+    grids, state, B, D, rho_u, ju, jb = flame_batch(mech, n_flames=2, n_min=10, n_max=12, seed=5, width=2e-3,
+                                                    thickness=3e-4, T_b=1500.0)
+    opts = SourceOptions.defaults(kinetics_model=KINETICS_STANDARD)
+    dt = 1e-6
+    gm = GpuMechanism(mech)
+    solver = FlameBatchSplitSolver(gm, grids, dt, method=QSS, source_options=opts,
+                                   diffusion_algorithm=L.DIFFUSION_SERIAL)
+    solver.set_transport(B, D)
+    R = mech.n_reactions
+    s0 = torch.tensor(state, dtype=torch.float64, requires_grad=True)
+    lk = torch.zeros(R, dtype=torch.float64, requires_grad=True)
+    out = split_step_objectives(solver, s0, lk, 0.0, rho_u, ju, jb, 4096)
+    w = torch.tensor([1.0, -0.5, 2e3, 1e3], dtype=torch.float64)  # Q_0, Q_1, S_c,0, S_c,1
+    (out * w).sum().backward()
+    g_state = s0.grad.numpy()
+    g_lnk = lk.grad.numpy()
+    om = OracleMech(mech)
+
+    def J(st, mult=None):
+        om.set_multipliers(mult)
+        y, *_ = osplit.split_steps(om, grids, st, 0.0, B, D, dt, 1, QSS, opts)
+        _, hr, cs = osplit.objectives(om, grids, y, opts.pressure, opts.kinetics_model, rho_u, ju, jb)
+        return float(np.dot(w.numpy(), np.concatenate([hr, cs])))
+
+    om.set_multipliers(None)
+    y_ref, *_ = osplit.split_steps(om, grids, state, 0.0, B, D, dt, 1, QSS, opts)
+    _, hr_ref, cs_ref = osplit.objectives(om, grids, y_ref, opts.pressure, opts.kinetics_model, rho_u, ju, jb)
+    assert np.array_equal(out.detach().numpy(), np.concatenate([hr_ref, cs_ref]))
+    n0 = grids[0].n_points
+    for (p, k) in [(3, 1), (n0 + 5, 1), (4, 2), (n0 + 6, 3), (2, 4), (n0 - 2, 5)]:
+        assert state[p, k] > 1e-6
+        hstep = 1e-6 * abs(state[p, k])
+        e = np.zeros_like(state)
+        e[p, k] = hstep
+        fd = (J(state + e) - J(state - e)) / (2 * hstep)
+        assert abs(g_state[p, k] - fd) <= 1e-4 * abs(fd) + 1e-9 * np.abs(g_state).max(), (p, k, g_state[p, k], fd)
+    rng = np.random.default_rng(5)
+    for i in list(np.argsort(-np.abs(g_lnk))[:3]) + list(rng.choice(R, 3, replace=False)):
+        mp, mm = np.ones(R), np.ones(R)
+        mp[i], mm[i] = np.exp(1e-6), np.exp(-1e-6)
+        fd = (J(state, mp) - J(state, mm)) / 2e-6
+        assert abs(g_lnk[i] - fd) <= 1e-4 * abs(fd) + 1e-7 * np.abs(g_lnk).max(), (i, g_lnk[i], fd)
+    om.set_multipliers(None)
