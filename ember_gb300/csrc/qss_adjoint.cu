@@ -124,11 +124,19 @@ struct QaPoint {
     double *q2 = nullptr, *d2 = nullptr, *ycp = nullptr;
     double *ysb = nullptr, *q0b = nullptr, *d0b = nullptr, *rtaub = nullptr, *qnb = nullptr, *dnb = nullptr;
     double *rtsb = nullptr, *rtsbc = nullptr, *scrb = nullptr, *yfb = nullptr, *qjb = nullptr, *djb = nullptr;
-    double *yjb = nullptr, *att = nullptr, *fdb = nullptr;
+    double *yjb = nullptr, *att = nullptr, *fdb = nullptr, *sav = nullptr;
 
-    static __host__ __device__ size_t work_doubles(int n, int I) {
+    // One saved evaluation: what the adjoint of an evaluation reads that
+    // depends on the composition (the temperature-only values stay in the
+    // rate-constant cache, since every evaluation of a step but the
+    // temperature differences runs at the predictor's T).
+    static __host__ __device__ size_t save_doubles(const MechView& mv) {
+        return size_t(4) * mv.S + mv.n_tb + size_t(2) * mv.R + size_t(4) * mv.n_fo + 4;
+    }
+    static __host__ __device__ size_t work_doubles(const MechView& mv, int I) {
+        const int n = mv.S + 2;
         return size_t(21 + I) * n + size_t(kQaMaxAttempts) * size_t(4 + 4 * I) * n +
-               size_t(kQaMaxAttempts) * I * 2 * n;
+               size_t(kQaMaxAttempts) * I * 2 * n + (1 + size_t(kQaMaxAttempts) * I) * save_doubles(mv);
     }
     __device__ void carve_work(double* g) {
         ys = g;
@@ -154,7 +162,10 @@ struct QaPoint {
         yjb = djb + n + 2 * size_t(n);
         att = yjb + size_t(I) * n;
         fdb = att + size_t(kQaMaxAttempts) * (4 + 4 * I) * n;
+        sav = fdb + size_t(kQaMaxAttempts) * I * 2 * n;
     }
+    // saved evaluations: slot 0 the predictor, 1 + a I + j corrector j of attempt a
+    __device__ double* sv_slot(int slot) const { return sav + size_t(slot) * save_doubles(m); }
     __device__ double* at_rtaus(int a) const { return att + size_t(a) * (4 + 4 * I) * n; }
     __device__ double* at_scrp(int a) const { return at_rtaus(a) + n; }
     __device__ double* at_y(int a, int j) const { return at_rtaus(a) + size_t(2 + 4 * j) * n; }
@@ -171,7 +182,7 @@ struct QaPoint {
 
     // SourceSystemQSS::odefun with the operations of the forward kernel's
     // right-hand side (source.cu, SourceQssOde::eval). Starts and ends with a barrier.
-    __device__ void eval(double t, const double* y, double* q, double* d, bool corrector) {
+    __device__ void eval(double t, const double* y, double* q, double* d, bool corrector, double* save = nullptr) {
         const int tid = threadIdx.x;
         __syncthreads();
         if (!corrector) T = y[1];
@@ -192,6 +203,36 @@ struct QaPoint {
         const double qd =
             -block_sum<NT>(w.red, S, [&](int k, double p) { return fma(wq[k] - wd[k], hk[k], p); }) + igniter(*a, t, x);
         qdot = qd;
+        if (save) {
+            const int S_ = S, R = m.R, ntb = m.n_tb, nfo = m.n_fo;
+            double* p = save;
+            for (int k = tid; k < S_; k += NT) {
+                p[k] = w.c[k];
+                p[S_ + k] = w.ym[k];
+                p[2 * S_ + k] = w.wq[k];
+                p[3 * S_ + k] = w.wd[k];
+            }
+            p += 4 * S_;
+            for (int s2 = tid; s2 < ntb; s2 += NT) p[s2] = w.concm[s2];
+            p += ntb;
+            for (int i = tid; i < R; i += NT) {
+                p[i] = w.ropf[i];
+                p[R + i] = w.ropr[i];
+            }
+            p += 2 * R;
+            for (int f = tid; f < nfo; f += NT) {
+                p[f] = w.fo_F[f];
+                p[nfo + f] = w.fo_pr[f];
+                p[2 * nfo + f] = w.fo_dF[f];
+                p[3 * nfo + f] = w.kfm[m.fo_rxn[f]];
+            }
+            p += 4 * nfo;
+            if (tid == 0) {
+                p[0] = w.mmw;
+                p[1] = rc;
+                p[2] = qd;
+            }
+        }
         for (int i = tid; i < n; i += NT) {
             const double sc = split ? split[i] : 0.0;
             if (i == 0) {
@@ -215,10 +256,23 @@ struct QaPoint {
     // corrector call adds the adjoints of the rrho / rrc it used to *rrho_b
     // and *rrc_b; a predictor call takes the correctors' adjoints of its
     // rrho, rrc (ext_*) and sends all of them to rho and cp.
-    __device__ void vjp(const double* y, const double* qb, const double* db, bool predictor, double ext_rrho_b,
-                        double ext_rrc_b, double* yb, double* pb, double* rrho_b, double* rrc_b) {
+    __device__ void vjp(const double* y, const double* sv, const double* qb, const double* db, bool predictor,
+                        double ext_rrho_b, double ext_rrc_b, double* yb, double* pb, double* rrho_b, double* rrc_b) {
         const int tid = threadIdx.x;
         const double* Y = y + 2;
+        const int nfo = m.n_fo;
+        const double* c = sv;
+        const double* ym = c + S;
+        const double* wq = ym + S;
+        const double* wd = wq + S;
+        const double* concm = wd + S;
+        const double* ropf = concm + m.n_tb;
+        const double* ropr = ropf + m.R;
+        const double* foF = ropr + m.R;
+        const double* fopr = foF + nfo;
+        const double* fodF = fopr + nfo;
+        const double* fokfm = fodF + nfo;
+        const double mmw = fokfm[nfo], rho = fokfm[nfo + 1], qdot_s = fokfm[nfo + 2];
         __syncthreads();
         const double qdb = qb[1] * rrc;
         double part = 0.0;
@@ -226,10 +280,10 @@ struct QaPoint {
             wqb[k] = qb[2 + k] * m.W[k] * rrho - qdb * w.hk[k];
             wdb[k] = db[2 + k] * m.W[k] * rrho + qdb * w.hk[k];
             cb[k] = 0.0;
-            part += qb[2 + k] * w.wq[k] * m.W[k] + db[2 + k] * w.wd[k] * m.W[k];
+            part += qb[2 + k] * wq[k] * m.W[k] + db[2 + k] * wd[k] * m.W[k];
         }
         const double own_rrho_b = block_add<NT>(w.red, part);
-        const double own_rrc_b = qb[1] * qdot;
+        const double own_rrc_b = qb[1] * qdot_s;
         double rho_b_in = 0.0, cp_b_in = 0.0;
         if (predictor) {
             const double rr_b = own_rrho_b + ext_rrho_b, rc_b = own_rrc_b + ext_rrc_b;
@@ -254,19 +308,22 @@ struct QaPoint {
                 if (pd4[o] != 0xffff) {
                     fb += wqb[pd4[o]];
                     rbb += wdb[pd4[o]];
-                    pp *= w.c[pd4[o]];
+                    pp *= c[pd4[o]];
                 }
                 if (rc4[o] != 0xffff) {
                     fb += wdb[rc4[o]];
                     rbb += wqb[rc4[o]];
-                    pf *= w.c[rc4[o]];
+                    pf *= c[rc4[o]];
                 }
             }
-            pb[i] += fb * w.ropf[i] + rbb * w.ropr[i];
-            const double kfm = w.kfm[i];
-            int slot = -1;
-            if (ty != RXN_ELEMENTARY) slot = rinfo_tbslot(info);
-            const double rf = ty == RXN_THREE_BODY ? kfm * w.concm[slot] : kfm;
+            pb[i] += fb * ropf[i] + rbb * ropr[i];
+            int slot = -1, fo = -1;
+            if (ty != RXN_ELEMENTARY) {
+                slot = rinfo_tbslot(info);
+                fo = m.tb_fo[slot];
+            }
+            const double kfm = fo >= 0 ? fokfm[fo] : w.kfm[i];
+            const double rf = ty == RXN_THREE_BODY ? kfm * concm[slot] : kfm;
             const double kr = rev ? w.rkc[i] : 0.0;
 #pragma unroll
             for (int o = 0; o < 4; ++o) {
@@ -274,7 +331,7 @@ struct QaPoint {
                 double dv = rf;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
-                    if (q != o && rc4[q] != 0xffff) dv *= w.c[rc4[q]];
+                    if (q != o && rc4[q] != 0xffff) dv *= c[rc4[q]];
                 atomicAdd(&cb[rc4[o]], fb * dv);
             }
             if (rev) {
@@ -284,7 +341,7 @@ struct QaPoint {
                     double dv = rf * kr;
 #pragma unroll
                     for (int q = 0; q < 4; ++q)
-                        if (q != o && pd4[q] != 0xffff) dv *= w.c[pd4[q]];
+                        if (q != o && pd4[q] != 0xffff) dv *= c[pd4[q]];
                     atomicAdd(&cb[pd4[o]], rbb * dv);
                 }
             }
@@ -293,9 +350,9 @@ struct QaPoint {
                 if (ty == RXN_THREE_BODY) {
                     Mb = fb * (kfm * pf) + rbb * (kfm * kr * pp);
                 } else {
-                    const int f = m.tb_fo[slot];
-                    const double prr = w.fo_pr[f], pr1 = 1.0 + prr;
-                    const double dkdm = (w.fo_F[f] / (pr1 * pr1) + (prr / pr1) * w.fo_dF[f]) *
+                    const int f = fo;
+                    const double prr = fopr[f], pr1 = 1.0 + prr;
+                    const double dkdm = (foF[f] / (pr1 * pr1) + (prr / pr1) * fodF[f]) *
                                         (w.fo_k0[f] * w.fo_rkinf[f]) * w.fo_kinf[f] * m.mult[i];
                     Mb = (fb * pf + rbb * kr * pp) * dkdm;
                 }
@@ -307,14 +364,13 @@ struct QaPoint {
         const double ctotb = block_add<NT>(w.red, ctot_part);  // also the barrier after the atomics
         // composition: c = ym rho, ctot = rho / mmw, rho = p mmw / (R T), mmw = 1 / sum ym,
         // ym = max(Y, 0) rnorm / W, rnorm = 1 / sum max(Y, 0); predictor: cp = R cpsum / mmw
-        const double rho = rho_c, mmw = w.mmw;
         part = 0.0;
         double cps = 0.0, ycp_s = 0.0;
         for (int k = tid; k < S; k += NT) {
-            part += cb[k] * w.ym[k];
+            part += cb[k] * ym[k];
             if (predictor) {
-                cps += w.ym[k] * mmw * w.cpR[k];
-                ycp_s += w.ym[k] * w.cpR[k];
+                cps += ym[k] * mmw * w.cpR[k];
+                ycp_s += ym[k] * w.cpR[k];
             }
         }
         const double rhob = rho_b_in + ctotb / mmw + block_add<NT>(w.red, part);
@@ -350,11 +406,11 @@ struct QaPoint {
     // time; *dt the next step's size. Returns 0, -1 (dtmin) or -33 (more
     // than kQaMaxAttempts attempts).
     __device__ int step_run(const double* ys_in, double ts, bool first, double* dt, double* tn_out, double* y_out,
-                            QaScalars& sc) {
+                            QaScalars& sc, bool keep) {
         const int tid = threadIdx.x;
         const double tfd = 1.000008;
         for (int i = tid; i < n; i += NT) ys[i] = ys_in[i];
-        eval(ts + tstart, ys, q0, d0, false);
+        eval(ts + tstart, ys, q0, d0, false, keep ? sv_slot(0) : nullptr);
         if (tid == 0) {
             sc.T = T;
             sc.rrho = rrho;
@@ -423,7 +479,7 @@ struct QaPoint {
                 for (int i = tid; i < n; i += NT) yj[i] = dmaxr(ymin(i), fma(dta, scr[i], ys[i]));
                 if (j == 0) tn = ts + dta;
                 double *qj = at_q(at, j), *dj = at_d(at, j), *sj = at_scr(at, j);
-                eval(tn + tstart, yj, qj, dj, true);
+                eval(tn + tstart, yj, qj, dj, true, keep ? sv_slot(1 + at * I + j) : nullptr);
                 for (int i = tid; i < n; i += NT) {
                     const double rb = en(i) ? 0.5 * (rtaus[i] + dta * dj[i] / yj[i]) : 0.0;
                     const double an = pade_an(rb), ad = pade_den(rb);
@@ -661,12 +717,11 @@ struct QaPoint {
                     fd[i] = djbi;
                 }
                 dtb_a[at] += block_add<NT>(w.red, part);
-                // the corrector evaluation at yj (the predictor's T, rho, cp)
+                // the corrector evaluation at yj (the predictor's T, rho, cp), from its saved values
                 T = sc.T;
                 rrho = sc.rrho;
                 rrc = sc.rrc;
-                eval(ts + dta + tstart, yj, q2, d2, true);
-                vjp(yj, qjb, djb, false, 0.0, 0.0, ybj, pb, &rrho_b, &rrc_b);
+                vjp(yj, sv_slot(1 + at * I + j), qjb, djb, false, 0.0, 0.0, ybj, pb, &rrho_b, &rrc_b);
                 // yj = max(ymin, ys + dt scr_{j-1})
                 const double* sp = (j > 0) ? at_scr(at, j - 1) : at_scrp(at);
                 part = 0.0;
@@ -736,8 +791,12 @@ struct QaPoint {
             *dtb = dtb_a[0];
         }
         // the predictor evaluation at ys, its rrho / rrc also used by the correctors
-        eval(ts + tstart, ys, q2, d2, false);
-        vjp(ys, q0b, d0b, true, rrho_b, rrc_b, ysb, pb, nullptr, nullptr);
+        T = sc.T;
+        rrho = sc.rrho;
+        rrc = sc.rrc;
+        rho_p = sc.rho;
+        cp_p = sc.cp;
+        vjp(ys, sv_slot(0), q0b, d0b, true, rrho_b, rrc_b, ysb, pb, nullptr, nullptr);
         // temperature by a forward difference, every evaluation of the step at T + dT
         const double T0 = sc.T;
         const double dT = fabs(T0) * 1.4901161193847656e-08;
@@ -833,7 +892,7 @@ __global__ void __launch_bounds__(NT) k_source_qss_adjoint(const __grid_constant
                 rec[1] = dt;
             }
             double tnew = tn;
-            const int r = P.step_run(y, tn, N == 0, &dt, &tnew, yb, sc);
+            const int r = P.step_run(y, tn, N == 0, &dt, &tnew, yb, sc, false);
             ++N;
             if (r != 0) {
                 status = r;
@@ -860,7 +919,7 @@ __global__ void __launch_bounds__(NT) k_source_qss_adjoint(const __grid_constant
             for (int k = N - 1; k >= 0 && status == 0; --k) {
                 const double* rec = tp + size_t(k) * (n + 2);
                 double dtk = rec[1], tk = 0.0;
-                const int r = P.step_run(rec + 2, rec[0], k == 0, &dtk, &tk, y, sc);
+                const int r = P.step_run(rec + 2, rec[0], k == 0, &dtk, &tk, y, sc, true);
                 if (r != 0) {
                     status = r;
                     break;
@@ -899,7 +958,7 @@ int launch_qss_adjoint_nt(const MechView& m, const SourceArgs& a, int tape_cap, 
     EMBER_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_source_qss_adjoint<NT>, NT, per));
     per_sm = std::max(1, std::min(per_sm, 4));
     const int blocks = std::max(1, std::min(a.n, sms * per_sm));
-    const size_t wstride = QaPoint<NT>::work_doubles(n, a.qss_itermax);
+    const size_t wstride = QaPoint<NT>::work_doubles(m, a.qss_itermax);
     double *kcache = nullptr, *work = nullptr, *tape = nullptr;
     EMBER_TRY(scr.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));
     EMBER_TRY(scr.alloc(&work, size_t(blocks) * wstride));
