@@ -57,6 +57,10 @@ struct QssResume {
     int steps, gcount, rcount, started;
 };
 constexpr int kQssSuspended = -31;
+// QSS tape of a point (SourceArgs::tape with a QSS launch): a header of
+// kQssTapeHeader doubles (steps taken, overflow flag), then one record of
+// n + 2 doubles per step start (see qss_integrate_block).
+constexpr int kQssTapeHeader = 2;
 
 __device__ __forceinline__ double rsign(double x) { return (x > 0) ? 1.0 : (x < 0) ? -1.0 : 0.0; }
 
@@ -70,10 +74,14 @@ __device__ __forceinline__ double pade_an(double r) { return fma(r, fma(r, 11.0 
 // step_cap > 0: stop before step step_cap + 1 (counted from the first step
 // of the point, across resumptions), save the loop state in *rs and return
 // kQssSuspended. rs with started set: continue from that state.
+// tape (or null): the start of every step k < tape_cap is recorded at
+// tape + k (n + 2): time, step size carried into the step (0 before the
+// first), state (for the adjoint, qss_adjoint.cu).
 template <int NT, class Ode, class Enforce, class Ymin>
 __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, const QssParams& P, Enforce enforce,
                                                    Ymin ymin, double tf, double tstart, double* red, QssStats& st,
-                                                   int step_cap = 0, QssResume* rs = nullptr) {
+                                                   int step_cap = 0, QssResume* rs = nullptr, double* tape = nullptr,
+                                                   int tape_cap = 0) {
     const int t0 = threadIdx.x;
     const double tfd = 1.000008;
     const bool stab_on = P.stability_check != 0;
@@ -111,6 +119,14 @@ __device__ __forceinline__ int qss_integrate_block(Ode& ode, QssSmem& v, int n, 
             break;
         }
         ++steps;
+        if (tape && steps <= tape_cap) {
+            double* rec = tape + size_t(steps - 1) * (n + 2);
+            if (t0 == 0) {
+                rec[0] = tn;
+                rec[1] = dt;
+            }
+            for (int i = t0; i < n; i += NT) rec[2 + i] = v.y[i];
+        }
         // ---- integrateOneStep --------------------------------------------
         ode.eval(tn + tstart, v.y, v.q, v.d, false);
         gcount += 1;

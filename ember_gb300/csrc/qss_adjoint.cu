@@ -821,15 +821,18 @@ struct QaPoint {
     }
 };
 
-// Per point: the forward integration with a tape of step starts, then the
-// backward pass. status: the integrator's (0, -1 dtmin, -20 max_steps),
-// -30 (tape full), -33 (attempt cap).
+// Per point: the step starts from the forward kernel's tape (a.tape, when it
+// holds the whole integration), or else from this kernel's own forward
+// integration with a per-CTA tape; then the backward pass. fwd_status: the
+// forward kernel's status per point (with a.tape). status: the integrator's
+// (0, -1 dtmin, -20 max_steps), -30 (tape full), -33 (attempt cap).
 template <int NT>
 __global__ void __launch_bounds__(NT) k_source_qss_adjoint(const __grid_constant__ MechView m,
                                                             const __grid_constant__ SourceArgs a, int* counter,
                                                             double* kcache, double* work, size_t work_stride,
-                                                            double* tape, int tape_cap, const double* ybar_out,
-                                                            double* ybar_in, double* pbar, int* adj_status) {
+                                                            double* tape, int tape_cap, const int* fwd_status,
+                                                            const double* ybar_out, double* ybar_in, double* pbar,
+                                                            int* adj_status) {
     extern __shared__ double smem[];
     __shared__ int next_point;
     __shared__ int ired[kMaxChemThreads / 32];
@@ -871,12 +874,23 @@ __global__ void __launch_bounds__(NT) k_source_qss_adjoint(const __grid_constant
         P.x = a.x ? a.x[j] : 0.0;
         P.tf = a.dt[j];
         const double* yin = a.state_in + size_t(j) * n;
+        int N = 0, status = 0;
+        const double* recs = tp;  // step records: (time, step size, state) each
+        bool have_tape = false;
+        if (a.tape) {
+            const double* hdr = a.tape + size_t(j) * a.tape_stride;
+            status = fwd_status ? fwd_status[j] : 0;
+            if (status == 0 && hdr[1] == 0.0) {
+                have_tape = true;
+                N = static_cast<int>(hdr[0]);
+                recs = hdr + kQssTapeHeader;
+            }
+        }
         for (int i = tid; i < n; i += NT) y[i] = P.en(i) ? dmaxr(yin[i], P.ymin(i)) : yin[i];
         __syncthreads();
         // forward, keeping each step's start (state, time, step size)
-        int N = 0, status = 0;
         double tn = 0.0, dt = 0.0;
-        while (tfd * tn < P.tf) {
+        while (!have_tape && status == 0 && tfd * tn < P.tf) {
             if (N >= a.max_steps) {
                 status = -20;
                 break;
@@ -902,14 +916,16 @@ __global__ void __launch_bounds__(NT) k_source_qss_adjoint(const __grid_constant
             for (int i = tid; i < n; i += NT) y[i] = yb[i];
             __syncthreads();
         }
-        int nonfinite = 0;
-        double* yout = a.state_out + size_t(j) * n;
-        for (int i = tid; i < n; i += NT) {
-            nonfinite |= !isfinite(y[i]);
-            yout[i] = y[i];
+        if (!have_tape) {
+            int nonfinite = 0;
+            double* yout = a.state_out + size_t(j) * n;
+            for (int i = tid; i < n; i += NT) {
+                nonfinite |= !isfinite(y[i]);
+                yout[i] = y[i];
+            }
+            nonfinite = __syncthreads_or(nonfinite);
+            if (status == 0 && nonfinite) status = -21;
         }
-        nonfinite = __syncthreads_or(nonfinite);
-        if (status == 0 && nonfinite) status = -21;
         double* pb = pbar + size_t(j) * m.R;
         for (int i = tid; i < m.R; i += NT) pb[i] = 0.0;
         if (status == 0) {
@@ -917,7 +933,7 @@ __global__ void __launch_bounds__(NT) k_source_qss_adjoint(const __grid_constant
             double tsb = 0.0, dtb = 0.0;
             __syncthreads();
             for (int k = N - 1; k >= 0 && status == 0; --k) {
-                const double* rec = tp + size_t(k) * (n + 2);
+                const double* rec = recs + size_t(k) * (n + 2);
                 double dtk = rec[1], tk = 0.0;
                 const int r = P.step_run(rec + 2, rec[0], k == 0, &dtk, &tk, y, sc, true);
                 if (r != 0) {
@@ -932,8 +948,8 @@ __global__ void __launch_bounds__(NT) k_source_qss_adjoint(const __grid_constant
             ybar_in[size_t(j) * n + i] = (status == 0 && !(P.en(i) && yin[i] < P.ymin(i))) ? yb[i] : 0.0;
         if (tid == 0) {
             adj_status[j] = status;
-            if (a.status) a.status[j] = status;
-            if (a.stats) {
+            if (a.status && !a.tape) a.status[j] = status;
+            if (a.stats && !a.tape) {
                 a.stats[4 * size_t(j) + 0] = N;
                 a.stats[4 * size_t(j) + 1] = 0;
                 a.stats[4 * size_t(j) + 2] = 0;
@@ -945,8 +961,9 @@ __global__ void __launch_bounds__(NT) k_source_qss_adjoint(const __grid_constant
 }
 
 template <int NT>
-int launch_qss_adjoint_nt(const MechView& m, const SourceArgs& a, int tape_cap, int* counter, const double* ybar_out,
-                          double* ybar_in, double* pbar, int* adj_status, Scratch& scr, cudaStream_t st) {
+int launch_qss_adjoint_nt(const MechView& m, const SourceArgs& a, int tape_cap, int* counter, const int* fwd_status,
+                          const double* ybar_out, double* ybar_in, double* pbar, int* adj_status, Scratch& scr,
+                          cudaStream_t st) {
     const int n = m.S + 2;
     const size_t per = sizeof(double) * (ChemSmem::doubles(m.S, m.R, m.n_tb, m.n_fo, false) + 3 * size_t(m.n_fo) +
                                          3 * size_t(m.S));
@@ -959,12 +976,15 @@ int launch_qss_adjoint_nt(const MechView& m, const SourceArgs& a, int tape_cap, 
     per_sm = std::max(1, std::min(per_sm, 4));
     const int blocks = std::max(1, std::min(a.n, sms * per_sm));
     const size_t wstride = QaPoint<NT>::work_doubles(m, a.qss_itermax);
+    // the per-CTA tape of points integrated again here (no forward tape, or
+    // one that overflowed): at least 4096 step starts
+    const int cta_cap = std::max(tape_cap, 4096);
     double *kcache = nullptr, *work = nullptr, *tape = nullptr;
     EMBER_TRY(scr.alloc(&kcache, size_t(blocks) * ChemSmem::global_doubles(m)));
     EMBER_TRY(scr.alloc(&work, size_t(blocks) * wstride));
-    EMBER_TRY(scr.alloc(&tape, size_t(blocks) * size_t(tape_cap) * (n + 2)));
-    k_source_qss_adjoint<NT><<<blocks, NT, per, st>>>(m, a, counter, kcache, work, wstride, tape, tape_cap, ybar_out,
-                                                      ybar_in, pbar, adj_status);
+    EMBER_TRY(scr.alloc(&tape, size_t(blocks) * size_t(cta_cap) * (n + 2)));
+    k_source_qss_adjoint<NT><<<blocks, NT, per, st>>>(m, a, counter, kcache, work, wstride, tape, cta_cap,
+                                                      fwd_status, ybar_out, ybar_in, pbar, adj_status);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
 }
@@ -980,25 +1000,49 @@ __global__ void k_sum_point_rows(int n, int R, const double* __restrict__ rows, 
 }  // namespace
 
 int launch_source_qss_adjoint(const MechView& m, const SourceArgs& a, int tape_cap, int* counter,
-                              const double* ybar_out, double* ybar_in, double* pbar, int* adj_status, Scratch& sc,
-                              cudaStream_t st) {
+                              const int* fwd_status, const double* ybar_out, double* ybar_in, double* pbar,
+                              int* adj_status, Scratch& sc, cudaStream_t st) {
     EMBER_CHECK_ARG(a.qss_stability_check == 0, "the QSS adjoint needs qss_stability_check = 0");
     EMBER_CHECK_ARG(a.qss_itermax >= 1 && a.qss_itermax <= kQaMaxIter, "the QSS adjoint supports 1-%d iterations",
                     kQaMaxIter);
     EMBER_CHECK_ARG(tape_cap >= 1, "bad tape_cap %d", tape_cap);
-    if (m.S + 2 <= 64) return launch_qss_adjoint_nt<64>(m, a, tape_cap, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
-    return launch_qss_adjoint_nt<128>(m, a, tape_cap, counter, ybar_out, ybar_in, pbar, adj_status, sc, st);
+    if (m.S + 2 <= 64)
+        return launch_qss_adjoint_nt<64>(m, a, tape_cap, counter, fwd_status, ybar_out, ybar_in, pbar, adj_status,
+                                         sc, st);
+    return launch_qss_adjoint_nt<128>(m, a, tape_cap, counter, fwd_status, ybar_out, ybar_in, pbar, adj_status, sc,
+                                      st);
 }
 
-int source_qss_adjoint_run(const MechView& m, const SourceArgs& a, int tape_cap, const double* ybar_out,
+size_t qss_tape_doubles(const MechView& m, int n_points, int tape_cap) {
+    return size_t(n_points) * (kQssTapeHeader + size_t(tape_cap) * (m.S + 4));
+}
+
+int source_qss_adjoint_run(const MechView& m, const SourceArgs& a_in, int tape_cap, const double* ybar_out,
                            double* ybar_in, double* lnk_bar, double* lnk_bar_points, int* adj_status, Scratch& sc,
                            cudaStream_t st) {
+    SourceArgs a = a_in;
     int* counter = nullptr;
     EMBER_TRY(sc.alloc(&counter, 1));
     EMBER_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(int), st));
     double* rows = lnk_bar_points;
     if (!rows) EMBER_TRY(sc.alloc(&rows, size_t(a.n) * std::max(m.R, 1)));
-    EMBER_TRY(launch_source_qss_adjoint(m, a, tape_cap, counter, ybar_out, ybar_in, rows, adj_status, sc, st));
+    // With room for a whole tape, the forward kernel records every step start
+    // and the adjoint does not integrate again.
+    if (qss_tape_doubles(m, a.n, tape_cap) * sizeof(double) <= kQssTapeBudgetBytes) {
+        a.tape_cap = tape_cap;
+        a.tape_stride = int64_t(kQssTapeHeader) + int64_t(tape_cap) * (m.S + 4);
+        EMBER_TRY(sc.alloc(&a.tape, qss_tape_doubles(m, a.n, tape_cap)));
+        int* fcounter = nullptr;
+        EMBER_TRY(sc.alloc(&fcounter, 1));
+        EMBER_CUDA_TRY(cudaMemsetAsync(fcounter, 0, sizeof(int), st));
+        EMBER_TRY(launch_source_qss(m, a, fcounter, sc, st));
+        EMBER_TRY(launch_source_qss_adjoint(m, a, tape_cap, counter, a.status, ybar_out, ybar_in, rows, adj_status,
+                                            sc, st));
+    } else {
+        a.tape = nullptr;
+        EMBER_TRY(launch_source_qss_adjoint(m, a, tape_cap, counter, nullptr, ybar_out, ybar_in, rows, adj_status, sc,
+                                            st));
+    }
     if (lnk_bar && m.R > 0) k_sum_point_rows<<<blocks_for(m.R, 128), 128, 0, st>>>(a.n, m.R, rows, lnk_bar);
     EMBER_CUDA_TRY(cudaGetLastError());
     return EMBER_OK;
@@ -1040,6 +1084,8 @@ extern "C" int ember_source_adjoint_qss(ember_mech m, int n, const double* state
     EMBER_TRY(sc.alloc(&d_adj, n));
     SourceArgs a = make_source_args(opts, n, d_in, d_split, d_dt, t_start, d_x, d_out, d_status, nullptr);
     EMBER_TRY(source_qss_adjoint_run(m->view, a, tape_cap, d_bar, d_inbar, d_lnk, nullptr, d_adj, sc, st));
+    // status: the forward's, or the adjoint's when the forward succeeded
+    EMBER_CUDA_TRY(cudaMemcpyAsync(d_status, d_adj, sizeof(int) * n, cudaMemcpyDeviceToDevice, st));
     EMBER_TRY(stage_out(state_out, d_out, size_t(n) * nv, mem, st));
     EMBER_TRY(stage_out(status, d_status, n, mem, st));
     EMBER_TRY(stage_out(state_in_bar, d_inbar, size_t(n) * nv, mem, st));

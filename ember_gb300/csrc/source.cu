@@ -254,9 +254,11 @@ __global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView 
         QssStats st;
         QssResume rs{};
         if (a.resuming) rs = a.resume[j];
+        double* tape = a.tape ? a.tape + size_t(j) * a.tape_stride : nullptr;
         int ret = qss_integrate_block<NT>(ode, v, n, P, EnforceNotMomentum(), SourceYmin{a.qss_minval}, a.dt[j],
                                           a.t_start_dev ? *a.t_start_dev : a.t_start, ode.w.red, st, a.step_cap,
-                                          a.resume ? &rs : nullptr);
+                                          a.resume ? &rs : nullptr, tape ? tape + kQssTapeHeader : nullptr,
+                                          a.tape_cap);
         int nonfinite = 0;
         double* yout = a.state_out + size_t(j) * n;
         for (int i = tid; i < n; i += NT) {
@@ -270,6 +272,9 @@ __global__ void __launch_bounds__(NT, qss_min_blocks(NT)) k_source_qss(MechView 
             if (ret == kQssSuspended) {
                 a.resume[j] = rs;
                 a.susp_list[atomicAdd(a.susp_n, 1)] = j;
+            } else if (tape) {
+                tape[0] = st.steps;
+                tape[1] = st.steps > a.tape_cap ? 1.0 : 0.0;
             }
             a.status[j] = ret;
             if (a.stats) {

@@ -31,9 +31,11 @@ struct SourceArgs {
     double bdf_reltol, bdf_atol_u, bdf_atol_t, bdf_atol_y, bdf_min_step;
     int bdf_max_steps;
     double ign_tstart, ign_duration, ign_energy, ign_center, ign_stddev;
-    // BDF trajectory tape for the adjoint (null: none): per point, at
-    // tape + j * tape_stride, a header of kTapeHeader doubles and one record
-    // of n + 4 doubles per accepted step (at most tape_cap records).
+    // Trajectory tape for the adjoint (null: none), per point at tape + j *
+    // tape_stride. BDF: a header of kTapeHeader doubles and one record of
+    // n + 4 doubles per accepted step (at most tape_cap records). QSS: a
+    // header of kQssTapeHeader doubles and one record of n + 2 doubles per
+    // step start (at most tape_cap).
     double* tape;
     int64_t tape_stride;
     int tape_cap;
@@ -99,9 +101,16 @@ int source_bdf_adjoint_run(const MechView& m, SourceArgs a, int tape_cap, const 
 // per-CTA tape of at most tape_cap step starts, then the backward pass: ybar_in
 // [n][S+2] and, per point, pbar [n][R]; adj_status [n]: 0, the forward status,
 // -30 (tape full), -33 (more than 32 attempts in a step).
+// With a.tape (a QSS tape of the same points, written by launch_source_qss),
+// the step starts come from it for every point whose tape did not overflow;
+// fwd_status is then the forward launch's status.
 int launch_source_qss_adjoint(const MechView& m, const SourceArgs& a, int tape_cap, int* counter,
-                              const double* ybar_out, double* ybar_in, double* pbar, int* adj_status, Scratch& sc,
-                              cudaStream_t st);
+                              const int* fwd_status, const double* ybar_out, double* ybar_in, double* pbar,
+                              int* adj_status, Scratch& sc, cudaStream_t st);
+// Doubles of a QSS tape of n_points with tape_cap step starts each, and the
+// largest tape the adjoint paths allocate (beyond it they integrate again).
+size_t qss_tape_doubles(const MechView& m, int n_points, int tape_cap);
+constexpr size_t kQssTapeBudgetBytes = size_t(2) << 30;
 int source_qss_adjoint_run(const MechView& m, const SourceArgs& a, int tape_cap, const double* ybar_out,
                            double* ybar_in, double* lnk_bar, double* lnk_bar_points, int* adj_status, Scratch& sc,
                            cudaStream_t st);

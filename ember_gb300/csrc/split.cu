@@ -1506,13 +1506,20 @@ extern "C" int ember_split_adjoint(ember_split h, const double* w_heat_release, 
     const int64_t np = h->n_pts, nv = h->n_vals;
     const int nf = h->n_flames;
     // ---- forward: one taped step, then the objectives (the QSS adjoint
-    // replays the source stage from its input, kept in xD2, with a tape of
-    // its own)
+    // replays each step of the source stage from the recorded step starts;
+    // its input stays in xD2)
     StepTape tape{};
-    tape.cap = qss ? 0 : tape_cap;
-    tape.stride = qss ? 0 : bdf_tape_doubles(n, tape_cap);
+    tape.cap = tape_cap;
     EMBER_TRY(sc.alloc(&tape.t_saved, 1));
-    if (!qss) EMBER_TRY(sc.alloc(&tape.buf, size_t(np) * tape.stride));
+    if (!qss) {
+        tape.stride = bdf_tape_doubles(n, tape_cap);
+        EMBER_TRY(sc.alloc(&tape.buf, size_t(np) * tape.stride));
+    } else if (qss_tape_doubles(m, static_cast<int>(np), tape_cap) * sizeof(double) <= kQssTapeBudgetBytes) {
+        // the forward step's QSS launch records every step start; beyond the
+        // budget the adjoint integrates the stage again from its input
+        tape.stride = int64_t(kQssTapeHeader) + int64_t(tape_cap) * (n + 2);
+        EMBER_TRY(sc.alloc(&tape.buf, qss_tape_doubles(m, static_cast<int>(np), tape_cap)));
+    }
     EMBER_TRY(sc.alloc(&tape.xF, size_t(nv)));
     EMBER_TRY(enqueue_step(h, st, &tape));
     double *T, *Y, *net, *hk, *cp, *q, *qcp, *work, *hr, *cs;
@@ -1599,7 +1606,8 @@ extern "C" int ember_split_adjoint(ember_split h, const double* w_heat_release, 
             EMBER_TRY(sc.alloc(&a.state_out, size_t(nv)));
             a.status = nullptr;
             a.stats = nullptr;
-            EMBER_TRY(launch_source_qss_adjoint(m, a, tape_cap, counter, ybar, ybar2, prow_src, adj_status, sc, st));
+            EMBER_TRY(launch_source_qss_adjoint(m, a, tape_cap, counter, h->src_status, ybar, ybar2, prow_src,
+                                                adj_status, sc, st));
         } else {
             EMBER_TRY(launch_source_bdf_adjoint(m, a, counter, ybar, ybar2, prow_src, adj_status, sc, st));
         }

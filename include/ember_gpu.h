@@ -577,7 +577,10 @@ int ember_source_adjoint(ember_mech mech, int n_points, const double* state_in, 
  * difference in T; accept / reject decisions are held fixed. Finite
  * differences of the adaptive forward map agree with it to their own noise
  * at the reference's default tolerances. Needs qss_stability_check = 0 and
- * qss_iteration_count 1-4. tape_cap: step starts kept per point (0: 4096).
+ * qss_iteration_count 1-4. tape_cap: step starts the forward pass records per
+ * point (0: 4096) while the whole record fits in 2 GiB; points that need more,
+ * or all points beyond that size, are integrated again by the adjoint with a
+ * record of max(tape_cap, 4096) step starts per point.
  * There is no counterpart in the reference (QssIntegrator runs forward
  * only); it serves the gradients of FlameSolver's objectives
  * (src/flameSolver.cpp:926-961) with the QSS source

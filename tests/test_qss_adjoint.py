@@ -94,6 +94,13 @@ def test_gpu_qss_adjoint_matches_the_oracle_adjoint(gpu_lib, kinetics):
     np.testing.assert_allclose(g_state, ref_g, rtol=1e-9, atol=1e-12 * np.abs(ref_g).max())
     ref_lnk = ref_p.sum(axis=0)
     np.testing.assert_allclose(g_lnk, ref_lnk, rtol=1e-9, atol=1e-12 * np.abs(ref_lnk).max())
+    # a forward record too short for any point (16 step starts): the adjoint
+    # integrates every point again itself, with the same result
+    out2, status2, g2, l2 = source_adjoint(gm, st, dt, opts, bar, split_const=sc, x=x, method=QSS, tape_cap=16)
+    assert (status2 == 0).all()
+    assert np.array_equal(out2, out)
+    np.testing.assert_allclose(g2, ref_g, rtol=1e-9, atol=1e-12 * np.abs(ref_g).max())
+    np.testing.assert_allclose(l2, ref_lnk, rtol=1e-9, atol=1e-12 * np.abs(ref_lnk).max())
 
 
 @pytest.mark.gpu
