@@ -69,6 +69,9 @@ def parse_args():
                    help="qss workload: skip the secondary figures (BDF, diffusion, split steps, adjoint)")
     p.add_argument("--regrid-interval", type=int, default=20,
                    help="sweep workload: steps between regrids (regridStepInterval)")
+    p.add_argument("--bdf-layout", type=int, default=0, choices=[0, 1, 2, 3, 4],
+                   help="bdf workload with --threads: matrix placement (codes of ember_mech_get_tuning; 0: first "
+                        "that fits)")
     p.add_argument("--threads", type=int, default=0,
                    help="QSS threads per point; 0: ember_source_autotune picks it before the timed region")
     return p.parse_args()
@@ -310,6 +313,7 @@ def run_ours(args):
     else:
         width = args.threads
         opts.threads_per_point = width
+        opts.bdf_layout = args.bdf_layout
 
     def step():
         integrate_production_terms(gm, method, st_d, dt_d, opts, out=out_d, status=status_d, stats=stats_d,
