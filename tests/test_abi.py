@@ -58,6 +58,10 @@ def test_bad_arguments_are_rejected_without_device():
     assert lib.ember_convection_integrate(1, None, 10, None, None, None, None, None, None, None, None, None, 0,
                                           None) == _lib.EINVAL
     assert "null" in _lib.last_error()
+    # the QSS adjoint: null mechanism, then missing arrays
+    assert lib.ember_source_adjoint_qss(None, 1, None, None, None, 0.0, None, None, None, 0, None, None, None, None,
+                                        0, None) == _lib.EINVAL
+    assert "mechanism" in _lib.last_error()
     from ember_gb300.split import _lib as split_lib
     assert split_lib().ember_split_set_convection(None, None, None, None) == _lib.EINVAL
 
