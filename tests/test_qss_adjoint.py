@@ -160,3 +160,33 @@ def test_split_step_qss_gradients_match_central_differences_of_the_oracle(gpu_li
         fd = (J(state, mp) - J(state, mm)) / 2e-6
         assert abs(g_lnk[i] - fd) <= 1e-4 * abs(fd) + 1e-7 * np.abs(g_lnk).max(), (i, g_lnk[i], fd)
     om.set_multipliers(None)
+
+
+@pytest.mark.gpu
+def test_gpu_qss_adjoint_at_the_c4_size(gpu_lib):
+    # The C4 sizes: the 400-point flame profile of the 53-species / 325-reaction
+    # mechanism, one 2e-5 s source stage at the default options (interpolated
+    # kinetics), 150 QSS steps per point on average and 475 at most. The device
+    # adjoint against the oracle's. (Central differences are no check at this
+    # size: with 400 points a perturbation of 1e-6 already flips some accept /
+    # reject decisions, and the quotients of the large gradients vary by tens of
+    # per cent between steps of 1e-4, 1e-5 and 1e-6.)
+    from oracle import chem
+    from ember_gb300.source import GpuMechanism, source_adjoint
+    from ember_gb300.split import flame_batch
+    mech = synthetic_mechanism(n_species=53, n_reactions=325, seed=53325)
+    grids, state, B, D, rho_u, ju, jb = flame_batch(mech, n_flames=1, n_min=400, n_max=400, seed=4000)
+    opts = SourceOptions.defaults()
+    rng = np.random.default_rng(7)
+    bar = rng.normal(size=state.shape)
+    bar[:, 1] *= 1e-3
+    gm = GpuMechanism(mech)
+    out, status, g_state, g_lnk = source_adjoint(gm, state, 2e-5, opts, bar, method=QSS)
+    om = chem.OracleMech(mech)
+    ref_out, ref_g, ref_p, ref_status, steps = chem.qss_adjoint(om, state, 2e-5, opts, bar)
+    assert (status == 0).all() and (ref_status == 0).all()
+    assert steps.max() > 300
+    assert np.array_equal(out, ref_out)
+    np.testing.assert_allclose(g_state, ref_g, rtol=1e-9, atol=1e-12 * np.abs(ref_g).max())
+    ref_lnk = ref_p.sum(axis=0)
+    np.testing.assert_allclose(g_lnk, ref_lnk, rtol=1e-9, atol=1e-12 * np.abs(ref_lnk).max())
