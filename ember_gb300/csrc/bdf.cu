@@ -381,11 +381,12 @@ struct BdfPoint {
         __syncwarp();
     }
 
-    // The row interchanges of panel [k0, k1), in pivot order, on every column outside it.
-    __device__ void lu_deferred_swaps(int k0, int k1) {
-        for (int j = threadIdx.x; j < n; j += NT) {
-            if (j >= k0 && j < k1) continue;
-            double* colj = M + size_t(j) * n;
+    // The row interchanges of panel [k0, k1), in pivot order, on columns
+    // [j0, j1) (j1 - j0 <= 32), a lane per column, by the calling warp.
+    __device__ void lu_swaps_warp(int k0, int k1, int j0, int j1) {
+        const int lane = threadIdx.x & 31;
+        if (j0 + lane < j1) {
+            double* colj = M + size_t(j0 + lane) * n;
             for (int c = k0; c < k1; ++c) {
                 const int p = v.piv[c];
                 if (p != c) {
@@ -395,43 +396,68 @@ struct BdfPoint {
                 }
             }
         }
+        __syncwarp();
     }
 
+    // A panel's row interchanges reach the columns to its right just before
+    // they take the panel's steps (the warp that updates a column group swaps
+    // it first), and the columns to its left (the L factors, which no later
+    // step reads) at the end. Every column still receives every interchange
+    // in pivot order before any step that reads it, so the factors are those
+    // of applying each interchange to whole rows at once. One barrier per
+    // panel; the work counters alternate so that the next panel's is reset
+    // while this one's is in use.
     __device__ int lu_factor() {
         const int tid = threadIdx.x;
         const int warp = tid >> 5, lane = tid & 31;
-        __shared__ int s_sing, s_next;
+        __shared__ int s_sing, s_next[2];
         const int k1 = min(kLuPanel, n);
         if (warp == 0) {
             const int sg = lu_panel_warp(0, k1);
             if (lane == 0) s_sing = sg;
         }
+        if (tid == 0) {
+            s_next[0] = 0;
+            s_next[1] = 0;
+        }
         __syncthreads();
         if (s_sing) return s_sing;
-        lu_deferred_swaps(0, k1);
-        if (tid == 0) s_next = 0;
-        __syncthreads();
-        for (int k = 0; k + kLuPanel < n; k += kLuPanel) {
+        int it = 0;
+        for (int k = 0; k + kLuPanel < n; k += kLuPanel, ++it) {
             const int kend = k + kLuPanel;
             const int k2e = min(kend + kLuPanel, n);
+            int* counter = &s_next[it & 1];
             if (warp == 0) {
+                lu_swaps_warp(k, kend, kend, k2e);
                 lu_panel_update(k, kend, kend, k2e);
                 const int sg = lu_panel_warp(kend, k2e);
                 if (lane == 0) s_sing = sg;
             }
             for (;;) {
                 int g = 0;
-                if (lane == 0) g = atomicAdd(&s_next, 1);
+                if (lane == 0) g = atomicAdd(counter, 1);
                 g = __shfl_sync(0xffffffffu, g, 0);
                 const int j0 = k2e + g * kLuGroup;
                 if (j0 >= n) break;
-                lu_panel_update(k, kend, j0, min(j0 + kLuGroup, n));
+                const int j1 = min(j0 + kLuGroup, n);
+                lu_swaps_warp(k, kend, j0, j1);
+                lu_panel_update(k, kend, j0, j1);
             }
+            if (tid == 0) s_next[(it + 1) & 1] = 0;
             __syncthreads();
             if (s_sing) return s_sing;
-            lu_deferred_swaps(kend, k2e);
-            if (tid == 0) s_next = 0;
-            __syncthreads();
+        }
+        // the L factors: the interchanges of every panel after the column's own
+        for (int j = tid; j < n; j += NT) {
+            double* colj = M + size_t(j) * n;
+            for (int c = (j / kLuPanel + 1) * kLuPanel; c < n; ++c) {
+                const int p = v.piv[c];
+                if (p != c) {
+                    const double tt = colj[c];
+                    colj[c] = colj[p];
+                    colj[p] = tt;
+                }
+            }
         }
         lu_compose_interchanges();
         return 0;
