@@ -841,9 +841,17 @@ __device__ int bdf_integrate(BdfPoint<NT>& P, double tf, double t_start, int* st
                     nstlj = nst;
                     jcur = true;
                 }
-                for (size_t e = tid; e < size_t(n) * n; e += NT) {
-                    const int c = static_cast<int>(e / n), r = static_cast<int>(e - size_t(c) * n);
-                    P.M[e] = (r == c ? 1.0 : 0.0) - gamma * P.J[e];
+                {
+                    // M = I - gamma J, column-major; (row, column) of element e advanced without a division
+                    int c = tid / n, r = tid - c * n;
+                    for (size_t e = tid; e < size_t(n) * n; e += NT) {
+                        P.M[e] = (r == c ? 1.0 : 0.0) - gamma * P.J[e];
+                        r += NT;
+                        while (r >= n) {
+                            r -= n;
+                            ++c;
+                        }
+                    }
                 }
                 __syncthreads();
                 const int sing = P.lu_factor();

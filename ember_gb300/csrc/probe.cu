@@ -41,8 +41,9 @@ __global__ void k_probe_dmma(double* out, int iters) {
 
 // Issue cost of FP64 warp instructions: one CTA of `warps` warps per SM,
 // lanes below `active` running `iters` x CHAINS operations (MODE 0: DFMA,
-// 1: DADD, 2: DMUL, 3: division, 4: fmax, 5: compare-and-select), clocked
-// per CTA with clock64.
+// 1: DADD, 2: DMUL, 3: division, 4: fmax, 5: compare-and-select, 6: the
+// reciprocal 1.0 / x, 7: the reciprocal as __drcp_rn), clocked per CTA with
+// clock64.
 template <int CHAINS, int MODE>
 __global__ void k_probe_issue(double* sink, long long* cyc, int iters, int active) {
     const int lane = threadIdx.x & 31;
@@ -62,7 +63,9 @@ __global__ void k_probe_issue(double* sink, long long* cyc, int iters, int activ
                 else if (MODE == 2) acc[c] = acc[c] * s;
                 else if (MODE == 3) acc[c] = s / acc[c];
                 else if (MODE == 4) acc[c] = fmax(acc[c] - s, s * 0.5);
-                else acc[c] = (acc[c] < s) ? acc[c] + s : acc[c] - s;
+                else if (MODE == 5) acc[c] = (acc[c] < s) ? acc[c] + s : acc[c] - s;
+                else if (MODE == 6) acc[c] = 1.0 / acc[c];
+                else acc[c] = __drcp_rn(acc[c]);
             }
         }
     }
@@ -82,8 +85,9 @@ using namespace ember;
 
 extern "C" int ember_probe_fp64_issue(int op, int chains, int warps, int active_lanes, double* cycles_per_inst) {
     EMBER_CHECK_ARG(cycles_per_inst != nullptr, "null output");
-    EMBER_CHECK_ARG(op >= 0 && op <= 5,
-                    "op must be 0 (DFMA), 1 (DADD), 2 (DMUL), 3 (division), 4 (fmax + DADD) or 5 (compare + DADD)");
+    EMBER_CHECK_ARG(op >= 0 && op <= 7,
+                    "op must be 0 (DFMA), 1 (DADD), 2 (DMUL), 3 (division), 4 (fmax + DADD), 5 (compare + DADD), "
+                    "6 (1.0 / x) or 7 (__drcp_rn)");
     EMBER_CHECK_ARG(chains == 1 || chains == 8, "chains must be 1 or 8");
     EMBER_CHECK_ARG(warps >= 1 && warps <= 32, "warps must be 1..32");
     EMBER_CHECK_ARG(active_lanes >= 1 && active_lanes <= 32, "active_lanes must be 1..32");
@@ -99,7 +103,7 @@ extern "C" int ember_probe_fp64_issue(int op, int chains, int warps, int active_
         set_error("probe: no device memory");
         return EMBER_ECUDA;
     }
-    const int iters = op == 3 ? 256 : 1024;
+    const int iters = (op == 3 || op >= 6) ? 256 : 1024;
     void (*kern)(double*, long long*, int, int) = nullptr;
     switch (op * 2 + (chains == 8)) {
         case 0: kern = k_probe_issue<1, 0>; break;
@@ -113,7 +117,11 @@ extern "C" int ember_probe_fp64_issue(int op, int chains, int warps, int active_
         case 8: kern = k_probe_issue<1, 4>; break;
         case 9: kern = k_probe_issue<8, 4>; break;
         case 10: kern = k_probe_issue<1, 5>; break;
-        default: kern = k_probe_issue<8, 5>; break;
+        case 11: kern = k_probe_issue<8, 5>; break;
+        case 12: kern = k_probe_issue<1, 6>; break;
+        case 13: kern = k_probe_issue<8, 6>; break;
+        case 14: kern = k_probe_issue<1, 7>; break;
+        default: kern = k_probe_issue<8, 7>; break;
     }
     for (int rep = 0; rep < 2; ++rep) kern<<<sms, warps * 32>>>(sink, cyc, iters, active_lanes);
     cudaError_t err = cudaDeviceSynchronize();

@@ -160,6 +160,10 @@ FP64_ISSUE_CASES = (
     ("division issue, 8 warps/SM", 3, 8, 8, 32),
     ("fmax + DADD issue, 8 warps/SM", 4, 8, 8, 32),
     ("compare-select + DADD issue, 8 warps/SM", 5, 8, 8, 32),
+    ("reciprocal 1.0/x latency, 1 warp", 6, 1, 1, 32),
+    ("reciprocal __drcp_rn latency, 1 warp", 7, 1, 1, 32),
+    ("reciprocal 1.0/x issue, 8 warps/SM", 6, 8, 8, 32),
+    ("reciprocal __drcp_rn issue, 8 warps/SM", 7, 8, 8, 32),
 )
 
 

@@ -75,8 +75,9 @@ int ember_probe_fp64_rate(int kind, double* flops_per_second);
  * warps on every SM, the first `active_lanes` lanes of each warp running
  * `chains` (1: a dependent chain, latency; 8: independent chains, issue
  * rate) of op 0 (DFMA), 1 (DADD), 2 (DMUL), 3 (division), 4 (fmax and a
- * DADD) or 5 (a compare, a DADD and a select); the median over SMs. No
- * reference counterpart. */
+ * DADD), 5 (a compare, a DADD and a select), 6 (the reciprocal 1.0 / x) or
+ * 7 (the reciprocal __drcp_rn); the median over SMs. No reference
+ * counterpart. */
 int ember_probe_fp64_issue(int op, int chains, int warps, int active_lanes, double* cycles_per_inst);
 
 /* ======================================================================
