@@ -71,13 +71,15 @@ def test_oracle_qss_adjoint_matches_central_differences():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kinetics", [KINETICS_STANDARD, KINETICS_INTERP])
-def test_gpu_qss_adjoint_matches_the_oracle_adjoint(gpu_lib, kinetics):
+@pytest.mark.parametrize("kinetics,iterations", [(KINETICS_STANDARD, 1), (KINETICS_INTERP, 1), (KINETICS_STANDARD, 2)])
+def test_gpu_qss_adjoint_matches_the_oracle_adjoint(gpu_lib, kinetics, iterations):
     # the device adjoint (its forward replay and its backward pass) against
-    # the CPU restatement, with split constants and the igniter on
+    # the CPU restatement, with split constants and the igniter on; also with
+    # two corrector iterations per attempt (qss_iteration_count)
     from oracle import chem
     from ember_gb300.source import GpuMechanism, integrate_production_terms, source_adjoint
     mech, st, dt, opts, bar = _case(kinetics, n=8, seed=12)
+    opts.qss_iteration_count = iterations
     opts.ignition_energy, opts.ignition_duration, opts.ignition_stddev = 2e6, 1.0, 5e-4
     rng = np.random.default_rng(3)
     sc = rng.normal(scale=1e-2, size=st.shape) * np.abs(st).clip(1e-3)
