@@ -385,6 +385,131 @@ int diffusion_adjoint_run(const DiffusionView& dv_in, double* y, double* work, i
 
 }  // namespace ember
 
+namespace ember {
+
+static bool pinned_host(const void* p) {
+    if (!p) return true;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();  // a plain host pointer is no error
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+// A host-memory call on page-locked arrays, split into groups of flames that
+// each copy in, integrate and copy out on a stream of their own, so that one
+// group's copies overlap another's kernels. Each system is integrated by the
+// same kernels as in one call, so the results are the same.
+constexpr int kDiffusionPipelineChunks = 4;
+
+static int diffusion_pipelined(int n_flames, const ember_diffusion_grid* grids, int n_vars, const double* x, const double* B,
+                        const double* D, const double* split_const, double* y, const ember_diffusion_options* opts,
+                        int* status, cudaStream_t st) {
+    const int K = kDiffusionPipelineChunks;
+    const int n_sys = n_flames * n_vars;
+    std::vector<int64_t> pt(n_flames + 1, 0);
+    for (int f = 0; f < n_flames; ++f) pt[f + 1] = pt[f] + grids[f].n_points;
+    const int64_t n_pts = pt[n_flames], n_vals = n_pts * n_vars;
+    // flame boundaries of the chunks, by values
+    std::vector<int> fb(1, 0);
+    for (int c = 1; c < K; ++c) {
+        int f = fb.back();
+        while (f < n_flames && pt[f] * K < pt[n_flames] * c) ++f;
+        if (f > fb.back() && f < n_flames) fb.push_back(f);
+    }
+    fb.push_back(n_flames);
+    const int nc = static_cast<int>(fb.size()) - 1;
+    Scratch sc(st);
+    double *dx, *dB, *dD, *dS = nullptr, *dy, *dh = nullptr, *dw = nullptr, *dyi = nullptr;
+    int* dstat;
+    EMBER_TRY(sc.alloc(&dx, size_t(n_pts)));
+    EMBER_TRY(sc.alloc(&dB, size_t(n_vals)));
+    EMBER_TRY(sc.alloc(&dD, size_t(n_vals)));
+    if (split_const) EMBER_TRY(sc.alloc(&dS, size_t(n_vals)));
+    EMBER_TRY(sc.alloc(&dy, size_t(n_vals)));
+    if (opts->h) EMBER_TRY(sc.alloc(&dh, size_t(n_sys)));
+    if (opts->wall_const) EMBER_TRY(sc.alloc(&dw, size_t(n_sys)));
+    if (opts->y_inf) EMBER_TRY(sc.alloc(&dyi, size_t(n_sys)));
+    EMBER_TRY(sc.alloc(&dstat, size_t(n_sys)));
+    cudaStream_t cs[kDiffusionPipelineChunks] = {};
+    cudaEvent_t ready = nullptr, done[kDiffusionPipelineChunks] = {};
+    int rc = EMBER_OK;
+    auto cu = [&](cudaError_t e, const char* what) {
+        if (e != cudaSuccess && rc == EMBER_OK) {
+            set_error("%s failed: %s", what, cudaGetErrorString(e));
+            rc = EMBER_ECUDA;
+        }
+    };
+    cu(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "cudaEventCreate");
+    cu(cudaEventRecord(ready, st), "cudaEventRecord");  // after the allocations above
+    for (int c = 0; c < nc && rc == EMBER_OK; ++c) {
+        cu(cudaStreamCreateWithFlags(&cs[c], cudaStreamNonBlocking), "cudaStreamCreate");
+        cu(cudaEventCreateWithFlags(&done[c], cudaEventDisableTiming), "cudaEventCreate");
+        if (rc != EMBER_OK) break;
+        cu(cudaStreamWaitEvent(cs[c], ready, 0), "cudaStreamWaitEvent");
+        const int f0 = fb[c], f1 = fb[c + 1];
+        const int64_t p0 = pt[f0], p1 = pt[f1], v0 = p0 * n_vars, v1 = p1 * n_vars;
+        const int s0 = f0 * n_vars, s1 = f1 * n_vars;
+        const size_t dbl = sizeof(double);
+        cu(cudaMemcpyAsync(dx + p0, x + p0, dbl * (p1 - p0), cudaMemcpyHostToDevice, cs[c]), "cudaMemcpyAsync");
+        cu(cudaMemcpyAsync(dB + v0, B + v0, dbl * (v1 - v0), cudaMemcpyHostToDevice, cs[c]), "cudaMemcpyAsync");
+        cu(cudaMemcpyAsync(dD + v0, D + v0, dbl * (v1 - v0), cudaMemcpyHostToDevice, cs[c]), "cudaMemcpyAsync");
+        if (dS) cu(cudaMemcpyAsync(dS + v0, split_const + v0, dbl * (v1 - v0), cudaMemcpyHostToDevice, cs[c]),
+                   "cudaMemcpyAsync");
+        cu(cudaMemcpyAsync(dy + v0, y + v0, dbl * (v1 - v0), cudaMemcpyHostToDevice, cs[c]), "cudaMemcpyAsync");
+        ember_diffusion_options oc = *opts;
+        if (dh) {
+            cu(cudaMemcpyAsync(dh + s0, opts->h + s0, dbl * (s1 - s0), cudaMemcpyHostToDevice, cs[c]), "cudaMemcpyAsync");
+            oc.h = dh + s0;
+        }
+        if (dw) {
+            cu(cudaMemcpyAsync(dw + s0, opts->wall_const + s0, dbl * (s1 - s0), cudaMemcpyHostToDevice, cs[c]),
+               "cudaMemcpyAsync");
+            oc.wall_const = dw + s0;
+        }
+        if (dyi) {
+            cu(cudaMemcpyAsync(dyi + s0, opts->y_inf + s0, dbl * (s1 - s0), cudaMemcpyHostToDevice, cs[c]),
+               "cudaMemcpyAsync");
+            oc.y_inf = dyi + s0;
+        }
+        if (rc != EMBER_OK) break;
+        rc = ember_diffusion_integrate(f1 - f0, grids + f0, n_vars, dx + p0, dB + v0, dD + v0, dS ? dS + v0 : nullptr,
+                                       dy + v0, &oc, dstat + s0, EMBER_MEM_DEVICE, cs[c]);
+        if (rc != EMBER_OK) break;
+        cu(cudaMemcpyAsync(y + v0, dy + v0, dbl * (v1 - v0), cudaMemcpyDeviceToHost, cs[c]), "cudaMemcpyAsync");
+        cu(cudaEventRecord(done[c], cs[c]), "cudaEventRecord");
+        cu(cudaStreamWaitEvent(st, done[c], 0), "cudaStreamWaitEvent");
+    }
+    std::vector<int> h_status(n_sys);
+    if (rc == EMBER_OK && status)
+        cu(cudaMemcpyAsync(h_status.data(), dstat, sizeof(int) * n_sys, cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+    sc.release();
+    if (rc == EMBER_OK) rc = finish_call(EMBER_MEM_HOST, st);
+    else cudaStreamSynchronize(st);
+    for (int c = 0; c < nc; ++c) {
+        if (cs[c]) {
+            cudaStreamSynchronize(cs[c]);
+            cudaStreamDestroy(cs[c]);
+        }
+        if (done[c]) cudaEventDestroy(done[c]);
+    }
+    if (ready) cudaEventDestroy(ready);
+    if (rc != EMBER_OK || !status) return rc;
+    int bad = 0;
+    for (int k = 0; k < n_sys; ++k) {
+        status[k] = h_status[k];
+        bad += h_status[k] != 0;
+    }
+    if (bad) {
+        set_error("%d of %d diffusion systems failed (see status)", bad, n_sys);
+        return EMBER_EFAIL;
+    }
+    return EMBER_OK;
+}
+
+}  // namespace ember
+
 extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_grid* grids, int n_vars,
                                          const double* x, const double* B, const double* D,
                                          const double* split_const, double* y,
@@ -425,6 +550,10 @@ extern "C" int ember_diffusion_integrate(int n_flames, const ember_diffusion_gri
                     "bad diffusion algorithm %d", opts->algorithm);
 
     cudaStream_t st = as_stream(stream);
+    // large host-memory calls on page-locked arrays: copies overlap the kernels of other flame groups
+    if (mem == EMBER_MEM_HOST && n_flames >= 2 * kDiffusionPipelineChunks && n_vals >= (int64_t(1) << 20) &&
+        pinned_host(B) && pinned_host(D) && pinned_host(y) && pinned_host(split_const))
+        return diffusion_pipelined(n_flames, grids, n_vars, x, B, D, split_const, y, opts, status, st);
     Scratch sc(st);
     DiffSysInfo* d_info = nullptr;
     EMBER_TRY(sc.alloc(&d_info, n_sys));

@@ -325,3 +325,38 @@ def test_diffusion_minimal_grids(gpu_lib, algorithm):
             assert np.array_equal(out[f], ref[f])
         else:
             _assert_close_per_system(out[f], ref[f], f"grid {f}")
+
+
+@pytest.mark.parametrize("algorithm", [L.DIFFUSION_PARALLEL, L.DIFFUSION_SERIAL])
+def test_diffusion_pinned_host_call_matches_device_call(gpu_lib, algorithm):
+    # A large host-memory call on page-locked arrays runs as groups of flames
+    # whose copies overlap each other's kernels; every system must come out as
+    # from the single-group call on device arrays (and from pageable arrays),
+    # statuses included, with explicit h, wall constants and y_inf per system.
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(21)
+    n_vars = 20
+    grids, B, D, S, Y = _diffusion_case(rng, 16, n_vars, 2800, 4000, spread=0.1, max_ratio=4.0)
+    n_sys = 16 * n_vars
+    h = np.full(n_sys, 2.5e-6)
+    wall = rng.uniform(0.0, 1e3, n_sys)
+    yinf = rng.normal(size=n_sys)
+    flat = lambda arrs: np.concatenate([a.reshape(-1) for a in arrs])
+    assert flat(Y).size >= 1 << 20
+    dev = lambda a: torch.as_tensor(a, device="cuda")
+    yd = dev(flat(Y))
+    _, st_dev = integrate_diffusion_terms(grids, dev(flat(B)), dev(flat(D)), dev(flat(S)), yd, 0.0, 1e-5,
+                                          h=dev(h), wall_const=dev(wall), y_inf=dev(yinf), algorithm=algorithm)
+    torch.cuda.synchronize()
+    ref = yd.cpu().numpy()
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+    yp = pin(flat(Y))
+    _, st_pin = integrate_diffusion_terms(grids, pin(flat(B)), pin(flat(D)), pin(flat(S)), yp, 0.0, 1e-5, h=h,
+                                          wall_const=wall, y_inf=yinf, algorithm=algorithm)
+    yq = flat(Y).copy()
+    _, st_page = integrate_diffusion_terms(grids, flat(B), flat(D), flat(S), yq, 0.0, 1e-5, h=h, wall_const=wall,
+                                           y_inf=yinf, algorithm=algorithm)
+    assert np.isfinite(ref).all()
+    assert np.array_equal(yp, ref) and np.array_equal(yq, ref)
+    assert np.array_equal(np.asarray(st_pin), st_dev.cpu().numpy())
+    assert np.array_equal(np.asarray(st_pin), np.asarray(st_page))
