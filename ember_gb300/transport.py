@@ -124,15 +124,21 @@ class GpuTransport:
         except Exception:
             pass
 
-    def eval(self, T, Y, pressure: float = 101325.0, threshold: float = APPROX_THRESHOLD, stream=None):
+    def eval(self, T, Y, pressure: float = 101325.0, threshold: float = APPROX_THRESHOLD, stream=None, out=None):
         """Properties of the states (T [n], Y [n, S]; numpy arrays or torch CUDA
-        tensors). Returns a dict of arrays shaped like the inputs."""
+        tensors). Returns a dict of arrays shaped like the inputs; ``out``: such
+        a dict to fill instead (e.g. page-locked host arrays)."""
         mem = L.mem_of(T)
         n = int(T.shape[0])
         S = self.S
         shapes = {"density": (n,), "mean_mol_weight": (n,), "cp_mass": (n,), "cp_species": (n, S),
                   "h_species": (n, S), "conductivity": (n,), "viscosity": (n,), "rho_d": (n, S)}
-        if mem == L.MEM_HOST:
+        if out is not None:
+            assert set(out) == set(shapes) and all(tuple(out[k].shape) == s for k, s in shapes.items())
+            if mem == L.MEM_HOST:
+                T = np.ascontiguousarray(T, dtype=np.float64)
+                Y = np.ascontiguousarray(Y, dtype=np.float64)
+        elif mem == L.MEM_HOST:
             T = np.ascontiguousarray(T, dtype=np.float64)
             Y = np.ascontiguousarray(Y, dtype=np.float64)
             out = {k: np.empty(s) for k, s in shapes.items()}
