@@ -365,17 +365,42 @@ struct BdfPoint {
             }
         }
         __syncwarp();
-        for (int j = j0; j < j1; ++j) {
-            double* colj = M + size_t(j) * n;
-            double u[kLuPanel];
+        if (n - kend <= 64) {
+            // few rows: columns outer, the column's u in registers
+            for (int j = j0; j < j1; ++j) {
+                double* colj = M + size_t(j) * n;
+                double u[kLuPanel];
 #pragma unroll
-            for (int t = 0; t < kLuPanel; ++t) u[t] = (k + t < kend) ? colj[k + t] : 0.0;
-            for (int i = kend + lane; i < n; i += 32) {
-                double a = colj[i];
+                for (int t = 0; t < kLuPanel; ++t) u[t] = (k + t < kend) ? colj[k + t] : 0.0;
+                for (int i = kend + lane; i < n; i += 32) {
+                    double a = colj[i];
 #pragma unroll
-                for (int t = 0; t < kLuPanel; ++t)
-                    if (k + t < kend) a = fma(-M[size_t(k + t) * n + i], u[t], a);
-                colj[i] = a;
+                    for (int t = 0; t < kLuPanel; ++t)
+                        if (k + t < kend) a = fma(-M[size_t(k + t) * n + i], u[t], a);
+                    colj[i] = a;
+                }
+            }
+            __syncwarp();
+            return;
+        }
+        // many rows: rows outer, columns inner, so that a lane loads its row's
+        // panel multipliers once for the whole column group (u is the same for
+        // every lane); each element takes the same steps in the same order
+        for (int i0 = kend; i0 < n; i0 += 32) {
+            const int i = i0 + lane;
+            const bool in = i < n;
+            double l[kLuPanel];
+#pragma unroll
+            for (int t = 0; t < kLuPanel; ++t) l[t] = (in && k + t < kend) ? M[size_t(k + t) * n + i] : 0.0;
+            if (in) {
+                for (int j = j0; j < j1; ++j) {
+                    double* colj = M + size_t(j) * n;
+                    double a = colj[i];
+#pragma unroll
+                    for (int t = 0; t < kLuPanel; ++t)
+                        if (k + t < kend) a = fma(-l[t], colj[k + t], a);
+                    colj[i] = a;
+                }
             }
         }
         __syncwarp();
