@@ -414,18 +414,20 @@ __device__ __forceinline__ void chem_rates(const MechView& m, ChemSmem& w, doubl
             const int np = (ent >> 24) & 0xf;
             const int nr = (ent >> 28) & 0xf;
             const double f = w.ropf[i], r = w.ropr[i];
-            if (np == 1 && nr == 0) {
+            if (np + nr == 1) {
+                // once a product (np = 1) or once a reactant (nr = 1), nearly
+                // every entry: the operands are selected, not branched on, so
+                // lanes of both kinds issue one pair of adds together. The
+                // sums are the two branches' bit for bit (x - y == x + (-y)).
+                const bool prod = np == 1;
                 if (want_qd) {
-                    q = q + f;
-                    d = d + r;
+                    q = q + (prod ? f : r);
+                    d = d + (prod ? r : f);
                 }
-                if (want_net) nt = nt + (f - r);
-            } else if (np == 0 && nr == 1) {
-                if (want_qd) {
-                    q = q + r;
-                    d = d + f;
+                if (want_net) {
+                    const double net = f - r;
+                    nt = nt + (prod ? net : -net);
                 }
-                if (want_net) nt = nt - (f - r);
             } else {
                 if (want_qd) {
                     for (int o = 0; o < np; ++o) q = q + f;

@@ -606,9 +606,9 @@ __device__ __forceinline__ double center_volume(const double* x, int alpha) {
 
 // per-flame scratch inside the UTW slice, after the work vectors
 struct UtwView {
-    double *y3, *hh, *rph, *Wm, *sW, *rho, *rV, *V, *m, *mb;
+    double *y3, *hh, *rph, *Wm, *sW, *rho, *rV, *V;
 };
-constexpr int kUtwScratch = 13;  // doubles per point after the work vectors
+constexpr int kUtwScratch = 10;  // doubles per point after the work vectors
 
 __device__ UtwView utw_view(const ConvArgs& a, const ConvFlame& F) {
     const int N = F.f.n_points;
@@ -622,8 +622,6 @@ __device__ UtwView utw_view(const ConvArgs& a, const ConvFlame& F) {
     v.rho = v.sW + N;
     v.rV = v.rho + N;
     v.V = v.rV + N;
-    v.m = v.V + N;
-    v.mb = v.m + N;
     return v;
 }
 
