@@ -68,6 +68,7 @@ def _declare(lib):
                                               C.POINTER(DiffusionOptions), vp, C.c_int, vp]),
         "ember_probe_fp64_rate": (C.c_int, [C.c_int, C.POINTER(C.c_double)]),
         "ember_probe_fp64_issue": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
+        "ember_math_eval": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_int64]),
         "ember_mech_create": (C.c_int, [vp, C.POINTER(vp)]),
         "ember_mech_destroy": (C.c_int, [vp]),
         "ember_mech_set_multipliers": (C.c_int, [vp, vp, C.c_int, vp]),

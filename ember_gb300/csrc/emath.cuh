@@ -22,7 +22,7 @@ namespace ember {
 #define EMATH_LN2_HI 0.6931471805599453
 #define EMATH_LN2_LO 2.3190468138462996e-17
 #define EMATH_LOG2E 1.4426950408889634
-#define EMATH_SQRT2 1.4142135623730951
+#define EMATH_SQRT2_BITS 0x3ff6a09e667f3bcdLL  // 1.4142135623730951, the double nearest sqrt 2
 #define EMATH_LN10 2.302585092994046
 #define EMATH_LOG10E 0.4342944819032518
 
@@ -30,10 +30,17 @@ __device__ __forceinline__ double em_pow2i(int k) {
     return __longlong_as_double(static_cast<long long>(k + 1023) << 52);
 }
 
+// |x| <= 708 as a test of the magnitude bits on the integer pipe: inside it
+// none of em_exp's range cases applies, so the FP64 compares run only
+// outside it, with the same results.
+#define EMATH_EXP_PLAIN_BITS 0x4086200000000000LL  // 708.0
+
 __device__ __forceinline__ double em_exp(double x) {
-    if (x != x) return x;
-    if (x > 709.782712893384) return __longlong_as_double(0x7ff0000000000000LL);
-    if (x < -745.1332191019412) return 0.0;
+    if ((__double_as_longlong(x) & 0x7fffffffffffffffLL) > EMATH_EXP_PLAIN_BITS) {
+        if (x != x) return x;
+        if (x > 709.782712893384) return __longlong_as_double(0x7ff0000000000000LL);
+        if (x < -745.1332191019412) return 0.0;
+    }
     const double kd = rint(x * EMATH_LOG2E);
     double r = fma(-kd, EMATH_LN2_HI, x);
     r = fma(-kd, EMATH_LN2_LO, r);
@@ -58,9 +65,13 @@ __device__ __forceinline__ double em_exp(double x) {
 }
 
 __device__ __forceinline__ double em_log(double x) {
-    if (!(x > 0.0)) return x == 0.0 ? __longlong_as_double(0xfff0000000000000LL) : __longlong_as_double(0x7ff8000000000000LL);
     long long bits = __double_as_longlong(x);
-    if (bits >= 0x7ff0000000000000LL) return x;  // +inf
+    // positive and finite exactly when 0 < bits < the bits of +inf; the
+    // special cases (zero, negative, NaN, +inf) are tested only outside
+    if (bits <= 0 || bits >= 0x7ff0000000000000LL) {
+        if (!(x > 0.0)) return x == 0.0 ? __longlong_as_double(0xfff0000000000000LL) : __longlong_as_double(0x7ff8000000000000LL);
+        return x;  // +inf
+    }
     int e = 0;
     if (bits < 0x0010000000000000LL) {  // subnormal: scale by 2^54
         x *= 18014398509481984.0;
@@ -68,11 +79,15 @@ __device__ __forceinline__ double em_log(double x) {
         e = -54;
     }
     e += static_cast<int>((bits >> 52) & 0x7ff) - 1023;
-    double m = __longlong_as_double((bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL);
-    if (m > EMATH_SQRT2) {
-        m *= 0.5;
+    // m in [1, 2); above sqrt 2 it is halved (exactly: the exponent field
+    // drops by one). Positive doubles order as their bit patterns, so the
+    // comparison with sqrt 2 runs on the integer pipe.
+    long long mb = (bits & 0x000fffffffffffffLL) | 0x3ff0000000000000LL;
+    if (mb > EMATH_SQRT2_BITS) {
+        mb -= 0x0010000000000000LL;
         e += 1;
     }
+    const double m = __longlong_as_double(mb);
     const double s = (m - 1.0) / (m + 1.0);
     const double s2 = s * s;
     double q = 0.09523809523809523;

@@ -2,8 +2,10 @@
 // (DFMA) and the FP64 tensor path (DMMA m8n8k4), both run as a fixed amount
 // of independent work on every SM and timed with CUDA events; and the issue
 // cost of single FP64 warp instructions (clock64 per CTA), which shows how
-// the pipe is shared between warps and lanes.
+// the pipe is shared between warps and lanes. Also the kinetics kernels'
+// exp / log functions evaluated on an array, for their parity tests.
 #include "common.cuh"
+#include "emath.cuh"
 
 #include <algorithm>
 #include <vector>
@@ -77,6 +79,14 @@ __global__ void k_probe_issue(double* sink, long long* cyc, int iters, int activ
     for (int c = 0; c < CHAINS; ++c) r += acc[c];
     if (r == 1234.5) sink[0] = r;
     if (threadIdx.x == 0) cyc[blockIdx.x] = t1 - t0;
+}
+
+// y[i] = em_exp, em_log, em_log10 or em_exp10 (op 0..3) of x[i]
+__global__ void k_math_eval(int op, const double* x, double* y, int64_t n) {
+    const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = x[i];
+    y[i] = op == 0 ? em_exp(v) : op == 1 ? em_log(v) : op == 2 ? em_log10(v) : em_exp10(v);
 }
 
 }  // namespace ember
@@ -179,5 +189,27 @@ extern "C" int ember_probe_fp64_rate(int kind, double* flops_per_second) {
     else
         flops = 1024.0 * iters * double(threads / 32) * blocks;  // 2 mma (8x8x4, 512 flop each) per iter per warp
     *flops_per_second = flops / (best_ms * 1e-3);
+    return EMBER_OK;
+}
+
+extern "C" int ember_math_eval(int op, const double* x, double* y, int64_t n) {
+    EMBER_CHECK_ARG(op >= 0 && op <= 3, "op must be 0 (exp), 1 (log), 2 (log10) or 3 (exp10), got %d", op);
+    EMBER_CHECK_ARG(n >= 0 && n <= (int64_t(1) << 26), "n must be in [0, 2^26], got %lld", (long long)n);
+    EMBER_CHECK_ARG(n == 0 || (x != nullptr && y != nullptr), "null array");
+    if (n == 0) return EMBER_OK;
+    EMBER_TRY(ensure_device());
+    double* d = nullptr;
+    EMBER_CUDA_TRY(cudaMalloc(&d, sizeof(double) * 2 * size_t(n)));
+    cudaError_t err = cudaMemcpy(d, x, sizeof(double) * size_t(n), cudaMemcpyHostToDevice);
+    if (err == cudaSuccess) {
+        k_math_eval<<<unsigned((n + 255) / 256), 256>>>(op, d, d + n, n);
+        err = cudaGetLastError();
+    }
+    if (err == cudaSuccess) err = cudaMemcpy(y, d + n, sizeof(double) * size_t(n), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (err != cudaSuccess) {
+        set_error("math kernel failed: %s", cudaGetErrorString(err));
+        return EMBER_ECUDA;
+    }
     return EMBER_OK;
 }

@@ -80,6 +80,13 @@ int ember_probe_fp64_rate(int kind, double* flops_per_second);
  * counterpart. */
 int ember_probe_fp64_issue(int op, int chains, int warps, int active_lanes, double* cycles_per_inst);
 
+/* y[i] = exp, log, log10 or exp10 (op 0..3) of x[i], i < n (n <= 2^26), host
+ * arrays, as the kinetics kernels evaluate them (their own FP64 exp and log;
+ * exp10 x = exp(x ln 10), log10 x = log(x) log10(e)). For parity tests of
+ * those functions. No reference counterpart (the reference calls the C
+ * library's exp and log). */
+int ember_math_eval(int op, const double* x, double* y, int64_t n);
+
 /* ======================================================================
  * Batched tridiagonal integrator
  *

@@ -64,6 +64,9 @@ def test_bad_arguments_are_rejected_without_device():
     assert "mechanism" in _lib.last_error()
     from ember_gb300.split import _lib as split_lib
     assert split_lib().ember_split_set_convection(None, None, None, None) == _lib.EINVAL
+    assert lib.ember_math_eval(4, None, None, 1) == _lib.EINVAL
+    assert lib.ember_math_eval(0, None, None, 1) == _lib.EINVAL
+    assert lib.ember_math_eval(0, None, None, 0) == 0  # nothing to do: no device needed
 
 
 def test_no_device_is_reported_not_crashed():
